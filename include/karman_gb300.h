@@ -1,0 +1,223 @@
+/*
+ * karman_gb300.h -- C ABI of libkarman_gb300.so, the GB300 (sm_103a) kernels
+ * behind the karman_taichi SIMPLE hot path.
+ *
+ * Everything crossing this boundary is a plain pointer, size or POD struct:
+ * device arrays are caller-owned (allocated by the caller, e.g. from torch),
+ * the stream is a cudaStream_t passed as void*, and no exception, abort or
+ * device trap crosses the ABI.  Every entry point returns an int status:
+ *     0          success (for solvers: converged)
+ *     > 0        a solver outcome (KC_MAXITER, KC_BREAKDOWN_*, KC_NONFINITE, KC_STALL)
+ *     < 0        an argument or CUDA error (KC_ERR_*); kc_last_error() explains it.
+ * Calls are stream ordered.  A workspace must not be shared by calls that can
+ * run concurrently; otherwise the functions are reentrant.
+ *
+ * Linear systems are 5-point stencils on a flat index k in [0, n) with far
+ * stride S (for a padded 2-D field [NX][NY], k = i*NY + j and S = NY):
+ *     y[k] = c0 x[k] + c1 x[k-S] + c2 x[k+S] + c3 x[k+1] + c4 x[k-1]
+ * with reads outside [0, n) returning 0.  Component c is read at
+ * coef[c*cs + k*es]: SoA planes use (cs = n, es = 1); the reference's
+ * coef[i,j,0..4] array-of-structs layout is (cs = 1, es = 5).
+ */
+#ifndef KARMAN_GB300_H
+#define KARMAN_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define KC_OK               0
+#define KC_MAXITER          1   /* iteration cap reached                           */
+#define KC_BREAKDOWN_RHO    2   /* rho = (r, r~) == 0   (bicgsolver.py:96-98)      */
+#define KC_BREAKDOWN_OMEGA  3   /* omega == 0           (karman_taichi.py:451-454) */
+#define KC_NONFINITE        4   /* a NaN/Inf appeared in a scalar of the recurrence */
+#define KC_STALL            5   /* preconditioned residual stopped decreasing      */
+#define KC_ERR_ARG        (-1)
+#define KC_ERR_CUDA       (-2)
+#define KC_ERR_WORKSPACE  (-3)
+#define KC_ERR_UNSUPPORTED (-4)
+
+#define KC_F64 0
+#define KC_F32 1
+
+#define KC_X0_ZERO 0   /* cold start x = 0, r = b          (bicgsolver.py:21-36)     */
+#define KC_X0_WARM 1   /* warm start r = b - A x           (karman_taichi.py:362-371) */
+
+#define KC_PRECOND_NONE   0   /* M = I                    (bicgsolver.py:48-58)          */
+#define KC_PRECOND_JACOBI 1   /* right Jacobi, p^ = M^-1 p (karman_taichi.py:398-399,418) */
+
+#define KC_REL_R0 0   /* stop when ||r|| / ||r0|| < eps (reference definition) */
+#define KC_REL_B  1   /* stop when ||r|| / ||b||  < eps                         */
+
+typedef struct {
+    long long n;          /* number of unknowns                                 */
+    long long cs, es;     /* coefficient component stride, element stride       */
+    const void* coef;     /* 5 components aP, aW(k-S), aE(k+S), aN(k+1), aS(k-1) */
+    int stride;           /* far stride S                                       */
+    int dtype;            /* KC_F64 or KC_F32 (vectors and coefficients)        */
+} kc_system;
+
+typedef struct {
+    double eps;           /* relative residual tolerance                        */
+    long long max_iter;   /* iteration cap (reference: NX*NY or 100*n)          */
+    int x0;               /* KC_X0_ZERO | KC_X0_WARM                             */
+    int precond;          /* KC_PRECOND_NONE | KC_PRECOND_JACOBI                 */
+    int omega_break;      /* stop on omega == 0 (karman_taichi.py:451)           */
+    int rel_to;           /* KC_REL_R0 | KC_REL_B                                */
+    int check_every;      /* host polls convergence every N iterations (0: auto)*/
+    int use_graph;        /* capture iteration chunks in a CUDA graph            */
+    double* history;      /* device array or NULL: history[k] = ||r_k||_2       */
+    long long history_len;/* capacity of history (entries beyond are dropped)   */
+} kc_solve_opts;
+
+typedef struct {
+    int status;           /* KC_OK or a solver outcome                          */
+    int refinements;      /* refinement sweeps (kc_bicgstab_refined only)       */
+    long long iters;      /* completed iterations (summed over sweeps)          */
+    double rel_res;       /* final relative residual                            */
+    double r0;            /* ||r0|| (2-norm)                                     */
+} kc_solve_info;
+
+/* ---- library ------------------------------------------------------------- */
+int         kc_version(void);
+const char* kc_status_str(int status);
+const char* kc_last_error(void);
+int         kc_device_count(void);
+
+/* ---- stencil linear algebra --------------------------------------------- */
+/* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),
+ * CGSolver.compute_Ap/compute_Ax (cgsolver.py:56-66) and the 7-offset gather
+ * of karman_taichi.py:362-366, 403-407. */
+int kc_spmv(const kc_system* A, const void* x, void* y, void* stream);
+
+/* out_dev[0] = sum_k p[k] q[k] in FP64 with a deterministic two-stage
+ * reduction.  Replaces CGSolver.reduce (cgsolver.py:49-54). */
+size_t kc_dot_ws_bytes(long long n);
+int kc_dot(int dtype, long long n, const void* p, const void* q, double* out_dev,
+           void* ws, size_t ws_bytes, void* stream);
+
+/* BiCGSTAB.  Replaces BICGSolver.solve (bicgsolver.py:88-135) and the
+ * bicgstab kernel of karman_taichi.py:342-456.  x is overwritten (cold start)
+ * or used as the initial guess (warm start).  M is the Jacobi diagonal (may
+ * differ from A's, as in karman_taichi.py:218) or NULL. */
+size_t kc_bicgstab_ws_bytes(long long n, int stride, int dtype);
+int kc_bicgstab(const kc_system* A, const void* b, void* x, const void* M,
+                void* ws, size_t ws_bytes, const kc_solve_opts* opts,
+                kc_solve_info* info, void* stream);
+
+/* Conjugate gradients.  Replaces CGSolver.solve (cgsolver.py:83-114). */
+size_t kc_cg_ws_bytes(long long n, int stride, int dtype);
+int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes,
+          const kc_solve_opts* opts, kc_solve_info* info, void* stream);
+
+/* Mixed precision: FP64 residual r = b - A64 x, FP32 BiCGSTAB correction on
+ * A32 (FP64 inner products), x += d, until ||r||/||b|| < opts->eps.  The
+ * pressure-correction solve of the mixed SIMPLE path (simple.py:252-255,
+ * karman_taichi.py:497-504 with precision split). */
+size_t kc_refined_ws_bytes(long long n, int stride);
+int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b,
+                        double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
+                        double eps_inner, int max_refine, kc_solve_info* info, void* stream);
+
+/* ---- SIMPLE assembly and correction (staggered padded fields) ----------- */
+#define KC_MODE_SIMPLE   0   /* simple.py set_bc incl. the east-wall aW term (simple.py:215) */
+#define KC_MODE_BICGSIMP 1   /* bicgsimp.py: east-wall fix (:196), p' pinned at (1,1) (:146-151) */
+#define KC_MODE_CHANNEL  2   /* velocity inlet, zero-gradient outlet, walls, blocked cells */
+
+typedef struct {
+    int nx, ny;               /* interior cells; u [nx+3][ny+2], v [nx+2][ny+3], p [nx+2][ny+2] */
+    int mode;                 /* KC_MODE_*                                                       */
+    int pad_;
+    double dx, dy, rho, mu, dt;
+    double U;                 /* channel inlet velocity                                          */
+    double bc[4][2];          /* simple.py bc dict order w, e, n, s: [normal, tangential]        */
+    double alpha_m, alpha_u, alpha_p;
+} kc_phys;
+
+/* Size of the small reduction workspace used by the kernels below. */
+size_t kc_reduce_ws_bytes(void);
+
+/* Momentum coefficients a_P..a_S and source for u and v faces with the
+ * boundary conditions folded in.  Replaces compute_coef_u/compute_coef_v +
+ * set_bc (simple.py:77-110, 172-216).  solid may be NULL.  The optional
+ * FP32 outputs (NULL to skip) receive a rounded copy for the mixed path. */
+int kc_assemble_momentum(const kc_phys* P, const double* u, const double* v,
+                         const double* p, const double* u0, const double* v0,
+                         const unsigned char* solid,
+                         double* coef_u, double* b_u, double* coef_v, double* b_v,
+                         float* coef_u32, float* b_u32, float* coef_v32, float* b_v32,
+                         void* stream);
+
+/* Boundary velocities written by set_bc (simple.py:181, 186, 192, 196). */
+int kc_apply_bc_values(const kc_phys* P, double* u, double* v, void* stream);
+
+/* u = a*u_mid + (1-a)*u on unknown faces (simple.py:232-238; bicgsimp.py:212-225);
+ * diff_dev (nullable) receives sqrt(max|du|^2 + max|dv|^2). */
+int kc_relax_velocity(const kc_phys* P, const unsigned char* solid, const double* u_mid,
+                      const double* v_mid, double* u, double* v, double* diff_dev,
+                      void* ws, void* stream);
+
+/* Channel outlet: zero-gradient copy then mass-flow rescale
+ * (karman_taichi.py:178-183, 586-601). */
+int kc_outlet_conserve(const kc_phys* P, double* u, void* stream);
+
+/* Pressure-correction coefficients and mass source.  Replaces compute_coef_p
+ * (simple.py:143-170; bicgsimp.py:124-151).  mass_dev[0] = max|mdiv| over
+ * fluid cells, mass_dev[1] = sum mdiv^2. */
+int kc_assemble_pcorr(const kc_phys* P, const double* u, const double* v,
+                      const double* coef_u, const double* coef_v, const unsigned char* solid,
+                      double* coef_p, double* b_p, float* coef_p32, float* b_p32,
+                      double* mdiv, double* mass_dev, void* ws, void* stream);
+
+/* Velocity and pressure correction.  Replaces correct_velocity and
+ * correct_pressure (simple.py:218-230); pcor_max_dev = max|p'|. */
+int kc_correct(const kc_phys* P, const double* pcor, const double* coef_u,
+               const double* coef_v, const unsigned char* solid, double* u, double* v,
+               double* p, double* pcor_max_dev, void* ws, void* stream);
+
+/* mdiv and max|mdiv| of the current field (simple.py:137-141; bicgsimp.py:114-122). */
+int kc_mass_residual(const kc_phys* P, const double* u, const double* v,
+                     const unsigned char* solid, double* mdiv, double* mass_dev,
+                     void* ws, void* stream);
+
+/* ---- karman_taichi.py assembled-matrix path ----------------------------- */
+typedef struct {
+    int nx, ny;
+    double dx, dy, rho, mu, dt, velo_rel, p_rel;
+} kc_karman;
+
+/* Rows of fill_Au (karman_taichi.py:162-248), fill_Av (:251-294) and
+ * fill_Ap (:297-339) as flat 5-point planes (cs = n, es = 1) + b + Jacobi
+ * diagonal M.  u: n = (nx+1)*ny, S = ny; v: n = nx*(ny+1), S = ny+1;
+ * p: n = nx*ny, S = ny.  ct is the int32 cell-type field [nx+2][ny+2]. */
+int kc_karman_fill_u(const kc_karman* K, const int* ct, const double* u, const double* v,
+                     const double* p, const double* u0, double* coef, double* b, double* M,
+                     void* stream);
+int kc_karman_fill_v(const kc_karman* K, const int* ct, const double* u, const double* v,
+                     const double* p, const double* v0, double* coef, double* b, double* M,
+                     void* stream);
+int kc_karman_fill_p(const kc_karman* K, const int* ct, const double* u, const double* v,
+                     const double* coef_u, const double* coef_v, double* coef, double* b,
+                     double* M, void* stream);
+/* xu_back / xv_back / xp_back (karman_taichi.py:459-478); which = 0, 1, 2. */
+int kc_karman_back(const kc_karman* K, int which, const double* x, double* field, void* stream);
+/* puv_correction (karman_taichi.py:507-542); pcor_max_dev = max|pcor|. */
+int kc_karman_puv_correction(const kc_karman* K, const int* ct, const double* pcor,
+                             const double* coef_u, const double* coef_v, double* u,
+                             double* v, double* p, double* pcor_max_dev, void* ws,
+                             void* stream);
+/* correct_conserv (karman_taichi.py:586-614); udiv may be NULL. */
+int kc_karman_correct_conserv(const kc_karman* K, double* u, const double* v, double* udiv,
+                              void* stream);
+
+/* ---- utilities ------------------------------------------------------------ */
+/* dst = src (device to device), e.g. time_forward (karman_taichi.py:617-622). */
+int kc_copy(void* dst, const void* src, size_t bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KARMAN_GB300_H */

@@ -1,0 +1,151 @@
+"""ctypes binding of libkarman_gb300.so (declarations in include/karman_gb300.h).
+
+The library is the only compute path: importing an op whose library is
+missing raises ``KcLibraryMissing`` -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkarman_gb300.so")
+
+# status codes (karman_gb300.h)
+OK, MAXITER, BREAKDOWN_RHO, BREAKDOWN_OMEGA, NONFINITE, STALL = 0, 1, 2, 3, 4, 5
+ERR_ARG, ERR_CUDA, ERR_WORKSPACE, ERR_UNSUPPORTED = -1, -2, -3, -4
+F64, F32 = 0, 1
+X0_ZERO, X0_WARM = 0, 1
+PRECOND_NONE, PRECOND_JACOBI = 0, 1
+REL_R0, REL_B = 0, 1
+MODE_SIMPLE, MODE_BICGSIMP, MODE_CHANNEL = 0, 1, 2
+
+STATUS_NAMES = {OK: "OK", MAXITER: "MAXITER", BREAKDOWN_RHO: "BREAKDOWN_RHO",
+                BREAKDOWN_OMEGA: "BREAKDOWN_OMEGA", NONFINITE: "NONFINITE", STALL: "STALL"}
+
+
+class KcLibraryMissing(RuntimeError):
+    pass
+
+
+class KcError(RuntimeError):
+    def __init__(self, rc, what, detail):
+        super().__init__(f"{what} failed with status {rc}: {detail}")
+        self.rc = rc
+
+
+class KcSystem(C.Structure):
+    _fields_ = [("n", C.c_longlong), ("cs", C.c_longlong), ("es", C.c_longlong),
+                ("coef", C.c_void_p), ("stride", C.c_int), ("dtype", C.c_int)]
+
+
+class KcSolveOpts(C.Structure):
+    _fields_ = [("eps", C.c_double), ("max_iter", C.c_longlong), ("x0", C.c_int),
+                ("precond", C.c_int), ("omega_break", C.c_int), ("rel_to", C.c_int),
+                ("check_every", C.c_int), ("use_graph", C.c_int),
+                ("history", C.c_void_p), ("history_len", C.c_longlong)]
+
+
+class KcSolveInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("refinements", C.c_int), ("iters", C.c_longlong),
+                ("rel_res", C.c_double), ("r0", C.c_double)]
+
+
+class KcPhys(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("mode", C.c_int), ("pad_", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("rho", C.c_double), ("mu", C.c_double),
+                ("dt", C.c_double), ("U", C.c_double), ("bc", (C.c_double * 2) * 4),
+                ("alpha_m", C.c_double), ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
+
+
+class KcKarman(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+                ("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double),
+                ("velo_rel", C.c_double), ("p_rel", C.c_double)]
+
+
+P_ = C.c_void_p
+I_ = C.c_int
+L_ = C.c_longlong
+S_ = C.c_size_t
+D_ = C.c_double
+PD = C.POINTER(C.c_double)
+
+# name -> (restype, argtypes); every symbol declared in include/karman_gb300.h
+SIGNATURES = {
+    "kc_version": (I_, []),
+    "kc_status_str": (C.c_char_p, [I_]),
+    "kc_last_error": (C.c_char_p, []),
+    "kc_device_count": (I_, []),
+    "kc_spmv": (I_, [C.POINTER(KcSystem), P_, P_, P_]),
+    "kc_dot_ws_bytes": (S_, [L_]),
+    "kc_dot": (I_, [I_, L_, P_, P_, P_, P_, S_, P_]),
+    "kc_bicgstab_ws_bytes": (S_, [L_, I_, I_]),
+    "kc_bicgstab": (I_, [C.POINTER(KcSystem), P_, P_, P_, P_, S_, C.POINTER(KcSolveOpts),
+                         C.POINTER(KcSolveInfo), P_]),
+    "kc_cg_ws_bytes": (S_, [L_, I_, I_]),
+    "kc_cg": (I_, [C.POINTER(KcSystem), P_, P_, P_, S_, C.POINTER(KcSolveOpts),
+                   C.POINTER(KcSolveInfo), P_]),
+    "kc_refined_ws_bytes": (S_, [L_, I_]),
+    "kc_bicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
+                                 C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
+    "kc_reduce_ws_bytes": (S_, []),
+    "kc_assemble_momentum": (I_, [C.POINTER(KcPhys)] + [P_] * 14 + [P_]),
+    "kc_apply_bc_values": (I_, [C.POINTER(KcPhys), P_, P_, P_]),
+    "kc_relax_velocity": (I_, [C.POINTER(KcPhys)] + [P_] * 8),
+    "kc_outlet_conserve": (I_, [C.POINTER(KcPhys), P_, P_]),
+    "kc_assemble_pcorr": (I_, [C.POINTER(KcPhys)] + [P_] * 13),
+    "kc_correct": (I_, [C.POINTER(KcPhys)] + [P_] * 10),
+    "kc_mass_residual": (I_, [C.POINTER(KcPhys)] + [P_] * 7),
+    "kc_karman_fill_u": (I_, [C.POINTER(KcKarman)] + [P_] * 9),
+    "kc_karman_fill_v": (I_, [C.POINTER(KcKarman)] + [P_] * 9),
+    "kc_karman_fill_p": (I_, [C.POINTER(KcKarman)] + [P_] * 9),
+    "kc_karman_back": (I_, [C.POINTER(KcKarman), I_, P_, P_, P_]),
+    "kc_karman_puv_correction": (I_, [C.POINTER(KcKarman)] + [P_] * 10),
+    "kc_karman_correct_conserv": (I_, [C.POINTER(KcKarman), P_, P_, P_, P_]),
+    "kc_copy": (I_, [P_, P_, S_, P_]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load() -> C.CDLL:
+    """Load libkarman_gb300.so once; raises KcLibraryMissing if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise KcLibraryMissing(
+                f"{LIB_PATH} is missing: build it with `python -m karman_taichi_gb300.build` "
+                "(or __graft_entry__.build()); there is no CPU fallback")
+        h = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(h, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = h
+    return _lib
+
+
+def last_error() -> str:
+    return load().kc_last_error().decode(errors="replace")
+
+
+def check(rc: int, what: str) -> int:
+    """Raise KcError for argument/CUDA errors (rc < 0); return solver outcomes."""
+    if rc < 0:
+        raise KcError(rc, what, last_error())
+    return rc
+
+
+def status_name(rc: int) -> str:
+    return STATUS_NAMES.get(rc, str(rc))

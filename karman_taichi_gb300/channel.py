@@ -1,0 +1,192 @@
+"""Channel SIMPLE driver on the GPU (blocked-cell cylinder in a channel).
+
+One time step is the SIMPLE outer loop of karman_taichi.py:633-659 /
+simple.py:270-281 with the discretisation of simple.py (mid-point convection,
+set_bc-style wall and Dirichlet folding) and the outlet treatment of
+karman_taichi.py (zero-gradient row + mass-flow rescale):
+
+    assemble u, v momentum   (kc_assemble_momentum)
+    solve u*, v*             (BiCGSTAB, cold start, rel tol eps)
+    relax + outlet           (kc_relax_velocity, kc_outlet_conserve)
+    assemble p'              (kc_assemble_pcorr; its max|mdiv| is the mass residual)
+    solve p'                 (BiCGSTAB)
+    correct u, v, p          (kc_correct)
+    stop when mass residual <= mass_tol or after max_outer iterations
+    u0 <- u, v0 <- v         (time_forward, karman_taichi.py:617-622)
+
+``precision='fp64'`` is the plain method; ``precision='mixed'`` assembles an
+FP32 copy of every system and solves with FP32 BiCGSTAB (FP64 inner products)
+inside an FP64 iterative refinement; ``precond='learned'`` adds the learned
+initial guess / preconditioner for p' (karman_taichi_gb300.learned).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import geometry
+from .config import ChannelConfig
+from .linalg import Stencil, Workspace, bicgstab, bicgstab_refined, ptr, stream_handle
+
+
+class ChannelSolver:
+    def __init__(self, cfg: ChannelConfig, device="cuda", precision="fp64", use_graph=True,
+                 eps_inner=1e-3, learned=None):
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.cfg, self.precision, self.use_graph = cfg, precision, use_graph
+        self.eps_inner = eps_inner
+        self.learned = learned
+        self.device = torch.device(device)
+        L.load()
+        nx, ny = cfg.nx, cfg.ny
+        f64 = dict(dtype=torch.float64, device=self.device)
+        f32 = dict(dtype=torch.float32, device=self.device)
+        z = torch.zeros
+        self.solid_np = geometry.solid_mask(nx, ny, cfg.obstacles)
+        self.solid = torch.from_numpy(self.solid_np).to(self.device)
+        self.u, self.v, self.p = z((nx + 3, ny + 2), **f64), z((nx + 2, ny + 3), **f64), z((nx + 2, ny + 2), **f64)
+        self.u0, self.v0 = z_like(self.u), z_like(self.v)
+        self.pcor = z_like(self.p)
+        self.u_mid, self.v_mid = z_like(self.u), z_like(self.v)
+        self.coef_u, self.b_u = z((5, nx + 3, ny + 2), **f64), z_like(self.u)
+        self.coef_v, self.b_v = z((5, nx + 2, ny + 3), **f64), z_like(self.v)
+        self.coef_p, self.b_p = z((5, nx + 2, ny + 2), **f64), z_like(self.p)
+        if precision == "mixed":
+            self.coef_u32, self.b_u32 = z((5, nx + 3, ny + 2), **f32), z((nx + 3, ny + 2), **f32)
+            self.coef_v32, self.b_v32 = z((5, nx + 2, ny + 3), **f32), z((nx + 2, ny + 3), **f32)
+            self.coef_p32, self.b_p32 = z((5, nx + 2, ny + 2), **f32), z((nx + 2, ny + 2), **f32)
+        else:
+            self.coef_u32 = self.b_u32 = self.coef_v32 = self.b_v32 = self.coef_p32 = self.b_p32 = None
+        self.mass = z(2, **f64)
+        self.pmax = z(1, **f64)
+        self.rws = torch.zeros(L.load().kc_reduce_ws_bytes(), dtype=torch.uint8, device=self.device)
+        self.ws_u, self.ws_v, self.ws_p = Workspace(self.device), Workspace(self.device), Workspace(self.device)
+        self.A_u, self.A_v, self.A_p = Stencil(self.coef_u), Stencil(self.coef_v), Stencil(self.coef_p)
+        if precision == "mixed":
+            self.A_u32, self.A_v32, self.A_p32 = Stencil(self.coef_u32), Stencil(self.coef_v32), Stencil(self.coef_p32)
+        ph = L.KcPhys()
+        ph.nx, ph.ny, ph.mode = nx, ny, L.MODE_CHANNEL
+        ph.dx, ph.dy, ph.rho, ph.mu, ph.dt, ph.U = cfg.dx, cfg.dy, cfg.rho, cfg.mu, cfg.dt, cfg.U
+        ph.alpha_m, ph.alpha_u, ph.alpha_p = cfg.alpha_m, cfg.alpha_u, cfg.alpha_p
+        self.phys = ph
+        self.history = []        # per time step: list of per-outer-iteration records
+        self.reset()
+
+    # ---- state ------------------------------------------------------------------
+    def reset(self, seed=None):
+        cfg = self.cfg
+        u, v, p = geometry.channel_initial_fields(cfg.nx, cfg.ny, self.solid_np, cfg.U, cfg.noise,
+                                                  cfg.seed if seed is None else seed)
+        self.set_state(u, v, p)
+
+    def set_state(self, u, v, p, u0=None, v0=None):
+        def put(dst, src):
+            src = torch.as_tensor(src, dtype=torch.float64)
+            dst.copy_(src.to(self.device, non_blocking=True))
+        put(self.u, u); put(self.v, v); put(self.p, p)
+        put(self.u0, u if u0 is None else u0); put(self.v0, v if v0 is None else v0)
+        self.pcor.zero_()
+
+    def state_numpy(self):
+        return {k: getattr(self, k).cpu().numpy() for k in ("u", "v", "p", "u0", "v0", "pcor")}
+
+    # ---- stages -----------------------------------------------------------------
+    def _s(self):
+        return stream_handle(self.device)
+
+    def assemble_momentum(self):
+        lib = L.load()
+        L.check(lib.kc_assemble_momentum(C.byref(self.phys), ptr(self.u), ptr(self.v), ptr(self.p), ptr(self.u0),
+                                         ptr(self.v0), ptr(self.solid), ptr(self.coef_u), ptr(self.b_u),
+                                         ptr(self.coef_v), ptr(self.b_v), ptr(self.coef_u32), ptr(self.b_u32),
+                                         ptr(self.coef_v32), ptr(self.b_v32), self._s()), "kc_assemble_momentum")
+
+    def _solve(self, A, A32, b, x, ws):
+        cfg = self.cfg
+        if self.precision == "fp64":
+            return bicgstab(A, b, x, eps=cfg.eps, max_iter=A.n, ws=ws, use_graph=self.use_graph)
+        return bicgstab_refined(A, A32, b, x, eps=cfg.eps, eps_inner=self.eps_inner, ws=ws,
+                                use_graph=self.use_graph)
+
+    def solve_momentum(self):
+        iu = self._solve(self.A_u, getattr(self, "A_u32", None), self.b_u, self.u_mid, self.ws_u)
+        iv = self._solve(self.A_v, getattr(self, "A_v32", None), self.b_v, self.v_mid, self.ws_v)
+        return iu, iv
+
+    def relax(self):
+        lib = L.load()
+        L.check(lib.kc_relax_velocity(C.byref(self.phys), ptr(self.solid), ptr(self.u_mid), ptr(self.v_mid),
+                                      ptr(self.u), ptr(self.v), None, ptr(self.rws), self._s()), "kc_relax_velocity")
+        L.check(lib.kc_outlet_conserve(C.byref(self.phys), ptr(self.u), self._s()), "kc_outlet_conserve")
+
+    def assemble_p(self):
+        lib = L.load()
+        L.check(lib.kc_assemble_pcorr(C.byref(self.phys), ptr(self.u), ptr(self.v), ptr(self.coef_u),
+                                      ptr(self.coef_v), ptr(self.solid), ptr(self.coef_p), ptr(self.b_p),
+                                      ptr(self.coef_p32), ptr(self.b_p32), None, ptr(self.mass), ptr(self.rws),
+                                      self._s()), "kc_assemble_pcorr")
+
+    def solve_p(self):
+        if self.learned is not None:
+            return self.learned.solve(self)
+        return self._solve(self.A_p, getattr(self, "A_p32", None), self.b_p, self.pcor, self.ws_p)
+
+    def correct(self):
+        lib = L.load()
+        L.check(lib.kc_correct(C.byref(self.phys), ptr(self.pcor), ptr(self.coef_u), ptr(self.coef_v),
+                               ptr(self.solid), ptr(self.u), ptr(self.v), ptr(self.p), ptr(self.pmax),
+                               ptr(self.rws), self._s()), "kc_correct")
+
+    def time_forward(self):
+        lib = L.load()
+        L.check(lib.kc_copy(ptr(self.u0), ptr(self.u), self.u.numel() * 8, self._s()), "kc_copy")
+        L.check(lib.kc_copy(ptr(self.v0), ptr(self.v), self.v.numel() * 8, self._s()), "kc_copy")
+
+    def outer_iteration(self):
+        self.assemble_momentum()
+        iu, iv = self.solve_momentum()
+        self.relax()
+        self.assemble_p()
+        ip = self.solve_p()
+        self.correct()
+        mass = float(self.mass[0].item())
+        return dict(mass=mass, it_u=iu.iters, it_v=iv.iters, it_p=ip.iters,
+                    st=(iu.status, iv.status, ip.status), ref=(iu.refinements, iv.refinements, ip.refinements))
+
+    def step(self):
+        """One time step; returns the per-outer-iteration records."""
+        rec = []
+        for _ in range(self.cfg.max_outer):
+            s = self.outer_iteration()
+            rec.append(s)
+            if s["mass"] <= self.cfg.mass_tol:
+                break
+        self.time_forward()
+        self.history.append(rec)
+        return rec
+
+    def run(self, n_steps=None, callback=None):
+        n = self.cfg.n_steps if n_steps is None else n_steps
+        for k in range(n):
+            t = time.perf_counter()
+            rec = self.step()
+            if callback:
+                callback(k, rec, time.perf_counter() - t)
+        return self.history
+
+    def mass_residual(self) -> float:
+        """max |mdiv| of the current (corrected) field."""
+        lib = L.load()
+        out = torch.zeros(2, dtype=torch.float64, device=self.device)
+        L.check(lib.kc_mass_residual(C.byref(self.phys), ptr(self.u), ptr(self.v), ptr(self.solid), None,
+                                     ptr(out), ptr(self.rws), self._s()), "kc_mass_residual")
+        return float(out[0].item())
+
+
+def z_like(t):
+    return torch.zeros_like(t)

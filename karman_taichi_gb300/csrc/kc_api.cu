@@ -1,0 +1,64 @@
+// Library-level entry points of libkarman_gb300: version, status strings,
+// thread-local error text and device-to-device copies.
+#include "kc_common.cuh"
+#include <stdarg.h>
+#include <stdio.h>
+
+namespace kc {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+    set_error("%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    return KC_ERR_CUDA;
+}
+
+}  // namespace kc
+
+extern "C" {
+
+int kc_version(void) { return 10000; }
+
+const char* kc_status_str(int status) {
+    switch (status) {
+        case KC_OK: return "converged";
+        case KC_MAXITER: return "iteration cap reached";
+        case KC_BREAKDOWN_RHO: return "breakdown: rho == 0";
+        case KC_BREAKDOWN_OMEGA: return "breakdown: omega == 0";
+        case KC_NONFINITE: return "non-finite value in the recurrence";
+        case KC_STALL: return "residual stalled";
+        case KC_ERR_ARG: return "invalid argument";
+        case KC_ERR_CUDA: return "CUDA error";
+        case KC_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
+        case KC_ERR_UNSUPPORTED: return "unsupported configuration";
+        default: return "unknown status";
+    }
+}
+
+const char* kc_last_error(void) { return kc::g_err; }
+
+int kc_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int kc_copy(void* dst, const void* src, size_t bytes, void* stream) {
+    if (!dst || !src) return kc::set_error("kc_copy: null pointer"), KC_ERR_ARG;
+    if (bytes == 0) return KC_OK;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, kc::as_stream(stream));
+    if (e != cudaSuccess) return kc::cuda_status(e, "kc_copy");
+    return KC_OK;
+}
+
+}  // extern "C"

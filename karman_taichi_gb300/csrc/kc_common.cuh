@@ -1,0 +1,138 @@
+// Shared device helpers for libkarman_gb300: error reporting, deterministic
+// block reductions and the "last block finalises" ticket.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+#include "karman_gb300.h"
+
+namespace kc {
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---- host-side error bookkeeping (thread local message) -------------------
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+#define KC_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return ::kc::cuda_status(e_, #call); \
+    } while (0)
+#define KC_LAUNCH_CHECK(what)                                      \
+    do {                                                           \
+        cudaError_t e_ = cudaGetLastError();                       \
+        if (e_ != cudaSuccess) return ::kc::cuda_status(e_, what); \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// ---- warp / block reductions (fixed order => bitwise reproducible) --------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(kFull, v, o));
+    return v;
+}
+
+// Sums NV values over the block; the result is valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = warp_sum(v[q]);
+        if (lane == 0) sh[q][w] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = lane < nw ? sh[q][lane] : 0.0;
+            v[q] = warp_sum(s);
+        }
+    }
+    __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ void block_max(double (&v)[NV]) {
+    __shared__ double sh[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = warp_max(v[q]);
+        if (lane == 0) sh[q][w] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = lane < nw ? sh[q][lane] : 0.0;
+            v[q] = warp_max(s);
+        }
+    }
+    __syncthreads();
+}
+
+// Every block calls this after writing its partials; returns true in exactly
+// one block (the last to arrive), which then owns the final reduction and
+// resets the ticket.  No block ever waits on another.
+__device__ __forceinline__ bool arrive_last(unsigned* ticket, unsigned nblocks) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == nblocks - 1);
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// Fixed-order sum of partials[0..count) (stride between vectors: ld) for NV
+// vectors, executed by one whole block; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void reduce_partials(const double* partials, int ld, int count,
+                                                double (&out)[NV]) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < count; i += blockDim.x)
+            s += __ldcg(partials + q * ld + i);
+        out[q] = s;
+    }
+    block_sum<NV>(out);
+}
+
+template <int NV>
+__device__ __forceinline__ void reduce_partials_max(const double* partials, int ld, int count,
+                                                    double (&out)[NV]) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < count; i += blockDim.x)
+            s = fmax(s, __ldcg(partials + q * ld + i));
+        out[q] = s;
+    }
+    block_max<NV>(out);
+}
+
+// Small reduction workspace used by assembly / correction kernels.
+struct ReduceWs {
+    unsigned ticket[8];
+    double pad[4];
+    double partials[4][4096];
+};
+constexpr int kReduceMaxBlocks = 4096;
+
+}  // namespace kc

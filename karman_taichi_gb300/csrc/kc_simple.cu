@@ -1,0 +1,671 @@
+// SIMPLE assembly and correction kernels on staggered padded fields.
+//
+// Reference behaviour (houkensjtu/karman_taichi):
+//   compute_coef_u / compute_coef_v   simple.py:77-110   (mid-point convection + diffusion)
+//   set_bc                            simple.py:172-216  (east wall adds aW: simple.py:215;
+//                                                         bicgsimp.py:196 adds aE)
+//   compute_mdiv / compute_coef_p     simple.py:137-170, bicgsimp.py:114-151
+//   correct_pressure/velocity         simple.py:218-230
+//   update_velocity                   simple.py:232-238, bicgsimp.py:212-225
+//   outlet zero gradient + rescale    karman_taichi.py:178-183, 586-601
+//
+// Field layout (row-major, j fastest): u [nx+3][ny+2], v [nx+2][ny+3],
+// p [nx+2][ny+2]; coefficient outputs are 5 SoA planes over the same padded
+// field followed by b.  One thread owns one face/cell; faces that are not
+// unknowns become zero rows (so a solver over the whole padded field leaves
+// them at 0, as the reference's full-field solves do), blocked faces in the
+// channel mode become identity rows.
+//
+// This file is compiled with -fmad=false: the coefficient expressions keep
+// the reference's left-to-right IEEE operation order, so the CPU restatement
+// reproduces them bit for bit.
+#include "kc_common.cuh"
+#include <algorithm>
+
+namespace kc {
+
+struct Dims {
+    int nx, ny;
+    int NYu, NYv, NYp;
+};
+__host__ __device__ inline Dims dims_of(const kc_phys& P) { return {P.nx, P.ny, P.ny + 2, P.ny + 3, P.ny + 2}; }
+
+struct Solid {
+    const unsigned char* s;
+    int NYp;
+    __device__ __forceinline__ bool cell(int i, int j) const { return s && s[(long long)i * NYp + j]; }
+    // u face (i,j) lies between cells (i-1,j) and (i,j)
+    __device__ __forceinline__ bool bu(int i, int j) const { return cell(i - 1, j) || cell(i, j); }
+    // v face (i,j) lies between cells (i,j-1) and (i,j)
+    __device__ __forceinline__ bool bv(int i, int j) const { return cell(i, j - 1) || cell(i, j); }
+};
+
+__device__ __forceinline__ bool unk_u(const kc_phys& P, const Solid& S, int i, int j) {
+    if (i < 2 || i > P.nx || j < 1 || j > P.ny) return false;
+    return P.mode != KC_MODE_CHANNEL || !S.bu(i, j);
+}
+__device__ __forceinline__ bool unk_v(const kc_phys& P, const Solid& S, int i, int j) {
+    if (i < 1 || i > P.nx || j < 2 || j > P.ny) return false;
+    return P.mode != KC_MODE_CHANNEL || !S.bv(i, j);
+}
+
+// ---- momentum ---------------------------------------------------------------
+__device__ void u_row(const kc_phys& P, const Dims& D, const Solid& S, const double* u, const double* v,
+                      const double* p, const double* u0, int i, int j, double (&c)[5], double& b) {
+    c[0] = c[1] = c[2] = c[3] = c[4] = 0.0;
+    b = 0.0;
+    const int nx = D.nx, ny = D.ny;
+    if (i < 2 || i > nx || j < 1 || j > ny) return;
+    if (P.mode == KC_MODE_CHANNEL && S.bu(i, j)) {
+        c[0] = 1.0;
+        return;
+    }
+    const double mu = P.mu, rho = P.rho, dx = P.dx, dy = P.dy, dt = P.dt;
+#define U_(a, bb) u[(long long)(a) * D.NYu + (bb)]
+#define V_(a, bb) v[(long long)(a) * D.NYv + (bb)]
+#define P_(a, bb) p[(long long)(a) * D.NYp + (bb)]
+    const double ui = U_(i, j), uw = U_(i - 1, j), ue = U_(i + 1, j);
+    const double vnw = V_(i - 1, j + 1), vne = V_(i, j + 1), vsw = V_(i - 1, j), vse = V_(i, j);
+    double aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (ui + uw) * dy);
+    double aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ui + ue) * dy);
+    double aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vnw + vne) * dx);
+    double aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vsw + vse) * dx);
+    double aP = -(aW + aE + aN + aS) + rho * 0.5 * (ui + ue) * dy - rho * 0.5 * (ui + uw) * dy +
+                rho * 0.5 * (vnw + vne) * dx - rho * 0.5 * (vsw + vse) * dx + rho * dx * dy / dt;
+    double bb = (P_(i - 1, j) - P_(i, j)) * dy + rho * dx * dy / dt * u0[(long long)i * D.NYu + j];
+    if (P.mode == KC_MODE_CHANNEL) {
+        const double wall = 2 * mu * dx / dy;
+        if (i == 2) {
+            bb += -aW * P.U;
+            aW = 0.0;
+        } else if (S.bu(i - 1, j)) {
+            aW = 0.0;
+        }
+        if (i == nx) {
+            aP = aP + aE;
+            aE = 0.0;
+        } else if (S.bu(i + 1, j)) {
+            aE = 0.0;
+        }
+        if (j == 1 || S.bu(i, j - 1)) {
+            aP = aP + (aS + wall);
+            aS = 0.0;
+        }
+        if (j == ny || S.bu(i, j + 1)) {
+            aP = aP + (aN + wall);
+            aN = 0.0;
+        }
+    } else {
+        // set_bc, simple.py:177-207 (w, e, then south/north sliding walls)
+        if (i == 2) {
+            bb += -aW * P.bc[0][0];
+            aW = 0.0;
+        }
+        if (i == nx) {
+            bb += -aE * P.bc[1][0];
+            aE = 0.0;
+        }
+        if (j == 1) {
+            bb += 2 * mu * P.bc[3][1] * dx / dy;
+            aP += (aS + 2 * mu * dx / dy);
+            aS = 0.0;
+        }
+        if (j == ny) {
+            bb += 2 * mu * P.bc[2][1] * dx / dy;
+            aP += (aN + 2 * mu * dx / dy);
+            aN = 0.0;
+        }
+    }
+    c[0] = aP;
+    c[1] = aW;
+    c[2] = aE;
+    c[3] = aN;
+    c[4] = aS;
+    b = bb;
+}
+
+__device__ void v_row(const kc_phys& P, const Dims& D, const Solid& S, const double* u, const double* v,
+                      const double* p, const double* v0, int i, int j, double (&c)[5], double& b) {
+    c[0] = c[1] = c[2] = c[3] = c[4] = 0.0;
+    b = 0.0;
+    const int nx = D.nx, ny = D.ny;
+    if (i < 1 || i > nx || j < 2 || j > ny) return;
+    if (P.mode == KC_MODE_CHANNEL && S.bv(i, j)) {
+        c[0] = 1.0;
+        return;
+    }
+    const double mu = P.mu, rho = P.rho, dx = P.dx, dy = P.dy, dt = P.dt;
+    const double uc = U_(i, j), us = U_(i, j - 1), uec = U_(i + 1, j), ues = U_(i + 1, j - 1);
+    const double vc = V_(i, j), vn = V_(i, j + 1), vs = V_(i, j - 1);
+    double aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (uc + us) * dy);
+    double aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ues + uec) * dy);
+    double aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vn + vc) * dx);
+    double aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vs + vc) * dx);
+    double aP = -(aW + aE + aN + aS) + rho * 0.5 * (ues + uec) * dy - rho * 0.5 * (uc + us) * dy +
+                rho * 0.5 * (vn + vc) * dx - rho * 0.5 * (vs + vc) * dx + rho * dx * dy / dt;
+    double bb = (P_(i, j - 1) - P_(i, j)) * dx + rho * dx * dy / dt * v0[(long long)i * D.NYv + j];
+    if (P.mode == KC_MODE_CHANNEL) {
+        const double wall = 2 * mu * dy / dx;
+        if (j == 2 || S.bv(i, j - 1)) aS = 0.0;
+        if (j == ny || S.bv(i, j + 1)) aN = 0.0;
+        if (i == 1 || S.bv(i - 1, j)) {
+            aP = aP + (aW + wall);
+            aW = 0.0;
+        }
+        if (i == nx) {
+            aP = aP + aE;
+            aE = 0.0;
+        } else if (S.bv(i + 1, j)) {
+            aP = aP + (aE + wall);
+            aE = 0.0;
+        }
+    } else {
+        // set_bc, simple.py:188-216 (s, n, then west/east sliding walls)
+        if (j == 2) {
+            bb += -aS * P.bc[3][0];
+            aS = 0.0;
+        }
+        if (j == ny) {
+            bb += -aN * P.bc[2][0];
+            aN = 0.0;
+        }
+        if (i == 1) {
+            bb += 2 * mu * P.bc[0][1] * dy / dx;
+            aP += (aW + 2 * mu * dy / dx);
+            aW = 0.0;
+        }
+        if (i == nx) {
+            bb += 2 * mu * P.bc[1][1] * dy / dx;
+            aP += ((P.mode == KC_MODE_BICGSIMP ? aE : aW) + 2 * mu * dy / dx);
+            aE = 0.0;
+        }
+    }
+    c[0] = aP;
+    c[1] = aW;
+    c[2] = aE;
+    c[3] = aN;
+    c[4] = aS;
+    b = bb;
+}
+
+struct MomOut {
+    double *cu, *bu, *cv, *bv;
+    float *cu32, *bu32, *cv32, *bv32;
+};
+
+__global__ void __launch_bounds__(256)
+    k_assemble_momentum(kc_phys P, const double* u, const double* v, const double* p, const double* u0,
+                        const double* v0, const unsigned char* solid, MomOut O) {
+    const Dims D = dims_of(P);
+    const Solid S{solid, D.NYp};
+    const bool isv = blockIdx.z == 1;
+    const int NX = isv ? D.nx + 2 : D.nx + 3, NY = isv ? D.NYv : D.NYu;
+    const long long n = (long long)NX * NY;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    if (j >= NY) return;
+    for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+        double c[5], b;
+        const long long k = (long long)i * NY + j;
+        if (isv) {
+            v_row(P, D, S, u, v, p, v0, i, j, c, b);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) O.cv[q * n + k] = c[q];
+            O.bv[k] = b;
+            if (O.cv32) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) O.cv32[q * n + k] = (float)c[q];
+                O.bv32[k] = (float)b;
+            }
+        } else {
+            u_row(P, D, S, u, v, p, u0, i, j, c, b);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) O.cu[q * n + k] = c[q];
+            O.bu[k] = b;
+            if (O.cu32) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) O.cu32[q * n + k] = (float)c[q];
+                O.bu32[k] = (float)b;
+            }
+        }
+    }
+}
+
+__global__ void k_apply_bc_values(kc_phys P, double* u, double* v) {
+    const Dims D = dims_of(P);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 1 && t <= D.ny) {
+        u[(long long)1 * D.NYu + t] = P.bc[0][0];
+        u[(long long)(D.nx + 1) * D.NYu + t] = P.bc[1][0];
+    }
+    if (t >= 1 && t <= D.nx) {
+        v[(long long)t * D.NYv + 1] = P.bc[3][0];
+        v[(long long)t * D.NYv + D.ny + 1] = P.bc[2][0];
+    }
+}
+
+// ---- under-relaxation --------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_relax(kc_phys P, const unsigned char* solid, const double* um, const double* vm, double* u, double* v,
+            ReduceWs* ws, double* diff_out) {
+    const Dims D = dims_of(P);
+    const Solid S{solid, D.NYp};
+    const bool isv = blockIdx.z == 1;
+    const int NX = isv ? D.nx + 2 : D.nx + 3, NY = isv ? D.NYv : D.NYu;
+    const double a = P.alpha_m;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    double dm[1] = {0.0};
+    if (j < NY) {
+        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+            const long long k = (long long)i * NY + j;
+            if (isv ? unk_v(P, S, i, j) : unk_u(P, S, i, j)) {
+                const double* mid = isv ? vm : um;
+                double* f = isv ? v : u;
+                const double m = mid[k], old = f[k];
+                dm[0] = fmax(dm[0], fabs(m - old));
+                f[k] = a * m + (1 - a) * old;
+            }
+        }
+    }
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    // block max (reuse block_max with linear thread index)
+    __shared__ double sh[8];
+    double wv = warp_max(dm[0]);
+    if ((tid & 31) == 0) sh[tid >> 5] = wv;
+    __syncthreads();
+    const int nbz = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < 8; ++q) m = fmax(m, sh[q]);
+        ws->partials[blockIdx.z][bid] = m;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(2 * nbz - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (tid == 0) {
+        double du = 0.0, dv = 0.0;
+        for (int q = 0; q < nbz; ++q) {
+            du = fmax(du, __ldcg(&ws->partials[0][q]));
+            dv = fmax(dv, __ldcg(&ws->partials[1][q]));
+        }
+        if (diff_out) *diff_out = sqrt(du * du + dv * dv);
+        ws->ticket[0] = 0;
+    }
+}
+
+// ---- channel outlet: zero gradient + mass-flow rescale (single block) --------
+__global__ void __launch_bounds__(256) k_outlet_conserve(kc_phys P, double* u) {
+    const Dims D = dims_of(P);
+    double acc[2] = {0.0, 0.0};
+    for (int j = 1 + threadIdx.x; j <= D.ny; j += blockDim.x) {
+        const double w = u[(long long)D.nx * D.NYu + j];
+        u[(long long)(D.nx + 1) * D.NYu + j] = w;
+        acc[0] += u[(long long)1 * D.NYu + j];
+        acc[1] += w;
+    }
+    block_sum<2>(acc);
+    __shared__ double coef;
+    if (threadIdx.x == 0) coef = acc[0] / acc[1];
+    __syncthreads();
+    for (int j = 1 + threadIdx.x; j <= D.ny; j += blockDim.x) {
+        double* o = u + (long long)(D.nx + 1) * D.NYu + j;
+        *o = coef * *o;
+    }
+}
+
+// ---- pressure correction -----------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_assemble_pcorr(kc_phys P, const double* u, const double* v, const double* apu, const double* apv,
+                     const unsigned char* solid, double* cp, double* bp, float* cp32, float* bp32,
+                     double* mdiv_out, ReduceWs* ws, double* mass_out) {
+    const Dims D = dims_of(P);
+    const Solid S{solid, D.NYp};
+    const int NX = D.nx + 2, NY = D.NYp;
+    const long long n = (long long)NX * NY;
+    const int nx = D.nx, ny = D.ny;
+    const double rho = P.rho, dx = P.dx, dy = P.dy;
+    const bool channel = P.mode == KC_MODE_CHANNEL;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    double mx[1] = {0.0}, sq[1] = {0.0};
+    if (j < NY) {
+        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+            const long long k = (long long)i * NY + j;
+            double c[5] = {0, 0, 0, 0, 0}, b = 0.0;
+            if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
+                const double md = rho * (U_(i, j) - U_(i + 1, j)) * dy + rho * (V_(i, j) - V_(i, j + 1)) * dx;
+                if (mdiv_out) mdiv_out[k] = md;
+                if (channel && S.cell(i, j)) {
+                    c[0] = 1.0;
+                } else if (channel) {
+                    double aW = 0.0, aE = 0.0, aN = 0.0, aS = 0.0;
+                    if (unk_u(P, S, i, j)) aW = -rho * dy * dy / apu[(long long)i * D.NYu + j];
+                    if (unk_u(P, S, i + 1, j)) aE = -rho * dy * dy / apu[(long long)(i + 1) * D.NYu + j];
+                    if (i == nx && unk_u(P, S, nx, j)) aE = -rho * dy * dy / apu[(long long)nx * D.NYu + j];
+                    if (unk_v(P, S, i, j + 1)) aN = -rho * dx * dx / apv[(long long)i * D.NYv + j + 1];
+                    if (unk_v(P, S, i, j)) aS = -rho * dx * dx / apv[(long long)i * D.NYv + j];
+                    c[0] = -(aW + aE + aN + aS);
+                    c[1] = aW;
+                    c[2] = aE;
+                    c[3] = aN;
+                    c[4] = aS;
+                    b = md;
+                    mx[0] = fmax(mx[0], fabs(md));
+                    sq[0] += md * md;
+                } else {
+                    // compute_coef_p, simple.py:146-163 (bicgsimp.py:146-151 pins (1,1))
+                    double aW = i == 1 ? 0.0 : -rho * dy * dy / apu[(long long)i * D.NYu + j];
+                    double aE = i == nx ? 0.0 : -rho * dy * dy / apu[(long long)(i + 1) * D.NYu + j];
+                    double aN = j == ny ? 0.0 : -rho * dx * dx / apv[(long long)i * D.NYv + j + 1];
+                    double aS = j == 1 ? 0.0 : -rho * dx * dx / apv[(long long)i * D.NYv + j];
+                    c[0] = -(aW + aE + aN + aS);
+                    c[1] = aW;
+                    c[2] = aE;
+                    c[3] = aN;
+                    c[4] = aS;
+                    b = md;
+                    if (P.mode == KC_MODE_BICGSIMP && i == 1 && j == 1) {
+                        c[1] = c[2] = c[3] = c[4] = 0.0;
+                        c[0] = 1.0;
+                        b = 0.0;
+                    }
+                    mx[0] = fmax(mx[0], fabs(md));
+                    sq[0] += md * md;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; ++q) cp[q * n + k] = c[q];
+            bp[k] = b;
+            if (cp32) {
+#pragma unroll
+                for (int q = 0; q < 5; ++q) cp32[q * n + k] = (float)c[q];
+                bp32[k] = (float)b;
+            }
+        }
+    }
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    __shared__ double shm[8], shs[8];
+    double a = warp_max(mx[0]), s2 = warp_sum(sq[0]);
+    if ((tid & 31) == 0) {
+        shm[tid >> 5] = a;
+        shs[tid >> 5] = s2;
+    }
+    __syncthreads();
+    const int nb = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        double m = 0.0, s = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            m = fmax(m, shm[q]);
+            s += shs[q];
+        }
+        ws->partials[0][bid] = m;
+        ws->partials[1][bid] = s;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(nb - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (tid == 0) {
+        double m = 0.0, s = 0.0;
+        for (int q = 0; q < nb; ++q) {
+            m = fmax(m, __ldcg(&ws->partials[0][q]));
+            s += __ldcg(&ws->partials[1][q]);
+        }
+        if (mass_out) {
+            mass_out[0] = m;
+            mass_out[1] = s;
+        }
+        ws->ticket[0] = 0;
+    }
+}
+
+// ---- correction: z = 0 u faces, 1 v faces, 2 p cells --------------------------
+__global__ void __launch_bounds__(256)
+    k_correct(kc_phys P, const double* pc, const double* apu, const double* apv, const unsigned char* solid,
+              double* u, double* v, double* p, ReduceWs* ws, double* pmax_out) {
+    const Dims D = dims_of(P);
+    const Solid S{solid, D.NYp};
+    const int z = blockIdx.z;
+    const int NX = z == 0 ? D.nx + 3 : D.nx + 2;
+    const int NY = z == 0 ? D.NYu : (z == 1 ? D.NYv : D.NYp);
+    const int nx = D.nx, ny = D.ny;
+    const bool channel = P.mode == KC_MODE_CHANNEL;
+    const double au = P.alpha_u, ap = P.alpha_p, dx = P.dx, dy = P.dy;
+#define PC_(a, bb) pc[(long long)(a) * D.NYp + (bb)]
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    double mx = 0.0;
+    if (j < NY) {
+        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+            const long long k = (long long)i * NY + j;
+            if (z == 0) {
+                if (unk_u(P, S, i, j)) {
+                    u[k] = u[k] + au * (PC_(i - 1, j) - PC_(i, j)) * dy / apu[k];
+                } else if (channel && i == nx + 1 && j >= 1 && j <= ny && unk_u(P, S, nx, j)) {
+                    u[k] = u[k] + au * (PC_(nx, j) - PC_(nx + 1, j)) * dy / apu[(long long)nx * D.NYu + j];
+                }
+            } else if (z == 1) {
+                if (unk_v(P, S, i, j)) v[k] = v[k] + au * (PC_(i, j - 1) - PC_(i, j)) * dx / apv[k];
+            } else {
+                const double q = pc[k];
+                mx = fmax(mx, fabs(q));
+                if (i >= 1 && i <= nx && j >= 1 && j <= ny && !(channel && S.cell(i, j))) p[k] = p[k] + ap * q;
+            }
+        }
+    }
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    __shared__ double shm[8];
+    double a = warp_max(mx);
+    if ((tid & 31) == 0) shm[tid >> 5] = a;
+    __syncthreads();
+    const int nbz = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < 8; ++q) m = fmax(m, shm[q]);
+        ws->partials[z][bid] = m;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(3 * nbz - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < nbz; ++q) m = fmax(m, __ldcg(&ws->partials[2][q]));
+        if (pmax_out) *pmax_out = m;
+        ws->ticket[0] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_mass_residual(kc_phys P, const double* u, const double* v, const unsigned char* solid, double* mdiv_out,
+                    ReduceWs* ws, double* mass_out) {
+    const Dims D = dims_of(P);
+    const Solid S{solid, D.NYp};
+    const int NX = D.nx + 2, NY = D.NYp;
+    const double rho = P.rho, dx = P.dx, dy = P.dy;
+    const bool channel = P.mode == KC_MODE_CHANNEL;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    double mx = 0.0, sq = 0.0;
+    if (j >= 1 && j <= D.ny) {
+        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+            if (i < 1 || i > D.nx) continue;
+            const long long k = (long long)i * NY + j;
+            double md = rho * (U_(i, j) - U_(i + 1, j)) * dy + rho * (V_(i, j) - V_(i, j + 1)) * dx;
+            if (mdiv_out) mdiv_out[k] = md;
+            if (channel && S.cell(i, j)) continue;
+            mx = fmax(mx, fabs(md));
+            sq += md * md;
+        }
+    }
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    __shared__ double shm[8], shs[8];
+    double a = warp_max(mx), s2 = warp_sum(sq);
+    if ((tid & 31) == 0) {
+        shm[tid >> 5] = a;
+        shs[tid >> 5] = s2;
+    }
+    __syncthreads();
+    const int nb = gridDim.x * gridDim.y;
+    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        double m = 0.0, s = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            m = fmax(m, shm[q]);
+            s += shs[q];
+        }
+        ws->partials[0][bid] = m;
+        ws->partials[1][bid] = s;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(nb - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (tid == 0) {
+        double m = 0.0, s = 0.0;
+        for (int q = 0; q < nb; ++q) {
+            m = fmax(m, __ldcg(&ws->partials[0][q]));
+            s += __ldcg(&ws->partials[1][q]);
+        }
+        mass_out[0] = m;
+        mass_out[1] = s;
+        ws->ticket[0] = 0;
+    }
+}
+#undef U_
+#undef V_
+#undef P_
+#undef PC_
+
+static dim3 field_grid(int NX, int NY, int zdim) {
+    int gx = (NY + 31) / 32;
+    int gy = (NX + 7) / 8;
+    int cap = std::max(1, kReduceMaxBlocks / (gx > 0 ? gx : 1));
+    if (gy > cap) gy = cap;
+    if (gy > 64) gy = 64;
+    return dim3(gx, gy, zdim);
+}
+
+static int check_phys(const kc_phys* P) {
+    if (!P) return set_error("kc_phys is null"), KC_ERR_ARG;
+    if (P->nx < 2 || P->ny < 2) return set_error("kc_phys: nx=%d ny=%d must be >= 2", P->nx, P->ny), KC_ERR_ARG;
+    if (P->mode < KC_MODE_SIMPLE || P->mode > KC_MODE_CHANNEL)
+        return set_error("kc_phys: unknown mode %d", P->mode), KC_ERR_ARG;
+    if ((long long)(P->ny + 3 + 31) / 32 > kReduceMaxBlocks)
+        return set_error("kc_phys: ny=%d too large", P->ny), KC_ERR_ARG;
+    return KC_OK;
+}
+
+}  // namespace kc
+
+using namespace kc;
+
+extern "C" {
+
+size_t kc_reduce_ws_bytes(void) { return sizeof(ReduceWs); }
+
+int kc_assemble_momentum(const kc_phys* P, const double* u, const double* v, const double* p, const double* u0,
+                         const double* v0, const unsigned char* solid, double* coef_u, double* b_u,
+                         double* coef_v, double* b_v, float* coef_u32, float* b_u32, float* coef_v32,
+                         float* b_v32, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u || !v || !p || !u0 || !v0 || !coef_u || !b_u || !coef_v || !b_v)
+        return set_error("kc_assemble_momentum: null field"), KC_ERR_ARG;
+    if (P->mode == KC_MODE_CHANNEL && !solid) solid = nullptr;
+    if ((coef_u32 == nullptr) != (b_u32 == nullptr) || (coef_v32 == nullptr) != (b_v32 == nullptr))
+        return set_error("kc_assemble_momentum: FP32 outputs must be given in pairs"), KC_ERR_ARG;
+    MomOut O{coef_u, b_u, coef_v, b_v, coef_u32, b_u32, coef_v32, b_v32};
+    dim3 g = field_grid(P->nx + 3, P->ny + 3, 2);
+    k_assemble_momentum<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, p, u0, v0, solid, O);
+    KC_LAUNCH_CHECK("k_assemble_momentum");
+    return KC_OK;
+}
+
+int kc_apply_bc_values(const kc_phys* P, double* u, double* v, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u || !v) return set_error("kc_apply_bc_values: null field"), KC_ERR_ARG;
+    int m = std::max(P->nx, P->ny) + 1;
+    k_apply_bc_values<<<(m + 255) / 256, 256, 0, as_stream(stream)>>>(*P, u, v);
+    KC_LAUNCH_CHECK("k_apply_bc_values");
+    return KC_OK;
+}
+
+int kc_relax_velocity(const kc_phys* P, const unsigned char* solid, const double* u_mid, const double* v_mid,
+                      double* u, double* v, double* diff_dev, void* ws, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u_mid || !v_mid || !u || !v) return set_error("kc_relax_velocity: null field"), KC_ERR_ARG;
+    if (!ws) return set_error("kc_relax_velocity: null workspace"), KC_ERR_WORKSPACE;
+    dim3 g = field_grid(P->nx + 3, P->ny + 3, 2);
+    k_relax<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, solid, u_mid, v_mid, u, v, (ReduceWs*)ws, diff_dev);
+    KC_LAUNCH_CHECK("k_relax");
+    return KC_OK;
+}
+
+int kc_outlet_conserve(const kc_phys* P, double* u, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u) return set_error("kc_outlet_conserve: null u"), KC_ERR_ARG;
+    k_outlet_conserve<<<1, 256, 0, as_stream(stream)>>>(*P, u);
+    KC_LAUNCH_CHECK("k_outlet_conserve");
+    return KC_OK;
+}
+
+int kc_assemble_pcorr(const kc_phys* P, const double* u, const double* v, const double* coef_u,
+                      const double* coef_v, const unsigned char* solid, double* coef_p, double* b_p,
+                      float* coef_p32, float* b_p32, double* mdiv, double* mass_dev, void* ws, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u || !v || !coef_u || !coef_v || !coef_p || !b_p)
+        return set_error("kc_assemble_pcorr: null field"), KC_ERR_ARG;
+    if ((coef_p32 == nullptr) != (b_p32 == nullptr))
+        return set_error("kc_assemble_pcorr: FP32 outputs must be given in pairs"), KC_ERR_ARG;
+    if (!ws) return set_error("kc_assemble_pcorr: null workspace"), KC_ERR_WORKSPACE;
+    dim3 g = field_grid(P->nx + 2, P->ny + 2, 1);
+    k_assemble_pcorr<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, coef_u, coef_v, solid, coef_p, b_p,
+                                                               coef_p32, b_p32, mdiv, (ReduceWs*)ws, mass_dev);
+    KC_LAUNCH_CHECK("k_assemble_pcorr");
+    return KC_OK;
+}
+
+int kc_correct(const kc_phys* P, const double* pcor, const double* coef_u, const double* coef_v,
+               const unsigned char* solid, double* u, double* v, double* p, double* pcor_max_dev, void* ws,
+               void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!pcor || !coef_u || !coef_v || !u || !v || !p) return set_error("kc_correct: null field"), KC_ERR_ARG;
+    if (!ws) return set_error("kc_correct: null workspace"), KC_ERR_WORKSPACE;
+    dim3 g = field_grid(P->nx + 3, P->ny + 3, 3);
+    k_correct<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, pcor, coef_u, coef_v, solid, u, v, p, (ReduceWs*)ws,
+                                                        pcor_max_dev);
+    KC_LAUNCH_CHECK("k_correct");
+    return KC_OK;
+}
+
+int kc_mass_residual(const kc_phys* P, const double* u, const double* v, const unsigned char* solid,
+                     double* mdiv, double* mass_dev, void* ws, void* stream) {
+    int rc = check_phys(P);
+    if (rc) return rc;
+    if (!u || !v || !mass_dev) return set_error("kc_mass_residual: null argument"), KC_ERR_ARG;
+    if (!ws) return set_error("kc_mass_residual: null workspace"), KC_ERR_WORKSPACE;
+    dim3 g = field_grid(P->nx + 2, P->ny + 2, 1);
+    k_mass_residual<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, solid, mdiv, (ReduceWs*)ws, mass_dev);
+    KC_LAUNCH_CHECK("k_mass_residual");
+    return KC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,221 @@
+"""Torch-facing wrappers around the stencil solvers of libkarman_gb300.
+
+Tensors stay on the GPU; every call passes raw device pointers and the
+current torch stream through the C ABI.  Nothing here computes on the host:
+if the library is missing, ``KcLibraryMissing`` is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib as L
+
+
+@dataclass
+class SolveInfo:
+    """Outcome of a solve (the reference returns None and prints instead)."""
+    status: int
+    iters: int
+    rel_res: float
+    r0: float
+    refinements: int = 0
+
+    @property
+    def ok(self) -> bool:
+        return self.status == L.OK
+
+    @property
+    def status_name(self) -> str:
+        return L.status_name(self.status)
+
+
+def ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_handle(device=None):
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def dtype_code(t: torch.Tensor) -> int:
+    if t.dtype == torch.float64:
+        return L.F64
+    if t.dtype == torch.float32:
+        return L.F32
+    raise TypeError(f"unsupported dtype {t.dtype}: expected float64 or float32")
+
+
+def require_cuda(*ts):
+    for t in ts:
+        if t is None:
+            continue
+        if not t.is_cuda:
+            raise ValueError("karman_taichi_gb300 operates on CUDA tensors only (no CPU fallback)")
+        if not t.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+
+
+class Stencil:
+    """5-point stencil operator ``A`` on ``n`` unknowns with far stride ``S``.
+
+    ``coef`` is either SoA planes ``[5, NX, NY]`` / ``[5, n]`` or the
+    reference's array-of-structs ``[NX, NY, 5]`` (simple.py:42-47), read in
+    place without conversion (component stride 1, element stride 5).
+    Component order: aP, aW (k-S), aE (k+S), aN (k+1), aS (k-1).
+    """
+
+    def __init__(self, coef: torch.Tensor, stride: int | None = None, layout: str | None = None):
+        require_cuda(coef)
+        if layout is None:
+            layout = "aos" if (coef.dim() == 3 and coef.shape[-1] == 5 and coef.shape[0] != 5) else "soa"
+        self.coef, self.layout = coef, layout
+        if layout == "aos":
+            NX, NY = coef.shape[0], coef.shape[1]
+            self.n, self.cs, self.es = NX * NY, 1, 5
+            self.stride = NY if stride is None else stride
+            self.shape = (NX, NY)
+        else:
+            if coef.shape[0] != 5:
+                raise ValueError("SoA coefficients must have 5 leading planes")
+            self.n = coef[0].numel()
+            self.cs, self.es = self.n, 1
+            if stride is None:
+                if coef.dim() != 3:
+                    raise ValueError("stride required for flat [5, n] coefficients")
+                stride = coef.shape[2]
+            self.stride = stride
+            self.shape = tuple(coef.shape[1:])
+        self.dtype = dtype_code(coef)
+        self._sys = L.KcSystem(self.n, self.cs, self.es, coef.data_ptr(), int(self.stride), self.dtype)
+
+    @property
+    def system(self) -> L.KcSystem:
+        return self._sys
+
+    @property
+    def device(self):
+        return self.coef.device
+
+
+class Workspace:
+    """Grow-only device scratch buffer (zero-filled on allocation)."""
+
+    def __init__(self, device=None):
+        self.device = device
+        self.buf = None
+
+    def get(self, nbytes: int) -> torch.Tensor:
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = torch.zeros(max(int(nbytes), 256), dtype=torch.uint8, device=self.device)
+        return self.buf
+
+
+def spmv(A: Stencil, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """y = A x (bicgsolver.py:65-76)."""
+    require_cuda(x)
+    if out is None:
+        out = torch.empty_like(x)
+    L.check(L.load().kc_spmv(C.byref(A.system), ptr(x), ptr(out), stream_handle(x.device)), "kc_spmv")
+    return out
+
+
+_dot_ws = {}
+
+
+def dot_device(p: torch.Tensor, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """FP64 sum(p*q) into a 1-element device tensor (no host sync)."""
+    require_cuda(p, q)
+    if p.numel() != q.numel() or p.dtype != q.dtype:
+        raise ValueError("dot: shape/dtype mismatch")
+    dev = p.device
+    lib = L.load()
+    ws = _dot_ws.get(dev)
+    if ws is None:
+        ws = torch.zeros(lib.kc_dot_ws_bytes(p.numel()), dtype=torch.uint8, device=dev)
+        _dot_ws[dev] = ws
+    if out is None:
+        out = torch.empty(1, dtype=torch.float64, device=dev)
+    L.check(lib.kc_dot(dtype_code(p), p.numel(), ptr(p), ptr(q), ptr(out), ptr(ws), ws.numel(),
+                       stream_handle(dev)), "kc_dot")
+    return out
+
+
+def dot(p: torch.Tensor, q: torch.Tensor) -> float:
+    """CGSolver.reduce (cgsolver.py:49-54): returns a Python float (host sync)."""
+    return float(dot_device(p, q).item())
+
+
+def _opts(eps, max_iter, x0, precond, omega_break, rel_to, check_every=0, use_graph=True,
+          history=None):
+    o = L.KcSolveOpts()
+    o.eps, o.max_iter, o.x0, o.precond = float(eps), int(max_iter), int(x0), int(precond)
+    o.omega_break, o.rel_to, o.check_every, o.use_graph = int(omega_break), int(rel_to), int(check_every), int(use_graph)
+    if history is not None:
+        o.history, o.history_len = history.data_ptr(), history.numel()
+    else:
+        o.history, o.history_len = None, 0
+    return o
+
+
+def bicgstab(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None, warm=False,
+             M: torch.Tensor | None = None, omega_break=False, rel_to_b=False, ws: Workspace | None = None,
+             history: torch.Tensor | None = None, check_every=0, use_graph=True) -> SolveInfo:
+    """BiCGSTAB on the device (bicgsolver.py:88-135; karman_taichi.py:342-456)."""
+    require_cuda(b, x, M)
+    if b.numel() != A.n or x.numel() != A.n:
+        raise ValueError(f"b/x have {b.numel()}/{x.numel()} elements, operator has {A.n}")
+    if b.dtype != A.coef.dtype or x.dtype != A.coef.dtype:
+        raise TypeError("b, x and the coefficients must share a dtype")
+    lib = L.load()
+    nbytes = lib.kc_bicgstab_ws_bytes(A.n, A.stride, A.dtype)
+    buf = (ws or Workspace(b.device)).get(nbytes)
+    o = _opts(eps, A.n if max_iter is None else max_iter, L.X0_WARM if warm else L.X0_ZERO,
+              L.PRECOND_JACOBI if M is not None else L.PRECOND_NONE, omega_break,
+              L.REL_B if rel_to_b else L.REL_R0, check_every, use_graph, history)
+    info = L.KcSolveInfo()
+    rc = lib.kc_bicgstab(C.byref(A.system), ptr(b), ptr(x), ptr(M), ptr(buf), buf.numel(), C.byref(o),
+                         C.byref(info), stream_handle(b.device))
+    L.check(rc, "kc_bicgstab")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0)
+
+
+def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None, ws: Workspace | None = None,
+       history: torch.Tensor | None = None, check_every=0, use_graph=True) -> SolveInfo:
+    """Conjugate gradients on the device (cgsolver.py:83-114)."""
+    require_cuda(b, x)
+    if b.numel() != A.n or x.numel() != A.n:
+        raise ValueError("b/x size does not match the operator")
+    lib = L.load()
+    nbytes = lib.kc_cg_ws_bytes(A.n, A.stride, A.dtype)
+    buf = (ws or Workspace(b.device)).get(nbytes)
+    o = _opts(eps, A.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0,
+              check_every, use_graph, history)
+    info = L.KcSolveInfo()
+    rc = lib.kc_cg(C.byref(A.system), ptr(b), ptr(x), ptr(buf), buf.numel(), C.byref(o), C.byref(info),
+                   stream_handle(b.device))
+    L.check(rc, "kc_cg")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0)
+
+
+def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8,
+                     eps_inner=1e-3, max_refine=30, max_iter=None, ws: Workspace | None = None,
+                     use_graph=True) -> SolveInfo:
+    """FP64-residual iterative refinement around an FP32 BiCGSTAB with FP64
+    inner products; stops when ||b - A64 x|| / ||b|| < eps."""
+    require_cuda(b, x)
+    if A64.dtype != L.F64 or A32.dtype != L.F32:
+        raise TypeError("bicgstab_refined needs an FP64 and an FP32 operator")
+    lib = L.load()
+    nbytes = lib.kc_refined_ws_bytes(A64.n, A64.stride)
+    buf = (ws or Workspace(b.device)).get(nbytes)
+    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0,
+              0, use_graph)
+    info = L.KcSolveInfo()
+    rc = lib.kc_bicgstab_refined(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x), ptr(buf),
+                                 buf.numel(), C.byref(o), float(eps_inner), int(max_refine), C.byref(info),
+                                 stream_handle(b.device))
+    L.check(rc, "kc_bicgstab_refined")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)

@@ -1,0 +1,928 @@
+"""CPU oracle for the karman_taichi SIMPLE hot path -- TEST INFRASTRUCTURE ONLY.
+
+A NumPy FP64 restatement of the reference algorithms. Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import this
+module, and only as the checker; the product (``karman_taichi_gb300``) never
+imports anything under ``oracle/``.
+
+Parity status
+-------------
+* Linear solvers (``bicgstab``, ``cg``, ``spmv``) are pinned against the
+  reference's own known-answer tests, restated with seeded inputs in
+  ``tests/test_oracle_kat.py``: debug/ti_bicg_test.py:21-98 (random
+  diagonally dominant 5-diagonal matrix vs ``np.linalg.solve``),
+  benchmark/cg_to_sparse/validation.py:7-45 and test_cg_sparse.py:10-41
+  (Laplacian + offset vs a direct sparse solve / SciPy BiCGSTAB).
+* SIMPLE fields (u, v, p after N steps): **parity unpinned**. Taichi 0.9.0 is
+  not importable here and the reference commits no field fixtures, so this
+  restatement is the only field oracle.
+
+Conventions shared with the CUDA library
+----------------------------------------
+Every linear system is a 5-point stencil on a *flat* index ``k in [0, n)``
+with far stride ``S``: ``y[k] = c0 x[k] + cW x[k-S] + cE x[k+S] + cN x[k+1]
++ cS x[k-1]``; reads outside ``[0, n)`` return 0 (Taichi reads of unwritten
+sparse entries return 0: debug/ti_sparse_test.py:38-39). Coefficients are
+planes ``coef[0..4] = aP, aW, aE, aN, aS`` -- the component order of the
+reference's ``coef[i,j,0..4]`` (simple.py:42-47). For a padded 2-D field
+``[NX, NY]`` the flat stride is ``S = NY`` and ``(i, j)`` is ``k = i*NY + j``.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Solver status codes (mirrors include/karman_gb300.h)
+OK, MAXITER, BREAKDOWN_RHO, BREAKDOWN_OMEGA, NONFINITE, STALL = 0, 1, 2, 3, 4, 5
+
+
+# ----------------------------------------------------------------------------
+# Stencil operator and solvers
+# ----------------------------------------------------------------------------
+def spmv(coef, x, S, order="simple"):
+    """y = A x for a flat 5-point stencil (bicgsolver.py:65-76, cgsolver.py:56-66).
+
+    ``order='simple'`` adds the terms as bicgsolver.py:75-76 writes them
+    (P, W, E, N, S); ``order='karman'`` follows the gather order of
+    karman_taichi.py:403-407 (k-S, k-1, k, k+1, k+S).
+    """
+    coef = coef.reshape(5, -1)
+    x = x.reshape(-1)
+    n = x.size
+    xW = np.zeros(n); xE = np.zeros(n); xN = np.zeros(n); xS = np.zeros(n)
+    if S < n:
+        xW[S:] = x[:n - S]
+        xE[:n - S] = x[S:]
+    xS[1:] = x[:-1]
+    xN[:-1] = x[1:]
+    if order == "simple":
+        y = coef[0] * x + coef[1] * xW + coef[2] * xE + coef[3] * xN + coef[4] * xS
+    else:
+        y = 0.0 + coef[1] * xW
+        y = y + coef[4] * xS
+        y = y + coef[0] * x
+        y = y + coef[3] * xN
+        y = y + coef[2] * xE
+    return y
+
+
+def dot(p, q):
+    """CGSolver.reduce (cgsolver.py:49-54): FP64 sum of p*q over the whole field."""
+    return float(np.dot(p.reshape(-1), q.reshape(-1)))
+
+
+@dataclass
+class SolveResult:
+    x: np.ndarray
+    status: int
+    iters: int
+    rel_res: float
+    history: list = field(default_factory=list)
+
+
+def bicgstab(coef, b, S, eps=1e-8, max_iter=None, x0=None, M=None,
+             omega_break=False, order="simple", rel_to="r0"):
+    """BiCGSTAB restated from bicgsolver.py:88-135 and karman_taichi.py:342-456.
+
+    * ``x0=None``: cold start, x = 0, r = b (bicgsolver.py:21-36).
+    * ``x0`` array: warm start, r = b - A x0 (karman_taichi.py:362-371).
+    * ``M``: right-Jacobi diagonal, p_hat = (1/M) p, s_hat = (1/M) s
+      (karman_taichi.py:398-399, 418-419); None means M = I (bicgsolver.py:52).
+    * stop when sqrt(rTr / r0Tr) < eps (bicgsolver.py:130; karman :446), on
+      rho == 0 (bicgsolver.py:96-98) and, for karman, on omega == 0 (:451-454).
+    * ``rel_to='b'`` measures the residual against ||b|| instead of ||r0||.
+    """
+    b = b.reshape(-1).astype(np.float64)
+    n = b.size
+    if max_iter is None:
+        max_iter = n
+    if x0 is None:
+        x = np.zeros(n)
+        r = b.copy()
+    else:
+        x = np.array(x0, dtype=np.float64).reshape(-1).copy()
+        r = b - spmv(coef, x, S, order)
+    rt = r.copy()
+    r0 = dot(r, r)
+    den = dot(b, b) if rel_to == "b" else r0
+    invM = None if M is None else 1.0 / M.reshape(-1)
+    rho_1 = alpha = omega = 1.0
+    p = np.zeros(n); v = np.zeros(n)
+    status, it, rel = MAXITER, 0, (0.0 if den == 0 else math.sqrt(r0 / den))
+    if r0 == 0.0:
+        return SolveResult(x, OK, 0, 0.0)
+    if rel_to == "b" and rel < eps:
+        return SolveResult(x, OK, 0, rel)
+    with np.errstate(all="ignore"):
+        for i in range(max_iter):
+            rho = dot(r, rt)
+            if rho == 0.0:
+                status = BREAKDOWN_RHO
+                break
+            if i == 0:
+                p = r.copy()
+            else:
+                beta = (rho / rho_1) * (alpha / omega)
+                p = r + beta * (p - omega * v)
+            ph = p if invM is None else invM * p
+            v = spmv(coef, ph, S, order)
+            alpha = rho / dot(rt, v)
+            s = r - alpha * v
+            sh = s if invM is None else invM * s
+            t = spmv(coef, sh, S, order)
+            omega = dot(t, s) / dot(t, t)
+            x = x + (alpha * ph + omega * sh)
+            r = s - omega * t
+            rTr = dot(r, r)
+            it = i + 1
+            rel = math.sqrt(rTr / den) if den > 0 else 0.0
+            if rel < eps:
+                status = OK
+                break
+            if not np.isfinite(rTr):
+                status = NONFINITE
+                break
+            if omega_break and omega == 0.0:
+                status = BREAKDOWN_OMEGA
+                break
+            rho_1 = rho
+    return SolveResult(x, status, it, rel)
+
+
+def cg(coef, b, S, eps=1e-8, max_iter=None):
+    """Conjugate gradients restated from cgsolver.py:83-114 (cold start, x = 0;
+    stop when sqrt(new_rTr) < sqrt(r0Tr) * eps, cgsolver.py:102)."""
+    b = b.reshape(-1).astype(np.float64)
+    n = b.size
+    if max_iter is None:
+        max_iter = n
+    x = np.zeros(n)
+    r = b.copy()
+    r0 = dot(r, r)
+    hist = [math.sqrt(r0)]
+    if r0 == 0.0:
+        return SolveResult(x, OK, 0, 0.0, hist)
+    old = r0
+    p = r.copy()
+    status, it, rel = MAXITER, 0, 1.0
+    with np.errstate(all="ignore"):
+        for i in range(max_iter):
+            Ap = spmv(coef, p, S)
+            alpha = old / dot(p, Ap)
+            x = x + alpha * p
+            r = r - alpha * Ap
+            new = dot(r, r)
+            it = i + 1
+            rel = math.sqrt(new) / math.sqrt(r0)
+            if math.sqrt(new) < math.sqrt(r0) * eps:
+                status = OK
+                break
+            if not np.isfinite(new):
+                status = NONFINITE
+                break
+            beta = new / old
+            p = r + beta * p
+            old = new
+            hist.append(math.sqrt(new))
+    return SolveResult(x, status, it, rel, hist)
+
+
+def bicgstab_refined(coef, b, S, eps=1e-8, eps_inner=1e-4, max_refine=20,
+                     max_iter=None):
+    """Mixed-precision iterative refinement: FP64 residual, FP32 BiCGSTAB
+    correction with FP64 inner products (emulated by rounding the vectors and
+    coefficients to float32 after every update)."""
+    b = b.reshape(-1).astype(np.float64)
+    n = b.size
+    max_iter = max_iter or n
+    c32 = coef.reshape(5, -1).astype(np.float32).astype(np.float64)
+    x = np.zeros(n)
+    bn = math.sqrt(dot(b, b))
+    total = 0
+    if bn == 0:
+        return SolveResult(x, OK, 0, 0.0)
+    for _ in range(max_refine):
+        r = b - spmv(coef, x, S)
+        rel = math.sqrt(dot(r, r)) / bn
+        if rel < eps:
+            return SolveResult(x, OK, total, rel)
+        r32 = r.astype(np.float32).astype(np.float64)
+        res = _bicgstab_f32(c32, r32, S, eps_inner, max_iter)
+        total += res.iters
+        x = x + res.x
+    r = b - spmv(coef, x, S)
+    rel = math.sqrt(dot(r, r)) / bn
+    return SolveResult(x, OK if rel < eps else MAXITER, total, rel)
+
+
+def _f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def _bicgstab_f32(c32, b, S, eps, max_iter):
+    n = b.size
+    x = np.zeros(n); r = b.copy(); rt = r.copy()
+    r0 = dot(r, r)
+    rho_1 = alpha = omega = 1.0
+    p = np.zeros(n); v = np.zeros(n)
+    it = 0
+    for i in range(max_iter):
+        rho = dot(r, rt)
+        if rho == 0:
+            break
+        if i == 0:
+            p = r.copy()
+        else:
+            beta = (rho / rho_1) * (alpha / omega)
+            p = _f32(r + _f32(beta) * (p - _f32(omega) * v))
+        v = _f32(spmv(c32, p, S))
+        alpha = rho / dot(rt, v)
+        s = _f32(r - _f32(alpha) * v)
+        t = _f32(spmv(c32, s, S))
+        omega = dot(t, s) / dot(t, t)
+        x = _f32(x + _f32(alpha) * p + _f32(omega) * s)
+        r = _f32(s - _f32(omega) * t)
+        it = i + 1
+        if math.sqrt(dot(r, r) / r0) < eps:
+            break
+        rho_1 = rho
+    return SolveResult(x, OK, it, 0.0)
+
+
+def to_csr(coef, S):
+    """Assemble the flat 5-point stencil as a scipy CSR matrix (test helper)."""
+    import scipy.sparse as sp
+    coef = coef.reshape(5, -1)
+    n = coef.shape[1]
+    rows, cols, vals = [], [], []
+    for c, off in ((0, 0), (1, -S), (2, S), (3, 1), (4, -1)):
+        k = np.arange(n)
+        m = (k + off >= 0) & (k + off < n) & (coef[c] != 0)
+        rows.append(k[m]); cols.append(k[m] + off); vals.append(coef[c][m])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+
+
+# ----------------------------------------------------------------------------
+# simple.py: matrix-free SIMPLESolver (cavity / generic bc dict)
+# ----------------------------------------------------------------------------
+class SimpleOracle:
+    """Restatement of simple.py:11-285 (and the bicgsimp.py:114-151, 196
+    variant when ``bicgsimp=True``: p' pinned at (1,1), east-wall fix)."""
+
+    def __init__(self, lx, ly, nx, ny, bicgsimp=False):
+        self.lx, self.ly, self.nx, self.ny = lx, ly, nx, ny
+        self.dx, self.dy = lx / nx, ly / ny
+        self.rho, self.mu, self.dt = 1.0, 0.01, 10000.0
+        self.alpha_p = self.alpha_u = self.alpha_m = 0.001
+        self.bicgsimp = bicgsimp
+        z = np.zeros
+        self.u = z((nx + 3, ny + 2)); self.v = z((nx + 2, ny + 3))
+        self.u_mid = z((nx + 3, ny + 2)); self.v_mid = z((nx + 2, ny + 3))
+        self.u0 = z((nx + 3, ny + 2)); self.v0 = z((nx + 2, ny + 3))
+        self.p = z((nx + 2, ny + 2)); self.pcor = z((nx + 2, ny + 2)); self.mdiv = z((nx + 2, ny + 2))
+        self.bc = {"w": [0.0, 0.0], "e": [0.0, 0.0], "n": [0.0, 0.0], "s": [0.0, 0.0]}
+        self.coef_u = z((5, nx + 3, ny + 2)); self.b_u = z((nx + 3, ny + 2))
+        self.coef_v = z((5, nx + 2, ny + 3)); self.b_v = z((nx + 2, ny + 3))
+        self.coef_p = z((5, nx + 2, ny + 2)); self.b_p = z((nx + 2, ny + 2))
+
+    def compute_coef_u(self):  # simple.py:77-92
+        nx, ny, dx, dy, dt, rho, mu = self.nx, self.ny, self.dx, self.dy, self.dt, self.rho, self.mu
+        u, v, p, u0, c = self.u, self.v, self.p, self.u0, self.coef_u
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        ui, uw, ue = u[I, J], u[1:nx, J], u[3:nx + 2, J]
+        vnw, vne, vsw, vse = v[1:nx, 2:ny + 2], v[2:nx + 1, 2:ny + 2], v[1:nx, J], v[2:nx + 1, J]
+        c[1, I, J] = -(mu * dy / dx + 0.5 * rho * 0.5 * (ui + uw) * dy)
+        c[2, I, J] = -(mu * dy / dx - 0.5 * rho * 0.5 * (ui + ue) * dy)
+        c[3, I, J] = -(mu * dx / dy - 0.5 * rho * 0.5 * (vnw + vne) * dx)
+        c[4, I, J] = -(mu * dx / dy + 0.5 * rho * 0.5 * (vsw + vse) * dx)
+        c[0, I, J] = (-(c[1, I, J] + c[2, I, J] + c[3, I, J] + c[4, I, J])
+                      + rho * 0.5 * (ui + ue) * dy - rho * 0.5 * (ui + uw) * dy
+                      + rho * 0.5 * (vnw + vne) * dx - rho * 0.5 * (vsw + vse) * dx
+                      + rho * dx * dy / dt)
+        self.b_u[I, J] = (p[1:nx, J] - p[2:nx + 1, J]) * dy + rho * dx * dy / dt * u0[I, J]
+
+    def compute_coef_v(self):  # simple.py:95-110
+        nx, ny, dx, dy, dt, rho, mu = self.nx, self.ny, self.dx, self.dy, self.dt, self.rho, self.mu
+        u, v, p, v0, c = self.u, self.v, self.p, self.v0, self.coef_v
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        uc, us = u[I, J], u[I, 1:ny]
+        uec, ues = u[2:nx + 2, J], u[2:nx + 2, 1:ny]
+        vc, vn, vs = v[I, J], v[I, 3:ny + 2], v[I, 1:ny]
+        c[1, I, J] = -(mu * dy / dx + 0.5 * rho * 0.5 * (uc + us) * dy)
+        c[2, I, J] = -(mu * dy / dx - 0.5 * rho * 0.5 * (ues + uec) * dy)
+        c[3, I, J] = -(mu * dx / dy - 0.5 * rho * 0.5 * (vn + vc) * dx)
+        c[4, I, J] = -(mu * dx / dy + 0.5 * rho * 0.5 * (vs + vc) * dx)
+        c[0, I, J] = (-(c[1, I, J] + c[2, I, J] + c[3, I, J] + c[4, I, J])
+                      + rho * 0.5 * (ues + uec) * dy - rho * 0.5 * (uc + us) * dy
+                      + rho * 0.5 * (vn + vc) * dx - rho * 0.5 * (vs + vc) * dx
+                      + rho * dx * dy / dt)
+        self.b_v[I, J] = (p[I, 1:ny] - p[I, J]) * dx + rho * dx * dy / dt * self.v0[I, J]
+
+    def set_bc(self):  # simple.py:172-216 (bicgsimp.py:153-197 when bicgsimp)
+        nx, ny, bc, mu, dx, dy = self.nx, self.ny, self.bc, self.mu, self.dx, self.dy
+        cu, bu, cv, bv = self.coef_u, self.b_u, self.coef_v, self.b_v
+        J = slice(1, ny + 1)
+        bu[2, J] += -cu[1, 2, J] * bc["w"][0]; cu[1, 2, J] = 0.0; self.u[1, J] = bc["w"][0]
+        bu[nx, J] += -cu[2, nx, J] * bc["e"][0]; cu[2, nx, J] = 0.0; self.u[nx + 1, J] = bc["e"][0]
+        I = slice(1, nx + 1)
+        bv[I, 2] += -cv[4, I, 2] * bc["s"][0]; cv[4, I, 2] = 0.0; self.v[I, 1] = bc["s"][0]
+        bv[I, ny] += -cv[3, I, ny] * bc["n"][0]; cv[3, I, ny] = 0.0; self.v[I, ny + 1] = bc["n"][0]
+        I = slice(2, nx + 1)
+        bu[I, 1] += 2 * mu * bc["s"][1] * dx / dy
+        cu[0, I, 1] += (cu[4, I, 1] + 2 * mu * dx / dy); cu[4, I, 1] = 0.0
+        bu[I, ny] += 2 * mu * bc["n"][1] * dx / dy
+        cu[0, I, ny] += (cu[3, I, ny] + 2 * mu * dx / dy); cu[3, I, ny] = 0.0
+        J = slice(2, ny + 1)
+        bv[1, J] += 2 * mu * bc["w"][1] * dy / dx
+        cv[0, 1, J] += (cv[1, 1, J] + 2 * mu * dy / dx); cv[1, 1, J] = 0.0
+        bv[nx, J] += 2 * mu * bc["e"][1] * dy / dx
+        # simple.py:215 adds aW (component 1) here; bicgsimp.py:196 adds aE.
+        cv[0, nx, J] += (cv[2 if self.bicgsimp else 1, nx, J] + 2 * mu * dy / dx); cv[2, nx, J] = 0.0
+
+    def compute_mdiv(self):  # simple.py:137-141; bicgsimp.py:114-122 returns max|mdiv|
+        nx, ny, dx, dy, rho = self.nx, self.ny, self.dx, self.dy, self.rho
+        u, v = self.u, self.v
+        I, J = slice(1, nx + 1), slice(1, ny + 1)
+        self.mdiv[I, J] = rho * (u[I, J] - u[2:nx + 2, J]) * dy + rho * (v[I, J] - v[I, 2:ny + 2]) * dx
+        return float(np.abs(self.mdiv[I, J]).max())
+
+    def compute_coef_p(self):  # simple.py:143-170 (bicgsimp.py:124-151)
+        nx, ny, dx, dy, rho = self.nx, self.ny, self.dx, self.dy, self.rho
+        self.compute_mdiv()
+        I, J = slice(1, nx + 1), slice(1, ny + 1)
+        c, cu, cv = self.coef_p, self.coef_u, self.coef_v
+        self.b_p[I, J] = self.mdiv[I, J]
+        with np.errstate(divide="ignore"):
+            c[1, I, J] = -rho * dy * dy / cu[0, I, J]
+            c[2, I, J] = -rho * dy * dy / cu[0, 2:nx + 2, J]
+            c[3, I, J] = -rho * dx * dx / cv[0, I, 2:ny + 2]
+            c[4, I, J] = -rho * dx * dx / cv[0, I, J]
+        c[1, 1, J] = 0.0; c[2, nx, J] = 0.0; c[4, I, 1] = 0.0; c[3, I, ny] = 0.0
+        c[0, I, J] = -(c[1, I, J] + c[2, I, J] + c[3, I, J] + c[4, I, J])
+        if self.bicgsimp:
+            c[1:5, 1, 1] = 0.0; c[0, 1, 1] = 1.0; self.b_p[1, 1] = 0.0
+
+    def correct_pressure(self):  # simple.py:218-222
+        nx, ny = self.nx, self.ny
+        self.p[1:nx + 1, 1:ny + 1] += self.alpha_p * self.pcor[1:nx + 1, 1:ny + 1]
+
+    def correct_velocity(self):  # simple.py:224-230
+        nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
+        pc = self.pcor
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        self.u[I, J] += self.alpha_u * (pc[1:nx, J] - pc[I, J]) * dy / self.coef_u[0, I, J]
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        self.v[I, J] += self.alpha_u * (pc[I, 1:ny] - pc[I, J]) * dx / self.coef_v[0, I, J]
+
+    def update_velocity(self):  # simple.py:232-238 (bicgsimp.py:212-225 returns max diff)
+        nx, ny, a = self.nx, self.ny, self.alpha_m
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        du = np.abs(self.u_mid[I, J] - self.u[I, J]).max(initial=0.0)
+        self.u[I, J] = a * self.u_mid[I, J] + (1 - a) * self.u[I, J]
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        dv = np.abs(self.v_mid[I, J] - self.v[I, J]).max(initial=0.0)
+        self.v[I, J] = a * self.v_mid[I, J] + (1 - a) * self.v[I, J]
+        return math.sqrt(du ** 2 + dv ** 2)
+
+    def solve_momentum_eqn(self, n_iter=1, eps=1e-1):  # simple.py:241-250
+        for _ in range(n_iter):
+            self.compute_coef_u(); self.compute_coef_v(); self.set_bc()
+            ru = bicgstab(self.coef_u, self.b_u, self.b_u.shape[1], eps=eps)
+            rv = bicgstab(self.coef_v, self.b_v, self.b_v.shape[1], eps=eps)
+            self.u_mid[...] = ru.x.reshape(self.u_mid.shape)
+            self.v_mid[...] = rv.x.reshape(self.v_mid.shape)
+            self.update_velocity()
+        return ru, rv
+
+    def solve_pcorrection_eqn(self, eps=1e-2):  # simple.py:252-255
+        self.compute_coef_p()
+        res = cg(self.coef_p, self.b_p, self.b_p.shape[1], eps=eps)
+        self.pcor[...] = res.x.reshape(self.pcor.shape)
+        return res
+
+    def init(self):  # simple.py:257-264
+        self.u[...] = 0.0; self.v[...] = 0.0; self.p[...] = 0.0
+
+    def solve(self, n_steps=2000):  # simple.py:266-285 without the CSV/PNG dumps
+        self.init()
+        for _ in range(n_steps):
+            self.solve_momentum_eqn(1)
+            self.compute_mdiv()
+            self.solve_pcorrection_eqn()
+            self.correct_pressure(); self.correct_velocity()
+            self.compute_mdiv()
+
+
+# ----------------------------------------------------------------------------
+# Channel preset: velocity inlet, zero-gradient outlet, no-slip walls,
+# blocked-cell cylinder (the benchmark configurations)
+# ----------------------------------------------------------------------------
+def channel_solid_mask(nx, ny, obstacles):
+    """uint8 [nx+2, ny+2]; 1 = blocked cell.  ``obstacles`` is a list of
+    ``(shape, ci, cj, D)`` in padded cell indices.  'square': cells
+    [c - D//2, c - D//2 + D - 1] in i and j.  'circle': the reference's
+    rule (i - ci)^2 + (j - cj)^2 < (D/2)^2 (karman_taichi.py:148-150)."""
+    m = np.zeros((nx + 2, ny + 2), dtype=np.uint8)
+    ii, jj = np.meshgrid(np.arange(nx + 2), np.arange(ny + 2), indexing="ij")
+    inside = (ii >= 1) & (ii <= nx) & (jj >= 1) & (jj <= ny)
+    for shape, ci, cj, D in obstacles:
+        if shape == "square":
+            lo_i, lo_j = ci - D // 2, cj - D // 2
+            sel = (ii >= lo_i) & (ii <= lo_i + D - 1) & (jj >= lo_j) & (jj <= lo_j + D - 1)
+        else:
+            r2 = (D * D) // 4 if D % 2 == 0 else (D * D) / 4.0
+            sel = ((ii - ci) ** 2 + (jj - cj) ** 2) < r2
+        m[sel & inside] = 1
+    return m
+
+
+@dataclass
+class ChannelParams:
+    nx: int
+    ny: int
+    dx: float
+    dy: float
+    rho: float
+    mu: float
+    dt: float
+    U: float = 1.0
+    alpha_m: float = 0.7
+    alpha_u: float = 1.0
+    alpha_p: float = 0.3
+    eps: float = 1e-8
+    mass_tol: float = 1e-6
+    max_outer: int = 50
+
+
+class ChannelOracle:
+    """FP64 restatement of the channel SIMPLE step.  The discretisation is
+    simple.py's mid-point scheme (simple.py:77-110) with set_bc's wall and
+    Dirichlet folding (simple.py:172-216); the outlet uses karman_taichi.py's
+    zero-gradient row and mass-flow rescale (karman_taichi.py:178-183,
+    586-614); blocked faces become identity rows (karman_taichi.py:225-229)."""
+
+    def __init__(self, prm: ChannelParams, solid, u, v, p):
+        self.P = prm
+        nx, ny = prm.nx, prm.ny
+        self.solid = solid.astype(bool)
+        self.u = u.astype(np.float64).copy(); self.v = v.astype(np.float64).copy()
+        self.p = p.astype(np.float64).copy()
+        self.u0 = self.u.copy(); self.v0 = self.v.copy()
+        self.pcor = np.zeros((nx + 2, ny + 2))
+        s = self.solid
+        bu = np.zeros((nx + 3, ny + 2), bool)
+        bu[1:nx + 2, :] = s[0:nx + 1, :] | s[1:nx + 2, :]
+        bv = np.zeros((nx + 2, ny + 3), bool)
+        bv[:, 1:ny + 2] = s[:, 0:ny + 1] | s[:, 1:ny + 2]
+        self.blk_u, self.blk_v = bu, bv
+        unk_u = np.zeros_like(bu); unk_u[2:nx + 1, 1:ny + 1] = ~bu[2:nx + 1, 1:ny + 1]
+        unk_v = np.zeros_like(bv); unk_v[1:nx + 1, 2:ny + 1] = ~bv[1:nx + 1, 2:ny + 1]
+        self.unk_u, self.unk_v = unk_u, unk_v
+        self.coef_u = np.zeros((5, nx + 3, ny + 2)); self.b_u = np.zeros((nx + 3, ny + 2))
+        self.coef_v = np.zeros((5, nx + 2, ny + 3)); self.b_v = np.zeros((nx + 2, ny + 3))
+        self.coef_p = np.zeros((5, nx + 2, ny + 2)); self.b_p = np.zeros((nx + 2, ny + 2))
+        self.stats = []
+
+    # -- momentum ----------------------------------------------------------
+    def assemble_momentum(self):
+        P = self.P
+        nx, ny, dx, dy, dt, rho, mu = P.nx, P.ny, P.dx, P.dy, P.dt, P.rho, P.mu
+        u, v, p = self.u, self.v, self.p
+        c, b = self.coef_u, self.b_u
+        c[...] = 0.0; b[...] = 0.0
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        ui, uw, ue = u[I, J], u[1:nx, J], u[3:nx + 2, J]
+        vnw, vne, vsw, vse = v[1:nx, 2:ny + 2], v[2:nx + 1, 2:ny + 2], v[1:nx, J], v[2:nx + 1, J]
+        aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (ui + uw) * dy)
+        aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ui + ue) * dy)
+        aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vnw + vne) * dx)
+        aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vsw + vse) * dx)
+        aP = (-(aW + aE + aN + aS) + rho * 0.5 * (ui + ue) * dy - rho * 0.5 * (ui + uw) * dy
+              + rho * 0.5 * (vnw + vne) * dx - rho * 0.5 * (vsw + vse) * dx + rho * dx * dy / dt)
+        bb = (p[1:nx, J] - p[I, J]) * dy + rho * dx * dy / dt * self.u0[I, J]
+        ii = np.arange(2, nx + 1)[:, None] + 0 * np.arange(ny)[None, :]
+        jj = np.arange(1, ny + 1)[None, :] + 0 * ii
+        bu = self.blk_u
+        wall_x = 2 * mu * dx / dy
+        # west
+        m = ii == 2
+        bb = np.where(m, bb + (-aW * P.U), bb); aW = np.where(m, 0.0, aW)
+        m = (ii > 2) & bu[1:nx, J]
+        aW = np.where(m, 0.0, aW)
+        # east
+        m = ii == nx
+        aP = np.where(m, aP + aE, aP); aE = np.where(m, 0.0, aE)
+        m = (ii < nx) & bu[3:nx + 2, J]
+        aE = np.where(m, 0.0, aE)
+        # south
+        m = (jj == 1) | bu[I, 0:ny]
+        aP = np.where(m, aP + (aS + wall_x), aP); aS = np.where(m, 0.0, aS)
+        # north
+        m = (jj == ny) | bu[I, 2:ny + 2]
+        aP = np.where(m, aP + (aN + wall_x), aP); aN = np.where(m, 0.0, aN)
+        blk = bu[I, J]
+        c[0, I, J] = np.where(blk, 1.0, aP)
+        c[1, I, J] = np.where(blk, 0.0, aW); c[2, I, J] = np.where(blk, 0.0, aE)
+        c[3, I, J] = np.where(blk, 0.0, aN); c[4, I, J] = np.where(blk, 0.0, aS)
+        b[I, J] = np.where(blk, 0.0, bb)
+
+        c, b = self.coef_v, self.b_v
+        c[...] = 0.0; b[...] = 0.0
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        uc, us = u[I, J], u[I, 1:ny]
+        uec, ues = u[2:nx + 2, J], u[2:nx + 2, 1:ny]
+        vc, vn, vs = v[I, J], v[I, 3:ny + 2], v[I, 1:ny]
+        aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (uc + us) * dy)
+        aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ues + uec) * dy)
+        aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vn + vc) * dx)
+        aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vs + vc) * dx)
+        aP = (-(aW + aE + aN + aS) + rho * 0.5 * (ues + uec) * dy - rho * 0.5 * (uc + us) * dy
+              + rho * 0.5 * (vn + vc) * dx - rho * 0.5 * (vs + vc) * dx + rho * dx * dy / dt)
+        bb = (p[I, 1:ny] - p[I, J]) * dx + rho * dx * dy / dt * self.v0[I, J]
+        ii = np.arange(1, nx + 1)[:, None] + 0 * np.arange(ny - 1)[None, :]
+        jj = np.arange(2, ny + 1)[None, :] + 0 * ii
+        bv = self.blk_v
+        wall_y = 2 * mu * dy / dx
+        # south / north: Dirichlet v = 0 (walls and obstacle faces)
+        m = (jj == 2) | bv[I, 1:ny]
+        aS = np.where(m, 0.0, aS)
+        m = (jj == ny) | bv[I, 3:ny + 2]
+        aN = np.where(m, 0.0, aN)
+        # west: inlet (tangential v = 0) or obstacle side -> wall
+        m = (ii == 1) | bv[0:nx, J]
+        aP = np.where(m, aP + (aW + wall_y), aP); aW = np.where(m, 0.0, aW)
+        # east: outlet zero gradient, obstacle side -> wall
+        m = ii == nx
+        aP = np.where(m, aP + aE, aP); aE = np.where(m, 0.0, aE)
+        m = (ii < nx) & bv[2:nx + 2, J]
+        aP = np.where(m, aP + (aE + wall_y), aP); aE = np.where(m, 0.0, aE)
+        blk = bv[I, J]
+        c[0, I, J] = np.where(blk, 1.0, aP)
+        c[1, I, J] = np.where(blk, 0.0, aW); c[2, I, J] = np.where(blk, 0.0, aE)
+        c[3, I, J] = np.where(blk, 0.0, aN); c[4, I, J] = np.where(blk, 0.0, aS)
+        b[I, J] = np.where(blk, 0.0, bb)
+
+    def relax(self, u_mid, v_mid):
+        """Explicit under-relaxation of the momentum solution (simple.py:232-238),
+        then the zero-gradient outlet and the mass-flow rescale
+        (karman_taichi.py:586-601)."""
+        a = self.P.alpha_m
+        m = self.unk_u
+        self.u[m] = a * u_mid[m] + (1 - a) * self.u[m]
+        m = self.unk_v
+        self.v[m] = a * v_mid[m] + (1 - a) * self.v[m]
+        nx, ny = self.P.nx, self.P.ny
+        J = slice(1, ny + 1)
+        self.u[nx + 1, J] = self.u[nx, J]
+        mdot_in = float(np.sum(self.u[1, J]))
+        mdot_out = float(np.sum(self.u[nx + 1, J]))
+        self.u[nx + 1, J] = (mdot_in / mdot_out) * self.u[nx + 1, J]
+
+    # -- pressure correction ------------------------------------------------
+    def assemble_p(self):
+        P = self.P
+        nx, ny, dx, dy, rho = P.nx, P.ny, P.dx, P.dy, P.rho
+        u, v = self.u, self.v
+        c, b = self.coef_p, self.b_p
+        c[...] = 0.0; b[...] = 0.0
+        I, J = slice(1, nx + 1), slice(1, ny + 1)
+        mdiv = rho * (u[I, J] - u[2:nx + 2, J]) * dy + rho * (v[I, J] - v[I, 2:ny + 2]) * dx
+        apu, apv = self.coef_u[0], self.coef_v[0]
+        uu, uv = self.unk_u, self.unk_v
+        with np.errstate(divide="ignore", invalid="ignore"):
+            aW = np.where(uu[I, J], -rho * dy * dy / apu[I, J], 0.0)
+            aE = np.where(uu[2:nx + 2, J], -rho * dy * dy / apu[2:nx + 2, J], 0.0)
+            out = np.zeros_like(aE, dtype=bool); out[nx - 1, :] = uu[nx, J]
+            aE = np.where(out, -rho * dy * dy / apu[nx:nx + 1, J], aE)
+            aN = np.where(uv[I, 2:ny + 2], -rho * dx * dx / apv[I, 2:ny + 2], 0.0)
+            aS = np.where(uv[I, J], -rho * dx * dx / apv[I, J], 0.0)
+        aP = -(aW + aE + aN + aS)
+        sol = self.solid[I, J]
+        c[0, I, J] = np.where(sol, 1.0, aP)
+        c[1, I, J] = np.where(sol, 0.0, aW); c[2, I, J] = np.where(sol, 0.0, aE)
+        c[3, I, J] = np.where(sol, 0.0, aN); c[4, I, J] = np.where(sol, 0.0, aS)
+        b[I, J] = np.where(sol, 0.0, mdiv)
+        return float(np.abs(np.where(sol, 0.0, mdiv)).max())
+
+    def correct(self):
+        """Velocity/pressure correction (simple.py:218-230 with alpha_u, and
+        the outlet face corrected against p' = 0 beyond the outlet)."""
+        P = self.P
+        nx, ny, dx, dy = P.nx, P.ny, P.dx, P.dy
+        pc = self.pcor
+        apu, apv = self.coef_u[0], self.coef_v[0]
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        m = self.unk_u[I, J]
+        self.u[I, J] = np.where(m, self.u[I, J] + P.alpha_u * (pc[1:nx, J] - pc[I, J]) * dy
+                                / np.where(m, apu[I, J], 1.0), self.u[I, J])
+        m = self.unk_u[nx, J]
+        self.u[nx + 1, J] = np.where(m, self.u[nx + 1, J] + P.alpha_u * (pc[nx, J] - pc[nx + 1, J]) * dy
+                                     / np.where(m, apu[nx, J], 1.0), self.u[nx + 1, J])
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        m = self.unk_v[I, J]
+        self.v[I, J] = np.where(m, self.v[I, J] + P.alpha_u * (pc[I, 1:ny] - pc[I, J]) * dx
+                                / np.where(m, apv[I, J], 1.0), self.v[I, J])
+        I, J = slice(1, nx + 1), slice(1, ny + 1)
+        fl = ~self.solid[I, J]
+        self.p[I, J] = np.where(fl, self.p[I, J] + P.alpha_p * pc[I, J], self.p[I, J])
+        return float(np.abs(pc).max())
+
+    def mass_residual(self):
+        """max |mdiv| over fluid cells of the current field (bicgsimp.py:114-122)."""
+        P = self.P
+        nx, ny, dx, dy, rho = P.nx, P.ny, P.dx, P.dy, P.rho
+        I, J = slice(1, nx + 1), slice(1, ny + 1)
+        mdiv = rho * (self.u[I, J] - self.u[2:nx + 2, J]) * dy + rho * (self.v[I, J] - self.v[I, 2:ny + 2]) * dx
+        return float(np.abs(np.where(self.solid[I, J], 0.0, mdiv)).max())
+
+    def outer_iteration(self):
+        P = self.P
+        self.assemble_momentum()
+        ru = bicgstab(self.coef_u, self.b_u, self.b_u.shape[1], eps=P.eps)
+        rv = bicgstab(self.coef_v, self.b_v, self.b_v.shape[1], eps=P.eps)
+        self.relax(ru.x.reshape(self.u.shape), rv.x.reshape(self.v.shape))
+        R = self.assemble_p()
+        rp = bicgstab(self.coef_p, self.b_p, self.b_p.shape[1], eps=P.eps)
+        self.pcor[...] = rp.x.reshape(self.pcor.shape)
+        pmax = self.correct()
+        return dict(mass=R, it_u=ru.iters, it_v=rv.iters, it_p=rp.iters,
+                    st=(ru.status, rv.status, rp.status), pcor_max=pmax)
+
+    def step(self):
+        """One time step: SIMPLE outer iterations until the momentum-predicted
+        mass residual is <= mass_tol or max_outer, then u0 <- u, v0 <- v
+        (karman_taichi.py:617-622)."""
+        rec = []
+        for k in range(self.P.max_outer):
+            s = self.outer_iteration()
+            rec.append(s)
+            if s["mass"] <= self.P.mass_tol:
+                break
+        self.u0 = self.u.copy(); self.v0 = self.v.copy()
+        self.stats.append(rec)
+        return rec
+
+
+# ----------------------------------------------------------------------------
+# karman_taichi.py: assembled-matrix driver, literal sparse emulation
+# ----------------------------------------------------------------------------
+class SparseRows:
+    """Pointer-SNode stand-in: a persistent dict of written (row, col) entries;
+    unwritten entries read 0 and writes outside [0, n) are dropped."""
+
+    def __init__(self, n):
+        self.n = n
+        self.e = {}
+
+    def __setitem__(self, rc, val):
+        r, c = rc
+        if 0 <= r < self.n and 0 <= c < self.n:
+            self.e[(r, c)] = float(val)
+
+    def __getitem__(self, rc):
+        return self.e.get(rc, 0.0)
+
+    def planes(self, S):
+        """Convert to flat 5-point planes [P, W(-S), E(+S), N(+1), S(-1)];
+        asserts that nothing else is stored on the stencil's 7-offset gather."""
+        n = self.n
+        c = np.zeros((5, n))
+        slot = {0: 0, -S: 1, S: 2, 1: 3, -1: 4}
+        for (r, col), val in self.e.items():
+            off = col - r
+            if off in slot:
+                c[slot[off], r] = val
+            elif abs(off) in (S - 1, S + 1) and val != 0.0:
+                raise AssertionError(f"entry off the 5-point pattern: {(r, col)}")
+        return c
+
+
+class KarmanOracle:
+    """Restatement of karman_taichi.py (channel + circle, pressure-driven).
+    Geometry and constants follow karman_taichi.py:7-25; ``nx=320, ny=64`` is
+    debug/karman_taichi.py:11-12."""
+
+    def __init__(self, nx=640, ny=128, lx=0.5, ly=0.1, rho=1.0, mu=0.01, dt=1e-5,
+                 velo_rel=0.8, p_rel=0.2, circle=(64, 32, 144)):
+        self.nx, self.ny = nx, ny
+        self.dx, self.dy = lx / nx, ly / ny
+        self.rho, self.mu, self.dt = rho, mu, dt
+        self.velo_rel, self.p_rel = velo_rel, p_rel
+        self.circle = circle
+        self.nu, self.nv, self.np_ = (nx + 1) * ny, nx * (ny + 1), nx * ny
+        self.Au, self.Mu = SparseRows(self.nu), SparseRows(self.nu)
+        self.Av, self.Mv = SparseRows(self.nv), SparseRows(self.nv)
+        self.Ap, self.Mp = SparseRows(self.np_), SparseRows(self.np_)
+        self.bu, self.xu = np.zeros(self.nu), np.zeros(self.nu)
+        self.bv, self.xv = np.zeros(self.nv), np.zeros(self.nv)
+        self.bp, self.xp = np.zeros(self.np_), np.zeros(self.np_)
+        self.init()
+
+    def init(self):  # karman_taichi.py:130-154
+        nx, ny = self.nx, self.ny
+        i = np.arange(nx + 2)[:, None] * np.ones((1, ny + 2))
+        self.p = 100 - 4000.0 * i / nx
+        self.pcor = np.zeros((nx + 2, ny + 2))
+        self.u = np.zeros((nx + 3, ny + 2)); self.u0 = np.zeros((nx + 3, ny + 2))
+        self.v = np.zeros((nx + 2, ny + 3)); self.v0 = np.zeros((nx + 2, ny + 3))
+        ct = np.ones((nx + 2, ny + 2), dtype=np.int32)
+        ct[1:nx + 1, 1:ny + 1] = -1
+        ci, cj, r2 = self.circle
+        ii, jj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+        sel = ((ii - ci) ** 2 + (jj - cj) ** 2) < r2
+        ct[:nx, :ny][sel] = 1
+        self.ct = ct
+        self.udiv = np.zeros((nx + 2, ny + 2))
+
+    def fill_Au(self):  # karman_taichi.py:162-248
+        nx, ny, dx, dy, dt, rho, mu = self.nx, self.ny, self.dx, self.dy, self.dt, self.rho, self.mu
+        ct, u, v, p, u0 = self.ct, self.u, self.v, self.p, self.u0
+        A, M, b = self.Au, self.Mu, self.bu
+        for i in range(1, nx + 2):
+            for j in range(1, ny + 1):
+                k = (i - 1) * ny + (j - 1)
+                if ct[i - 1, j] == 1:
+                    A[k, k] = 1.0; A[k, k + ny] = -1.0; b[k] = 0.0
+                elif ct[i, j] == 1:
+                    A[k, k] = 1.0; A[k, k - ny] = -1.0; b[k] = 0.0
+                elif (ct[i, j] + ct[i, j - 1]) == 0:
+                    A[k, k + 1] = -mu * dx / dy - rho * 0.5 * (v[i - 1, j + 1] + v[i, j + 1]) * dx
+                    A[k, k - ny] = -mu * dy / dx - rho * 0.5 * (u[i, j] + u[i - 1, j]) * dy
+                    A[k, k + ny] = -mu * dy / dx - (-rho * 0.5 * (u[i, j] + u[i + 1, j]) * dy)
+                    A[k, k] = -A[k, k + 1] - A[k, k - ny] - A[k, k + ny] + rho * dx * dy / dt + 2 * mu * dx / dy
+                    b[k] = (p[i - 1, j] - p[i, j]) * dy + rho * dx * dy / dt * u0[i, j]
+                elif (ct[i, j] + ct[i, j + 1]) == 0:
+                    A[k, k - 1] = -mu * dx / dy - (-rho * 0.5 * (v[i - 1, j] + v[i, j]) * dx)
+                    A[k, k - ny] = -mu * dy / dx - rho * 0.5 * (u[i, j] + u[i - 1, j]) * dy
+                    A[k, k + ny] = -mu * dy / dx - (-rho * 0.5 * (u[i, j] + u[i + 1, j]) * dy)
+                    A[k, k] = -A[k, k - 1] - A[k, k - ny] - A[k, k + ny] + rho * dx * dy / dt + 2 * mu * dx / dy
+                    b[k] = (p[i - 1, j] - p[i, j]) * dy + rho * dx * dy / dt * u0[i, j]
+                else:
+                    A[k, k - 1] = -mu * dx / dy - (-rho * 0.5 * (v[i - 1, j] + v[i, j]) * dx)
+                    A[k, k + 1] = -mu * dx / dy - rho * 0.5 * (v[i - 1, j + 1] + v[i, j + 1]) * dx
+                    A[k, k - ny] = -mu * dy / dx - rho * 0.5 * (u[i, j] + u[i - 1, j]) * dy
+                    A[k, k + ny] = -mu * dy / dx - (-rho * 0.5 * (u[i, j] + u[i + 1, j]) * dy)
+                    A[k, k] = -A[k, k - 1] - A[k, k + 1] - A[k, k - ny] - A[k, k + ny] + rho * dx * dy / dt
+                    b[k] = (p[i - 1, j] - p[i, j]) * dy + rho * dx * dy / dt * u0[i, j]
+                M[k, k] = A[k, k]
+        for i in range(2, nx + 1):
+            for j in range(2, ny):
+                k = (i - 1) * ny + (j - 1)
+                if (ct[i - 1, j] + ct[i, j]) == 0 or (ct[i - 1, j] + ct[i, j]) == 2:
+                    for nb in (k - ny, k - 1, k + 1, k + ny):
+                        A[k, nb] = 0.0
+                    A[k, k] = 1.0; b[k] = 0.0
+                elif (ct[i, j] + ct[i, j - 1]) == 0 or (ct[i - 1, j] + ct[i - 1, j - 1]) == 0:
+                    A[k, k + 1] = -mu * dx / dy - rho * 0.5 * (v[i - 1, j + 1] + v[i, j + 1]) * dx
+                    A[k, k - ny] = -mu * dy / dx - rho * 0.5 * (u[i, j] + u[i - 1, j]) * dy
+                    A[k, k + ny] = -mu * dy / dx - (-rho * 0.5 * (u[i, j] + u[i + 1, j]) * dy)
+                    A[k, k] = -A[k, k + 1] - A[k, k - ny] - A[k, k + ny] + rho * dx * dy / dt + 2 * mu * dx / dy
+                    b[k] = (p[i - 1, j] - p[i, j]) * dy + rho * dx * dy / dt * u0[i, j]
+
+    def fill_Av(self):  # karman_taichi.py:251-294
+        nx, ny, dx, dy, dt, rho, mu = self.nx, self.ny, self.dx, self.dy, self.dt, self.rho, self.mu
+        ct, u, v, p, v0 = self.ct, self.u, self.v, self.p, self.v0
+        A, M, b = self.Av, self.Mv, self.bv
+        for i in range(1, nx + 1):
+            for j in range(1, ny + 2):
+                k = (i - 1) * (ny + 1) + (j - 1)
+                if (ct[i, j] + ct[i, j - 1]) == 0 or (ct[i, j] + ct[i, j - 1]) == 2:
+                    A[k, k] = 1.0; b[k] = v[i, j]
+                elif (ct[i, j] + ct[i - 1, j]) == 0:
+                    A[k, k - 1] = -mu * dx / dy - (-rho * 0.5 * (v[i, j - 1] + v[i, j]) * dx)
+                    A[k, k + 1] = -mu * dx / dy - (rho * 0.5 * (v[i, j + 1] + v[i, j]) * dx)
+                    A[k, k + ny + 1] = -mu * dy / dx - (-rho * 0.5 * (u[i + 1, j - 1] + u[i + 1, j]) * dy)
+                    A[k, k] = -A[k, k - 1] - A[k, k + 1] - A[k, k + ny + 1] + rho * dx * dy / dt + 2 * mu * dy / dx
+                    b[k] = (p[i, j] - p[i, j - 1]) * dx + rho * dx * dy / dt * v0[i, j]
+                elif (ct[i, j] + ct[i + 1, j]) == 0:
+                    A[k, k - 1] = -mu * dx / dy - (-rho * 0.5 * (v[i, j - 1] + v[i, j]) * dx)
+                    A[k, k + 1] = -mu * dx / dy - (rho * 0.5 * (v[i, j + 1] + v[i, j]) * dx)
+                    A[k, k - ny - 1] = -mu * dy / dx - (rho * 0.5 * (u[i, j] + u[i, j - 1]) * dy)
+                    A[k, k] = -A[k, k - 1] - A[k, k + 1] - A[k, k - ny - 1] + rho * dx * dy / dt + 2 * mu * dy / dx
+                    b[k] = (p[i, j] - p[i, j - 1]) * dx + rho * dx * dy / dt * v0[i, j]
+                else:
+                    A[k, k - 1] = -mu * dx / dy - (-rho * 0.5 * (v[i, j - 1] + v[i, j]) * dx)
+                    A[k, k + 1] = -mu * dx / dy - (rho * 0.5 * (v[i, j + 1] + v[i, j]) * dx)
+                    A[k, k - ny - 1] = -mu * dy / dx - (rho * 0.5 * (u[i, j] + u[i, j - 1]) * dy)
+                    A[k, k + ny + 1] = -mu * dy / dx - (-rho * 0.5 * (u[i + 1, j - 1] + u[i + 1, j]) * dy)
+                    A[k, k] = (-A[k, k - 1] - A[k, k + 1] - A[k, k - ny - 1] - A[k, k + ny + 1]
+                               + rho * dx * dy / dt)
+                    b[k] = (p[i, j] - p[i, j - 1]) * dx + rho * dx * dy / dt * v0[i, j]
+        for i in range(1, nx + 1):
+            for j in range(1, ny + 2):
+                k = (i - 1) * (ny + 1) + (j - 1)
+                M[k, k] = A[k, k]
+
+    def fill_Ap(self):  # karman_taichi.py:297-339
+        nx, ny, dx, dy, rho = self.nx, self.ny, self.dx, self.dy, self.rho
+        ct, u, v = self.ct, self.u, self.v
+        A, M, b, Au, Av = self.Ap, self.Mp, self.bp, self.Au, self.Av
+        n = nx * ny
+        with np.errstate(divide="ignore"):
+            for i in range(1, nx + 1):
+                for j in range(1, ny + 1):
+                    k = (i - 1) * ny + (j - 1)
+                    b[k] = rho * (u[i, j] - u[i + 1, j]) * dy + rho * (v[i, j + 1] - v[i, j]) * dx
+                    vk = (i - 1) * (ny + 1) + (j - 1)
+                    A[k, k - 1] = -rho * dx * dx / np.float64(Av[vk, vk])
+                    A[k, k + 1] = -rho * dx * dx / np.float64(Av[vk + 1, vk + 1])
+                    uk = k
+                    A[k, k - ny] = -rho * dy * dy / np.float64(Au[uk, uk])
+                    A[k, k + ny] = -rho * dy * dy / np.float64(Au[uk + ny, uk + ny])
+                    if (ct[i, j] + ct[i, j - 1]) == 0:
+                        A[k, k - 1] = 0
+                    if (ct[i, j] + ct[i, j + 1]) == 0:
+                        A[k, k + 1] = 0
+                    if (ct[i, j] + ct[i - 1, j]) == 0:
+                        A[k, k - ny] = 0
+                    if (ct[i, j] + ct[i + 1, j]) == 0:
+                        A[k, k + ny] = 0
+                    A[k, k] = -A[k, k - 1] - A[k, k + 1] - A[k, k - ny] - A[k, k + ny]
+                    M[k, k] = A[k, k]
+        # second loop: inlet rows pinned with off-diagonals cleared; the outlet
+        # pins rows n-ny+1 .. n-1 (row n is out of range) and keeps their links
+        for i in range(ny):
+            for key in [kk for kk in A.e if kk[0] == i and kk[1] != i]:
+                A.e[key] = 0.0
+            A[i, i] = 1.0; M[i, i] = 1.0; b[i] = 0.0
+            A[n - i, n - i] = 1.0; M[n - i, n - i] = 1.0
+            if n - i < n:
+                b[n - i] = 0.0
+
+    def solve(self, A, M, b, x, eps):  # karman_taichi.py:342-456
+        n = b.size
+        S = self.ny if n in (self.nu, self.np_) else self.ny + 1
+        planes = A.planes(S)
+        diag = np.array([M[k, k] for k in range(n)])
+        res = bicgstab(planes, b, S, eps=eps, max_iter=100 * n, x0=x, M=diag,
+                       omega_break=True, order="karman")
+        x[...] = res.x
+        return res
+
+    def solve_momentum_bicgstab(self, eps=1e-8, max_iterations=1):  # :482-494
+        for _ in range(max_iterations):
+            self.fill_Au(); self.fill_Av()
+            ru = self.solve(self.Au, self.Mu, self.bu, self.xu, eps)
+            rv = self.solve(self.Av, self.Mv, self.bv, self.xv, eps)
+            self.xu_back(); self.xv_back()
+        return ru, rv
+
+    def xu_back(self):  # :459-464
+        nx, ny, a = self.nx, self.ny, self.velo_rel
+        xu = self.xu.reshape(nx + 1, ny)
+        self.u[1:nx + 2, 1:ny + 1] = self.u[1:nx + 2, 1:ny + 1] + a * (xu - self.u[1:nx + 2, 1:ny + 1])
+
+    def xv_back(self):  # :467-472
+        nx, ny, a = self.nx, self.ny, self.velo_rel
+        xv = self.xv.reshape(nx, ny + 1)
+        self.v[1:nx + 1, 1:ny + 2] = self.v[1:nx + 1, 1:ny + 2] + a * (xv - self.v[1:nx + 1, 1:ny + 2])
+
+    def xp_back(self):  # :475-478
+        self.pcor[1:self.nx + 1, 1:self.ny + 1] = self.xp.reshape(self.nx, self.ny)
+
+    def solve_pcorrection_bicgstab(self, eps=1e-8):  # :497-504
+        self.fill_Ap()
+        res = self.solve(self.Ap, self.Mp, self.bp, self.xp, eps)
+        self.xp_back()
+        return res
+
+    def puv_correction(self):  # :507-542
+        nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
+        ct, pc = self.ct, self.pcor
+        for i in range(1, nx + 2):
+            for j in range(1, ny + 1):
+                k = (i - 1) * ny + (j - 1)
+                s = ct[i - 1, j] + ct[i, j]
+                if s != 0 and s != 2:
+                    self.u[i, j] = self.u[i, j] + (pc[i - 1, j] - pc[i, j]) * dy / self.Au[k, k]
+        for i in range(1, nx + 1):
+            for j in range(1, ny + 2):
+                k = (i - 1) * (ny + 1) + (j - 1)
+                s = ct[i, j] + ct[i, j - 1]
+                if s != 0 and s != 2:
+                    self.v[i, j] = self.v[i, j] + (pc[i, j] - pc[i, j - 1]) * dx / self.Av[k, k]
+        fl = ct != 1
+        self.p[fl] = self.p[fl] + self.p_rel * pc[fl]
+        return float(np.abs(pc).max())
+
+    def correct_conserv(self):  # :586-614
+        nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
+        J = slice(1, ny + 1)
+        coef = float(np.sum(self.u[1, J])) / float(np.sum(self.u[nx + 1, J]))
+        self.u[nx + 1, J] = coef * self.u[nx + 1, J]
+        I = slice(1, nx + 1)
+        self.udiv[I, J] = (self.u[I, J] - self.u[2:nx + 2, J]) * dy + (self.v[I, 2:ny + 2] - self.v[I, J]) * dx
+
+    def time_forward(self):  # :617-622
+        self.u0 = self.u.copy(); self.v0 = self.v.copy()
+
+    def substep(self):
+        """One SIMPLE sub-iteration of the __main__ loop (karman_taichi.py:636-651)."""
+        ru, rv = self.solve_momentum_bicgstab(1e-8, 1)
+        self.correct_conserv()
+        rp = self.solve_pcorrection_bicgstab(1e-8)
+        pmax = self.puv_correction()
+        return dict(it_u=ru.iters, it_v=rv.iters, it_p=rp.iters, pcor_max=pmax,
+                    st=(ru.status, rv.status, rp.status))

@@ -1,0 +1,225 @@
+"""GPU parity of the stencil solvers (C ABI via ctypes) against the CPU oracle.
+
+Tolerances: FP64 SpMV <= 1e-13 relative (only FMA contraction differs);
+FP64 solves agree with the oracle / direct solves to <= 1e-6 relative, the
+field tolerance of the FP64 path; FP32 SpMV <= 1e-5 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import np_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand_system(n, S, seed, diag_shift=0.1, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    c = np.zeros((5, n))
+    k = np.arange(n)
+    for comp, off in ((1, -S), (2, S), (3, 1), (4, -1)):
+        ok = (k + off >= 0) & (k + off < n)
+        c[comp][ok] = -rng.random(n)[ok]
+    c[0] = -(c[1] + c[2] + c[3] + c[4]) + diag_shift
+    return c.astype(dtype)
+
+
+def _laplacian(N, offset=0.1):
+    """5-point Laplacian + offset on an N x N grid (benchmark/cg_to_sparse/
+    cgsolver.py compute_Ap: (4 + offset) x - neighbours, zero outside)."""
+    n = N * N
+    c = np.zeros((5, N, N))
+    c[0] = 4.0 + offset
+    c[1, 1:, :] = -1.0
+    c[2, :-1, :] = -1.0
+    c[3, :, :-1] = -1.0
+    c[4, :, 1:] = -1.0
+    return c.reshape(5, n)
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("n,S", [(1, 1), (7, 3), (320, 3), (1000, 33), (514 * 40 + 17, 514), (4096, 64),
+                                 (5000, 1), (3 * 5000, 5000)])
+def test_spmv_f64_matches_oracle(dev, n, S):
+    from karman_taichi_gb300 import linalg
+    c = _rand_system(n, S, seed=n + S)
+    x = np.random.default_rng(3).standard_normal(n)
+    y = linalg.spmv(linalg.Stencil(_t(c, dev), stride=S), _t(x, dev)).cpu().numpy()
+    ref = O.spmv(c, x, S)
+    assert np.abs(y - ref).max() <= 1e-13 * max(np.abs(ref).max(), 1.0)
+
+
+def test_spmv_f32(dev):
+    from karman_taichi_gb300 import linalg
+    n, S = 9000, 90
+    c = _rand_system(n, S, seed=5).astype(np.float32)
+    x = np.random.default_rng(4).standard_normal(n).astype(np.float32)
+    y = linalg.spmv(linalg.Stencil(_t(c, dev), stride=S), _t(x, dev)).cpu().numpy()
+    ref = O.spmv(c.astype(np.float64), x.astype(np.float64), S)
+    assert np.abs(y - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_spmv_aos_layout(dev):
+    """The reference's coef[i, j, 0..4] layout (simple.py:42) read in place."""
+    from karman_taichi_gb300 import linalg
+    NX, NY = 37, 29
+    c = _rand_system(NX * NY, NY, seed=9)
+    aos = np.ascontiguousarray(c.reshape(5, NX, NY).transpose(1, 2, 0))
+    x = np.random.default_rng(1).standard_normal((NX, NY))
+    y = linalg.spmv(linalg.Stencil(_t(aos, dev)), _t(x, dev)).cpu().numpy()
+    assert np.allclose(y.reshape(-1), O.spmv(c, x, NY), rtol=1e-13, atol=1e-13)
+
+
+def test_dot_deterministic(dev):
+    from karman_taichi_gb300 import linalg
+    rng = np.random.default_rng(2)
+    p, q = rng.standard_normal(1_000_003), rng.standard_normal(1_000_003)
+    tp, tq = _t(p, dev), _t(q, dev)
+    a = linalg.dot(tp, tq)
+    b = linalg.dot(tp, tq)
+    assert a == b
+    assert abs(a - float(np.dot(p, q))) <= 1e-12 * np.abs(p * q).sum()
+
+
+def test_bicgstab_kat_dense_solve(dev):
+    """debug/ti_bicg_test.py:21-98 restated with a seed: 5-diagonal (offsets
+    +-1, +-3), diag = -sum(off) + 0.1, n = 320, compared with np.linalg.solve."""
+    from karman_taichi_gb300 import linalg
+    n, S = 320, 3
+    c = _rand_system(n, S, seed=2022)
+    b = np.random.default_rng(2023).random(n)
+    xs = np.linalg.solve(O.to_csr(c, S).toarray(), b)
+    x = _t(np.zeros(n), dev)
+    info = linalg.bicgstab(linalg.Stencil(_t(c, dev), stride=S), _t(b, dev), x, eps=1e-8, max_iter=100 * n)
+    assert info.ok
+    xg = x.cpu().numpy()
+    assert np.allclose(xg, xs)
+    ref = O.bicgstab(c, b, S, eps=1e-8, max_iter=100 * n)
+    assert abs(info.iters - ref.iters) <= 1
+    assert np.abs(xg - ref.x).max() <= 1e-6 * np.abs(ref.x).max()
+
+
+def test_bicgstab_poisson_vs_direct(dev):
+    """benchmark/cg_to_sparse/test_cg_sparse.py:10-41: Laplacian + 0.1 I,
+    RHS sin*sin, BiCGSTAB vs a direct sparse solve."""
+    import scipy.sparse.linalg as spla
+    from karman_taichi_gb300 import linalg
+    N = 96
+    c = _laplacian(N)
+    xl = np.arange(N) * 2.0 / N
+    b = (np.sin(2 * np.pi * xl)[:, None] * np.sin(2 * np.pi * xl)[None, :]).reshape(-1)
+    xs = spla.spsolve(O.to_csr(c, N).tocsc(), b)
+    x = _t(np.zeros(N * N), dev)
+    info = linalg.bicgstab(linalg.Stencil(_t(c, dev), stride=N), _t(b, dev), x, eps=1e-10)
+    assert info.ok
+    assert np.abs(x.cpu().numpy() - xs).max() <= 1e-7 * np.abs(xs).max()
+
+
+def test_cg_poisson_and_history(dev):
+    import scipy.sparse.linalg as spla
+    from karman_taichi_gb300 import linalg
+    import torch
+    N = 64
+    c = _laplacian(N)
+    b = np.random.default_rng(0).standard_normal(N * N)
+    xs = spla.spsolve(O.to_csr(c, N).tocsc(), b)
+    x = _t(np.zeros(N * N), dev)
+    hist = torch.zeros(1000, dtype=torch.float64, device=dev)
+    info = linalg.cg(linalg.Stencil(_t(c, dev), stride=N), _t(b, dev), x, eps=1e-10, history=hist)
+    assert info.ok
+    assert np.abs(x.cpu().numpy() - xs).max() <= 1e-7 * np.abs(xs).max()
+    ref = O.cg(c, b, N, eps=1e-10)
+    assert abs(info.iters - ref.iters) <= 1
+    h = hist[: info.iters + 1].cpu().numpy()
+    assert h[0] == pytest.approx(math.sqrt(np.dot(b, b)), rel=1e-12)
+    assert h[-1] < 1e-10 * h[0]
+
+
+def test_jacobi_warm_start_matches_oracle(dev):
+    """karman_taichi.py:342-456: right Jacobi with an M that differs from A's
+    diagonal, warm start, omega == 0 break."""
+    from karman_taichi_gb300 import linalg
+    n, S = 2000, 40
+    c = _rand_system(n, S, seed=11, diag_shift=0.5)
+    M = c[0] * (1 + 0.1 * np.random.default_rng(1).random(n))
+    b = np.random.default_rng(12).standard_normal(n)
+    x0 = np.random.default_rng(13).standard_normal(n) * 0.1
+    ref = O.bicgstab(c, b, S, eps=1e-8, max_iter=100 * n, x0=x0, M=M, omega_break=True, order="karman")
+    x = _t(x0, dev)
+    info = linalg.bicgstab(linalg.Stencil(_t(c, dev), stride=S), _t(b, dev), x, eps=1e-8, max_iter=100 * n,
+                           warm=True, M=_t(M, dev), omega_break=True)
+    assert info.ok and ref.status == O.OK
+    assert abs(info.iters - ref.iters) <= 1
+    assert np.abs(x.cpu().numpy() - ref.x).max() <= 1e-6 * np.abs(ref.x).max()
+
+
+def test_graph_and_direct_launch_agree_bitwise(dev):
+    from karman_taichi_gb300 import linalg
+    N = 80
+    c = _laplacian(N, 0.05)
+    b = np.random.default_rng(7).standard_normal(N * N)
+    A = linalg.Stencil(_t(c, dev), stride=N)
+    xs = []
+    for g in (True, False, True):
+        x = _t(np.zeros(N * N), dev)
+        info = linalg.bicgstab(A, _t(b, dev), x, eps=1e-9, use_graph=g)
+        assert info.ok
+        xs.append(x.cpu().numpy())
+    assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[0], xs[2])
+
+
+def test_zero_rhs_nan_and_maxiter(dev):
+    """Failure detection on the host side of the ABI: b = 0 converges at once,
+    a NaN in b reports NONFINITE, a tiny cap reports MAXITER -- no trap."""
+    from karman_taichi_gb300 import linalg, _lib as L
+    N = 32
+    c = _laplacian(N)
+    A = linalg.Stencil(_t(c, dev), stride=N)
+    x = _t(np.ones(N * N), dev)
+    info = linalg.bicgstab(A, _t(np.zeros(N * N), dev), x)
+    assert info.status == L.OK and info.iters == 0 and float(x.abs().max()) == 0.0
+    b = np.random.default_rng(0).standard_normal(N * N)
+    b[17] = np.nan
+    info = linalg.bicgstab(A, _t(b, dev), _t(np.zeros(N * N), dev))
+    assert info.status == L.NONFINITE
+    b[17] = 1.0
+    info = linalg.bicgstab(A, _t(b, dev), _t(np.zeros(N * N), dev), max_iter=3)
+    assert info.status == L.MAXITER and info.iters == 3
+    info = linalg.cg(A, _t(b, dev), _t(np.zeros(N * N), dev), max_iter=2)
+    assert info.status == L.MAXITER and info.iters == 2
+
+
+def test_bad_arguments_raise(dev):
+    import torch
+    from karman_taichi_gb300 import linalg, _lib as L
+    c = _t(_laplacian(8), dev)
+    A = linalg.Stencil(c, stride=8)
+    with pytest.raises(ValueError):
+        linalg.bicgstab(A, _t(np.zeros(10), dev), _t(np.zeros(10), dev))
+    with pytest.raises(ValueError):
+        linalg.spmv(A, torch.zeros(64, dtype=torch.float64))   # CPU tensor: no fallback
+    lib = L.load()
+    assert lib.kc_spmv(None, None, None, None) == L.ERR_ARG
+    assert "null" in L.last_error()
+
+
+def test_refined_mixed_precision(dev):
+    import scipy.sparse.linalg as spla
+    from karman_taichi_gb300 import linalg
+    N = 128
+    c = _laplacian(N, 0.01)
+    b = np.random.default_rng(5).standard_normal(N * N)
+    xs = spla.spsolve(O.to_csr(c, N).tocsc(), b)
+    x = _t(np.zeros(N * N), dev)
+    info = linalg.bicgstab_refined(linalg.Stencil(_t(c, dev), stride=N),
+                                   linalg.Stencil(_t(c.astype(np.float32), dev), stride=N),
+                                   _t(b, dev), x, eps=1e-9, eps_inner=1e-3)
+    assert info.ok and info.refinements >= 2
+    r = b - O.to_csr(c, N) @ x.cpu().numpy()
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-9
+    assert np.abs(x.cpu().numpy() - xs).max() <= 1e-6 * np.abs(xs).max()
