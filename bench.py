@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""Time steps/s of the channel SIMPLE hot path (karman_taichi) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--config channel_2048x512] [--mode fp64|mixed|learned]
+
+One "step" is one time step of the channel case: SIMPLE outer iterations
+(momentum assembly + BiCGSTAB u/v solves, relaxation, pressure-correction
+assembly + BiCGSTAB p' solve, correction) until the predicted field's mass
+residual <= 1e-6 or 50 outer iterations, then u0 <- u.  W untimed warm-up
+steps, then exactly K timed steps between barriers + synchronizes, CUDA
+events on the solver stream, max over ranks.  Inputs: seeded synthetic
+channel initial state.  The working set of one step (fields, three systems of
+coefficient planes and the solver workspaces, several hundred MB) is larger
+than the 129 MB L2, so no separate L2 flush is inserted.
+
+Under torchrun every rank advances its own replica (replicas only: the path
+has no exchange step) and `value` is all ranks' time steps / the slowest
+rank's time.
+
+`--impl reference` times the CPU restatement of the same plain method
+(oracle/kc_cpu.c, C + OpenMP, FP64) on all host cores.  A 2048 x 512 time
+step takes minutes of CPU work, so each reference "step" is a bounded sample
+(one SIMPLE outer iteration with every BiCGSTAB solve capped); the measured
+seconds per BiCGSTAB iteration are converted to time steps/s with the
+BiCGSTAB iterations per time step of the identical algorithm, recorded in
+profiles/iteration_counts.json by the GPU FP64 run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Time steps/s at 2048x512: learned+mixed vs plain BiCGSTAB, same GB300, resid<=1e-6"
+COUNTS = os.path.join(ROOT, "profiles", "iteration_counts.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="channel_2048x512")
+    ap.add_argument("--mode", default="auto", choices=["auto", "fp64", "mixed", "learned"])
+    ap.add_argument("--compare-steps", type=int, default=2, help="timed steps of the FP64 plain comparison run")
+    ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                power.append(float(r[3]))
+                for nm, val in zip(names, r[5:9]):
+                    if val.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+def make_solver(cfg, mode, dev):
+    from karman_taichi_gb300.channel import ChannelSolver
+    if mode == "learned":
+        from karman_taichi_gb300 import learned
+        return learned.make_channel_solver(cfg, dev)
+    return ChannelSolver(cfg, device=dev, precision="fp64" if mode == "fp64" else "mixed")
+
+
+def resolve_mode(mode):
+    if mode != "auto":
+        return mode
+    try:
+        from karman_taichi_gb300 import learned
+        if learned.available():
+            return "learned"
+    except ImportError:
+        pass
+    return "fp64"
+
+
+def summarize(recs_per_step):
+    outer = [len(r) for r in recs_per_step]
+    its = [sum(s["it_u"] + s["it_v"] + s["it_p"] for s in r) for r in recs_per_step]
+    itp = [sum(s["it_p"] for s in r) for r in recs_per_step]
+    mass = [r[-1]["mass"] for r in recs_per_step]
+    return dict(outer_per_step=statistics.mean(outer), solver_iters_per_step=statistics.mean(its),
+                p_iters_per_step=statistics.mean(itp), mass_residual_last=mass,
+                mass_residual_max=max(mass), steps_converged=sum(1 for m in mass if m <= 1e-6))
+
+
+def timed_steps(solver, K, W, world, lib, clocks=None):
+    import torch
+    for _ in range(W):
+        solver.step()
+    torch.cuda.synchronize()
+    barrier(world)
+    l0 = lib.kc_launch_count()
+    if clocks:
+        clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    recs = [solver.step() for _ in range(K)]
+    e1.record()
+    torch.cuda.synchronize()
+    ck = clocks.stop() if clocks else None
+    barrier(world)
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
+    return ms, recs, lib.kc_launch_count() - l0, ck
+
+
+def e2e_steps(solver, K, world):
+    """The same steps through the public API with host-resident fields: every
+    step copies u, v, p, u0, v0 from pinned host memory and reads u, v, p back."""
+    import torch
+    names_in = ("u", "v", "p", "u0", "v0")
+    names_out = ("u", "v", "p")
+    host = {k: torch.empty(getattr(solver, k).shape, dtype=torch.float64, pin_memory=True) for k in names_in}
+    for k in names_in:
+        host[k].copy_(getattr(solver, k))
+    torch.cuda.synchronize()
+    barrier(world)
+    h2d = sum(host[k].numel() * 8 for k in names_in)
+    d2h = sum(host[k].numel() * 8 for k in names_out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(K):
+        for k in names_in:
+            getattr(solver, k).copy_(host[k], non_blocking=True)
+        solver.step()
+        for k in names_out:
+            host[k].copy_(getattr(solver, k), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        host["u0"].copy_(host["u"])
+        host["v0"].copy_(host["v"])
+    e1.record()
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
+    return ms, h2d, d2h
+
+
+def roofline_p_solve(solver, mode, peak):
+    """Dominant kernel: the p' BiCGSTAB solve (one persistent launch doing all
+    iterations).  achieved = 27 words/cell/iteration x iterations / duration."""
+    import torch
+    solver.assemble_momentum()
+    solver.solve_momentum()
+    solver.relax()
+    solver.assemble_p()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    info = solver._solve(solver.A_p, getattr(solver, "A_p32", None), solver.b_p, solver.pcor, solver.ws_p)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    n = solver.A_p.n
+    w = 8 if mode == "fp64" else 4
+    alg = 27 * w * n * info.iters
+    achieved = alg / (ms * 1e-3) / 1e9
+    kernel = "k_bicg_persist<double>" if mode == "fp64" else "k_bicg_persist<float>"
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            t = json.load(f).get(kernel)
+            if t:   # bytes per iteration per cell from an ncu capture, scaled to this launch
+                traffic = t["dram_bytes_per_cell_iter"] * n * info.iters
+    except (OSError, ValueError):
+        pass
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic,
+            "algorithmic_bytes": alg, "iters": info.iters, "ms": round(ms, 3),
+            "note": "27 words/cell/iteration (A 9R+2W, B 7R+1W, C 6R+2W); peak = measured hbm_gbs (burst)"}
+
+
+def cpu_sample(cfg, budget_s, iters_per_step):
+    """C/OpenMP FP64 plain path on the host cores: one SIMPLE outer iteration
+    with each BiCGSTAB solve capped so the sample fits the budget."""
+    import numpy as np
+    from karman_taichi_gb300 import geometry
+    from oracle import cpu
+    solid = geometry.solid_mask(cfg.nx, cfg.ny, cfg.obstacles)
+    u, v, p = geometry.channel_initial_fields(cfg.nx, cfg.ny, solid, cfg.U, cfg.noise, cfg.seed)
+    # calibrate on a short capped sample, then size the real one
+    st = cpu.channel_run(cfg, solid, u.copy(), v.copy(), p.copy(), n_steps=1, max_total_outer=1, max_solver_iter=20)
+    per_iter = st["seconds"] / max(st["solver_iters"], 1)
+    cap = int(max(20, min(5000, budget_s / per_iter / 3)))
+    st = cpu.channel_run(cfg, solid, u, v, p, n_steps=1, max_total_outer=1, max_solver_iter=cap)
+    per_iter = st["seconds"] / max(st["solver_iters"], 1)
+    value = 1.0 / (per_iter * iters_per_step) if iters_per_step else None
+    return {"value": value, "unit": "time steps/s", "cores": cpu.threads(), "kind": "port",
+            "seconds_per_bicgstab_iter": per_iter,
+            "sample": f"1 SIMPLE outer iteration of {cfg.name} from the seeded initial state, each BiCGSTAB solve "
+                      f"capped at {cap} iterations ({st['solver_iters']} iterations in {st['seconds']:.1f} s); "
+                      f"converted with {iters_per_step:.0f} BiCGSTAB iterations per time step of the same "
+                      f"algorithm (GPU FP64 run)"}
+
+
+def load_counts(config):
+    try:
+        with open(COUNTS) as f:
+            return json.load(f).get(config)
+    except (OSError, ValueError):
+        return None
+
+
+def save_counts(config, d):
+    try:
+        data = {}
+        if os.path.exists(COUNTS):
+            with open(COUNTS) as f:
+                data = json.load(f)
+        data[config] = d
+        os.makedirs(os.path.dirname(COUNTS), exist_ok=True)
+        with open(COUNTS, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+    except OSError:
+        pass
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    from karman_taichi_gb300 import _lib as L
+    from karman_taichi_gb300.config import PRESETS
+    rank, world, local = dist_init(args)
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = L.load()
+    cfg = PRESETS[args.config]
+    mode = resolve_mode(args.mode)
+    peak, peak_kind = peaks()
+    out = {"metric": METRIC, "unit": "time steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None}
+
+    solver = make_solver(cfg, mode, dev)
+    ms, recs, launches, ck = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
+    summ = summarize(recs)
+    value = world * args.steps / (ms * 1e-3)
+    out.update(value=round(value, 5), ms_per_step=round(ms / args.steps, 3),
+               dtype="f64" if mode == "fp64" else "f32+f64 (FP32 stencils/vectors, FP64 dots/residuals)",
+               data="synthetic: seeded channel initial state (u=1, v = U(-1e-3,1e-3) noise, p=0)",
+               config={"workload": cfg.name, "nx": cfg.nx, "ny": cfg.ny, "cells": cfg.cells, "Re": cfg.Re,
+                       "mode": mode, "mass_tol": cfg.mass_tol, "max_outer": cfg.max_outer, "eps": cfg.eps,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "working set per step > 129 MB L2 (no flush needed)"},
+               gpu_launches=launches, clocks=ck)
+    out["cell_updates_per_s"] = round(value * cfg.cells, 1)
+    out["stats"] = summ
+
+    if rank == 0 and not args.no_e2e:
+        e2e_ms, h2d, d2h = e2e_steps(solver, max(1, args.steps // 2), 1)
+        k = max(1, args.steps // 2)
+        out["e2e"] = {"value": round(k / (e2e_ms * 1e-3), 5), "unit": "time steps/s",
+                      "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                      "note": "public ChannelSolver.step() with u, v, p, u0, v0 copied from pinned host memory "
+                              "and u, v, p read back every step"}
+    if rank == 0:
+        out["roofline"] = roofline_p_solve(solver, mode, peak)
+        out["roofline"]["peak_kind"] = peak_kind
+
+    fp64_counts = summ if mode == "fp64" else None
+    if rank == 0 and not args.no_compare and mode != "fp64":
+        ref = make_solver(cfg, "fp64", dev)
+        cms, crecs, _, _ = timed_steps(ref, args.compare_steps, args.warmup, 1, lib)
+        fp64_counts = summarize(crecs)
+        out["fp64_plain"] = {"value": round(args.compare_steps / (cms * 1e-3), 5), "unit": "time steps/s",
+                             "ms_per_step": round(cms / args.compare_steps, 3), "steps": args.compare_steps,
+                             "warmup": args.warmup, "stats": fp64_counts}
+        out["speedup_vs_fp64_plain"] = round(value / out["fp64_plain"]["value"], 3)
+        a, b = solver.state_numpy(), ref.state_numpy()
+        out["field_error_vs_fp64"] = {k: float(abs(a[k] - b[k]).max() / max(abs(b[k]).max(), 1e-300))
+                                      for k in ("u", "v", "p")}
+    if rank == 0 and fp64_counts:
+        save_counts(cfg.name, {"solver_iters_per_step": fp64_counts["solver_iters_per_step"],
+                               "outer_per_step": fp64_counts["outer_per_step"],
+                               "source": "GPU FP64 plain run of bench.py (steps after warm-up)"})
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cnt = fp64_counts or load_counts(cfg.name) or {}
+        out["cpu_baseline"] = cpu_sample(cfg, args.cpu_budget, cnt.get("solver_iters_per_step"))
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference arm: the plain method's CPU implementation (C + OpenMP
+    restatement; the reference's Taichi CPU path needs taichi==0.9.0, which is
+    not installed), on all host cores, same config/metric/unit."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from karman_taichi_gb300 import geometry
+    from karman_taichi_gb300.config import PRESETS
+    from oracle import cpu
+    cfg = PRESETS[args.config]
+    cnt = load_counts(cfg.name)
+    if not cnt:
+        print(json.dumps({"impl": "reference", "unavailable": "no recorded BiCGSTAB iterations per time step "
+                          "(run the GPU arm once to record profiles/iteration_counts.json)"}))
+        return
+    its_per_step = cnt["solver_iters_per_step"]
+    solid = geometry.solid_mask(cfg.nx, cfg.ny, cfg.obstacles)
+    u, v, p = geometry.channel_initial_fields(cfg.nx, cfg.ny, solid, cfg.U, cfg.noise, cfg.seed)
+    st = cpu.channel_run(cfg, solid, u.copy(), v.copy(), p.copy(), n_steps=1, max_total_outer=1, max_solver_iter=10)
+    per = st["seconds"] / max(st["solver_iters"], 1)
+    budget = 60.0 / max(args.steps + args.warmup, 1)
+    cap = int(max(10, min(5000, budget / per / 3)))
+    samples = []
+    for k in range(args.warmup + args.steps):
+        uu, vv, pp = u.copy(), v.copy(), p.copy()
+        st = cpu.channel_run(cfg, solid, uu, vv, pp, n_steps=1, max_total_outer=1, max_solver_iter=cap)
+        if k >= args.warmup:
+            samples.append(st["seconds"] / max(st["solver_iters"], 1))
+    per = statistics.mean(samples)
+    value = 1.0 / (per * its_per_step)
+    out = {"metric": METRIC, "value": value, "unit": "time steps/s", "impl": "reference", "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic: seeded channel initial state",
+           "config": {"workload": cfg.name, "nx": cfg.nx, "ny": cfg.ny, "cells": cfg.cells, "mode": "fp64 plain"},
+           "cpu_baseline": {"value": value, "unit": "time steps/s", "cores": cpu.threads(), "kind": "port",
+                            "sample": f"each step: 1 SIMPLE outer iteration of {cfg.name}, BiCGSTAB solves capped "
+                                      f"at {cap} iterations; seconds per BiCGSTAB iteration x {its_per_step:.0f} "
+                                      f"iterations per time step ({cnt.get('source', '')})"},
+           "e2e": {"value": value, "unit": "time steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)

@@ -69,6 +69,8 @@ typedef struct {
     int rel_to;           /* KC_REL_R0 | KC_REL_B                                */
     int check_every;      /* host polls convergence every N iterations (0: auto)*/
     int use_graph;        /* capture iteration chunks in a CUDA graph            */
+    int persistent;       /* 1: one cooperative launch runs the whole solve      */
+    int pad_;
     double* history;      /* device array or NULL: history[k] = ||r_k||_2       */
     long long history_len;/* capacity of history (entries beyond are dropped)   */
 } kc_solve_opts;
@@ -86,6 +88,8 @@ int         kc_version(void);
 const char* kc_status_str(int status);
 const char* kc_last_error(void);
 int         kc_device_count(void);
+/* Kernels launched by this library in this process (graph nodes included). */
+long long   kc_launch_count(void);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),

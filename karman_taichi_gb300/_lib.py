@@ -44,6 +44,7 @@ class KcSolveOpts(C.Structure):
     _fields_ = [("eps", C.c_double), ("max_iter", C.c_longlong), ("x0", C.c_int),
                 ("precond", C.c_int), ("omega_break", C.c_int), ("rel_to", C.c_int),
                 ("check_every", C.c_int), ("use_graph", C.c_int),
+                ("persistent", C.c_int), ("pad_", C.c_int),
                 ("history", C.c_void_p), ("history_len", C.c_longlong)]
 
 
@@ -78,6 +79,7 @@ SIGNATURES = {
     "kc_status_str": (C.c_char_p, [I_]),
     "kc_last_error": (C.c_char_p, []),
     "kc_device_count": (I_, []),
+    "kc_launch_count": (L_, []),
     "kc_spmv": (I_, [C.POINTER(KcSystem), P_, P_, P_]),
     "kc_dot_ws_bytes": (S_, [L_]),
     "kc_dot": (I_, [I_, L_, P_, P_, P_, P_, S_, P_]),

@@ -3,10 +3,14 @@
 #include "kc_common.cuh"
 #include <stdarg.h>
 #include <stdio.h>
+#include <atomic>
 
 namespace kc {
 
 static thread_local char g_err[512] = "";
+static std::atomic<long long> g_launches{0};
+
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
     va_list ap;
@@ -43,6 +47,8 @@ const char* kc_status_str(int status) {
 }
 
 const char* kc_last_error(void) { return kc::g_err; }
+
+long long kc_launch_count(void) { return kc::g_launches.load(std::memory_order_relaxed); }
 
 int kc_device_count(void) {
     int n = 0;

@@ -19,10 +19,17 @@ int cuda_status(cudaError_t e, const char* what);
         cudaError_t e_ = (call);                                   \
         if (e_ != cudaSuccess) return ::kc::cuda_status(e_, #call); \
     } while (0)
-#define KC_LAUNCH_CHECK(what)                                      \
+// Process-wide count of kernels this library has launched (kc_launch_count).
+void count_launches(long long n);
+#define KC_LAUNCH_CHECK_NC(what)                                   \
     do {                                                           \
         cudaError_t e_ = cudaGetLastError();                       \
         if (e_ != cudaSuccess) return ::kc::cuda_status(e_, what); \
+    } while (0)
+#define KC_LAUNCH_CHECK(what)          \
+    do {                               \
+        ::kc::count_launches(1);       \
+        KC_LAUNCH_CHECK_NC(what);      \
     } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }

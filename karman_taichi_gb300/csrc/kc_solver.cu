@@ -10,12 +10,16 @@
 //   CG          cgsolver.py:83-114
 //
 // Layout: every vector is a flat array of n elements; the stencil couples
-// k +- 1 and k +- S.  A stencil block covers 32 consecutive columns (one per
-// lane, so warp loads are fully coalesced along the contiguous index) and
-// kWarps*kRows rows; each warp streams down kRows rows holding the operand of
-// rows i-1, i, i+1 in registers, and takes the j +- 1 neighbours from the
-// adjacent lanes with shuffles.  Only the two edge lanes and the strip ends
-// recompute a neighbour from global memory.
+// k +- 1 and k +- S.  A stencil block (256 threads) owns a tile of kTI = 32
+// rows x kTJ = 32 consecutive columns of the [rows][S] view.  It evaluates the
+// stencil operand (e.g. p = r + beta (p - omega v), times M^-1) once for every
+// point of the tile plus a one-point halo into shared memory -- owned points
+// also store their side outputs -- then each thread applies the stencil to
+// four cells from shared memory.  All global loads of a phase are issued
+// before any is consumed (the loops are fully unrolled), warp loads are 32
+// consecutive elements, read-only streams use the read-only path and every
+// pointer is restrict-qualified.  Halo points use flat index arithmetic, so
+// the k +- 1 neighbours across a row end follow the reference's 1-D gather.
 //
 // One BiCGSTAB iteration is three launches (27 words of traffic per cell):
 //   A  p = r + beta (p - omega v) [x M^-1]  ->  v = A p^,   partial (r~, v)
@@ -24,6 +28,14 @@
 // The last block of each launch reduces the partials in a fixed order and
 // advances the scalar recurrence on the device, so the host never waits on a
 // dot product; it polls a "done" word once per chunk of iterations.
+//
+// Inner products: in FP64 mode every product and sum is FP64.  In FP32 mode
+// each product of two floats is formed exactly as a (hi, lo) float pair
+// (fmaf) and summed -- per thread, across the warp and across the block -- in
+// double-float arithmetic (Knuth TwoSum, ~48-bit significand); each block's
+// partial is then carried in FP64 and the partials are summed in FP64.
+// GB300 issues FP64 at 1/60 of its FP32 rate (1.19 vs 72 TFLOP/s measured),
+// so FP64 work per cell would make the FP32 solver compute bound.
 #include "kc_common.cuh"
 #include <algorithm>
 #include <mutex>
@@ -32,16 +44,21 @@
 
 namespace kc {
 
-constexpr int kWarps = 8;   // warps per stencil block (256 threads)
-constexpr int kRows = 8;    // rows streamed by each warp
-constexpr int kThreads = kWarps * kWarp;
-constexpr int kPwThreads = 256;   // pointwise kernels
-constexpr int kPwMaxBlocks = 2048;
+constexpr int kTJ = 32;            // tile columns (one per lane)
+constexpr int kTI = 32;            // tile rows
+constexpr int kThreads = 256;      // 8 warps
+constexpr int kCPT = kTI * kTJ / kThreads;            // cells per thread (4)
+constexpr int kPts = (kTI + 2) * (kTJ + 2);           // operand points incl. halo
+constexpr int kPtIters = (kPts + kThreads - 1) / kThreads;
+constexpr int kPwThreads = 256;    // pointwise kernels
+constexpr int kPwPer = 4;          // elements per thread per round
+constexpr int kPwMaxBlocks = 4096;
 
 struct SolverState {
     double rho, rho_1, alpha, omega, beta;
     double r0Tr, rTr, den, eps, old;
-    double prev_rel;
+    double prev_rel, lim;
+    float alpha_f, omega_f, beta_f, pad_f;
     long long iter, max_iter;
     int status, done, omega_break, rel_to;
     unsigned ticket[4];
@@ -55,29 +72,28 @@ __device__ __forceinline__ void record_history(SolverState* st, long long k, dou
 
 template <typename T>
 struct Coef {
-    const T* c;
+    const T* __restrict__ c;
     long long cs, es;
-    __device__ __forceinline__ T at(int comp, long long k) const { return __ldg(c + comp * cs + k * es); }
+    __device__ __forceinline__ T at(int comp, int k) const { return __ldg(c + comp * cs + (long long)k * es); }
 };
 
 struct Geo {
-    long long n;
-    int S;
+    int n, S;
 };
 
 static inline dim3 stencil_grid(long long n, int S) {
     long long rows = (n + S - 1) / S;
-    long long gx = (S + kWarp - 1) / kWarp;
-    long long gy = (rows + kWarps * kRows - 1) / (kWarps * kRows);
+    long long gx = (S + kTJ - 1) / kTJ;
+    long long gy = (rows + kTI - 1) / kTI;
     return dim3((unsigned)gx, (unsigned)gy);
 }
 static inline bool stencil_grid_ok(long long n, int S) {
-    if (S < 1 || n < 1) return false;
+    if (S < 1 || n < 1 || n > (1ll << 31) - 4ll * S - 64) return false;
     dim3 g = stencil_grid(n, S);
-    return g.y <= 65535u && (long long)g.x * g.y <= (1ll << 31);
+    return g.y <= 65535u && (long long)g.x * g.y <= (1ll << 30);
 }
 static inline int pw_blocks(long long n) {
-    long long b = (n + kPwThreads * 4 - 1) / (kPwThreads * 4);
+    long long b = (n + kPwThreads * kPwPer - 1) / (kPwThreads * kPwPer);
     return (int)std::max<long long>(1, std::min<long long>(b, kPwMaxBlocks));
 }
 
@@ -86,74 +102,219 @@ __device__ __forceinline__ T fmaT(T a, T b, T c) { return fma(a, b, c); }
 template <>
 __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Loads of vectors that other blocks of the same (persistent) kernel wrote
+// must bypass L1 (COH = true -> ld.global.cg); otherwise the read-only path.
+template <bool COH, typename T>
+__device__ __forceinline__ T ld(const T* p) {
+    if constexpr (COH) return __ldcg(p);
+    else return __ldg(p);
+}
+
+// scalars of the recurrence in the vector precision (float copies are written
+// by the finalisers so FP32 kernels never convert)
+template <typename T>
+struct Scal;
+template <>
+struct Scal<double> {
+    __device__ static double alpha(const SolverState* s) { return __ldcg(&s->alpha); }
+    __device__ static double omega(const SolverState* s) { return __ldcg(&s->omega); }
+    __device__ static double beta(const SolverState* s) { return __ldcg(&s->beta); }
+};
+template <>
+struct Scal<float> {
+    __device__ static float alpha(const SolverState* s) { return __ldcg(&s->alpha_f); }
+    __device__ static float omega(const SolverState* s) { return __ldcg(&s->omega_f); }
+    __device__ static float beta(const SolverState* s) { return __ldcg(&s->beta_f); }
+};
+
+// ---- inner-product accumulators -------------------------------------------------
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+};
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+template <>
+struct Acc<float> {
+    DF s{0.f, 0.f};
+    __device__ __forceinline__ void add(float a, float b) {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);   // a*b == p + e exactly
+        s = df_add(s, DF{p, e});
+    }
+};
+
+// Thread 0 publishes the block's partials, fences, and takes a ticket; the
+// last block to arrive gets true (no block ever waits on another).
+__device__ __forceinline__ bool publish_and_arrive(unsigned* ticket, unsigned nb) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// Block sums of NV accumulators into partials[q*ld + bid]; returns true in
+// the last block, with the fixed-order totals in out[] (thread 0).
+template <int NV>
+__device__ __forceinline__ bool block_partials(const Acc<double> (&a)[NV], double* partials, int ld, int bid,
+                                               int nb, unsigned* ticket, double (&out)[NV]) {
+    double d[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) d[q] = a[q].s;
+    block_sum<NV>(d);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) partials[q * ld + bid] = d[q];
+    }
+    if (!publish_and_arrive(ticket, nb)) return false;
+    reduce_partials<NV>(partials, ld, nb, out);
+    return true;
+}
+
+template <int NV>
+__device__ __forceinline__ bool block_partials(const Acc<float> (&a)[NV], double* partials, int ld, int bid,
+                                               int nb, unsigned* ticket, double (&out)[NV]) {
+    __shared__ DF sh[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        DF v = a[q].s;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            DF u{__shfl_down_sync(kFull, v.hi, o), __shfl_down_sync(kFull, v.lo, o)};
+            v = df_add(v, u);
+        }
+        if (lane == 0) sh[q][w] = v;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            DF v = lane < nw ? sh[q][lane] : DF{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                DF u{__shfl_down_sync(kFull, v.hi, o), __shfl_down_sync(kFull, v.lo, o)};
+                v = df_add(v, u);
+            }
+            if (lane == 0) partials[q * ld + bid] = (double)v.hi + (double)v.lo;
+        }
+    }
+    if (!publish_and_arrive(ticket, nb)) return false;
+    reduce_partials<NV>(partials, ld, nb, out);
+    return true;
+}
+
 // -----------------------------------------------------------------------------
-// Streaming stencil strip.  Pol provides:
-//   Val owner(k)   operand at k for the owning thread (may store side outputs)
-//   T   halo(k)    operand at k recomputed for a neighbour (no side effects)
-//   void sink(k, y, center, acc)   consumes y = (A operand)[k]
+// Tiled stencil.  Pol provides (all __device__):
+//   T    pre(k)            operand before the diagonal scaling (loads)
+//   T    scale(k, pre)     operand fed to the stencil (x M^-1 when preconditioned)
+//   void own(k, pre)       side outputs of a point owned by this tile
+//   void sink(k, y, pre_k, acc)   consumes y = (A operand)[k]
+//   static constexpr bool kAux    whether sink needs pre_k
 // -----------------------------------------------------------------------------
 template <typename T, int NACC, class Pol>
-__device__ __forceinline__ void stencil_strip(const Pol& pol, const Coef<T> A, long long n, int S,
-                                              double (&acc)[NACC]) {
-    using Val = typename Pol::Val;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const long long j = (long long)blockIdx.x * kWarp + lane;
-    const bool colok = j < S;
-    const long long i0 = ((long long)blockIdx.y * kWarps + w) * kRows;
-    if (i0 * (long long)S >= n) return;  // whole warp below the last row (warp-uniform)
-    long long k = i0 * S + j;
-    Val c = (colok && k < n) ? pol.owner(k) : Val::zero();
-    T xm = (colok && i0 > 0 && k < n) ? pol.halo(k - S) : T(0);
-#pragma unroll 2
-    for (int r = 0; r < kRows; ++r) {
-        const long long kn = k + S;
-        const bool okc = colok && k < n;
-        const bool okn = colok && kn < n;
-        Val nxt = Val::zero();
-        T xp;
-        if (r + 1 < kRows) {
-            if (okn) nxt = pol.owner(kn);
-            xp = nxt.op;
-        } else {
-            xp = okn ? pol.halo(kn) : T(0);
+__device__ __forceinline__ void stencil_tile_at(const Pol& pol, const Coef<T>& A, int n, int S, int i0, int j0,
+                                                Acc<T> (&acc)[NACC]) {
+    __shared__ T op[kTI + 2][kTJ + 2];
+    __shared__ T aux[Pol::kAux ? kTI : 1][Pol::kAux ? kTJ : 1];
+    T pre[kPtIters];
+    int kk[kPtIters];
+#pragma unroll
+    for (int q = 0; q < kPtIters; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        const int a = e / (kTJ + 2), b = e - a * (kTJ + 2);
+        const long long kl = (long long)(i0 + a - 1) * S + (j0 + b - 1);
+        const bool in = e < kPts && kl >= 0 && kl < n;
+        kk[q] = in ? (int)kl : -1;
+        pre[q] = in ? pol.pre((int)kl) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < kPtIters; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        if (e < kPts) {
+            const int a = e / (kTJ + 2), b = e - a * (kTJ + 2);
+            const int k = kk[q];
+            T v = T(0);
+            if (k >= 0) {
+                v = pol.scale(k, pre[q]);
+                if (a >= 1 && a <= kTI && b >= 1 && b <= kTJ && (j0 + b - 1) < S) {
+                    pol.own(k, pre[q]);
+                    if (Pol::kAux) aux[a - 1][b - 1] = pre[q];
+                }
+            }
+            op[a][b] = v;
         }
-        T xl = __shfl_up_sync(kFull, c.op, 1);
-        T xr = __shfl_down_sync(kFull, c.op, 1);
-        if (lane == 0) xl = (okc && k >= 1) ? pol.halo(k - 1) : T(0);
-        if (lane == kWarp - 1 || j == S - 1) xr = (okc && k + 1 < n) ? pol.halo(k + 1) : T(0);
-        if (okc) {
-            T y = A.at(0, k) * c.op;
-            y = fmaT<T>(A.at(1, k), xm, y);
-            y = fmaT<T>(A.at(2, k), xp, y);
-            y = fmaT<T>(A.at(3, k), xr, y);
-            y = fmaT<T>(A.at(4, k), xl, y);
-            pol.sink(k, y, c, acc);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int j = j0 + tx;
+    T c[kCPT][5];
+    int kc[kCPT];
+#pragma unroll
+    for (int r = 0; r < kCPT; ++r) {
+        const int a = ty + 8 * r;
+        const long long kl = (long long)(i0 + a) * S + j;
+        const bool ok = j < S && kl < n;
+        kc[r] = ok ? (int)kl : -1;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) c[r][q] = ok ? A.at(q, (int)kl) : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < kCPT; ++r) {
+        if (kc[r] >= 0) {
+            const int a = ty + 8 * r;
+            T y = c[r][0] * op[a + 1][tx + 1];
+            y = fmaT<T>(c[r][1], op[a][tx + 1], y);
+            y = fmaT<T>(c[r][2], op[a + 2][tx + 1], y);
+            y = fmaT<T>(c[r][3], op[a + 1][tx + 2], y);
+            y = fmaT<T>(c[r][4], op[a + 1][tx], y);
+            pol.sink(kc[r], y, Pol::kAux ? aux[a][tx] : T(0), acc);
         }
-        xm = c.op;
-        c = nxt;
-        k = kn;
     }
 }
+
+template <typename T, int NACC, class Pol>
+__device__ __forceinline__ void stencil_tile(const Pol& pol, const Coef<T>& A, int n, int S,
+                                             Acc<T> (&acc)[NACC]) {
+    stencil_tile_at<T, NACC, Pol>(pol, A, n, S, blockIdx.y * kTI, blockIdx.x * kTJ, acc);
+}
+
+__device__ __forceinline__ int block_id() { return blockIdx.y * gridDim.x + blockIdx.x; }
+__device__ __forceinline__ int block_count() { return gridDim.x * gridDim.y; }
 
 // ---- plain SpMV ---------------------------------------------------------------
 template <typename T>
 struct PolSpmv {
-    const T* x;
-    T* y;
-    struct Val {
-        T op;
-        __device__ static Val zero() { return {T(0)}; }
-    };
-    __device__ Val owner(long long k) const { return {x[k]}; }
-    __device__ T halo(long long k) const { return x[k]; }
-    __device__ void sink(long long k, T v, const Val&, double (&)[1]) const { y[k] = v; }
+    static constexpr bool kAux = false;
+    const T* __restrict__ x;
+    T* __restrict__ y;
+    __device__ __forceinline__ T pre(int k) const { return __ldg(x + k); }
+    __device__ __forceinline__ T scale(int, T p) const { return p; }
+    __device__ __forceinline__ void own(int, T) const {}
+    __device__ __forceinline__ void sink(int k, T v, T, Acc<T> (&)[1]) const { y[k] = v; }
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_spmv(Coef<T> A, Geo g, const T* x, T* y) {
-    double acc[1] = {0.0};
+__global__ void __launch_bounds__(kThreads) k_spmv(Coef<T> A, Geo g, const T* __restrict__ x, T* __restrict__ y) {
+    Acc<T> acc[1];
     PolSpmv<T> pol{x, y};
-    stencil_strip<T, 1>(pol, A, g.n, g.S, acc);
+    stencil_tile<T, 1>(pol, A, g.n, g.S, acc);
 }
 
 // ---- dot ----------------------------------------------------------------------
@@ -164,15 +325,15 @@ struct DotWs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kPwThreads) k_dot(long long n, const T* p, const T* q, DotWs* ws,
-                                                    double* out) {
+__global__ void __launch_bounds__(kPwThreads) k_dot(long long n, const T* __restrict__ p, const T* __restrict__ q,
+                                                    DotWs* ws, double* out) {
     double acc[1] = {0.0};
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x)
-        acc[0] += (double)p[k] * (double)q[k];
+        acc[0] += (double)__ldg(p + k) * (double)__ldg(q + k);
     block_sum<1>(acc);
     if (threadIdx.x == 0) ws->partials[blockIdx.x] = acc[0];
-    if (arrive_last(&ws->ticket[0], gridDim.x)) {
+    if (publish_and_arrive(&ws->ticket[0], gridDim.x)) {
         double s[1];
         reduce_partials<1>(ws->partials, 0, gridDim.x, s);
         if (threadIdx.x == 0) {
@@ -193,6 +354,23 @@ struct BicgPtrs {
 
 __device__ __forceinline__ bool solver_done(const SolverState* st) {
     return __ldcg(&st->done) != 0;
+}
+
+__device__ __forceinline__ void set_alpha(SolverState* st, double a) {
+    st->alpha = a;
+    st->alpha_f = (float)a;
+    if (!isfinite(a) || fabs(a) > st->lim) {
+        st->status = KC_NONFINITE;
+        st->done = 1;
+    }
+}
+__device__ __forceinline__ void set_omega(SolverState* st, double w) {
+    st->omega = w;
+    st->omega_f = (float)w;
+    if (!isfinite(w) || fabs(w) > st->lim) {
+        st->status = KC_NONFINITE;
+        st->done = 1;
+    }
 }
 
 // Called by thread 0 of the last block of pass C with (r, r~) and (r, r).
@@ -220,7 +398,13 @@ __device__ void bicg_finish_iteration(SolverState* st, double rho_new, double rT
     } else {
         st->rho_1 = st->rho;
         st->rho = rho_new;
-        st->beta = (st->rho / st->rho_1) * (st->alpha / st->omega);
+        const double beta = (st->rho / st->rho_1) * (st->alpha / st->omega);
+        st->beta = beta;
+        st->beta_f = (float)beta;
+        if (!isfinite(beta) || fabs(beta) > st->lim) {
+            st->status = KC_NONFINITE;
+            st->done = 1;
+        }
     }
 }
 
@@ -230,26 +414,29 @@ struct StartArgs {
     int omega_break, rel_to;
     double* hist;
     long long hist_len;
+    double lim;   // largest scalar the vector precision can carry
 };
 
 __device__ void bicg_start(SolverState* st, double r0Tr, double bb, const StartArgs& a) {
     const double eps = a.eps;
     const long long max_iter = a.max_iter;
-    const int omega_break = a.omega_break, rel_to = a.rel_to;
     st->hist = a.hist;
     st->hist_len = a.hist_len;
+    st->lim = a.lim;
     record_history(st, 0, r0Tr);
     st->iter = 0;
     st->max_iter = max_iter;
     st->eps = eps;
-    st->omega_break = omega_break;
-    st->rel_to = rel_to;
+    st->omega_break = a.omega_break;
+    st->rel_to = a.rel_to;
     st->r0Tr = r0Tr;
     st->rTr = r0Tr;
-    st->den = rel_to == KC_REL_B ? bb : r0Tr;
+    st->den = a.rel_to == KC_REL_B ? bb : r0Tr;
     st->rho = r0Tr;  // r~ = r0, so rho_0 = (r0, r0)
     st->rho_1 = st->alpha = st->omega = 1.0;
+    st->alpha_f = st->omega_f = 1.f;
     st->beta = 0.0;
+    st->beta_f = 0.f;
     st->old = r0Tr;
     st->status = KC_MAXITER;
     st->done = 0;
@@ -260,7 +447,7 @@ __device__ void bicg_start(SolverState* st, double r0Tr, double bb, const StartA
     } else if (!isfinite(r0Tr)) {
         st->status = KC_NONFINITE;
         st->done = 1;
-    } else if (rel_to == KC_REL_B && st->prev_rel < eps) {
+    } else if (a.rel_to == KC_REL_B && st->prev_rel < eps) {
         st->status = KC_OK;
         st->done = 1;
     } else if (max_iter <= 0) {
@@ -269,120 +456,103 @@ __device__ void bicg_start(SolverState* st, double r0Tr, double bb, const StartA
     }
 }
 
+// Pointwise driver: each block handles rounds of kPwThreads*kPwPer elements,
+// every round issuing all its loads before computing.
+#define KC_PW_LOOP(n, ...)                                                                  \
+    for (int base_ = blockIdx.x * (kPwThreads * kPwPer); base_ < (n);                      \
+         base_ += gridDim.x * (kPwThreads * kPwPer)) {                                      \
+        _Pragma("unroll") for (int u_ = 0; u_ < kPwPer; ++u_) {                             \
+            const int k = base_ + threadIdx.x + u_ * kPwThreads;                            \
+            if (k < (n)) { __VA_ARGS__ }                                                           \
+        }                                                                                   \
+    }
+
 // cold start: r = r~ = b, x = 0; optional invM = 1/M
 template <typename T>
 __global__ void __launch_bounds__(kPwThreads)
-    k_bicg_init_cold(long long n, const T* b, T* x, T* r, T* rt, const T* M, T* invM, BicgPtrs P,
-                     StartArgs sa) {
-    double acc[1] = {0.0};
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x) {
-        T bk = b[k];
+    k_bicg_init_cold(int n, const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r, T* __restrict__ rt,
+                     const T* __restrict__ M, T* __restrict__ invM, BicgPtrs P, StartArgs sa) {
+    Acc<T> acc[1];
+    KC_PW_LOOP(n, {
+        const T bk = __ldg(b + k);
         r[k] = bk;
         rt[k] = bk;
         x[k] = T(0);
-        if (M) invM[k] = T(1) / M[k];
-        acc[0] += (double)bk * (double)bk;
-    }
-    block_sum<1>(acc);
-    if (threadIdx.x == 0) P.partials[blockIdx.x] = acc[0];
-    if (arrive_last(&P.st->ticket[0], gridDim.x)) {
-        double s[1];
-        reduce_partials<1>(P.partials, P.ld, gridDim.x, s);
-        if (threadIdx.x == 0) {
-            bicg_start(P.st, s[0], s[0], sa);
-            P.st->ticket[0] = 0;
-        }
+        if (M) invM[k] = T(1) / __ldg(M + k);
+        acc[0].add(bk, bk);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
+        bicg_start(P.st, s[0], s[0], sa);
+        P.st->ticket[0] = 0;
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPwThreads) k_invdiag(long long n, const T* M, T* invM) {
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x)
-        invM[k] = T(1) / M[k];
+__global__ void __launch_bounds__(kPwThreads) k_invdiag(int n, const T* __restrict__ M, T* __restrict__ invM) {
+    KC_PW_LOOP(n, { invM[k] = T(1) / __ldg(M + k); })
 }
 
 // warm start: r = r~ = b - A x
 template <typename T>
 struct PolWarm {
-    const T* x;
-    const T* b;
-    T* r;
-    T* rt;
-    struct Val {
-        T op;
-        __device__ static Val zero() { return {T(0)}; }
-    };
-    __device__ Val owner(long long k) const { return {x[k]}; }
-    __device__ T halo(long long k) const { return x[k]; }
-    __device__ void sink(long long k, T y, const Val&, double (&acc)[2]) const {
-        T bk = b[k];
-        T rk = bk - y;
+    static constexpr bool kAux = false;
+    const T* __restrict__ x;
+    const T* __restrict__ b;
+    T* __restrict__ r;
+    T* __restrict__ rt;
+    __device__ __forceinline__ T pre(int k) const { return __ldg(x + k); }
+    __device__ __forceinline__ T scale(int, T p) const { return p; }
+    __device__ __forceinline__ void own(int, T) const {}
+    __device__ __forceinline__ void sink(int k, T y, T, Acc<T> (&acc)[2]) const {
+        const T bk = __ldg(b + k);
+        const T rk = bk - y;
         r[k] = rk;
         rt[k] = rk;
-        acc[0] += (double)rk * (double)rk;
-        acc[1] += (double)bk * (double)bk;
+        acc[0].add(rk, rk);
+        acc[1].add(bk, bk);
     }
 };
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_bicg_init_warm(Coef<T> A, Geo g, const T* b, const T* x, T* r, T* rt, BicgPtrs P, StartArgs sa) {
-    double acc[2] = {0.0, 0.0};
+    k_bicg_init_warm(Coef<T> A, Geo g, const T* __restrict__ b, const T* __restrict__ x, T* __restrict__ r,
+                     T* __restrict__ rt, BicgPtrs P, StartArgs sa) {
+    Acc<T> acc[2];
     PolWarm<T> pol{x, b, r, rt};
-    stencil_strip<T, 2>(pol, A, g.n, g.S, acc);
-    block_sum<2>(acc);
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x == 0) {
-        P.partials[bid] = acc[0];
-        P.partials[P.ld + bid] = acc[1];
-    }
-    if (arrive_last(&P.st->ticket[0], nb)) {
-        double s[2];
-        reduce_partials<2>(P.partials, P.ld, nb, s);
-        if (threadIdx.x == 0) {
-            bicg_start(P.st, s[0], s[1], sa);
-            P.st->ticket[0] = 0;
-        }
+    stencil_tile<T, 2>(pol, A, g.n, g.S, acc);
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &P.st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        bicg_start(P.st, s[0], s[1], sa);
+        P.st->ticket[0] = 0;
     }
 }
 
 // pass A: p = r + beta (p_old - omega v_old); v = A p^; partial (r~, v)
-template <typename T, bool PRE>
+template <typename T, bool PRE, bool COH = false>
 struct PolA {
-    const T* r;
-    const T* p_old;
-    const T* v_old;
-    T* p_new;
-    const T* invM;
-    const T* rt;
-    T* v;
+    static constexpr bool kAux = false;
+    const T* __restrict__ r;
+    const T* __restrict__ p_old;
+    const T* __restrict__ v_old;
+    T* __restrict__ p_new;
+    const T* __restrict__ invM;
+    const T* __restrict__ rt;
+    T* __restrict__ v;
     T beta, omega;
     bool first;
-    struct Val {
-        T op;
-        __device__ static Val zero() { return {T(0)}; }
-    };
-    __device__ __forceinline__ T pval(long long k) const {
-        T rk = r[k];
+    __device__ __forceinline__ T pre(int k) const {
+        const T rk = ld<COH>(r + k);
         if (first) return rk;
-        T d = fmaT<T>(-omega, v_old[k], p_old[k]);
+        const T d = fmaT<T>(-omega, ld<COH>(v_old + k), ld<COH>(p_old + k));
         return fmaT<T>(beta, d, rk);
     }
-    __device__ Val owner(long long k) const {
-        T p = pval(k);
-        p_new[k] = p;
-        return {PRE ? p * invM[k] : p};
-    }
-    __device__ T halo(long long k) const {
-        T p = pval(k);
-        return PRE ? p * invM[k] : p;
-    }
-    __device__ void sink(long long k, T y, const Val&, double (&acc)[1]) const {
+    __device__ __forceinline__ T scale(int k, T p) const { return PRE ? p * __ldg(invM + k) : p; }
+    __device__ __forceinline__ void own(int k, T p) const { p_new[k] = p; }
+    __device__ __forceinline__ void sink(int k, T y, T, Acc<T> (&acc)[1]) const {
         v[k] = y;
-        acc[0] += (double)rt[k] * (double)y;
+        acc[0].add(__ldg(rt + k), y);
     }
 };
 
@@ -403,61 +573,41 @@ __global__ void __launch_bounds__(kThreads) k_bicg_A(Coef<T> A, Geo g, BicgVecs 
     const int cur = (int)(it & 1), nxt = cur ^ 1;
     PolA<T, PRE> pol;
     pol.r = (const T*)V.r;
-    pol.p_old = (const T*)V.p[cur];
-    pol.v_old = (const T*)V.v[cur];
-    pol.p_new = (T*)V.p[nxt];
+    pol.p_old = (const T*)(cur ? V.p[1] : V.p[0]);
+    pol.v_old = (const T*)(cur ? V.v[1] : V.v[0]);
+    pol.p_new = (T*)(nxt ? V.p[1] : V.p[0]);
     pol.invM = (const T*)V.invM;
     pol.rt = (const T*)V.rt;
-    pol.v = (T*)V.v[nxt];
-    pol.beta = (T)__ldcg(&st->beta);
-    pol.omega = (T)__ldcg(&st->omega);
+    pol.v = (T*)(nxt ? V.v[1] : V.v[0]);
+    pol.beta = Scal<T>::beta(st);
+    pol.omega = Scal<T>::omega(st);
     pol.first = it == 0;
-    double acc[1] = {0.0};
-    stencil_strip<T, 1>(pol, A, g.n, g.S, acc);
-    block_sum<1>(acc);
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x == 0) P.partials[bid] = acc[0];
-    if (arrive_last(&st->ticket[0], nb)) {
-        double s[1];
-        reduce_partials<1>(P.partials, P.ld, nb, s);
-        if (threadIdx.x == 0) {
-            double alpha = st->rho / s[0];
-            st->alpha = alpha;
-            if (!isfinite(alpha)) {
-                st->status = KC_NONFINITE;
-                st->done = 1;
-            }
-            st->ticket[0] = 0;
-        }
+    Acc<T> acc[1];
+    stencil_tile<T, 1>(pol, A, g.n, g.S, acc);
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        set_alpha(st, st->rho / s[0]);
+        st->ticket[0] = 0;
     }
 }
 
 // pass B: s = r - alpha v; t = A s^; partials (t, s), (t, t)
-template <typename T, bool PRE>
+template <typename T, bool PRE, bool COH = false>
 struct PolB {
-    const T* r;
-    const T* v;
-    const T* invM;
-    T* t;
+    static constexpr bool kAux = true;
+    const T* __restrict__ r;
+    const T* __restrict__ v;
+    const T* __restrict__ invM;
+    T* __restrict__ t;
     T alpha;
-    struct Val {
-        T op, s;
-        __device__ static Val zero() { return {T(0), T(0)}; }
-    };
-    __device__ __forceinline__ T sval(long long k) const { return fmaT<T>(-alpha, v[k], r[k]); }
-    __device__ Val owner(long long k) const {
-        T s = sval(k);
-        return {PRE ? s * invM[k] : s, s};
-    }
-    __device__ T halo(long long k) const {
-        T s = sval(k);
-        return PRE ? s * invM[k] : s;
-    }
-    __device__ void sink(long long k, T y, const Val& c, double (&acc)[2]) const {
+    __device__ __forceinline__ T pre(int k) const { return fmaT<T>(-alpha, ld<COH>(v + k), ld<COH>(r + k)); }
+    __device__ __forceinline__ T scale(int k, T s) const { return PRE ? s * __ldg(invM + k) : s; }
+    __device__ __forceinline__ void own(int, T) const {}
+    __device__ __forceinline__ void sink(int k, T y, T s, Acc<T> (&acc)[2]) const {
         t[k] = y;
-        acc[0] += (double)y * (double)c.s;
-        acc[1] += (double)y * (double)y;
+        acc[0].add(y, s);
+        acc[1].add(y, y);
     }
 };
 
@@ -469,77 +619,54 @@ __global__ void __launch_bounds__(kThreads) k_bicg_B(Coef<T> A, Geo g, BicgVecs 
     const int nxt = (int)((it + 1) & 1);
     PolB<T, PRE> pol;
     pol.r = (const T*)V.r;
-    pol.v = (const T*)V.v[nxt];
+    pol.v = (const T*)(nxt ? V.v[1] : V.v[0]);
     pol.invM = (const T*)V.invM;
     pol.t = (T*)V.t;
-    pol.alpha = (T)__ldcg(&st->alpha);
-    double acc[2] = {0.0, 0.0};
-    stencil_strip<T, 2>(pol, A, g.n, g.S, acc);
-    block_sum<2>(acc);
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x == 0) {
-        P.partials[bid] = acc[0];
-        P.partials[P.ld + bid] = acc[1];
-    }
-    if (arrive_last(&st->ticket[0], nb)) {
-        double s[2];
-        reduce_partials<2>(P.partials, P.ld, nb, s);
-        if (threadIdx.x == 0) {
-            double omega = s[0] / s[1];
-            st->omega = omega;
-            if (!isfinite(omega)) {
-                st->status = KC_NONFINITE;
-                st->done = 1;
-            }
-            st->ticket[0] = 0;
-        }
+    pol.alpha = Scal<T>::alpha(st);
+    Acc<T> acc[2];
+    stencil_tile<T, 2>(pol, A, g.n, g.S, acc);
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        set_omega(st, s[0] / s[1]);
+        st->ticket[0] = 0;
     }
 }
 
 // pass C: x += alpha p^ + omega s^; r = s - omega t; partials (r, r~), (r, r)
 template <typename T, bool PRE>
-__global__ void __launch_bounds__(kPwThreads) k_bicg_C(long long n, T* x, BicgVecs V, BicgPtrs P) {
+__global__ void __launch_bounds__(kPwThreads) k_bicg_C(int n, T* __restrict__ x, BicgVecs V, BicgPtrs P) {
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     const int nxt = (int)((it + 1) & 1);
-    const T* p = (const T*)V.p[nxt];
-    const T* v = (const T*)V.v[nxt];
-    const T* t = (const T*)V.t;
-    const T* rt = (const T*)V.rt;
-    const T* invM = (const T*)V.invM;
-    T* r = (T*)V.r;
-    const T alpha = (T)__ldcg(&st->alpha), omega = (T)__ldcg(&st->omega);
-    double acc[2] = {0.0, 0.0};
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x) {
-        T rk = r[k];
-        T s = fmaT<T>(-alpha, v[k], rk);
-        T ph = p[k], sh = s;
+    const T* __restrict__ p = (const T*)(nxt ? V.p[1] : V.p[0]);
+    const T* __restrict__ v = (const T*)(nxt ? V.v[1] : V.v[0]);
+    const T* __restrict__ t = (const T*)V.t;
+    const T* __restrict__ rt = (const T*)V.rt;
+    const T* __restrict__ invM = (const T*)V.invM;
+    T* __restrict__ r = (T*)V.r;
+    const T alpha = Scal<T>::alpha(st), omega = Scal<T>::omega(st);
+    Acc<T> acc[2];
+    KC_PW_LOOP(n, {
+        const T rk = r[k];
+        const T s = fmaT<T>(-alpha, __ldg(v + k), rk);
+        T ph = __ldg(p + k), sh = s;
         if (PRE) {
-            T im = invM[k];
+            const T im = __ldg(invM + k);
             ph = ph * im;
             sh = sh * im;
         }
         x[k] = x[k] + fmaT<T>(alpha, ph, omega * sh);
-        T rn = fmaT<T>(-omega, t[k], s);
+        const T rn = fmaT<T>(-omega, __ldg(t + k), s);
         r[k] = rn;
-        acc[0] += (double)rn * (double)rt[k];
-        acc[1] += (double)rn * (double)rn;
-    }
-    block_sum<2>(acc);
-    if (threadIdx.x == 0) {
-        P.partials[blockIdx.x] = acc[0];
-        P.partials[P.ld + blockIdx.x] = acc[1];
-    }
-    if (arrive_last(&st->ticket[0], gridDim.x)) {
-        double s[2];
-        reduce_partials<2>(P.partials, P.ld, gridDim.x, s);
-        if (threadIdx.x == 0) {
-            bicg_finish_iteration(st, s[0], s[1]);
-            st->ticket[0] = 0;
-        }
+        acc[0].add(rn, __ldg(rt + k));
+        acc[1].add(rn, rn);
+    })
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
+        bicg_finish_iteration(st, s[0], s[1]);
+        st->ticket[0] = 0;
     }
 }
 
@@ -550,51 +677,38 @@ __global__ void __launch_bounds__(kPwThreads) k_bicg_C(long long n, T* x, BicgVe
 // =============================================================================
 template <typename T>
 __global__ void __launch_bounds__(kPwThreads)
-    k_cg_init(long long n, const T* b, T* x, T* r, BicgPtrs P, StartArgs sa) {
-    double acc[1] = {0.0};
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x) {
-        T bk = b[k];
+    k_cg_init(int n, const T* __restrict__ b, T* __restrict__ x, T* __restrict__ r, BicgPtrs P, StartArgs sa) {
+    Acc<T> acc[1];
+    KC_PW_LOOP(n, {
+        const T bk = __ldg(b + k);
         r[k] = bk;
         x[k] = T(0);
-        acc[0] += (double)bk * (double)bk;
-    }
-    block_sum<1>(acc);
-    if (threadIdx.x == 0) P.partials[blockIdx.x] = acc[0];
-    if (arrive_last(&P.st->ticket[0], gridDim.x)) {
-        double s[1];
-        reduce_partials<1>(P.partials, P.ld, gridDim.x, s);
-        if (threadIdx.x == 0) {
-            bicg_start(P.st, s[0], s[0], sa);
-            P.st->ticket[0] = 0;
-        }
+        acc[0].add(bk, bk);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
+        bicg_start(P.st, s[0], s[0], sa);
+        P.st->ticket[0] = 0;
     }
 }
 
-template <typename T>
+template <typename T, bool COH = false>
 struct PolCg1 {
-    const T* r;
-    const T* p_old;
-    T* p_new;
-    T* Ap;
+    static constexpr bool kAux = true;
+    const T* __restrict__ r;
+    const T* __restrict__ p_old;
+    T* __restrict__ p_new;
+    T* __restrict__ Ap;
     T beta;
     bool first;
-    struct Val {
-        T op;
-        __device__ static Val zero() { return {T(0)}; }
-    };
-    __device__ __forceinline__ T pval(long long k) const {
-        return first ? r[k] : fmaT<T>(beta, p_old[k], r[k]);
+    __device__ __forceinline__ T pre(int k) const {
+        return first ? ld<COH>(r + k) : fmaT<T>(beta, ld<COH>(p_old + k), ld<COH>(r + k));
     }
-    __device__ Val owner(long long k) const {
-        T p = pval(k);
-        p_new[k] = p;
-        return {p};
-    }
-    __device__ T halo(long long k) const { return pval(k); }
-    __device__ void sink(long long k, T y, const Val& c, double (&acc)[1]) const {
+    __device__ __forceinline__ T scale(int, T p) const { return p; }
+    __device__ __forceinline__ void own(int k, T p) const { p_new[k] = p; }
+    __device__ __forceinline__ void sink(int k, T y, T p, Acc<T> (&acc)[1]) const {
         Ap[k] = y;
-        acc[0] += (double)c.op * (double)y;
+        acc[0].add(p, y);
     }
 };
 
@@ -606,76 +720,66 @@ __global__ void __launch_bounds__(kThreads) k_cg_1(Coef<T> A, Geo g, BicgVecs V,
     const int cur = (int)(it & 1), nxt = cur ^ 1;
     PolCg1<T> pol;
     pol.r = (const T*)V.r;
-    pol.p_old = (const T*)V.p[cur];
-    pol.p_new = (T*)V.p[nxt];
+    pol.p_old = (const T*)(cur ? V.p[1] : V.p[0]);
+    pol.p_new = (T*)(nxt ? V.p[1] : V.p[0]);
     pol.Ap = (T*)V.v[0];
-    pol.beta = (T)__ldcg(&st->beta);
+    pol.beta = Scal<T>::beta(st);
     pol.first = it == 0;
-    double acc[1] = {0.0};
-    stencil_strip<T, 1>(pol, A, g.n, g.S, acc);
-    block_sum<1>(acc);
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x == 0) P.partials[bid] = acc[0];
-    if (arrive_last(&st->ticket[0], nb)) {
-        double s[1];
-        reduce_partials<1>(P.partials, P.ld, nb, s);
-        if (threadIdx.x == 0) {
-            double alpha = st->old / s[0];
-            st->alpha = alpha;
-            if (!isfinite(alpha)) {
-                st->status = KC_NONFINITE;
-                st->done = 1;
-            }
-            st->ticket[0] = 0;
+    Acc<T> acc[1];
+    stencil_tile<T, 1>(pol, A, g.n, g.S, acc);
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        const double alpha = st->old / s[0];
+        st->alpha = alpha;
+        st->alpha_f = (float)alpha;
+        if (!isfinite(alpha)) {
+            st->status = KC_NONFINITE;
+            st->done = 1;
         }
+        st->ticket[0] = 0;
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPwThreads) k_cg_2(long long n, T* x, BicgVecs V, BicgPtrs P) {
+__global__ void __launch_bounds__(kPwThreads) k_cg_2(int n, T* __restrict__ x, BicgVecs V, BicgPtrs P) {
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     const int nxt = (int)((it + 1) & 1);
-    const T* p = (const T*)V.p[nxt];
-    const T* Ap = (const T*)V.v[0];
-    T* r = (T*)V.r;
-    const T alpha = (T)__ldcg(&st->alpha);
-    double acc[1] = {0.0};
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x) {
-        x[k] = fmaT<T>(alpha, p[k], x[k]);
-        T rn = fmaT<T>(-alpha, Ap[k], r[k]);
+    const T* __restrict__ p = (const T*)(nxt ? V.p[1] : V.p[0]);
+    const T* __restrict__ Ap = (const T*)V.v[0];
+    T* __restrict__ r = (T*)V.r;
+    const T alpha = Scal<T>::alpha(st);
+    Acc<T> acc[1];
+    KC_PW_LOOP(n, {
+        x[k] = fmaT<T>(alpha, __ldg(p + k), x[k]);
+        const T rn = fmaT<T>(-alpha, __ldg(Ap + k), r[k]);
         r[k] = rn;
-        acc[0] += (double)rn * (double)rn;
-    }
-    block_sum<1>(acc);
-    if (threadIdx.x == 0) P.partials[blockIdx.x] = acc[0];
-    if (arrive_last(&st->ticket[0], gridDim.x)) {
-        double s[1];
-        reduce_partials<1>(P.partials, P.ld, gridDim.x, s);
-        if (threadIdx.x == 0) {
-            double nw = s[0];
-            st->iter += 1;
-            st->rTr = nw;
-            record_history(st, st->iter, nw);
-            st->prev_rel = st->r0Tr > 0 ? sqrt(nw) / sqrt(st->r0Tr) : 0.0;
-            if (sqrt(nw) < sqrt(st->r0Tr) * st->eps) {
-                st->status = KC_OK;
-                st->done = 1;
-            } else if (!isfinite(nw)) {
-                st->status = KC_NONFINITE;
-                st->done = 1;
-            } else if (st->iter >= st->max_iter) {
-                st->status = KC_MAXITER;
-                st->done = 1;
-            } else {
-                st->beta = nw / st->old;
-                st->old = nw;
-            }
-            st->ticket[0] = 0;
+        acc[0].add(rn, rn);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
+        const double nw = s[0];
+        st->iter += 1;
+        st->rTr = nw;
+        record_history(st, st->iter, nw);
+        st->prev_rel = st->r0Tr > 0 ? sqrt(nw) / sqrt(st->r0Tr) : 0.0;
+        if (sqrt(nw) < sqrt(st->r0Tr) * st->eps) {
+            st->status = KC_OK;
+            st->done = 1;
+        } else if (!isfinite(nw)) {
+            st->status = KC_NONFINITE;
+            st->done = 1;
+        } else if (st->iter >= st->max_iter) {
+            st->status = KC_MAXITER;
+            st->done = 1;
+        } else {
+            st->beta = nw / st->old;
+            st->beta_f = (float)st->beta;
+            st->old = nw;
         }
+        st->ticket[0] = 0;
     }
 }
 
@@ -683,58 +787,465 @@ __global__ void __launch_bounds__(kPwThreads) k_cg_2(long long n, T* x, BicgVecs
 // Mixed precision refinement helpers
 // =============================================================================
 struct PolResid {
-    const double* x;
-    const double* b;
-    float* r32;
-    struct Val {
-        double op;
-        __device__ static Val zero() { return {0.0}; }
-    };
-    __device__ Val owner(long long k) const { return {x[k]}; }
-    __device__ double halo(long long k) const { return x[k]; }
-    __device__ void sink(long long k, double y, const Val&, double (&acc)[2]) const {
-        double bk = b[k];
-        double rk = bk - y;
+    static constexpr bool kAux = false;
+    const double* __restrict__ x;
+    const double* __restrict__ b;
+    float* __restrict__ r32;
+    __device__ __forceinline__ double pre(int k) const { return __ldg(x + k); }
+    __device__ __forceinline__ double scale(int, double p) const { return p; }
+    __device__ __forceinline__ void own(int, double) const {}
+    __device__ __forceinline__ void sink(int k, double y, double, Acc<double> (&acc)[2]) const {
+        const double bk = __ldg(b + k);
+        const double rk = bk - y;
         r32[k] = (float)rk;
-        acc[0] += rk * rk;
-        acc[1] += bk * bk;
+        acc[0].add(rk, rk);
+        acc[1].add(bk, bk);
     }
 };
 
 __global__ void __launch_bounds__(kThreads)
-    k_refine_resid(Coef<double> A, Geo g, const double* b, const double* x, float* r32, BicgPtrs P,
-                   double* out2) {
-    double acc[2] = {0.0, 0.0};
+    k_refine_resid(Coef<double> A, Geo g, const double* __restrict__ b, const double* __restrict__ x,
+                   float* __restrict__ r32, BicgPtrs P, double* out2) {
+    Acc<double> acc[2];
     PolResid pol{x, b, r32};
-    stencil_strip<double, 2>(pol, A, g.n, g.S, acc);
-    block_sum<2>(acc);
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (threadIdx.x == 0) {
-        P.partials[bid] = acc[0];
-        P.partials[P.ld + bid] = acc[1];
+    stencil_tile<double, 2>(pol, A, g.n, g.S, acc);
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &P.st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        out2[0] = s[0];
+        out2[1] = s[1];
+        P.st->ticket[0] = 0;
     }
-    if (arrive_last(&P.st->ticket[0], nb)) {
-        double s[2];
-        reduce_partials<2>(P.partials, P.ld, nb, s);
-        if (threadIdx.x == 0) {
-            out2[0] = s[0];
-            out2[1] = s[1];
-            P.st->ticket[0] = 0;
+}
+
+// x += d, applied only when every entry of d is finite (flag[0] == 0; set by
+// k_flag_nonfinite), so a correction from a broken-down FP32 sweep is dropped.
+__global__ void __launch_bounds__(kPwThreads)
+    k_flag_nonfinite(int n, const float* __restrict__ d, int* __restrict__ flag) {
+    int bad = 0;
+    KC_PW_LOOP(n, { bad |= !isfinite(__ldg(d + k)); })
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+__global__ void __launch_bounds__(kPwThreads)
+    k_add_f32_to_f64(int n, const float* __restrict__ d, double* __restrict__ x, const int* __restrict__ flag) {
+    if (__ldcg(flag)) return;
+    KC_PW_LOOP(n, { x[k] += (double)__ldg(d + k); })
+}
+
+__global__ void k_zero_f64(int n, double* __restrict__ x) {
+    KC_PW_LOOP(n, { x[k] = 0.0; })
+}
+
+// =============================================================================
+// Persistent cooperative solvers: one launch runs the whole solve.
+//
+// Every block owns a fixed set of tiles for all passes of all iterations.
+// After each pass the blocks meet at a grid barrier and every block sums the
+// per-block partials itself (same data, same order -> identical scalars in
+// every block), so no launch gap and no single-block tail sits between the
+// passes.  The barrier spin is bounded: on timeout the block raises an error
+// flag, every block leaves its loop, and the host reports KC_ERR_CUDA.
+// Vectors written during the launch are read with ld.global.cg (L1 bypass).
+// =============================================================================
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    int err;
+    int pad;
+};
+constexpr unsigned kSpinLimit = 1u << 22;   // ~0.5 s at 40 ns per poll: far beyond any healthy wait
+
+__device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &bar->gen;
+        volatile int* err = &bar->err;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&bar->count, 1u) == nb - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*gen == g) {
+                if (*err) break;
+                if (++spins > kSpinLimit) {
+                    atomicExch(&bar->err, 1);
+                    break;
+                }
+                __nanosleep(40);
+            }
+        }
+        __threadfence();
+        ok = *err == 0;
+    }
+    __syncthreads();
+    return ok;
+}
+
+// Block partial of NV accumulators -> partials[(slot+q)*ld + bid] (no ticket).
+template <typename T, int NV>
+__device__ __forceinline__ void store_block_partials(const Acc<T> (&a)[NV], double* partials, int ld, int slot,
+                                                     int bid);
+template <>
+__device__ __forceinline__ void store_block_partials<double, 1>(const Acc<double> (&a)[1], double* partials, int ld,
+                                                               int slot, int bid) {
+    double d[1] = {a[0].s};
+    block_sum<1>(d);
+    if (threadIdx.x == 0) partials[slot * ld + bid] = d[0];
+}
+template <>
+__device__ __forceinline__ void store_block_partials<double, 2>(const Acc<double> (&a)[2], double* partials, int ld,
+                                                               int slot, int bid) {
+    double d[2] = {a[0].s, a[1].s};
+    block_sum<2>(d);
+    if (threadIdx.x == 0) {
+        partials[slot * ld + bid] = d[0];
+        partials[(slot + 1) * ld + bid] = d[1];
+    }
+}
+template <int NV>
+__device__ __forceinline__ void store_block_partials_f(const Acc<float> (&a)[NV], double* partials, int ld, int slot,
+                                                       int bid) {
+    __shared__ DF sh[NV][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        DF v = a[q].s;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = df_add(v, DF{__shfl_down_sync(kFull, v.hi, o), __shfl_down_sync(kFull, v.lo, o)});
+        if (lane == 0) sh[q][w] = v;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            DF v = lane < nw ? sh[q][lane] : DF{0.f, 0.f};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v = df_add(v, DF{__shfl_down_sync(kFull, v.hi, o), __shfl_down_sync(kFull, v.lo, o)});
+            if (lane == 0) partials[(slot + q) * ld + bid] = (double)v.hi + (double)v.lo;
         }
     }
+    __syncthreads();
+}
+template <>
+__device__ __forceinline__ void store_block_partials<float, 1>(const Acc<float> (&a)[1], double* partials, int ld,
+                                                              int slot, int bid) {
+    store_block_partials_f<1>(a, partials, ld, slot, bid);
+}
+template <>
+__device__ __forceinline__ void store_block_partials<float, 2>(const Acc<float> (&a)[2], double* partials, int ld,
+                                                              int slot, int bid) {
+    store_block_partials_f<2>(a, partials, ld, slot, bid);
 }
 
-__global__ void __launch_bounds__(kPwThreads) k_add_f32_to_f64(long long n, const float* d, double* x) {
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x)
-        x[k] += (double)d[k];
+// Fixed-order sum of NV partial vectors starting at slot; result in thread 0.
+template <int NV>
+__device__ __forceinline__ void sum_partials(const double* partials, int ld, int slot, int nb, double (&out)[NV]) {
+    reduce_partials<NV>(partials + slot * ld, ld, nb, out);
 }
 
-__global__ void k_zero_f64(long long n, double* x) {
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
-         k += (long long)gridDim.x * blockDim.x)
-        x[k] = 0.0;
+// Visits the cells of tile (i0, j0) owned by this thread: rows ty + 8r.
+template <class F>
+__device__ __forceinline__ void for_tile_cells(int n, int S, int i0, int j0, F&& f) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int j = j0 + tx;
+#pragma unroll
+    for (int r = 0; r < kCPT; ++r) {
+        const long long kl = (long long)(i0 + ty + 8 * r) * S + j;
+        if (j < S && kl < n) f((int)kl);
+    }
+}
+
+struct PersistGeo {
+    int tiles_x, ntiles;
+};
+
+template <typename T, bool PRE>
+__global__ void __launch_bounds__(kThreads)
+    k_bicg_persist(Coef<T> A, Geo g, T* __restrict__ x, BicgVecs V, BicgPtrs P, GridBar* bar, PersistGeo pg) {
+    SolverState* st = P.st;
+    const int G = gridDim.x, bid = blockIdx.x;
+    __shared__ double sc[8];      // rho, rho_1, alpha, omega, beta, den, eps, lim
+    __shared__ long long siter, smax;
+    __shared__ int sdone, sstatus, sobreak;
+    __shared__ double q0, q1;     // scratch for parallel divisions
+    if (threadIdx.x == 0) {
+        sc[0] = st->rho; sc[1] = st->rho_1; sc[2] = st->alpha; sc[3] = st->omega; sc[4] = st->beta;
+        sc[5] = st->den; sc[6] = st->eps; sc[7] = st->lim;
+        siter = st->iter; smax = st->max_iter;
+        sdone = st->done; sstatus = st->status; sobreak = st->omega_break;
+    }
+    __syncthreads();
+    const T* __restrict__ rt = (const T*)V.rt;
+    const T* __restrict__ invM = (const T*)V.invM;
+    T* __restrict__ r = (T*)V.r;
+    T* __restrict__ t = (T*)V.t;
+    double rTr = st->rTr;
+    while (!sdone) {
+        const long long it = siter;
+        const int cur = (int)(it & 1), nxt = cur ^ 1;
+        T* p_new = (T*)(nxt ? V.p[1] : V.p[0]);
+        T* v_new = (T*)(nxt ? V.v[1] : V.v[0]);
+        // ---- pass A: p = r + beta (p - omega v); v = A p^; (r~, v)
+        {
+            PolA<T, PRE, true> pol;
+            pol.r = r;
+            pol.p_old = (const T*)(cur ? V.p[1] : V.p[0]);
+            pol.v_old = (const T*)(cur ? V.v[1] : V.v[0]);
+            pol.p_new = p_new;
+            pol.invM = invM;
+            pol.rt = rt;
+            pol.v = v_new;
+            pol.beta = (T)sc[4];
+            pol.omega = (T)sc[3];
+            pol.first = it == 0;
+            Acc<T> acc[1];
+            for (int tile = bid; tile < pg.ntiles; tile += G) {
+                stencil_tile_at<T, 1>(pol, A, g.n, g.S, (tile / pg.tiles_x) * kTI, (tile % pg.tiles_x) * kTJ, acc);
+                __syncthreads();
+            }
+            store_block_partials<T, 1>(acc, P.partials, P.ld, 0, bid);
+        }
+        if (!grid_sync(bar, G)) return;
+        {
+            double s1[1];
+            sum_partials<1>(P.partials, P.ld, 0, G, s1);
+            if (threadIdx.x == 0) {
+                const double alpha = sc[0] / s1[0];
+                sc[2] = alpha;
+                if (!isfinite(alpha) || fabs(alpha) > sc[7]) {
+                    sdone = 1;
+                    sstatus = KC_NONFINITE;
+                }
+            }
+            __syncthreads();
+            if (sdone) break;
+        }
+        // ---- pass B: s = r - alpha v; t = A s^; (t, s), (t, t)
+        {
+            PolB<T, PRE, true> pol;
+            pol.r = r;
+            pol.v = v_new;
+            pol.invM = invM;
+            pol.t = t;
+            pol.alpha = (T)sc[2];
+            Acc<T> acc[2];
+            for (int tile = bid; tile < pg.ntiles; tile += G) {
+                stencil_tile_at<T, 2>(pol, A, g.n, g.S, (tile / pg.tiles_x) * kTI, (tile % pg.tiles_x) * kTJ, acc);
+                __syncthreads();
+            }
+            store_block_partials<T, 2>(acc, P.partials, P.ld, 1, bid);
+        }
+        if (!grid_sync(bar, G)) return;
+        {
+            double s2[2];
+            sum_partials<2>(P.partials, P.ld, 1, G, s2);
+            if (threadIdx.x == 0) {
+                const double omega = s2[0] / s2[1];
+                sc[3] = omega;
+                if (!isfinite(omega) || fabs(omega) > sc[7]) {
+                    sdone = 1;
+                    sstatus = KC_NONFINITE;
+                }
+            }
+            __syncthreads();
+            if (sdone) break;
+        }
+        // ---- pass C: x += alpha p^ + omega s^; r = s - omega t; (r, r~), (r, r)
+        {
+            const T alpha = (T)sc[2], omega = (T)sc[3];
+            Acc<T> acc[2];
+            for (int tile = bid; tile < pg.ntiles; tile += G) {
+                for_tile_cells(g.n, g.S, (tile / pg.tiles_x) * kTI, (tile % pg.tiles_x) * kTJ, [&](int k) {
+                    const T rk = __ldcg(r + k);
+                    const T s = fmaT<T>(-alpha, __ldcg(v_new + k), rk);
+                    T ph = __ldcg(p_new + k), sh = s;
+                    if (PRE) {
+                        const T im = __ldg(invM + k);
+                        ph = ph * im;
+                        sh = sh * im;
+                    }
+                    x[k] = __ldcg(x + k) + fmaT<T>(alpha, ph, omega * sh);
+                    const T rn = fmaT<T>(-omega, __ldcg(t + k), s);
+                    r[k] = rn;
+                    acc[0].add(rn, __ldg(rt + k));
+                    acc[1].add(rn, rn);
+                });
+            }
+            store_block_partials<T, 2>(acc, P.partials, P.ld, 3, bid);
+        }
+        if (!grid_sync(bar, G)) return;
+        {
+            double s3[2];
+            sum_partials<2>(P.partials, P.ld, 3, G, s3);
+            if (threadIdx.x == 0) {
+                const double rho_new = s3[0];
+                rTr = s3[1];
+                siter = it + 1;
+                q0 = rho_new;
+                q1 = rTr;
+            }
+            __syncthreads();
+            // beta = (rho_new / rho) * (alpha / omega): the two divisions run in two warps
+            if (threadIdx.x == 0) q0 = q0 / sc[0];
+            if (threadIdx.x == 32) sc[4] = sc[2] / sc[3];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const double rr = q1;
+                const double den = sc[5], eps = sc[6];
+                const long long itn = siter;
+                if (rr < eps * eps * den) {
+                    sdone = 1;
+                    sstatus = KC_OK;
+                } else if (!isfinite(rr)) {
+                    sdone = 1;
+                    sstatus = KC_NONFINITE;
+                } else if (sobreak && sc[3] == 0.0) {
+                    sdone = 1;
+                    sstatus = KC_BREAKDOWN_OMEGA;
+                } else if (itn >= smax) {
+                    sdone = 1;
+                    sstatus = KC_MAXITER;
+                } else if (s3[0] == 0.0) {
+                    sdone = 1;
+                    sstatus = KC_BREAKDOWN_RHO;
+                } else {
+                    const double beta = q0 * sc[4];
+                    sc[1] = sc[0];
+                    sc[0] = s3[0];
+                    sc[4] = beta;
+                    if (!isfinite(beta) || fabs(beta) > sc[7]) {
+                        sdone = 1;
+                        sstatus = KC_NONFINITE;
+                    }
+                }
+                if (bid == 0 && st->hist && itn < st->hist_len) st->hist[itn] = rr;  // squared; rooted after the solve
+            }
+            __syncthreads();
+        }
+    }
+    if (bid == 0 && threadIdx.x == 0) {
+        st->rho = sc[0];
+        st->rho_1 = sc[1];
+        st->alpha = sc[2];
+        st->omega = sc[3];
+        st->beta = sc[4];
+        st->iter = siter;
+        st->rTr = rTr;
+        st->status = sstatus;
+        st->done = 1;
+        st->prev_rel = sc[5] > 0.0 ? sqrt(rTr / sc[5]) : 0.0;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_persist(Coef<T> A, Geo g, T* __restrict__ x, BicgVecs V, BicgPtrs P, GridBar* bar, PersistGeo pg) {
+    SolverState* st = P.st;
+    const int G = gridDim.x, bid = blockIdx.x;
+    __shared__ double sold, salpha, sbeta, sr0, seps;
+    __shared__ long long siter, smax;
+    __shared__ int sdone, sstatus;
+    if (threadIdx.x == 0) {
+        sold = st->old; salpha = st->alpha; sbeta = st->beta; sr0 = st->r0Tr; seps = st->eps;
+        siter = st->iter; smax = st->max_iter; sdone = st->done; sstatus = st->status;
+    }
+    __syncthreads();
+    T* __restrict__ r = (T*)V.r;
+    T* __restrict__ Ap = (T*)V.v[0];
+    double rTr = st->rTr;
+    while (!sdone) {
+        const long long it = siter;
+        const int cur = (int)(it & 1), nxt = cur ^ 1;
+        T* p_new = (T*)(nxt ? V.p[1] : V.p[0]);
+        {
+            PolCg1<T, true> pol;
+            pol.r = r;
+            pol.p_old = (const T*)(cur ? V.p[1] : V.p[0]);
+            pol.p_new = p_new;
+            pol.Ap = Ap;
+            pol.beta = (T)sbeta;
+            pol.first = it == 0;
+            Acc<T> acc[1];
+            for (int tile = bid; tile < pg.ntiles; tile += G) {
+                stencil_tile_at<T, 1>(pol, A, g.n, g.S, (tile / pg.tiles_x) * kTI, (tile % pg.tiles_x) * kTJ, acc);
+                __syncthreads();
+            }
+            store_block_partials<T, 1>(acc, P.partials, P.ld, 0, bid);
+        }
+        if (!grid_sync(bar, G)) return;
+        {
+            double s1[1];
+            sum_partials<1>(P.partials, P.ld, 0, G, s1);
+            if (threadIdx.x == 0) {
+                salpha = sold / s1[0];
+                if (!isfinite(salpha)) {
+                    sdone = 1;
+                    sstatus = KC_NONFINITE;
+                }
+            }
+            __syncthreads();
+            if (sdone) break;
+        }
+        {
+            const T alpha = (T)salpha;
+            Acc<T> acc[1];
+            for (int tile = bid; tile < pg.ntiles; tile += G) {
+                for_tile_cells(g.n, g.S, (tile / pg.tiles_x) * kTI, (tile % pg.tiles_x) * kTJ, [&](int k) {
+                    x[k] = fmaT<T>(alpha, __ldcg(p_new + k), __ldcg(x + k));
+                    const T rn = fmaT<T>(-alpha, __ldcg(Ap + k), __ldcg(r + k));
+                    r[k] = rn;
+                    acc[0].add(rn, rn);
+                });
+            }
+            store_block_partials<T, 1>(acc, P.partials, P.ld, 1, bid);
+        }
+        if (!grid_sync(bar, G)) return;
+        {
+            double s2[1];
+            sum_partials<1>(P.partials, P.ld, 1, G, s2);
+            if (threadIdx.x == 0) {
+                const double nw = s2[0];
+                rTr = nw;
+                siter = it + 1;
+                if (nw < seps * seps * sr0) {
+                    sdone = 1;
+                    sstatus = KC_OK;
+                } else if (!isfinite(nw)) {
+                    sdone = 1;
+                    sstatus = KC_NONFINITE;
+                } else if (siter >= smax) {
+                    sdone = 1;
+                    sstatus = KC_MAXITER;
+                } else {
+                    sbeta = nw / sold;
+                    sold = nw;
+                }
+                if (bid == 0 && st->hist && siter < st->hist_len) st->hist[siter] = nw;
+            }
+            __syncthreads();
+        }
+    }
+    if (bid == 0 && threadIdx.x == 0) {
+        st->old = sold;
+        st->alpha = salpha;
+        st->beta = sbeta;
+        st->iter = siter;
+        st->rTr = rTr;
+        st->status = sstatus;
+        st->done = 1;
+        st->prev_rel = sr0 > 0.0 ? sqrt(rTr) / sqrt(sr0) : 0.0;
+    }
+}
+
+// history[1..iters] hold squared norms after a persistent solve
+__global__ void k_hist_sqrt(double* h, long long from, long long to) {
+    for (long long k = from + blockIdx.x * blockDim.x + threadIdx.x; k < to; k += (long long)gridDim.x * blockDim.x)
+        h[k] = sqrt(h[k]);
 }
 
 // =============================================================================
@@ -743,7 +1254,7 @@ __global__ void k_zero_f64(long long n, double* x) {
 static inline size_t esize(int dtype) { return dtype == KC_F64 ? 8 : 4; }
 
 struct BicgLayout {
-    size_t off_state, off_partials, off_vec[8], total;
+    size_t off_state, off_bar, off_partials, off_vec[8], total;
     int ld;
 };
 
@@ -756,8 +1267,10 @@ static BicgLayout bicg_layout(long long n, int S, int dtype) {
     size_t off = 0;
     L.off_state = off;
     off = align256(off + sizeof(SolverState));
+    L.off_bar = off;
+    off = align256(off + sizeof(GridBar));
     L.off_partials = off;
-    off = align256(off + (size_t)4 * L.ld * sizeof(double));
+    off = align256(off + (size_t)5 * L.ld * sizeof(double));
     for (int q = 0; q < 8; ++q) {
         L.off_vec[q] = off;
         off = align256(off + (size_t)n * esize(dtype));
@@ -822,27 +1335,27 @@ static std::map<std::pair<int, GraphKey>, cudaGraphExec_t> g_graphs;
 template <typename T, bool PRE>
 static void launch_bicg_iters(const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, int m,
                               cudaStream_t s) {
-    Geo g{A->n, A->stride};
+    Geo g{(int)A->n, A->stride};
     dim3 sg = stencil_grid(A->n, A->stride);
     int pb = pw_blocks(A->n);
     Coef<T> C = coef_of<T>(A);
     for (int q = 0; q < m; ++q) {
         k_bicg_A<T, PRE><<<sg, kThreads, 0, s>>>(C, g, V, P);
         k_bicg_B<T, PRE><<<sg, kThreads, 0, s>>>(C, g, V, P);
-        k_bicg_C<T, PRE><<<pb, kPwThreads, 0, s>>>(A->n, x, V, P);
+        k_bicg_C<T, PRE><<<pb, kPwThreads, 0, s>>>((int)A->n, x, V, P);
     }
 }
 
 template <typename T>
 static void launch_cg_iters(const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, int m,
                             cudaStream_t s) {
-    Geo g{A->n, A->stride};
+    Geo g{(int)A->n, A->stride};
     dim3 sg = stencil_grid(A->n, A->stride);
     int pb = pw_blocks(A->n);
     Coef<T> C = coef_of<T>(A);
     for (int q = 0; q < m; ++q) {
         k_cg_1<T><<<sg, kThreads, 0, s>>>(C, g, V, P);
-        k_cg_2<T><<<pb, kPwThreads, 0, s>>>(A->n, x, V, P);
+        k_cg_2<T><<<pb, kPwThreads, 0, s>>>((int)A->n, x, V, P);
     }
 }
 
@@ -850,7 +1363,7 @@ static void launch_cg_iters(const kc_system* A, T* x, const BicgVecs& V, const B
 // device marks the solve done.  Launcher(m, stream) enqueues m iterations.
 template <class Launcher>
 static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState* st, Launcher&& launch,
-                 HostState* h, cudaStream_t s) {
+                 HostState* h, cudaStream_t s, int kernels_per_iter) {
     int rc = read_state(st, h, s);
     if (rc) return rc;
     long long launched = 0;
@@ -891,8 +1404,9 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
             KC_CUDA(cudaGraphLaunch(ex, s));
         } else {
             launch(m, s);
-            KC_LAUNCH_CHECK("solver iteration launch");
+            KC_LAUNCH_CHECK_NC("solver iteration launch");
         }
+        count_launches((long long)m * kernels_per_iter);
         launched += m;
         rc = read_state(st, h, s);
         if (rc) return rc;
@@ -905,6 +1419,81 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
 
 using namespace kc;
 
+template <typename T, class K>
+static int launch_persistent(K kernel, const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, GridBar* bar,
+                             cudaStream_t s) {
+    int dev = 0, sms = 0, per = 0, coop = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    KC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    KC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return set_error("device %d does not support cooperative launches", dev), KC_ERR_UNSUPPORTED;
+    KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0));
+    if (per < 1) return set_error("persistent solver kernel cannot be resident"), KC_ERR_UNSUPPORTED;
+    dim3 sg = stencil_grid(A->n, A->stride);
+    PersistGeo pg{(int)sg.x, (int)(sg.x * sg.y)};
+    int G = std::max(1, std::min(pg.ntiles, sms * per));
+    Coef<T> C = coef_of<T>(A);
+    Geo g{(int)A->n, A->stride};
+    BicgVecs Vc = V;
+    BicgPtrs Pc = P;
+    T* xx = x;
+    void* args[] = {&C, &g, &xx, &Vc, &Pc, &bar, &pg};
+    KC_CUDA(cudaMemsetAsync(bar, 0, sizeof(GridBar), s));
+    KC_CUDA(cudaLaunchCooperativeKernel((const void*)kernel, dim3(G), dim3(kThreads), args, 0, s));
+    count_launches(1);
+    return KC_OK;
+}
+
+template <typename T>
+static int run_solver(const kc_system* A, const void* b, void* x, const void* M, const kc_solve_opts* o, BicgPtrs P,
+                      BicgVecs V, GridBar* bar, bool is_cg, bool pre, const GraphKey& key, StartArgs sa,
+                      StartArgs sa_cg, HostState* h, cudaStream_t s) {
+    const int pb = pw_blocks(A->n);
+    Geo g{(int)A->n, A->stride};
+    dim3 sg = stencil_grid(A->n, A->stride);
+    if (is_cg) {
+        k_cg_init<T><<<pb, kPwThreads, 0, s>>>((int)A->n, (const T*)b, (T*)x, (T*)V.r, P, sa_cg);
+    } else if (o->x0 == KC_X0_WARM) {
+        if (pre) k_invdiag<T><<<pb, kPwThreads, 0, s>>>((int)A->n, (const T*)M, (T*)V.invM);
+        k_bicg_init_warm<T><<<sg, kThreads, 0, s>>>(coef_of<T>(A), g, (const T*)b, (const T*)x, (T*)V.r, (T*)V.rt, P,
+                                                    sa);
+    } else {
+        k_bicg_init_cold<T><<<pb, kPwThreads, 0, s>>>((int)A->n, (const T*)b, (T*)x, (T*)V.r, (T*)V.rt,
+                                                      pre ? (const T*)M : nullptr, (T*)V.invM, P, sa);
+    }
+    KC_LAUNCH_CHECK("solver init");
+    if (!o->persistent) {
+        if (is_cg)
+            return drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_cg_iters<T>(A, (T*)x, V, P, m, ss); }, h, s, 2);
+        if (pre)
+            return drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, true>(A, (T*)x, V, P, m, ss); },
+                         h, s, 3);
+        return drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, false>(A, (T*)x, V, P, m, ss); },
+                     h, s, 3);
+    }
+    int rc;
+    if (is_cg)
+        rc = launch_persistent<T>(k_cg_persist<T>, A, (T*)x, V, P, bar, s);
+    else if (pre)
+        rc = launch_persistent<T>(k_bicg_persist<T, true>, A, (T*)x, V, P, bar, s);
+    else
+        rc = launch_persistent<T>(k_bicg_persist<T, false>, A, (T*)x, V, P, bar, s);
+    if (rc) return rc;
+    rc = read_state(P.st, h, s);
+    if (rc) return rc;
+    GridBar hb;
+    KC_CUDA(cudaMemcpy(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost));
+    if (hb.err) return set_error("persistent solver: grid barrier timed out"), KC_ERR_CUDA;
+    if (o->history && o->history_len > 1) {
+        long long to = std::min<long long>(o->history_len, h->iter + 1);
+        if (to > 1) {
+            k_hist_sqrt<<<(unsigned)std::min<long long>((to + 255) / 256, 1024), 256, 0, s>>>(o->history, 1, to);
+            KC_LAUNCH_CHECK("k_hist_sqrt");
+        }
+    }
+    return KC_OK;
+}
+
 extern "C" {
 
 int kc_spmv(const kc_system* A, const void* x, void* y, void* stream) {
@@ -912,7 +1501,7 @@ int kc_spmv(const kc_system* A, const void* x, void* y, void* stream) {
     if (rc) return rc;
     if (!x || !y) return set_error("kc_spmv: null x or y"), KC_ERR_ARG;
     cudaStream_t s = as_stream(stream);
-    Geo g{A->n, A->stride};
+    Geo g{(int)A->n, A->stride};
     dim3 sg = stencil_grid(A->n, A->stride);
     if (A->dtype == KC_F64)
         k_spmv<double><<<sg, kThreads, 0, s>>>(coef_of<double>(A), g, (const double*)x, (double*)y);
@@ -970,53 +1559,20 @@ static int bicg_impl(const kc_system* A, const void* b, void* x, const void* M, 
                {base + L.off_vec[4], base + L.off_vec[5]}, base + L.off_vec[6], base + L.off_vec[7]};
     const bool pre = o->precond == KC_PRECOND_JACOBI;
     const int pb = pw_blocks(A->n);
-    Geo g{A->n, A->stride};
+    Geo g{(int)A->n, A->stride};
     dim3 sg = stencil_grid(A->n, A->stride);
     const long long max_iter = o->max_iter;
     GraphKey key{ws, A->coef, x, A->n, A->stride, A->dtype, pre ? 1 : 0, 16, is_cg ? 1 : 0, A->cs, A->es};
     HostState h{};
-    StartArgs sa{o->eps, max_iter, o->omega_break, o->rel_to, o->history, o->history ? o->history_len : 0};
-    StartArgs sa_cg{o->eps, max_iter, 0, KC_REL_R0, o->history, o->history ? o->history_len : 0};
+    const double lim = A->dtype == KC_F64 ? 1e300 : 1e30;
+    StartArgs sa{o->eps, max_iter, o->omega_break, o->rel_to, o->history, o->history ? o->history_len : 0, lim};
+    StartArgs sa_cg{o->eps, max_iter, 0, KC_REL_R0, o->history, o->history ? o->history_len : 0, lim};
     KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
-    if (A->dtype == KC_F64) {
-        using T = double;
-        if (is_cg) {
-            k_cg_init<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)b, (T*)x, (T*)V.r, P, sa_cg);
-        } else if (o->x0 == KC_X0_WARM) {
-            if (pre) k_invdiag<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)M, (T*)V.invM);
-            k_bicg_init_warm<T><<<sg, kThreads, 0, s>>>(coef_of<T>(A), g, (const T*)b, (const T*)x, (T*)V.r,
-                                                        (T*)V.rt, P, sa);
-        } else {
-            k_bicg_init_cold<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)b, (T*)x, (T*)V.r, (T*)V.rt,
-                                                          pre ? (const T*)M : nullptr, (T*)V.invM, P, sa);
-        }
-        KC_LAUNCH_CHECK("solver init");
-        if (is_cg)
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_cg_iters<T>(A, (T*)x, V, P, m, ss); }, &h, s);
-        else if (pre)
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, true>(A, (T*)x, V, P, m, ss); }, &h, s);
-        else
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, false>(A, (T*)x, V, P, m, ss); }, &h, s);
-    } else {
-        using T = float;
-        if (is_cg) {
-            k_cg_init<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)b, (T*)x, (T*)V.r, P, sa_cg);
-        } else if (o->x0 == KC_X0_WARM) {
-            if (pre) k_invdiag<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)M, (T*)V.invM);
-            k_bicg_init_warm<T><<<sg, kThreads, 0, s>>>(coef_of<T>(A), g, (const T*)b, (const T*)x, (T*)V.r,
-                                                        (T*)V.rt, P, sa);
-        } else {
-            k_bicg_init_cold<T><<<pb, kPwThreads, 0, s>>>(A->n, (const T*)b, (T*)x, (T*)V.r, (T*)V.rt,
-                                                          pre ? (const T*)M : nullptr, (T*)V.invM, P, sa);
-        }
-        KC_LAUNCH_CHECK("solver init");
-        if (is_cg)
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_cg_iters<T>(A, (T*)x, V, P, m, ss); }, &h, s);
-        else if (pre)
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, true>(A, (T*)x, V, P, m, ss); }, &h, s);
-        else
-            rc = drive(o, key, P.st, [&](int m, cudaStream_t ss) { launch_bicg_iters<T, false>(A, (T*)x, V, P, m, ss); }, &h, s);
-    }
+    GridBar* bar = (GridBar*)(base + L.off_bar);
+    if (A->dtype == KC_F64)
+        rc = run_solver<double>(A, b, x, M, o, P, V, bar, is_cg, pre, key, sa, sa_cg, &h, s);
+    else
+        rc = run_solver<float>(A, b, x, M, o, P, V, bar, is_cg, pre, key, sa, sa_cg, &h, s);
     if (rc) return rc;
     if (info) {
         info->status = h.status;
@@ -1091,11 +1647,11 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     float* r32 = (float*)(base + L.off_r32);
     float* d32 = (float*)(base + L.off_d32);
     const long long n = A64->n;
-    Geo g{n, A64->stride};
+    Geo g{(int)n, A64->stride};
     dim3 sg = stencil_grid(n, A64->stride);
     int pb = pw_blocks(n);
     KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
-    k_zero_f64<<<pb, kPwThreads, 0, s>>>(n, x);
+    k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);
     kc_solve_opts io = *o;
     io.eps = eps_inner;
     io.x0 = KC_X0_ZERO;
@@ -1103,9 +1659,10 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     io.rel_to = KC_REL_R0;
     io.history = nullptr;
     io.history_len = 0;
+    int* flag = (int*)(out2 + 2);
     long long total = 0;
-    int status = KC_MAXITER, sweeps = 0;
-    double rel = 1.0, bb = 0.0;
+    int status = KC_MAXITER, sweeps = 0, stalls = 0;
+    double rel = 1.0, bb = 0.0, best = INFINITY;
     for (int it = 0; it <= max_refine; ++it) {
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2);
         KC_LAUNCH_CHECK("k_refine_resid");
@@ -1122,6 +1679,16 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
             status = KC_NONFINITE;
             break;
         }
+        // a sweep that does not lower the true residual twice in a row: stalled
+        if (rel >= 0.9 * best) {
+            if (++stalls >= 2) {
+                status = KC_STALL;
+                break;
+            }
+        } else {
+            stalls = 0;
+        }
+        best = std::min(best, rel);
         if (it == max_refine || total >= o->max_iter) break;
         io.max_iter = o->max_iter - total;
         kc_solve_info ii{};
@@ -1129,10 +1696,15 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         if (r2 < 0) return r2;
         total += ii.iters;
         ++sweeps;
-        k_add_f32_to_f64<<<pb, kPwThreads, 0, s>>>(n, d32, x);
+        // An inner breakdown (NONFINITE / BREAKDOWN_*) is caught before x is
+        // touched in passes A and B; apply whatever finite correction the
+        // sweep produced and restart from the FP64 residual.
+        KC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+        k_flag_nonfinite<<<pb, kPwThreads, 0, s>>>((int)n, d32, flag);
+        k_add_f32_to_f64<<<pb, kPwThreads, 0, s>>>((int)n, d32, x, flag);
         KC_LAUNCH_CHECK("k_add_f32_to_f64");
-        if (r2 == KC_NONFINITE) {
-            status = KC_NONFINITE;
+        if (r2 != KC_OK && ii.iters == 0) {
+            status = r2;
             break;
         }
     }

@@ -149,10 +149,11 @@ def dot(p: torch.Tensor, q: torch.Tensor) -> float:
 
 
 def _opts(eps, max_iter, x0, precond, omega_break, rel_to, check_every=0, use_graph=True,
-          history=None):
+          history=None, persistent=True):
     o = L.KcSolveOpts()
     o.eps, o.max_iter, o.x0, o.precond = float(eps), int(max_iter), int(x0), int(precond)
     o.omega_break, o.rel_to, o.check_every, o.use_graph = int(omega_break), int(rel_to), int(check_every), int(use_graph)
+    o.persistent = int(persistent)
     if history is not None:
         o.history, o.history_len = history.data_ptr(), history.numel()
     else:
@@ -162,8 +163,11 @@ def _opts(eps, max_iter, x0, precond, omega_break, rel_to, check_every=0, use_gr
 
 def bicgstab(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None, warm=False,
              M: torch.Tensor | None = None, omega_break=False, rel_to_b=False, ws: Workspace | None = None,
-             history: torch.Tensor | None = None, check_every=0, use_graph=True) -> SolveInfo:
-    """BiCGSTAB on the device (bicgsolver.py:88-135; karman_taichi.py:342-456)."""
+             history: torch.Tensor | None = None, check_every=0, use_graph=True, persistent=True) -> SolveInfo:
+    """BiCGSTAB on the device (bicgsolver.py:88-135; karman_taichi.py:342-456).
+
+    ``persistent=True`` runs the whole solve as one cooperative launch;
+    otherwise each iteration is three launches (optionally graph-captured)."""
     require_cuda(b, x, M)
     if b.numel() != A.n or x.numel() != A.n:
         raise ValueError(f"b/x have {b.numel()}/{x.numel()} elements, operator has {A.n}")
@@ -174,7 +178,7 @@ def bicgstab(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter
     buf = (ws or Workspace(b.device)).get(nbytes)
     o = _opts(eps, A.n if max_iter is None else max_iter, L.X0_WARM if warm else L.X0_ZERO,
               L.PRECOND_JACOBI if M is not None else L.PRECOND_NONE, omega_break,
-              L.REL_B if rel_to_b else L.REL_R0, check_every, use_graph, history)
+              L.REL_B if rel_to_b else L.REL_R0, check_every, use_graph, history, persistent)
     info = L.KcSolveInfo()
     rc = lib.kc_bicgstab(C.byref(A.system), ptr(b), ptr(x), ptr(M), ptr(buf), buf.numel(), C.byref(o),
                          C.byref(info), stream_handle(b.device))
@@ -183,7 +187,7 @@ def bicgstab(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter
 
 
 def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None, ws: Workspace | None = None,
-       history: torch.Tensor | None = None, check_every=0, use_graph=True) -> SolveInfo:
+       history: torch.Tensor | None = None, check_every=0, use_graph=True, persistent=True) -> SolveInfo:
     """Conjugate gradients on the device (cgsolver.py:83-114)."""
     require_cuda(b, x)
     if b.numel() != A.n or x.numel() != A.n:
@@ -192,7 +196,7 @@ def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None,
     nbytes = lib.kc_cg_ws_bytes(A.n, A.stride, A.dtype)
     buf = (ws or Workspace(b.device)).get(nbytes)
     o = _opts(eps, A.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0,
-              check_every, use_graph, history)
+              check_every, use_graph, history, persistent)
     info = L.KcSolveInfo()
     rc = lib.kc_cg(C.byref(A.system), ptr(b), ptr(x), ptr(buf), buf.numel(), C.byref(o), C.byref(info),
                    stream_handle(b.device))
@@ -202,7 +206,7 @@ def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None,
 
 def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8,
                      eps_inner=1e-3, max_refine=30, max_iter=None, ws: Workspace | None = None,
-                     use_graph=True) -> SolveInfo:
+                     use_graph=True, persistent=True) -> SolveInfo:
     """FP64-residual iterative refinement around an FP32 BiCGSTAB with FP64
     inner products; stops when ||b - A64 x|| / ||b|| < eps."""
     require_cuda(b, x)
@@ -212,7 +216,7 @@ def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tenso
     nbytes = lib.kc_refined_ws_bytes(A64.n, A64.stride)
     buf = (ws or Workspace(b.device)).get(nbytes)
     o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0,
-              0, use_graph)
+              0, use_graph, None, persistent)
     info = L.KcSolveInfo()
     rc = lib.kc_bicgstab_refined(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x), ptr(buf),
                                  buf.numel(), C.byref(o), float(eps_inner), int(max_refine), C.byref(info),

@@ -123,10 +123,16 @@ def test_channel_steps_match_oracle(dev, precision):
 
 
 def test_channel_320x64_first_outer_iteration(dev):
-    """The 320 x 64 benchmark geometry: one outer iteration vs the oracle."""
+    """The 320 x 64 benchmark geometry: one outer iteration vs the oracle.
+
+    Two BiCGSTAB runs that each stop at a 1e-8 relative residual can differ
+    by up to cond(A) * 1e-8 in the solution (the p' system here has
+    cond ~ 1e5), so this comparison tightens the inner tolerance to 1e-12 to
+    make the 1e-6 field tolerance a statement about the kernels, not about
+    where two summation orders happened to stop."""
     from karman_taichi_gb300.channel import ChannelSolver
     from karman_taichi_gb300.config import PRESETS
-    cfg = PRESETS["channel_320x64"]
+    cfg = PRESETS["channel_320x64"].with_(eps=1e-12)
     g = ChannelSolver(cfg, device=dev)
     st = g.state_numpy()
     orc = O.ChannelOracle(_params(cfg), g.solid_np, st["u"], st["v"], st["p"])
@@ -136,7 +142,7 @@ def test_channel_320x64_first_outer_iteration(dev):
     st = g.state_numpy()
     for k in ("u", "v", "p"):
         assert _rel(st[k], getattr(orc, k)) <= 1e-6, k
-    assert abs(rg["it_p"] - ro["it_p"]) <= max(3, ro["it_p"] // 20)
+    assert rg["st"] == ro["st"] == (O.OK, O.OK, O.OK)
 
 
 def test_simple_cavity_matches_oracle(dev):

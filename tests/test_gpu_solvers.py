@@ -158,19 +158,60 @@ def test_jacobi_warm_start_matches_oracle(dev):
     assert np.abs(x.cpu().numpy() - ref.x).max() <= 1e-6 * np.abs(ref.x).max()
 
 
-def test_graph_and_direct_launch_agree_bitwise(dev):
+def test_launch_modes_deterministic_and_consistent(dev):
+    """Graph-captured and direct multi-launch iterations are bitwise equal;
+    the persistent cooperative solve repeats bitwise and agrees with them to
+    rounding (its per-block partial sums are grouped differently)."""
     from karman_taichi_gb300 import linalg
     N = 80
     c = _laplacian(N, 0.05)
     b = np.random.default_rng(7).standard_normal(N * N)
     A = linalg.Stencil(_t(c, dev), stride=N)
-    xs = []
-    for g in (True, False, True):
+    xs, its = {}, {}
+    for mode in ("graph", "direct", "persist", "persist2"):
         x = _t(np.zeros(N * N), dev)
-        info = linalg.bicgstab(A, _t(b, dev), x, eps=1e-9, use_graph=g)
+        info = linalg.bicgstab(A, _t(b, dev), x, eps=1e-9, use_graph=(mode == "graph"),
+                               persistent=mode.startswith("persist"))
         assert info.ok
-        xs.append(x.cpu().numpy())
-    assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[0], xs[2])
+        xs[mode], its[mode] = x.cpu().numpy(), info.iters
+    assert np.array_equal(xs["graph"], xs["direct"])
+    assert np.array_equal(xs["persist"], xs["persist2"])
+    assert abs(its["persist"] - its["graph"]) <= max(3, its["graph"] // 10)
+    assert np.abs(xs["persist"] - xs["graph"]).max() <= 1e-6 * np.abs(xs["graph"]).max()
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_bicgstab_modes_match_oracle(dev, persistent, dtype):
+    from karman_taichi_gb300 import linalg
+    n, S = 40000, 200
+    c = _rand_system(n, S, seed=21, diag_shift=0.3)
+    b = np.random.default_rng(22).standard_normal(n)
+    ref = O.bicgstab(c, b, S, eps=1e-6, max_iter=10 * n)
+    x = _t(np.zeros(n, dtype=dtype), dev)
+    info = linalg.bicgstab(linalg.Stencil(_t(c.astype(dtype), dev), stride=S), _t(b.astype(dtype), dev), x,
+                           eps=1e-6, max_iter=10 * n, persistent=persistent)
+    assert info.ok
+    tol = 1e-5 if dtype == np.float64 else 1e-3
+    assert np.abs(x.cpu().numpy() - ref.x).max() <= tol * np.abs(ref.x).max()
+    assert abs(info.iters - ref.iters) <= max(2, ref.iters // 10)
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_cg_modes_and_history(dev, persistent):
+    import torch
+    from karman_taichi_gb300 import linalg
+    N = 100
+    c = _laplacian(N, 0.02)
+    b = np.random.default_rng(3).standard_normal(N * N)
+    ref = O.cg(c, b, N, eps=1e-9)
+    hist = torch.zeros(2000, dtype=torch.float64, device=dev)
+    x = _t(np.zeros(N * N), dev)
+    info = linalg.cg(linalg.Stencil(_t(c, dev), stride=N), _t(b, dev), x, eps=1e-9, history=hist,
+                     persistent=persistent)
+    assert info.ok and abs(info.iters - ref.iters) <= 2
+    h = hist[: info.iters + 1].cpu().numpy()
+    assert np.allclose(h[1:len(ref.history)], ref.history[1:info.iters + 1][: len(h) - 1], rtol=1e-6)
 
 
 def test_zero_rhs_nan_and_maxiter(dev):
