@@ -112,6 +112,25 @@ int kc_bicgstab(const kc_system* A, const void* b, void* x, const void* M,
                 void* ws, size_t ws_bytes, const kc_solve_opts* opts,
                 kc_solve_info* info, void* stream);
 
+/* BiCGSTAB that allocates nothing.  No counterpart in the reference: it is
+ * for callers that cannot allocate device memory for a workspace -- a plugin
+ * inside a host framework whose allocator owns all device memory, or a loop
+ * in which cudaMalloc/cudaFree (which can synchronise the device) are not
+ * acceptable.  Same arguments and results as kc_bicgstab, minus the
+ * workspace: scratch comes from a static device array built into the library
+ * (about 4.5 MB, held on every GPU that loads the library until exit), which
+ * limits the system to KC_NOALLOC_MAX_N unknowns; larger systems are
+ * rejected with KC_ERR_ARG and an explanation in kc_last_error().
+ * The first call on a device looks up that array's device address (once per
+ * device, with the device current); make that first call before any stream
+ * capture.  Every call uses the same array and each call clears the state it
+ * needs, but calls that overlap on the GPU (concurrent streams, threads or
+ * processes sharing a context) race on it.  Iterations are launched directly
+ * (opts->use_graph is ignored). */
+#define KC_NOALLOC_MAX_N 65536
+int kc_bicgstab_noalloc(const kc_system* A, const void* b, void* x, const void* M,
+                        const kc_solve_opts* opts, kc_solve_info* info, void* stream);
+
 /* Conjugate gradients.  Replaces CGSolver.solve (cgsolver.py:83-114). */
 size_t kc_cg_ws_bytes(long long n, int stride, int dtype);
 int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes,

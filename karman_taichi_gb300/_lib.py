@@ -86,6 +86,8 @@ SIGNATURES = {
     "kc_bicgstab_ws_bytes": (S_, [L_, I_, I_]),
     "kc_bicgstab": (I_, [C.POINTER(KcSystem), P_, P_, P_, P_, S_, C.POINTER(KcSolveOpts),
                          C.POINTER(KcSolveInfo), P_]),
+    "kc_bicgstab_noalloc": (I_, [C.POINTER(KcSystem), P_, P_, P_, C.POINTER(KcSolveOpts),
+                                 C.POINTER(KcSolveInfo), P_]),
     "kc_cg_ws_bytes": (S_, [L_, I_, I_]),
     "kc_cg": (I_, [C.POINTER(KcSystem), P_, P_, P_, S_, C.POINTER(KcSolveOpts),
                    C.POINTER(KcSolveInfo), P_]),

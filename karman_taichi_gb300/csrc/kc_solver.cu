@@ -1594,6 +1594,66 @@ int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes,
     return bicg_impl(A, b, x, nullptr, ws, ws_bytes, opts, info, stream, true);
 }
 
+}  // extern "C"
+
+// ---- BiCGSTAB without caller-provided memory -------------------------------------
+// Some callers cannot allocate device memory for a workspace: a plugin running
+// inside a host framework whose device memory is owned by that framework's
+// allocator, or a tight loop in which cudaMalloc/cudaFree (which can
+// synchronise the whole device) are not acceptable.  kc_bicgstab_noalloc
+// serves them from this file-scope scratch array instead.  It is sized for
+// systems of up to KC_NOALLOC_MAX_N unknowns (about 4.5 MB, held by every GPU
+// that loads the library until the process exits).  In host code the
+// array's name is only a host-side stand-in, so its device address is looked
+// up with cudaGetSymbolAddress, once per device, with that device current.
+namespace kc {
+constexpr size_t kNoallocBytes = 4718592;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error("kc_bicgstab_noalloc: device index %d out of range", dev), KC_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return KC_OK;
+}
+}  // namespace kc
+
+extern "C" {
+
+int kc_bicgstab_noalloc(const kc_system* A, const void* b, void* x, const void* M, const kc_solve_opts* opts,
+                        kc_solve_info* info, void* stream) {
+    int rc = check_system(A);
+    if (rc) return rc;
+    if (!opts) return set_error("kc_bicgstab_noalloc: null opts"), KC_ERR_ARG;
+    if (A->n > KC_NOALLOC_MAX_N)
+        return set_error("kc_bicgstab_noalloc: n = %lld exceeds the static scratch limit of %d unknowns; "
+                         "use kc_bicgstab with a caller-allocated workspace",
+                         A->n, KC_NOALLOC_MAX_N),
+               KC_ERR_ARG;
+    const size_t need = bicg_layout(A->n, A->stride, A->dtype).total;
+    if (need > kNoallocBytes)
+        return set_error("kc_bicgstab_noalloc: this system needs %zu bytes of scratch, the static array holds %zu",
+                         need, kNoallocBytes),
+               KC_ERR_ARG;
+    void* scratch = nullptr;
+    rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    // the graph path would instantiate graphs (allocations); launch directly
+    kc_solve_opts o = *opts;
+    o.use_graph = 0;
+    return bicg_impl(A, b, x, M, scratch, kNoallocBytes, &o, info, stream, false);
+}
+
 // ---- mixed precision refinement ----------------------------------------------
 struct RefineLayout {
     size_t off_state, off_partials, off_out, off_r32, off_d32, off_inner, total, inner_bytes;
