@@ -52,12 +52,24 @@ extern "C" {
 #define KC_REL_R0 0   /* stop when ||r|| / ||r0|| < eps (reference definition) */
 #define KC_REL_B  1   /* stop when ||r|| / ||b||  < eps                         */
 
+/* Coefficient forms.  KC_FORM_STANDARD: component 0 is aP and
+ *   y = aP x + sum_nb a_nb x_nb.
+ * KC_FORM_LAPLACIAN: component 0 holds the row sum rs = aP + sum_nb a_nb and
+ *   y = rs x + sum_nb a_nb (x_nb - x)   (the same operator, written so that
+ * rounding the links to FP32 cannot perturb the row sums -- zero for every
+ * fluid row of the pressure-correction system, whose only Dirichlet
+ * condition is the outlet). */
+#define KC_FORM_STANDARD  0
+#define KC_FORM_LAPLACIAN 1
+
 typedef struct {
     long long n;          /* number of unknowns                                 */
     long long cs, es;     /* coefficient component stride, element stride       */
-    const void* coef;     /* 5 components aP, aW(k-S), aE(k+S), aN(k+1), aS(k-1) */
+    const void* coef;     /* 5 components aP|rs, aW(k-S), aE(k+S), aN(k+1), aS(k-1) */
     int stride;           /* far stride S                                       */
     int dtype;            /* KC_F64 or KC_F32 (vectors and coefficients)        */
+    int form;             /* KC_FORM_STANDARD or KC_FORM_LAPLACIAN              */
+    int pad_;
 } kc_system;
 
 typedef struct {
@@ -145,6 +157,55 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
                         double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
                         double eps_inner, int max_refine, kc_solve_info* info, void* stream);
 
+/* ---- multigrid preconditioner (FP32) --------------------------------------
+ * The reference names multigrid as its missing next step (README.md:31;
+ * debug/note.md:6); it has Jacobi only (karman_taichi.py:398-399).
+ * Aggregation multigrid V-cycle for 2-D 5-point operators: 2x2 Galerkin
+ * coarsening, red-black Gauss-Seidel smoothing with per-level weights
+ * omega[l], coarse corrections scaled by alpha[l].  The operator must be a
+ * genuine 2-D stencil on [n/stride][stride] (no links across row ends). */
+#define KC_MG_MAX_LEVELS 16
+typedef struct {
+    int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */
+    int coarsest_sweeps;          /* Jacobi sweeps on the coarsest level (<= 1024 cells)   */
+    int max_levels;
+    float omega[KC_MG_MAX_LEVELS];/* smoother weight per level                            */
+    float alpha[KC_MG_MAX_LEVELS];/* coarse-correction scale per level                    */
+} kc_mg_opts;
+void   kc_mg_default_opts(kc_mg_opts* opts);
+size_t kc_mg_ws_bytes(long long n, int stride, const kc_mg_opts* opts);
+/* Builds the coarse levels of A32 (FP32) into mg_ws; re-run when A changes. */
+int kc_mg_setup(const kc_system* A32, void* mg_ws, size_t mg_ws_bytes, const kc_mg_opts* opts, void* stream);
+/* z = M r: one V-cycle (r, z: n floats). */
+int kc_mg_apply(const kc_system* A32, void* mg_ws, const kc_mg_opts* opts, const float* r, float* z,
+                void* stream);
+
+/* Mixed precision with the multigrid preconditioner: FP64 residual
+ * refinement around an FP32 right-preconditioned BiCGSTAB (FP32 vectors, FP64
+ * iterate and inner products), stopping when ||b - A64 x|| / ||b|| <
+ * opts->eps.  Each inner solve runs to a relative residual eps_inner; at most
+ * max_refine of them.  x0 (nullable, FP64) is an initial guess; kc_mg_setup
+ * must have been run on mg_ws.  No reference counterpart: the reference's
+ * pressure solve is the plain or Jacobi BiCGSTAB above.  A correction that
+ * raises the true residual is undone and the call returns KC_STALL with x
+ * the best iterate. */
+size_t kc_pbicgstab_ws_bytes(long long n, int stride);
+int kc_pbicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x,
+                         const double* x0, void* mg_ws, const kc_mg_opts* mg_opts, void* ws,
+                         size_t ws_bytes, const kc_solve_opts* opts, double eps_inner,
+                         int max_refine, kc_solve_info* info, void* stream);
+/* The same with multigrid-preconditioned CG as the inner solver, for
+ * symmetric systems (the pressure correction: its links are the face
+ * coefficients rho*dy^2/aP_face, shared by both cells of a face) -- one
+ * operator and one V-cycle per iteration.  Workspace: kc_pbicgstab_ws_bytes.
+ * A non-positive (p, A p) or (r, M r) ends the inner solve with
+ * KC_BREAKDOWN_RHO.  The pressure-correction solve of the accelerated SIMPLE
+ * path. */
+int kc_pcg_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x,
+                   const double* x0, void* mg_ws, const kc_mg_opts* mg_opts, void* ws,
+                   size_t ws_bytes, const kc_solve_opts* opts, double eps_inner,
+                   int max_refine, kc_solve_info* info, void* stream);
+
 /* ---- SIMPLE assembly and correction (staggered padded fields) ----------- */
 #define KC_MODE_SIMPLE   0   /* simple.py set_bc incl. the east-wall aW term (simple.py:215) */
 #define KC_MODE_BICGSIMP 1   /* bicgsimp.py: east-wall fix (:196), p' pinned at (1,1) (:146-151) */
@@ -189,7 +250,8 @@ int kc_outlet_conserve(const kc_phys* P, double* u, void* stream);
 
 /* Pressure-correction coefficients and mass source.  Replaces compute_coef_p
  * (simple.py:143-170; bicgsimp.py:124-151).  mass_dev[0] = max|mdiv| over
- * fluid cells, mass_dev[1] = sum mdiv^2. */
+ * fluid cells, mass_dev[1] = sum mdiv^2.  The optional FP32 copy coef_p32 is
+ * written in KC_FORM_LAPLACIAN (component 0 = row sum). */
 int kc_assemble_pcorr(const kc_phys* P, const double* u, const double* v,
                       const double* coef_u, const double* coef_v, const unsigned char* solid,
                       double* coef_p, double* b_p, float* coef_p32, float* b_p32,

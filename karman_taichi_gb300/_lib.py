@@ -37,7 +37,11 @@ class KcError(RuntimeError):
 
 class KcSystem(C.Structure):
     _fields_ = [("n", C.c_longlong), ("cs", C.c_longlong), ("es", C.c_longlong),
-                ("coef", C.c_void_p), ("stride", C.c_int), ("dtype", C.c_int)]
+                ("coef", C.c_void_p), ("stride", C.c_int), ("dtype", C.c_int),
+                ("form", C.c_int), ("pad_", C.c_int)]
+
+
+FORM_STANDARD, FORM_LAPLACIAN = 0, 1
 
 
 class KcSolveOpts(C.Structure):
@@ -58,6 +62,11 @@ class KcPhys(C.Structure):
                 ("dx", C.c_double), ("dy", C.c_double), ("rho", C.c_double), ("mu", C.c_double),
                 ("dt", C.c_double), ("U", C.c_double), ("bc", (C.c_double * 2) * 4),
                 ("alpha_m", C.c_double), ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
+
+
+class KcMgOpts(C.Structure):
+    _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("coarsest_sweeps", C.c_int), ("max_levels", C.c_int),
+                ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
 
 
 class KcKarman(C.Structure):
@@ -94,6 +103,15 @@ SIGNATURES = {
     "kc_refined_ws_bytes": (S_, [L_, I_]),
     "kc_bicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
                                  C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
+    "kc_mg_default_opts": (None, [C.POINTER(KcMgOpts)]),
+    "kc_mg_ws_bytes": (S_, [L_, I_, C.POINTER(KcMgOpts)]),
+    "kc_mg_setup": (I_, [C.POINTER(KcSystem), P_, S_, C.POINTER(KcMgOpts), P_]),
+    "kc_mg_apply": (I_, [C.POINTER(KcSystem), P_, C.POINTER(KcMgOpts), P_, P_, P_]),
+    "kc_pbicgstab_ws_bytes": (S_, [L_, I_]),
+    "kc_pbicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, P_, C.POINTER(KcMgOpts),
+                                  P_, S_, C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
+    "kc_pcg_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, P_, C.POINTER(KcMgOpts),
+                            P_, S_, C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
     "kc_reduce_ws_bytes": (S_, []),
     "kc_assemble_momentum": (I_, [C.POINTER(KcPhys)] + [P_] * 14 + [P_]),
     "kc_apply_bc_values": (I_, [C.POINTER(KcPhys), P_, P_, P_]),

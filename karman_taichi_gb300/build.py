@@ -27,6 +27,7 @@ SOURCES = {
     "kc_solver.cu": [],
     "kc_simple.cu": ["-fmad=false"],
     "kc_karman.cu": ["-fmad=false"],
+    "kc_mg.cu": [],
     "kc_unet.cu": [],
 }
 

@@ -14,10 +14,14 @@ karman_taichi.py (zero-gradient row + mass-flow rescale):
     stop when mass residual <= mass_tol or after max_outer iterations
     u0 <- u, v0 <- v         (time_forward, karman_taichi.py:617-622)
 
-``precision='fp64'`` is the plain method; ``precision='mixed'`` assembles an
+``precision='fp64'`` is the plain method.  ``precision='mixed'`` assembles an
 FP32 copy of every system and solves with FP32 BiCGSTAB (FP64 inner products)
-inside an FP64 iterative refinement; ``precond='learned'`` adds the learned
-initial guess / preconditioner for p' (karman_taichi_gb300.learned).
+inside an FP64 iterative refinement; its pressure correction (symmetric) is
+solved by CG preconditioned with the aggregation multigrid V-cycle
+(``pcorr_precond='mg'``, the multigrid step the reference names as missing,
+README.md:31), and an
+optional ``learned`` object supplies the initial guess of p'
+(karman_taichi_gb300.learned).
 """
 from __future__ import annotations
 
@@ -30,16 +34,16 @@ import torch
 from . import _lib as L
 from . import geometry
 from .config import ChannelConfig
-from .linalg import Stencil, Workspace, bicgstab, bicgstab_refined, ptr, stream_handle
+from .linalg import Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_refined, ptr, stream_handle
 
 
 class ChannelSolver:
     def __init__(self, cfg: ChannelConfig, device="cuda", precision="fp64", use_graph=True,
-                 eps_inner=1e-3, learned=None):
+                 eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4):
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.cfg, self.precision, self.use_graph = cfg, precision, use_graph
-        self.eps_inner = eps_inner
+        self.eps_inner, self.eps_inner_p = eps_inner, eps_inner_p
         self.learned = learned
         self.device = torch.device(device)
         L.load()
@@ -67,8 +71,17 @@ class ChannelSolver:
         self.rws = torch.zeros(L.load().kc_reduce_ws_bytes(), dtype=torch.uint8, device=self.device)
         self.ws_u, self.ws_v, self.ws_p = Workspace(self.device), Workspace(self.device), Workspace(self.device)
         self.A_u, self.A_v, self.A_p = Stencil(self.coef_u), Stencil(self.coef_v), Stencil(self.coef_p)
+        self.mg = None
+        self.pcorr_precond = pcorr_precond if precision == "mixed" else "none"
         if precision == "mixed":
-            self.A_u32, self.A_v32, self.A_p32 = Stencil(self.coef_u32), Stencil(self.coef_v32), Stencil(self.coef_p32)
+            self.A_u32, self.A_v32 = Stencil(self.coef_u32), Stencil(self.coef_v32)
+            # the FP32 pressure system comes out of the assembly in Laplacian form
+            self.A_p32 = Stencil(self.coef_p32, form=L.FORM_LAPLACIAN)
+            if self.pcorr_precond == "mg":
+                self.mg = Multigrid(self.A_p32, **(mg_opts or {}))
+        self.x0_p = None     # optional initial guess for p' (set by a learned predictor)
+        self.fallbacks = 0   # accelerated p' solves that fell back to plain BiCGSTAB
+        self.last_accel = None  # SolveInfo of the last accelerated p' solve
         ph = L.KcPhys()
         ph.nx, ph.ny, ph.mode = nx, ny, L.MODE_CHANNEL
         ph.dx, ph.dy, ph.rho, ph.mu, ph.dt, ph.U = cfg.dx, cfg.dy, cfg.rho, cfg.mu, cfg.dt, cfg.U
@@ -133,7 +146,21 @@ class ChannelSolver:
 
     def solve_p(self):
         if self.learned is not None:
-            return self.learned.solve(self)
+            self.x0_p = self.learned.predict(self)
+        if self.mg is not None:
+            self.mg.setup()
+            # the pressure correction is symmetric: multigrid-preconditioned CG
+            info = pcg_refined(self.A_p, self.A_p32, self.b_p, self.pcor, self.mg, eps=self.cfg.eps,
+                               eps_inner=self.eps_inner_p, x0=self.x0_p, ws=self.ws_p, use_graph=self.use_graph)
+            self.last_accel = info
+            if info.ok:
+                return info
+            # accelerated solve stalled: plain BiCGSTAB is the fallback
+            self.fallbacks += 1
+            plain = bicgstab(self.A_p, self.b_p, self.pcor, eps=self.cfg.eps, max_iter=self.A_p.n, ws=self.ws_p,
+                             use_graph=self.use_graph)
+            plain.iters += info.iters
+            return plain
         return self._solve(self.A_p, getattr(self, "A_p32", None), self.b_p, self.pcor, self.ws_p)
 
     def correct(self):

@@ -1,0 +1,426 @@
+// Aggregation multigrid V-cycle for 2-D 5-point operators (FP32), used as the
+// preconditioner of the mixed-precision pressure-correction solve (CG, or
+// right-preconditioned BiCGSTAB).
+//
+// The reference has no preconditioner beyond Jacobi (karman_taichi.py:398-399,
+// 418-419) and names multigrid as its missing next step (README.md:31).  This
+// is a GB300 implementation of that step:
+//   * coarsening: 2x2 aggregates, Galerkin coarse operator A_c = P^T A P with
+//     piecewise-constant P, kept in Laplacian form [row sum, links] so no
+//     coarse coefficient is the difference of large numbers (k_mg_coarsen);
+//   * rows without off-diagonal links (halo zero rows, identity rows of
+//     blocked cells) are "isolated": solved pointwise, never aggregated, and
+//     links into them are folded into the row sum -- so a Dirichlet ghost
+//     keeps acting as Dirichlet on coarse levels and unit identity rows do not
+//     swamp the ~1e-3-scaled pressure rows;
+//   * smoother: red-black Gauss-Seidel with a per-level weight omega_l
+//     (isolated rows use the exact pointwise solve); coarse corrections are scaled by
+//     alpha_l (aggregation multigrid needs over-correction).  The post-smoother
+//     visits the colours in the reverse order of the pre-smoother and the
+//     coarsest solve is a fixed number of Jacobi sweeps, so for a symmetric
+//     operator the V-cycle is a symmetric linear operator (usable by CG);
+//   * coarsest level (<= kCoarsestMax cells): Jacobi sweeps in shared memory
+//     by one block.
+// Level 0 is the caller's system (n = NX*NY, far stride NY); levels >= 1 live
+// in the multigrid workspace.  All kernels take an optional "done" word and
+// return at once when it is set, so a solver that converged mid-chunk skips
+// the remaining preconditioner work of a captured graph.
+#include "kc_common.cuh"
+#include "kc_mg.h"
+#include <algorithm>
+
+namespace kc {
+
+constexpr int kCoarsestMax = 1024;
+
+__device__ __forceinline__ bool mg_done(const int* done) { return done && __ldcg(done) != 0; }
+
+// ---- setup ---------------------------------------------------------------------
+// Level-0 scaled inverse diagonal and isolation flags from the caller's FP32
+// coefficients (component stride cs, element stride es; standard or
+// Laplacian form: the diagonal is aP, or rs - sum of links).
+__global__ void k_mg_diag0(const float* __restrict__ c, long long cs, long long es, int lap, int n, float omega,
+                           float* __restrict__ winv, unsigned char* __restrict__ iso) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const long long e = (long long)k * es;
+        const float w = c[cs + e], ea = c[2 * cs + e], no = c[3 * cs + e], so = c[4 * cs + e];
+        const float d = lap ? c[e] - (w + ea + no + so) : c[e];
+        const bool linked = w != 0.f || ea != 0.f || no != 0.f || so != 0.f;
+        iso[k] = linked ? 0 : 1;
+        winv[k] = d == 0.f ? 0.f : (linked ? omega / d : 1.f / d);
+    }
+}
+
+// Coarse operator of level l+1 from level l, in Laplacian form
+// [rs, aW, aE, aN, aS].  Galerkin with piecewise-constant P: the coarse row
+// sum is the sum of the fine row sums, coarse links are the sums of the fine
+// links that cross into a neighbouring aggregate, and links inside an
+// aggregate cancel exactly.  A link into an isolated cell (or outside the
+// grid) sees a zero value there, so it is folded into the row sum.  Nothing
+// is subtracted from anything: FP32 storage cannot perturb the row sums.
+__global__ void k_mg_coarsen(const float* __restrict__ cf, long long cs, long long es, int lapf,
+                             const unsigned char* __restrict__ isof, int NXf, int NYf, float* __restrict__ cc, int NXc,
+                             int NYc, float omega, float* __restrict__ winv, unsigned char* __restrict__ isoc) {
+    const int J = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = blockIdx.y;
+    if (J >= NYc || I >= NXc) return;
+    float rs = 0.f, aW = 0.f, aE = 0.f, aN = 0.f, aS = 0.f;
+    for (int di = 0; di < 2; ++di) {
+        const int i = 2 * I + di;
+        if (i >= NXf) continue;
+        for (int dj = 0; dj < 2; ++dj) {
+            const int j = 2 * J + dj;
+            if (j >= NYf) continue;
+            const int k = i * NYf + j;
+            if (isof[k]) continue;
+            const long long e = (long long)k * es;
+            const float w = cf[cs + e], ea = cf[2 * cs + e], no = cf[3 * cs + e], so = cf[4 * cs + e];
+            float r = lapf ? cf[e] : cf[e] + (w + ea + no + so);
+            if (i - 1 < 0 || isof[k - NYf]) r -= w;
+            else if (di == 0) aW += w;
+            if (i + 1 >= NXf || isof[k + NYf]) r -= ea;
+            else if (di == 1) aE += ea;
+            if (j + 1 >= NYf || isof[k + 1]) r -= no;
+            else if (dj == 1) aN += no;
+            if (j - 1 < 0 || isof[k - 1]) r -= so;
+            else if (dj == 0) aS += so;
+            rs += r;
+        }
+    }
+    const int kc = I * NYc + J;
+    const long long nc = (long long)NXc * NYc;
+    cc[kc] = rs;
+    cc[nc + kc] = aW;
+    cc[2 * nc + kc] = aE;
+    cc[3 * nc + kc] = aN;
+    cc[4 * nc + kc] = aS;
+    const bool linked = aW != 0.f || aE != 0.f || aN != 0.f || aS != 0.f;
+    const float d = rs - (aW + aE + aN + aS);
+    isoc[kc] = linked ? 0 : 1;
+    winv[kc] = d == 0.f ? 0.f : (linked ? omega / d : 1.f / d);
+}
+
+// ---- cycle kernels -----------------------------------------------------------------
+struct Lvl {
+    const float* c;     // coefficients
+    long long cs, es;
+    int NX, NY;
+    int lap;            // Laplacian form (component 0 = row sum)
+    const float* winv;
+    const unsigned char* iso;
+};
+
+__device__ __forceinline__ float mg_Ax(const Lvl& L, const float* __restrict__ x, int k) {
+    const long long e = (long long)k * L.es;
+    const int n = L.NX * L.NY;
+    const float xk = x[k];
+    const float xw = k >= L.NY ? x[k - L.NY] : 0.f, xe = k + L.NY < n ? x[k + L.NY] : 0.f;
+    const float xn = k + 1 < n ? x[k + 1] : 0.f, xs = k >= 1 ? x[k - 1] : 0.f;
+    float y = __ldg(L.c + e) * xk;
+    if (L.lap) {
+        y = fmaf(__ldg(L.c + L.cs + e), xw - xk, y);
+        y = fmaf(__ldg(L.c + 2 * L.cs + e), xe - xk, y);
+        y = fmaf(__ldg(L.c + 3 * L.cs + e), xn - xk, y);
+        y = fmaf(__ldg(L.c + 4 * L.cs + e), xs - xk, y);
+    } else {
+        y = fmaf(__ldg(L.c + L.cs + e), xw, y);
+        y = fmaf(__ldg(L.c + 2 * L.cs + e), xe, y);
+        y = fmaf(__ldg(L.c + 3 * L.cs + e), xn, y);
+        y = fmaf(__ldg(L.c + 4 * L.cs + e), xs, y);
+    }
+    return y;
+}
+
+// Red-black Gauss-Seidel half-sweep on cells with (i + j) % 2 == color:
+// x += W (b - A x).  In place: a cell of one colour reads only the other.
+__global__ void k_mg_rbgs(Lvl L, const float* __restrict__ b, float* __restrict__ x, int color, const int* done) {
+    if (mg_done(done)) return;
+    const int n = L.NX * L.NY;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = k / L.NY, j = k - i * L.NY;
+        if (((i + j) & 1) != color) continue;
+        const float r = __ldg(b + k) - mg_Ax(L, x, k);
+        x[k] = fmaf(__ldg(L.winv + k), r, x[k]);
+    }
+}
+
+// first half-sweep from x = 0: red cells x = W b, black cells 0
+__global__ void k_mg_first(Lvl L, const float* __restrict__ b, float* __restrict__ x, const int* done) {
+    if (mg_done(done)) return;
+    const int n = L.NX * L.NY;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = k / L.NY, j = k - i * L.NY;
+        x[k] = ((i + j) & 1) == 0 ? __ldg(L.winv + k) * __ldg(b + k) : 0.f;
+    }
+}
+
+// b_c(I,J) = sum of the fine residual b - A x over the aggregate's coupled cells
+__global__ void k_mg_restrict(Lvl F, const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ bc,
+                              int NXc, int NYc, const int* done) {
+    if (mg_done(done)) return;
+    const int J = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = blockIdx.y;
+    if (J >= NYc || I >= NXc) return;
+    float s = 0.f;
+    for (int di = 0; di < 2; ++di) {
+        const int i = 2 * I + di;
+        if (i >= F.NX) continue;
+        for (int dj = 0; dj < 2; ++dj) {
+            const int j = 2 * J + dj;
+            if (j >= F.NY) continue;
+            const int k = i * F.NY + j;
+            if (F.iso[k]) continue;
+            s += __ldg(b + k) - mg_Ax(F, x, k);
+        }
+    }
+    bc[I * NYc + J] = s;
+}
+
+// x_f += alpha * x_c(aggregate) on coupled fine cells
+__global__ void k_mg_prolong(Lvl F, float* __restrict__ x, const float* __restrict__ xc, int NYc, float alpha,
+                             const int* done) {
+    if (mg_done(done)) return;
+    const int n = F.NX * F.NY;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (F.iso[k]) continue;
+        const int i = k / F.NY, j = k - (k / F.NY) * F.NY;
+        x[k] = fmaf(alpha, __ldg(xc + (i >> 1) * NYc + (j >> 1)), x[k]);
+    }
+}
+
+// coarsest level: Jacobi sweeps in shared memory (one block, n <= kCoarsestMax)
+__global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float* __restrict__ b,
+                                                              float* __restrict__ x, int sweeps, const int* done) {
+    if (mg_done(done)) return;
+    __shared__ float xs[2][kCoarsestMax];
+    const int n = L.NX * L.NY;
+    const int k = threadIdx.x;
+    float bk = 0.f, w = 0.f, c[5] = {0, 0, 0, 0, 0};
+    if (k < n) {
+        bk = b[k];
+        w = L.winv[k];
+        const long long e = (long long)k * L.es;
+        for (int q = 0; q < 5; ++q) c[q] = L.c[q * L.cs + e];
+        xs[0][k] = w * bk;
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int s = 0; s < sweeps; ++s) {
+        if (k < n) {
+            const float* xv = xs[cur];
+            const float xk = xv[k];
+            const float xw = k >= L.NY ? xv[k - L.NY] : 0.f, xe = k + L.NY < n ? xv[k + L.NY] : 0.f;
+            const float xn = k + 1 < n ? xv[k + 1] : 0.f, xso = k >= 1 ? xv[k - 1] : 0.f;
+            float y = c[0] * xk;
+            if (L.lap) y += c[1] * (xw - xk) + c[2] * (xe - xk) + c[3] * (xn - xk) + c[4] * (xso - xk);
+            else y += c[1] * xw + c[2] * xe + c[3] * xn + c[4] * xso;
+            xs[cur ^ 1][k] = xk + w * (bk - y);
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (k < n) x[k] = xs[cur][k];
+}
+
+// ---- host ----------------------------------------------------------------------------
+static int mg_levels(int NX, int NY, const kc_mg_opts* o, int* nx, int* ny) {
+    int L = 0;
+    nx[0] = NX;
+    ny[0] = NY;
+    const int maxl = std::max(1, std::min(o ? o->max_levels : KC_MG_MAX_LEVELS, (int)KC_MG_MAX_LEVELS));
+    while (L + 1 < maxl && (long long)nx[L] * ny[L] > kCoarsestMax) {
+        nx[L + 1] = (nx[L] + 1) / 2;
+        ny[L + 1] = (ny[L] + 1) / 2;
+        ++L;
+    }
+    return L + 1;
+}
+
+MgLayout mg_layout(int NX, int NY, const kc_mg_opts* o) {
+    MgLayout M{};
+    M.levels = mg_levels(NX, NY, o, M.nx, M.ny);
+    size_t off = 0;
+    for (int l = 0; l < M.levels; ++l) {
+        const size_t n = (size_t)M.nx[l] * M.ny[l];
+        M.off_winv[l] = off;
+        off = align256(off + n * 4);
+        M.off_iso[l] = off;
+        off = align256(off + n);
+        if (l >= 1) {
+            M.off_coef[l] = off;
+            off = align256(off + 5 * n * 4);
+            M.off_b[l] = off;
+            off = align256(off + n * 4);
+        }
+        M.off_x[l] = off;
+        off = align256(off + n * 4);
+        M.off_t[l] = off;
+        off = align256(off + n * 4);
+    }
+    M.total = off;
+    return M;
+}
+
+static Lvl level_of(const MgLayout& M, char* base, int l, const float* c0, long long cs0, long long es0,
+                    int lap0) {
+    Lvl L;
+    const long long n = (long long)M.nx[l] * M.ny[l];
+    if (l == 0) {
+        L.c = c0;
+        L.cs = cs0;
+        L.es = es0;
+        L.lap = lap0;
+    } else {
+        L.c = (const float*)(base + M.off_coef[l]);
+        L.cs = n;
+        L.es = 1;
+        L.lap = 1;
+    }
+    L.NX = M.nx[l];
+    L.NY = M.ny[l];
+    L.winv = (const float*)(base + M.off_winv[l]);
+    L.iso = (const unsigned char*)(base + M.off_iso[l]);
+    return L;
+}
+
+static inline unsigned pw_grid(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096)); }
+
+int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o, cudaStream_t s) {
+    if (!A || !A->coef || A->dtype != KC_F32) return set_error("multigrid needs FP32 coefficients"), KC_ERR_ARG;
+    const int NY = A->stride;
+    if (NY < 1 || A->n % NY != 0) return set_error("multigrid: n = %lld is not a multiple of the stride %d", A->n, NY), KC_ERR_ARG;
+    const int NX = (int)(A->n / NY);
+    MgLayout M = mg_layout(NX, NY, o);
+    if (!ws || ws_bytes < M.total) return set_error("multigrid workspace %zu < %zu", ws_bytes, M.total), KC_ERR_WORKSPACE;
+    char* base = (char*)ws;
+    const float* c0 = (const float*)A->coef;
+    k_mg_diag0<<<pw_grid(A->n), 256, 0, s>>>(c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN, (int)A->n, o->omega[0],
+                                              (float*)(base + M.off_winv[0]), (unsigned char*)(base + M.off_iso[0]));
+    KC_LAUNCH_CHECK("k_mg_diag0");
+    for (int l = 0; l + 1 < M.levels; ++l) {
+        const float* cf = l == 0 ? c0 : (const float*)(base + M.off_coef[l]);
+        const long long cs = l == 0 ? A->cs : (long long)M.nx[l] * M.ny[l];
+        const long long es = l == 0 ? A->es : 1;
+        dim3 g((M.ny[l + 1] + 127) / 128, M.nx[l + 1]);
+        const int lapf = l == 0 ? (A->form == KC_FORM_LAPLACIAN) : 1;
+        k_mg_coarsen<<<g, 128, 0, s>>>(cf, cs, es, lapf, (const unsigned char*)(base + M.off_iso[l]), M.nx[l], M.ny[l],
+                                       (float*)(base + M.off_coef[l + 1]), M.nx[l + 1], M.ny[l + 1],
+                                       o->omega[std::min(l + 1, KC_MG_MAX_LEVELS - 1)],
+                                       (float*)(base + M.off_winv[l + 1]), (unsigned char*)(base + M.off_iso[l + 1]));
+        KC_LAUNCH_CHECK("k_mg_coarsen");
+    }
+    return KC_OK;
+}
+
+// Enqueues one V-cycle z = M r (level-0 input r, output z; both n floats).
+int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r, float* z, const int* done,
+               cudaStream_t s, int* kernels) {
+    int nk = 0;
+    const int NY = A->stride;
+    const int NX = (int)(A->n / NY);
+    MgLayout M = mg_layout(NX, NY, o);
+    char* base = (char*)ws;
+    const float* c0 = (const float*)A->coef;
+    const float* bl[KC_MG_MAX_LEVELS];
+    float* xl[KC_MG_MAX_LEVELS];
+    for (int l = 0; l < M.levels; ++l) {
+        bl[l] = l == 0 ? r : (const float*)(base + M.off_b[l]);
+        xl[l] = l == 0 ? z : (float*)(base + M.off_x[l]);
+    }
+    // downward leg: nu_pre red-black sweeps (the first from x = 0), restrict
+    for (int l = 0; l < M.levels; ++l) {
+        Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
+        const long long n = (long long)M.nx[l] * M.ny[l];
+        if (l == M.levels - 1) {
+            k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, bl[l], xl[l], o->coarsest_sweeps, done);
+            KC_LAUNCH_CHECK_NC("k_mg_coarsest");
+            ++nk;
+            break;
+        }
+        k_mg_first<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], done);
+        KC_LAUNCH_CHECK_NC("k_mg_first");
+        ++nk;
+        k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
+        KC_LAUNCH_CHECK_NC("k_mg_rbgs");
+        ++nk;
+        for (int q = 1; q < o->nu_pre; ++q) {
+            k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 0, done);
+            k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
+            KC_LAUNCH_CHECK_NC("k_mg_rbgs");
+            nk += 2;
+        }
+        dim3 g((M.ny[l + 1] + 127) / 128, M.nx[l + 1]);
+        k_mg_restrict<<<g, 128, 0, s>>>(L, bl[l], xl[l], (float*)bl[l + 1], M.nx[l + 1], M.ny[l + 1], done);
+        KC_LAUNCH_CHECK_NC("k_mg_restrict");
+        ++nk;
+    }
+    // upward leg: over-corrected prolongation, nu_post red-black sweeps
+    for (int l = M.levels - 2; l >= 0; --l) {
+        Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
+        const long long n = (long long)M.nx[l] * M.ny[l];
+        k_mg_prolong<<<pw_grid(n), 256, 0, s>>>(L, xl[l], xl[l + 1], M.ny[l + 1],
+                                                o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], done);
+        KC_LAUNCH_CHECK_NC("k_mg_prolong");
+        ++nk;
+        for (int q = 0; q < o->nu_post; ++q) {
+            k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
+            k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 0, done);
+            KC_LAUNCH_CHECK_NC("k_mg_rbgs");
+            nk += 2;
+        }
+    }
+    if (kernels) *kernels = nk;
+    return KC_OK;
+}
+
+}  // namespace kc
+
+using namespace kc;
+
+extern "C" {
+
+void kc_mg_default_opts(kc_mg_opts* o) {
+    if (!o) return;
+    o->nu_pre = 2;
+    o->nu_post = 2;
+    o->coarsest_sweeps = 64;
+    o->max_levels = KC_MG_MAX_LEVELS;
+    for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
+        o->omega[l] = 0.8f;
+        o->alpha[l] = 1.8f;
+    }
+}
+
+size_t kc_mg_ws_bytes(long long n, int stride, const kc_mg_opts* opts) {
+    if (n < 1 || stride < 1 || n % stride) return 0;
+    kc_mg_opts d;
+    if (!opts) {
+        kc_mg_default_opts(&d);
+        opts = &d;
+    }
+    return mg_layout((int)(n / stride), stride, opts).total;
+}
+
+int kc_mg_setup(const kc_system* A32, void* mg_ws, size_t mg_ws_bytes, const kc_mg_opts* opts, void* stream) {
+    kc_mg_opts d;
+    if (!opts) {
+        kc_mg_default_opts(&d);
+        opts = &d;
+    }
+    return mg_setup(A32, mg_ws, mg_ws_bytes, opts, as_stream(stream));
+}
+
+int kc_mg_apply(const kc_system* A32, void* mg_ws, const kc_mg_opts* opts, const float* r, float* z, void* stream) {
+    if (!A32 || !mg_ws || !r || !z) return set_error("kc_mg_apply: null argument"), KC_ERR_ARG;
+    kc_mg_opts d;
+    if (!opts) {
+        kc_mg_default_opts(&d);
+        opts = &d;
+    }
+    int nk = 0;
+    const int rc = mg_enqueue(A32, mg_ws, opts, r, z, nullptr, as_stream(stream), &nk);
+    count_launches(nk);
+    return rc;
+}
+
+}  // extern "C"

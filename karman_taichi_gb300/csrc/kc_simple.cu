@@ -380,8 +380,12 @@ __global__ void __launch_bounds__(256)
             for (int q = 0; q < 5; ++q) cp[q * n + k] = c[q];
             bp[k] = b;
             if (cp32) {
+                // FP32 copy in Laplacian form: component 0 is the row sum,
+                // evaluated in the order aP was built in, so it is exactly 0
+                // on every fluid row (see KC_FORM_LAPLACIAN)
+                cp32[k] = (float)(c[0] + (((c[1] + c[2]) + c[3]) + c[4]));
 #pragma unroll
-                for (int q = 0; q < 5; ++q) cp32[q * n + k] = (float)c[q];
+                for (int q = 1; q < 5; ++q) cp32[q * n + k] = (float)c[q];
                 bp32[k] = (float)b;
             }
         }

@@ -37,10 +37,12 @@
 // GB300 issues FP64 at 1/60 of its FP32 rate (1.19 vs 72 TFLOP/s measured),
 // so FP64 work per cell would make the FP32 solver compute bound.
 #include "kc_common.cuh"
+#include "kc_mg.h"
 #include <algorithm>
 #include <mutex>
 #include <map>
 #include <tuple>
+#include <cstring>
 
 namespace kc {
 
@@ -74,6 +76,7 @@ template <typename T>
 struct Coef {
     const T* __restrict__ c;
     long long cs, es;
+    int lap;   // KC_FORM_LAPLACIAN: component 0 holds the row sum
     __device__ __forceinline__ T at(int comp, int k) const { return __ldg(c + comp * cs + (long long)k * es); }
 };
 
@@ -279,11 +282,19 @@ __device__ __forceinline__ void stencil_tile_at(const Pol& pol, const Coef<T>& A
     for (int r = 0; r < kCPT; ++r) {
         if (kc[r] >= 0) {
             const int a = ty + 8 * r;
-            T y = c[r][0] * op[a + 1][tx + 1];
-            y = fmaT<T>(c[r][1], op[a][tx + 1], y);
-            y = fmaT<T>(c[r][2], op[a + 2][tx + 1], y);
-            y = fmaT<T>(c[r][3], op[a + 1][tx + 2], y);
-            y = fmaT<T>(c[r][4], op[a + 1][tx], y);
+            const T o = op[a + 1][tx + 1];
+            T y = c[r][0] * o;
+            if (A.lap) {
+                y = fmaT<T>(c[r][1], op[a][tx + 1] - o, y);
+                y = fmaT<T>(c[r][2], op[a + 2][tx + 1] - o, y);
+                y = fmaT<T>(c[r][3], op[a + 1][tx + 2] - o, y);
+                y = fmaT<T>(c[r][4], op[a + 1][tx] - o, y);
+            } else {
+                y = fmaT<T>(c[r][1], op[a][tx + 1], y);
+                y = fmaT<T>(c[r][2], op[a + 2][tx + 1], y);
+                y = fmaT<T>(c[r][3], op[a + 1][tx + 2], y);
+                y = fmaT<T>(c[r][4], op[a + 1][tx], y);
+            }
             pol.sink(kc[r], y, Pol::kAux ? aux[a][tx] : T(0), acc);
         }
     }
@@ -828,9 +839,31 @@ __global__ void __launch_bounds__(kPwThreads)
 }
 
 __global__ void __launch_bounds__(kPwThreads)
+    k_flag_nonfinite_f64(int n, const double* __restrict__ d, int* __restrict__ flag) {
+    int bad = 0;
+    KC_PW_LOOP(n, { bad |= !isfinite(__ldg(d + k)); })
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+__global__ void __launch_bounds__(kPwThreads)
+    k_add_f64(int n, const double* __restrict__ d, double* __restrict__ x, const int* __restrict__ flag) {
+    if (__ldcg(flag)) return;
+    KC_PW_LOOP(n, { x[k] += __ldg(d + k); })
+}
+
+__global__ void __launch_bounds__(kPwThreads) k_sub_f64(int n, const double* __restrict__ d, double* __restrict__ x) {
+    KC_PW_LOOP(n, { x[k] -= __ldg(d + k); })
+}
+
+__global__ void __launch_bounds__(kPwThreads)
     k_add_f32_to_f64(int n, const float* __restrict__ d, double* __restrict__ x, const int* __restrict__ flag) {
     if (__ldcg(flag)) return;
     KC_PW_LOOP(n, { x[k] += (double)__ldg(d + k); })
+}
+
+__global__ void __launch_bounds__(kPwThreads)
+    k_sub_f32_from_f64(int n, const float* __restrict__ d, double* __restrict__ x) {
+    KC_PW_LOOP(n, { x[k] -= (double)__ldg(d + k); })
 }
 
 __global__ void k_zero_f64(int n, double* __restrict__ x) {
@@ -1249,6 +1282,234 @@ __global__ void k_hist_sqrt(double* h, long long from, long long to) {
 }
 
 // =============================================================================
+// Right-preconditioned BiCGSTAB (FP32 vectors, FP64 scalars) for a general
+// preconditioner M applied between the passes (multigrid V-cycle):
+//   P1  p = r + beta (p - omega v)           [pointwise]
+//   M   p^ = M p
+//   P2  v = A p^, partial (r~, v) -> alpha   [stencil]
+//   P3  s = r - alpha v                      [pointwise]
+//   M   s^ = M s
+//   P4  t = A s^, partials (t, s), (t, t) -> omega
+//   P5  x += alpha p^ + omega s^, r = s - omega t, (r, r~), (r, r)
+// The iterate x is FP64: for the pressure correction of a long channel
+// (cond ~ 1e7) an FP32 iterate carries rounding noise of relative size u32,
+// and A applied to that noise is as large as the residual being solved for,
+// so FP32 storage alone would stop the outer refinement.
+// =============================================================================
+struct PbVecs {
+    float *r, *rt, *p, *ph, *v, *s, *sh, *t;
+    double* x;
+};
+
+__global__ void __launch_bounds__(kPwThreads) k_pb_p(int n, PbVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const bool first = __ldcg(&st->iter) == 0;
+    const float beta = __ldcg(&st->beta_f), omega = __ldcg(&st->omega_f);
+    KC_PW_LOOP(n, {
+        const float rk = V.r[k];
+        V.p[k] = first ? rk : fmaf(beta, fmaf(-omega, V.v[k], V.p[k]), rk);
+    })
+}
+
+template <bool TWO>
+struct PolPb {
+    static constexpr bool kAux = false;
+    const float* __restrict__ x;     // operand (p^ or s^)
+    float* __restrict__ y;           // output (v or t)
+    const float* __restrict__ rt;
+    const float* __restrict__ s;
+    __device__ __forceinline__ float pre(int k) const { return __ldg(x + k); }
+    __device__ __forceinline__ float scale(int, float p) const { return p; }
+    __device__ __forceinline__ void own(int, float) const {}
+    __device__ __forceinline__ void sink(int k, float v, float, Acc<float> (&acc)[TWO ? 2 : 1]) const {
+        y[k] = v;
+        if (TWO) {
+            acc[0].add(v, __ldg(s + k));
+            acc[TWO ? 1 : 0].add(v, v);
+        } else {
+            acc[0].add(__ldg(rt + k), v);
+        }
+    }
+};
+
+__global__ void __launch_bounds__(kThreads) k_pb_Av(Coef<float> A, Geo g, PbVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    PolPb<false> pol{V.ph, V.v, V.rt, nullptr};
+    Acc<float> acc[1];
+    stencil_tile<float, 1>(pol, A, g.n, g.S, acc);
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        set_alpha(st, st->rho / s[0]);
+        st->ticket[0] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kPwThreads) k_pb_s(int n, PbVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const float alpha = __ldcg(&st->alpha_f);
+    KC_PW_LOOP(n, { V.s[k] = fmaf(-alpha, V.v[k], V.r[k]); })
+}
+
+__global__ void __launch_bounds__(kThreads) k_pb_At(Coef<float> A, Geo g, PbVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    PolPb<true> pol{V.sh, V.t, nullptr, V.s};
+    Acc<float> acc[2];
+    stencil_tile<float, 2>(pol, A, g.n, g.S, acc);
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        set_omega(st, s[0] / s[1]);
+        st->ticket[0] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kPwThreads) k_pb_x(int n, PbVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const float alpha = __ldcg(&st->alpha_f), omega = __ldcg(&st->omega_f);
+    const double alpha_d = __ldcg(&st->alpha), omega_d = __ldcg(&st->omega);
+    Acc<float> acc[2];
+    KC_PW_LOOP(n, {
+        V.x[k] = fma(alpha_d, (double)V.ph[k], fma(omega_d, (double)V.sh[k], V.x[k]));
+        const float rn = fmaf(-omega, V.t[k], V.s[k]);
+        V.r[k] = rn;
+        acc[0].add(rn, __ldg(V.rt + k));
+        acc[1].add(rn, rn);
+    })
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
+        bicg_finish_iteration(st, s[0], s[1]);
+        st->ticket[0] = 0;
+    }
+}
+
+// =============================================================================
+// Preconditioned CG (FP32 vectors, FP64 iterate and scalars) for symmetric
+// systems with a symmetric preconditioner M (the multigrid V-cycle, whose
+// post-smoother mirrors its pre-smoother):
+//   K1  p = z + beta p (formed in the stencil tile), q = A p, (p, q) -> alpha
+//   K2  x += alpha p, r -= alpha q, (r, r) -> convergence
+//   M   z = M r
+//   K3  (r, z) -> beta
+// One operator and one V-cycle per iteration, half of BiCGSTAB's.  The start
+// is K0 (r = b, x = 0, (r, r)), M, K3.
+// =============================================================================
+struct PcVecs {
+    float *r, *z, *p[2], *q;
+    double* x;
+};
+
+struct PolPc1 {
+    static constexpr bool kAux = true;
+    const float* __restrict__ z;
+    const float* __restrict__ p_old;
+    float* __restrict__ p_new;
+    float* __restrict__ q;
+    float beta;
+    bool first;
+    __device__ __forceinline__ float pre(int k) const {
+        return first ? __ldg(z + k) : fmaf(beta, __ldg(p_old + k), __ldg(z + k));
+    }
+    __device__ __forceinline__ float scale(int, float p) const { return p; }
+    __device__ __forceinline__ void own(int k, float p) const { p_new[k] = p; }
+    __device__ __forceinline__ void sink(int k, float y, float p, Acc<float> (&acc)[1]) const {
+        q[k] = y;
+        acc[0].add(p, y);
+    }
+};
+
+__global__ void __launch_bounds__(kThreads) k_pc_1(Coef<float> A, Geo g, PcVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const long long it = __ldcg(&st->iter);
+    const int cur = (int)(it & 1);
+    PolPc1 pol{V.z, V.p[cur], V.p[cur ^ 1], V.q, __ldcg(&st->beta_f), it == 0};
+    Acc<float> acc[1];
+    stencil_tile<float, 1>(pol, A, g.n, g.S, acc);
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        if (!(s[0] > 0.0)) {  // (p, A p) <= 0: the preconditioned operator is not positive definite
+            st->status = isfinite(s[0]) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            st->done = 1;
+        } else {
+            set_alpha(st, st->old / s[0]);
+        }
+        st->ticket[0] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kPwThreads) k_pc_2(int n, PcVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const long long it = __ldcg(&st->iter);
+    const float* __restrict__ p = V.p[(int)((it + 1) & 1)];
+    const float alpha = __ldcg(&st->alpha_f);
+    const double alpha_d = __ldcg(&st->alpha);
+    Acc<float> acc[1];
+    KC_PW_LOOP(n, {
+        const float pk = __ldg(p + k);
+        V.x[k] = fma(alpha_d, (double)pk, V.x[k]);
+        const float rn = fmaf(-alpha, __ldg(V.q + k), V.r[k]);
+        V.r[k] = rn;
+        acc[0].add(rn, rn);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
+        const double nw = s[0];
+        st->iter += 1;
+        st->rTr = nw;
+        record_history(st, st->iter, nw);
+        const double rel = st->den > 0.0 ? sqrt(nw / st->den) : 0.0;
+        st->prev_rel = rel;
+        if (rel < st->eps) {
+            st->status = KC_OK;
+            st->done = 1;
+        } else if (!isfinite(nw)) {
+            st->status = KC_NONFINITE;
+            st->done = 1;
+        } else if (st->iter >= st->max_iter) {
+            st->status = KC_MAXITER;
+            st->done = 1;
+        }
+        st->ticket[0] = 0;
+    }
+}
+
+// (r, z) -> beta = (r, z) / (r, z)_old; at the start it only records (r0, z0)
+__global__ void __launch_bounds__(kPwThreads) k_pc_3(int n, PcVecs V, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    Acc<float> acc[1];
+    KC_PW_LOOP(n, { acc[0].add(__ldg(V.r + k), __ldg(V.z + k)); })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
+        const double rz = s[0];
+        if (!(rz > 0.0)) {  // (r, M r) <= 0: M is not positive definite
+            st->status = isfinite(rz) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            st->done = 1;
+        } else {
+            if (__ldcg(&st->iter) > 0) {
+                const double beta = rz / st->old;
+                st->beta = beta;
+                st->beta_f = (float)beta;
+            }
+            st->old = rz;
+        }
+        st->ticket[0] = 0;
+    }
+}
+
+__global__ void k_copy_f64(int n, const double* __restrict__ a, double* __restrict__ b) {
+    KC_PW_LOOP(n, { b[k] = a[k]; })
+}
+
+// =============================================================================
 // Host side
 // =============================================================================
 static inline size_t esize(int dtype) { return dtype == KC_F64 ? 8 : 4; }
@@ -1288,12 +1549,14 @@ static int check_system(const kc_system* A) {
         return set_error("kc_system: stride %d unsupported for n = %lld", A->stride, A->n), KC_ERR_ARG;
     if (A->cs < 0 || A->es < 1)
         return set_error("kc_system: bad coefficient strides cs=%lld es=%lld", A->cs, A->es), KC_ERR_ARG;
+    if (A->form != KC_FORM_STANDARD && A->form != KC_FORM_LAPLACIAN)
+        return set_error("kc_system: unknown coefficient form %d", A->form), KC_ERR_ARG;
     return KC_OK;
 }
 
 template <typename T>
 static Coef<T> coef_of(const kc_system* A) {
-    return Coef<T>{(const T*)A->coef, A->cs, A->es};
+    return Coef<T>{(const T*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN ? 1 : 0};
 }
 
 struct HostState {
@@ -1373,13 +1636,15 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
     const int gchunk = 16;
     while (!h->done && launched < cap) {
         int m = (int)std::min<long long>(chunk, cap - launched);
-        if (o->use_graph && m == gchunk) {
+        if (o->use_graph && (fixed ? m == chunk : m == gchunk)) {
             int dev = 0;
             KC_CUDA(cudaGetDevice(&dev));
+            GraphKey gk = key;
+            gk.chunk = m;
             cudaGraphExec_t ex = nullptr;
             {
                 std::lock_guard<std::mutex> lk(g_graph_mu);
-                auto it = g_graphs.find({dev, key});
+                auto it = g_graphs.find({dev, gk});
                 if (it != g_graphs.end()) ex = it->second;
             }
             if (!ex) {
@@ -1399,7 +1664,7 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
                     for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
                     g_graphs.clear();
                 }
-                g_graphs[{dev, key}] = ex;
+                g_graphs[{dev, gk}] = ex;
             }
             KC_CUDA(cudaGraphLaunch(ex, s));
         } else {
@@ -1712,6 +1977,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     int pb = pw_blocks(n);
     KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
     k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);
+    KC_CUDA(cudaMemsetAsync(out2, 0, 4 * sizeof(double), s));
     kc_solve_opts io = *o;
     io.eps = eps_inner;
     io.x0 = KC_X0_ZERO;
@@ -1723,14 +1989,26 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     long long total = 0;
     int status = KC_MAXITER, sweeps = 0, stalls = 0;
     double rel = 1.0, bb = 0.0, best = INFINITY;
+    bool applied = false;
     for (int it = 0; it <= max_refine; ++it) {
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2);
         KC_LAUNCH_CHECK("k_refine_resid");
-        double h2[2];
+        double h2[3];
         KC_CUDA(cudaMemcpyAsync(h2, out2, sizeof(h2), cudaMemcpyDeviceToHost, s));
         KC_CUDA(cudaStreamSynchronize(s));
         bb = h2[1];
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
+        int skipped = 0;
+        memcpy(&skipped, &h2[2], sizeof(int));
+        if (applied && skipped == 0 && !(rel < best)) {
+            // the last correction raised the true residual: undo it, keep the best iterate
+            k_sub_f32_from_f64<<<pb, kPwThreads, 0, s>>>((int)n, d32, x);
+            KC_LAUNCH_CHECK("undo correction");
+            rel = best;
+            status = KC_STALL;
+            break;
+        }
+        applied = false;
         if (bb == 0.0 || rel < o->eps) {
             status = KC_OK;
             break;
@@ -1763,6 +2041,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         k_flag_nonfinite<<<pb, kPwThreads, 0, s>>>((int)n, d32, flag);
         k_add_f32_to_f64<<<pb, kPwThreads, 0, s>>>((int)n, d32, x, flag);
         KC_LAUNCH_CHECK("k_add_f32_to_f64");
+        applied = true;
         if (r2 != KC_OK && ii.iters == 0) {
             status = r2;
             break;
@@ -1776,6 +2055,247 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         info->r0 = sqrt(bb);
     }
     return status;
+}
+
+}  // extern "C"
+
+// ---- multigrid-preconditioned refinement -------------------------------------------
+namespace kc {
+struct PbLayout {
+    size_t off_state, off_partials, off_rstate, off_rpart, off_out, off_r32, off_vec[8], off_x, total;
+    int ld;
+};
+static PbLayout pb_layout(long long n, int S) {
+    PbLayout L{};
+    dim3 g = stencil_grid(n, std::max(S, 1));
+    int nb = std::max<int>((int)(g.x * g.y), pw_blocks(n));
+    L.ld = (int)align256((size_t)nb * 8) / 8;
+    size_t off = 0;
+    L.off_state = off;
+    off = align256(off + sizeof(SolverState));
+    L.off_partials = off;
+    off = align256(off + (size_t)5 * L.ld * 8);
+    L.off_rstate = off;
+    off = align256(off + sizeof(SolverState));
+    L.off_rpart = off;
+    off = align256(off + (size_t)2 * L.ld * 8);
+    L.off_out = off;
+    off = align256(off + 64);
+    L.off_r32 = off;
+    off = align256(off + (size_t)n * 4);
+    for (int q = 0; q < 8; ++q) {
+        L.off_vec[q] = off;
+        off = align256(off + (size_t)n * 4);
+    }
+    L.off_x = off;
+    off = align256(off + (size_t)n * 8);
+    L.total = off;
+    return L;
+}
+
+// m iterations of the preconditioned BiCGSTAB; *kernels = launches per iteration
+static int launch_pb_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* mo, const PbVecs& V, const BicgPtrs& P,
+                           int m, cudaStream_t s, int* kernels) {
+    Geo g{(int)A32->n, A32->stride};
+    dim3 sg = stencil_grid(A32->n, A32->stride);
+    const int pb = pw_blocks(A32->n);
+    Coef<float> C = coef_of<float>(A32);
+    const int* done = &P.st->done;
+    int k1 = 0, k2 = 0;
+    for (int q = 0; q < m; ++q) {
+        k_pb_p<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+        int rc = mg_enqueue(A32, mg_ws, mo, V.p, V.ph, done, s, &k1);
+        if (rc) return rc;
+        k_pb_Av<<<sg, kThreads, 0, s>>>(C, g, V, P);
+        k_pb_s<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+        rc = mg_enqueue(A32, mg_ws, mo, V.s, V.sh, done, s, &k2);
+        if (rc) return rc;
+        k_pb_At<<<sg, kThreads, 0, s>>>(C, g, V, P);
+        k_pb_x<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+        KC_LAUNCH_CHECK_NC("preconditioned iteration");
+    }
+    if (kernels) *kernels = 5 + k1 + k2;
+    return KC_OK;
+}
+
+// m iterations of the preconditioned CG; *kernels = launches per iteration
+static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* mo, const PcVecs& V, const BicgPtrs& P,
+                           int m, cudaStream_t s, int* kernels) {
+    Geo g{(int)A32->n, A32->stride};
+    dim3 sg = stencil_grid(A32->n, A32->stride);
+    const int pb = pw_blocks(A32->n);
+    Coef<float> C = coef_of<float>(A32);
+    const int* done = &P.st->done;
+    int k1 = 0;
+    for (int q = 0; q < m; ++q) {
+        k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
+        k_pc_2<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+        int rc = mg_enqueue(A32, mg_ws, mo, V.r, V.z, done, s, &k1);
+        if (rc) return rc;
+        k_pc_3<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+        KC_LAUNCH_CHECK_NC("preconditioned CG iteration");
+    }
+    if (kernels) *kernels = 3 + k1;
+    return KC_OK;
+}
+// Multigrid-preconditioned FP32 Krylov solve (BiCGSTAB or CG) inside FP64
+// iterative refinement: r = b - A64 x in FP64, inner solve A32 d = r to
+// eps_inner from d = 0 (d accumulated in FP64), x += d, until
+// ||b - A64 x|| / ||b|| < eps.  A correction that raises the true residual is
+// undone and ends the solve with KC_STALL, as do two sweeps in a row that
+// gain less than 10 %.
+static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const double* b, double* x, const double* x0,
+                      void* mg_ws, const kc_mg_opts* mg_opts, void* ws, size_t ws_bytes, const kc_solve_opts* o,
+                      double eps_inner, int max_refine, kc_solve_info* info, void* stream) {
+    const char* name = cg ? "kc_pcg_refined" : "kc_pbicgstab_refined";
+    int rc = check_system(A64);
+    if (rc) return rc;
+    rc = check_system(A32);
+    if (rc) return rc;
+    if (A64->dtype != KC_F64 || A32->dtype != KC_F32 || A64->n != A32->n || A64->stride != A32->stride)
+        return set_error("%s: need matching FP64 and FP32 systems", name), KC_ERR_ARG;
+    if (!b || !x || !o || !mg_ws || !mg_opts) return set_error("%s: null argument", name), KC_ERR_ARG;
+    PbLayout L = pb_layout(A64->n, A64->stride);
+    if (!ws || ws_bytes < L.total) return set_error("%s: workspace %zu < %zu", name, ws_bytes, L.total), KC_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    char* base = (char*)ws;
+    BicgPtrs P{(SolverState*)(base + L.off_state), (double*)(base + L.off_partials), L.ld};
+    BicgPtrs R{(SolverState*)(base + L.off_rstate), (double*)(base + L.off_rpart), L.ld};
+    double* out2 = (double*)(base + L.off_out);
+    int* flag = (int*)(out2 + 2);
+    float* r32 = (float*)(base + L.off_r32);
+    float* fv[8];
+    for (int q = 0; q < 8; ++q) fv[q] = (float*)(base + L.off_vec[q]);
+    double* d64 = (double*)(base + L.off_x);
+    PbVecs V{fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], fv[6], fv[7], d64};
+    PcVecs W{fv[0], fv[1], {fv[2], fv[3]}, fv[4], d64};
+    const long long n = A64->n;
+    Geo g{(int)n, A64->stride};
+    dim3 sg = stencil_grid(n, A64->stride);
+    const int pb = pw_blocks(n);
+    KC_CUDA(cudaMemsetAsync(R.st, 0, sizeof(SolverState), s));
+    KC_CUDA(cudaMemsetAsync(out2, 0, 4 * sizeof(double), s));
+    if (x0) k_copy_f64<<<pb, kPwThreads, 0, s>>>((int)n, x0, x);
+    else k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);
+    KC_LAUNCH_CHECK("x0");
+    long long total = 0;
+    int status = KC_MAXITER, sweeps = 0, stalls = 0;
+    double rel = 1.0, bb = 0.0, best = INFINITY;
+    bool applied = false;
+    const StartArgs sa{eps_inner, 0, 0, KC_REL_R0, nullptr, 0, 1e30};
+    GraphKey key{ws, A32->coef, mg_ws, n, A32->stride, KC_F32, cg ? 8 : 7, 4, 2, A32->cs, A32->es};
+    for (int it = 0; it <= max_refine; ++it) {
+        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2);
+        KC_LAUNCH_CHECK("k_refine_resid");
+        double h2[3];
+        KC_CUDA(cudaMemcpyAsync(h2, out2, sizeof(h2), cudaMemcpyDeviceToHost, s));
+        KC_CUDA(cudaStreamSynchronize(s));
+        bb = h2[1];
+        rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
+        int skipped = 0;
+        memcpy(&skipped, &h2[2], sizeof(int));
+        if (applied && skipped == 0 && !(rel < best)) {
+            // the last correction raised the true residual: undo it, keep the best iterate
+            k_sub_f64<<<pb, kPwThreads, 0, s>>>((int)n, d64, x);
+            KC_LAUNCH_CHECK("undo correction");
+            rel = best;
+            status = KC_STALL;
+            break;
+        }
+        applied = false;
+        if (bb == 0.0 || rel < o->eps) {
+            status = KC_OK;
+            break;
+        }
+        if (!isfinite(rel)) {
+            status = KC_NONFINITE;
+            break;
+        }
+        if (rel >= 0.9 * best) {
+            if (++stalls >= 2) {
+                status = KC_STALL;
+                break;
+            }
+        } else {
+            stalls = 0;
+        }
+        best = std::min(best, rel);
+        if (it == max_refine || total >= o->max_iter) break;
+        // inner FP32 solve of A d = r32 from d = 0
+        StartArgs si = sa;
+        si.max_iter = o->max_iter - total;
+        KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
+        // the cold start zeroes an FP32 iterate and writes r~: both go to
+        // slots that are scratch until a V-cycle writes them
+        k_bicg_init_cold<float><<<pb, kPwThreads, 0, s>>>((int)n, r32, V.sh, V.r, V.rt, nullptr, nullptr, P, si);
+        k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, d64);
+        KC_LAUNCH_CHECK("inner init");
+        if (cg) {
+            int mk = 0;
+            rc = mg_enqueue(A32, mg_ws, mg_opts, W.r, W.z, &P.st->done, s, &mk);
+            if (rc) return rc;
+            k_pc_3<<<pb, kPwThreads, 0, s>>>((int)n, W, P);
+            KC_LAUNCH_CHECK("pcg start");
+            count_launches(mk);
+        }
+        kc_solve_opts io = *o;
+        io.max_iter = si.max_iter;
+        io.check_every = o->check_every > 0 ? o->check_every : 4;
+        int per_iter = 0;
+        if (cg) launch_pc_iters(A32, mg_ws, mg_opts, W, P, 0, s, &per_iter);
+        else launch_pb_iters(A32, mg_ws, mg_opts, V, P, 0, s, &per_iter);
+        HostState h{};
+        if (cg)
+            rc = drive(&io, key, P.st,
+                       [&](int m, cudaStream_t ss) { (void)launch_pc_iters(A32, mg_ws, mg_opts, W, P, m, ss, nullptr); },
+                       &h, s, per_iter);
+        else
+            rc = drive(&io, key, P.st,
+                       [&](int m, cudaStream_t ss) { (void)launch_pb_iters(A32, mg_ws, mg_opts, V, P, m, ss, nullptr); },
+                       &h, s, per_iter);
+        if (rc) return rc;
+        total += h.iter;
+        ++sweeps;
+        KC_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+        k_flag_nonfinite_f64<<<pb, kPwThreads, 0, s>>>((int)n, d64, flag);
+        k_add_f64<<<pb, kPwThreads, 0, s>>>((int)n, d64, x, flag);
+        KC_LAUNCH_CHECK("correction");
+        count_launches(1);
+        applied = true;
+        if (h.status != KC_OK && h.iter == 0) {
+            status = h.status;
+            break;
+        }
+    }
+    if (info) {
+        info->status = status;
+        info->refinements = sweeps;
+        info->iters = total;
+        info->rel_res = rel;
+        info->r0 = sqrt(bb);
+    }
+    return status;
+}
+
+}  // namespace kc
+
+extern "C" {
+
+size_t kc_pbicgstab_ws_bytes(long long n, int stride) {
+    if (n < 1 || stride < 1) return 0;
+    return pb_layout(n, stride).total;
+}
+
+int kc_pbicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, const double* x0,
+                         void* mg_ws, const kc_mg_opts* mg_opts, void* ws, size_t ws_bytes, const kc_solve_opts* o,
+                         double eps_inner, int max_refine, kc_solve_info* info, void* stream) {
+    return mg_refined(false, A64, A32, b, x, x0, mg_ws, mg_opts, ws, ws_bytes, o, eps_inner, max_refine, info, stream);
+}
+
+int kc_pcg_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, const double* x0,
+                   void* mg_ws, const kc_mg_opts* mg_opts, void* ws, size_t ws_bytes, const kc_solve_opts* o,
+                   double eps_inner, int max_refine, kc_solve_info* info, void* stream) {
+    return mg_refined(true, A64, A32, b, x, x0, mg_ws, mg_opts, ws, ws_bytes, o, eps_inner, max_refine, info, stream);
 }
 
 }  // extern "C"

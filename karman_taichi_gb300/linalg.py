@@ -67,8 +67,10 @@ class Stencil:
     Component order: aP, aW (k-S), aE (k+S), aN (k+1), aS (k-1).
     """
 
-    def __init__(self, coef: torch.Tensor, stride: int | None = None, layout: str | None = None):
+    def __init__(self, coef: torch.Tensor, stride: int | None = None, layout: str | None = None,
+                 form: int = L.FORM_STANDARD):
         require_cuda(coef)
+        self.form = int(form)
         if layout is None:
             layout = "aos" if (coef.dim() == 3 and coef.shape[-1] == 5 and coef.shape[0] != 5) else "soa"
         self.coef, self.layout = coef, layout
@@ -89,7 +91,7 @@ class Stencil:
             self.stride = stride
             self.shape = tuple(coef.shape[1:])
         self.dtype = dtype_code(coef)
-        self._sys = L.KcSystem(self.n, self.cs, self.es, coef.data_ptr(), int(self.stride), self.dtype)
+        self._sys = L.KcSystem(self.n, self.cs, self.es, coef.data_ptr(), int(self.stride), self.dtype, self.form)
 
     @property
     def system(self) -> L.KcSystem:
@@ -223,3 +225,74 @@ def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tenso
                                  stream_handle(b.device))
     L.check(rc, "kc_bicgstab_refined")
     return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)
+
+
+class Multigrid:
+    """Aggregation multigrid V-cycle (FP32) for a 2-D 5-point operator; the
+    right preconditioner of the mixed-precision pressure-correction solve.
+    ``omega`` / ``alpha`` are per-level smoother weights and coarse-correction
+    scales (scalars broadcast to all levels)."""
+
+    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=64, omega=1.0, alpha=1.6,
+                 max_levels=16):
+        if A32.dtype != L.F32:
+            raise TypeError("multigrid runs on FP32 coefficients")
+        self.A = A32
+        o = L.KcMgOpts()
+        o.nu_pre, o.nu_post, o.coarsest_sweeps, o.max_levels = nu_pre, nu_post, coarsest_sweeps, max_levels
+        om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
+        al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
+        for l in range(16):
+            o.omega[l] = float(om[min(l, len(om) - 1)])
+            o.alpha[l] = float(al[min(l, len(al) - 1)])
+        self.opts = o
+        lib = L.load()
+        self.ws = torch.zeros(lib.kc_mg_ws_bytes(A32.n, A32.stride, C.byref(o)), dtype=torch.uint8,
+                              device=A32.device)
+
+    def setup(self):
+        """(Re)build the coarse operators from the current fine coefficients."""
+        L.check(L.load().kc_mg_setup(C.byref(self.A.system), ptr(self.ws), self.ws.numel(), C.byref(self.opts),
+                                     stream_handle(self.A.device)), "kc_mg_setup")
+        return self
+
+    def apply(self, r: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        require_cuda(r)
+        out = torch.empty_like(r) if out is None else out
+        L.check(L.load().kc_mg_apply(C.byref(self.A.system), ptr(self.ws), C.byref(self.opts), ptr(r), ptr(out),
+                                     stream_handle(r.device)), "kc_mg_apply")
+        return out
+
+
+def _mg_refined(fn, A64, A32, b, x, mg, eps, eps_inner, max_refine, max_iter, x0, ws, use_graph, check_every):
+    require_cuda(b, x, x0)
+    lib = L.load()
+    buf = (ws or Workspace(b.device)).get(lib.kc_pbicgstab_ws_bytes(A64.n, A64.stride))
+    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_B,
+              check_every, use_graph, None, False)
+    info = L.KcSolveInfo()
+    rc = getattr(lib, fn)(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x), ptr(x0), ptr(mg.ws),
+                          C.byref(mg.opts), ptr(buf), buf.numel(), C.byref(o), float(eps_inner),
+                          int(max_refine), C.byref(info), stream_handle(b.device))
+    L.check(rc, fn)
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)
+
+
+def pbicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, mg: Multigrid, *, eps=1e-8,
+                      eps_inner=1e-4, max_refine=30, max_iter=None, x0: torch.Tensor | None = None,
+                      ws: Workspace | None = None, use_graph=True, check_every=4) -> SolveInfo:
+    """Multigrid-preconditioned FP32 BiCGSTAB (FP64 iterate and inner products)
+    inside FP64 iterative refinement; stops when ||b - A64 x|| / ||b|| < eps.
+    ``x0`` is an optional FP64 initial guess (e.g. the learned network's
+    prediction)."""
+    return _mg_refined("kc_pbicgstab_refined", A64, A32, b, x, mg, eps, eps_inner, max_refine, max_iter, x0, ws,
+                       use_graph, check_every)
+
+
+def pcg_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, mg: Multigrid, *, eps=1e-8,
+                eps_inner=1e-4, max_refine=30, max_iter=None, x0: torch.Tensor | None = None,
+                ws: Workspace | None = None, use_graph=True, check_every=4) -> SolveInfo:
+    """Multigrid-preconditioned FP32 CG (symmetric systems) inside FP64
+    iterative refinement; same contract as :func:`pbicgstab_refined`."""
+    return _mg_refined("kc_pcg_refined", A64, A32, b, x, mg, eps, eps_inner, max_refine, max_iter, x0, ws,
+                       use_graph, check_every)

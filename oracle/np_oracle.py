@@ -251,6 +251,16 @@ def _bicgstab_f32(c32, b, S, eps, max_iter):
     return SolveResult(x, OK, it, 0.0)
 
 
+def to_laplacian32(coef):
+    """FP32 copy of a standard-form stencil in Laplacian form: component 0 is
+    the row sum aP + (((aW + aE) + aN) + aS), formed in FP64 and rounded once
+    (the FP32 pressure-correction output of kc_assemble_pcorr)."""
+    c = np.asarray(coef, dtype=np.float64).reshape(5, -1)
+    out = c.astype(np.float32)
+    out[0] = (c[0] + (((c[1] + c[2]) + c[3]) + c[4])).astype(np.float32)
+    return out.reshape(np.shape(coef))
+
+
 def to_csr(coef, S):
     """Assemble the flat 5-point stencil as a scipy CSR matrix (test helper)."""
     import scipy.sparse as sp
@@ -926,3 +936,130 @@ class KarmanOracle:
         pmax = self.puv_correction()
         return dict(it_u=ru.iters, it_v=rv.iters, it_p=rp.iters, pcor_max=pmax,
                     st=(ru.status, rv.status, rp.status))
+
+
+# ----------------------------------------------------------------------------
+# Aggregation multigrid V-cycle (restatement of the GB300 preconditioner, FP32)
+# ----------------------------------------------------------------------------
+class MultigridOracle:
+    """2x2 Galerkin aggregation in Laplacian form (rows without off-diagonal
+    links are isolated: solved pointwise, never aggregated, links into them
+    folded into the row sum), red-black
+    Gauss-Seidel smoothing weighted by omega[l], coarse corrections scaled by
+    alpha[l], Jacobi sweeps on the coarsest level (<= 1024 cells)."""
+
+    COARSEST = 1024
+
+    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=64, omega=1.0, alpha=1.6, max_levels=16,
+                 lap=False):
+        f32 = np.float32
+        om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
+        al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
+        self.omega = [f32(om[min(l, len(om) - 1)]) for l in range(16)]
+        self.alpha = [f32(al[min(l, len(al) - 1)]) for l in range(16)]
+        self.nu_pre, self.nu_post, self.sweeps = nu_pre, nu_post, coarsest_sweeps
+        c = np.asarray(coef, dtype=f32).reshape(5, NX, NY)
+        self.levels = [self._level(c, NX, NY, self.omega[0], lap)]
+        while len(self.levels) < max_levels and NX * NY > self.COARSEST:
+            NXc, NYc = (NX + 1) // 2, (NY + 1) // 2
+            c = self._coarsen(c, self.levels[-1]["iso"], NX, NY, NXc, NYc, self.levels[-1]["lap"])
+            NX, NY = NXc, NYc
+            self.levels.append(self._level(c, NX, NY, self.omega[min(len(self.levels), 15)], True))
+
+    @staticmethod
+    def _level(c, NX, NY, omega, lap):
+        linked = (c[1] != 0) | (c[2] != 0) | (c[3] != 0) | (c[4] != 0)
+        d = (c[0] - (c[1] + c[2] + c[3] + c[4])).astype(np.float32) if lap else c[0]
+        with np.errstate(divide="ignore"):
+            winv = np.where(d == 0, np.float32(0), np.where(linked, omega / d, np.float32(1) / d))
+        return dict(c=c, NX=NX, NY=NY, iso=~linked, winv=winv.astype(np.float32), lap=lap)
+
+    @staticmethod
+    def _coarsen(c, iso, NXf, NYf, NXc, NYc, lapf):
+        """Galerkin coarse operator in Laplacian form [rs, aW, aE, aN, aS].
+
+        The four children of an aggregate are visited in the order
+        (0,0), (0,1), (1,0), (1,1) and each child's links in the order W, E,
+        N, S, every sum rounded to FP32 as it is formed (the order of
+        k_mg_coarsen); absent or isolated children contribute exact zeros."""
+        f = np.float32
+        # fine arrays padded to (2 NXc, 2 NYc); padded cells count as isolated
+        cp = np.zeros((5, 2 * NXc, 2 * NYc), dtype=f)
+        cp[:, :NXf, :NYf] = c
+        isop = np.ones((2 * NXc + 2, 2 * NYc + 2), dtype=bool)   # one-cell isolated frame
+        isop[1:NXf + 1, 1:NYf + 1] = iso
+        rs, aW, aE, aN, aS = (np.zeros((NXc, NYc), dtype=f) for _ in range(5))
+        for di in (0, 1):
+            for dj in (0, 1):
+                sl = (slice(di, 2 * NXc, 2), slice(dj, 2 * NYc, 2))
+                w, e, n, s_ = (cp[q][sl] for q in (1, 2, 3, 4))
+                me = ~isop[1 + di:2 * NXc + 1:2, 1 + dj:2 * NYc + 1:2]
+                isoW = isop[di:2 * NXc:2, 1 + dj:2 * NYc + 1:2]
+                isoE = isop[2 + di:2 * NXc + 2:2, 1 + dj:2 * NYc + 1:2]
+                isoN = isop[1 + di:2 * NXc + 1:2, 2 + dj:2 * NYc + 2:2]
+                isoS = isop[1 + di:2 * NXc + 1:2, dj:2 * NYc:2]
+                r = cp[0][sl].copy() if lapf else (cp[0][sl] + (((w + e) + n) + s_)).astype(f)
+                z = f(0)
+                r = (r - np.where(isoW, w, z)).astype(f)
+                r = (r - np.where(isoE, e, z)).astype(f)
+                r = (r - np.where(isoN, n, z)).astype(f)
+                r = (r - np.where(isoS, s_, z)).astype(f)
+                if di == 0:
+                    aW = (aW + np.where(me & ~isoW, w, z)).astype(f)
+                else:
+                    aE = (aE + np.where(me & ~isoE, e, z)).astype(f)
+                if dj == 1:
+                    aN = (aN + np.where(me & ~isoN, n, z)).astype(f)
+                else:
+                    aS = (aS + np.where(me & ~isoS, s_, z)).astype(f)
+                rs = (rs + np.where(me, r, z)).astype(f)
+        return np.stack([rs, aW, aE, aN, aS]).astype(f)
+
+    @staticmethod
+    def _Ax(L, x):
+        c = L["c"]
+        xw = np.zeros_like(x); xe = np.zeros_like(x); xn = np.zeros_like(x); xs = np.zeros_like(x)
+        xw[1:, :] = x[:-1, :]; xe[:-1, :] = x[1:, :]; xn[:, :-1] = x[:, 1:]; xs[:, 1:] = x[:, :-1]
+        if L["lap"]:
+            return c[0] * x + c[1] * (xw - x) + c[2] * (xe - x) + c[3] * (xn - x) + c[4] * (xs - x)
+        return c[0] * x + c[1] * xw + c[2] * xe + c[3] * xn + c[4] * xs
+
+    def _rb(self, L, b, x, color):
+        ii, jj = np.meshgrid(np.arange(L["NX"]), np.arange(L["NY"]), indexing="ij")
+        m = ((ii + jj) & 1) == color
+        r = b - self._Ax(L, x)
+        x[m] = (x + L["winv"] * r)[m]
+
+    def apply(self, r):
+        r = np.asarray(r, dtype=np.float32)
+        L0 = self.levels[0]
+        bs = [r.reshape(L0["NX"], L0["NY"])]
+        xs = []
+        nlev = len(self.levels)
+        for l, L in enumerate(self.levels):
+            b = bs[l]
+            if l == nlev - 1:
+                x = L["winv"] * b
+                for _ in range(self.sweeps):
+                    x = x + L["winv"] * (b - self._Ax(L, x))
+                xs.append(x)
+                break
+            ii, jj = np.meshgrid(np.arange(L["NX"]), np.arange(L["NY"]), indexing="ij")
+            x = np.where(((ii + jj) & 1) == 0, L["winv"] * b, np.float32(0)).astype(np.float32)
+            self._rb(L, b, x, 1)
+            for _ in range(1, self.nu_pre):
+                self._rb(L, b, x, 0); self._rb(L, b, x, 1)
+            xs.append(x)
+            res = np.where(L["iso"], np.float32(0), b - self._Ax(L, x))
+            Lc = self.levels[l + 1]
+            pad = np.zeros((2 * Lc["NX"], 2 * Lc["NY"]), dtype=np.float32)
+            pad[:L["NX"], :L["NY"]] = res
+            bs.append(pad.reshape(Lc["NX"], 2, Lc["NY"], 2).sum(axis=(1, 3)).astype(np.float32))
+        for l in range(nlev - 2, -1, -1):
+            L = self.levels[l]
+            xc = xs[l + 1]
+            up = np.repeat(np.repeat(xc, 2, axis=0), 2, axis=1)[:L["NX"], :L["NY"]]
+            xs[l] = np.where(L["iso"], xs[l], xs[l] + self.alpha[min(l, 15)] * up).astype(np.float32)
+            for _ in range(self.nu_post):
+                self._rb(L, bs[l], xs[l], 1); self._rb(L, bs[l], xs[l], 0)
+        return xs[0].reshape(-1)

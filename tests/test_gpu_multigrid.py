@@ -1,0 +1,176 @@
+"""GPU multigrid preconditioner vs its CPU restatement, and the
+multigrid-preconditioned mixed-precision solve.
+
+Tolerances: one V-cycle agrees with the FP32 NumPy restatement to 1e-4
+relative (both FP32; the GPU contracts to FMA); the refined solve meets the
+FP64 tolerance ||b - A x|| / ||b|| < 1e-8 and matches a direct solve to 1e-6.
+"""
+import numpy as np
+import pytest
+
+from oracle import np_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _channel_pcorr(nx, ny, D, ci, cj):
+    """p' system of the first outer iteration of a small channel (oracle)."""
+    from karman_taichi_gb300 import geometry
+    solid = geometry.solid_mask(nx, ny, [("square", ci, cj, D)])
+    u, v, p = geometry.channel_initial_fields(nx, ny, solid)
+    h = 1.0 / ny
+    P = O.ChannelParams(nx=nx, ny=ny, dx=h, dy=h, rho=1.0, mu=D * h / 150, dt=0.5 * h)
+    orc = O.ChannelOracle(P, solid, u, v, p)
+    orc.assemble_momentum()
+    ru = O.bicgstab(orc.coef_u, orc.b_u, orc.b_u.shape[1])
+    rv = O.bicgstab(orc.coef_v, orc.b_v, orc.b_v.shape[1])
+    orc.relax(ru.x.reshape(orc.u.shape), rv.x.reshape(orc.v.shape))
+    orc.assemble_p()
+    return orc.coef_p, orc.b_p
+
+
+def _poisson(NX, NY, block=None):
+    """Standard-form 5-point Poisson system on a padded [NX][NY] grid: halo
+    rows empty, Neumann walls, Dirichlet through the east halo, an optional
+    blocked square (identity rows, links to it removed)."""
+    c = np.zeros((5, NX, NY))
+    inner = np.zeros((NX, NY), dtype=bool)
+    inner[1:NX - 1, 1:NY - 1] = True
+    if block is not None:
+        i0, i1, j0, j1 = block
+        inner[i0:i1, j0:j1] = False
+    ii, jj = np.nonzero(inner)
+    for q, (di, dj) in zip((1, 2, 3, 4), ((-1, 0), (1, 0), (0, 1), (0, -1))):
+        ni, nj = ii + di, jj + dj
+        link = inner[ni, nj] | (ni == NX - 1)          # east halo: Dirichlet
+        c[q, ii, jj] = np.where(link, -1.0, 0.0)
+    c[0, ii, jj] = -(c[1] + c[2] + c[3] + c[4])[ii, jj]
+    if block is not None:
+        c[0, i0:i1, j0:j1] = 1.0
+    return c
+
+
+def _t(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _fp32(coef, lap):
+    from karman_taichi_gb300 import _lib as L
+    if lap:
+        return O.to_laplacian32(coef), L.FORM_LAPLACIAN
+    return coef.astype(np.float32), L.FORM_STANDARD
+
+
+@pytest.mark.parametrize("lap", [False, True])
+@pytest.mark.parametrize("alpha", [1.0, 1.6])
+def test_vcycle_matches_restatement(dev, alpha, lap):
+    from karman_taichi_gb300 import linalg
+    coef, b = _channel_pcorr(96, 40, 6, 30, 20)
+    NX, NY = coef.shape[1:]
+    c32, form = _fp32(coef, lap)
+    A = linalg.Stencil(_t(c32, dev), form=form)
+    mg = linalg.Multigrid(A, alpha=alpha).setup()
+    r = np.random.default_rng(0).standard_normal(NX * NY).astype(np.float32)
+    r[coef[0].reshape(-1) == 0] = 0.0
+    z = mg.apply(_t(r.reshape(NX, NY), dev)).cpu().numpy().reshape(-1)
+    ref = O.MultigridOracle(c32.reshape(5, -1), NX, NY, alpha=alpha, lap=lap).apply(r)
+    assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_laplacian_spmv_matches_standard(dev):
+    """The Laplacian-form FP32 stencil is the same operator (FP32 tolerance)."""
+    from karman_taichi_gb300 import linalg
+    coef, b = _channel_pcorr(96, 40, 6, 30, 20)
+    NX, NY = coef.shape[1:]
+    x = np.random.default_rng(1).standard_normal((NX, NY)).astype(np.float32)
+    c32, form = _fp32(coef, True)
+    A = linalg.Stencil(_t(c32, dev), form=form)
+    y = linalg.spmv(A, _t(x, dev)).cpu().numpy().reshape(-1)
+    ref = O.spmv(coef.reshape(5, -1), x.reshape(-1).astype(np.float64), NY)
+    assert np.abs(y - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("lap", [False, True])
+def test_mg_preconditioned_solve(dev, lap):
+    import scipy.sparse.linalg as spla
+    from karman_taichi_gb300 import linalg
+    coef, b = _channel_pcorr(256, 64, 8, 64, 32)
+    NX, NY = coef.shape[1:]
+    S = NY
+    A64 = linalg.Stencil(_t(coef, dev))
+    c32, form = _fp32(coef, lap)
+    A32 = linalg.Stencil(_t(c32, dev), form=form)
+    mg = linalg.Multigrid(A32).setup()
+    x = _t(np.zeros((NX, NY)), dev)
+    info = linalg.pbicgstab_refined(A64, A32, _t(b, dev), x, mg, eps=1e-8)
+    assert info.ok, info
+    xg = x.cpu().numpy().reshape(-1)
+    res = b.reshape(-1) - O.spmv(coef.reshape(5, -1), xg, S)
+    assert np.linalg.norm(res) / np.linalg.norm(b) < 1e-8
+    plain = O.bicgstab(coef, b, S, eps=1e-8)
+    assert info.iters * 8 < plain.iters          # the preconditioner must pay for itself
+    Acsr = O.to_csr(coef.reshape(5, -1), S)
+    rows = np.flatnonzero(coef[0].reshape(-1) != 0)
+    xs = np.zeros_like(xg)
+    xs[rows] = spla.spsolve(Acsr[rows][:, rows].tocsc(), b.reshape(-1)[rows])
+    assert np.abs(xg - xs).max() <= 1e-6 * np.abs(xs).max()
+
+
+def test_mg_initial_guess_is_used(dev):
+    """An exact initial guess finishes with zero inner iterations."""
+    from karman_taichi_gb300 import linalg
+    coef, b = _channel_pcorr(128, 32, 6, 40, 16)
+    NX, NY = coef.shape[1:]
+    A64 = linalg.Stencil(_t(coef, dev))
+    c32, form = _fp32(coef, True)
+    A32 = linalg.Stencil(_t(c32, dev), form=form)
+    mg = linalg.Multigrid(A32).setup()
+    x = _t(np.zeros((NX, NY)), dev)
+    linalg.pbicgstab_refined(A64, A32, _t(b, dev), x, mg, eps=1e-10)
+    x2 = _t(np.zeros((NX, NY)), dev)
+    info = linalg.pbicgstab_refined(A64, A32, _t(b, dev), x2, mg, eps=1e-8, x0=x)
+    assert info.ok and info.iters == 0
+
+
+def test_vcycle_matches_restatement_above_one_million_cells(dev):
+    """More cells than one grid-stride pass of the capped launch covers."""
+    from karman_taichi_gb300 import _lib as L, linalg
+    NX, NY = 1026, 1026
+    c32 = O.to_laplacian32(_poisson(NX, NY, (500, 540, 480, 520)))
+    A = linalg.Stencil(_t(c32, dev), form=L.FORM_LAPLACIAN)
+    mg = linalg.Multigrid(A).setup()
+    r = np.random.default_rng(2).standard_normal(NX * NY).astype(np.float32)
+    r[(c32[1:] == 0).all(axis=0).reshape(-1)] = 0.0
+    z = mg.apply(_t(r.reshape(NX, NY), dev)).cpu().numpy().reshape(-1)
+    ref = O.MultigridOracle(c32.reshape(5, -1), NX, NY, lap=True).apply(r)
+    assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("case", ["channel", "poisson_large"])
+def test_pcg_refined_solve(dev, case):
+    import scipy.sparse.linalg as spla
+    from karman_taichi_gb300 import _lib as L, linalg
+    if case == "channel":
+        coef, b = _channel_pcorr(256, 64, 8, 64, 32)
+    else:
+        coef = _poisson(1026, 1026, (500, 540, 480, 520))
+        b = np.random.default_rng(3).standard_normal(coef.shape[1:])
+        b[(coef[1:] == 0).all(axis=0)] = 0.0
+    NX, NY = coef.shape[1:]
+    A64 = linalg.Stencil(_t(coef, dev))
+    A32 = linalg.Stencil(_t(O.to_laplacian32(coef), dev), form=L.FORM_LAPLACIAN)
+    mg = linalg.Multigrid(A32).setup()
+    x = _t(np.zeros((NX, NY)), dev)
+    info = linalg.pcg_refined(A64, A32, _t(b, dev), x, mg, eps=1e-8)
+    assert info.ok, info
+    xg = x.cpu().numpy().reshape(-1)
+    res = b.reshape(-1) - O.spmv(coef.reshape(5, -1), xg, NY)
+    assert np.linalg.norm(res) / np.linalg.norm(b) < 1e-8
+    assert info.iters < 150, info
+    if case == "channel":
+        Acsr = O.to_csr(coef.reshape(5, -1), NY)
+        rows = np.flatnonzero(coef[0].reshape(-1) != 0)
+        xs = np.zeros_like(xg)
+        xs[rows] = spla.spsolve(Acsr[rows][:, rows].tocsc(), b.reshape(-1)[rows])
+        assert np.abs(xg - xs).max() <= 1e-6 * np.abs(xs).max()
