@@ -157,7 +157,7 @@ def resolve_mode(mode):
             return "learned"
     except ImportError:
         pass
-    return "fp64"
+    return "mixed"
 
 
 def summarize(recs_per_step):
@@ -190,10 +190,15 @@ def timed_steps(solver, K, W, world, lib, clocks=None):
     return ms, recs, lib.kc_launch_count() - l0, ck
 
 
-def e2e_steps(solver, K, world):
-    """The same steps through the public API with host-resident fields: every
-    step copies u, v, p, u0, v0 from pinned host memory and reads u, v, p back."""
+def e2e_steps(solver, K, W, world):
+    """The same time steps as the device-timed run (reset, W untimed warm-up
+    steps, K timed) through the public API with host-resident fields: every
+    timed step copies u, v, p, u0, v0 from pinned host memory and reads u, v,
+    p back."""
     import torch
+    solver.reset()
+    for _ in range(W):
+        solver.step()
     names_in = ("u", "v", "p", "u0", "v0")
     names_out = ("u", "v", "p")
     host = {k: torch.empty(getattr(solver, k).shape, dtype=torch.float64, pin_memory=True) for k in names_in}
@@ -220,9 +225,28 @@ def e2e_steps(solver, K, world):
     return ms, h2d, d2h
 
 
+# Algorithmic bytes per fine cell of one multigrid-preconditioned CG
+# iteration (FP32 vectors and coefficients, FP64 iterate), each array read or
+# written once per kernel:
+#   K1 p = z + beta p, q = A p         read z, p, 5 coef; write p, q      36
+#   K2 x += alpha p, r -= alpha q      read p, q, r, x(8); write x(8), r  32
+#   K3 (r, z)                          read r, z                           8
+#   V-cycle, level 0 (1 pre + 1 post red-black sweep):
+#     first half-sweep                 read b, winv; write x              12
+#     3 red-black half-sweeps          read x, b, 5 coef, winv (half), write half, x x3  60
+#     restrict                         read b, x, 5 coef, iso; write 1/4  30
+#     prolong                          read x, iso, 1/4; write x          10
+#   coarse levels: the level-0 V-cycle bytes x (1/4 + 1/16 + ...) = x 1/3
+PCG_MG_BYTES_PER_CELL = 36 + 32 + 8 + round((12 + 60 + 30 + 10) * 4 / 3)
+
+
 def roofline_p_solve(solver, mode, peak):
-    """Dominant kernel: the p' BiCGSTAB solve (one persistent launch doing all
-    iterations).  achieved = 27 words/cell/iteration x iterations / duration."""
+    """Roofline of the dominant unit of work, the pressure-correction solve.
+
+    fp64: one persistent BiCGSTAB launch, 27 words/cell/iteration.
+    mixed: the multigrid-preconditioned CG (kernels K1, K2, K3 and the V-cycle
+    per iteration), PCG_MG_BYTES_PER_CELL bytes/cell/iteration; the FP64
+    refinement residuals add 2 x (5 coef + x + b) x 8 B per cell."""
     import torch
     solver.assemble_momentum()
     solver.solve_momentum()
@@ -231,15 +255,21 @@ def roofline_p_solve(solver, mode, peak):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    info = solver._solve(solver.A_p, getattr(solver, "A_p32", None), solver.b_p, solver.pcor, solver.ws_p)
+    info = solver.solve_p()
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     n = solver.A_p.n
-    w = 8 if mode == "fp64" else 4
-    alg = 27 * w * n * info.iters
+    if mode == "fp64":
+        alg = 27 * 8 * n * info.iters
+        kernel = "k_bicg_persist<double>"
+        note = "27 words/cell/iteration (A 9R+2W, B 7R+1W, C 6R+2W)"
+    else:
+        alg = PCG_MG_BYTES_PER_CELL * n * info.iters + (info.refinements + 1) * 7 * 8 * n
+        kernel = "kc_pcg_refined (k_pc_1/2/3 + multigrid V-cycle)"
+        note = (f"{PCG_MG_BYTES_PER_CELL} B/cell/PCG iteration (K1 36, K2 32, K3 8, V-cycle 150) + "
+                f"56 B/cell per FP64 refinement residual")
     achieved = alg / (ms * 1e-3) / 1e9
-    kernel = "k_bicg_persist<double>" if mode == "fp64" else "k_bicg_persist<float>"
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -251,7 +281,7 @@ def roofline_p_solve(solver, mode, peak):
     return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "algorithmic_bytes": alg, "iters": info.iters, "ms": round(ms, 3),
-            "note": "27 words/cell/iteration (A 9R+2W, B 7R+1W, C 6R+2W); peak = measured hbm_gbs (burst)"}
+            "note": note + "; peak = hbm_gbs of MEASURED_PEAKS.json (burst)"}
 
 
 def cpu_sample(cfg, budget_s, iters_per_step):
@@ -338,28 +368,36 @@ def run_gpu(args):
     out["stats"] = summ
 
     if rank == 0 and not args.no_e2e:
-        e2e_ms, h2d, d2h = e2e_steps(solver, max(1, args.steps // 2), 1)
-        k = max(1, args.steps // 2)
-        out["e2e"] = {"value": round(k / (e2e_ms * 1e-3), 5), "unit": "time steps/s",
+        e2e_ms, h2d, d2h = e2e_steps(solver, args.steps, args.warmup, 1)
+        out["e2e"] = {"value": round(args.steps / (e2e_ms * 1e-3), 5), "unit": "time steps/s",
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                      "note": "public ChannelSolver.step() with u, v, p, u0, v0 copied from pinned host memory "
-                              "and u, v, p read back every step"}
+                      "note": "the same K time steps (after reset + W warm-up) through the public "
+                              "ChannelSolver.step() with u, v, p, u0, v0 copied from pinned host memory and "
+                              "u, v, p read back every step"}
     if rank == 0:
         out["roofline"] = roofline_p_solve(solver, mode, peak)
         out["roofline"]["peak_kind"] = peak_kind
 
     fp64_counts = summ if mode == "fp64" else None
     if rank == 0 and not args.no_compare and mode != "fp64":
+        # plain FP64 BiCGSTAB on the same GPU: the same first W + C time steps
+        C = args.compare_steps
         ref = make_solver(cfg, "fp64", dev)
-        cms, crecs, _, _ = timed_steps(ref, args.compare_steps, args.warmup, 1, lib)
+        cms, crecs, _, _ = timed_steps(ref, C, args.warmup, 1, lib)
         fp64_counts = summarize(crecs)
-        out["fp64_plain"] = {"value": round(args.compare_steps / (cms * 1e-3), 5), "unit": "time steps/s",
-                             "ms_per_step": round(cms / args.compare_steps, 3), "steps": args.compare_steps,
+        out["fp64_plain"] = {"value": round(C / (cms * 1e-3), 5), "unit": "time steps/s",
+                             "ms_per_step": round(cms / C, 3), "steps": C,
                              "warmup": args.warmup, "stats": fp64_counts}
         out["speedup_vs_fp64_plain"] = round(value / out["fp64_plain"]["value"], 3)
+        # field error after the same W + C steps from the same initial state
+        solver.reset()
+        for _ in range(args.warmup + C):
+            solver.step()
         a, b = solver.state_numpy(), ref.state_numpy()
         out["field_error_vs_fp64"] = {k: float(abs(a[k] - b[k]).max() / max(abs(b[k]).max(), 1e-300))
                                       for k in ("u", "v", "p")}
+        out["field_error_vs_fp64"]["after_steps"] = args.warmup + C
+        out["field_error_vs_fp64"]["definition"] = "max |x - x_fp64| / max |x_fp64| over the padded field"
     if rank == 0 and fp64_counts:
         save_counts(cfg.name, {"solver_iters_per_step": fp64_counts["solver_iters_per_step"],
                                "outer_per_step": fp64_counts["outer_per_step"],

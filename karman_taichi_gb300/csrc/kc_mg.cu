@@ -22,7 +22,9 @@
 //   * coarsest level (<= kCoarsestMax cells): Jacobi sweeps in shared memory
 //     by one block.
 // Level 0 is the caller's system (n = NX*NY, far stride NY); levels >= 1 live
-// in the multigrid workspace.  All kernels take an optional "done" word and
+// in the multigrid workspace.  The cycle treats every level as a 2-D
+// [NX][NY] grid with zero values outside it (a link across the end of a row
+// of the flat stencil is a link to a zero cell).  All kernels take an optional "done" word and
 // return at once when it is set, so a solver that converged mid-chunk skips
 // the remaining preconditioner work of a captured graph.
 #include "kc_common.cuh"
@@ -113,9 +115,10 @@ struct Lvl {
 __device__ __forceinline__ float mg_Ax(const Lvl& L, const float* __restrict__ x, int k) {
     const long long e = (long long)k * L.es;
     const int n = L.NX * L.NY;
+    const int j = k % L.NY;
     const float xk = x[k];
     const float xw = k >= L.NY ? x[k - L.NY] : 0.f, xe = k + L.NY < n ? x[k + L.NY] : 0.f;
-    const float xn = k + 1 < n ? x[k + 1] : 0.f, xs = k >= 1 ? x[k - 1] : 0.f;
+    const float xn = j + 1 < L.NY ? x[k + 1] : 0.f, xs = j >= 1 ? x[k - 1] : 0.f;
     float y = __ldg(L.c + e) * xk;
     if (L.lap) {
         y = fmaf(__ldg(L.c + L.cs + e), xw - xk, y);
@@ -209,8 +212,9 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
         if (k < n) {
             const float* xv = xs[cur];
             const float xk = xv[k];
+            const int j = k % L.NY;
             const float xw = k >= L.NY ? xv[k - L.NY] : 0.f, xe = k + L.NY < n ? xv[k + L.NY] : 0.f;
-            const float xn = k + 1 < n ? xv[k + 1] : 0.f, xso = k >= 1 ? xv[k - 1] : 0.f;
+            const float xn = j + 1 < L.NY ? xv[k + 1] : 0.f, xso = j >= 1 ? xv[k - 1] : 0.f;
             float y = c[0] * xk;
             if (L.lap) y += c[1] * (xw - xk) + c[2] * (xe - xk) + c[3] * (xn - xk) + c[4] * (xso - xk);
             else y += c[1] * xw + c[2] * xe + c[3] * xn + c[4] * xso;
@@ -221,6 +225,25 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
     }
     if (k < n) x[k] = xs[cur][k];
 }
+
+// ---- fused cycle kernels (one pre- and one post-sweep per level) ---------------------
+template <int TI, int TJ, int NT>
+__global__ void __launch_bounds__(NT) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
+                                                float* __restrict__ bc, int NXc, int NYc, const int* done) {
+    if (mg_done(done)) return;
+    mg_down_tile<TI, TJ, NT>(L, MgBLoad{b}, MgOwnNone{}, xout, bc, NXc, NYc);
+}
+
+template <int TI, int TJ, int NT>
+__global__ void __launch_bounds__(NT) k_mg_up(MgLvl L, const float* __restrict__ xpre, const float* __restrict__ xc,
+                                              int NYc, float alpha, const float* __restrict__ b,
+                                              float* __restrict__ xout, const int* done) {
+    if (mg_done(done)) return;
+    mg_up_tile<TI, TJ, NT>(L, xpre, xc, NYc, alpha, MgBLoad{b}, MgOwnNone{}, xout);
+}
+
+// large levels use 16 x 64 tiles, small ones 8 x 32 (more blocks in flight)
+static inline bool mg_big(int NX, int NY) { return (long long)NX * NY >= 200000; }
 
 // ---- host ----------------------------------------------------------------------------
 static int mg_levels(int NX, int NY, const kc_mg_opts* o, int* nx, int* ny) {
@@ -283,6 +306,38 @@ static Lvl level_of(const MgLayout& M, char* base, int l, const float* c0, long 
     return L;
 }
 
+static MgLvl mg_lvl(const Lvl& L) { return MgLvl{L.c, L.cs, L.es, L.NX, L.NY, L.lap, L.winv, L.iso}; }
+
+static bool mg_fusable(const MgLayout& M, const kc_mg_opts* o) {
+    return o->nu_pre == 1 && o->nu_post == 1 && M.levels >= 2;
+}
+
+static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, float* xout, float* bc, const int* done,
+                       cudaStream_t s) {
+    const MgLvl G = mg_lvl(L);
+    if (l == 0 || mg_big(L.NX, L.NY))
+        k_mg_down<kMgTI0, kMgTJ0, kMgNT0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+            G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
+    else
+        k_mg_down<8, 32, 128><<<mg_tile_grid(L.NX, L.NY, 8, 32), 128, 0, s>>>(G, b, xout, bc, M.nx[l + 1],
+                                                                             M.ny[l + 1], done);
+    KC_LAUNCH_CHECK_NC("k_mg_down");
+    return KC_OK;
+}
+
+static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, const float* xc, float alpha,
+                     const float* b, float* xout, const int* done, cudaStream_t s) {
+    const MgLvl G = mg_lvl(L);
+    if (l == 0 || mg_big(L.NX, L.NY))
+        k_mg_up<kMgTI0, kMgTJ0, kMgNT0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+            G, xpre, xc, M.ny[l + 1], alpha, b, xout, done);
+    else
+        k_mg_up<8, 32, 128><<<mg_tile_grid(L.NX, L.NY, 8, 32), 128, 0, s>>>(G, xpre, xc, M.ny[l + 1], alpha, b,
+                                                                           xout, done);
+    KC_LAUNCH_CHECK_NC("k_mg_up");
+    return KC_OK;
+}
+
 static inline unsigned pw_grid(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096)); }
 
 int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o, cudaStream_t s) {
@@ -312,6 +367,70 @@ int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o,
     return KC_OK;
 }
 
+int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o) {
+    const int NY = A->stride;
+    const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
+    if (mg_fusable(M, o)) return 2 * (M.levels - 1) + 1;
+    const int down = 2 + 2 * std::max(0, o->nu_pre - 1) + 1, up = 1 + 2 * std::max(0, o->nu_post);
+    return (M.levels - 1) * (down + up) + 1;
+}
+
+// output of level l in the fused cycle (the caller's z for level 0)
+static float* mg_final(const MgLayout& M, char* base, int l) { return (float*)(base + M.off_t[l]); }
+
+MgFused mg_fused(const kc_system* A, void* ws, const kc_mg_opts* o) {
+    MgFused F{};
+    const int NY = A->stride;
+    const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
+    F.ok = mg_fusable(M, o);
+    if (!F.ok) return F;
+    char* base = (char*)ws;
+    F.L0 = mg_lvl(level_of(M, base, 0, (const float*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN));
+    F.x0pre = (float*)(base + M.off_x[0]);
+    F.b1 = (float*)(base + M.off_b[1]);
+    F.final1 = mg_final(M, base, 1);
+    F.NX1 = M.nx[1];
+    F.NY1 = M.ny[1];
+    F.alpha0 = o->alpha[0];
+    return F;
+}
+
+// levels >= 1 of the fused cycle: b_1 in, final_1 out
+int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const int* done, cudaStream_t s,
+                      int* kernels) {
+    const int NY = A->stride;
+    const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
+    char* base = (char*)ws;
+    const float* c0 = (const float*)A->coef;
+    const int lap0 = A->form == KC_FORM_LAPLACIAN;
+    int nk = 0, rc;
+    for (int l = 1; l + 1 < M.levels; ++l) {
+        const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
+        rc = launch_down(M, L, l, (const float*)(base + M.off_b[l]), (float*)(base + M.off_x[l]),
+                         (float*)(base + M.off_b[l + 1]), done, s);
+        if (rc) return rc;
+        ++nk;
+    }
+    {
+        const int l = M.levels - 1;
+        const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
+        k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, (const float*)(base + M.off_b[l]), mg_final(M, base, l),
+                                                 o->coarsest_sweeps, done);
+        KC_LAUNCH_CHECK_NC("k_mg_coarsest");
+        ++nk;
+    }
+    for (int l = M.levels - 2; l >= 1; --l) {
+        const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
+        rc = launch_up(M, L, l, (const float*)(base + M.off_x[l]), mg_final(M, base, l + 1),
+                       o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], (const float*)(base + M.off_b[l]),
+                       mg_final(M, base, l), done, s);
+        if (rc) return rc;
+        ++nk;
+    }
+    if (kernels) *kernels = nk;
+    return KC_OK;
+}
+
 // Enqueues one V-cycle z = M r (level-0 input r, output z; both n floats).
 int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r, float* z, const int* done,
                cudaStream_t s, int* kernels) {
@@ -320,6 +439,18 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
     const int NX = (int)(A->n / NY);
     MgLayout M = mg_layout(NX, NY, o);
     char* base = (char*)ws;
+    if (mg_fusable(M, o)) {
+        const Lvl L0 = level_of(M, base, 0, (const float*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
+        int rc = launch_down(M, L0, 0, r, (float*)(base + M.off_x[0]), (float*)(base + M.off_b[1]), done, s);
+        if (rc) return rc;
+        int kc = 0;
+        rc = mg_enqueue_coarse(A, ws, o, done, s, &kc);
+        if (rc) return rc;
+        rc = launch_up(M, L0, 0, (const float*)(base + M.off_x[0]), mg_final(M, base, 1), o->alpha[0], r, z, done, s);
+        if (rc) return rc;
+        if (kernels) *kernels = kc + 2;
+        return KC_OK;
+    }
     const float* c0 = (const float*)A->coef;
     const float* bl[KC_MG_MAX_LEVELS];
     float* xl[KC_MG_MAX_LEVELS];

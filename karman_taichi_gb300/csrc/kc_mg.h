@@ -3,8 +3,17 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "karman_gb300.h"
+#include "kc_mg_tile.cuh"
 
 namespace kc {
+
+// level-0 tile of the fused cycle (also used by the preconditioned CG's fused level-0 kernels)
+constexpr int kMgTI0 = 16, kMgTJ0 = 64, kMgNT0 = 256;
+inline dim3 mg_tile_grid(int NX, int NY, int TI, int TJ) { return dim3((NY + TJ - 1) / TJ, (NX + TI - 1) / TI); }
+inline int mg_fused_blocks0(long long n, int S) {
+    const dim3 g = mg_tile_grid((int)(n / S), S, kMgTI0, kMgTJ0);
+    return (int)(g.x * g.y);
+}
 
 struct MgLayout {
     int levels;
@@ -15,6 +24,26 @@ struct MgLayout {
 };
 
 MgLayout mg_layout(int NX, int NY, const kc_mg_opts* o);
+// number of kernels one mg_enqueue launches for A
+int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o);
+
+// The fused cycle (one pre- and one post-sweep per level, at least two
+// levels) split at level 0, for solvers that fuse their own pointwise work
+// into the level-0 launches: the caller's level-0 DOWN writes x0pre and b1,
+// mg_enqueue_coarse runs levels >= 1 and leaves their result in final1, the
+// caller's level-0 UP prolongs final1 with alpha0.
+struct MgFused {
+    bool ok;
+    MgLvl L0;
+    float* x0pre;
+    float* b1;
+    const float* final1;
+    int NX1, NY1;
+    float alpha0;
+};
+MgFused mg_fused(const kc_system* A, void* ws, const kc_mg_opts* o);
+int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const int* done, cudaStream_t s,
+                      int* kernels);
 int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o, cudaStream_t s);
 // Enqueues z = M r; kernels return at once when *done != 0 (done may be
 // null).  Launches are not counted: *kernels (if not null) receives their number.

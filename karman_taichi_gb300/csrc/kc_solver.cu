@@ -1400,9 +1400,43 @@ __global__ void __launch_bounds__(kPwThreads) k_pb_x(int n, PbVecs V, BicgPtrs P
 // is K0 (r = b, x = 0, (r, r)), M, K3.
 // =============================================================================
 struct PcVecs {
-    float *r, *z, *p[2], *q;
+    float *r[2], *z, *p[2], *q;   // r: ping-pong pair in the fused level-0 path, r[0] otherwise
     double* x;
 };
+
+// called by thread 0 of the last block once (r, r) of the new residual is known
+__device__ __forceinline__ void pc_finish_iteration(SolverState* st, double nw) {
+    st->iter += 1;
+    st->rTr = nw;
+    record_history(st, st->iter, nw);
+    const double rel = st->den > 0.0 ? sqrt(nw / st->den) : 0.0;
+    st->prev_rel = rel;
+    if (rel < st->eps) {
+        st->status = KC_OK;
+        st->done = 1;
+    } else if (!isfinite(nw)) {
+        st->status = KC_NONFINITE;
+        st->done = 1;
+    } else if (st->iter >= st->max_iter) {
+        st->status = KC_MAXITER;
+        st->done = 1;
+    }
+}
+
+// called by thread 0 of the last block once (r, z) is known
+__device__ __forceinline__ void pc_finish_rz(SolverState* st, double rz) {
+    if (!(rz > 0.0)) {  // (r, M r) <= 0: M is not positive definite
+        st->status = isfinite(rz) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+        st->done = 1;
+    } else {
+        if (st->iter > 0) {
+            const double beta = rz / st->old;
+            st->beta = beta;
+            st->beta_f = (float)beta;
+        }
+        st->old = rz;
+    }
+}
 
 struct PolPc1 {
     static constexpr bool kAux = true;
@@ -1452,31 +1486,17 @@ __global__ void __launch_bounds__(kPwThreads) k_pc_2(int n, PcVecs V, BicgPtrs P
     const float alpha = __ldcg(&st->alpha_f);
     const double alpha_d = __ldcg(&st->alpha);
     Acc<float> acc[1];
+    float* __restrict__ r = V.r[0];
     KC_PW_LOOP(n, {
         const float pk = __ldg(p + k);
         V.x[k] = fma(alpha_d, (double)pk, V.x[k]);
-        const float rn = fmaf(-alpha, __ldg(V.q + k), V.r[k]);
-        V.r[k] = rn;
+        const float rn = fmaf(-alpha, __ldg(V.q + k), r[k]);
+        r[k] = rn;
         acc[0].add(rn, rn);
     })
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
-        const double nw = s[0];
-        st->iter += 1;
-        st->rTr = nw;
-        record_history(st, st->iter, nw);
-        const double rel = st->den > 0.0 ? sqrt(nw / st->den) : 0.0;
-        st->prev_rel = rel;
-        if (rel < st->eps) {
-            st->status = KC_OK;
-            st->done = 1;
-        } else if (!isfinite(nw)) {
-            st->status = KC_NONFINITE;
-            st->done = 1;
-        } else if (st->iter >= st->max_iter) {
-            st->status = KC_MAXITER;
-            st->done = 1;
-        }
+        pc_finish_iteration(st, s[0]);
         st->ticket[0] = 0;
     }
 }
@@ -1486,21 +1506,84 @@ __global__ void __launch_bounds__(kPwThreads) k_pc_3(int n, PcVecs V, BicgPtrs P
     SolverState* st = P.st;
     if (solver_done(st)) return;
     Acc<float> acc[1];
-    KC_PW_LOOP(n, { acc[0].add(__ldg(V.r + k), __ldg(V.z + k)); })
+    KC_PW_LOOP(n, { acc[0].add(__ldg(V.r[0] + k), __ldg(V.z + k)); })
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], s) && threadIdx.x == 0) {
-        const double rz = s[0];
-        if (!(rz > 0.0)) {  // (r, M r) <= 0: M is not positive definite
-            st->status = isfinite(rz) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
-            st->done = 1;
-        } else {
-            if (__ldcg(&st->iter) > 0) {
-                const double beta = rz / st->old;
-                st->beta = beta;
-                st->beta_f = (float)beta;
-            }
-            st->old = rz;
-        }
+        pc_finish_rz(st, s[0]);
+        st->ticket[0] = 0;
+    }
+}
+
+// ---- fused level 0: CG's pointwise passes inside the V-cycle's level-0 tiles ----
+// DOWN_0 with update: b = r_new = r_old - alpha q is formed per cell (halo
+// included) from the previous residual, owned cells store r_new, advance
+// x += alpha p and accumulate (r_new, r_new) -- pass K2.  r alternates
+// between two buffers so no block reads a residual another block rewrote.
+// Without update (the start) b = r_0.
+struct PcDownSrc {
+    const float* __restrict__ r_in;
+    const float* __restrict__ q;
+    float alpha;
+    bool update;
+    __device__ __forceinline__ float operator()(int k) const {
+        const float r = __ldg(r_in + k);
+        return update ? fmaf(-alpha, __ldg(q + k), r) : r;
+    }
+};
+struct PcDownOwn {
+    float* __restrict__ r_out;
+    double* __restrict__ x;
+    const float* __restrict__ p;
+    double alpha;
+    Acc<float>* acc;
+    bool update;
+    __device__ __forceinline__ void operator()(int k, float rn) const {
+        if (!update) return;
+        r_out[k] = rn;
+        x[k] = fma(alpha, (double)__ldg(p + k), x[k]);
+        acc->add(rn, rn);
+    }
+};
+
+template <int TI, int TJ, int NT>
+__global__ void __launch_bounds__(NT) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1, int NX1,
+                                                  int NY1, PcVecs V, BicgPtrs P, int update) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const long long it = __ldcg(&st->iter);
+    const int cur = (int)(it & 1);
+    Acc<float> acc[1];
+    const PcDownSrc src{V.r[cur], V.q, __ldcg(&st->alpha_f), update != 0};
+    const PcDownOwn own{V.r[cur ^ 1], V.x, V.p[cur ^ 1], __ldcg(&st->alpha), &acc[0], update != 0};
+    mg_down_tile<TI, TJ, NT>(L, src, own, x0pre, b1, NX1, NY1);
+    if (!update) return;
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        pc_finish_iteration(st, s[0]);
+        st->ticket[0] = 0;
+    }
+}
+
+// UP_0 writes z and accumulates (r, z) -- pass K3
+struct PcUpOwn {
+    Acc<float>* acc;
+    __device__ __forceinline__ void operator()(int, float z, float r) const { acc->add(r, z); }
+};
+
+template <int TI, int TJ, int NT>
+__global__ void __launch_bounds__(NT) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
+                                                const float* __restrict__ final1, int NY1, float alpha0, PcVecs V,
+                                                BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const long long it = __ldcg(&st->iter);
+    Acc<float> acc[1];
+    mg_up_tile<TI, TJ, NT>(L, x0pre, final1, NY1, alpha0, MgBLoad{V.r[(int)(it & 1)]}, PcUpOwn{&acc[0]}, V.z);
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
+        threadIdx.x == 0) {
+        pc_finish_rz(st, s[0]);
         st->ticket[0] = 0;
     }
 }
@@ -2069,6 +2152,7 @@ static PbLayout pb_layout(long long n, int S) {
     PbLayout L{};
     dim3 g = stencil_grid(n, std::max(S, 1));
     int nb = std::max<int>((int)(g.x * g.y), pw_blocks(n));
+    nb = std::max(nb, mg_fused_blocks0(n, std::max(S, 1)));
     L.ld = (int)align256((size_t)nb * 8) / 8;
     size_t off = 0;
     L.off_state = off;
@@ -2126,17 +2210,36 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
     const int pb = pw_blocks(A32->n);
     Coef<float> C = coef_of<float>(A32);
     const int* done = &P.st->done;
+    const MgFused F = mg_fused(A32, mg_ws, mo);
     int k1 = 0;
     for (int q = 0; q < m; ++q) {
         k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
-        k_pc_2<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
-        int rc = mg_enqueue(A32, mg_ws, mo, V.r, V.z, done, s, &k1);
-        if (rc) return rc;
-        k_pc_3<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
-        KC_LAUNCH_CHECK_NC("preconditioned CG iteration");
+        if (F.ok) {
+            // K2 and K3 ride in the V-cycle's level-0 launches
+            const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
+            k_pcf_down0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1);
+            KC_LAUNCH_CHECK_NC("k_pcf_down0");
+            int rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
+            if (rc) return rc;
+            k_pcf_up0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NY1, F.alpha0, V, P);
+            KC_LAUNCH_CHECK_NC("k_pcf_up0");
+            k1 += 2;
+        } else {
+            k_pc_2<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+            int rc = mg_enqueue(A32, mg_ws, mo, V.r[0], V.z, done, s, &k1);
+            if (rc) return rc;
+            k_pc_3<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
+            KC_LAUNCH_CHECK_NC("preconditioned CG iteration");
+            k1 += 2;
+        }
     }
-    if (kernels) *kernels = 3 + k1;
+    if (kernels) *kernels = 1 + k1;
     return KC_OK;
+}
+
+// number of kernels one preconditioned CG iteration launches
+static int pc_iter_kernels(const kc_system* A32, void* mg_ws, const kc_mg_opts* mo) {
+    return 1 + mg_cycle_kernels(A32, mo) + (mg_fused(A32, mg_ws, mo).ok ? 0 : 2);
 }
 // Multigrid-preconditioned FP32 Krylov solve (BiCGSTAB or CG) inside FP64
 // iterative refinement: r = b - A64 x in FP64, inner solve A32 d = r to
@@ -2168,7 +2271,7 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     for (int q = 0; q < 8; ++q) fv[q] = (float*)(base + L.off_vec[q]);
     double* d64 = (double*)(base + L.off_x);
     PbVecs V{fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], fv[6], fv[7], d64};
-    PcVecs W{fv[0], fv[1], {fv[2], fv[3]}, fv[4], d64};
+    PcVecs W{{fv[0], fv[5]}, fv[1], {fv[2], fv[3]}, fv[4], d64};
     const long long n = A64->n;
     Geo g{(int)n, A64->stride};
     dim3 sg = stencil_grid(n, A64->stride);
@@ -2231,19 +2334,29 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
         k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, d64);
         KC_LAUNCH_CHECK("inner init");
         if (cg) {
+            // z_0 = M r_0 and (r_0, z_0)
+            const MgFused F = mg_fused(A32, mg_ws, mg_opts);
             int mk = 0;
-            rc = mg_enqueue(A32, mg_ws, mg_opts, W.r, W.z, &P.st->done, s, &mk);
-            if (rc) return rc;
-            k_pc_3<<<pb, kPwThreads, 0, s>>>((int)n, W, P);
-            KC_LAUNCH_CHECK("pcg start");
+            if (F.ok) {
+                const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
+                k_pcf_down0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, W, P, 0);
+                KC_LAUNCH_CHECK("k_pcf_down0");
+                rc = mg_enqueue_coarse(A32, mg_ws, mg_opts, &P.st->done, s, &mk);
+                if (rc) return rc;
+                k_pcf_up0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NY1, F.alpha0, W, P);
+                KC_LAUNCH_CHECK("k_pcf_up0");
+            } else {
+                rc = mg_enqueue(A32, mg_ws, mg_opts, W.r[0], W.z, &P.st->done, s, &mk);
+                if (rc) return rc;
+                k_pc_3<<<pb, kPwThreads, 0, s>>>((int)n, W, P);
+                KC_LAUNCH_CHECK("pcg start");
+            }
             count_launches(mk);
         }
         kc_solve_opts io = *o;
         io.max_iter = si.max_iter;
         io.check_every = o->check_every > 0 ? o->check_every : 4;
-        int per_iter = 0;
-        if (cg) launch_pc_iters(A32, mg_ws, mg_opts, W, P, 0, s, &per_iter);
-        else launch_pb_iters(A32, mg_ws, mg_opts, V, P, 0, s, &per_iter);
+        const int per_iter = cg ? pc_iter_kernels(A32, mg_ws, mg_opts) : 5 + 2 * mg_cycle_kernels(A32, mg_opts);
         HostState h{};
         if (cg)
             rc = drive(&io, key, P.st,
