@@ -227,22 +227,23 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
 }
 
 // ---- fused cycle kernels (one pre- and one post-sweep per level) ---------------------
-template <int TI, int TJ, int NT>
-__global__ void __launch_bounds__(NT) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
-                                                float* __restrict__ bc, int NXc, int NYc, const int* done) {
+template <int TI, int AJ, int RY>
+__global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
+                                                     float* __restrict__ bc, int NXc, int NYc, const int* done) {
     if (mg_done(done)) return;
-    mg_down_tile<TI, TJ, NT>(L, MgBLoad{b}, MgOwnNone{}, xout, bc, NXc, NYc);
+    mg_down_tile<TI, AJ, RY, false>(L, b, nullptr, 0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc);
 }
 
-template <int TI, int TJ, int NT>
-__global__ void __launch_bounds__(NT) k_mg_up(MgLvl L, const float* __restrict__ xpre, const float* __restrict__ xc,
-                                              int NYc, float alpha, const float* __restrict__ b,
-                                              float* __restrict__ xout, const int* done) {
+template <int TI, int AJ, int RY>
+__global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restrict__ xpre,
+                                                   const float* __restrict__ xc, int NXc, int NYc, float alpha,
+                                                   const float* __restrict__ b, float* __restrict__ xout,
+                                                   const int* done) {
     if (mg_done(done)) return;
-    mg_up_tile<TI, TJ, NT>(L, xpre, xc, NYc, alpha, MgBLoad{b}, MgOwnNone{}, xout);
+    mg_up_tile<TI, AJ, RY>(L, xpre, xc, NXc, NYc, alpha, b, MgOwnNone{}, xout);
 }
 
-// large levels use 16 x 64 tiles, small ones 8 x 32 (more blocks in flight)
+// large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
 static inline bool mg_big(int NX, int NY) { return (long long)NX * NY >= 200000; }
 
 // ---- host ----------------------------------------------------------------------------
@@ -316,11 +317,11 @@ static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, f
                        cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_down<kMgTI0, kMgTJ0, kMgNT0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+        k_mg_down<kMgTI0, kMgAJ0, kMgRY0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
             G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
     else
-        k_mg_down<8, 32, 128><<<mg_tile_grid(L.NX, L.NY, 8, 32), 128, 0, s>>>(G, b, xout, bc, M.nx[l + 1],
-                                                                             M.ny[l + 1], done);
+        k_mg_down<kMgTI1, kMgAJ1, kMgRY1><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
+            G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
     KC_LAUNCH_CHECK_NC("k_mg_down");
     return KC_OK;
 }
@@ -329,11 +330,11 @@ static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, 
                      const float* b, float* xout, const int* done, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_up<kMgTI0, kMgTJ0, kMgNT0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
-            G, xpre, xc, M.ny[l + 1], alpha, b, xout, done);
+        k_mg_up<kMgTI0, kMgAJ0, kMgRY0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+            G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
     else
-        k_mg_up<8, 32, 128><<<mg_tile_grid(L.NX, L.NY, 8, 32), 128, 0, s>>>(G, xpre, xc, M.ny[l + 1], alpha, b,
-                                                                           xout, done);
+        k_mg_up<kMgTI1, kMgAJ1, kMgRY1><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
+            G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
     KC_LAUNCH_CHECK_NC("k_mg_up");
     return KC_OK;
 }

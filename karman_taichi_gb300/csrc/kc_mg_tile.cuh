@@ -17,9 +17,16 @@
 // exchanged, so a launch has no inter-block dependence.  The operator is the
 // 2-D 5-point stencil with zero values outside [0,NX) x [0,NY).
 //
-// The level-0 launches of the preconditioned CG fold CG's pointwise passes in
-// through the BSrc (where b comes from) and Own (what happens to each owned
-// cell) policies.
+// Staging is asynchronous (cp.async, zero-filled outside the grid): every
+// thread issues all of its copies before waiting, so a block has its whole
+// tile in flight at once -- the kernels are bound by memory latency
+// otherwise.  (A tensor-map TMA box needs 16-byte row pitches, which the
+// padded [nx+2][ny+2] fields do not have in general.)
+//
+// The level-0 launches of the preconditioned CG fold CG's pointwise passes in:
+// DOWN_0 forms b = r - alpha q from two staged arrays and hands every owned
+// cell to an Own policy; a Mid policy runs between issuing and awaiting the
+// copies (CG's x update, whose loads then overlap the staging).
 #pragma once
 #include "kc_common.cuh"
 
@@ -33,6 +40,15 @@ struct MgLvl {
     const float* winv;     // smoother weights (1/d for isolated rows)
     const unsigned char* iso;
 };
+
+// ---- asynchronous global -> shared copies (zero fill when !valid) -------------
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 __device__ __forceinline__ float mg_row(float c0, float cw, float ce, float cn, float cs_, int lap, float x,
                                         float xw, float xe, float xn, float xs) {
@@ -51,164 +67,197 @@ __device__ __forceinline__ float mg_row(float c0, float cw, float ce, float cn, 
     return y;
 }
 
-// b from a plain array
-struct MgBLoad {
-    const float* __restrict__ b;
-    __device__ __forceinline__ float operator()(int k) const { return __ldg(b + k); }
+struct MgNoMid {
+    __device__ __forceinline__ void operator()() const {}
 };
+// Own policies see every owned cell once and may accumulate into a per-thread
+// value of type Own::Sum, which the tile function returns.
 struct MgOwnNone {
-    __device__ __forceinline__ void operator()(int, float) const {}
-    __device__ __forceinline__ void operator()(int, float, float) const {}
+    struct Sum {};
+    __device__ __forceinline__ void operator()(int, float, Sum&) const {}
+    __device__ __forceinline__ void operator()(int, float, float, Sum&) const {}
 };
 
-template <int TI, int TJ>
-struct MgTileDims {
-    static constexpr int AI = TI + 4, AJ = TJ + 4;   // 2-cell halo
-    static constexpr int CI = TI + 2, CJ = TJ + 2;   // 1-cell halo
+// Tile geometry: rows of AJ = 32 or 64 staged cells (TJ = AJ - 4 owned
+// columns plus the 2-cell halo on each side), so a row is one or two warps
+// and every index is a shift; RY thread rows walk the AI = TI + 4 staged rows.
+// All staged arrays share the [AI][AJ] layout.  i0 and j0 are even (TI and TJ
+// are), so a cell's colour (i + j) & 1 is (a + b) & 1 in tile coordinates.
+template <int TI, int AJ_, int RY_>
+struct MgTile {
+    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY;
+    static constexpr int TJ = AJ - 4, AI = TI + 4, A = AI * AJ;
+    static_assert(TI % 2 == 0 && TJ % 2 == 0, "aggregates must not straddle tiles");
+    static_assert((AJ & (AJ - 1)) == 0, "row width must be a power of two");
+    __device__ static __forceinline__ int tx() { return threadIdx.x & (AJ - 1); }
+    __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
+    __device__ static __forceinline__ int i0() { return blockIdx.y * TI; }
+    __device__ static __forceinline__ int j0() { return blockIdx.x * TJ; }
 };
 
-// stage the 5 coefficient components over the 1-cell halo ring (0 outside)
-template <int TI, int TJ, int NT>
-__device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, float (*sc)[(TI + 2) * (TJ + 2)]) {
-    using D = MgTileDims<TI, TJ>;
-    for (int t = threadIdx.x; t < D::CI * D::CJ; t += NT) {
-        const int ii = t / D::CJ, jj = t - ii * D::CJ;
-        const int i = i0 + ii - 1, j = j0 + jj - 1;
-        const bool in = i >= 0 && i < L.NX && j >= 0 && j < L.NY;
-        const long long e = in ? (long long)(i * L.NY + j) * L.es : 0;
+// stage the 5 coefficient components over the whole staged region
+template <int TI, class T>
+__device__ __forceinline__ void mg_stage_coef(const MgLvl& L, float* sc) {
+    const int b = T::tx(), j = T::j0() + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = T::i0() + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const float* g = in ? L.c + (long long)(i * L.NY + j) * L.es : L.c;
+        const int u = a * T::AJ + b;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) sc[q][t] = in ? __ldg(L.c + q * L.cs + e) : 0.f;
+        for (int q = 0; q < 5; ++q) cp_async4(sc + q * T::A + u, g + q * L.cs, in);
     }
 }
 
-// (A x)(cell at 2-halo coords (a, b)); x staged over the 2-cell halo, coefficients over the 1-cell halo
-template <int TI, int TJ>
-__device__ __forceinline__ float mg_ax_smem(const float* sx, const float (*sc)[(TI + 2) * (TJ + 2)], int lap, int a,
-                                            int b) {
-    using D = MgTileDims<TI, TJ>;
-    const int t = (a - 1) * D::CJ + (b - 1);
-    const int u = a * D::AJ + b;
-    return mg_row(sc[0][t], sc[1][t], sc[2][t], sc[3][t], sc[4][t], lap, sx[u], sx[u - D::AJ], sx[u + D::AJ],
-                  sx[u + 1], sx[u - 1]);
+// (A x) at staged index u
+template <class T>
+__device__ __forceinline__ float mg_ax_smem(const float* sx, const float* sc, int lap, int u) {
+    return mg_row(sc[u], sc[T::A + u], sc[2 * T::A + u], sc[3 * T::A + u], sc[4 * T::A + u], lap, sx[u],
+                  sx[u - T::AJ], sx[u + T::AJ], sx[u + 1], sx[u - 1]);
+}
+template <class T>
+__device__ __forceinline__ bool mg_linked_smem(const float* sc, int u) {
+    return sc[T::A + u] != 0.f || sc[2 * T::A + u] != 0.f || sc[3 * T::A + u] != 0.f || sc[4 * T::A + u] != 0.f;
 }
 
-template <int TI, int TJ, int NT, class BSrc, class Own>
-__device__ __forceinline__ void mg_down_tile(const MgLvl& L, const BSrc& bsrc, const Own& own,
-                                             float* __restrict__ xout, float* __restrict__ bc, int NXc, int NYc) {
-    using D = MgTileDims<TI, TJ>;
-    __shared__ float sb[D::AI * D::AJ], sw[D::AI * D::AJ], sx[D::AI * D::AJ];
-    __shared__ float sc[5][D::CI * D::CJ];
-    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
-    // b and W over the 2-cell halo; red cells start at W b, black at 0
-    for (int t = threadIdx.x; t < D::AI * D::AJ; t += NT) {
-        const int a = t / D::AJ, b = t - a * D::AJ;
-        const int i = i0 + a - 2, j = j0 + b - 2;
-        float bv = 0.f, wv = 0.f;
-        if (i >= 0 && i < L.NX && j >= 0 && j < L.NY) {
-            const int k = i * L.NY + j;
-            bv = bsrc(k);
-            wv = __ldg(L.winv + k);
-            if (a >= 2 && a < TI + 2 && b >= 2 && b < TJ + 2) own(k, bv);
+// DOWN tile.  b = HasQ ? b_in - alpha q : b_in over the staged region.
+template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own>
+__device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const float* __restrict__ b_in,
+                                                          const float* __restrict__ q, float alpha, const Mid& mid,
+                                                          const Own& own, float* __restrict__ xout,
+                                                          float* __restrict__ bc, int NXc, int NYc) {
+    using T = MgTile<TI, AJ, RY>;
+    __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
+    __shared__ __align__(16) float sq[HasQ ? T::A : 1];
+    __shared__ __align__(16) float sc[5 * T::A];
+    const int b = T::tx(), j = T::j0() + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
+    typename Own::Sum sum{};
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = T::i0() + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(sb + u, b_in + k, in);
+        if (HasQ) cp_async4(sq + u, q + k, in);
+        cp_async4(sw + u, L.winv + k, in);
+    }
+    mg_stage_coef<TI, T>(L, sc);
+    cp_async_commit();
+    mid();
+    cp_async_wait_all();
+    __syncthreads();
+    // b, owned cells, red start (x = W b on red, 0 on black)
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int u = a * T::AJ + b;
+        const int i = T::i0() + a - 2;
+        float bv = sb[u];
+        if (HasQ) {
+            bv = fmaf(-alpha, sq[u], bv);
+            sb[u] = bv;
         }
-        sb[t] = bv;
-        sw[t] = wv;
-        sx[t] = ((i + j) & 1) == 0 ? wv * bv : 0.f;
-    }
-    mg_stage_coef<TI, TJ, NT>(L, i0, j0, sc);
-    __syncthreads();
-    // black half-sweep over the 1-cell halo (reads red neighbours only)
-    for (int t = threadIdx.x; t < D::CI * D::CJ; t += NT) {
-        const int a = t / D::CJ + 1, b = t - (t / D::CJ) * D::CJ + 1;
-        const int i = i0 + a - 2, j = j0 + b - 2;
-        if (((i + j) & 1) == 0) continue;
-        const int u = a * D::AJ + b;
-        sx[u] = fmaf(sw[u], sb[u] - mg_ax_smem<TI, TJ>(sx, sc, L.lap, a, b), sx[u]);
+        if (jown && a >= 2 && a < TI + 2 && i < L.NX) own(i * L.NY + j, bv, sum);
+        sx[u] = ((a + b) & 1) == 0 ? sw[u] * bv : 0.f;
     }
     __syncthreads();
-    // owned cells: write x; aggregates: restricted residual
-    for (int t = threadIdx.x; t < TI * TJ; t += NT) {
-        const int a = t / TJ, b = t - a * TJ;
-        const int i = i0 + a, j = j0 + b;
-        if (i < L.NX && j < L.NY) xout[i * L.NY + j] = sx[(a + 2) * D::AJ + b + 2];
-    }
-    for (int t = threadIdx.x; t < (TI / 2) * (TJ / 2); t += NT) {
-        const int ag = t / (TJ / 2), bg = t - ag * (TJ / 2);
-        const int I = (i0 >> 1) + ag, J = (j0 >> 1) + bg;
+    // black half-sweep over the 1-cell ring (reads red neighbours only)
+    if (b >= 1 && b < AJ - 1)
+        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
+            if (((a + b) & 1) == 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), sx[u]);
+        }
+    __syncthreads();
+    // owned cells: write x
+    if (jown)
+        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
+            const int i = T::i0() + a - 2;
+            if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + b];
+        }
+    // aggregates: restricted residual over coupled cells
+    for (int t = threadIdx.x; t < (TI / 2) * (T::TJ / 2); t += T::NT) {
+        const int ag = t / (T::TJ / 2), bg = t - ag * (T::TJ / 2);
+        const int I = (T::i0() >> 1) + ag, J = (T::j0() >> 1) + bg;
         if (I >= NXc || J >= NYc) continue;
         float s = 0.f;
 #pragma unroll
         for (int di = 0; di < 2; ++di)
 #pragma unroll
             for (int dj = 0; dj < 2; ++dj) {
-                const int a = 2 * ag + di + 2, b = 2 * bg + dj + 2;
-                const int i = i0 + a - 2, j = j0 + b - 2;
-                if (i >= L.NX || j >= L.NY) continue;
-                const int tc = (a - 1) * D::CJ + (b - 1);
-                const bool linked = sc[1][tc] != 0.f || sc[2][tc] != 0.f || sc[3][tc] != 0.f || sc[4][tc] != 0.f;
-                if (!linked) continue;
-                s += sb[a * D::AJ + b] - mg_ax_smem<TI, TJ>(sx, sc, L.lap, a, b);
+                const int a = 2 * ag + di + 2, bb = 2 * bg + dj + 2;
+                if (T::i0() + a - 2 >= L.NX || T::j0() + bb - 2 >= L.NY) continue;
+                const int u = a * T::AJ + bb;
+                if (!mg_linked_smem<T>(sc, u)) continue;
+                s += sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u);
             }
         bc[I * NYc + J] = s;
     }
+    return sum;
 }
 
-template <int TI, int TJ, int NT, class BSrc, class Own>
-__device__ __forceinline__ void mg_up_tile(const MgLvl& L, const float* __restrict__ xpre,
-                                           const float* __restrict__ xc, int NYc, float alpha, const BSrc& bsrc,
-                                           const Own& own, float* __restrict__ xout) {
-    using D = MgTileDims<TI, TJ>;
-    __shared__ float sx[D::AI * D::AJ];
-    __shared__ float sb[D::CI * D::CJ], sw[D::CI * D::CJ];
-    __shared__ float sc[5][D::CI * D::CJ];
-    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
-    // prolongation over the 2-cell halo
-    for (int t = threadIdx.x; t < D::AI * D::AJ; t += NT) {
-        const int a = t / D::AJ, b = t - a * D::AJ;
-        const int i = i0 + a - 2, j = j0 + b - 2;
-        float xv = 0.f;
-        if (i >= 0 && i < L.NX && j >= 0 && j < L.NY) {
-            const int k = i * L.NY + j;
-            xv = __ldg(xpre + k);
-            if (!__ldg(L.iso + k)) xv = fmaf(alpha, __ldg(xc + (i >> 1) * NYc + (j >> 1)), xv);
-        }
-        sx[t] = xv;
+// UP tile: prolong (coupled cells, told apart by their links), black
+// half-sweep over the 1-cell ring, red half-sweep on the owned cells.
+template <int TI, int AJ, int RY, class Own>
+__device__ __forceinline__ typename Own::Sum mg_up_tile(const MgLvl& L, const float* __restrict__ xpre,
+                                                        const float* __restrict__ xc, int NXc, int NYc, float alpha,
+                                                        const float* __restrict__ b_in, const Own& own,
+                                                        float* __restrict__ xout) {
+    using T = MgTile<TI, AJ, RY>;
+    constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
+    __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
+    __shared__ __align__(16) float sc[5 * T::A];
+    const int b = T::tx(), j = T::j0() + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    typename Own::Sum sum{};
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = T::i0() + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(sx + u, xpre + k, in);
+        cp_async4(sb + u, b_in + k, in);
+        cp_async4(sw + u, L.winv + k, in);
     }
-    for (int t = threadIdx.x; t < D::CI * D::CJ; t += NT) {
-        const int a = t / D::CJ, b = t - a * D::CJ;
-        const int i = i0 + a - 1, j = j0 + b - 1;
-        float bv = 0.f, wv = 0.f;
-        if (i >= 0 && i < L.NX && j >= 0 && j < L.NY) {
-            const int k = i * L.NY + j;
-            bv = bsrc(k);
-            wv = __ldg(L.winv + k);
-        }
-        sb[t] = bv;
-        sw[t] = wv;
+    for (int t = threadIdx.x; t < XI * XJ; t += T::NT) {
+        const int ca = t / XJ, cb = t - ca * XJ;
+        const int I = (T::i0() >> 1) - 1 + ca, J = (T::j0() >> 1) - 1 + cb;
+        const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
+        cp_async4(sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    mg_stage_coef<TI, TJ, NT>(L, i0, j0, sc);
+    mg_stage_coef<TI, T>(L, sc);
+    cp_async_commit();
+    cp_async_wait_all();
     __syncthreads();
-    // black half-sweep over the 1-cell halo
-    for (int t = threadIdx.x; t < D::CI * D::CJ; t += NT) {
-        const int a = t / D::CJ + 1, b = t - (t / D::CJ) * D::CJ + 1;
-        const int i = i0 + a - 2, j = j0 + b - 2;
-        if (((i + j) & 1) == 0) continue;
-        const int u = a * D::AJ + b;
-        sx[u] = fmaf(sw[t], sb[t] - mg_ax_smem<TI, TJ>(sx, sc, L.lap, a, b), sx[u]);
+    // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-2, j0-2)
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int u = a * T::AJ + b;
+        if (!mg_linked_smem<T>(sc, u)) continue;
+        sx[u] = fmaf(alpha, sxc[(a >> 1) * XJ + (b >> 1)], sx[u]);
     }
+    __syncthreads();
+    // black half-sweep over the 1-cell ring
+    if (b >= 1 && b < AJ - 1)
+        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
+            if (((a + b) & 1) == 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), sx[u]);
+        }
     __syncthreads();
     // red half-sweep on the owned cells, then write
-    for (int t = threadIdx.x; t < TI * TJ; t += NT) {
-        const int a = t / TJ + 2, b = t - (t / TJ) * TJ + 2;
-        const int i = i0 + a - 2, j = j0 + b - 2;
-        if (i >= L.NX || j >= L.NY) continue;
-        const int u = a * D::AJ + b;
-        const int tc = (a - 1) * D::CJ + (b - 1);
-        float xv = sx[u];
-        if (((i + j) & 1) == 0) xv = fmaf(sw[tc], sb[tc] - mg_ax_smem<TI, TJ>(sx, sc, L.lap, a, b), xv);
-        const int k = i * L.NY + j;
-        xout[k] = xv;
-        own(k, xv, sb[tc]);
-    }
+    if (b >= 2 && b < T::TJ + 2 && j < L.NY)
+        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
+            const int i = T::i0() + a - 2;
+            if (i >= L.NX) continue;
+            const int u = a * T::AJ + b;
+            float xv = sx[u];
+            if (((a + b) & 1) == 0) xv = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), xv);
+            const int k = i * L.NY + j;
+            xout[k] = xv;
+            own(k, xv, sb[u], sum);
+        }
+    return sum;
 }
 
 }  // namespace kc

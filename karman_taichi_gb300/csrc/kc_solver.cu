@@ -1516,47 +1516,62 @@ __global__ void __launch_bounds__(kPwThreads) k_pc_3(int n, PcVecs V, BicgPtrs P
 
 // ---- fused level 0: CG's pointwise passes inside the V-cycle's level-0 tiles ----
 // DOWN_0 with update: b = r_new = r_old - alpha q is formed per cell (halo
-// included) from the previous residual, owned cells store r_new, advance
-// x += alpha p and accumulate (r_new, r_new) -- pass K2.  r alternates
-// between two buffers so no block reads a residual another block rewrote.
-// Without update (the start) b = r_0.
-struct PcDownSrc {
-    const float* __restrict__ r_in;
-    const float* __restrict__ q;
-    float alpha;
-    bool update;
-    __device__ __forceinline__ float operator()(int k) const {
-        const float r = __ldg(r_in + k);
-        return update ? fmaf(-alpha, __ldg(q + k), r) : r;
-    }
-};
-struct PcDownOwn {
-    float* __restrict__ r_out;
+// included) from the previous residual, owned cells store r_new and
+// accumulate (r_new, r_new), and x += alpha p runs while the tile is being
+// staged -- pass K2.  r alternates between two buffers so no block reads a
+// residual another block rewrote.  Without update (the start) b = r_0.
+template <int TI, int TJ, int NT>
+struct PcMidX {   // x += alpha p on the owned TI x TJ cells (FP64 iterate)
     double* __restrict__ x;
     const float* __restrict__ p;
     double alpha;
-    Acc<float>* acc;
-    bool update;
-    __device__ __forceinline__ void operator()(int k, float rn) const {
-        if (!update) return;
+    int NX, NY;
+    bool on;
+    __device__ __forceinline__ void operator()() const {
+        if (!on) return;
+        const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+        constexpr int R = (TI * TJ + NT - 1) / NT;
+        float pv[R];
+        int kk[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) {
+            const int t = threadIdx.x + m * NT;
+            const int a = t / TJ, b = t - a * TJ;
+            const int i = i0 + a, j = j0 + b;
+            kk[m] = (t < TI * TJ && i < NX && j < NY) ? i * NY + j : -1;
+            pv[m] = kk[m] >= 0 ? __ldg(p + kk[m]) : 0.f;
+        }
+#pragma unroll
+        for (int m = 0; m < R; ++m)
+            if (kk[m] >= 0) x[kk[m]] = fma(alpha, (double)pv[m], x[kk[m]]);
+    }
+};
+struct PcOwnR {
+    using Sum = Acc<float>;
+    float* __restrict__ r_out;
+    bool on;
+    __device__ __forceinline__ void operator()(int k, float rn, Sum& acc) const {
+        if (!on) return;
         r_out[k] = rn;
-        x[k] = fma(alpha, (double)__ldg(p + k), x[k]);
-        acc->add(rn, rn);
+        acc.add(rn, rn);
     }
 };
 
-template <int TI, int TJ, int NT>
-__global__ void __launch_bounds__(NT) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1, int NX1,
-                                                  int NY1, PcVecs V, BicgPtrs P, int update) {
+template <int TI, int AJ, int RY>
+__global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
+                                                       int NX1, int NY1, PcVecs V, BicgPtrs P, int update) {
+    constexpr int TJ = AJ - 4, NT = AJ * RY;
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     const int cur = (int)(it & 1);
+    // the start passes b = r - 0 * r (q := r, finite) and skips the CG updates
+    const bool up = update != 0;
+    const PcMidX<TI, TJ, NT> mid{V.x, V.p[cur ^ 1], __ldcg(&st->alpha), L.NX, L.NY, up};
     Acc<float> acc[1];
-    const PcDownSrc src{V.r[cur], V.q, __ldcg(&st->alpha_f), update != 0};
-    const PcDownOwn own{V.r[cur ^ 1], V.x, V.p[cur ^ 1], __ldcg(&st->alpha), &acc[0], update != 0};
-    mg_down_tile<TI, TJ, NT>(L, src, own, x0pre, b1, NX1, NY1);
-    if (!update) return;
+    acc[0] = mg_down_tile<TI, AJ, RY, true>(L, V.r[cur], up ? V.q : V.r[cur], up ? __ldcg(&st->alpha_f) : 0.f, mid,
+                                            PcOwnR{V.r[cur ^ 1], up}, x0pre, b1, NX1, NY1);
+    if (!up) return;
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {
@@ -1567,19 +1582,19 @@ __global__ void __launch_bounds__(NT) k_pcf_down0(MgLvl L, float* __restrict__ x
 
 // UP_0 writes z and accumulates (r, z) -- pass K3
 struct PcUpOwn {
-    Acc<float>* acc;
-    __device__ __forceinline__ void operator()(int, float z, float r) const { acc->add(r, z); }
+    using Sum = Acc<float>;
+    __device__ __forceinline__ void operator()(int, float z, float r, Sum& acc) const { acc.add(r, z); }
 };
 
-template <int TI, int TJ, int NT>
-__global__ void __launch_bounds__(NT) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
-                                                const float* __restrict__ final1, int NY1, float alpha0, PcVecs V,
-                                                BicgPtrs P) {
+template <int TI, int AJ, int RY>
+__global__ void __launch_bounds__(AJ * RY) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
+                                                     const float* __restrict__ final1, int NX1, int NY1, float alpha0,
+                                                     PcVecs V, BicgPtrs P) {
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     Acc<float> acc[1];
-    mg_up_tile<TI, TJ, NT>(L, x0pre, final1, NY1, alpha0, MgBLoad{V.r[(int)(it & 1)]}, PcUpOwn{&acc[0]}, V.z);
+    acc[0] = mg_up_tile<TI, AJ, RY>(L, x0pre, final1, NX1, NY1, alpha0, V.r[(int)(it & 1)], PcUpOwn{}, V.z);
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {
@@ -2217,11 +2232,11 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
         if (F.ok) {
             // K2 and K3 ride in the V-cycle's level-0 launches
             const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
-            k_pcf_down0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1);
+            k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1);
             KC_LAUNCH_CHECK_NC("k_pcf_down0");
             int rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
             if (rc) return rc;
-            k_pcf_up0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NY1, F.alpha0, V, P);
+            k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P);
             KC_LAUNCH_CHECK_NC("k_pcf_up0");
             k1 += 2;
         } else {
@@ -2339,11 +2354,11 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
             int mk = 0;
             if (F.ok) {
                 const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
-                k_pcf_down0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, W, P, 0);
+                k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, W, P, 0);
                 KC_LAUNCH_CHECK("k_pcf_down0");
                 rc = mg_enqueue_coarse(A32, mg_ws, mg_opts, &P.st->done, s, &mk);
                 if (rc) return rc;
-                k_pcf_up0<kMgTI0, kMgTJ0, kMgNT0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NY1, F.alpha0, W, P);
+                k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, W, P);
                 KC_LAUNCH_CHECK("k_pcf_up0");
             } else {
                 rc = mg_enqueue(A32, mg_ws, mg_opts, W.r[0], W.z, &P.st->done, s, &mk);
