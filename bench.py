@@ -57,6 +57,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--spmv-sweep", action="store_true",
+                    help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
+    ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
+                    help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
+                         "(the command the committed ncu summaries were captured on)")
     return ap.parse_args()
 
 
@@ -228,25 +233,22 @@ def e2e_steps(solver, K, W, world):
 # Algorithmic bytes per fine cell of one multigrid-preconditioned CG
 # iteration (FP32 vectors and coefficients, FP64 iterate), each array read or
 # written once per kernel:
-#   K1 p = z + beta p, q = A p         read z, p, 5 coef; write p, q      36
-#   K2 x += alpha p, r -= alpha q      read p, q, r, x(8); write x(8), r  32
-#   K3 (r, z)                          read r, z                           8
-#   V-cycle, level 0 (1 pre + 1 post red-black sweep):
-#     first half-sweep                 read b, winv; write x              12
-#     3 red-black half-sweeps          read x, b, 5 coef, winv (half), write half, x x3  60
-#     restrict                         read b, x, 5 coef, iso; write 1/4  30
-#     prolong                          read x, iso, 1/4; write x          10
-#   coarse levels: the level-0 V-cycle bytes x (1/4 + 1/16 + ...) = x 1/3
-PCG_MG_BYTES_PER_CELL = 36 + 32 + 8 + round((12 + 60 + 30 + 10) * 4 / 3)
+#   k_pc_1       p = z + beta p, q = A p: read z, p, 5 coef; write p, q          36
+#   k_pcf_down0  r = r - alpha q, x += alpha p (FP64), pre-smooth, restrict:
+#                read r, q, W, 5 coef, p, x(8); write r, x(8), x_pre, b_1/4   61
+#   k_pcf_up0    prolong + post-smooth, (r, z): read x_pre, x_1/4, r, W, 5 coef;
+#                write z                                                        37
+#   levels >= 1  DOWN 33 + UP 37 bytes per coarse cell, n/3 coarse cells         23
+PCG_MG_BYTES_PER_CELL = 36 + 61 + 37 + 23
 
 
 def roofline_p_solve(solver, mode, peak):
     """Roofline of the dominant unit of work, the pressure-correction solve.
 
     fp64: one persistent BiCGSTAB launch, 27 words/cell/iteration.
-    mixed: the multigrid-preconditioned CG (kernels K1, K2, K3 and the V-cycle
-    per iteration), PCG_MG_BYTES_PER_CELL bytes/cell/iteration; the FP64
-    refinement residuals add 2 x (5 coef + x + b) x 8 B per cell."""
+    mixed: the multigrid-preconditioned CG, PCG_MG_BYTES_PER_CELL
+    bytes/cell/iteration over its 2L launches per iteration (L multigrid
+    levels); each FP64 refinement residual adds (5 coef + x + b) x 8 B/cell."""
     import torch
     solver.assemble_momentum()
     solver.solve_momentum()
@@ -266,9 +268,9 @@ def roofline_p_solve(solver, mode, peak):
         note = "27 words/cell/iteration (A 9R+2W, B 7R+1W, C 6R+2W)"
     else:
         alg = PCG_MG_BYTES_PER_CELL * n * info.iters + (info.refinements + 1) * 7 * 8 * n
-        kernel = "kc_pcg_refined (k_pc_1/2/3 + multigrid V-cycle)"
-        note = (f"{PCG_MG_BYTES_PER_CELL} B/cell/PCG iteration (K1 36, K2 32, K3 8, V-cycle 150) + "
-                f"56 B/cell per FP64 refinement residual")
+        kernel = "kc_pcg_refined"
+        note = (f"{PCG_MG_BYTES_PER_CELL} B/cell/PCG iteration (k_pc_1 36, k_pcf_down0 61, k_pcf_up0 37, "
+                f"levels>=1 23) + 56 B/cell per FP64 refinement residual")
     achieved = alg / (ms * 1e-3) / 1e9
     traffic = None
     try:
@@ -282,6 +284,38 @@ def roofline_p_solve(solver, mode, peak):
             "frac": round(achieved / peak, 4), "traffic": traffic,
             "algorithmic_bytes": alg, "iters": info.iters, "ms": round(ms, 3),
             "note": note + "; peak = hbm_gbs of MEASURED_PEAKS.json (burst)"}
+
+
+def spmv_roofline(solver, peak):
+    """SpMV (k_spmv) on the workload's assembled pressure-correction system,
+    FP64 and FP32, each launch timed with CUDA events after writing a
+    256 MB buffer (larger than L2); 7 words/cell algorithmic."""
+    import torch
+    from karman_taichi_gb300 import linalg
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=solver.device)
+    out = {}
+    systems = [("f64", solver.A_p, torch.float64, 8)]
+    if getattr(solver, "A_p32", None) is not None:
+        systems.append(("f32", linalg.Stencil(solver.coef_p32), torch.float32, 4))
+    for name, A, dt, w in systems:
+        x = torch.rand(A.n, dtype=dt, device=solver.device)
+        y = torch.empty_like(x)
+        for _ in range(3):
+            linalg.spmv(A, x, y)
+        ts = []
+        for _ in range(10):
+            flush.add_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            linalg.spmv(A, x, y)
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        t = sorted(ts)[len(ts) // 2]
+        gbs = 7 * w * A.n / (t * 1e-3) / 1e9
+        out[name] = {"cells": A.n, "us": round(t * 1e3, 2), "achieved_gbs": round(gbs, 1),
+                     "frac": round(gbs / peak, 4)}
+    return out
 
 
 def cpu_sample(cfg, budget_s, iters_per_step):
@@ -377,6 +411,7 @@ def run_gpu(args):
     if rank == 0:
         out["roofline"] = roofline_p_solve(solver, mode, peak)
         out["roofline"]["peak_kind"] = peak_kind
+        out["spmv"] = spmv_roofline(solver, peak)
 
     fp64_counts = summ if mode == "fp64" else None
     if rank == 0 and not args.no_compare and mode != "fp64":
@@ -456,9 +491,58 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_spmv_sweep(args):
+    """k_spmv bandwidth against system size: random coefficients and operand,
+    each launch timed with CUDA events after writing a 256 MB buffer; 7
+    words/cell algorithmic."""
+    import torch
+    from karman_taichi_gb300 import linalg
+    peak, kind = peaks()
+    dev = torch.device("cuda", 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    rows = []
+    for NX, NY in ((2050, 514), (4098, 1026), (8194, 2050)):
+        for dt, w in ((torch.float64, 8), (torch.float32, 4)):
+            g = torch.Generator(device=dev).manual_seed(0)
+            A = linalg.Stencil(torch.rand((5, NX, NY), dtype=dt, device=dev, generator=g))
+            x = torch.rand((NX, NY), dtype=dt, device=dev, generator=g)
+            y = torch.empty_like(x)
+            for _ in range(3):
+                linalg.spmv(A, x, y)
+            ts = []
+            for _ in range(20):
+                flush.add_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                linalg.spmv(A, x, y)
+                e1.record()
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            t = sorted(ts)[len(ts) // 2]
+            gbs = 7 * w * NX * NY / (t * 1e-3) / 1e9
+            rows.append({"grid": f"{NX}x{NY}", "dtype": "f64" if w == 8 else "f32", "us": round(t * 1e3, 2),
+                         "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4), "peak_kind": kind})
+    print(json.dumps({"spmv_sweep": rows}), flush=True)
+
+
+def run_profile_outer(args):
+    import torch
+    from karman_taichi_gb300.config import PRESETS
+    cfg = PRESETS[args.config]
+    solver = make_solver(cfg, resolve_mode(args.mode), torch.device("cuda", 0))
+    for _ in range(args.profile_outer):
+        rec = solver.outer_iteration()
+    torch.cuda.synchronize()
+    print(json.dumps({"config": cfg.name, "outer_iterations": args.profile_outer, "last": rec}), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.profile_outer > 0:
+        run_profile_outer(a)
+    elif a.spmv_sweep:
+        run_spmv_sweep(a)
     else:
         run_gpu(a)

@@ -236,6 +236,22 @@ __device__ __forceinline__ void stencil_tile_at(const Pol& pol, const Coef<T>& A
                                                 Acc<T> (&acc)[NACC]) {
     __shared__ T op[kTI + 2][kTJ + 2];
     __shared__ T aux[Pol::kAux ? kTI : 1][Pol::kAux ? kTJ : 1];
+    // The coefficients of the owned points do not depend on the staged
+    // operand: their loads are issued first, so they are in flight together
+    // with the operand's and the tile waits on memory once.
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int j = j0 + tx;
+    T c[kCPT][5];
+    int kc[kCPT];
+#pragma unroll
+    for (int r = 0; r < kCPT; ++r) {
+        const int a = ty + 8 * r;
+        const long long kl = (long long)(i0 + a) * S + j;
+        const bool ok = j < S && kl < n;
+        kc[r] = ok ? (int)kl : -1;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) c[r][q] = ok ? A.at(q, (int)kl) : T(0);
+    }
     T pre[kPtIters];
     int kk[kPtIters];
 #pragma unroll
@@ -265,19 +281,6 @@ __device__ __forceinline__ void stencil_tile_at(const Pol& pol, const Coef<T>& A
         }
     }
     __syncthreads();
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int j = j0 + tx;
-    T c[kCPT][5];
-    int kc[kCPT];
-#pragma unroll
-    for (int r = 0; r < kCPT; ++r) {
-        const int a = ty + 8 * r;
-        const long long kl = (long long)(i0 + a) * S + j;
-        const bool ok = j < S && kl < n;
-        kc[r] = ok ? (int)kl : -1;
-#pragma unroll
-        for (int q = 0; q < 5; ++q) c[r][q] = ok ? A.at(q, (int)kl) : T(0);
-    }
 #pragma unroll
     for (int r = 0; r < kCPT; ++r) {
         if (kc[r] >= 0) {
@@ -1532,7 +1535,9 @@ struct PcMidX {   // x += alpha p on the owned TI x TJ cells (FP64 iterate)
         const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
         constexpr int R = (TI * TJ + NT - 1) / NT;
         float pv[R];
+        double xv[R];
         int kk[R];
+        // all loads first (the cells are distinct, so no store can feed a later load)
 #pragma unroll
         for (int m = 0; m < R; ++m) {
             const int t = threadIdx.x + m * NT;
@@ -1540,10 +1545,11 @@ struct PcMidX {   // x += alpha p on the owned TI x TJ cells (FP64 iterate)
             const int i = i0 + a, j = j0 + b;
             kk[m] = (t < TI * TJ && i < NX && j < NY) ? i * NY + j : -1;
             pv[m] = kk[m] >= 0 ? __ldg(p + kk[m]) : 0.f;
+            xv[m] = kk[m] >= 0 ? __ldcg(x + kk[m]) : 0.0;
         }
 #pragma unroll
         for (int m = 0; m < R; ++m)
-            if (kk[m] >= 0) x[kk[m]] = fma(alpha, (double)pv[m], x[kk[m]]);
+            if (kk[m] >= 0) x[kk[m]] = fma(alpha, (double)pv[m], xv[m]);
     }
 };
 struct PcOwnR {
