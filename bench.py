@@ -391,7 +391,8 @@ def run_gpu(args):
     summ = summarize(recs)
     value = world * args.steps / (ms * 1e-3)
     out.update(value=round(value, 5), ms_per_step=round(ms / args.steps, 3),
-               dtype="f64" if mode == "fp64" else "f32+f64 (FP32 stencils/vectors, FP64 dots/residuals)",
+               dtype="f64" if mode == "fp64" else ("f32+f64 (FP32 stencils/vectors, FP64 dots/residuals)"
+                                                   + (" + bf16 U-Net initial guess" if mode == "learned" else "")),
                data="synthetic: seeded channel initial state (u=1, v = U(-1e-3,1e-3) noise, p=0)",
                config={"workload": cfg.name, "nx": cfg.nx, "ny": cfg.ny, "cells": cfg.cells, "Re": cfg.Re,
                        "mode": mode, "mass_tol": cfg.mass_tol, "max_outer": cfg.max_outer, "eps": cfg.eps,

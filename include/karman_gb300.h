@@ -298,6 +298,64 @@ int kc_karman_puv_correction(const kc_karman* K, const int* ct, const double* pc
 int kc_karman_correct_conserv(const kc_karman* K, double* u, const double* v, double* udiv,
                               void* stream);
 
+/* ---- learned initial guess (U-Net) ---------------------------------------- */
+/* No reference counterpart: the learned row of the accelerated path.
+ * Activations are NHWC bfloat16 [H][W][C] with C a multiple of 16; 3x3
+ * weights are bfloat16 [9][cout][cin] (tap = 3*ky + kx); biases FP32.
+ * y = act(conv3x3(x, w) + bias) with zero padding, act 0 = none, 1 = ReLU,
+ * cout in {16, 32, 48, 64}; weight (tap, co, ci) at w[tap*wtap + co*cin + ci]
+ * (wtap 0: cout*cin) and output (px, co) at y[px*ldy + co] (ldy 0: cout) --
+ * a channel group of a wider tensor.  mask (nullable, indexed like y): y = 0
+ * where mask <= 0 (the ReLU derivative of the layer below, when the call
+ * computes a data gradient with flipped weights).  Tensor cores (BF16
+ * operands, FP32 accumulation). */
+int kc_unet_conv3x3(const void* x, int H, int W, int cin, const void* w, long long wtap,
+                    const float* bias, int cout, int act, const void* mask, void* y, int ldy,
+                    void* stream);
+/* dw[9][cout][cin] += sum_px dy[px][co] x[px + tap][ci]; db[cout] += sum_px dy (db nullable). */
+int kc_unet_conv3x3_wgrad(const void* x, const void* dy, int H, int W, int cin, int cout, float* dw,
+                          float* db, void* stream);
+/* wt[9][cin][cout] = w[8 - tap][cout][cin] (input channels >= cin_real zeroed): the weights
+ * of the data-gradient convolution. */
+int kc_unet_flip_weights(const void* w, int cout, int cin, int cin_real, void* wt, void* stream);
+/* 2x2 average pooling and its gradient (dx = or += dy / 4). */
+int kc_unet_pool2(const void* x, int H, int W, int C, void* y, void* stream);
+int kc_unet_pool2_bwd(const void* dy, int H, int W, int C, void* dx, int accumulate, void* stream);
+/* y[H][W][cu + cs] = concat(nearest 2x upsampling of u[H/2][W/2][cu], s[H][W][cs]) and its gradient. */
+int kc_unet_up2_concat(const void* u, int cu, const void* s, int cs, int H, int W, void* y, void* stream);
+int kc_unet_up2_concat_bwd(const void* dy, int cu, int cs, int H, int W, void* du, void* ds,
+                           int accumulate_s, void* stream);
+/* dy = 0 where y <= 0 (in place). */
+int kc_unet_relu_bwd(void* dy, const void* y, long long n, void* stream);
+/* 1x1 head C -> 1 (FP32 out, C <= 64) and its gradient (dw, db accumulated). */
+int kc_unet_head(const void* x, int C, long long npx, const float* w, const float* b, float* out,
+                 void* stream);
+int kc_unet_head_bwd(const void* x, int C, long long npx, const float* w, const float* dout, void* dx,
+                     float* dw, float* db, void* stream);
+/* loss += sum (weight (out - target))^2 * inv_count; dout = 2 weight^2 (out - target) inv_count. */
+int kc_unet_mse(const float* out, const float* target, const float* weight, long long npx,
+                float inv_count, float* dout, float* loss, void* stream);
+/* Adam step (bias-corrected, step >= 1) on FP32 parameters; p_bf16 (nullable) receives a copy. */
+int kc_unet_adam(float* p, const float* g, float* m, float* v, long long n, float lr, float b1,
+                 float b2, float eps, int step, void* p_bf16, void* stream);
+int kc_unet_to_bf16(const float* a, void* b, long long n, void* stream);
+/* Network input of the p' system A x = b (b FP64 [NX][NY], coef32 its FP32
+ * Laplacian-form planes, SoA): feat[H][W][16] bf16 (H >= NX, W >= NY; zero
+ * outside the fluid) with channels b/s_b, fluid, d/mean(d), P1/s_p, where P1
+ * is the 1-D solution of the column-summed system (Neumann at i = 0,
+ * Dirichlet beyond i = NX-1); fluid (nullable) FP32 [NX][NY]; scales[4] =
+ * {s_b, mean d, s_p, fluid count} (device).  ws: kc_unet_features_ws_bytes(NX). */
+size_t kc_unet_features_ws_bytes(int NX);
+int kc_unet_features(const double* b, const float* coef32, int NX, int NY, int H, int W, void* feat,
+                     float* fluid, double* scales, void* ws, size_t ws_bytes, void* stream);
+/* x0 = s_p * bilinear 2x upsampling of the half-resolution prediction out[Hh][Wh] on fluid cells
+ * (0 elsewhere), FP64 [NX][NY]. */
+int kc_unet_guess_up2(const float* out, int Hh, int Wh, const float* coef32, int NX, int NY,
+                      const double* scales, double* x0, void* stream);
+/* Half-resolution training target: 2x2 fluid average of p / s_p and the fluid share as weight. */
+int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, const double* scales,
+                         int Hh, int Wh, float* target, float* weight, void* stream);
+
 /* ---- utilities ------------------------------------------------------------ */
 /* dst = src (device to device), e.g. time_forward (karman_taichi.py:617-622). */
 int kc_copy(void* dst, const void* src, size_t bytes, void* stream);

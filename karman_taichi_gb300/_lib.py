@@ -127,6 +127,23 @@ SIGNATURES = {
     "kc_karman_puv_correction": (I_, [C.POINTER(KcKarman)] + [P_] * 10),
     "kc_karman_correct_conserv": (I_, [C.POINTER(KcKarman), P_, P_, P_, P_]),
     "kc_copy": (I_, [P_, P_, S_, P_]),
+    "kc_unet_conv3x3": (I_, [P_, I_, I_, I_, P_, L_, P_, I_, I_, P_, P_, I_, P_]),
+    "kc_unet_conv3x3_wgrad": (I_, [P_, P_, I_, I_, I_, I_, P_, P_, P_]),
+    "kc_unet_flip_weights": (I_, [P_, I_, I_, I_, P_, P_]),
+    "kc_unet_pool2": (I_, [P_, I_, I_, I_, P_, P_]),
+    "kc_unet_pool2_bwd": (I_, [P_, I_, I_, I_, P_, I_, P_]),
+    "kc_unet_up2_concat": (I_, [P_, I_, P_, I_, I_, I_, P_, P_]),
+    "kc_unet_up2_concat_bwd": (I_, [P_, I_, I_, I_, I_, P_, P_, I_, P_]),
+    "kc_unet_relu_bwd": (I_, [P_, P_, L_, P_]),
+    "kc_unet_head": (I_, [P_, I_, L_, P_, P_, P_, P_]),
+    "kc_unet_head_bwd": (I_, [P_, I_, L_, P_, P_, P_, P_, P_, P_]),
+    "kc_unet_mse": (I_, [P_, P_, P_, L_, C.c_float, P_, P_, P_]),
+    "kc_unet_adam": (I_, [P_, P_, P_, P_, L_, C.c_float, C.c_float, C.c_float, C.c_float, I_, P_, P_]),
+    "kc_unet_to_bf16": (I_, [P_, P_, L_, P_]),
+    "kc_unet_features_ws_bytes": (S_, [I_]),
+    "kc_unet_features": (I_, [P_, P_, I_, I_, I_, I_, P_, P_, P_, P_, S_, P_]),
+    "kc_unet_guess_up2": (I_, [P_, I_, I_, P_, I_, I_, P_, P_, P_]),
+    "kc_unet_target_down2": (I_, [P_, P_, I_, I_, P_, I_, I_, P_, P_, P_]),
 }
 
 _lock = threading.Lock()

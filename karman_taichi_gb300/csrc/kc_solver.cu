@@ -1684,6 +1684,9 @@ static int read_state(const SolverState* st, HostState* h, cudaStream_t s) {
 }
 
 // ---- CUDA-graph cache for chunks of iterations --------------------------------
+// A captured chunk bakes in every pointer and parameter its launches take, so
+// the key holds all of them: buffers can be freed and their addresses handed
+// out again for a system of another form, size or multigrid configuration.
 struct GraphKey {
     const void* ws;
     const void* coef;
@@ -1691,11 +1694,22 @@ struct GraphKey {
     long long n;
     int stride, dtype, pre, chunk, kind;
     long long cs, es;
+    int form = 0;
+    unsigned long long ohash = 0;   // hash of the multigrid options (0: none)
     bool operator<(const GraphKey& o) const {
-        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es) <
-               std::tie(o.ws, o.coef, o.x, o.n, o.stride, o.dtype, o.pre, o.chunk, o.kind, o.cs, o.es);
+        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es, form, ohash) <
+               std::tie(o.ws, o.coef, o.x, o.n, o.stride, o.dtype, o.pre, o.chunk, o.kind, o.cs, o.es, o.form,
+                        o.ohash);
     }
 };
+
+// FNV-1a over the bytes of an options struct
+static unsigned long long bytes_hash(const void* p, size_t n) {
+    unsigned long long h = 1469598103934665603ull;
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h | 1ull;
+}
 static std::mutex g_graph_mu;
 static std::map<std::pair<int, GraphKey>, cudaGraphExec_t> g_graphs;
 
@@ -1932,6 +1946,7 @@ static int bicg_impl(const kc_system* A, const void* b, void* x, const void* M, 
     dim3 sg = stencil_grid(A->n, A->stride);
     const long long max_iter = o->max_iter;
     GraphKey key{ws, A->coef, x, A->n, A->stride, A->dtype, pre ? 1 : 0, 16, is_cg ? 1 : 0, A->cs, A->es};
+    key.form = A->form;
     HostState h{};
     const double lim = A->dtype == KC_F64 ? 1e300 : 1e30;
     StartArgs sa{o->eps, max_iter, o->omega_break, o->rel_to, o->history, o->history ? o->history_len : 0, lim};
@@ -2308,6 +2323,8 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     bool applied = false;
     const StartArgs sa{eps_inner, 0, 0, KC_REL_R0, nullptr, 0, 1e30};
     GraphKey key{ws, A32->coef, mg_ws, n, A32->stride, KC_F32, cg ? 8 : 7, 4, 2, A32->cs, A32->es};
+    key.form = A32->form;
+    key.ohash = bytes_hash(mg_opts, sizeof(kc_mg_opts));
     for (int it = 0; it <= max_refine; ++it) {
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2);
         KC_LAUNCH_CHECK("k_refine_resid");
@@ -2345,9 +2362,12 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
         }
         best = std::min(best, rel);
         if (it == max_refine || total >= o->max_iter) break;
-        // inner FP32 solve of A d = r32 from d = 0
+        // inner FP32 solve of A d = r32 from d = 0, to eps_inner -- or less
+        // far when that overshoots the target: a sweep that reduces its
+        // residual by 0.5 eps / rel reaches ||r|| / ||b|| < eps
         StartArgs si = sa;
         si.max_iter = o->max_iter - total;
+        si.eps = std::max(eps_inner, 0.5 * o->eps / rel);
         KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
         // the cold start zeroes an FP32 iterate and writes r~: both go to
         // slots that are scratch until a V-cycle writes them

@@ -190,3 +190,30 @@ def test_pcg_refined_solve(dev, case):
         xs = np.zeros_like(xg)
         xs[rows] = spla.spsolve(Acsr[rows][:, rows].tocsc(), b.reshape(-1)[rows])
         assert np.abs(xg - xs).max() <= 1e-6 * np.abs(xs).max()
+
+
+def test_graph_cache_tells_forms_apart(dev):
+    """Captured iteration graphs bake in the coefficient form: solving a
+    standard-form and then a Laplacian-form system in the same buffers (same
+    addresses, as a recycling allocator would hand out) must not replay the
+    first system's graph."""
+    from karman_taichi_gb300 import _lib as L, linalg
+    coef, b = _channel_pcorr(256, 64, 8, 64, 32)
+    NX, NY = coef.shape[1:]
+    A64 = linalg.Stencil(_t(coef, dev))
+    buf = _t(coef.astype(np.float32), dev)
+    ws = linalg.Workspace(dev)
+    bt = _t(b, dev)
+    mg = linalg.Multigrid(linalg.Stencil(buf)).setup()
+    x = _t(np.zeros((NX, NY)), dev)
+    first = linalg.pcg_refined(A64, linalg.Stencil(buf), bt, x, mg, eps=1e-8, ws=ws)
+    assert first.ok, first
+    buf.copy_(_t(O.to_laplacian32(coef), dev))                 # same address, Laplacian form
+    lap = linalg.Stencil(buf, form=L.FORM_LAPLACIAN)
+    mg.A = lap
+    mg.setup()
+    x.zero_()
+    second = linalg.pcg_refined(A64, lap, bt, x, mg, eps=1e-8, ws=ws)
+    assert second.ok, second
+    res = b.reshape(-1) - O.spmv(coef.reshape(5, -1), x.cpu().numpy().reshape(-1), NY)
+    assert np.linalg.norm(res) / np.linalg.norm(b) < 1e-8
