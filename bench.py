@@ -153,12 +153,12 @@ def make_solver(cfg, mode, dev):
     return ChannelSolver(cfg, device=dev, precision="fp64" if mode == "fp64" else "mixed")
 
 
-def resolve_mode(mode):
+def resolve_mode(mode, config="channel_2048x512"):
     if mode != "auto":
         return mode
     try:
         from karman_taichi_gb300 import learned
-        if learned.available():
+        if learned.available(config):
             return "learned"
     except ImportError:
         pass
@@ -381,7 +381,7 @@ def run_gpu(args):
     torch.cuda.set_device(dev)
     lib = L.load()
     cfg = PRESETS[args.config]
-    mode = resolve_mode(args.mode)
+    mode = resolve_mode(args.mode, args.config)
     peak, peak_kind = peaks()
     out = {"metric": METRIC, "unit": "time steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None}
@@ -530,7 +530,7 @@ def run_profile_outer(args):
     import torch
     from karman_taichi_gb300.config import PRESETS
     cfg = PRESETS[args.config]
-    solver = make_solver(cfg, resolve_mode(args.mode), torch.device("cuda", 0))
+    solver = make_solver(cfg, resolve_mode(args.mode, cfg.name), torch.device("cuda", 0))
     for _ in range(args.profile_outer):
         rec = solver.outer_iteration()
     torch.cuda.synchronize()
