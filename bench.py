@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--spmv-sweep", action="store_true",
                     help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
+    ap.add_argument("--batch-instances", type=int, default=0, metavar="N",
+                    help="time the batched configuration (N independent channel instances, stream-parallel) and exit")
+    ap.add_argument("--batch-workers", type=int, default=16)
     ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
                     help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
                          "(the command the committed ncu summaries were captured on)")
@@ -318,6 +321,32 @@ def spmv_roofline(solver, peak):
     return out
 
 
+def field_writer_roofline(solver, peak):
+    """post_process_field (kc_post_process: cell-centre velocities, udiv, the
+    five display canvases) on the final state, timed with CUDA events after an
+    L2 flush.  Algorithmic bytes: u, v, p, pcor, udiv read and u_post, v_post,
+    udiv written (FP64) by the first kernel, the five fields read again (FP64)
+    and the canvases written (9 FP32 pixels per cell) by the second."""
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=solver.device)
+    solver.post_process()
+    ts = []
+    for _ in range(5):
+        flush.add_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        solver.post_process()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    t = sorted(ts)[len(ts) // 2]
+    n = solver.p.numel()
+    alg = 8 * (solver.u.numel() + solver.v.numel() + 3 * n) + 8 * 3 * n + 8 * 5 * n + 4 * 5 * 9 * n
+    gbs = alg / (t * 1e-3) / 1e9
+    return {"kernels": "k_post_cells + k_post_disp", "us": round(t * 1e3, 1), "algorithmic_bytes": alg,
+            "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+
+
 def cpu_sample(cfg, budget_s, iters_per_step):
     """C/OpenMP FP64 plain path on the host cores: one SIMPLE outer iteration
     with each BiCGSTAB solve capped so the sample fits the budget."""
@@ -413,6 +442,7 @@ def run_gpu(args):
         out["roofline"] = roofline_p_solve(solver, mode, peak)
         out["roofline"]["peak_kind"] = peak_kind
         out["spmv"] = spmv_roofline(solver, peak)
+        out["field_writer"] = field_writer_roofline(solver, peak)
 
     fp64_counts = summ if mode == "fp64" else None
     if rank == 0 and not args.no_compare and mode != "fp64":
@@ -526,6 +556,36 @@ def run_spmv_sweep(args):
     print(json.dumps({"spmv_sweep": rows}), flush=True)
 
 
+def run_batch(args):
+    """Instance time steps/s of the batched configuration: N instances (sizes
+    128x32 .. 640x128, D 4-16, Re 60-200) stepped concurrently, one CUDA stream
+    per instance, against the same instances stepped one after another on one
+    stream.  W warm-up steps, then K timed steps of every instance."""
+    import numpy as np
+    import torch
+    from karman_taichi_gb300.batch import BatchedChannels, batch_configs
+    mode = "fp64" if args.mode == "fp64" else "mixed"
+    cfgs = batch_configs(args.batch_instances, seed=0)
+    out = {"metric": "instance time steps/s, batched channel instances", "unit": "instance time steps/s",
+           "instances": len(cfgs), "cells": int(sum(c.cells for c in cfgs)), "mode": mode,
+           "steps": args.steps, "warmup": args.warmup}
+    for workers in (args.batch_workers, 1):
+        b = BatchedChannels(cfgs, precision=mode, workers=workers)
+        b.step(args.warmup)
+        t = b.step(args.steps)
+        outer = np.mean([len(r) for rec in b.records for r in rec[args.warmup:]])
+        key = "concurrent" if workers > 1 else "sequential"
+        out[key] = {"workers": workers, "seconds": round(t, 3),
+                    "value": round(len(cfgs) * args.steps / t, 2),
+                    "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
+                    "outer_per_step": round(float(outer), 2)}
+        b.close()
+        del b
+        torch.cuda.empty_cache()
+    out["speedup_concurrent_vs_sequential"] = round(out["concurrent"]["value"] / out["sequential"]["value"], 2)
+    print(json.dumps(out), flush=True)
+
+
 def run_profile_outer(args):
     import torch
     from karman_taichi_gb300.config import PRESETS
@@ -545,5 +605,7 @@ if __name__ == "__main__":
         run_profile_outer(a)
     elif a.spmv_sweep:
         run_spmv_sweep(a)
+    elif a.batch_instances > 0:
+        run_batch(a)
     else:
         run_gpu(a)

@@ -356,6 +356,24 @@ int kc_unet_guess_up2(const float* out, int Hh, int Wh, const float* coef32, int
 int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, const double* scales,
                          int Hh, int Wh, float* target, float* weight, void* stream);
 
+/* ---- output post-processing ----------------------------------------------- */
+/* post_process_field (karman_taichi.py:545-583) on the padded staggered fields
+ * (u [nx+3][ny+2], v [nx+2][ny+3], p and pcor [nx+2][ny+2]):
+ *   u_post[i][j] = (u[i][j] + u[i+1][j]) / 2, v_post[i][j] = (v[i][j] + v[i][j+1]) / 2,
+ *   udiv[i][j] = (u[i][j] - u[i+1][j]) dy + (v[i][j+1] - v[i][j]) dx for i in [1,nx], j in [1,ny]
+ *   (other entries of udiv untouched);
+ *   minmax[2f], minmax[2f+1] = min, max of field f in (u_post, v_post, p, pcor, udiv), starting
+ *   from max 0 and min 1e9 as scale_field does (karman_taichi.py:573-583);
+ *   disp (nullable, FP32 [5][3(nx+2)][3(ny+2)]): the display canvases, field f at cell (I/3, J/3)
+ *   scaled by (x - min) / (max - min + 1e-9).
+ * minmax is device memory (10 doubles); ws: kc_post_process_ws_bytes() bytes, zeroed before the
+ * first call. */
+size_t kc_post_process_ws_bytes(void);
+int kc_post_process(int nx, int ny, double dx, double dy, const double* u, const double* v,
+                    const double* p, const double* pcor, double* u_post, double* v_post,
+                    double* udiv, double* minmax, float* disp, void* ws, size_t ws_bytes,
+                    void* stream);
+
 /* ---- utilities ------------------------------------------------------------ */
 /* dst = src (device to device), e.g. time_forward (karman_taichi.py:617-622). */
 int kc_copy(void* dst, const void* src, size_t bytes, void* stream);

@@ -140,6 +140,8 @@ SIGNATURES = {
     "kc_unet_mse": (I_, [P_, P_, P_, L_, C.c_float, P_, P_, P_]),
     "kc_unet_adam": (I_, [P_, P_, P_, P_, L_, C.c_float, C.c_float, C.c_float, C.c_float, I_, P_, P_]),
     "kc_unet_to_bf16": (I_, [P_, P_, L_, P_]),
+    "kc_post_process_ws_bytes": (S_, []),
+    "kc_post_process": (I_, [I_, I_, D_, D_, P_, P_, P_, P_, P_, P_, P_, P_, P_, P_, S_, P_]),
     "kc_unet_features_ws_bytes": (S_, [I_]),
     "kc_unet_features": (I_, [P_, P_, I_, I_, I_, I_, P_, P_, P_, P_, S_, P_]),
     "kc_unet_guess_up2": (I_, [P_, I_, I_, P_, I_, I_, P_, P_, P_]),

@@ -1,0 +1,89 @@
+"""Many independent channel instances on one GPU (the batched configuration).
+
+Each instance is a full :class:`ChannelSolver` (its own fields, systems and
+workspaces) bound to its own CUDA stream.  A pool of host threads drives the
+instances -- worker w steps instances w, w + W, w + 2W, ... -- and every
+library call enqueues on the calling thread's current stream, so kernels of
+different instances run concurrently: an instance of 4k-82k cells fills a
+few SMs, a batch fills the 152.  The C library is safe for this use: error
+messages are thread-local, the captured-graph cache is guarded, captures run
+in thread-local mode on private streams, and the launch counter is atomic.
+The ctypes calls and stream synchronisations release the Python GIL.
+
+An instance run in a batch computes bit for bit what it computes alone (the
+kernels and reductions are deterministic and instances share no buffers).
+The reference has no batched mode; instances are independent, so there is no
+exchange between them ("replicas" at the scale of one GPU).
+"""
+from __future__ import annotations
+
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import torch
+
+from .channel import ChannelSolver
+from .config import ChannelConfig
+
+SIZES = ((128, 32), (256, 64), (320, 64), (512, 128), (640, 128))
+
+
+def batch_configs(n=256, seed=0, n_steps=50):
+    """The batched configuration: n channel instances, sizes from SIZES, obstacle
+    diameter D in [4, 16] cells, centre x in [0.15, 0.3] of the length, y within
+    +-10% of the centre line, Re ~ U[60, 200], per-instance noise seed; dx = dy =
+    1/ny (unit channel height)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        nx, ny = SIZES[int(rng.integers(len(SIZES)))]
+        D = int(rng.integers(4, 17))
+        ci = int(round(nx * rng.uniform(0.15, 0.3)))
+        cj = int(round(ny * (0.5 + rng.uniform(-0.1, 0.1))))
+        Re = float(rng.uniform(60.0, 200.0))
+        out.append(ChannelConfig(f"batch{k:03d}_{nx}x{ny}", nx, ny, 1.0 / ny, D, (("circle", ci, cj, D),), Re=Re,
+                                 n_steps=n_steps, seed=int(rng.integers(2 ** 31))))
+    return out
+
+
+class BatchedChannels:
+    def __init__(self, configs, device="cuda", precision="mixed", workers=16, use_graph=True):
+        dev = torch.device(device)
+        self.device = torch.device("cuda", torch.cuda.current_device() if dev.index is None else dev.index)
+        self.configs = list(configs)
+        self.workers = max(1, min(workers, len(self.configs)))
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in self.configs]
+        self.solvers = []
+        for cfg, st in zip(self.configs, self.streams):
+            with torch.cuda.stream(st):
+                self.solvers.append(ChannelSolver(cfg, device=self.device, precision=precision, use_graph=use_graph))
+        torch.cuda.synchronize(self.device)
+        self.pool = ThreadPoolExecutor(max_workers=self.workers)
+        self.records = [[] for _ in self.configs]
+        self._err = None
+
+    def _run_group(self, w, n_steps):
+        torch.cuda.set_device(self.device)
+        for k in range(w, len(self.solvers), self.workers):
+            with torch.cuda.stream(self.streams[k]):
+                for _ in range(n_steps):
+                    self.records[k].append(self.solvers[k].step())
+            self.streams[k].synchronize()
+
+    def step(self, n_steps=1):
+        """n_steps time steps of every instance; returns the wall time in seconds."""
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        futs = [self.pool.submit(self._run_group, w, n_steps) for w in range(self.workers)]
+        for f in futs:
+            f.result()
+        torch.cuda.synchronize(self.device)
+        return time.perf_counter() - t0
+
+    def cells(self):
+        return sum(c.cells for c in self.configs)
+
+    def close(self):
+        self.pool.shutdown(wait=True)

@@ -29,6 +29,7 @@ SOURCES = {
     "kc_karman.cu": ["-fmad=false"],
     "kc_mg.cu": [],
     "kc_unet.cu": [],
+    "kc_fields.cu": [],
 }
 
 

@@ -26,6 +26,7 @@ optional ``learned`` object supplies the initial guess of p'
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -205,6 +206,27 @@ class ChannelSolver:
             if callback:
                 callback(k, rec, time.perf_counter() - t)
         return self.history
+
+    def post_process(self, canvases=True):
+        """post_process_field (karman_taichi.py:545-583) of the current fields: device arrays
+        u_post, v_post, udiv, minmax and (canvases) u/v/p/pcor/udiv_disp."""
+        from .fields import PostProcessor
+        if getattr(self, "_post", None) is None:
+            self._post = PostProcessor(self.cfg.nx, self.cfg.ny, self.device)
+            self.udiv = torch.zeros_like(self.p)
+        return self._post(self.u, self.v, self.p, self.pcor, self.udiv, self.cfg.dx, self.cfg.dy, canvases)
+
+    def write_fields(self, step, directory=".", images=False):
+        """The every-10-steps dump of karman_taichi.py:677-683 (CSV), optionally the five canvases as PGM."""
+        from . import fields
+        out = self.post_process(canvases=images)
+        paths = fields.write_timestep(step, {"pcor": self.pcor, "p": self.p, "u": self.u, "v": self.v,
+                                             "udiv": self.udiv}, directory)
+        if images:
+            for name in fields.CANVASES:
+                paths.append(fields.write_pgm(out[name + "_disp"], os.path.join(directory,
+                                                                                f"timestep{step:06}_{name}.pgm")))
+        return paths
 
     def mass_residual(self) -> float:
         """max |mdiv| of the current (corrected) field."""

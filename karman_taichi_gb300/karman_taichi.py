@@ -139,6 +139,20 @@ def correct_conserv(st):
             "kc_karman_correct_conserv")
 
 
+def post_process_field(st, canvases=True):
+    """karman_taichi.py:545-583: cell-centre velocities, udiv, display canvases (device arrays)."""
+    from .fields import PostProcessor
+    if getattr(st, "_post", None) is None:
+        st._post = PostProcessor(st.cfg.nx, st.cfg.ny, st.device)
+    return st._post(st.u, st.v, st.p, st.pcor, st.udiv, st.cfg.dx, st.cfg.dy, canvases)
+
+
+def write_matrix(mat, name):
+    """karman_taichi.py:157-159."""
+    from .fields import write_matrix as wm
+    wm(mat, name)
+
+
 def time_forward(st):
     """karman_taichi.py:617-622."""
     lib = L.load()

@@ -19,6 +19,7 @@ compute_mdiv / update_velocity (bicgsimp.py:114-122, 212-225).
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import torch
 
@@ -161,6 +162,23 @@ class SIMPLESolver:
 
     def bicg_solve_pcorrection_eqn(self, eps):
         return self.solve_pcorrection_eqn(eps)
+
+    def dump_matrix(self, step, msg, directory="log"):
+        """simple.py:51-54: u, v, p, mdiv, pcor to {directory}/{step:06}-{name}-{msg}.csv."""
+        from .fields import savetxt
+        os.makedirs(directory, exist_ok=True)
+        for name, val in {"u": self.u, "v": self.v, "p": self.p, "mdiv": self.mdiv, "pcor": self.pcor}.items():
+            savetxt(os.path.join(directory, f"{step:06}-{name}-{msg}.csv"), val)
+
+    def dump_coef(self, step, msg, directory="log"):
+        """simple.py:56-75: the five coefficient planes and b of u, v, p (file names as the reference's,
+        including the space in 'bu -', 'bv -', 'bp -')."""
+        from .fields import savetxt
+        os.makedirs(directory, exist_ok=True)
+        for tag, coef, b in (("u", self.coef_u, self.b_u), ("v", self.coef_v, self.b_v), ("p", self.coef_p, self.b_p)):
+            for k, comp in enumerate(("ap", "aw", "ae", "an", "as")):
+                savetxt(os.path.join(directory, f"{step:06}-{comp}{tag}-{msg}.csv"), coef[k])
+            savetxt(os.path.join(directory, f"{step:06}-b{tag} -{msg}.csv"), b)
 
     def init(self):
         """simple.py:257-264 (bicgsimp.py:246-256 also zeroes u0, v0, pcor)."""

@@ -1063,3 +1063,23 @@ class MultigridOracle:
             for _ in range(self.nu_post):
                 self._rb(L, bs[l], xs[l], 1); self._rb(L, bs[l], xs[l], 0)
         return xs[0].reshape(-1)
+
+
+def post_process_field(u, v, p, pcor, udiv, dx, dy):
+    """post_process_field, karman_taichi.py:545-583, and scale_field, :573-583
+    (whose min / max start from 1e9 / 0).  Returns u_post, v_post, udiv (interior
+    updated, rest as given), minmax [5][2] for (u_post, v_post, p, pcor, udiv)
+    and the five 3x-upsampled canvases scaled to [0, 1]."""
+    u, v, p, pcor = (np.asarray(a, dtype=np.float64) for a in (u, v, p, pcor))
+    udiv = np.array(udiv, dtype=np.float64, copy=True)
+    NX, NY = p.shape
+    nx, ny = NX - 2, NY - 2
+    u_post = 0.5 * (u[:NX, :] + u[1:NX + 1, :])
+    v_post = 0.5 * (v[:, :NY] + v[:, 1:NY + 1])
+    udiv[1:nx + 1, 1:ny + 1] = ((u[1:nx + 1, 1:ny + 1] - u[2:nx + 2, 1:ny + 1]) * dy
+                                + (v[1:nx + 1, 2:ny + 2] - v[1:nx + 1, 1:ny + 1]) * dx)
+    fields = (u_post, v_post, p, pcor, udiv)
+    minmax = np.array([[min(1.0e9, f.min()), max(0.0, f.max())] for f in fields])
+    disp = np.stack([np.repeat(np.repeat((f - lo) / (hi - lo + 1.0e-9), 3, axis=0), 3, axis=1)
+                     for f, (lo, hi) in zip(fields, minmax)])
+    return u_post, v_post, udiv, minmax, disp

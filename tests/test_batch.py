@@ -1,0 +1,35 @@
+"""Batched channel instances: the configuration generator (CPU) and bitwise
+equality of an instance run in a batch with the same instance run alone (GPU)."""
+import numpy as np
+import pytest
+
+
+def test_batch_configs_follow_the_spec():
+    from karman_taichi_gb300.batch import SIZES, batch_configs
+    cfgs = batch_configs(256, seed=0)
+    assert len(cfgs) == 256 and cfgs == batch_configs(256, seed=0)
+    for c in cfgs:
+        assert (c.nx, c.ny) in SIZES
+        assert 4 <= c.D <= 16 and 60 <= c.Re <= 200
+        shape, ci, cj, D = c.obstacles[0]
+        assert 0.15 * c.nx - 1 <= ci <= 0.3 * c.nx + 1 and abs(cj - c.ny / 2) <= 0.1 * c.ny + 1
+    assert len({c.seed for c in cfgs}) > 250
+    mean_cells = np.mean([c.cells for c in cfgs])
+    assert 25_000 < mean_cells < 50_000
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_instances_match_solo_runs(dev, precision):
+    from karman_taichi_gb300.batch import BatchedChannels, batch_configs
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfgs = [c.with_(max_outer=8) for c in batch_configs(6, seed=3)]
+    b = BatchedChannels(cfgs, device=dev, precision=precision, workers=3)
+    b.step(2)
+    for cfg, s in zip(cfgs, b.solvers):
+        solo = ChannelSolver(cfg, device=dev, precision=precision)
+        solo.step(); solo.step()
+        a, r = s.state_numpy(), solo.state_numpy()
+        for k in ("u", "v", "p"):
+            assert np.array_equal(a[k], r[k]), (cfg.name, k)
+    b.close()
