@@ -169,7 +169,7 @@ def resolve_mode(mode, config="channel_2048x512"):
 
 
 def summarize(recs_per_step):
-    outer = [len(r) for r in recs_per_step]
+    outer = [sum(s.get("outer", 1) for s in r) for r in recs_per_step]
     its = [sum(s["it_u"] + s["it_v"] + s["it_p"] for s in r) for r in recs_per_step]
     itp = [sum(s["it_p"] for s in r) for r in recs_per_step]
     mass = [r[-1]["mass"] for r in recs_per_step]
@@ -569,20 +569,22 @@ def run_batch(args):
     out = {"metric": "instance time steps/s, batched channel instances", "unit": "instance time steps/s",
            "instances": len(cfgs), "cells": int(sum(c.cells for c in cfgs)), "mode": mode,
            "steps": args.steps, "warmup": args.warmup}
-    for workers in (args.batch_workers, 1):
+    for key, workers, native in (("native_concurrent", args.batch_workers, True), ("sequential", 1, True)):
         b = BatchedChannels(cfgs, precision=mode, workers=workers)
-        b.step(args.warmup)
-        t = b.step(args.steps)
-        outer = np.mean([len(r) for rec in b.records for r in rec[args.warmup:]])
-        key = "concurrent" if workers > 1 else "sequential"
-        out[key] = {"workers": workers, "seconds": round(t, 3),
+        run = b.step_native if native else b.step
+        run(args.warmup)
+        t = run(args.steps)
+        outer = np.mean([sum(s.get("outer", 1) for s in r) for rec in b.records for r in rec[args.warmup:]])
+        out[key] = {"workers": workers, "driver": "native threads" if native else "python threads",
+                    "seconds": round(t, 3),
                     "value": round(len(cfgs) * args.steps / t, 2),
                     "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
                     "outer_per_step": round(float(outer), 2)}
         b.close()
         del b
         torch.cuda.empty_cache()
-    out["speedup_concurrent_vs_sequential"] = round(out["concurrent"]["value"] / out["sequential"]["value"], 2)
+    out["value"] = out["native_concurrent"]["value"]
+    out["speedup_concurrent_vs_sequential"] = round(out["native_concurrent"]["value"] / out["sequential"]["value"], 2)
     print(json.dumps(out), flush=True)
 
 

@@ -102,6 +102,8 @@ const char* kc_last_error(void);
 int         kc_device_count(void);
 /* Kernels launched by this library in this process (graph nodes included). */
 long long   kc_launch_count(void);
+/* sizeof of an ABI struct by name ("kc_system", "kc_channel", ...; 0 if unknown). */
+size_t      kc_struct_size(const char* name);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),
@@ -355,6 +357,50 @@ int kc_unet_guess_up2(const float* out, int Hh, int Wh, const float* coef32, int
 /* Half-resolution training target: 2x2 fluid average of p / s_p and the fluid share as weight. */
 int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, const double* scales,
                          int Hh, int Wh, float* target, float* weight, void* stream);
+
+/* ---- native SIMPLE step and the batched executor --------------------------- */
+/* One channel instance (caller-owned device buffers, shapes as kc_assemble_*).
+ * precision KC_F64: the plain method (every solve FP64 BiCGSTAB, cold start,
+ * rel. tol eps, cap n); KC_F32: the accelerated path (momentum: FP32 BiCGSTAB
+ * in FP64 refinement, inner tol eps_inner; p': multigrid CG in FP64
+ * refinement on coef_p32 in Laplacian form, inner tol eps_inner_p, with the
+ * plain FP64 BiCGSTAB as fallback).  Workspaces: ws_u / ws_v of
+ * kc_bicgstab_ws_bytes (F64) or kc_refined_ws_bytes (F32) bytes; ws_p of
+ * kc_bicgstab_ws_bytes (F64) or the larger of that and kc_pbicgstab_ws_bytes
+ * (F32); mg_ws of kc_mg_ws_bytes (F32 only); rws of kc_reduce_ws_bytes. */
+typedef struct {
+    kc_phys phys;                       /* mode must be KC_MODE_CHANNEL */
+    int precision, max_outer, use_graph;
+    int persistent;                     /* 1: BiCGSTAB solves as one cooperative launch, 0: graph chunks */
+    double mass_tol, eps, eps_inner, eps_inner_p;
+    double *u, *v, *p, *u0, *v0, *pcor, *u_mid, *v_mid;
+    const unsigned char* solid;         /* [nx+2][ny+2], 1 = blocked cell */
+    double *coef_u, *b_u, *coef_v, *b_v, *coef_p, *b_p;
+    float *coef_u32, *b_u32, *coef_v32, *b_v32, *coef_p32, *b_p32;
+    double *mass, *pmax;                /* device scalars: [2] and [1] */
+    void* rws;
+    void *ws_u, *ws_v, *ws_p;
+    size_t ws_u_bytes, ws_v_bytes, ws_p_bytes;
+    void* mg_ws;
+    size_t mg_ws_bytes;
+    kc_mg_opts mg_opts;
+} kc_channel;
+
+typedef struct {
+    int outer, fallbacks, status, pad_;   /* status: KC_OK, or KC_MAXITER if a solve missed eps */
+    long long it_u, it_v, it_p;
+    double mass;                          /* max|mdiv| of the last outer iteration */
+} kc_channel_stats;
+
+/* One time step: SIMPLE outer iterations (karman_taichi.py:633-659, simple.py:270-281)
+ * until max|mdiv| <= mass_tol or max_outer, then u0 = u, v0 = v (karman_taichi.py:617-622).
+ * No reference counterpart as a single call: the reference drives these stages from Python. */
+int kc_channel_step(const kc_channel* ch, kc_channel_stats* stats, void* stream);
+/* steps time steps of n independent instances, instance k on streams[k], driven by
+ * `workers` native threads (instance k by thread k mod workers); stats[k] (nullable) gets
+ * instance k's last step.  The first error stops all workers and is returned. */
+int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* streams, int workers,
+                          int steps, kc_channel_stats* stats);
 
 /* ---- output post-processing ----------------------------------------------- */
 /* post_process_field (karman_taichi.py:545-583) on the padded staggered fields

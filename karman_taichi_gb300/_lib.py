@@ -69,6 +69,23 @@ class KcMgOpts(C.Structure):
                 ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
 
 
+class KcChannel(C.Structure):
+    _fields_ = [("phys", KcPhys),
+                ("precision", C.c_int), ("max_outer", C.c_int), ("use_graph", C.c_int), ("persistent", C.c_int),
+                ("mass_tol", C.c_double), ("eps", C.c_double), ("eps_inner", C.c_double), ("eps_inner_p", C.c_double)]
+    _fields_ += [(k, C.c_void_p) for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid",
+                                          "coef_u", "b_u", "coef_v", "b_v", "coef_p", "b_p",
+                                          "coef_u32", "b_u32", "coef_v32", "b_v32", "coef_p32", "b_p32",
+                                          "mass", "pmax", "rws", "ws_u", "ws_v", "ws_p")]
+    _fields_ += [("ws_u_bytes", C.c_size_t), ("ws_v_bytes", C.c_size_t), ("ws_p_bytes", C.c_size_t),
+                 ("mg_ws", C.c_void_p), ("mg_ws_bytes", C.c_size_t), ("mg_opts", KcMgOpts)]
+
+
+class KcChannelStats(C.Structure):
+    _fields_ = [("outer", C.c_int), ("fallbacks", C.c_int), ("status", C.c_int), ("pad_", C.c_int),
+                ("it_u", C.c_longlong), ("it_v", C.c_longlong), ("it_p", C.c_longlong), ("mass", C.c_double)]
+
+
 class KcKarman(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
                 ("rho", C.c_double), ("mu", C.c_double), ("dt", C.c_double),
@@ -89,6 +106,7 @@ SIGNATURES = {
     "kc_last_error": (C.c_char_p, []),
     "kc_device_count": (I_, []),
     "kc_launch_count": (L_, []),
+    "kc_struct_size": (S_, [C.c_char_p]),
     "kc_spmv": (I_, [C.POINTER(KcSystem), P_, P_, P_]),
     "kc_dot_ws_bytes": (S_, [L_]),
     "kc_dot": (I_, [I_, L_, P_, P_, P_, P_, S_, P_]),
@@ -140,6 +158,9 @@ SIGNATURES = {
     "kc_unet_mse": (I_, [P_, P_, P_, L_, C.c_float, P_, P_, P_]),
     "kc_unet_adam": (I_, [P_, P_, P_, P_, L_, C.c_float, C.c_float, C.c_float, C.c_float, I_, P_, P_]),
     "kc_unet_to_bf16": (I_, [P_, P_, L_, P_]),
+    "kc_channel_step": (I_, [C.POINTER(KcChannel), C.POINTER(KcChannelStats), P_]),
+    "kc_channel_batch_step": (I_, [C.POINTER(C.POINTER(KcChannel)), I_, C.POINTER(P_), I_, I_,
+                                   C.POINTER(KcChannelStats)]),
     "kc_post_process_ws_bytes": (S_, []),
     "kc_post_process": (I_, [I_, I_, D_, D_, P_, P_, P_, P_, P_, P_, P_, P_, P_, P_, S_, P_]),
     "kc_unet_features_ws_bytes": (S_, [I_]),

@@ -30,6 +30,7 @@ SOURCES = {
     "kc_mg.cu": [],
     "kc_unet.cu": [],
     "kc_fields.cu": [],
+    "kc_channel.cu": [],
 }
 
 

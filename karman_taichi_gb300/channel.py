@@ -40,7 +40,7 @@ from .linalg import Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, p
 
 class ChannelSolver:
     def __init__(self, cfg: ChannelConfig, device="cuda", precision="fp64", use_graph=True,
-                 eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4):
+                 eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4, native=True):
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.cfg, self.precision, self.use_graph = cfg, precision, use_graph
@@ -89,6 +89,11 @@ class ChannelSolver:
         ph.alpha_m, ph.alpha_u, ph.alpha_p = cfg.alpha_m, cfg.alpha_u, cfg.alpha_p
         self.phys = ph
         self.history = []        # per time step: list of per-outer-iteration records
+        # the native step (kc_channel_step) runs the whole outer loop in the library; the
+        # Python loop below it is kept for the learned guess and for stage-by-stage use
+        self.native = bool(native) and (precision == "fp64" or self.mg is not None)
+        self.persistent = True   # BiCGSTAB solves as one cooperative launch (native step)
+        self._chan = None
         self.reset()
 
     # ---- state ------------------------------------------------------------------
@@ -186,8 +191,54 @@ class ChannelSolver:
         return dict(mass=mass, it_u=iu.iters, it_v=iv.iters, it_p=ip.iters,
                     st=(iu.status, iv.status, ip.status), ref=(iu.refinements, iv.refinements, ip.refinements))
 
+    # ---- native step ------------------------------------------------------------------
+    def native_struct(self):
+        """The kc_channel descriptor of this solver (buffers preallocated to the sizes the
+        native step needs)."""
+        if self._chan is not None:
+            return self._chan
+        lib = L.load()
+        c = L.KcChannel()
+        c.phys = self.phys
+        c.precision = L.F64 if self.precision == "fp64" else L.F32
+        c.max_outer, c.use_graph, c.persistent = self.cfg.max_outer, int(self.use_graph), int(self.persistent)
+        c.mass_tol, c.eps, c.eps_inner, c.eps_inner_p = self.cfg.mass_tol, self.cfg.eps, self.eps_inner, self.eps_inner_p
+        for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid", "coef_u", "b_u", "coef_v", "b_v",
+                  "coef_p", "b_p", "coef_u32", "b_u32", "coef_v32", "b_v32", "coef_p32", "b_p32", "mass", "pmax",
+                  "rws"):
+            t = getattr(self, k)
+            setattr(c, k, None if t is None else t.data_ptr())
+        sizes = {}
+        for k, A in (("u", self.A_u), ("v", self.A_v), ("p", self.A_p)):
+            plain = lib.kc_bicgstab_ws_bytes(A.n, A.stride, L.F64)
+            if self.precision == "fp64":
+                sizes[k] = plain
+            elif k == "p":
+                sizes[k] = max(plain, lib.kc_pbicgstab_ws_bytes(A.n, A.stride))
+            else:
+                sizes[k] = lib.kc_refined_ws_bytes(A.n, A.stride)
+        for k, ws in (("u", self.ws_u), ("v", self.ws_v), ("p", self.ws_p)):
+            buf = ws.get(sizes[k])
+            setattr(c, "ws_" + k, buf.data_ptr())
+            setattr(c, "ws_" + k + "_bytes", buf.numel())
+        if self.mg is not None:
+            c.mg_ws, c.mg_ws_bytes, c.mg_opts = self.mg.ws.data_ptr(), self.mg.ws.numel(), self.mg.opts
+        self._chan = c
+        return c
+
+    def _step_native(self):
+        st = L.KcChannelStats()
+        L.check(L.load().kc_channel_step(C.byref(self.native_struct()), C.byref(st), self._s()), "kc_channel_step")
+        self.fallbacks += st.fallbacks
+        rec = [dict(mass=st.mass, it_u=st.it_u, it_v=st.it_v, it_p=st.it_p, outer=st.outer, status=st.status)]
+        self.history.append(rec)
+        return rec
+
     def step(self):
-        """One time step; returns the per-outer-iteration records."""
+        """One time step; returns the per-outer-iteration records (native: one record
+        with the step's totals and its outer-iteration count)."""
+        if self.native and self.learned is None:
+            return self._step_native()
         rec = []
         for _ in range(self.cfg.max_outer):
             s = self.outer_iteration()

@@ -1,6 +1,7 @@
 // Library-level entry points of libkarman_gb300: version, status strings,
 // thread-local error text and device-to-device copies.
 #include "kc_common.cuh"
+#include <string>
 #include <stdarg.h>
 #include <stdio.h>
 #include <atomic>
@@ -22,6 +23,39 @@ void set_error(const char* fmt, ...) {
 int cuda_status(cudaError_t e, const char* what) {
     set_error("%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
     return KC_ERR_CUDA;
+}
+
+}  // namespace kc
+
+namespace kc {
+
+const void* readback(const void* src, size_t bytes, cudaStream_t s) {
+    struct Pinned {
+        void* p = nullptr;
+        ~Pinned() {
+            if (p) cudaFreeHost(p);
+        }
+    };
+    static thread_local Pinned buf;
+    if (bytes > 4096) {
+        set_error("readback of %zu bytes exceeds the 4096-byte pinned buffer", bytes);
+        return nullptr;
+    }
+    if (!buf.p) {
+        cudaError_t e = cudaMallocHost(&buf.p, 4096);
+        if (e != cudaSuccess) {
+            buf.p = nullptr;
+            cuda_status(e, "cudaMallocHost (readback buffer)");
+            return nullptr;
+        }
+    }
+    cudaError_t e = cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cuda_status(e, "readback");
+        return nullptr;
+    }
+    return buf.p;
 }
 
 }  // namespace kc
@@ -67,4 +101,19 @@ int kc_copy(void* dst, const void* src, size_t bytes, void* stream) {
     return KC_OK;
 }
 
+
+// sizeof of the ABI structs, for bindings that mirror them (ctypes, cgo, ...)
+size_t kc_struct_size(const char* name) {
+    if (!name) return 0;
+    const std::string n(name);
+    if (n == "kc_system") return sizeof(kc_system);
+    if (n == "kc_solve_opts") return sizeof(kc_solve_opts);
+    if (n == "kc_solve_info") return sizeof(kc_solve_info);
+    if (n == "kc_mg_opts") return sizeof(kc_mg_opts);
+    if (n == "kc_phys") return sizeof(kc_phys);
+    if (n == "kc_karman") return sizeof(kc_karman);
+    if (n == "kc_channel") return sizeof(kc_channel);
+    if (n == "kc_channel_stats") return sizeof(kc_channel_stats);
+    return 0;
+}
 }  // extern "C"

@@ -1,0 +1,191 @@
+// Native SIMPLE time step and the batched executor.
+//
+// kc_channel_step runs one time step of the channel case entirely in C++:
+// the outer loop of karman_taichi.py:633-659 / simple.py:270-281 over the
+// library's own entry points (assembly, linear solves, relaxation, outlet,
+// pressure correction, correction), reading back one scalar (the mass
+// residual) per outer iteration, then u0 <- u, v0 <- v (time_forward,
+// karman_taichi.py:617-622).  It makes exactly the calls, with the same
+// options, as karman_taichi_gb300.channel.ChannelSolver.step, so both give
+// bitwise identical fields.
+//
+// kc_channel_batch_step steps many independent instances with a pool of
+// native threads, each instance on its own stream: no interpreter between the
+// launches of small instances, and their kernels overlap on the GPU.
+#include "kc_common.cuh"
+#include <algorithm>
+#include <cstring>
+#include <atomic>
+#include <string>
+#include <thread>
+#include <vector>
+
+using namespace kc;
+
+namespace {
+
+kc_system sys_of(long long NX, long long NY, const void* coef, int dtype, int form) {
+    kc_system A{};
+    A.n = NX * NY;
+    A.cs = NX * NY;
+    A.es = 1;
+    A.coef = coef;
+    A.stride = (int)NY;
+    A.dtype = dtype;
+    A.form = form;
+    return A;
+}
+
+kc_solve_opts opts_of(double eps, long long max_iter, int rel_to, int check_every, int use_graph, int persistent) {
+    kc_solve_opts o{};
+    o.eps = eps;
+    o.max_iter = max_iter;
+    o.x0 = KC_X0_ZERO;
+    o.precond = KC_PRECOND_NONE;
+    o.omega_break = 0;
+    o.rel_to = rel_to;
+    o.check_every = check_every;
+    o.use_graph = use_graph;
+    o.persistent = persistent;
+    o.history = nullptr;
+    o.history_len = 0;
+    return o;
+}
+
+// One momentum / plain system solve as ChannelSolver._solve does it.
+int solve_sys(const kc_channel* c, const kc_system& A64, const kc_system& A32, const double* b, double* x, void* ws,
+              size_t ws_bytes, kc_solve_info* info, cudaStream_t s) {
+    if (c->precision == KC_F64) {
+        const kc_solve_opts o = opts_of(c->eps, A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+        return kc_bicgstab(&A64, b, x, nullptr, ws, ws_bytes, &o, info, s);
+    }
+    const kc_solve_opts o = opts_of(c->eps, 50 * A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+    return kc_bicgstab_refined(&A64, &A32, b, x, ws, ws_bytes, &o, c->eps_inner, 30, info, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
+    if (!c) return set_error("kc_channel_step: null channel"), KC_ERR_ARG;
+    if (c->phys.mode != KC_MODE_CHANNEL) return set_error("kc_channel_step: phys.mode must be KC_MODE_CHANNEL"), KC_ERR_ARG;
+    if (c->precision != KC_F64 && c->precision != KC_F32) return set_error("kc_channel_step: bad precision"), KC_ERR_ARG;
+    const bool mixed = c->precision == KC_F32;
+    if (mixed && (!c->coef_u32 || !c->coef_v32 || !c->coef_p32 || !c->b_u32 || !c->b_v32 || !c->b_p32 || !c->mg_ws))
+        return set_error("kc_channel_step: mixed precision needs the FP32 systems and a multigrid workspace"),
+               KC_ERR_ARG;
+    cudaStream_t s = as_stream(stream);
+    const kc_phys* P = &c->phys;
+    const long long nx = P->nx, ny = P->ny;
+    const kc_system Au = sys_of(nx + 3, ny + 2, c->coef_u, KC_F64, KC_FORM_STANDARD);
+    const kc_system Av = sys_of(nx + 2, ny + 3, c->coef_v, KC_F64, KC_FORM_STANDARD);
+    const kc_system Ap = sys_of(nx + 2, ny + 2, c->coef_p, KC_F64, KC_FORM_STANDARD);
+    const kc_system Au32 = sys_of(nx + 3, ny + 2, c->coef_u32, KC_F32, KC_FORM_STANDARD);
+    const kc_system Av32 = sys_of(nx + 2, ny + 3, c->coef_v32, KC_F32, KC_FORM_STANDARD);
+    const kc_system Ap32 = sys_of(nx + 2, ny + 2, c->coef_p32, KC_F32, KC_FORM_LAPLACIAN);
+    kc_channel_stats S{};
+    int rc = KC_OK;
+    double mass = 0.0;
+    for (int outer = 0; outer < c->max_outer; ++outer) {
+        rc = kc_assemble_momentum(P, c->u, c->v, c->p, c->u0, c->v0, c->solid, c->coef_u, c->b_u, c->coef_v, c->b_v,
+                                  c->coef_u32, c->b_u32, c->coef_v32, c->b_v32, s);
+        if (rc < 0) return rc;
+        kc_solve_info iu{}, iv{}, ip{};
+        rc = solve_sys(c, Au, Au32, c->b_u, c->u_mid, c->ws_u, c->ws_u_bytes, &iu, s);
+        if (rc < 0) return rc;
+        rc = solve_sys(c, Av, Av32, c->b_v, c->v_mid, c->ws_v, c->ws_v_bytes, &iv, s);
+        if (rc < 0) return rc;
+        rc = kc_relax_velocity(P, c->solid, c->u_mid, c->v_mid, c->u, c->v, nullptr, c->rws, s);
+        if (rc < 0) return rc;
+        rc = kc_outlet_conserve(P, c->u, s);
+        if (rc < 0) return rc;
+        rc = kc_assemble_pcorr(P, c->u, c->v, c->coef_u, c->coef_v, c->solid, c->coef_p, c->b_p, c->coef_p32,
+                               c->b_p32, nullptr, c->mass, c->rws, s);
+        if (rc < 0) return rc;
+        if (mixed) {
+            rc = kc_mg_setup(&Ap32, c->mg_ws, c->mg_ws_bytes, &c->mg_opts, s);
+            if (rc < 0) return rc;
+            const kc_solve_opts o = opts_of(c->eps, 50 * Ap.n, KC_REL_B, 4, c->use_graph, 0);
+            rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, nullptr, c->mg_ws, &c->mg_opts, c->ws_p, c->ws_p_bytes,
+                                &o, c->eps_inner_p, 30, &ip, s);
+            if (rc < 0) return rc;
+            if (ip.status != KC_OK) {   // accelerated solve stalled: plain BiCGSTAB is the fallback
+                ++S.fallbacks;
+                const long long before = ip.iters;
+                const kc_solve_opts of = opts_of(c->eps, Ap.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+                rc = kc_bicgstab(&Ap, c->b_p, c->pcor, nullptr, c->ws_p, c->ws_p_bytes, &of, &ip, s);
+                if (rc < 0) return rc;
+                ip.iters += before;
+            }
+        } else {
+            const kc_solve_opts o = opts_of(c->eps, Ap.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+            rc = kc_bicgstab(&Ap, c->b_p, c->pcor, nullptr, c->ws_p, c->ws_p_bytes, &o, &ip, s);
+            if (rc < 0) return rc;
+        }
+        rc = kc_correct(P, c->pcor, c->coef_u, c->coef_v, c->solid, c->u, c->v, c->p, c->pmax, c->rws, s);
+        if (rc < 0) return rc;
+        S.outer += 1;
+        S.it_u += iu.iters;
+        S.it_v += iv.iters;
+        S.it_p += ip.iters;
+        if (iu.status != KC_OK || iv.status != KC_OK || ip.status != KC_OK) S.status = KC_MAXITER;
+        const void* hp = readback(c->mass, sizeof(double), s);
+        if (!hp) return KC_ERR_CUDA;
+        memcpy(&mass, hp, sizeof(double));
+        S.mass = mass;
+        if (mass <= c->mass_tol) break;
+    }
+    rc = kc_copy(c->u0, c->u, (size_t)((nx + 3) * (ny + 2)) * sizeof(double), s);
+    if (rc < 0) return rc;
+    rc = kc_copy(c->v0, c->v, (size_t)((nx + 2) * (ny + 3)) * sizeof(double), s);
+    if (rc < 0) return rc;
+    if (st) *st = S;
+    return KC_OK;
+}
+
+int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* streams, int workers, int steps,
+                          kc_channel_stats* stats) {
+    if (!chs || !streams || n < 0 || steps < 0) return set_error("kc_channel_batch_step: bad arguments"), KC_ERR_ARG;
+    if (n == 0 || steps == 0) return KC_OK;
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    workers = std::max(1, std::min(workers, n));
+    std::atomic<int> first_err{0};
+    std::vector<std::string> msgs(workers);
+    std::vector<std::thread> pool;
+    pool.reserve(workers);
+    for (int w = 0; w < workers; ++w) {
+        pool.emplace_back([&, w] {
+            if (cudaSetDevice(dev) != cudaSuccess) {
+                int z = 0;
+                first_err.compare_exchange_strong(z, KC_ERR_CUDA);
+                msgs[w] = "cudaSetDevice failed in a batch worker";
+                return;
+            }
+            for (int k = w; k < n; k += workers) {
+                for (int t = 0; t < steps && first_err.load() == 0; ++t) {
+                    const int rc = kc_channel_step(chs[k], stats ? &stats[k] : nullptr, streams[k]);
+                    if (rc < 0) {
+                        int z = 0;
+                        first_err.compare_exchange_strong(z, rc);
+                        msgs[w] = "instance " + std::to_string(k) + ": " + kc_last_error();
+                        return;
+                    }
+                }
+            }
+        });
+    }
+    for (auto& t : pool) t.join();
+    const int rc = first_err.load();
+    if (rc) {
+        for (const auto& m : msgs)
+            if (!m.empty()) {
+                set_error("kc_channel_batch_step: %s", m.c_str());
+                break;
+            }
+    }
+    return rc;
+}
+
+}  // extern "C"

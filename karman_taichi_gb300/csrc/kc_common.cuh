@@ -33,6 +33,14 @@ void count_launches(long long n);
     } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Small device -> host readbacks (solver state, residual norms) go through a
+// per-thread pinned buffer: a copy into pageable memory is staged by the
+// driver and serialises host threads that each drive their own stream.
+// Copies `bytes` (<= 4096) from device src on stream s, waits, returns a
+// pointer to the host copy (valid until this thread's next call), or null on
+// a CUDA error (reported through set_error).
+const void* readback(const void* src, size_t bytes, cudaStream_t s);
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // ---- warp / block reductions (fixed order => bitwise reproducible) --------

@@ -1670,9 +1670,10 @@ struct HostState {
 };
 
 static int read_state(const SolverState* st, HostState* h, cudaStream_t s) {
+    const void* hp = readback(st, sizeof(SolverState), s);
+    if (!hp) return KC_ERR_CUDA;
     SolverState tmp;
-    KC_CUDA(cudaMemcpyAsync(&tmp, st, sizeof(SolverState), cudaMemcpyDeviceToHost, s));
-    KC_CUDA(cudaStreamSynchronize(s));
+    memcpy(&tmp, hp, sizeof(SolverState));
     h->status = tmp.status;
     h->done = tmp.done;
     h->iter = tmp.iter;
@@ -2113,8 +2114,11 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[3];
-        KC_CUDA(cudaMemcpyAsync(h2, out2, sizeof(h2), cudaMemcpyDeviceToHost, s));
-        KC_CUDA(cudaStreamSynchronize(s));
+        {
+            const void* hp = readback(out2, sizeof(h2), s);
+            if (!hp) return KC_ERR_CUDA;
+            memcpy(h2, hp, sizeof(h2));
+        }
         bb = h2[1];
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
@@ -2329,8 +2333,11 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[3];
-        KC_CUDA(cudaMemcpyAsync(h2, out2, sizeof(h2), cudaMemcpyDeviceToHost, s));
-        KC_CUDA(cudaStreamSynchronize(s));
+        {
+            const void* hp = readback(out2, sizeof(h2), s);
+            if (!hp) return KC_ERR_CUDA;
+            memcpy(h2, hp, sizeof(h2));
+        }
         bb = h2[1];
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;

@@ -68,3 +68,15 @@ def test_library_has_no_cpu_fallback_symbols(lib):
     finally:
         L.LIB_PATH = real
         L._lib = old
+
+
+def test_struct_layouts_match_the_header():
+    """ctypes mirrors of the ABI structs have the C sizes (kc_struct_size)."""
+    import ctypes as C
+    from karman_taichi_gb300 import _lib as L
+    lib = L.load()
+    for name, cls in (("kc_system", L.KcSystem), ("kc_solve_opts", L.KcSolveOpts), ("kc_solve_info", L.KcSolveInfo),
+                      ("kc_mg_opts", L.KcMgOpts), ("kc_phys", L.KcPhys), ("kc_karman", L.KcKarman),
+                      ("kc_channel", L.KcChannel), ("kc_channel_stats", L.KcChannelStats)):
+        assert lib.kc_struct_size(name.encode()) == C.sizeof(cls), name
+    assert lib.kc_struct_size(b"nope") == 0

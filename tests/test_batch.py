@@ -33,3 +33,37 @@ def test_batched_instances_match_solo_runs(dev, precision):
         for k in ("u", "v", "p"):
             assert np.array_equal(a[k], r[k]), (cfg.name, k)
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_native_step_matches_python_step(dev, precision):
+    """kc_channel_step makes the calls ChannelSolver's Python loop makes: same fields bit for bit."""
+    from karman_taichi_gb300.batch import batch_configs
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfg = batch_configs(1, seed=5)[0].with_(max_outer=10)
+    a = ChannelSolver(cfg, device=dev, precision=precision, native=True)
+    b = ChannelSolver(cfg, device=dev, precision=precision, native=False)
+    for _ in range(2):
+        ra, rb = a.step(), b.step()
+        assert ra[0]["outer"] == len(rb)
+        assert ra[0]["it_p"] == sum(r["it_p"] for r in rb)
+    sa, sb = a.state_numpy(), b.state_numpy()
+    for k in ("u", "v", "p", "u0", "v0"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.gpu
+def test_native_batch_matches_solo_runs(dev):
+    from karman_taichi_gb300.batch import BatchedChannels, batch_configs
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfgs = [c.with_(max_outer=8) for c in batch_configs(8, seed=4)]
+    b = BatchedChannels(cfgs, device=dev, precision="mixed", workers=4)
+    b.step_native(2)
+    for cfg, s in zip(cfgs, b.solvers):
+        solo = ChannelSolver(cfg, device=dev, precision="mixed", native=False)
+        solo.step(); solo.step()
+        a, r = s.state_numpy(), solo.state_numpy()
+        for k in ("u", "v", "p"):
+            assert np.array_equal(a[k], r[k]), (cfg.name, k)
+    b.close()
