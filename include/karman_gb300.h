@@ -164,12 +164,18 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
  * debug/note.md:6); it has Jacobi only (karman_taichi.py:398-399).
  * Aggregation multigrid V-cycle for 2-D 5-point operators: 2x2 Galerkin
  * coarsening, red-black Gauss-Seidel smoothing with per-level weights
- * omega[l], coarse corrections scaled by alpha[l].  The operator must be a
- * genuine 2-D stencil on [n/stride][stride] (no links across row ends). */
+ * omega[l], coarse corrections scaled by alpha[l].  Links across the end of a
+ * row of [n/stride][stride] are treated as links to a zero cell.
+ * nu_pre = nu_post = 1 selects the fused cycle (two launches per level).
+ * coarsest_sweeps = 0: coarsening stops at <= 128 cells, whose dense
+ * operator is inverted at setup (exact coarsest solve; a non-positive pivot
+ * falls back to 64 Jacobi sweeps); > 0: coarsening stops at <= 1024 cells,
+ * solved by that many Jacobi sweeps.  kc_mg_default_opts: nu 1/1, exact
+ * coarsest solve, omega 1.0, alpha 1.6. */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */
-    int coarsest_sweeps;          /* Jacobi sweeps on the coarsest level (<= 1024 cells)   */
+    int coarsest_sweeps;          /* 0: exact coarsest solve; > 0: Jacobi sweeps            */
     int max_levels;
     float omega[KC_MG_MAX_LEVELS];/* smoother weight per level                            */
     float alpha[KC_MG_MAX_LEVELS];/* coarse-correction scale per level                    */

@@ -128,9 +128,10 @@ class ChannelSolver:
     def _solve(self, A, A32, b, x, ws):
         cfg = self.cfg
         if self.precision == "fp64":
-            return bicgstab(A, b, x, eps=cfg.eps, max_iter=A.n, ws=ws, use_graph=self.use_graph)
+            return bicgstab(A, b, x, eps=cfg.eps, max_iter=A.n, ws=ws, use_graph=self.use_graph,
+                            persistent=self.persistent)
         return bicgstab_refined(A, A32, b, x, eps=cfg.eps, eps_inner=self.eps_inner, ws=ws,
-                                use_graph=self.use_graph)
+                                use_graph=self.use_graph, persistent=self.persistent)
 
     def solve_momentum(self):
         iu = self._solve(self.A_u, getattr(self, "A_u32", None), self.b_u, self.u_mid, self.ws_u)
@@ -164,7 +165,7 @@ class ChannelSolver:
             # accelerated solve stalled: plain BiCGSTAB is the fallback
             self.fallbacks += 1
             plain = bicgstab(self.A_p, self.b_p, self.pcor, eps=self.cfg.eps, max_iter=self.A_p.n, ws=self.ws_p,
-                             use_graph=self.use_graph)
+                             use_graph=self.use_graph, persistent=self.persistent)
             plain.iters += info.iters
             return plain
         return self._solve(self.A_p, getattr(self, "A_p32", None), self.b_p, self.pcor, self.ws_p)

@@ -150,4 +150,45 @@ struct ReduceWs {
 };
 constexpr int kReduceMaxBlocks = 4096;
 
+// ---- bounded grid barrier for cooperative (persistent) kernels ---------------
+// Blocks meet here between phases.  A wait gives up after kSpinLimit polls,
+// raises err and every block leaves: no wait can run forever.
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    int err;
+    int pad;
+};
+constexpr unsigned kSpinLimit = 1u << 22;   // ~0.5 s at 40 ns per poll: far beyond any healthy wait
+
+__device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &bar->gen;
+        volatile int* err = &bar->err;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&bar->count, 1u) == nb - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            unsigned spins = 0;
+            while (*gen == g) {
+                if (*err) break;
+                if (++spins > kSpinLimit) {
+                    atomicExch(&bar->err, 1);
+                    break;
+                }
+                __nanosleep(40);
+            }
+        }
+        __threadfence();
+        ok = *err == 0;
+    }
+    __syncthreads();
+    return ok;
+}
+
 }  // namespace kc

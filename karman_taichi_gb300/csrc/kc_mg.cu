@@ -19,8 +19,9 @@
 //     visits the colours in the reverse order of the pre-smoother and the
 //     coarsest solve is a fixed number of Jacobi sweeps, so for a symmetric
 //     operator the V-cycle is a symmetric linear operator (usable by CG);
-//   * coarsest level (<= kCoarsestMax cells): Jacobi sweeps in shared memory
-//     by one block.
+//   * coarsest level: exact (<= kCoarseDirectMax cells, dense inverse formed at
+//     setup, coarsest_sweeps = 0) or Jacobi sweeps in shared memory by one
+//     block (<= kCoarsestMax cells, coarsest_sweeps > 0).
 // Level 0 is the caller's system (n = NX*NY, far stride NY); levels >= 1 live
 // in the multigrid workspace.  The cycle treats every level as a 2-D
 // [NX][NY] grid with zero values outside it (a link across the end of a row
@@ -33,7 +34,9 @@
 
 namespace kc {
 
-constexpr int kCoarsestMax = 1024;
+constexpr int kCoarsestMax = 1024;      // coarsest level of the Jacobi variant (cells)
+constexpr int kCoarseDirectMax = 128;   // coarsest level of the direct variant (cells)
+constexpr int kCoarseFallbackSweeps = 64;
 
 __device__ __forceinline__ bool mg_done(const int* done) { return done && __ldcg(done) != 0; }
 
@@ -191,12 +194,84 @@ __global__ void k_mg_prolong(Lvl F, float* __restrict__ x, const float* __restri
     }
 }
 
-// coarsest level: Jacobi sweeps in shared memory (one block, n <= kCoarsestMax)
+// ---- coarsest level ------------------------------------------------------------------
+// Direct variant (coarsest_sweeps == 0): coarsening stops at <= kCoarseDirectMax
+// cells, setup inverts the level's dense operator in place by Gauss-Jordan
+// elimination without pivoting (the operator is symmetric positive definite:
+// Galerkin coarsening of the symmetric p' operator with its Dirichlet outlet
+// folded into the row sums; a zero row -- no coupled child -- gets a unit
+// diagonal, its right-hand side is zero), and the cycle applies x = A^-1 b.
+// A non-positive or non-finite pivot sets the flag and the cycle falls back
+// to kCoarseFallbackSweeps Jacobi sweeps.
+__global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __restrict__ inv, int* __restrict__ flag) {
+    extern __shared__ float A[];   // n x n, row major
+    const int n = L.NX * L.NY, NY = L.NY;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = 0.f;
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const long long ce = (long long)k * L.es;
+        const float c0 = L.c[ce], w = L.c[L.cs + ce], ea = L.c[2 * L.cs + ce], no = L.c[3 * L.cs + ce],
+                    so = L.c[4 * L.cs + ce];
+        const int j = k % NY;
+        float d = L.lap ? c0 - (((w + ea) + no) + so) : c0;   // out-of-grid neighbours hold zero
+        if (w == 0.f && ea == 0.f && no == 0.f && so == 0.f && d == 0.f) d = 1.f;   // no coupled child
+        A[k * n + k] = d;
+        if (k >= NY) A[k * n + k - NY] = w;
+        if (k + NY < n) A[k * n + k + NY] = ea;
+        if (j + 1 < NY) A[k * n + k + 1] = no;
+        if (j >= 1) A[k * n + k - 1] = so;
+    }
+    __syncthreads();
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    __shared__ float col[kCoarseDirectMax];
+    for (int p = 0; p < n; ++p) {
+        const float piv = A[p * n + p];
+        if (!(piv > 0.f) || !isfinite(piv)) {
+            if (threadIdx.x == 0) bad = 1;
+            break;   // uniform: every thread reads the same pivot
+        }
+        const float ip = 1.f / piv;
+        __syncthreads();
+        // the pivot column of the other rows, and the scaled pivot row
+        for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = A[i * n + p];
+        for (int j = threadIdx.x; j < n; j += blockDim.x) A[p * n + j] = j == p ? ip : A[p * n + j] * ip;
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // eliminate (reads row p, writes the others)
+            const int i = e / n, j = e - i * n;
+            if (i == p) continue;
+            A[e] = j == p ? -col[i] * ip : fmaf(-col[i], A[p * n + j], A[e]);
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = A[e];
+    if (threadIdx.x == 0) *flag = bad;
+}
+
+// x = A^-1 b (one warp per row), or Jacobi sweeps when sweeps > 0 or the inverse failed
 __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float* __restrict__ b,
-                                                              float* __restrict__ x, int sweeps, const int* done) {
+                                                              float* __restrict__ x, int sweeps,
+                                                              const float* __restrict__ inv,
+                                                              const int* __restrict__ inv_bad, const int* done) {
     if (mg_done(done)) return;
-    __shared__ float xs[2][kCoarsestMax];
     const int n = L.NX * L.NY;
+    if (sweeps == 0) {
+        if (!__ldcg(inv_bad)) {
+            const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            for (int i = wp; i < n; i += nw) {
+                float sacc = 0.f;
+                for (int j = lane; j < n; j += 32) sacc = fmaf(inv[i * n + j], b[j], sacc);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sacc += __shfl_down_sync(kFull, sacc, o);
+                if (lane == 0) x[i] = sacc;
+            }
+            return;
+        }
+        sweeps = kCoarseFallbackSweeps;
+    }
+    __shared__ float xs[2][kCoarsestMax];
     const int k = threadIdx.x;
     float bk = 0.f, w = 0.f, c[5] = {0, 0, 0, 0, 0};
     if (k < n) {
@@ -231,7 +306,8 @@ template <int TI, int AJ, int RY>
 __global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
                                                      float* __restrict__ bc, int NXc, int NYc, const int* done) {
     if (mg_done(done)) return;
-    mg_down_tile<TI, AJ, RY, false>(L, b, nullptr, 0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc);
+    mg_down_tile<TI, AJ, RY, false>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, b, nullptr, 0.f, MgNoMid{}, MgOwnNone{},
+                                    xout, bc, NXc, NYc);
 }
 
 template <int TI, int AJ, int RY>
@@ -240,7 +316,7 @@ __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restr
                                                    const float* __restrict__ b, float* __restrict__ xout,
                                                    const int* done) {
     if (mg_done(done)) return;
-    mg_up_tile<TI, AJ, RY>(L, xpre, xc, NXc, NYc, alpha, b, MgOwnNone{}, xout);
+    mg_up_tile<TI, AJ, RY>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b, MgOwnNone{}, xout);
 }
 
 // large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
@@ -252,7 +328,8 @@ static int mg_levels(int NX, int NY, const kc_mg_opts* o, int* nx, int* ny) {
     nx[0] = NX;
     ny[0] = NY;
     const int maxl = std::max(1, std::min(o ? o->max_levels : KC_MG_MAX_LEVELS, (int)KC_MG_MAX_LEVELS));
-    while (L + 1 < maxl && (long long)nx[L] * ny[L] > kCoarsestMax) {
+    const long long target = (o && o->coarsest_sweeps == 0) ? kCoarseDirectMax : kCoarsestMax;
+    while (L + 1 < maxl && (long long)nx[L] * ny[L] > target) {
         nx[L + 1] = (nx[L] + 1) / 2;
         ny[L + 1] = (ny[L] + 1) / 2;
         ++L;
@@ -281,6 +358,10 @@ MgLayout mg_layout(int NX, int NY, const kc_mg_opts* o) {
         M.off_t[l] = off;
         off = align256(off + n * 4);
     }
+    M.off_inv = off;
+    off = align256(off + (size_t)kCoarseDirectMax * kCoarseDirectMax * 4);
+    M.off_flag = off;
+    off = align256(off + 16);
     M.total = off;
     return M;
 }
@@ -365,6 +446,20 @@ int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o,
                                        (float*)(base + M.off_winv[l + 1]), (unsigned char*)(base + M.off_iso[l + 1]));
         KC_LAUNCH_CHECK("k_mg_coarsen");
     }
+    if (o->coarsest_sweeps == 0) {   // direct coarsest solve: invert the coarsest operator
+        const int l = M.levels - 1;
+        const int nc = M.nx[l] * M.ny[l];
+        const Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
+        const size_t smem = (size_t)nc * nc * sizeof(float);
+        static bool attr_set = false;   // 64 KB of dynamic shared memory needs the opt-in once
+        if (!attr_set) {
+            KC_CUDA(cudaFuncSetAttribute(k_mg_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(kCoarseDirectMax * kCoarseDirectMax * sizeof(float))));
+            attr_set = true;
+        }
+        k_mg_coarse_inverse<<<1, 1024, smem, s>>>(L, (float*)(base + M.off_inv), (int*)(base + M.off_flag));
+        KC_LAUNCH_CHECK("k_mg_coarse_inverse");
+    }
     return KC_OK;
 }
 
@@ -416,7 +511,8 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
         const int l = M.levels - 1;
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
         k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, (const float*)(base + M.off_b[l]), mg_final(M, base, l),
-                                                 o->coarsest_sweeps, done);
+                                                 o->coarsest_sweeps, (const float*)(base + M.off_inv),
+                                                 (const int*)(base + M.off_flag), done);
         KC_LAUNCH_CHECK_NC("k_mg_coarsest");
         ++nk;
     }
@@ -464,7 +560,9 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
         Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
         const long long n = (long long)M.nx[l] * M.ny[l];
         if (l == M.levels - 1) {
-            k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, bl[l], xl[l], o->coarsest_sweeps, done);
+            k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, bl[l], xl[l], o->coarsest_sweeps,
+                                                     (const float*)(base + M.off_inv), (const int*)(base + M.off_flag),
+                                                     done);
             KC_LAUNCH_CHECK_NC("k_mg_coarsest");
             ++nk;
             break;
@@ -513,13 +611,13 @@ extern "C" {
 
 void kc_mg_default_opts(kc_mg_opts* o) {
     if (!o) return;
-    o->nu_pre = 2;
-    o->nu_post = 2;
-    o->coarsest_sweeps = 64;
+    o->nu_pre = 1;             // the fused two-launch-per-level cycle
+    o->nu_post = 1;
+    o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
     for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
-        o->omega[l] = 0.8f;
-        o->alpha[l] = 1.8f;
+        o->omega[l] = 1.0f;
+        o->alpha[l] = 1.6f;
     }
 }
 

@@ -91,17 +91,15 @@ struct MgTile {
     static_assert((AJ & (AJ - 1)) == 0, "row width must be a power of two");
     __device__ static __forceinline__ int tx() { return threadIdx.x & (AJ - 1); }
     __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
-    __device__ static __forceinline__ int i0() { return blockIdx.y * TI; }
-    __device__ static __forceinline__ int j0() { return blockIdx.x * TJ; }
 };
 
-// stage the 5 coefficient components over the whole staged region
+// stage the 5 coefficient components over the whole staged region of the tile at (i0, j0)
 template <int TI, class T>
-__device__ __forceinline__ void mg_stage_coef(const MgLvl& L, float* sc) {
-    const int b = T::tx(), j = T::j0() + b - 2;
+__device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, float* sc) {
+    const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = T::i0() + a - 2;
+        const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
         const float* g = in ? L.c + (long long)(i * L.NY + j) * L.es : L.c;
         const int u = a * T::AJ + b;
@@ -121,9 +119,9 @@ __device__ __forceinline__ bool mg_linked_smem(const float* sc, int u) {
     return sc[T::A + u] != 0.f || sc[2 * T::A + u] != 0.f || sc[3 * T::A + u] != 0.f || sc[4 * T::A + u] != 0.f;
 }
 
-// DOWN tile.  b = HasQ ? b_in - alpha q : b_in over the staged region.
+// DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
 template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own>
-__device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const float* __restrict__ b_in,
+__device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
                                                           const float* __restrict__ q, float alpha, const Mid& mid,
                                                           const Own& own, float* __restrict__ xout,
                                                           float* __restrict__ bc, int NXc, int NYc) {
@@ -131,12 +129,12 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
     __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
     __shared__ __align__(16) float sq[HasQ ? T::A : 1];
     __shared__ __align__(16) float sc[5 * T::A];
-    const int b = T::tx(), j = T::j0() + b - 2;
+    const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
     typename Own::Sum sum{};
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = T::i0() + a - 2;
+        const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
@@ -144,7 +142,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
         if (HasQ) cp_async4(sq + u, q + k, in);
         cp_async4(sw + u, L.winv + k, in);
     }
-    mg_stage_coef<TI, T>(L, sc);
+    mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     mid();
     cp_async_wait_all();
@@ -152,7 +150,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
     // b, owned cells, red start (x = W b on red, 0 on black)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
-        const int i = T::i0() + a - 2;
+        const int i = i0 + a - 2;
         float bv = sb[u];
         if (HasQ) {
             bv = fmaf(-alpha, sq[u], bv);
@@ -173,13 +171,13 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
     // owned cells: write x
     if (jown)
         for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
-            const int i = T::i0() + a - 2;
+            const int i = i0 + a - 2;
             if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + b];
         }
     // aggregates: restricted residual over coupled cells
     for (int t = threadIdx.x; t < (TI / 2) * (T::TJ / 2); t += T::NT) {
         const int ag = t / (T::TJ / 2), bg = t - ag * (T::TJ / 2);
-        const int I = (T::i0() >> 1) + ag, J = (T::j0() >> 1) + bg;
+        const int I = (i0 >> 1) + ag, J = (j0 >> 1) + bg;
         if (I >= NXc || J >= NYc) continue;
         float s = 0.f;
 #pragma unroll
@@ -187,7 +185,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
 #pragma unroll
             for (int dj = 0; dj < 2; ++dj) {
                 const int a = 2 * ag + di + 2, bb = 2 * bg + dj + 2;
-                if (T::i0() + a - 2 >= L.NX || T::j0() + bb - 2 >= L.NY) continue;
+                if (i0 + a - 2 >= L.NX || j0 + bb - 2 >= L.NY) continue;
                 const int u = a * T::AJ + bb;
                 if (!mg_linked_smem<T>(sc, u)) continue;
                 s += sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u);
@@ -197,10 +195,10 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(const MgLvl& L, const 
     return sum;
 }
 
-// UP tile: prolong (coupled cells, told apart by their links), black
-// half-sweep over the 1-cell ring, red half-sweep on the owned cells.
+// UP tile at (i0, j0): prolong (coupled cells, told apart by their links),
+// black half-sweep over the 1-cell ring, red half-sweep on the owned cells.
 template <int TI, int AJ, int RY, class Own>
-__device__ __forceinline__ typename Own::Sum mg_up_tile(const MgLvl& L, const float* __restrict__ xpre,
+__device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
                                                         const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                         const float* __restrict__ b_in, const Own& own,
                                                         float* __restrict__ xout) {
@@ -208,11 +206,11 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(const MgLvl& L, const fl
     constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
     __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
     __shared__ __align__(16) float sc[5 * T::A];
-    const int b = T::tx(), j = T::j0() + b - 2;
+    const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     typename Own::Sum sum{};
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = T::i0() + a - 2;
+        const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
@@ -222,11 +220,11 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(const MgLvl& L, const fl
     }
     for (int t = threadIdx.x; t < XI * XJ; t += T::NT) {
         const int ca = t / XJ, cb = t - ca * XJ;
-        const int I = (T::i0() >> 1) - 1 + ca, J = (T::j0() >> 1) - 1 + cb;
+        const int I = (i0 >> 1) - 1 + ca, J = (j0 >> 1) - 1 + cb;
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    mg_stage_coef<TI, T>(L, sc);
+    mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
@@ -248,7 +246,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(const MgLvl& L, const fl
     // red half-sweep on the owned cells, then write
     if (b >= 2 && b < T::TJ + 2 && j < L.NY)
         for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
-            const int i = T::i0() + a - 2;
+            const int i = i0 + a - 2;
             if (i >= L.NX) continue;
             const int u = a * T::AJ + b;
             float xv = sx[u];

@@ -884,44 +884,6 @@ __global__ void k_zero_f64(int n, double* __restrict__ x) {
 // flag, every block leaves its loop, and the host reports KC_ERR_CUDA.
 // Vectors written during the launch are read with ld.global.cg (L1 bypass).
 // =============================================================================
-struct GridBar {
-    unsigned count;
-    unsigned gen;
-    int err;
-    int pad;
-};
-constexpr unsigned kSpinLimit = 1u << 22;   // ~0.5 s at 40 ns per poll: far beyond any healthy wait
-
-__device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb) {
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* gen = &bar->gen;
-        volatile int* err = &bar->err;
-        const unsigned g = *gen;
-        __threadfence();
-        if (atomicAdd(&bar->count, 1u) == nb - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            unsigned spins = 0;
-            while (*gen == g) {
-                if (*err) break;
-                if (++spins > kSpinLimit) {
-                    atomicExch(&bar->err, 1);
-                    break;
-                }
-                __nanosleep(40);
-            }
-        }
-        __threadfence();
-        ok = *err == 0;
-    }
-    __syncthreads();
-    return ok;
-}
-
 // Block partial of NV accumulators -> partials[(slot+q)*ld + bid] (no ticket).
 template <typename T, int NV>
 __device__ __forceinline__ void store_block_partials(const Acc<T> (&a)[NV], double* partials, int ld, int slot,
@@ -1575,7 +1537,8 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restric
     const bool up = update != 0;
     const PcMidX<TI, TJ, NT> mid{V.x, V.p[cur ^ 1], __ldcg(&st->alpha), L.NX, L.NY, up};
     Acc<float> acc[1];
-    acc[0] = mg_down_tile<TI, AJ, RY, true>(L, V.r[cur], up ? V.q : V.r[cur], up ? __ldcg(&st->alpha_f) : 0.f, mid,
+    acc[0] = mg_down_tile<TI, AJ, RY, true>(blockIdx.y * TI, blockIdx.x * TJ, L, V.r[cur], up ? V.q : V.r[cur],
+                                            up ? __ldcg(&st->alpha_f) : 0.f, mid,
                                             PcOwnR{V.r[cur ^ 1], up}, x0pre, b1, NX1, NY1);
     if (!up) return;
     double s[1];
@@ -1600,7 +1563,8 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_up0(MgLvl L, const float* __res
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     Acc<float> acc[1];
-    acc[0] = mg_up_tile<TI, AJ, RY>(L, x0pre, final1, NX1, NY1, alpha0, V.r[(int)(it & 1)], PcUpOwn{}, V.z);
+    acc[0] = mg_up_tile<TI, AJ, RY>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, x0pre, final1, NX1, NY1, alpha0,
+                                    V.r[(int)(it & 1)], PcUpOwn{}, V.z);
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {

@@ -229,11 +229,12 @@ def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tenso
 
 class Multigrid:
     """Aggregation multigrid V-cycle (FP32) for a 2-D 5-point operator; the
-    right preconditioner of the mixed-precision pressure-correction solve.
+    preconditioner of the mixed-precision pressure-correction solve.
     ``omega`` / ``alpha`` are per-level smoother weights and coarse-correction
-    scales (scalars broadcast to all levels)."""
+    scales (scalars broadcast to all levels); ``coarsest_sweeps=0`` solves the
+    coarsest level (<= 128 cells) exactly."""
 
-    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=64, omega=1.0, alpha=1.6,
+    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.0, alpha=1.6,
                  max_levels=16):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")

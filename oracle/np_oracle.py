@@ -946,11 +946,13 @@ class MultigridOracle:
     links are isolated: solved pointwise, never aggregated, links into them
     folded into the row sum), red-black
     Gauss-Seidel smoothing weighted by omega[l], coarse corrections scaled by
-    alpha[l], Jacobi sweeps on the coarsest level (<= 1024 cells)."""
+    alpha[l]; on the coarsest level Jacobi sweeps (<= 1024 cells) or, with
+    coarsest_sweeps = 0, the exact solve by a dense FP32 inverse (<= 128 cells)."""
 
-    COARSEST = 1024
+    COARSEST = 1024          # coarsest level of the Jacobi variant (cells)
+    COARSEST_DIRECT = 128    # coarsest level of the direct variant (coarsest_sweeps = 0)
 
-    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=64, omega=1.0, alpha=1.6, max_levels=16,
+    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.0, alpha=1.6, max_levels=16,
                  lap=False):
         f32 = np.float32
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
@@ -960,11 +962,46 @@ class MultigridOracle:
         self.nu_pre, self.nu_post, self.sweeps = nu_pre, nu_post, coarsest_sweeps
         c = np.asarray(coef, dtype=f32).reshape(5, NX, NY)
         self.levels = [self._level(c, NX, NY, self.omega[0], lap)]
-        while len(self.levels) < max_levels and NX * NY > self.COARSEST:
+        target = self.COARSEST_DIRECT if coarsest_sweeps == 0 else self.COARSEST
+        while len(self.levels) < max_levels and NX * NY > target:
             NXc, NYc = (NX + 1) // 2, (NY + 1) // 2
             c = self._coarsen(c, self.levels[-1]["iso"], NX, NY, NXc, NYc, self.levels[-1]["lap"])
             NX, NY = NXc, NYc
             self.levels.append(self._level(c, NX, NY, self.omega[min(len(self.levels), 15)], True))
+        self.inv = self._coarse_inverse(self.levels[-1]) if coarsest_sweeps == 0 else None
+
+    @staticmethod
+    def _coarse_inverse(L):
+        """Dense FP32 inverse of the coarsest operator by in-place Gauss-Jordan
+        without pivoting (k_mg_coarse_inverse); None when a pivot is not positive."""
+        f = np.float32
+        c, NX, NY = L["c"], L["NX"], L["NY"]
+        n = NX * NY
+        cf = c.reshape(5, -1)
+        A = np.zeros((n, n), dtype=f)
+        for k in range(n):
+            w, e, no, so = cf[1, k], cf[2, k], cf[3, k], cf[4, k]
+            d = f(cf[0, k] - f(f(f(w + e) + no) + so)) if L["lap"] else cf[0, k]
+            if w == 0 and e == 0 and no == 0 and so == 0 and d == 0:
+                d = f(1)
+            A[k, k] = d
+            j = k % NY
+            if k >= NY: A[k, k - NY] = w
+            if k + NY < n: A[k, k + NY] = e
+            if j + 1 < NY: A[k, k + 1] = no
+            if j >= 1: A[k, k - 1] = so
+        for p in range(n):
+            piv = A[p, p]
+            if not (piv > 0) or not np.isfinite(piv):
+                return None
+            ip = f(1) / piv
+            col = A[:, p].copy()
+            A[p, :] = A[p, :] * ip
+            A[p, p] = ip
+            rows = np.arange(n) != p
+            A[rows, :] = (A[rows, :] - np.outer(col[rows], A[p, :])).astype(f)
+            A[rows, p] = (-col[rows] * ip).astype(f)
+        return A
 
     @staticmethod
     def _level(c, NX, NY, omega, lap):
@@ -1039,9 +1076,12 @@ class MultigridOracle:
         for l, L in enumerate(self.levels):
             b = bs[l]
             if l == nlev - 1:
-                x = L["winv"] * b
-                for _ in range(self.sweeps):
-                    x = x + L["winv"] * (b - self._Ax(L, x))
+                if self.sweeps == 0 and self.inv is not None:
+                    x = (self.inv @ b.reshape(-1)).astype(np.float32).reshape(b.shape)
+                else:
+                    x = L["winv"] * b
+                    for _ in range(self.sweeps if self.sweeps > 0 else 64):
+                        x = x + L["winv"] * (b - self._Ax(L, x))
                 xs.append(x)
                 break
             ii, jj = np.meshgrid(np.arange(L["NX"]), np.arange(L["NY"]), indexing="ij")

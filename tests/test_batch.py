@@ -28,6 +28,7 @@ def test_batched_instances_match_solo_runs(dev, precision):
     b.step(2)
     for cfg, s in zip(cfgs, b.solvers):
         solo = ChannelSolver(cfg, device=dev, precision=precision)
+        solo.persistent = False          # the batch solves in graph chunks (another reduction order)
         solo.step(); solo.step()
         a, r = s.state_numpy(), solo.state_numpy()
         for k in ("u", "v", "p"):
@@ -61,7 +62,8 @@ def test_native_batch_matches_solo_runs(dev):
     b = BatchedChannels(cfgs, device=dev, precision="mixed", workers=4)
     b.step_native(2)
     for cfg, s in zip(cfgs, b.solvers):
-        solo = ChannelSolver(cfg, device=dev, precision="mixed", native=False)
+        solo = ChannelSolver(cfg, device=dev, precision="mixed")
+        solo.persistent = False
         solo.step(); solo.step()
         a, r = s.state_numpy(), solo.state_numpy()
         for k in ("u", "v", "p"):

@@ -62,20 +62,24 @@ def _fp32(coef, lap):
     return coef.astype(np.float32), L.FORM_STANDARD
 
 
+@pytest.mark.parametrize("coarsest", [0, 64])   # 0: exact coarsest solve (dense inverse); 64: Jacobi sweeps
 @pytest.mark.parametrize("nu", [1, 2])   # 1: the fused two-launch-per-level cycle; 2: the general kernels
 @pytest.mark.parametrize("lap", [False, True])
 @pytest.mark.parametrize("alpha", [1.0, 1.6])
-def test_vcycle_matches_restatement(dev, alpha, lap, nu):
+def test_vcycle_matches_restatement(dev, alpha, lap, nu, coarsest):
     from karman_taichi_gb300 import linalg
     coef, b = _channel_pcorr(96, 40, 6, 30, 20)
     NX, NY = coef.shape[1:]
     c32, form = _fp32(coef, lap)
     A = linalg.Stencil(_t(c32, dev), form=form)
-    mg = linalg.Multigrid(A, alpha=alpha, nu_pre=nu, nu_post=nu).setup()
+    mg = linalg.Multigrid(A, alpha=alpha, nu_pre=nu, nu_post=nu, coarsest_sweeps=coarsest).setup()
     r = np.random.default_rng(0).standard_normal(NX * NY).astype(np.float32)
     r[coef[0].reshape(-1) == 0] = 0.0
     z = mg.apply(_t(r.reshape(NX, NY), dev)).cpu().numpy().reshape(-1)
-    ref = O.MultigridOracle(c32.reshape(5, -1), NX, NY, alpha=alpha, lap=lap, nu_pre=nu, nu_post=nu).apply(r)
+    orc = O.MultigridOracle(c32.reshape(5, -1), NX, NY, alpha=alpha, lap=lap, nu_pre=nu, nu_post=nu,
+                            coarsest_sweeps=coarsest)
+    assert coarsest != 0 or orc.inv is not None
+    ref = orc.apply(r)
     assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
