@@ -151,9 +151,11 @@ int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes,
           const kc_solve_opts* opts, kc_solve_info* info, void* stream);
 
 /* Mixed precision: FP64 residual r = b - A64 x, FP32 BiCGSTAB correction on
- * A32 (FP64 inner products), x += d, until ||r||/||b|| < opts->eps.  The
- * pressure-correction solve of the mixed SIMPLE path (simple.py:252-255,
- * karman_taichi.py:497-504 with precision split). */
+ * A32 (FP64 inner products), x += d, until ||r||/||b|| < opts->eps.  Each
+ * sweep solves to eps_inner, or only as far as the target needs
+ * (0.5 eps / the current ||r||/||b||) when that is looser.  opts->x0 =
+ * KC_X0_WARM starts from x (a warm start, as karman_taichi.py:362-371 does);
+ * otherwise x = 0.  The momentum solves of the mixed SIMPLE path. */
 size_t kc_refined_ws_bytes(long long n, int stride);
 int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b,
                         double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,

@@ -130,8 +130,10 @@ class ChannelSolver:
         if self.precision == "fp64":
             return bicgstab(A, b, x, eps=cfg.eps, max_iter=A.n, ws=ws, use_graph=self.use_graph,
                             persistent=self.persistent)
+        # warm start from the previous outer iteration's u*, v* (karman_taichi.py:362-371 warm-starts too);
+        # the stopping test is ||b - A x|| / ||b|| < eps, the reference's test for a cold start
         return bicgstab_refined(A, A32, b, x, eps=cfg.eps, eps_inner=self.eps_inner, ws=ws,
-                                use_graph=self.use_graph, persistent=self.persistent)
+                                use_graph=self.use_graph, persistent=self.persistent, warm=True)
 
     def solve_momentum(self):
         iu = self._solve(self.A_u, getattr(self, "A_u32", None), self.b_u, self.u_mid, self.ws_u)

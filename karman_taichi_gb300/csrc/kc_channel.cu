@@ -59,7 +59,8 @@ int solve_sys(const kc_channel* c, const kc_system& A64, const kc_system& A32, c
         const kc_solve_opts o = opts_of(c->eps, A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
         return kc_bicgstab(&A64, b, x, nullptr, ws, ws_bytes, &o, info, s);
     }
-    const kc_solve_opts o = opts_of(c->eps, 50 * A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+    kc_solve_opts o = opts_of(c->eps, 50 * A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
+    o.x0 = KC_X0_WARM;   // from the previous outer iteration's u*, v*
     return kc_bicgstab_refined(&A64, &A32, b, x, ws, ws_bytes, &o, c->eps_inner, 30, info, s);
 }
 

@@ -2060,7 +2060,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     dim3 sg = stencil_grid(n, A64->stride);
     int pb = pw_blocks(n);
     KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
-    k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);
+    if (o->x0 != KC_X0_WARM) k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);   // warm: x is the initial guess
     KC_CUDA(cudaMemsetAsync(out2, 0, 4 * sizeof(double), s));
     kc_solve_opts io = *o;
     io.eps = eps_inner;
@@ -2116,6 +2116,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         best = std::min(best, rel);
         if (it == max_refine || total >= o->max_iter) break;
         io.max_iter = o->max_iter - total;
+        io.eps = std::max(eps_inner, 0.5 * o->eps / rel);   // no deeper than the target needs
         kc_solve_info ii{};
         int r2 = kc_bicgstab(A32, r32, d32, nullptr, base + L.off_inner, L.inner_bytes, &io, &ii, stream);
         if (r2 < 0) return r2;

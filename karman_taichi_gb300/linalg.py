@@ -208,17 +208,18 @@ def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None,
 
 def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8,
                      eps_inner=1e-3, max_refine=30, max_iter=None, ws: Workspace | None = None,
-                     use_graph=True, persistent=True) -> SolveInfo:
+                     use_graph=True, persistent=True, warm=False) -> SolveInfo:
     """FP64-residual iterative refinement around an FP32 BiCGSTAB with FP64
-    inner products; stops when ||b - A64 x|| / ||b|| < eps."""
+    inner products; stops when ||b - A64 x|| / ||b|| < eps.  ``warm`` starts
+    from the given x instead of zero."""
     require_cuda(b, x)
     if A64.dtype != L.F64 or A32.dtype != L.F32:
         raise TypeError("bicgstab_refined needs an FP64 and an FP32 operator")
     lib = L.load()
     nbytes = lib.kc_refined_ws_bytes(A64.n, A64.stride)
     buf = (ws or Workspace(b.device)).get(nbytes)
-    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0,
-              0, use_graph, None, persistent)
+    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_WARM if warm else L.X0_ZERO,
+              L.PRECOND_NONE, 0, L.REL_R0, 0, use_graph, None, persistent)
     info = L.KcSolveInfo()
     rc = lib.kc_bicgstab_refined(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x), ptr(buf),
                                  buf.numel(), C.byref(o), float(eps_inner), int(max_refine), C.byref(info),
