@@ -173,7 +173,8 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
  * operator is inverted at setup (exact coarsest solve; a non-positive pivot
  * falls back to 64 Jacobi sweeps); > 0: coarsening stops at <= 1024 cells,
  * solved by that many Jacobi sweeps.  kc_mg_default_opts: nu 1/1, exact
- * coarsest solve, omega 1.0, alpha 1.6. */
+ * coarsest solve, omega 1.1, alpha 1.8 (the tuned setting for the channel's
+ * pressure correction). */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */

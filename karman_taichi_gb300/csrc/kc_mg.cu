@@ -302,21 +302,22 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
 }
 
 // ---- fused cycle kernels (one pre- and one post-sweep per level) ---------------------
-template <int TI, int AJ, int RY>
+template <int TI, int AJ, int RY, bool STAGED>
 __global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
                                                      float* __restrict__ bc, int NXc, int NYc, const int* done) {
     if (mg_done(done)) return;
-    mg_down_tile<TI, AJ, RY, false>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, b, nullptr, 0.f, MgNoMid{}, MgOwnNone{},
-                                    xout, bc, NXc, NYc);
+    mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, b, nullptr,
+                                                                0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc);
 }
 
-template <int TI, int AJ, int RY>
+template <int TI, int AJ, int RY, bool STAGED>
 __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restrict__ xpre,
                                                    const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                    const float* __restrict__ b, float* __restrict__ xout,
                                                    const int* done) {
     if (mg_done(done)) return;
-    mg_up_tile<TI, AJ, RY>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b, MgOwnNone{}, xout);
+    mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b,
+                                              MgOwnNone{}, xout);
 }
 
 // large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
@@ -398,10 +399,10 @@ static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, f
                        cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_down<kMgTI0, kMgAJ0, kMgRY0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+        k_mg_down<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
             G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
     else
-        k_mg_down<kMgTI1, kMgAJ1, kMgRY1><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
+        k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
             G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
     KC_LAUNCH_CHECK_NC("k_mg_down");
     return KC_OK;
@@ -411,10 +412,10 @@ static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, 
                      const float* b, float* xout, const int* done, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_up<kMgTI0, kMgAJ0, kMgRY0><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
+        k_mg_up<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
             G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
     else
-        k_mg_up<kMgTI1, kMgAJ1, kMgRY1><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
+        k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
             G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
     KC_LAUNCH_CHECK_NC("k_mg_up");
     return KC_OK;
@@ -616,8 +617,8 @@ void kc_mg_default_opts(kc_mg_opts* o) {
     o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
     for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
-        o->omega[l] = 1.0f;
-        o->alpha[l] = 1.6f;
+        o->omega[l] = 1.1f;
+        o->alpha[l] = 1.8f;
     }
 }
 

@@ -108,19 +108,32 @@ __device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, fl
     }
 }
 
-// (A x) at staged index u
-template <class T>
-__device__ __forceinline__ float mg_ax_smem(const float* sx, const float* sc, int lap, int u) {
-    return mg_row(sc[u], sc[T::A + u], sc[2 * T::A + u], sc[3 * T::A + u], sc[4 * T::A + u], lap, sx[u],
-                  sx[u - T::AJ], sx[u + T::AJ], sx[u + 1], sx[u - 1]);
-}
-template <class T>
-__device__ __forceinline__ bool mg_linked_smem(const float* sc, int u) {
-    return sc[T::A + u] != 0.f || sc[2 * T::A + u] != 0.f || sc[3 * T::A + u] != 0.f || sc[4 * T::A + u] != 0.f;
-}
+// Coefficients of a tile: staged in shared memory (STAGED) or read through
+// the read-only cache at the point of use (fewer staged arrays -> more
+// resident blocks).  Indexed by staged position u = a * AJ + b.
+template <class T, bool STAGED>
+struct MgCoef {
+    const float* sc;
+    MgLvl L;
+    int i0, j0;
+    __device__ __forceinline__ float get(int q, int u) const {
+        if (STAGED) return sc[q * T::A + u];
+        const int a = u / T::AJ, b = u - a * T::AJ;
+        const int i = i0 + a - 2, j = j0 + b - 2;
+        if (i < 0 || i >= L.NX || j < 0 || j >= L.NY) return 0.f;
+        return __ldg(L.c + q * L.cs + (long long)(i * L.NY + j) * L.es);
+    }
+    __device__ __forceinline__ float ax(const float* sx, int u) const {
+        return mg_row(get(0, u), get(1, u), get(2, u), get(3, u), get(4, u), L.lap, sx[u], sx[u - T::AJ],
+                      sx[u + T::AJ], sx[u + 1], sx[u - 1]);
+    }
+    __device__ __forceinline__ bool linked(int u) const {
+        return get(1, u) != 0.f || get(2, u) != 0.f || get(3, u) != 0.f || get(4, u) != 0.f;
+    }
+};
 
 // DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
-template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own>
+template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true>
 __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
                                                           const float* __restrict__ q, float alpha, const Mid& mid,
                                                           const Own& own, float* __restrict__ xout,
@@ -128,7 +141,8 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
     using T = MgTile<TI, AJ, RY>;
     __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
     __shared__ __align__(16) float sq[HasQ ? T::A : 1];
-    __shared__ __align__(16) float sc[5 * T::A];
+    __shared__ __align__(16) float sc[STAGED ? 5 * T::A : 1];
+    const MgCoef<T, STAGED> C{sc, L, i0, j0};
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
@@ -142,7 +156,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
         if (HasQ) cp_async4(sq + u, q + k, in);
         cp_async4(sw + u, L.winv + k, in);
     }
-    mg_stage_coef<TI, T>(L, i0, j0, sc);
+    if (STAGED) mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     mid();
     cp_async_wait_all();
@@ -165,7 +179,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
         for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
             if (((a + b) & 1) == 0) continue;
             const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), sx[u]);
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
         }
     __syncthreads();
     // owned cells: write x
@@ -187,8 +201,8 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
                 const int a = 2 * ag + di + 2, bb = 2 * bg + dj + 2;
                 if (i0 + a - 2 >= L.NX || j0 + bb - 2 >= L.NY) continue;
                 const int u = a * T::AJ + bb;
-                if (!mg_linked_smem<T>(sc, u)) continue;
-                s += sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u);
+                if (!C.linked(u)) continue;
+                s += sb[u] - C.ax(sx, u);
             }
         bc[I * NYc + J] = s;
     }
@@ -197,7 +211,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
 
 // UP tile at (i0, j0): prolong (coupled cells, told apart by their links),
 // black half-sweep over the 1-cell ring, red half-sweep on the owned cells.
-template <int TI, int AJ, int RY, class Own>
+template <int TI, int AJ, int RY, class Own, bool STAGED = true>
 __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
                                                         const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                         const float* __restrict__ b_in, const Own& own,
@@ -205,7 +219,8 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
     using T = MgTile<TI, AJ, RY>;
     constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
     __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
-    __shared__ __align__(16) float sc[5 * T::A];
+    __shared__ __align__(16) float sc[STAGED ? 5 * T::A : 1];
+    const MgCoef<T, STAGED> C{sc, L, i0, j0};
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     typename Own::Sum sum{};
@@ -224,14 +239,14 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    mg_stage_coef<TI, T>(L, i0, j0, sc);
+    if (STAGED) mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
     // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-2, j0-2)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
-        if (!mg_linked_smem<T>(sc, u)) continue;
+        if (!C.linked(u)) continue;
         sx[u] = fmaf(alpha, sxc[(a >> 1) * XJ + (b >> 1)], sx[u]);
     }
     __syncthreads();
@@ -240,7 +255,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
         for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
             if (((a + b) & 1) == 0) continue;
             const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), sx[u]);
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
         }
     __syncthreads();
     // red half-sweep on the owned cells, then write
@@ -250,7 +265,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
             if (i >= L.NX) continue;
             const int u = a * T::AJ + b;
             float xv = sx[u];
-            if (((a + b) & 1) == 0) xv = fmaf(sw[u], sb[u] - mg_ax_smem<T>(sx, sc, L.lap, u), xv);
+            if (((a + b) & 1) == 0) xv = fmaf(sw[u], sb[u] - C.ax(sx, u), xv);
             const int k = i * L.NY + j;
             xout[k] = xv;
             own(k, xv, sb[u], sum);

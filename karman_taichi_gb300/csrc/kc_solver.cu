@@ -1537,7 +1537,8 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restric
     const bool up = update != 0;
     const PcMidX<TI, TJ, NT> mid{V.x, V.p[cur ^ 1], __ldcg(&st->alpha), L.NX, L.NY, up};
     Acc<float> acc[1];
-    acc[0] = mg_down_tile<TI, AJ, RY, true>(blockIdx.y * TI, blockIdx.x * TJ, L, V.r[cur], up ? V.q : V.r[cur],
+    acc[0] = mg_down_tile<TI, AJ, RY, true, PcMidX<TI, TJ, NT>, PcOwnR, kMgStagedLarge>(
+        blockIdx.y * TI, blockIdx.x * TJ, L, V.r[cur], up ? V.q : V.r[cur],
                                             up ? __ldcg(&st->alpha_f) : 0.f, mid,
                                             PcOwnR{V.r[cur ^ 1], up}, x0pre, b1, NX1, NY1);
     if (!up) return;
@@ -1563,8 +1564,8 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_up0(MgLvl L, const float* __res
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     Acc<float> acc[1];
-    acc[0] = mg_up_tile<TI, AJ, RY>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, x0pre, final1, NX1, NY1, alpha0,
-                                    V.r[(int)(it & 1)], PcUpOwn{}, V.z);
+    acc[0] = mg_up_tile<TI, AJ, RY, PcUpOwn, kMgStagedLarge>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, x0pre, final1,
+                                                             NX1, NY1, alpha0, V.r[(int)(it & 1)], PcUpOwn{}, V.z);
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {

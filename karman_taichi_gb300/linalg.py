@@ -235,7 +235,7 @@ class Multigrid:
     scales (scalars broadcast to all levels); ``coarsest_sweeps=0`` solves the
     coarsest level (<= 128 cells) exactly."""
 
-    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.0, alpha=1.6,
+    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.1, alpha=1.8,
                  max_levels=16):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")
