@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <math.h>
+#include <utility>
 #include "karman_gb300.h"
 
 namespace kc {
@@ -33,6 +34,33 @@ void count_launches(long long n);
     } while (0)
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- programmatic dependent launch ---------------------------------------------
+// Kernels of a dependent chain (the CG iteration and its V-cycle) start with
+// pdl_wait(): it returns once the preceding grid has completed and its writes
+// are visible (at once when the kernel was launched without the attribute),
+// so it must come before any read of a predecessor's output.  pdl_trigger()
+// lets the next grid's blocks be scheduled while this grid finishes.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+constexpr bool kUsePDL = true;
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_chain(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                Args&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = kUsePDL ? at : nullptr;
+    cfg.numAttrs = kUsePDL ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Small device -> host readbacks (solver state, residual norms) go through a
 // per-thread pinned buffer: a copy into pageable memory is staged by the

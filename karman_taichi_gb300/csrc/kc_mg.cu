@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
                                                               float* __restrict__ x, int sweeps,
                                                               const float* __restrict__ inv,
                                                               const int* __restrict__ inv_bad, const int* done) {
+    pdl_wait();
+    pdl_trigger();   // one block: the next grid may queue up at once
     if (mg_done(done)) return;
     const int n = L.NX * L.NY;
     if (sweeps == 0) {
@@ -305,9 +307,12 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
 template <int TI, int AJ, int RY, bool STAGED>
 __global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
                                                      float* __restrict__ bc, int NXc, int NYc, const int* done) {
+    pdl_wait();
+    if (TI < kMgTI0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
     if (mg_done(done)) return;
     mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, b, nullptr,
                                                                 0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc);
+    pdl_trigger();
 }
 
 template <int TI, int AJ, int RY, bool STAGED>
@@ -315,9 +320,12 @@ __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restr
                                                    const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                    const float* __restrict__ b, float* __restrict__ xout,
                                                    const int* done) {
+    pdl_wait();
+    if (TI < kMgTI0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
     if (mg_done(done)) return;
     mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b,
                                               MgOwnNone{}, xout);
+    pdl_trigger();
 }
 
 // large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
@@ -399,11 +407,11 @@ static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, f
                        cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_down<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
-            G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
+        KC_CUDA(launch_chain(k_mg_down<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
+                             dim3(kMgNT0), 0, s, G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done));
     else
-        k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
-            G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done);
+        KC_CUDA(launch_chain(k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true>, mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1),
+                             dim3(kMgNT1), 0, s, G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done));
     KC_LAUNCH_CHECK_NC("k_mg_down");
     return KC_OK;
 }
@@ -412,11 +420,11 @@ static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, 
                      const float* b, float* xout, const int* done, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     if (l == 0 || mg_big(L.NX, L.NY))
-        k_mg_up<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge><<<mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0), kMgNT0, 0, s>>>(
-            G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
+        KC_CUDA(launch_chain(k_mg_up<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
+                             dim3(kMgNT0), 0, s, G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done));
     else
-        k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true><<<mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1), kMgNT1, 0, s>>>(
-            G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done);
+        KC_CUDA(launch_chain(k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true>, mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1),
+                             dim3(kMgNT1), 0, s, G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done));
     KC_LAUNCH_CHECK_NC("k_mg_up");
     return KC_OK;
 }
@@ -511,9 +519,9 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
     {
         const int l = M.levels - 1;
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
-        k_mg_coarsest<<<1, kCoarsestMax, 0, s>>>(L, (const float*)(base + M.off_b[l]), mg_final(M, base, l),
-                                                 o->coarsest_sweeps, (const float*)(base + M.off_inv),
-                                                 (const int*)(base + M.off_flag), done);
+        KC_CUDA(launch_chain(k_mg_coarsest, dim3(1), dim3(kCoarsestMax), 0, s, L, (const float*)(base + M.off_b[l]),
+                             mg_final(M, base, l), o->coarsest_sweeps, (const float*)(base + M.off_inv),
+                             (const int*)(base + M.off_flag), done));
         KC_LAUNCH_CHECK_NC("k_mg_coarsest");
         ++nk;
     }

@@ -1423,6 +1423,7 @@ struct PolPc1 {
 };
 
 __global__ void __launch_bounds__(kThreads) k_pc_1(Coef<float> A, Geo g, PcVecs V, BicgPtrs P) {
+    pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
@@ -1430,6 +1431,7 @@ __global__ void __launch_bounds__(kThreads) k_pc_1(Coef<float> A, Geo g, PcVecs 
     PolPc1 pol{V.z, V.p[cur], V.p[cur ^ 1], V.q, __ldcg(&st->beta_f), it == 0};
     Acc<float> acc[1];
     stencil_tile<float, 1>(pol, A, g.n, g.S, acc);
+    pdl_trigger();
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {
@@ -1529,6 +1531,7 @@ template <int TI, int AJ, int RY>
 __global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
                                                        int NX1, int NY1, PcVecs V, BicgPtrs P, int update) {
     constexpr int TJ = AJ - 4, NT = AJ * RY;
+    pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
@@ -1541,6 +1544,7 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restric
         blockIdx.y * TI, blockIdx.x * TJ, L, V.r[cur], up ? V.q : V.r[cur],
                                             up ? __ldcg(&st->alpha_f) : 0.f, mid,
                                             PcOwnR{V.r[cur ^ 1], up}, x0pre, b1, NX1, NY1);
+    pdl_trigger();
     if (!up) return;
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
@@ -1560,12 +1564,14 @@ template <int TI, int AJ, int RY>
 __global__ void __launch_bounds__(AJ * RY) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
                                                      const float* __restrict__ final1, int NX1, int NY1, float alpha0,
                                                      PcVecs V, BicgPtrs P) {
+    pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     Acc<float> acc[1];
     acc[0] = mg_up_tile<TI, AJ, RY, PcUpOwn, kMgStagedLarge>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, x0pre, final1,
                                                              NX1, NY1, alpha0, V.r[(int)(it & 1)], PcUpOwn{}, V.z);
+    pdl_trigger();
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
         threadIdx.x == 0) {
@@ -2219,18 +2225,20 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
     const MgFused F = mg_fused(A32, mg_ws, mo);
     int k1 = 0;
     for (int q = 0; q < m; ++q) {
-        k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
         if (F.ok) {
-            // K2 and K3 ride in the V-cycle's level-0 launches
+            // K2 and K3 ride in the V-cycle's level-0 launches; the chain is launched with
+            // programmatic dependencies (each kernel waits on its predecessor in-kernel)
+            KC_CUDA(launch_chain(k_pc_1, sg, dim3(kThreads), 0, s, C, g, V, P));
             const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
-            k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1);
-            KC_LAUNCH_CHECK_NC("k_pcf_down0");
+            KC_CUDA(launch_chain(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, tg, dim3(kMgNT0), 0, s, F.L0, F.x0pre, F.b1,
+                                 F.NX1, F.NY1, V, P, 1));
             int rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
             if (rc) return rc;
-            k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P);
-            KC_LAUNCH_CHECK_NC("k_pcf_up0");
+            KC_CUDA(launch_chain(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, tg, dim3(kMgNT0), 0, s, F.L0,
+                                 (const float*)F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P));
             k1 += 2;
         } else {
+            k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
             k_pc_2<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
             int rc = mg_enqueue(A32, mg_ws, mo, V.r[0], V.z, done, s, &k1);
             if (rc) return rc;
