@@ -161,6 +161,21 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
                         double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
                         double eps_inner, int max_refine, kc_solve_info* info, void* stream);
 
+/* One Jacobi sweep (FP64, standard form): x_mid = (b - sum_nb a_nb x_nb) / aP,
+ * y = (1 - omega) x + omega x_mid on the cells (i, j) of the [n/stride][stride]
+ * view with i0 <= i < i1, j0 <= j < j1 (y = x elsewhere and where aP = 0);
+ * max_diff_dev[0] = max |x_mid - x| there.  Replaces jacobian_solve_u /
+ * jacobian_solve_p (pressure_valid.py:192-233: region i in [2, nx] or [1, nx],
+ * j in [1, ny], omega = alpha_u or 1) and quick_jacobian
+ * (debug/20210828_karman_taihi.py:375-393: whole range, omega = 1).  Those
+ * overwrite the iterate inside a parallel loop, an order the reference leaves
+ * undefined; here every cell reads the previous iterate x (x != y).
+ * ws: kc_jacobi_ws_bytes() bytes, zeroed before the first call. */
+size_t kc_jacobi_ws_bytes(void);
+int kc_jacobi(const kc_system* A, const double* b, const double* x, double* y, double omega,
+              int i0, int i1, int j0, int j1, double* max_diff_dev, void* ws, size_t ws_bytes,
+              void* stream);
+
 /* ---- multigrid preconditioner (FP32) --------------------------------------
  * The reference names multigrid as its missing next step (README.md:31;
  * debug/note.md:6); it has Jacobi only (karman_taichi.py:398-399).

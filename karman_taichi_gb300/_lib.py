@@ -118,6 +118,8 @@ SIGNATURES = {
     "kc_cg_ws_bytes": (S_, [L_, I_, I_]),
     "kc_cg": (I_, [C.POINTER(KcSystem), P_, P_, P_, S_, C.POINTER(KcSolveOpts),
                    C.POINTER(KcSolveInfo), P_]),
+    "kc_jacobi_ws_bytes": (S_, []),
+    "kc_jacobi": (I_, [C.POINTER(KcSystem), P_, P_, P_, D_, I_, I_, I_, I_, P_, P_, S_, P_]),
     "kc_refined_ws_bytes": (S_, [L_, I_]),
     "kc_bicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
                                  C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),

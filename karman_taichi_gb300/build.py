@@ -31,6 +31,7 @@ SOURCES = {
     "kc_unet.cu": [],
     "kc_fields.cu": [],
     "kc_channel.cu": [],
+    "kc_smoothers.cu": [],
 }
 
 

@@ -124,6 +124,28 @@ def spmv(A: Stencil, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.
     return out
 
 
+_jac_ws = {}
+
+
+def jacobi(A: Stencil, b: torch.Tensor, x: torch.Tensor, y: torch.Tensor, *, omega=1.0, region=None,
+           max_diff: torch.Tensor | None = None) -> torch.Tensor:
+    """One Jacobi sweep y = (1 - omega) x + omega (b - sum_nb a_nb x_nb) / aP on
+    region = (i0, i1, j0, j1) of the [n/stride][stride] view (pressure_valid.py:
+    192-233, debug/20210828_karman_taihi.py:375-393); returns max |x_mid - x|
+    as a 1-element device tensor."""
+    require_cuda(b, x, y)
+    dev = b.device
+    lib = L.load()
+    ws = _jac_ws.get(dev)
+    if ws is None:
+        ws = _jac_ws[dev] = torch.zeros(lib.kc_jacobi_ws_bytes(), dtype=torch.uint8, device=dev)
+    out = max_diff if max_diff is not None else torch.empty(1, dtype=torch.float64, device=dev)
+    i0, i1, j0, j1 = region if region is not None else (0, A.n // A.stride, 0, A.stride)
+    L.check(lib.kc_jacobi(C.byref(A.system), ptr(b), ptr(x), ptr(y), float(omega), int(i0), int(i1), int(j0),
+                          int(j1), ptr(out), ptr(ws), ws.numel(), stream_handle(dev)), "kc_jacobi")
+    return out
+
+
 _dot_ws = {}
 
 

@@ -163,6 +163,46 @@ class SIMPLESolver:
     def bicg_solve_pcorrection_eqn(self, eps):
         return self.solve_pcorrection_eqn(eps)
 
+    # ---- Jacobi paths (pressure_valid.py:192-233) ----------------------------------
+    def jacobian_solve_u(self) -> float:
+        """One under-relaxed Jacobi sweep of the u equations on i in [2, nx], j in [1, ny]
+        (pressure_valid.py:192-206); returns max |u_mid - u|."""
+        from .linalg import Stencil, jacobi
+        nx, ny = self.nx, self.ny
+        if getattr(self, "_jac_u", None) is None:
+            self._jac_u = torch.empty_like(self.u)
+        d = jacobi(Stencil(self.coef_u), self.b_u, self.u, self._jac_u, omega=self.alpha_u,
+                   region=(2, nx + 1, 1, ny + 1))
+        self.u.copy_(self._jac_u)
+        return float(d.item())
+
+    def jacob_solve_momentum_eqn(self, n_iter):
+        """pressure_valid.py:208-214."""
+        self.compute_coef_u()
+        self.compute_coef_v()
+        self.set_bc()
+        return [self.jacobian_solve_u() for _ in range(n_iter)]
+
+    def jacobian_solve_p(self) -> float:
+        """One Jacobi sweep of the p' equations (right-hand side mdiv) on i in [1, nx], j in
+        [1, ny] (pressure_valid.py:221-233); returns max |pcor_mid - pcor|."""
+        from .linalg import Stencil, jacobi
+        nx, ny = self.nx, self.ny
+        if getattr(self, "_jac_p", None) is None:
+            self._jac_p = torch.empty_like(self.pcor)
+        d = jacobi(Stencil(self.coef_p), self.mdiv, self.pcor, self._jac_p, omega=1.0,
+                   region=(1, nx + 1, 1, ny + 1))
+        self.pcor.copy_(self._jac_p)
+        return float(d.item())
+
+    def jacob_solve_pcorrection_eqn(self, eps, max_iter=100000):
+        """pressure_valid.py:235-239, with an iteration cap."""
+        res, k = 1.0, 0
+        while res > eps and k < max_iter:
+            res = self.jacobian_solve_p()
+            k += 1
+        return res, k
+
     def dump_matrix(self, step, msg, directory="log"):
         """simple.py:51-54: u, v, p, mdiv, pcor to {directory}/{step:06}-{name}-{msg}.csv."""
         from .fields import savetxt

@@ -1123,3 +1123,84 @@ def post_process_field(u, v, p, pcor, udiv, dx, dy):
     disp = np.stack([np.repeat(np.repeat((f - lo) / (hi - lo + 1.0e-9), 3, axis=0), 3, axis=1)
                      for f, (lo, hi) in zip(fields, minmax)])
     return u_post, v_post, udiv, minmax, disp
+
+
+def pcorr_random_system(N=1024, seed=0, blocked=0.05):
+    """A seeded standalone pressure-correction system on an N x N grid (padded
+    [N+2][N+2], standard form, FP64): face coefficients 1/aP_face with aP_face
+    log-uniform in [1, 10]; square blocked blobs (side 4-16) covering about
+    `blocked` of the cells, whose rows are identities and whose links are
+    removed; p' pinned to zero at the first fluid cell as bicgsimp.py:146-151
+    pins (1, 1); right-hand side the divergence of a seeded Gaussian face
+    velocity smoothed by a 5 x 5 box filter, mean removed over the fluid.
+    Returns (coef [5][N+2][N+2], b [N+2][N+2])."""
+    rng = np.random.default_rng(seed)
+    NX = NY = N + 2
+    solid = np.zeros((NX, NY), dtype=bool)
+    target = blocked * N * N
+    while solid[1:-1, 1:-1].sum() < target:
+        s = int(rng.integers(4, 17))
+        i0, j0 = int(rng.integers(1, N - s + 2)), int(rng.integers(1, N - s + 2))
+        solid[i0:i0 + s, j0:j0 + s] = True
+    fluid = np.zeros((NX, NY), dtype=bool)
+    fluid[1:-1, 1:-1] = ~solid[1:-1, 1:-1]
+    ae = np.zeros((NX, NY))    # link between (i, j) and (i+1, j)
+    an = np.zeros((NX, NY))    # link between (i, j) and (i, j+1)
+    ae[1:N, 1:N + 1] = 1.0 / np.exp(rng.uniform(0.0, np.log(10.0), (N - 1, N)))
+    an[1:N + 1, 1:N] = 1.0 / np.exp(rng.uniform(0.0, np.log(10.0), (N, N - 1)))
+    ae[:-1] *= fluid[:-1] & fluid[1:]
+    an[:, :-1] *= fluid[:, :-1] & fluid[:, 1:]
+    pin = tuple(np.argwhere(fluid)[0])
+    c = np.zeros((5, NX, NY))
+    c[2, :-1] = -ae[:-1]            # aE of (i, j)
+    c[1, 1:] = -ae[:-1]             # aW of (i+1, j)
+    c[3, :, :-1] = -an[:, :-1]      # aN of (i, j)
+    c[4, :, 1:] = -an[:, :-1]       # aS of (i, j+1)
+    c[0] = -(c[1] + c[2] + c[3] + c[4])
+    for q in range(1, 5):
+        c[q][~fluid] = 0.0
+    c[0][~fluid] = 0.0
+    c[0][solid] = 1.0
+    c[:, pin[0], pin[1]] = 0.0
+    c[0, pin[0], pin[1]] = 1.0
+
+    def box5(a):
+        p = np.pad(a, 2, mode="edge")
+        out = np.zeros_like(a)
+        for di in range(5):
+            for dj in range(5):
+                out += p[di:di + a.shape[0], dj:dj + a.shape[1]]
+        return out / 25.0
+    u = box5(rng.standard_normal((NX + 1, NY)))
+    v = box5(rng.standard_normal((NX, NY + 1)))
+    b = (u[:-1] - u[1:]) + (v[:, :-1] - v[:, 1:])
+    b[~fluid] = 0.0
+    b[pin] = 0.0
+    m = fluid.copy()
+    m[pin] = False
+    b[m] -= b[m].mean()
+    return c, b
+
+
+def jacobi_sweep(coef, b, x, S, omega=1.0, region=None):
+    """One Jacobi sweep as kc_jacobi defines it (pressure_valid.py:192-233,
+    debug/20210828_karman_taihi.py:375-393 with every cell reading the previous
+    iterate): flat 5-point neighbours k -+ S, k -+ 1 (zero outside [0, n)).
+    Returns (y, max |x_mid - x| over the region)."""
+    c = np.asarray(coef, dtype=np.float64).reshape(5, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    x = np.asarray(x, dtype=np.float64).reshape(-1)
+    n = x.size
+    NX = n // S
+    i0, i1, j0, j1 = region if region is not None else (0, NX, 0, S)
+    xw = np.zeros(n); xw[S:] = x[:-S]
+    xe = np.zeros(n); xe[:-S] = x[S:]
+    xn = np.zeros(n); xn[:-1] = x[1:]
+    xs = np.zeros(n); xs[1:] = x[:-1]
+    r = (((b - c[1] * xw) - c[2] * xe) - c[3] * xn) - c[4] * xs
+    ii, jj = np.divmod(np.arange(n), S)
+    inside = (ii >= i0) & (ii < i1) & (jj >= j0) & (jj < j1) & (c[0] != 0)
+    xm = np.where(inside, r / np.where(c[0] != 0, c[0], 1.0), x)
+    y = np.where(inside, (1.0 - omega) * x + omega * xm, x)
+    d = np.abs(xm - x)[inside]
+    return y, (float(d.max()) if d.size else 0.0)
