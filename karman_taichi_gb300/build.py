@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "kc_api.cu": [],
     "kc_solver.cu": [],
-    "kc_simple.cu": ["-fmad=false"],
+    "kc_simple.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "kc_karman.cu": ["-fmad=false"],
     "kc_mg.cu": [],
     "kc_unet.cu": [],

@@ -30,6 +30,38 @@ struct Dims {
 };
 __host__ __device__ inline Dims dims_of(const kc_phys& P) { return {P.nx, P.ny, P.ny + 2, P.ny + 3, P.ny + 2}; }
 
+// Subexpressions of the coefficient formulas that do not depend on the face,
+// evaluated once on the host with the same operation tree as the per-face
+// expressions they replace (so every coefficient keeps its bits).  On GB300
+// FP64 arithmetic issues at a small fraction of the FP32 rate: a division
+// per face that need not be there costs more than the face's memory traffic.
+struct SimpleK {
+    double mdy_dx;   // mu * dy / dx
+    double mdx_dy;   // mu * dx / dy
+    double qrho;     // 0.5 * rho * 0.5
+    double hrho;     // rho * 0.5
+    double rdt;      // rho * dx * dy / dt
+    double wall_x;   // 2 * mu * dx / dy
+    double wall_y;   // 2 * mu * dy / dx
+    double nrdy2;    // -rho * dy * dy
+    double nrdx2;    // -rho * dx * dx
+    double one_m_am; // 1 - alpha_m
+};
+inline SimpleK consts_of(const kc_phys& P) {
+    SimpleK K;
+    K.mdy_dx = P.mu * P.dy / P.dx;
+    K.mdx_dy = P.mu * P.dx / P.dy;
+    K.qrho = 0.5 * P.rho * 0.5;
+    K.hrho = P.rho * 0.5;
+    K.rdt = P.rho * P.dx * P.dy / P.dt;
+    K.wall_x = 2 * P.mu * P.dx / P.dy;
+    K.wall_y = 2 * P.mu * P.dy / P.dx;
+    K.nrdy2 = -P.rho * P.dy * P.dy;
+    K.nrdx2 = -P.rho * P.dx * P.dx;
+    K.one_m_am = 1 - P.alpha_m;
+    return K;
+}
+
 struct Solid {
     const unsigned char* s;
     int NYp;
@@ -50,8 +82,9 @@ __device__ __forceinline__ bool unk_v(const kc_phys& P, const Solid& S, int i, i
 }
 
 // ---- momentum ---------------------------------------------------------------
-__device__ void u_row(const kc_phys& P, const Dims& D, const Solid& S, const double* u, const double* v,
-                      const double* p, const double* u0, int i, int j, double (&c)[5], double& b) {
+__device__ __forceinline__ void u_row(const kc_phys& P, const SimpleK& K, const Dims& D, const Solid& S,
+                                      const double* u, const double* v, const double* p, const double* u0, int i,
+                                      int j, double (&c)[5], double& b) {
     c[0] = c[1] = c[2] = c[3] = c[4] = 0.0;
     b = 0.0;
     const int nx = D.nx, ny = D.ny;
@@ -60,21 +93,21 @@ __device__ void u_row(const kc_phys& P, const Dims& D, const Solid& S, const dou
         c[0] = 1.0;
         return;
     }
-    const double mu = P.mu, rho = P.rho, dx = P.dx, dy = P.dy, dt = P.dt;
+    const double mu = P.mu, dx = P.dx, dy = P.dy;
 #define U_(a, bb) u[(long long)(a) * D.NYu + (bb)]
 #define V_(a, bb) v[(long long)(a) * D.NYv + (bb)]
 #define P_(a, bb) p[(long long)(a) * D.NYp + (bb)]
     const double ui = U_(i, j), uw = U_(i - 1, j), ue = U_(i + 1, j);
     const double vnw = V_(i - 1, j + 1), vne = V_(i, j + 1), vsw = V_(i - 1, j), vse = V_(i, j);
-    double aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (ui + uw) * dy);
-    double aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ui + ue) * dy);
-    double aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vnw + vne) * dx);
-    double aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vsw + vse) * dx);
-    double aP = -(aW + aE + aN + aS) + rho * 0.5 * (ui + ue) * dy - rho * 0.5 * (ui + uw) * dy +
-                rho * 0.5 * (vnw + vne) * dx - rho * 0.5 * (vsw + vse) * dx + rho * dx * dy / dt;
-    double bb = (P_(i - 1, j) - P_(i, j)) * dy + rho * dx * dy / dt * u0[(long long)i * D.NYu + j];
+    const double sw = ui + uw, se = ui + ue, sn = vnw + vne, ss = vsw + vse;
+    double aW = -(K.mdy_dx + K.qrho * sw * dy);
+    double aE = -(K.mdy_dx - K.qrho * se * dy);
+    double aN = -(K.mdx_dy - K.qrho * sn * dx);
+    double aS = -(K.mdx_dy + K.qrho * ss * dx);
+    double aP = -(aW + aE + aN + aS) + K.hrho * se * dy - K.hrho * sw * dy + K.hrho * sn * dx - K.hrho * ss * dx + K.rdt;
+    double bb = (P_(i - 1, j) - P_(i, j)) * dy + K.rdt * u0[(long long)i * D.NYu + j];
     if (P.mode == KC_MODE_CHANNEL) {
-        const double wall = 2 * mu * dx / dy;
+        const double wall = K.wall_x;
         if (i == 2) {
             bb += -aW * P.U;
             aW = 0.0;
@@ -107,12 +140,12 @@ __device__ void u_row(const kc_phys& P, const Dims& D, const Solid& S, const dou
         }
         if (j == 1) {
             bb += 2 * mu * P.bc[3][1] * dx / dy;
-            aP += (aS + 2 * mu * dx / dy);
+            aP += (aS + K.wall_x);
             aS = 0.0;
         }
         if (j == ny) {
             bb += 2 * mu * P.bc[2][1] * dx / dy;
-            aP += (aN + 2 * mu * dx / dy);
+            aP += (aN + K.wall_x);
             aN = 0.0;
         }
     }
@@ -124,8 +157,9 @@ __device__ void u_row(const kc_phys& P, const Dims& D, const Solid& S, const dou
     b = bb;
 }
 
-__device__ void v_row(const kc_phys& P, const Dims& D, const Solid& S, const double* u, const double* v,
-                      const double* p, const double* v0, int i, int j, double (&c)[5], double& b) {
+__device__ __forceinline__ void v_row(const kc_phys& P, const SimpleK& K, const Dims& D, const Solid& S,
+                                      const double* u, const double* v, const double* p, const double* v0, int i,
+                                      int j, double (&c)[5], double& b) {
     c[0] = c[1] = c[2] = c[3] = c[4] = 0.0;
     b = 0.0;
     const int nx = D.nx, ny = D.ny;
@@ -134,18 +168,18 @@ __device__ void v_row(const kc_phys& P, const Dims& D, const Solid& S, const dou
         c[0] = 1.0;
         return;
     }
-    const double mu = P.mu, rho = P.rho, dx = P.dx, dy = P.dy, dt = P.dt;
+    const double mu = P.mu, dx = P.dx, dy = P.dy;
     const double uc = U_(i, j), us = U_(i, j - 1), uec = U_(i + 1, j), ues = U_(i + 1, j - 1);
     const double vc = V_(i, j), vn = V_(i, j + 1), vs = V_(i, j - 1);
-    double aW = -(mu * dy / dx + 0.5 * rho * 0.5 * (uc + us) * dy);
-    double aE = -(mu * dy / dx - 0.5 * rho * 0.5 * (ues + uec) * dy);
-    double aN = -(mu * dx / dy - 0.5 * rho * 0.5 * (vn + vc) * dx);
-    double aS = -(mu * dx / dy + 0.5 * rho * 0.5 * (vs + vc) * dx);
-    double aP = -(aW + aE + aN + aS) + rho * 0.5 * (ues + uec) * dy - rho * 0.5 * (uc + us) * dy +
-                rho * 0.5 * (vn + vc) * dx - rho * 0.5 * (vs + vc) * dx + rho * dx * dy / dt;
-    double bb = (P_(i, j - 1) - P_(i, j)) * dx + rho * dx * dy / dt * v0[(long long)i * D.NYv + j];
+    const double sw = uc + us, se = ues + uec, sn = vn + vc, ss = vs + vc;
+    double aW = -(K.mdy_dx + K.qrho * sw * dy);
+    double aE = -(K.mdy_dx - K.qrho * se * dy);
+    double aN = -(K.mdx_dy - K.qrho * sn * dx);
+    double aS = -(K.mdx_dy + K.qrho * ss * dx);
+    double aP = -(aW + aE + aN + aS) + K.hrho * se * dy - K.hrho * sw * dy + K.hrho * sn * dx - K.hrho * ss * dx + K.rdt;
+    double bb = (P_(i, j - 1) - P_(i, j)) * dx + K.rdt * v0[(long long)i * D.NYv + j];
     if (P.mode == KC_MODE_CHANNEL) {
-        const double wall = 2 * mu * dy / dx;
+        const double wall = K.wall_y;
         if (j == 2 || S.bv(i, j - 1)) aS = 0.0;
         if (j == ny || S.bv(i, j + 1)) aN = 0.0;
         if (i == 1 || S.bv(i - 1, j)) {
@@ -171,12 +205,12 @@ __device__ void v_row(const kc_phys& P, const Dims& D, const Solid& S, const dou
         }
         if (i == 1) {
             bb += 2 * mu * P.bc[0][1] * dy / dx;
-            aP += (aW + 2 * mu * dy / dx);
+            aP += (aW + K.wall_y);
             aW = 0.0;
         }
         if (i == nx) {
             bb += 2 * mu * P.bc[1][1] * dy / dx;
-            aP += ((P.mode == KC_MODE_BICGSIMP ? aE : aW) + 2 * mu * dy / dx);
+            aP += ((P.mode == KC_MODE_BICGSIMP ? aE : aW) + K.wall_y);
             aE = 0.0;
         }
     }
@@ -193,21 +227,26 @@ struct MomOut {
     float *cu32, *bu32, *cv32, *bv32;
 };
 
+// Block layout of the field kernels: 256 threads as 8 rows of 32 lanes, lanes
+// along j (coalesced), rows strided by the grid.
+__device__ __forceinline__ int fk_lane() { return threadIdx.x & 31; }
+__device__ __forceinline__ int fk_row() { return threadIdx.x >> 5; }
+
 __global__ void __launch_bounds__(256)
-    k_assemble_momentum(kc_phys P, const double* u, const double* v, const double* p, const double* u0,
+    k_assemble_momentum(kc_phys P, SimpleK K, const double* u, const double* v, const double* p, const double* u0,
                         const double* v0, const unsigned char* solid, MomOut O) {
     const Dims D = dims_of(P);
     const Solid S{solid, D.NYp};
     const bool isv = blockIdx.z == 1;
     const int NX = isv ? D.nx + 2 : D.nx + 3, NY = isv ? D.NYv : D.NYu;
     const long long n = (long long)NX * NY;
-    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.x * 32 + fk_lane();
     if (j >= NY) return;
-    for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+    for (int i = blockIdx.y * 8 + fk_row(); i < NX; i += gridDim.y * 8) {
         double c[5], b;
         const long long k = (long long)i * NY + j;
         if (isv) {
-            v_row(P, D, S, u, v, p, v0, i, j, c, b);
+            v_row(P, K, D, S, u, v, p, v0, i, j, c, b);
 #pragma unroll
             for (int q = 0; q < 5; ++q) O.cv[q * n + k] = c[q];
             O.bv[k] = b;
@@ -217,7 +256,7 @@ __global__ void __launch_bounds__(256)
                 O.bv32[k] = (float)b;
             }
         } else {
-            u_row(P, D, S, u, v, p, u0, i, j, c, b);
+            u_row(P, K, D, S, u, v, p, u0, i, j, c, b);
 #pragma unroll
             for (int q = 0; q < 5; ++q) O.cu[q * n + k] = c[q];
             O.bu[k] = b;
@@ -229,6 +268,13 @@ __global__ void __launch_bounds__(256)
         }
     }
 }
+
+// Each block leaves its partials in ws->partials[z][block]; the last block of
+// the grid to arrive folds them with every thread (a strided pass, then a
+// block reduction) and resets the ticket.  Max is exact in any order; a sum is
+// folded in a fixed order, so it is reproducible run to run.
+__device__ __forceinline__ int fk_block() { return blockIdx.y * gridDim.x + blockIdx.x; }
+__device__ __forceinline__ int fk_blocks_z() { return gridDim.x * gridDim.y; }
 
 __global__ void k_apply_bc_values(kc_phys P, double* u, double* v) {
     const Dims D = dims_of(P);
@@ -245,54 +291,34 @@ __global__ void k_apply_bc_values(kc_phys P, double* u, double* v) {
 
 // ---- under-relaxation --------------------------------------------------------
 __global__ void __launch_bounds__(256)
-    k_relax(kc_phys P, const unsigned char* solid, const double* um, const double* vm, double* u, double* v,
-            ReduceWs* ws, double* diff_out) {
+    k_relax(kc_phys P, SimpleK K, const unsigned char* solid, const double* um, const double* vm, double* u,
+            double* v, ReduceWs* ws, double* diff_out) {
     const Dims D = dims_of(P);
     const Solid S{solid, D.NYp};
     const bool isv = blockIdx.z == 1;
     const int NX = isv ? D.nx + 2 : D.nx + 3, NY = isv ? D.NYv : D.NYu;
     const double a = P.alpha_m;
-    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.x * 32 + fk_lane();
     double dm[1] = {0.0};
     if (j < NY) {
-        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+        const double* mid = isv ? vm : um;
+        double* f = isv ? v : u;
+        for (int i = blockIdx.y * 8 + fk_row(); i < NX; i += gridDim.y * 8) {
             const long long k = (long long)i * NY + j;
             if (isv ? unk_v(P, S, i, j) : unk_u(P, S, i, j)) {
-                const double* mid = isv ? vm : um;
-                double* f = isv ? v : u;
                 const double m = mid[k], old = f[k];
                 dm[0] = fmax(dm[0], fabs(m - old));
-                f[k] = a * m + (1 - a) * old;
+                f[k] = a * m + K.one_m_am * old;
             }
         }
     }
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    // block max (reuse block_max with linear thread index)
-    __shared__ double sh[8];
-    double wv = warp_max(dm[0]);
-    if ((tid & 31) == 0) sh[tid >> 5] = wv;
-    __syncthreads();
-    const int nbz = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (tid == 0) {
-        double m = 0.0;
-        for (int q = 0; q < 8; ++q) m = fmax(m, sh[q]);
-        ws->partials[blockIdx.z][bid] = m;
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(2 * nbz - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (tid == 0) {
-        double du = 0.0, dv = 0.0;
-        for (int q = 0; q < nbz; ++q) {
-            du = fmax(du, __ldcg(&ws->partials[0][q]));
-            dv = fmax(dv, __ldcg(&ws->partials[1][q]));
-        }
-        if (diff_out) *diff_out = sqrt(du * du + dv * dv);
+    block_max<1>(dm);
+    if (threadIdx.x == 0) ws->partials[blockIdx.z][fk_block()] = dm[0];
+    if (!arrive_last(&ws->ticket[0], fk_blocks_z() * gridDim.z)) return;
+    double o[2];
+    reduce_partials_max<2>(&ws->partials[0][0], kReduceMaxBlocks, fk_blocks_z(), o);
+    if (threadIdx.x == 0) {
+        if (diff_out) *diff_out = sqrt(o[0] * o[0] + o[1] * o[1]);
         ws->ticket[0] = 0;
     }
 }
@@ -318,8 +344,36 @@ __global__ void __launch_bounds__(256) k_outlet_conserve(kc_phys P, double* u) {
 }
 
 // ---- pressure correction -----------------------------------------------------
+// A warp covers 31 cells of a row (lane 31 evaluates the halo column) and a
+// run of kPcRows consecutive rows.  Each face's link value -rho dy^2 / aP_u
+// (resp. -rho dx^2 / aP_v) is divided once and shared by the two cells on
+// either side of it -- through the row carry for u faces, a lane shuffle for
+// v faces -- instead of once per cell: half the FP64 divisions.
+constexpr int kPcRows = 4;
+constexpr int kPcCols = 31;
+
+__device__ __forceinline__ void finish_max_sum(double mx, double sq, ReduceWs* ws, double* mass_out) {
+    double a[1] = {mx}, b[1] = {sq};
+    block_max<1>(a);
+    block_sum<1>(b);
+    if (threadIdx.x == 0) {
+        ws->partials[0][fk_block()] = a[0];
+        ws->partials[1][fk_block()] = b[0];
+    }
+    if (!arrive_last(&ws->ticket[0], fk_blocks_z())) return;
+    reduce_partials_max<1>(&ws->partials[0][0], kReduceMaxBlocks, fk_blocks_z(), a);
+    reduce_partials<1>(&ws->partials[1][0], kReduceMaxBlocks, fk_blocks_z(), b);
+    if (threadIdx.x == 0) {
+        if (mass_out) {
+            mass_out[0] = a[0];
+            mass_out[1] = b[0];
+        }
+        ws->ticket[0] = 0;
+    }
+}
+
 __global__ void __launch_bounds__(256)
-    k_assemble_pcorr(kc_phys P, const double* u, const double* v, const double* apu, const double* apv,
+    k_assemble_pcorr(kc_phys P, SimpleK K, const double* u, const double* v, const double* apu, const double* apv,
                      const unsigned char* solid, double* cp, double* bp, float* cp32, float* bp32,
                      double* mdiv_out, ReduceWs* ws, double* mass_out) {
     const Dims D = dims_of(P);
@@ -329,105 +383,85 @@ __global__ void __launch_bounds__(256)
     const int nx = D.nx, ny = D.ny;
     const double rho = P.rho, dx = P.dx, dy = P.dy;
     const bool channel = P.mode == KC_MODE_CHANNEL;
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    double mx[1] = {0.0}, sq[1] = {0.0};
-    if (j < NY) {
-        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
-            const long long k = (long long)i * NY + j;
-            double c[5] = {0, 0, 0, 0, 0}, b = 0.0;
-            if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
-                const double md = rho * (U_(i, j) - U_(i + 1, j)) * dy + rho * (V_(i, j) - V_(i, j + 1)) * dx;
-                if (mdiv_out) mdiv_out[k] = md;
-                if (channel && S.cell(i, j)) {
-                    c[0] = 1.0;
-                } else if (channel) {
-                    double aW = 0.0, aE = 0.0, aN = 0.0, aS = 0.0;
-                    if (unk_u(P, S, i, j)) aW = -rho * dy * dy / apu[(long long)i * D.NYu + j];
-                    if (unk_u(P, S, i + 1, j)) aE = -rho * dy * dy / apu[(long long)(i + 1) * D.NYu + j];
-                    if (i == nx && unk_u(P, S, nx, j)) aE = -rho * dy * dy / apu[(long long)nx * D.NYu + j];
-                    if (unk_v(P, S, i, j + 1)) aN = -rho * dx * dx / apv[(long long)i * D.NYv + j + 1];
-                    if (unk_v(P, S, i, j)) aS = -rho * dx * dx / apv[(long long)i * D.NYv + j];
-                    c[0] = -(aW + aE + aN + aS);
-                    c[1] = aW;
-                    c[2] = aE;
-                    c[3] = aN;
-                    c[4] = aS;
-                    b = md;
-                    mx[0] = fmax(mx[0], fabs(md));
-                    sq[0] += md * md;
-                } else {
-                    // compute_coef_p, simple.py:146-163 (bicgsimp.py:146-151 pins (1,1))
-                    double aW = i == 1 ? 0.0 : -rho * dy * dy / apu[(long long)i * D.NYu + j];
-                    double aE = i == nx ? 0.0 : -rho * dy * dy / apu[(long long)(i + 1) * D.NYu + j];
-                    double aN = j == ny ? 0.0 : -rho * dx * dx / apv[(long long)i * D.NYv + j + 1];
-                    double aS = j == 1 ? 0.0 : -rho * dx * dx / apv[(long long)i * D.NYv + j];
-                    c[0] = -(aW + aE + aN + aS);
-                    c[1] = aW;
-                    c[2] = aE;
-                    c[3] = aN;
-                    c[4] = aS;
-                    b = md;
-                    if (P.mode == KC_MODE_BICGSIMP && i == 1 && j == 1) {
-                        c[1] = c[2] = c[3] = c[4] = 0.0;
+    const int lane = fk_lane();
+    const int j = blockIdx.x * kPcCols + lane;
+    const bool own = lane < kPcCols && j < NY;
+    double mx = 0.0, sq = 0.0;
+    // rows of u faces: 0..nx+2 (NX + 1 of them); columns of v faces: 0..ny+2
+    for (int rg = blockIdx.y * 8 + fk_row(); rg * kPcRows < NX; rg += gridDim.y * 8) {
+        const int i0 = rg * kPcRows;
+        double tw = j < NY ? K.nrdy2 / apu[(long long)i0 * D.NYu + j] : 0.0;   // u face (i0, j)
+        for (int r = 0; r < kPcRows; ++r) {
+            const int i = i0 + r;
+            if (i >= NX) break;   // uniform over the warp
+            const double te = j < NY ? K.nrdy2 / apu[(long long)(i + 1) * D.NYu + j] : 0.0;   // u face (i+1, j)
+            const double tv = j < D.NYv ? K.nrdx2 / apv[(long long)i * D.NYv + j] : 0.0;     // v face (i, j)
+            const double tn = __shfl_down_sync(kFull, tv, 1);                                 // v face (i, j+1)
+            if (own) {
+                const long long k = (long long)i * NY + j;
+                double c[5] = {0, 0, 0, 0, 0}, b = 0.0, xs = 0.0;
+                if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
+                    const double md = rho * (U_(i, j) - U_(i + 1, j)) * dy + rho * (V_(i, j) - V_(i, j + 1)) * dx;
+                    if (mdiv_out) mdiv_out[k] = md;
+                    if (channel && S.cell(i, j)) {
                         c[0] = 1.0;
-                        b = 0.0;
+                    } else if (channel) {
+                        double aW = 0.0, aE = 0.0, aN = 0.0, aS = 0.0;
+                        if (unk_u(P, S, i, j)) aW = tw;
+                        if (unk_u(P, S, i + 1, j)) aE = te;
+                        if (i == nx && unk_u(P, S, nx, j)) aE = tw;   // the outlet row links to face nx again
+                        if (unk_v(P, S, i, j + 1)) aN = tn;
+                        if (unk_v(P, S, i, j)) aS = tv;
+                        xs = aW + aE + aN + aS;
+                        c[0] = -xs;
+                        c[1] = aW;
+                        c[2] = aE;
+                        c[3] = aN;
+                        c[4] = aS;
+                        b = md;
+                        mx = fmax(mx, fabs(md));
+                        sq += md * md;
+                    } else {
+                        // compute_coef_p, simple.py:146-163 (bicgsimp.py:146-151 pins (1,1))
+                        const double aW = i == 1 ? 0.0 : tw;
+                        const double aE = i == nx ? 0.0 : te;
+                        const double aN = j == ny ? 0.0 : tn;
+                        const double aS = j == 1 ? 0.0 : tv;
+                        xs = aW + aE + aN + aS;
+                        c[0] = -xs;
+                        c[1] = aW;
+                        c[2] = aE;
+                        c[3] = aN;
+                        c[4] = aS;
+                        b = md;
+                        if (P.mode == KC_MODE_BICGSIMP && i == 1 && j == 1) {
+                            c[1] = c[2] = c[3] = c[4] = 0.0;
+                            c[0] = 1.0;
+                            b = 0.0;
+                            xs = 0.0;
+                        }
+                        mx = fmax(mx, fabs(md));
+                        sq += md * md;
                     }
-                    mx[0] = fmax(mx[0], fabs(md));
-                    sq[0] += md * md;
+                }
+#pragma unroll
+                for (int q = 0; q < 5; ++q) cp[q * n + k] = c[q];
+                bp[k] = b;
+                if (cp32) {
+                    // FP32 copy in Laplacian form: component 0 is the row sum
+                    // c0 + (((c1 + c2) + c3) + c4) -- the link sum xs in the
+                    // order aP was built in, so it is exactly 0 on every fluid
+                    // row (see KC_FORM_LAPLACIAN)
+                    cp32[k] = (float)(c[0] + xs);
+#pragma unroll
+                    for (int q = 1; q < 5; ++q) cp32[q * n + k] = (float)c[q];
+                    bp32[k] = (float)b;
                 }
             }
-#pragma unroll
-            for (int q = 0; q < 5; ++q) cp[q * n + k] = c[q];
-            bp[k] = b;
-            if (cp32) {
-                // FP32 copy in Laplacian form: component 0 is the row sum,
-                // evaluated in the order aP was built in, so it is exactly 0
-                // on every fluid row (see KC_FORM_LAPLACIAN)
-                cp32[k] = (float)(c[0] + (((c[1] + c[2]) + c[3]) + c[4]));
-#pragma unroll
-                for (int q = 1; q < 5; ++q) cp32[q * n + k] = (float)c[q];
-                bp32[k] = (float)b;
-            }
+            tw = te;
         }
     }
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    __shared__ double shm[8], shs[8];
-    double a = warp_max(mx[0]), s2 = warp_sum(sq[0]);
-    if ((tid & 31) == 0) {
-        shm[tid >> 5] = a;
-        shs[tid >> 5] = s2;
-    }
-    __syncthreads();
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (tid == 0) {
-        double m = 0.0, s = 0.0;
-        for (int q = 0; q < 8; ++q) {
-            m = fmax(m, shm[q]);
-            s += shs[q];
-        }
-        ws->partials[0][bid] = m;
-        ws->partials[1][bid] = s;
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(nb - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (tid == 0) {
-        double m = 0.0, s = 0.0;
-        for (int q = 0; q < nb; ++q) {
-            m = fmax(m, __ldcg(&ws->partials[0][q]));
-            s += __ldcg(&ws->partials[1][q]);
-        }
-        if (mass_out) {
-            mass_out[0] = m;
-            mass_out[1] = s;
-        }
-        ws->ticket[0] = 0;
-    }
+    finish_max_sum(mx, sq, ws, mass_out);
 }
 
 // ---- correction: z = 0 u faces, 1 v faces, 2 p cells --------------------------
@@ -443,10 +477,10 @@ __global__ void __launch_bounds__(256)
     const bool channel = P.mode == KC_MODE_CHANNEL;
     const double au = P.alpha_u, ap = P.alpha_p, dx = P.dx, dy = P.dy;
 #define PC_(a, bb) pc[(long long)(a) * D.NYp + (bb)]
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    double mx = 0.0;
+    const int j = blockIdx.x * 32 + fk_lane();
+    double mx[1] = {0.0};
     if (j < NY) {
-        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+        for (int i = blockIdx.y * 8 + fk_row(); i < NX; i += gridDim.y * 8) {
             const long long k = (long long)i * NY + j;
             if (z == 0) {
                 if (unk_u(P, S, i, j)) {
@@ -458,34 +492,17 @@ __global__ void __launch_bounds__(256)
                 if (unk_v(P, S, i, j)) v[k] = v[k] + au * (PC_(i, j - 1) - PC_(i, j)) * dx / apv[k];
             } else {
                 const double q = pc[k];
-                mx = fmax(mx, fabs(q));
+                mx[0] = fmax(mx[0], fabs(q));
                 if (i >= 1 && i <= nx && j >= 1 && j <= ny && !(channel && S.cell(i, j))) p[k] = p[k] + ap * q;
             }
         }
     }
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    __shared__ double shm[8];
-    double a = warp_max(mx);
-    if ((tid & 31) == 0) shm[tid >> 5] = a;
-    __syncthreads();
-    const int nbz = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (tid == 0) {
-        double m = 0.0;
-        for (int q = 0; q < 8; ++q) m = fmax(m, shm[q]);
-        ws->partials[z][bid] = m;
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(3 * nbz - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (tid == 0) {
-        double m = 0.0;
-        for (int q = 0; q < nbz; ++q) m = fmax(m, __ldcg(&ws->partials[2][q]));
-        if (pmax_out) *pmax_out = m;
+    block_max<1>(mx);
+    if (threadIdx.x == 0) ws->partials[z][fk_block()] = mx[0];
+    if (!arrive_last(&ws->ticket[0], fk_blocks_z() * gridDim.z)) return;
+    reduce_partials_max<1>(&ws->partials[2][0], kReduceMaxBlocks, fk_blocks_z(), mx);
+    if (threadIdx.x == 0) {
+        if (pmax_out) *pmax_out = mx[0];
         ws->ticket[0] = 0;
     }
 }
@@ -498,10 +515,10 @@ __global__ void __launch_bounds__(256)
     const int NX = D.nx + 2, NY = D.NYp;
     const double rho = P.rho, dx = P.dx, dy = P.dy;
     const bool channel = P.mode == KC_MODE_CHANNEL;
-    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.x * 32 + fk_lane();
     double mx = 0.0, sq = 0.0;
     if (j >= 1 && j <= D.ny) {
-        for (int i = blockIdx.y * 8 + threadIdx.y; i < NX; i += gridDim.y * 8) {
+        for (int i = blockIdx.y * 8 + fk_row(); i < NX; i += gridDim.y * 8) {
             if (i < 1 || i > D.nx) continue;
             const long long k = (long long)i * NY + j;
             double md = rho * (U_(i, j) - U_(i + 1, j)) * dy + rho * (V_(i, j) - V_(i, j + 1)) * dx;
@@ -511,42 +528,7 @@ __global__ void __launch_bounds__(256)
             sq += md * md;
         }
     }
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    __shared__ double shm[8], shs[8];
-    double a = warp_max(mx), s2 = warp_sum(sq);
-    if ((tid & 31) == 0) {
-        shm[tid >> 5] = a;
-        shs[tid >> 5] = s2;
-    }
-    __syncthreads();
-    const int nb = gridDim.x * gridDim.y;
-    const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-    if (tid == 0) {
-        double m = 0.0, s = 0.0;
-        for (int q = 0; q < 8; ++q) {
-            m = fmax(m, shm[q]);
-            s += shs[q];
-        }
-        ws->partials[0][bid] = m;
-        ws->partials[1][bid] = s;
-    }
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) last = atomicAdd(&ws->ticket[0], 1u) == (unsigned)(nb - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    if (tid == 0) {
-        double m = 0.0, s = 0.0;
-        for (int q = 0; q < nb; ++q) {
-            m = fmax(m, __ldcg(&ws->partials[0][q]));
-            s += __ldcg(&ws->partials[1][q]);
-        }
-        mass_out[0] = m;
-        mass_out[1] = s;
-        ws->ticket[0] = 0;
-    }
+    finish_max_sum(mx, sq, ws, mass_out);
 }
 #undef U_
 #undef V_
@@ -561,13 +543,21 @@ static dim3 field_grid(int NX, int NY, int zdim) {
     if (gy > 64) gy = 64;
     return dim3(gx, gy, zdim);
 }
+// k_assemble_pcorr: kPcCols cells per warp row, kPcRows rows per warp, 8 warps
+static dim3 pcorr_grid(int NX, int NY) {
+    int gx = (NY + kPcCols - 1) / kPcCols;
+    int gy = (NX + 8 * kPcRows - 1) / (8 * kPcRows);
+    int cap = std::max(1, kReduceMaxBlocks / (gx > 0 ? gx : 1));
+    if (gy > cap) gy = cap;
+    return dim3(gx, gy, 1);
+}
 
 static int check_phys(const kc_phys* P) {
     if (!P) return set_error("kc_phys is null"), KC_ERR_ARG;
     if (P->nx < 2 || P->ny < 2) return set_error("kc_phys: nx=%d ny=%d must be >= 2", P->nx, P->ny), KC_ERR_ARG;
     if (P->mode < KC_MODE_SIMPLE || P->mode > KC_MODE_CHANNEL)
         return set_error("kc_phys: unknown mode %d", P->mode), KC_ERR_ARG;
-    if ((long long)(P->ny + 3 + 31) / 32 > kReduceMaxBlocks)
+    if ((long long)(P->ny + 3 + kPcCols - 1) / kPcCols > kReduceMaxBlocks)
         return set_error("kc_phys: ny=%d too large", P->ny), KC_ERR_ARG;
     return KC_OK;
 }
@@ -593,7 +583,7 @@ int kc_assemble_momentum(const kc_phys* P, const double* u, const double* v, con
         return set_error("kc_assemble_momentum: FP32 outputs must be given in pairs"), KC_ERR_ARG;
     MomOut O{coef_u, b_u, coef_v, b_v, coef_u32, b_u32, coef_v32, b_v32};
     dim3 g = field_grid(P->nx + 3, P->ny + 3, 2);
-    k_assemble_momentum<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, p, u0, v0, solid, O);
+    k_assemble_momentum<<<g, 256, 0, as_stream(stream)>>>(*P, consts_of(*P), u, v, p, u0, v0, solid, O);
     KC_LAUNCH_CHECK("k_assemble_momentum");
     return KC_OK;
 }
@@ -615,7 +605,8 @@ int kc_relax_velocity(const kc_phys* P, const unsigned char* solid, const double
     if (!u_mid || !v_mid || !u || !v) return set_error("kc_relax_velocity: null field"), KC_ERR_ARG;
     if (!ws) return set_error("kc_relax_velocity: null workspace"), KC_ERR_WORKSPACE;
     dim3 g = field_grid(P->nx + 3, P->ny + 3, 2);
-    k_relax<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, solid, u_mid, v_mid, u, v, (ReduceWs*)ws, diff_dev);
+    k_relax<<<g, 256, 0, as_stream(stream)>>>(*P, consts_of(*P), solid, u_mid, v_mid, u, v, (ReduceWs*)ws,
+                                           diff_dev);
     KC_LAUNCH_CHECK("k_relax");
     return KC_OK;
 }
@@ -639,8 +630,8 @@ int kc_assemble_pcorr(const kc_phys* P, const double* u, const double* v, const 
     if ((coef_p32 == nullptr) != (b_p32 == nullptr))
         return set_error("kc_assemble_pcorr: FP32 outputs must be given in pairs"), KC_ERR_ARG;
     if (!ws) return set_error("kc_assemble_pcorr: null workspace"), KC_ERR_WORKSPACE;
-    dim3 g = field_grid(P->nx + 2, P->ny + 2, 1);
-    k_assemble_pcorr<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, coef_u, coef_v, solid, coef_p, b_p,
+    dim3 g = pcorr_grid(P->nx + 2, P->ny + 2);
+    k_assemble_pcorr<<<g, 256, 0, as_stream(stream)>>>(*P, consts_of(*P), u, v, coef_u, coef_v, solid, coef_p, b_p,
                                                                coef_p32, b_p32, mdiv, (ReduceWs*)ws, mass_dev);
     KC_LAUNCH_CHECK("k_assemble_pcorr");
     return KC_OK;
@@ -654,7 +645,7 @@ int kc_correct(const kc_phys* P, const double* pcor, const double* coef_u, const
     if (!pcor || !coef_u || !coef_v || !u || !v || !p) return set_error("kc_correct: null field"), KC_ERR_ARG;
     if (!ws) return set_error("kc_correct: null workspace"), KC_ERR_WORKSPACE;
     dim3 g = field_grid(P->nx + 3, P->ny + 3, 3);
-    k_correct<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, pcor, coef_u, coef_v, solid, u, v, p, (ReduceWs*)ws,
+    k_correct<<<g, 256, 0, as_stream(stream)>>>(*P, pcor, coef_u, coef_v, solid, u, v, p, (ReduceWs*)ws,
                                                         pcor_max_dev);
     KC_LAUNCH_CHECK("k_correct");
     return KC_OK;
@@ -667,7 +658,7 @@ int kc_mass_residual(const kc_phys* P, const double* u, const double* v, const u
     if (!u || !v || !mass_dev) return set_error("kc_mass_residual: null argument"), KC_ERR_ARG;
     if (!ws) return set_error("kc_mass_residual: null workspace"), KC_ERR_WORKSPACE;
     dim3 g = field_grid(P->nx + 2, P->ny + 2, 1);
-    k_mass_residual<<<g, dim3(32, 8), 0, as_stream(stream)>>>(*P, u, v, solid, mdiv, (ReduceWs*)ws, mass_dev);
+    k_mass_residual<<<g, 256, 0, as_stream(stream)>>>(*P, u, v, solid, mdiv, (ReduceWs*)ws, mass_dev);
     KC_LAUNCH_CHECK("k_mass_residual");
     return KC_OK;
 }
