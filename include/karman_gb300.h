@@ -187,14 +187,18 @@ int kc_jacobi(const kc_system* A, const double* b, const double* x, double* y, d
  * coarsest_sweeps = 0: coarsening stops at <= 128 cells, whose dense
  * operator is inverted at setup (exact coarsest solve; a non-positive pivot
  * falls back to 64 Jacobi sweeps); > 0: coarsening stops at <= 1024 cells,
- * solved by that many Jacobi sweeps.  kc_mg_default_opts: nu 1/1, exact
+ * solved by that many Jacobi sweeps.  tail = 1 (with the fused cycle and the
+ * exact coarsest solve) runs the levels of at most 1536 cells and the
+ * coarsest solve in one single-block launch, their arithmetic unchanged;
+ * 0 launches every level separately.  kc_mg_default_opts: nu 1/1, exact
  * coarsest solve, omega 1.1, alpha 1.8 (the tuned setting for the channel's
- * pressure correction). */
+ * pressure correction), tail 1. */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */
     int coarsest_sweeps;          /* 0: exact coarsest solve; > 0: Jacobi sweeps            */
     int max_levels;
+    int tail;                     /* 1: the smallest levels in one single-block launch     */
     float omega[KC_MG_MAX_LEVELS];/* smoother weight per level                            */
     float alpha[KC_MG_MAX_LEVELS];/* coarse-correction scale per level                    */
 } kc_mg_opts;

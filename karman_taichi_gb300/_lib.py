@@ -66,7 +66,7 @@ class KcPhys(C.Structure):
 
 class KcMgOpts(C.Structure):
     _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("coarsest_sweeps", C.c_int), ("max_levels", C.c_int),
-                ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
+                ("tail", C.c_int), ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
 
 
 class KcChannel(C.Structure):

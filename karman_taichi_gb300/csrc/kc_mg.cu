@@ -31,6 +31,7 @@
 #include "kc_common.cuh"
 #include "kc_mg.h"
 #include <algorithm>
+#include <mutex>
 
 namespace kc {
 
@@ -203,51 +204,94 @@ __global__ void k_mg_prolong(Lvl F, float* __restrict__ x, const float* __restri
 // diagonal, its right-hand side is zero), and the cycle applies x = A^-1 b.
 // A non-positive or non-finite pivot sets the flag and the cycle falls back
 // to kCoarseFallbackSweeps Jacobi sweeps.
+// The block is 32 x 32 threads; thread (ty, tx) keeps the entries of rows
+// ty + 32a and columns tx + 32c in registers (kGjR x kGjR of them), so a
+// pivot step is one barrier and a few FMAs per entry: the pivot row and
+// column go through shared memory, double-buffered so that step p + 1 may
+// write while slow readers still read step p's copy.
+constexpr int kGjR = kCoarseDirectMax / 32;
+
 __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __restrict__ inv, int* __restrict__ flag) {
-    extern __shared__ float A[];   // n x n, row major
+    __shared__ float rowp[2][kCoarseDirectMax], colp[2][kCoarseDirectMax];
     const int n = L.NX * L.NY, NY = L.NY;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = 0.f;
-    __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const long long ce = (long long)k * L.es;
-        const float c0 = L.c[ce], w = L.c[L.cs + ce], ea = L.c[2 * L.cs + ce], no = L.c[3 * L.cs + ce],
-                    so = L.c[4 * L.cs + ce];
-        const int j = k % NY;
-        float d = L.lap ? c0 - (((w + ea) + no) + so) : c0;   // out-of-grid neighbours hold zero
-        if (w == 0.f && ea == 0.f && no == 0.f && so == 0.f && d == 0.f) d = 1.f;   // no coupled child
-        A[k * n + k] = d;
-        if (k >= NY) A[k * n + k - NY] = w;
-        if (k + NY < n) A[k * n + k + NY] = ea;
-        if (j + 1 < NY) A[k * n + k + 1] = no;
-        if (j >= 1) A[k * n + k - 1] = so;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    float a[kGjR][kGjR];
+#pragma unroll
+    for (int r = 0; r < kGjR; ++r) {
+        const int i = ty + 32 * r;
+        float d = 0.f, w = 0.f, ea = 0.f, no = 0.f, so = 0.f;
+        if (i < n) {
+            const long long ce = (long long)i * L.es;
+            const float c0 = L.c[ce];
+            w = L.c[L.cs + ce];
+            ea = L.c[2 * L.cs + ce];
+            no = L.c[3 * L.cs + ce];
+            so = L.c[4 * L.cs + ce];
+            d = L.lap ? c0 - (((w + ea) + no) + so) : c0;   // out-of-grid neighbours hold zero
+            if (w == 0.f && ea == 0.f && no == 0.f && so == 0.f && d == 0.f) d = 1.f;   // no coupled child
+        }
+        const int jr = i % NY;
+#pragma unroll
+        for (int c = 0; c < kGjR; ++c) {
+            const int j = tx + 32 * c;
+            float v = 0.f;
+            if (i < n && j < n) {
+                if (j == i) v = d;
+                else if (j == i - NY) v = w;
+                else if (j == i + NY) v = ea;
+                else if (j == i + 1 && jr + 1 < NY) v = no;
+                else if (j == i - 1 && jr >= 1) v = so;
+            }
+            a[r][c] = v;
+        }
     }
-    __syncthreads();
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    __shared__ float col[kCoarseDirectMax];
+    int bad = 0;
     for (int p = 0; p < n; ++p) {
-        const float piv = A[p * n + p];
-        if (!(piv > 0.f) || !isfinite(piv)) {
-            if (threadIdx.x == 0) bad = 1;
-            break;   // uniform: every thread reads the same pivot
+        const int buf = p & 1, pr = p >> 5, pl = p & 31;
+        // the owners publish row p and column p as they stand before the step
+        if (ty == pl) {
+#pragma unroll
+            for (int r = 0; r < kGjR; ++r)
+                if (r == pr) {
+#pragma unroll
+                    for (int c = 0; c < kGjR; ++c) rowp[buf][tx + 32 * c] = a[r][c];
+                }
+        }
+        if (tx == pl) {
+#pragma unroll
+            for (int c = 0; c < kGjR; ++c)
+                if (c == pr) {
+#pragma unroll
+                    for (int r = 0; r < kGjR; ++r) colp[buf][ty + 32 * r] = a[r][c];
+                }
+        }
+        __syncthreads();
+        const float piv = rowp[buf][p];
+        if (!(piv > 0.f) || !isfinite(piv)) {   // uniform: every thread reads the same pivot
+            bad = 1;
+            break;
         }
         const float ip = 1.f / piv;
-        __syncthreads();
-        // the pivot column of the other rows, and the scaled pivot row
-        for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = A[i * n + p];
-        for (int j = threadIdx.x; j < n; j += blockDim.x) A[p * n + j] = j == p ? ip : A[p * n + j] * ip;
-        __syncthreads();
-        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {   // eliminate (reads row p, writes the others)
-            const int i = e / n, j = e - i * n;
-            if (i == p) continue;
-            A[e] = j == p ? -col[i] * ip : fmaf(-col[i], A[p * n + j], A[e]);
+#pragma unroll
+        for (int r = 0; r < kGjR; ++r) {
+            const int i = ty + 32 * r;
+            const float ci = colp[buf][i];
+#pragma unroll
+            for (int c = 0; c < kGjR; ++c) {
+                const int j = tx + 32 * c;
+                const float sp = j == p ? ip : rowp[buf][j] * ip;   // the scaled pivot row
+                a[r][c] = i == p ? sp : (j == p ? -ci * ip : fmaf(-ci, sp, a[r][c]));
+            }
         }
-        __syncthreads();
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) inv[e] = A[e];
-    if (threadIdx.x == 0) *flag = bad;
+#pragma unroll
+    for (int r = 0; r < kGjR; ++r)
+#pragma unroll
+        for (int c = 0; c < kGjR; ++c) {
+            const int i = ty + 32 * r, j = tx + 32 * c;
+            if (i < n && j < n) inv[i * n + j] = a[r][c];
+        }
+    if (tx == 0 && ty == 0) *flag = bad;
 }
 
 // x = A^-1 b (one warp per row), or Jacobi sweeps when sweeps > 0 or the inverse failed
@@ -326,6 +370,201 @@ __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restr
     mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b,
                                               MgOwnNone{}, xout);
     pdl_trigger();
+}
+
+// ---- coarse-level tail: the smallest levels of the fused cycle in one block ------------
+// A level of a few hundred cells costs two launches of ~3-5 us each for a few
+// microseconds of work: each waits for the previous grid to drain and reloads
+// its data.  Here one block runs the levels Ls..Lend (from the first level of
+// at most kTailMax cells down to the coarsest) with every array in shared
+// memory, phases separated by __syncthreads.  Smoother weights, coefficients
+// and the coarsest inverse do not depend on the previous launch: they are
+// staged before the grid dependency wait, behind the previous kernel's tail.
+// The arithmetic per cell is that of mg_down_tile / mg_up_tile /
+// k_mg_coarsest, operation for operation, so the cycle's result is bitwise
+// the same as with one launch per level.  (Spreading larger levels over a
+// thread-block cluster, rows exchanged through distributed shared memory,
+// was measured slower than their launches on GB300: 1.2-2.4 us per
+// cluster-barrier phase.)
+constexpr int kTailThreads = 1024;
+constexpr int kTailMax = 1536;    // levels of at most this many cells run in the tail block
+constexpr int kTailArrays = 8;    // per cell: x, b, smoother weight, 5 coefficients
+
+struct TailLevel {
+    const float* c;      // Laplacian-form coefficients, 5 planes of NX*NY
+    const float* winv;   // smoother weights
+    int NX, NY;
+    float alpha;         // weight of the coarse correction prolonged into this level
+    int so;              // shared-memory offset (floats) of the level's arrays
+    unsigned mNY, mHalf; // t / NY and t / ((NY + 1) / 2) by tdiv (exact for t, d < 2^16)
+};
+struct MgTail {
+    TailLevel lv[KC_MG_MAX_LEVELS];
+    int Ls, Lend, inv_so;
+    const float* b_in;   // right-hand side of level Ls (written by the previous launch)
+    float* x_out;        // result of level Ls
+    const float* inv;    // dense inverse of the coarsest level
+    const int* inv_bad;
+};
+
+// m = 0 stands for d = 1 (2^32 does not fit)
+__device__ __forceinline__ int tdiv(int t, unsigned m) { return m ? (int)__umulhi((unsigned)t, m) : t; }
+
+// one level in shared memory: cell k = i * NY + j
+struct TailArr {
+    float* x;
+    float* b;
+    const float* w;
+    const float* c;   // component q of cell k at c[q * n + k]
+    int n, NX, NY;
+    __device__ __forceinline__ float cq(int q, int k) const { return c[q * n + k]; }
+    __device__ __forceinline__ bool linked(int k) const {
+        return cq(1, k) != 0.f || cq(2, k) != 0.f || cq(3, k) != 0.f || cq(4, k) != 0.f;
+    }
+    __device__ __forceinline__ float xa(int i, int j) const {
+        return (j < 0 || j >= NY || i < 0 || i >= NX) ? 0.f : x[i * NY + j];
+    }
+    __device__ __forceinline__ float ax(int k, int i, int j, float xv) const {
+        return mg_row(cq(0, k), cq(1, k), cq(2, k), cq(3, k), cq(4, k), 1, xv, xa(i - 1, j), xa(i + 1, j),
+                      xa(i, j + 1), xa(i, j - 1));
+    }
+};
+__device__ __forceinline__ TailArr tail_arr(float* sm, const TailLevel& L) {
+    float* s = sm + L.so;
+    const int n = L.NX * L.NY;
+    return TailArr{s, s + n, s + 2 * n, s + 3 * n, n, L.NX, L.NY};
+}
+
+// half-sweep x += W (b - A x) over the cells of colour col ((i + j) & 1)
+__device__ __forceinline__ void tail_sweep(const TailArr& A, const TailLevel& L, int col) {
+    const int half = (A.NY + 1) >> 1;
+    const int cnt = A.NX * half;
+    for (int e = threadIdx.x; e < cnt; e += kTailThreads) {
+        const int i = tdiv(e, L.mHalf), m = e - i * half;
+        const int j = 2 * m + ((i + col) & 1);
+        if (j >= A.NY) continue;
+        const int k = i * A.NY + j;
+        const float xv = A.x[k];
+        A.x[k] = fmaf(A.w[k], A.b[k] - A.ax(k, i, j, xv), xv);
+    }
+}
+
+__global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int* done) {
+    extern __shared__ __align__(16) float sm[];
+    const int tid = threadIdx.x;
+    // weights, coefficients and the inverse first: they do not depend on the previous launch
+    for (int l = T.Ls; l <= T.Lend; ++l) {
+        const TailLevel& L = T.lv[l];
+        const TailArr A = tail_arr(sm, L);
+        float* w = const_cast<float*>(A.w);
+        float* c = const_cast<float*>(A.c);
+        for (int k = tid; k < A.n; k += kTailThreads) {
+            w[k] = __ldg(L.winv + k);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) c[q * A.n + k] = __ldg(L.c + q * A.n + k);
+        }
+    }
+    const int nc = T.lv[T.Lend].NX * T.lv[T.Lend].NY;
+    float* inv = sm + T.inv_so;
+    for (int e = tid; e < nc * nc; e += kTailThreads) inv[e] = __ldg(T.inv + e);
+    pdl_wait();
+    pdl_trigger();
+    if (mg_done(done)) return;
+    {
+        const TailArr A = tail_arr(sm, T.lv[T.Ls]);
+        for (int k = tid; k < A.n; k += kTailThreads) A.b[k] = __ldcg(T.b_in + k);
+    }
+    __syncthreads();
+    // downward: red start, black half-sweep, restriction
+    for (int l = T.Ls; l < T.Lend; ++l) {
+        const TailLevel& L = T.lv[l];
+        const TailLevel& Q = T.lv[l + 1];
+        const TailArr A = tail_arr(sm, L);
+        for (int k = tid; k < A.n; k += kTailThreads) {
+            const int i = tdiv(k, L.mNY), j = k - i * A.NY;
+            A.x[k] = ((i + j) & 1) == 0 ? A.w[k] * A.b[k] : 0.f;
+        }
+        __syncthreads();
+        tail_sweep(A, L, 1);
+        __syncthreads();
+        const TailArr B = tail_arr(sm, Q);
+        for (int t = tid; t < B.n; t += kTailThreads) {
+            const int I = tdiv(t, Q.mNY), J = t - I * B.NY;
+            float s = 0.f;
+#pragma unroll
+            for (int di = 0; di < 2; ++di)
+#pragma unroll
+                for (int dj = 0; dj < 2; ++dj) {
+                    const int i = 2 * I + di, j = 2 * J + dj;
+                    if (i >= A.NX || j >= A.NY) continue;
+                    const int k = i * A.NY + j;
+                    if (!A.linked(k)) continue;
+                    s += A.b[k] - A.ax(k, i, j, A.x[k]);
+                }
+            B.b[t] = s;
+        }
+        __syncthreads();
+    }
+    {   // coarsest: x = A^-1 b (one warp per row), or Jacobi sweeps when the inverse failed
+        const TailArr A = tail_arr(sm, T.lv[T.Lend]);
+        const int n = A.n;
+        if (!__ldcg(T.inv_bad)) {
+            const int lane = tid & 31, wp = tid >> 5, nw = kTailThreads >> 5;
+            for (int i = wp; i < n; i += nw) {
+                float sacc = 0.f;
+                for (int j = lane; j < n; j += 32) sacc = fmaf(inv[i * n + j], A.b[j], sacc);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sacc += __shfl_down_sync(kFull, sacc, o);
+                if (lane == 0) A.x[i] = sacc;
+            }
+        } else {
+            __shared__ float xs[2][kCoarseDirectMax];
+            float bk = 0.f, w = 0.f, c[5] = {0, 0, 0, 0, 0};
+            if (tid < n) {
+                bk = A.b[tid];
+                w = A.w[tid];
+                for (int q = 0; q < 5; ++q) c[q] = A.cq(q, tid);
+                xs[0][tid] = w * bk;
+            }
+            __syncthreads();
+            int cur = 0;
+            for (int s = 0; s < kCoarseFallbackSweeps; ++s) {
+                if (tid < n) {
+                    const float* xv = xs[cur];
+                    const float xk = xv[tid];
+                    const int j = tid % A.NY;
+                    const float xw = tid >= A.NY ? xv[tid - A.NY] : 0.f, xe = tid + A.NY < n ? xv[tid + A.NY] : 0.f;
+                    const float xn = j + 1 < A.NY ? xv[tid + 1] : 0.f, xso = j >= 1 ? xv[tid - 1] : 0.f;
+                    float y = c[0] * xk;
+                    y += c[1] * (xw - xk) + c[2] * (xe - xk) + c[3] * (xn - xk) + c[4] * (xso - xk);
+                    xs[cur ^ 1][tid] = xk + w * (bk - y);
+                }
+                __syncthreads();
+                cur ^= 1;
+            }
+            if (tid < n) A.x[tid] = xs[cur][tid];
+        }
+        __syncthreads();
+    }
+    // upward: prolongation, black then red half-sweep
+    for (int l = T.Lend - 1; l >= T.Ls; --l) {
+        const TailLevel& L = T.lv[l];
+        const TailLevel& Q = T.lv[l + 1];
+        const TailArr A = tail_arr(sm, L);
+        const float* xc = sm + Q.so;
+        for (int k = tid; k < A.n; k += kTailThreads) {
+            if (!A.linked(k)) continue;
+            const int i = tdiv(k, L.mNY), j = k - i * A.NY;
+            A.x[k] = fmaf(L.alpha, xc[(i >> 1) * Q.NY + (j >> 1)], A.x[k]);
+        }
+        __syncthreads();
+        tail_sweep(A, L, 1);
+        __syncthreads();
+        tail_sweep(A, L, 0);
+        __syncthreads();
+    }
+    const TailArr A = tail_arr(sm, T.lv[T.Ls]);
+    for (int k = tid; k < A.n; k += kTailThreads) T.x_out[k] = A.x[k];
 }
 
 // large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
@@ -459,25 +698,11 @@ int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o,
         const int l = M.levels - 1;
         const int nc = M.nx[l] * M.ny[l];
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
-        const size_t smem = (size_t)nc * nc * sizeof(float);
-        static bool attr_set = false;   // 64 KB of dynamic shared memory needs the opt-in once
-        if (!attr_set) {
-            KC_CUDA(cudaFuncSetAttribute(k_mg_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(kCoarseDirectMax * kCoarseDirectMax * sizeof(float))));
-            attr_set = true;
-        }
-        k_mg_coarse_inverse<<<1, 1024, smem, s>>>(L, (float*)(base + M.off_inv), (int*)(base + M.off_flag));
+        if (nc > kCoarseDirectMax) return set_error("kc_mg_setup: coarsest level of %d cells", nc), KC_ERR_ARG;
+        k_mg_coarse_inverse<<<1, dim3(32, 32), 0, s>>>(L, (float*)(base + M.off_inv), (int*)(base + M.off_flag));
         KC_LAUNCH_CHECK("k_mg_coarse_inverse");
     }
     return KC_OK;
-}
-
-int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o) {
-    const int NY = A->stride;
-    const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
-    if (mg_fusable(M, o)) return 2 * (M.levels - 1) + 1;
-    const int down = 2 + 2 * std::max(0, o->nu_pre - 1) + 1, up = 1 + 2 * std::max(0, o->nu_post);
-    return (M.levels - 1) * (down + up) + 1;
 }
 
 // output of level l in the fused cycle (the caller's z for level 0)
@@ -500,6 +725,92 @@ MgFused mg_fused(const kc_system* A, void* ws, const kc_mg_opts* o) {
     return F;
 }
 
+// ---- coarse-level tail: plan and launch ---------------------------------------------
+struct TailPlan {
+    bool ok;
+    int Ls, Lend;
+    size_t smem;
+};
+
+static unsigned tail_magic(int d) {
+    return d <= 1 ? 0u : (unsigned)((0x100000000ull + (unsigned long long)d - 1) / (unsigned long long)d);
+}
+
+// The tail takes the levels from the first one of at most kTailMax cells to
+// the coarsest, when that is at least one level above the coarsest (fused
+// cycle, exact coarsest solve) and their arrays fit the block's shared memory.
+static TailPlan tail_plan(const MgLayout& M, const kc_mg_opts* o) {
+    TailPlan P{};
+    if (!o->tail || o->coarsest_sweeps != 0 || !mg_fusable(M, o)) return P;
+    const int Lend = M.levels - 1;
+    int Ls = 1;
+    while (Ls < Lend && (long long)M.nx[Ls] * M.ny[Ls] > kTailMax) ++Ls;
+    if (Ls >= Lend) return P;
+    size_t cells = 0;
+    for (int l = Ls; l <= Lend; ++l) cells += (size_t)M.nx[l] * M.ny[l];
+    const size_t nc = (size_t)M.nx[Lend] * M.ny[Lend];
+    const size_t bytes = (kTailArrays * cells + nc * nc) * sizeof(float);
+    if (bytes > 200 * 1024) return P;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return (void)cudaGetLastError(), P;
+    static std::mutex mu;
+    static bool attr_done[64] = {false};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 0 && dev < 64 && !attr_done[dev]) {
+            if (cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                return P;
+            }
+            attr_done[dev] = true;
+        }
+    }
+    P = TailPlan{true, Ls, Lend, bytes};
+    return P;
+}
+
+static int launch_tail(const TailPlan& P, const MgLayout& M, char* base, const kc_mg_opts* o, const int* done,
+                       cudaStream_t s) {
+    MgTail T{};
+    int off = 0;
+    for (int l = P.Ls; l <= P.Lend; ++l) {
+        TailLevel& L = T.lv[l];
+        L.c = (const float*)(base + M.off_coef[l]);
+        L.winv = (const float*)(base + M.off_winv[l]);
+        L.NX = M.nx[l];
+        L.NY = M.ny[l];
+        L.alpha = o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)];
+        L.so = off;
+        L.mNY = tail_magic(L.NY);
+        L.mHalf = tail_magic((L.NY + 1) / 2);
+        off += kTailArrays * L.NX * L.NY;
+    }
+    T.inv_so = off;
+    const int nc = M.nx[P.Lend] * M.ny[P.Lend];
+    off += nc * nc;
+    if ((size_t)off * sizeof(float) != P.smem) return set_error("multigrid tail: shared memory plan mismatch"), KC_ERR_ARG;
+    T.Ls = P.Ls;
+    T.Lend = P.Lend;
+    T.b_in = (const float*)(base + M.off_b[P.Ls]);
+    T.x_out = mg_final(M, base, P.Ls);
+    T.inv = (const float*)(base + M.off_inv);
+    T.inv_bad = (const int*)(base + M.off_flag);
+    KC_CUDA(launch_chain(k_mg_tail, dim3(1), dim3(kTailThreads), P.smem, s, T, done));
+    return KC_OK;
+}
+
+int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o) {
+    const int NY = A->stride;
+    const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
+    if (mg_fusable(M, o)) {
+        const TailPlan P = tail_plan(M, o);
+        return P.ok ? 2 * P.Ls + 1 : 2 * (M.levels - 1) + 1;
+    }
+    const int down = 2 + 2 * std::max(0, o->nu_pre - 1) + 1, up = 1 + 2 * std::max(0, o->nu_post);
+    return (M.levels - 1) * (down + up) + 1;
+}
+
 // levels >= 1 of the fused cycle: b_1 in, final_1 out
 int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const int* done, cudaStream_t s,
                       int* kernels) {
@@ -509,6 +820,29 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
     const float* c0 = (const float*)A->coef;
     const int lap0 = A->form == KC_FORM_LAPLACIAN;
     int nk = 0, rc;
+    const TailPlan P = tail_plan(M, o);
+    if (P.ok) {   // levels 1..Ls-1 one launch each, Ls..coarsest in the tail block
+        for (int l = 1; l < P.Ls; ++l) {
+            const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
+            rc = launch_down(M, L, l, (const float*)(base + M.off_b[l]), (float*)(base + M.off_x[l]),
+                             (float*)(base + M.off_b[l + 1]), done, s);
+            if (rc) return rc;
+            ++nk;
+        }
+        rc = launch_tail(P, M, base, o, done, s);
+        if (rc) return rc;
+        ++nk;
+        for (int l = P.Ls - 1; l >= 1; --l) {
+            const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
+            rc = launch_up(M, L, l, (const float*)(base + M.off_x[l]), mg_final(M, base, l + 1),
+                           o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], (const float*)(base + M.off_b[l]),
+                           mg_final(M, base, l), done, s);
+            if (rc) return rc;
+            ++nk;
+        }
+        if (kernels) *kernels = nk;
+        return KC_OK;
+    }
     for (int l = 1; l + 1 < M.levels; ++l) {
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
         rc = launch_down(M, L, l, (const float*)(base + M.off_b[l]), (float*)(base + M.off_x[l]),
@@ -624,6 +958,7 @@ void kc_mg_default_opts(kc_mg_opts* o) {
     o->nu_post = 1;
     o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
+    o->tail = 1;               // the levels of at most 1536 cells in one single-block launch
     for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
         o->omega[l] = 1.1f;
         o->alpha[l] = 1.8f;

@@ -255,15 +255,17 @@ class Multigrid:
     preconditioner of the mixed-precision pressure-correction solve.
     ``omega`` / ``alpha`` are per-level smoother weights and coarse-correction
     scales (scalars broadcast to all levels); ``coarsest_sweeps=0`` solves the
-    coarsest level (<= 128 cells) exactly."""
+    coarsest level (<= 128 cells) exactly.  ``tail=True`` runs the levels of at
+    most 1536 cells in one single-block launch (same arithmetic)."""
 
     def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.1, alpha=1.8,
-                 max_levels=16):
+                 max_levels=16, tail=True):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")
         self.A = A32
         o = L.KcMgOpts()
         o.nu_pre, o.nu_post, o.coarsest_sweeps, o.max_levels = nu_pre, nu_post, coarsest_sweeps, max_levels
+        o.tail = int(bool(tail))
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
         al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
         for l in range(16):

@@ -83,19 +83,74 @@ def test_vcycle_matches_restatement(dev, alpha, lap, nu, coarsest):
     assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
-def test_vcycle_launch_count(dev):
-    """The fused cycle launches two kernels per level above the coarsest."""
+@pytest.mark.parametrize("tail", [False, True])
+def test_vcycle_launch_count(dev, tail):
+    """The fused cycle launches two kernels per level above the coarsest; with
+    the tail, the levels of at most 1536 cells (here every level below level 0)
+    and the coarsest solve are one launch."""
     from karman_taichi_gb300 import _lib as L, linalg
     coef, b = _channel_pcorr(96, 40, 6, 30, 20)
     NX, NY = coef.shape[1:]
     c32, form = _fp32(coef, True)
-    mg = linalg.Multigrid(linalg.Stencil(_t(c32, dev), form=form)).setup()
+    mg = linalg.Multigrid(linalg.Stencil(_t(c32, dev), form=form), tail=tail).setup()
     levels = len(O.MultigridOracle(c32.reshape(5, -1), NX, NY, lap=True).levels)
+    assert levels >= 3
     r = _t(np.ones((NX, NY), dtype=np.float32), dev)
     lib = L.load()
     n0 = lib.kc_launch_count()
     mg.apply(r)
-    assert lib.kc_launch_count() - n0 == 2 * (levels - 1) + 1
+    assert lib.kc_launch_count() - n0 == (3 if tail else 2 * (levels - 1) + 1)
+
+
+# grids of the workloads (p' of the 320x64 and 2048x512 channels, the 1024^2 system,
+# a 4096x1024 channel, small batched instances, a strip): the tail starts at levels 1..6
+@pytest.mark.parametrize("shape", [(98, 42), (130, 34), (322, 66), (1026, 1026), (2050, 514), (4098, 1026),
+                                   (3000, 7)])
+def test_tail_is_the_per_level_cycle(dev, shape):
+    """The smallest levels in one launch compute the V-cycle bit for bit as the
+    one-launch-per-level cycle does."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    NX, NY = shape
+    bi, bj = NX // 5, NY // 2
+    c32 = O.to_laplacian32(_poisson(NX, NY, (bi, bi + 8, max(bj - 4, 1), min(bj + 4, NY - 1))))
+    A = linalg.Stencil(_t(c32, dev), form=L.FORM_LAPLACIAN)
+    r = np.random.default_rng(NX).standard_normal((NX, NY)).astype(np.float32)
+    r[(c32[1:] == 0).all(axis=0)] = 0.0
+    rt = _t(r, dev)
+    lib = L.load()
+    zs = []
+    for tail in (False, True):
+        mg = linalg.Multigrid(A, tail=tail).setup()
+        n0 = lib.kc_launch_count()
+        zs.append(mg.apply(rt))
+        zs.append(mg.apply(rt))
+        zs.append(lib.kc_launch_count() - n0)
+    assert zs[5] < zs[2]   # fewer launches with the tail
+    assert torch.equal(zs[0], zs[3]) and torch.equal(zs[1], zs[4]) and torch.equal(zs[0], zs[1])
+    assert torch.isfinite(zs[3]).all()
+
+
+def test_pcg_tail_same_iterates(dev):
+    """The refined multigrid CG takes the same iterations to the same x with and
+    without the tail (graph-captured chunks included)."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    NX, NY = 1026, 1026
+    c64 = _poisson(NX, NY, (500, 540, 480, 520))
+    A64 = linalg.Stencil(_t(c64, dev))
+    A32 = linalg.Stencil(_t(O.to_laplacian32(c64), dev), form=L.FORM_LAPLACIAN)
+    b = np.random.default_rng(5).standard_normal((NX, NY))
+    b[(c64[1:] == 0).all(axis=0)] = 0.0
+    out = []
+    for tail in (False, True):
+        mg = linalg.Multigrid(A32, tail=tail).setup()
+        x = _t(np.zeros((NX, NY)), dev)
+        info = linalg.pcg_refined(A64, A32, _t(b, dev), x, mg, eps=1e-8)
+        assert info.ok
+        out.append((info.iters, x))
+    assert out[0][0] == out[1][0]
+    assert torch.equal(out[0][1], out[1][1])
 
 
 def test_laplacian_spmv_matches_standard(dev):
