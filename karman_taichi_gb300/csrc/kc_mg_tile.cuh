@@ -49,6 +49,9 @@ __device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool v
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// wait until at most N of this thread's most recent commit groups are pending
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ float mg_row(float c0, float cw, float ce, float cn, float cs_, int lap, float x,
                                         float xw, float xe, float xn, float xs) {
@@ -132,35 +135,58 @@ struct MgCoef {
     }
 };
 
-// DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
-template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true>
-__device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
-                                                          const float* __restrict__ q, float alpha, const Mid& mid,
-                                                          const Own& own, float* __restrict__ xout,
-                                                          float* __restrict__ bc, int NXc, int NYc) {
+// Shared-memory arrays of one tile, all [AI][AJ] except sxc (coarse cells
+// under the tile, [TI/2 + 2][AJ/2]).  DOWN stages sb, sq (HasQ), sw, sc and
+// uses sx as scratch; UP stages sx (the pre-smoothed iterate), sb, sw, sxc, sc.
+struct MgStage {
+    float* sb;
+    float* sq;
+    float* sw;
+    float* sc;    // 5 coefficient components
+    float* sx;
+    float* sxc;
+};
+template <int TI, int AJ, int RY>
+struct MgStageDims {
     using T = MgTile<TI, AJ, RY>;
-    __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
-    __shared__ __align__(16) float sq[HasQ ? T::A : 1];
-    __shared__ __align__(16) float sc[STAGED ? 5 * T::A : 1];
-    const MgCoef<T, STAGED> C{sc, L, i0, j0};
+    static constexpr int XI = TI / 2 + 2, XJ = AJ / 2, XC = XI * XJ;
+    // floats of the staged (double-buffered) part and of the single scratch x
+    static constexpr int kDown = 8 * T::A, kUp = 8 * T::A + XC, kX = T::A;
+};
+
+// DOWN, asynchronous part: stage b_in (and q) , W and the coefficients of the tile at (i0, j0)
+template <int TI, int AJ, int RY, bool HasQ>
+__device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
+                                              const float* __restrict__ q, MgStage S) {
+    using T = MgTile<TI, AJ, RY>;
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
-    const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
-    typename Own::Sum sum{};
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
-        cp_async4(sb + u, b_in + k, in);
-        if (HasQ) cp_async4(sq + u, q + k, in);
-        cp_async4(sw + u, L.winv + k, in);
+        cp_async4(S.sb + u, b_in + k, in);
+        if (HasQ) cp_async4(S.sq + u, q + k, in);
+        cp_async4(S.sw + u, L.winv + k, in);
     }
-    if (STAGED) mg_stage_coef<TI, T>(L, i0, j0, sc);
-    cp_async_commit();
-    mid();
-    cp_async_wait_all();
-    __syncthreads();
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
+
+// DOWN, after the tile's copies have landed: b = b_in - alpha q, red start,
+// black half-sweep over the 1-cell ring, x and the restricted residual out
+template <int TI, int AJ, int RY, bool HasQ, class Own>
+__device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
+                                                MgStage S, float* __restrict__ xout, float* __restrict__ bc,
+                                                int NXc, int NYc, typename Own::Sum& sum) {
+    using T = MgTile<TI, AJ, RY>;
+    float* sb = S.sb;
+    const float* sq = S.sq;
+    const float* sw = S.sw;
+    float* sx = S.sx;
+    const MgCoef<T, true> C{S.sc, L, i0, j0};
+    const int b = T::tx(), j = j0 + b - 2;
+    const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
     // b, owned cells, red start (x = W b on red, 0 on black)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
@@ -206,7 +232,161 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
             }
         bc[I * NYc + J] = s;
     }
+}
+
+// DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
+template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true>
+__device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
+                                                          const float* __restrict__ q, float alpha, const Mid& mid,
+                                                          const Own& own, float* __restrict__ xout,
+                                                          float* __restrict__ bc, int NXc, int NYc) {
+    using T = MgTile<TI, AJ, RY>;
+    if (STAGED) {
+        __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
+        __shared__ __align__(16) float sq[HasQ ? T::A : 1];
+        __shared__ __align__(16) float sc[5 * T::A];
+        const MgStage S{sb, sq, sw, sc, sx, nullptr};
+        mg_down_issue<TI, AJ, RY, HasQ>(i0, j0, L, b_in, q, S);
+        cp_async_commit();
+        mid();
+        cp_async_wait_all();
+        __syncthreads();
+        typename Own::Sum sum{};
+        mg_down_compute<TI, AJ, RY, HasQ, Own>(i0, j0, L, alpha, own, S, xout, bc, NXc, NYc, sum);
+        return sum;
+    }
+    __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
+    __shared__ __align__(16) float sq[HasQ ? T::A : 1];
+    const MgCoef<T, false> C{nullptr, L, i0, j0};
+    const int b = T::tx(), j = j0 + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
+    typename Own::Sum sum{};
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(sb + u, b_in + k, in);
+        if (HasQ) cp_async4(sq + u, q + k, in);
+        cp_async4(sw + u, L.winv + k, in);
+    }
+    cp_async_commit();
+    mid();
+    cp_async_wait_all();
+    __syncthreads();
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int u = a * T::AJ + b;
+        const int i = i0 + a - 2;
+        float bv = sb[u];
+        if (HasQ) {
+            bv = fmaf(-alpha, sq[u], bv);
+            sb[u] = bv;
+        }
+        if (jown && a >= 2 && a < TI + 2 && i < L.NX) own(i * L.NY + j, bv, sum);
+        sx[u] = ((a + b) & 1) == 0 ? sw[u] * bv : 0.f;
+    }
+    __syncthreads();
+    if (b >= 1 && b < AJ - 1)
+        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
+            if (((a + b) & 1) == 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+        }
+    __syncthreads();
+    if (jown)
+        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
+            const int i = i0 + a - 2;
+            if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + b];
+        }
+    for (int t = threadIdx.x; t < (TI / 2) * (T::TJ / 2); t += T::NT) {
+        const int ag = t / (T::TJ / 2), bg = t - ag * (T::TJ / 2);
+        const int I = (i0 >> 1) + ag, J = (j0 >> 1) + bg;
+        if (I >= NXc || J >= NYc) continue;
+        float s = 0.f;
+#pragma unroll
+        for (int di = 0; di < 2; ++di)
+#pragma unroll
+            for (int dj = 0; dj < 2; ++dj) {
+                const int a = 2 * ag + di + 2, bb = 2 * bg + dj + 2;
+                if (i0 + a - 2 >= L.NX || j0 + bb - 2 >= L.NY) continue;
+                const int u = a * T::AJ + bb;
+                if (!C.linked(u)) continue;
+                s += sb[u] - C.ax(sx, u);
+            }
+        bc[I * NYc + J] = s;
+    }
     return sum;
+}
+
+// UP, asynchronous part: stage x_pre, b_in, W, the coarse cells under the tile and the coefficients
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
+                                            const float* __restrict__ xc, int NXc, int NYc,
+                                            const float* __restrict__ b_in, MgStage S) {
+    using T = MgTile<TI, AJ, RY>;
+    constexpr int XI = TI / 2 + 2, XJ = AJ / 2;
+    const int b = T::tx(), j = j0 + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(S.sx + u, xpre + k, in);
+        cp_async4(S.sb + u, b_in + k, in);
+        cp_async4(S.sw + u, L.winv + k, in);
+    }
+    for (int t = threadIdx.x; t < XI * XJ; t += T::NT) {
+        const int ca = t / XJ, cb = t - ca * XJ;
+        const int I = (i0 >> 1) - 1 + ca, J = (j0 >> 1) - 1 + cb;
+        const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
+        cp_async4(S.sxc + t, xc + (in ? I * NYc + J : 0), in);
+    }
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
+
+// UP, after the copies have landed: prolong (coupled cells, told apart by
+// their links), black half-sweep over the 1-cell ring, red half-sweep on the
+// owned cells, write
+template <int TI, int AJ, int RY, class Own>
+__device__ __forceinline__ void mg_up_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
+                                              MgStage S, float* __restrict__ xout, typename Own::Sum& sum) {
+    using T = MgTile<TI, AJ, RY>;
+    constexpr int XJ = AJ / 2;
+    float* sx = S.sx;
+    const float* sb = S.sb;
+    const float* sw = S.sw;
+    const float* sxc = S.sxc;
+    const MgCoef<T, true> C{S.sc, L, i0, j0};
+    const int b = T::tx(), j = j0 + b - 2;
+    // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-2, j0-2)
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int u = a * T::AJ + b;
+        if (!C.linked(u)) continue;
+        sx[u] = fmaf(alpha, sxc[(a >> 1) * XJ + (b >> 1)], sx[u]);
+    }
+    __syncthreads();
+    // black half-sweep over the 1-cell ring
+    if (b >= 1 && b < AJ - 1)
+        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
+            if (((a + b) & 1) == 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+        }
+    __syncthreads();
+    // red half-sweep on the owned cells, then write
+    if (b >= 2 && b < T::TJ + 2 && j < L.NY)
+        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
+            const int i = i0 + a - 2;
+            if (i >= L.NX) continue;
+            const int u = a * T::AJ + b;
+            float xv = sx[u];
+            if (((a + b) & 1) == 0) xv = fmaf(sw[u], sb[u] - C.ax(sx, u), xv);
+            const int k = i * L.NY + j;
+            xout[k] = xv;
+            own(k, xv, sb[u], sum);
+        }
 }
 
 // UP tile at (i0, j0): prolong (coupled cells, told apart by their links),
@@ -218,9 +398,20 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
                                                         float* __restrict__ xout) {
     using T = MgTile<TI, AJ, RY>;
     constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
+    if (STAGED) {
+        __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
+        __shared__ __align__(16) float sc[5 * T::A];
+        const MgStage S{sb, nullptr, sw, sc, sx, sxc};
+        mg_up_issue<TI, AJ, RY>(i0, j0, L, xpre, xc, NXc, NYc, b_in, S);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        typename Own::Sum sum{};
+        mg_up_compute<TI, AJ, RY, Own>(i0, j0, L, alpha, own, S, xout, sum);
+        return sum;
+    }
     __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
-    __shared__ __align__(16) float sc[STAGED ? 5 * T::A : 1];
-    const MgCoef<T, STAGED> C{sc, L, i0, j0};
+    const MgCoef<T, false> C{nullptr, L, i0, j0};
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     typename Own::Sum sum{};
@@ -239,18 +430,15 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    if (STAGED) mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-2, j0-2)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
         if (!C.linked(u)) continue;
         sx[u] = fmaf(alpha, sxc[(a >> 1) * XJ + (b >> 1)], sx[u]);
     }
     __syncthreads();
-    // black half-sweep over the 1-cell ring
     if (b >= 1 && b < AJ - 1)
         for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
             if (((a + b) & 1) == 0) continue;
@@ -258,7 +446,6 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
             sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
         }
     __syncthreads();
-    // red half-sweep on the owned cells, then write
     if (b >= 2 && b < T::TJ + 2 && j < L.NY)
         for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
             const int i = i0 + a - 2;

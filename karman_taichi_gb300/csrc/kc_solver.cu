@@ -1488,15 +1488,14 @@ __global__ void __launch_bounds__(kPwThreads) k_pc_3(int n, PcVecs V, BicgPtrs P
 // staged -- pass K2.  r alternates between two buffers so no block reads a
 // residual another block rewrote.  Without update (the start) b = r_0.
 template <int TI, int TJ, int NT>
-struct PcMidX {   // x += alpha p on the owned TI x TJ cells (FP64 iterate)
+struct PcMidX {   // x += alpha p on the owned TI x TJ cells of the tile at (i0, j0) (FP64 iterate)
     double* __restrict__ x;
     const float* __restrict__ p;
     double alpha;
     int NX, NY;
     bool on;
-    __device__ __forceinline__ void operator()() const {
+    __device__ __forceinline__ void operator()(int i0, int j0) const {
         if (!on) return;
-        const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
         constexpr int R = (TI * TJ + NT - 1) / NT;
         float pv[R];
         double xv[R];
@@ -1527,10 +1526,24 @@ struct PcOwnR {
     }
 };
 
+// The level-0 kernels of the preconditioned CG walk the tiles of the grid
+// with a two-stage pipeline: a block (two per SM) stages tile t + G while it
+// computes tile t, so the copies of one tile overlap the arithmetic and
+// barriers of the other -- the one-tile-per-block form waited on memory and
+// on its own barriers in turn and reached a sixth of the DRAM bandwidth.
+struct PcfGeo {
+    int tiles_x, ntiles;
+};
+__device__ __forceinline__ int pcf_i0(const PcfGeo& g, int t, int TI) { return (t / g.tiles_x) * TI; }
+__device__ __forceinline__ int pcf_j0(const PcfGeo& g, int t, int TJ) { return (t % g.tiles_x) * TJ; }
+
 template <int TI, int AJ, int RY>
-__global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
-                                                       int NX1, int NY1, PcVecs V, BicgPtrs P, int update) {
+__global__ void __launch_bounds__(AJ * RY, 2) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
+                                                          int NX1, int NY1, PcVecs V, BicgPtrs P, int update, PcfGeo g) {
     constexpr int TJ = AJ - 4, NT = AJ * RY;
+    using D = MgStageDims<TI, AJ, RY>;
+    using T = MgTile<TI, AJ, RY>;
+    extern __shared__ __align__(16) float dsm[];
     pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
@@ -1538,18 +1551,36 @@ __global__ void __launch_bounds__(AJ * RY) k_pcf_down0(MgLvl L, float* __restric
     const int cur = (int)(it & 1);
     // the start passes b = r - 0 * r (q := r, finite) and skips the CG updates
     const bool up = update != 0;
-    const PcMidX<TI, TJ, NT> mid{V.x, V.p[cur ^ 1], __ldcg(&st->alpha), L.NX, L.NY, up};
+    const PcMidX<TI, TJ, NT> mid{V.x, cur ? V.p[0] : V.p[1], __ldcg(&st->alpha), L.NX, L.NY, up};
+    const float* r = cur ? V.r[1] : V.r[0];   // (selected, not indexed: no local copy of V)
+    const float* q = up ? V.q : r;
+    const float alpha = up ? __ldcg(&st->alpha_f) : 0.f;
+    const PcOwnR own{cur ? V.r[0] : V.r[1], up};
+    auto stage = [&](int sidx) {
+        float* b = dsm + sidx * D::kDown;
+        return MgStage{b, b + T::A, b + 2 * T::A, b + 3 * T::A, dsm + 2 * D::kDown, nullptr};
+    };
     Acc<float> acc[1];
-    acc[0] = mg_down_tile<TI, AJ, RY, true, PcMidX<TI, TJ, NT>, PcOwnR, kMgStagedLarge>(
-        blockIdx.y * TI, blockIdx.x * TJ, L, V.r[cur], up ? V.q : V.r[cur],
-                                            up ? __ldcg(&st->alpha_f) : 0.f, mid,
-                                            PcOwnR{V.r[cur ^ 1], up}, x0pre, b1, NX1, NY1);
+    int t = blockIdx.x, sidx = 0;
+    if (t < g.ntiles) mg_down_issue<TI, AJ, RY, true>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, q, stage(0));
+    cp_async_commit();
+    for (; t < g.ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        if (tn < g.ntiles) mg_down_issue<TI, AJ, RY, true>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, q, stage(sidx ^ 1));
+        cp_async_commit();
+        const int i0 = pcf_i0(g, t, TI), j0 = pcf_j0(g, t, TJ);
+        mid(i0, j0);
+        cp_async_wait_group<1>();
+        __syncthreads();
+        mg_down_compute<TI, AJ, RY, true, PcOwnR>(i0, j0, L, alpha, own, stage(sidx), x0pre, b1, NX1, NY1, acc[0]);
+        __syncthreads();   // the stage is refilled next
+        sidx ^= 1;
+    }
     pdl_trigger();
     if (!up) return;
-    double s[1];
-    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
-        threadIdx.x == 0) {
-        pc_finish_iteration(st, s[0]);
+    double sres[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], sres) && threadIdx.x == 0) {
+        pc_finish_iteration(st, sres[0]);
         st->ticket[0] = 0;
     }
 }
@@ -1561,23 +1592,84 @@ struct PcUpOwn {
 };
 
 template <int TI, int AJ, int RY>
-__global__ void __launch_bounds__(AJ * RY) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
-                                                     const float* __restrict__ final1, int NX1, int NY1, float alpha0,
-                                                     PcVecs V, BicgPtrs P) {
+__global__ void __launch_bounds__(AJ * RY, 2) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
+                                                        const float* __restrict__ final1, int NX1, int NY1, float alpha0,
+                                                        PcVecs V, BicgPtrs P, PcfGeo g) {
+    constexpr int TJ = AJ - 4;
+    using D = MgStageDims<TI, AJ, RY>;
+    using T = MgTile<TI, AJ, RY>;
+    extern __shared__ __align__(16) float dsm[];
     pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
+    const float* r = (it & 1) ? V.r[1] : V.r[0];
+    auto stage = [&](int sidx) {
+        float* b = dsm + sidx * D::kUp;
+        // x_pre is staged per tile: sx lives in the stage
+        return MgStage{b + T::A, nullptr, b + 2 * T::A, b + 3 * T::A, b, b + 8 * T::A};
+    };
     Acc<float> acc[1];
-    acc[0] = mg_up_tile<TI, AJ, RY, PcUpOwn, kMgStagedLarge>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, x0pre, final1,
-                                                             NX1, NY1, alpha0, V.r[(int)(it & 1)], PcUpOwn{}, V.z);
+    int t = blockIdx.x, sidx = 0;
+    if (t < g.ntiles) mg_up_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, x0pre, final1, NX1, NY1, r, stage(0));
+    cp_async_commit();
+    for (; t < g.ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        if (tn < g.ntiles)
+            mg_up_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, x0pre, final1, NX1, NY1, r, stage(sidx ^ 1));
+        cp_async_commit();
+        cp_async_wait_group<1>();
+        __syncthreads();
+        mg_up_compute<TI, AJ, RY, PcUpOwn>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, alpha0, PcUpOwn{}, stage(sidx), V.z,
+                                           acc[0]);
+        __syncthreads();
+        sidx ^= 1;
+    }
     pdl_trigger();
-    double s[1];
-    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) &&
-        threadIdx.x == 0) {
-        pc_finish_rz(st, s[0]);
+    double sres[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], sres) && threadIdx.x == 0) {
+        pc_finish_rz(st, sres[0]);
         st->ticket[0] = 0;
     }
+}
+
+// Launch shape of the pipelined level-0 kernels: as many blocks as are
+// resident (two per SM), at most one per tile; dynamic shared memory for two
+// stages (and DOWN's scratch x).
+struct PcfLaunch {
+    PcfGeo g;
+    int blocks;
+    size_t smem_down, smem_up;
+};
+static int pcf_launch(const MgLvl& L0, PcfLaunch* out) {
+    using D = MgStageDims<kMgTI0, kMgAJ0, kMgRY0>;
+    constexpr size_t down = (2 * D::kDown + D::kX) * sizeof(float), up = 2 * D::kUp * sizeof(float);
+    static std::mutex mu;
+    static int sms[64] = {0}, per[64] = {0};
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error("device index %d out of range", dev), KC_ERR_ARG;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!sms[dev]) {
+            int n = 0, pd = 0, pu = 0;
+            KC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+            KC_CUDA(cudaFuncSetAttribute(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)down));
+            KC_CUDA(cudaFuncSetAttribute(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)up));
+            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pd, k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, down));
+            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pu, k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, up));
+            per[dev] = std::max(1, std::min(pd, pu));
+            sms[dev] = n;
+        }
+    }
+    const dim3 tg = mg_tile_grid(L0.NX, L0.NY, kMgTI0, kMgTJ0);
+    out->g = PcfGeo{(int)tg.x, (int)(tg.x * tg.y)};
+    out->blocks = std::max(1, std::min(out->g.ntiles, per[dev] * sms[dev]));
+    out->smem_down = down;
+    out->smem_up = up;
+    return KC_OK;
 }
 
 __global__ void k_copy_f64(int n, const double* __restrict__ a, double* __restrict__ b) {
@@ -2228,14 +2320,16 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
         if (F.ok) {
             // K2 and K3 ride in the V-cycle's level-0 launches; the chain is launched with
             // programmatic dependencies (each kernel waits on its predecessor in-kernel)
-            KC_CUDA(launch_chain(k_pc_1, sg, dim3(kThreads), 0, s, C, g, V, P));
-            const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
-            KC_CUDA(launch_chain(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, tg, dim3(kMgNT0), 0, s, F.L0, F.x0pre, F.b1,
-                                 F.NX1, F.NY1, V, P, 1));
-            int rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
+            PcfLaunch pl;
+            int rc = pcf_launch(F.L0, &pl);
             if (rc) return rc;
-            KC_CUDA(launch_chain(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, tg, dim3(kMgNT0), 0, s, F.L0,
-                                 (const float*)F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P));
+            KC_CUDA(launch_chain(k_pc_1, sg, dim3(kThreads), 0, s, C, g, V, P));
+            KC_CUDA(launch_chain(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_down, s,
+                                 F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1, pl.g));
+            rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
+            if (rc) return rc;
+            KC_CUDA(launch_chain(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_up, s, F.L0,
+                                 (const float*)F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P, pl.g));
             k1 += 2;
         } else {
             k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
@@ -2360,12 +2454,16 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
             const MgFused F = mg_fused(A32, mg_ws, mg_opts);
             int mk = 0;
             if (F.ok) {
-                const dim3 tg = mg_tile_grid(F.L0.NX, F.L0.NY, kMgTI0, kMgTJ0);
-                k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.b1, F.NX1, F.NY1, W, P, 0);
+                PcfLaunch pl;
+                rc = pcf_launch(F.L0, &pl);
+                if (rc) return rc;
+                k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_down, s>>>(F.L0, F.x0pre, F.b1, F.NX1,
+                                                                                            F.NY1, W, P, 0, pl.g);
                 KC_LAUNCH_CHECK("k_pcf_down0");
                 rc = mg_enqueue_coarse(A32, mg_ws, mg_opts, &P.st->done, s, &mk);
                 if (rc) return rc;
-                k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<tg, kMgNT0, 0, s>>>(F.L0, F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, W, P);
+                k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_up, s>>>(F.L0, F.x0pre, F.final1, F.NX1,
+                                                                                        F.NY1, F.alpha0, W, P, pl.g);
                 KC_LAUNCH_CHECK("k_pcf_up0");
             } else {
                 rc = mg_enqueue(A32, mg_ws, mg_opts, W.r[0], W.z, &P.st->done, s, &mk);
