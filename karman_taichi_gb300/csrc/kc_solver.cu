@@ -1869,12 +1869,27 @@ using namespace kc;
 template <typename T, class K>
 static int launch_persistent(K kernel, const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, GridBar* bar,
                              cudaStream_t s) {
-    int dev = 0, sms = 0, per = 0, coop = 0;
+    // device and occupancy queries once per (device, kernel): a solve that
+    // takes a few iterations should not wait on host-side queries
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, std::pair<int, int>> cache;   // -> (SMs, blocks per SM)
+    int dev = 0, sms = 0, per = 0;
     KC_CUDA(cudaGetDevice(&dev));
-    KC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    KC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    if (!coop) return set_error("device %d does not support cooperative launches", dev), KC_ERR_UNSUPPORTED;
-    KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0));
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find({dev, (const void*)kernel});
+        if (it != cache.end()) {
+            sms = it->second.first;
+            per = it->second.second;
+        } else {
+            int coop = 0;
+            KC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            KC_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+            if (!coop) return set_error("device %d does not support cooperative launches", dev), KC_ERR_UNSUPPORTED;
+            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0));
+            cache[{dev, (const void*)kernel}] = {sms, per};
+        }
+    }
     if (per < 1) return set_error("persistent solver kernel cannot be resident"), KC_ERR_UNSUPPORTED;
     dim3 sg = stencil_grid(A->n, A->stride);
     PersistGeo pg{(int)sg.x, (int)(sg.x * sg.y)};
@@ -1926,10 +1941,27 @@ static int run_solver(const kc_system* A, const void* b, void* x, const void* M,
     else
         rc = launch_persistent<T>(k_bicg_persist<T, false>, A, (T*)x, V, P, bar, s);
     if (rc) return rc;
-    rc = read_state(P.st, h, s);
-    if (rc) return rc;
+    // the state and the grid barrier (laid out right after it) in one readback
+    const size_t span = (size_t)((const char*)bar - (const char*)P.st) + sizeof(GridBar);
     GridBar hb;
-    KC_CUDA(cudaMemcpy(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost));
+    if ((const char*)bar > (const char*)P.st && span <= 4096) {
+        const void* hp = readback(P.st, span, s);
+        if (!hp) return KC_ERR_CUDA;
+        SolverState tmp;
+        memcpy(&tmp, hp, sizeof(SolverState));
+        memcpy(&hb, (const char*)hp + ((const char*)bar - (const char*)P.st), sizeof(GridBar));
+        h->status = tmp.status;
+        h->done = tmp.done;
+        h->iter = tmp.iter;
+        h->rTr = tmp.rTr;
+        h->den = tmp.den;
+        h->r0Tr = tmp.r0Tr;
+        h->prev_rel = tmp.prev_rel;
+    } else {
+        rc = read_state(P.st, h, s);
+        if (rc) return rc;
+        KC_CUDA(cudaMemcpy(&hb, bar, sizeof(GridBar), cudaMemcpyDeviceToHost));
+    }
     if (hb.err) return set_error("persistent solver: grid barrier timed out"), KC_ERR_CUDA;
     if (o->history && o->history_len > 1) {
         long long to = std::min<long long>(o->history_len, h->iter + 1);
