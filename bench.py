@@ -233,16 +233,16 @@ def e2e_steps(solver, K, W, world):
     return ms, h2d, d2h
 
 
-# Algorithmic bytes per fine cell of one multigrid-preconditioned CG
-# iteration (FP32 vectors and coefficients, FP64 iterate), each array read or
-# written once per kernel:
-#   k_pc_1       p = z + beta p, q = A p: read z, p, 5 coef; write p, q          36
-#   k_pcf_down0  r = r - alpha q, x += alpha p (FP64), pre-smooth, restrict:
-#                read r, q, W, 5 coef, p, x(8); write r, x(8), x_pre, b_1/4   61
-#   k_pcf_up0    prolong + post-smooth, (r, z): read x_pre, x_1/4, r, W, 5 coef;
-#                write z                                                        37
+# Algorithmic bytes per fine cell of one iteration of the single-reduction
+# multigrid-preconditioned CG (FP32 vectors and coefficients, FP64 iterate),
+# each array read or written once per kernel:
+#   k_pcc_down0  s = w + beta s, r = r - alpha s, p = z + beta p, x += alpha p
+#                (FP64), pre-smooth, restrict: read r, w, s, W, 5 coef, z, p,
+#                x(8); write s, r, p, x(8), x_pre, b_1/4                         77
+#   k_pcc_up0    prolong + post-smooth, w = A z, (r, z), (w, z): read x_pre,
+#                x_1/4, r, W, 5 coef; write z, w                                 41
 #   levels >= 1  DOWN 33 + UP 37 bytes per coarse cell, n/3 coarse cells         23
-PCG_MG_BYTES_PER_CELL = 36 + 61 + 37 + 23
+PCG_MG_BYTES_PER_CELL = 77 + 41 + 23
 
 
 def roofline_p_solve(solver, mode, peak):
@@ -272,7 +272,7 @@ def roofline_p_solve(solver, mode, peak):
     else:
         alg = PCG_MG_BYTES_PER_CELL * n * info.iters + (info.refinements + 1) * 7 * 8 * n
         kernel = "kc_pcg_refined"
-        note = (f"{PCG_MG_BYTES_PER_CELL} B/cell/PCG iteration (k_pc_1 36, k_pcf_down0 61, k_pcf_up0 37, "
+        note = (f"{PCG_MG_BYTES_PER_CELL} B/cell/CG iteration (k_pcc_down0 77, k_pcc_up0 41, "
                 f"levels>=1 23) + 56 B/cell per FP64 refinement residual")
     achieved = alg / (ms * 1e-3) / 1e9
     traffic = None

@@ -97,12 +97,13 @@ struct MgTile {
 };
 
 // stage the 5 coefficient components over the whole staged region of the tile at (i0, j0)
-template <int TI, class T>
+// (H: halo width, the region starts at (i0 - H, j0 - H))
+template <int TI, class T, int H = 2>
 __device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, float* sc) {
-    const int b = T::tx(), j = j0 + b - 2;
+    const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = i0 + a - 2;
+        const int i = i0 + a - H;
         const bool in = jin && i >= 0 && i < L.NX;
         const float* g = in ? L.c + (long long)(i * L.NY + j) * L.es : L.c;
         const int u = a * T::AJ + b;
@@ -145,6 +146,7 @@ struct MgStage {
     float* sc;    // 5 coefficient components
     float* sx;
     float* sxc;
+    float* ss;    // a further staged array of the caller's (the single-reduction CG's previous s)
 };
 template <int TI, int AJ, int RY>
 struct MgStageDims {
@@ -175,13 +177,24 @@ __device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, co
 
 // DOWN, after the tile's copies have landed: b = b_in - alpha q, red start,
 // black half-sweep over the 1-cell ring, x and the restricted residual out
-template <int TI, int AJ, int RY, bool HasQ, class Own>
-__device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
-                                                MgStage S, float* __restrict__ xout, float* __restrict__ bc,
-                                                int NXc, int NYc, typename Own::Sum& sum) {
+// right-hand side of the DOWN pass at staged position u: b_in (MgPreB) or
+// b_in - alpha q (MgPreQ); k is the cell index of an owned cell, else -1
+struct MgPreB {
+    __device__ __forceinline__ float operator()(const MgStage& S, int u, int) const { return S.sb[u]; }
+};
+struct MgPreQ {
+    float alpha;
+    __device__ __forceinline__ float operator()(const MgStage& S, int u, int) const {
+        return fmaf(-alpha, S.sq[u], S.sb[u]);
+    }
+};
+
+template <int TI, int AJ, int RY, class Pre, class Own>
+__device__ __forceinline__ void mg_down_compute_pre(int i0, int j0, const MgLvl& L, const Pre& pre, const Own& own,
+                                                    MgStage S, float* __restrict__ xout, float* __restrict__ bc,
+                                                    int NXc, int NYc, typename Own::Sum& sum) {
     using T = MgTile<TI, AJ, RY>;
     float* sb = S.sb;
-    const float* sq = S.sq;
     const float* sw = S.sw;
     float* sx = S.sx;
     const MgCoef<T, true> C{S.sc, L, i0, j0};
@@ -191,12 +204,10 @@ __device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, 
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
         const int i = i0 + a - 2;
-        float bv = sb[u];
-        if (HasQ) {
-            bv = fmaf(-alpha, sq[u], bv);
-            sb[u] = bv;
-        }
-        if (jown && a >= 2 && a < TI + 2 && i < L.NX) own(i * L.NY + j, bv, sum);
+        const int k = (jown && a >= 2 && a < TI + 2 && i < L.NX) ? i * L.NY + j : -1;
+        const float bv = pre(S, u, k);
+        sb[u] = bv;
+        if (k >= 0) own(k, bv, sum);
         sx[u] = ((a + b) & 1) == 0 ? sw[u] * bv : 0.f;
     }
     __syncthreads();
@@ -234,6 +245,16 @@ __device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, 
     }
 }
 
+template <int TI, int AJ, int RY, bool HasQ, class Own>
+__device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
+                                                MgStage S, float* __restrict__ xout, float* __restrict__ bc,
+                                                int NXc, int NYc, typename Own::Sum& sum) {
+    if (HasQ)
+        mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, MgPreQ{alpha}, own, S, xout, bc, NXc, NYc, sum);
+    else
+        mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, MgPreB{}, own, S, xout, bc, NXc, NYc, sum);
+}
+
 // DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
 template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true>
 __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
@@ -245,7 +266,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
         __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
         __shared__ __align__(16) float sq[HasQ ? T::A : 1];
         __shared__ __align__(16) float sc[5 * T::A];
-        const MgStage S{sb, sq, sw, sc, sx, nullptr};
+        const MgStage S{sb, sq, sw, sc, sx, nullptr, nullptr};
         mg_down_issue<TI, AJ, RY, HasQ>(i0, j0, L, b_in, q, S);
         cp_async_commit();
         mid();
@@ -401,7 +422,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
     if (STAGED) {
         __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
         __shared__ __align__(16) float sc[5 * T::A];
-        const MgStage S{sb, nullptr, sw, sc, sx, sxc};
+        const MgStage S{sb, nullptr, sw, sc, sx, sxc, nullptr};
         mg_up_issue<TI, AJ, RY>(i0, j0, L, xpre, xc, NXc, NYc, b_in, S);
         cp_async_commit();
         cp_async_wait_all();
@@ -458,6 +479,101 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
             own(k, xv, sb[u], sum);
         }
     return sum;
+}
+
+// ---- UP with a 3-cell halo: z final on the owned cells and their 1-ring ----
+// The single-reduction CG needs w = A z next to z, so the UP pass also
+// finishes the red cells of the 1-ring (the black half-sweep then covers the
+// 2-ring): the staged region is the tile plus 3 cells, TJ = AJ - 6 owned
+// columns.  z on the owned cells is the same, operation for operation, as
+// with the 2-cell halo.
+template <int TI, int AJ_, int RY_>
+struct MgTile3 {
+    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY;
+    static constexpr int TJ = AJ - 6, AI = TI + 6, A = AI * AJ;
+    static constexpr int XI = TI / 2 + 4, XJ = AJ / 2 + 1, XC = XI * XJ;   // coarse cells under the region
+    static_assert(TI % 2 == 0 && TJ % 2 == 0, "aggregates must not straddle tiles");
+    static_assert((AJ & (AJ - 1)) == 0, "row width must be a power of two");
+    __device__ static __forceinline__ int tx() { return threadIdx.x & (AJ - 1); }
+    __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
+};
+
+// stage x_pre, b, W, the coefficients and the coarse cells for the tile at (i0, j0) (region from i0 - 3, j0 - 3)
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void mg_up3_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
+                                             const float* __restrict__ xc, int NXc, int NYc,
+                                             const float* __restrict__ b_in, MgStage S) {
+    using T = MgTile3<TI, AJ, RY>;
+    const int b = T::tx(), j = j0 + b - 3;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 3;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(S.sx + u, xpre + k, in);
+        cp_async4(S.sb + u, b_in + k, in);
+        cp_async4(S.sw + u, L.winv + k, in);
+    }
+    for (int t = threadIdx.x; t < T::XC; t += T::NT) {
+        const int ca = t / T::XJ, cb = t - ca * T::XJ;
+        const int I = (i0 >> 1) - 2 + ca, J = (j0 >> 1) - 2 + cb;
+        const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
+        cp_async4(S.sxc + t, xc + (in ? I * NYc + J : 0), in);
+    }
+    mg_stage_coef<TI, T, 3>(L, i0, j0, S.sc);
+}
+
+// prolong, black half-sweep over the 2-ring, red half-sweep over the 1-ring;
+// then on the owned cells z, w = A z and the sums (r, z), (w, z)
+template <int TI, int AJ, int RY, class Acc2>
+__device__ __forceinline__ void mg_up3_compute(int i0, int j0, const MgLvl& L, float alpha, MgStage S,
+                                               float* __restrict__ z_out, float* __restrict__ w_out, Acc2& rz,
+                                               Acc2& wz) {
+    using T = MgTile3<TI, AJ, RY>;
+    float* sx = S.sx;
+    const float* sb = S.sb;
+    const float* sw = S.sw;
+    const float* sxc = S.sxc;
+    const MgCoef<T, true> C{S.sc, L, i0, j0};
+    const int b = T::tx(), j = j0 + b - 3;
+    // prolongation over the staged region (coupled cells only); the coarse cell of staged (a, b) is ((a+1)/2, (b+1)/2)
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int u = a * T::AJ + b;
+        if (!C.linked(u)) continue;
+        sx[u] = fmaf(alpha, sxc[((a + 1) >> 1) * T::XJ + ((b + 1) >> 1)], sx[u]);
+    }
+    __syncthreads();
+    // black half-sweep over the 2-ring and inside ((a + b) odd <=> (i + j) odd: the offset 3 + 3 is even)
+    if (b >= 1 && b < AJ - 1)
+        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
+            if (((a + b) & 1) == 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+        }
+    __syncthreads();
+    // red half-sweep over the 1-ring and inside
+    if (b >= 2 && b < AJ - 2)
+        for (int a = 2 + T::ty(); a < T::AI - 2; a += T::RY) {
+            if (((a + b) & 1) != 0) continue;
+            const int u = a * T::AJ + b;
+            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+        }
+    __syncthreads();
+    // owned cells: z, w = A z, (r, z), (w, z)
+    if (b >= 3 && b < T::TJ + 3 && j < L.NY)
+        for (int a = 3 + T::ty(); a < TI + 3; a += T::RY) {
+            const int i = i0 + a - 3;
+            if (i >= L.NX) continue;
+            const int u = a * T::AJ + b;
+            const float zv = sx[u];
+            const float wv = C.ax(sx, u);
+            const int k = i * L.NY + j;
+            z_out[k] = zv;
+            w_out[k] = wv;
+            rz.add(sb[u], zv);
+            wz.add(wv, zv);
+        }
 }
 
 }  // namespace kc

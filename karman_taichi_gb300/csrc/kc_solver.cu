@@ -1367,6 +1367,7 @@ __global__ void __launch_bounds__(kPwThreads) k_pb_x(int n, PbVecs V, BicgPtrs P
 struct PcVecs {
     float *r[2], *z, *p[2], *q;   // r: ping-pong pair in the fused level-0 path, r[0] otherwise
     double* x;
+    float* s[2];                  // fused path: s = A p (ping-pong); q holds w = A z there
 };
 
 // called by thread 0 of the last block once (r, r) of the new residual is known
@@ -1487,17 +1488,30 @@ __global__ void __launch_bounds__(kPwThreads) k_pc_3(int n, PcVecs V, BicgPtrs P
 // accumulate (r_new, r_new), and x += alpha p runs while the tile is being
 // staged -- pass K2.  r alternates between two buffers so no block reads a
 // residual another block rewrote.  Without update (the start) b = r_0.
+// ---- fused level-0 passes of the single-reduction preconditioned CG ----------------
+// CG in the form of Chronopoulos and Gear: with z = M r and w = A z both
+// inner products of an iteration come out of one pass,
+//   gamma = (r, z), delta = (w, z),  beta = gamma / gamma_old,
+//   alpha = gamma / (delta - beta gamma / alpha_old),
+//   p = z + beta p,  s = w + beta s  (s = A p by recurrence),
+//   x += alpha p,  r -= alpha s,
+// so no separate pass forms A p: UP_0 (with a 3-cell halo, so that z is
+// final on the 1-ring) writes z and w = A z and sums both products; DOWN_0
+// forms s and the new r over its staged region, updates p and x on its own
+// cells and hands b = r to the V-cycle.  Two level-0 launches per iteration.
 template <int TI, int TJ, int NT>
-struct PcMidX {   // x += alpha p on the owned TI x TJ cells of the tile at (i0, j0) (FP64 iterate)
+struct PcMidCG {   // p = z + beta p, x += alpha p on the owned TI x TJ cells of the tile at (i0, j0)
     double* __restrict__ x;
-    const float* __restrict__ p;
+    float* __restrict__ p;
+    const float* __restrict__ z;
     double alpha;
+    float beta;
     int NX, NY;
-    bool on;
+    bool on, first;
     __device__ __forceinline__ void operator()(int i0, int j0) const {
         if (!on) return;
         constexpr int R = (TI * TJ + NT - 1) / NT;
-        float pv[R];
+        float zv[R], pv[R];
         double xv[R];
         int kk[R];
         // all loads first (the cells are distinct, so no store can feed a later load)
@@ -1507,12 +1521,29 @@ struct PcMidX {   // x += alpha p on the owned TI x TJ cells of the tile at (i0,
             const int a = t / TJ, b = t - a * TJ;
             const int i = i0 + a, j = j0 + b;
             kk[m] = (t < TI * TJ && i < NX && j < NY) ? i * NY + j : -1;
-            pv[m] = kk[m] >= 0 ? __ldg(p + kk[m]) : 0.f;
+            zv[m] = kk[m] >= 0 ? __ldcg(z + kk[m]) : 0.f;
+            pv[m] = (kk[m] >= 0 && !first) ? __ldcg(p + kk[m]) : 0.f;
             xv[m] = kk[m] >= 0 ? __ldcg(x + kk[m]) : 0.0;
         }
 #pragma unroll
         for (int m = 0; m < R; ++m)
-            if (kk[m] >= 0) x[kk[m]] = fma(alpha, (double)pv[m], xv[m]);
+            if (kk[m] >= 0) {
+                const float pn = first ? zv[m] : fmaf(beta, pv[m], zv[m]);
+                p[kk[m]] = pn;
+                x[kk[m]] = fma(alpha, (double)pn, xv[m]);
+            }
+    }
+};
+// right-hand side of DOWN_0: s = w + beta s_old (staged sq = w, ss = s_old), b = r - alpha s;
+// an owned cell also stores its s
+struct PcPreCG {
+    float alpha, beta;
+    bool first;
+    float* __restrict__ s_out;
+    __device__ __forceinline__ float operator()(const MgStage& S, int u, int k) const {
+        const float sv = first ? S.sq[u] : fmaf(beta, S.ss[u], S.sq[u]);
+        if (k >= 0) s_out[k] = sv;
+        return fmaf(-alpha, sv, S.sb[u]);
     }
 };
 struct PcOwnR {
@@ -1526,53 +1557,78 @@ struct PcOwnR {
     }
 };
 
-// The level-0 kernels of the preconditioned CG walk the tiles of the grid
-// with a two-stage pipeline: a block (two per SM) stages tile t + G while it
-// computes tile t, so the copies of one tile overlap the arithmetic and
-// barriers of the other -- the one-tile-per-block form waited on memory and
-// on its own barriers in turn and reached a sixth of the DRAM bandwidth.
+// DOWN_0 staging: r (sb), w (sq), s_old (ss), W, coefficients over the 2-cell-halo region
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void pcc_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ r,
+                                               const float* __restrict__ w, const float* __restrict__ s_old,
+                                               bool update, bool first, MgStage S) {
+    using T = MgTile<TI, AJ, RY>;
+    const int b = T::tx(), j = j0 + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + b;
+        cp_async4(S.sb + u, r + k, in);
+        if (update) cp_async4(S.sq + u, w + k, in);
+        if (update && !first) cp_async4(S.ss + u, s_old + k, in);
+        cp_async4(S.sw + u, L.winv + k, in);
+    }
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
+
+// The level-0 kernels walk the tiles of the grid with a two-stage pipeline:
+// a block (two per SM) stages tile t + G while it computes tile t, so the
+// copies of one tile overlap the arithmetic and barriers of the other.
 struct PcfGeo {
     int tiles_x, ntiles;
 };
 __device__ __forceinline__ int pcf_i0(const PcfGeo& g, int t, int TI) { return (t / g.tiles_x) * TI; }
 __device__ __forceinline__ int pcf_j0(const PcfGeo& g, int t, int TJ) { return (t % g.tiles_x) * TJ; }
 
+// update = 0: the start of a sweep (b = r, no CG vector updates)
 template <int TI, int AJ, int RY>
-__global__ void __launch_bounds__(AJ * RY, 2) k_pcf_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
+__global__ void __launch_bounds__(AJ * RY, 2) k_pcc_down0(MgLvl L, float* __restrict__ x0pre, float* __restrict__ b1,
                                                           int NX1, int NY1, PcVecs V, BicgPtrs P, int update, PcfGeo g) {
     constexpr int TJ = AJ - 4, NT = AJ * RY;
-    using D = MgStageDims<TI, AJ, RY>;
     using T = MgTile<TI, AJ, RY>;
+    constexpr int SA = 9 * T::A;   // staged floats per stage: sb, sq, ss, sw, sc[5]
     extern __shared__ __align__(16) float dsm[];
     pdl_wait();
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const long long it = __ldcg(&st->iter);
     const int cur = (int)(it & 1);
-    // the start passes b = r - 0 * r (q := r, finite) and skips the CG updates
-    const bool up = update != 0;
-    const PcMidX<TI, TJ, NT> mid{V.x, cur ? V.p[0] : V.p[1], __ldcg(&st->alpha), L.NX, L.NY, up};
+    const bool up = update != 0, first = it == 0;
     const float* r = cur ? V.r[1] : V.r[0];   // (selected, not indexed: no local copy of V)
-    const float* q = up ? V.q : r;
-    const float alpha = up ? __ldcg(&st->alpha_f) : 0.f;
+    const float* s_old = cur ? V.s[1] : V.s[0];
+    float* s_new = cur ? V.s[0] : V.s[1];
+    const float alpha = up ? __ldcg(&st->alpha_f) : 0.f, beta = up ? __ldcg(&st->beta_f) : 0.f;
+    const PcMidCG<TI, TJ, NT> mid{V.x, V.p[0], V.z, __ldcg(&st->alpha), beta, L.NX, L.NY, up, first};
     const PcOwnR own{cur ? V.r[0] : V.r[1], up};
     auto stage = [&](int sidx) {
-        float* b = dsm + sidx * D::kDown;
-        return MgStage{b, b + T::A, b + 2 * T::A, b + 3 * T::A, dsm + 2 * D::kDown, nullptr};
+        float* b = dsm + sidx * SA;
+        return MgStage{b, b + T::A, b + 3 * T::A, b + 4 * T::A, dsm + 2 * SA, nullptr, b + 2 * T::A};
     };
     Acc<float> acc[1];
     int t = blockIdx.x, sidx = 0;
-    if (t < g.ntiles) mg_down_issue<TI, AJ, RY, true>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, q, stage(0));
+    if (t < g.ntiles) pcc_down_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, V.q, s_old, up, first, stage(0));
     cp_async_commit();
     for (; t < g.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
-        if (tn < g.ntiles) mg_down_issue<TI, AJ, RY, true>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, q, stage(sidx ^ 1));
+        if (tn < g.ntiles)
+            pcc_down_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, V.q, s_old, up, first, stage(sidx ^ 1));
         cp_async_commit();
         const int i0 = pcf_i0(g, t, TI), j0 = pcf_j0(g, t, TJ);
         mid(i0, j0);
         cp_async_wait_group<1>();
         __syncthreads();
-        mg_down_compute<TI, AJ, RY, true, PcOwnR>(i0, j0, L, alpha, own, stage(sidx), x0pre, b1, NX1, NY1, acc[0]);
+        if (up)
+            mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, PcPreCG{alpha, beta, first, s_new}, own, stage(sidx), x0pre, b1,
+                                            NX1, NY1, acc[0]);
+        else
+            mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, MgPreB{}, own, stage(sidx), x0pre, b1, NX1, NY1, acc[0]);
         __syncthreads();   // the stage is refilled next
         sidx ^= 1;
     }
@@ -1585,19 +1641,35 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcf_down0(MgLvl L, float* __rest
     }
 }
 
-// UP_0 writes z and accumulates (r, z) -- pass K3
-struct PcUpOwn {
-    using Sum = Acc<float>;
-    __device__ __forceinline__ void operator()(int, float z, float r, Sum& acc) const { acc.add(r, z); }
-};
+// called by thread 0 of the last block once gamma = (r, z) and delta = (w, z) are known
+__device__ __forceinline__ void pcc_finish(SolverState* st, double gamma, double delta) {
+    if (!(gamma > 0.0)) {   // (r, M r) <= 0: M is not positive definite
+        st->status = isfinite(gamma) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+        st->done = 1;
+        return;
+    }
+    double beta = 0.0, den = delta;
+    if (st->iter > 0) {
+        beta = gamma / st->old;
+        den = delta - beta * gamma / st->alpha;
+    }
+    if (!(den > 0.0)) {   // (p, A p) <= 0: the operator is not positive definite
+        st->status = isfinite(den) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+        st->done = 1;
+        return;
+    }
+    st->beta = beta;
+    st->beta_f = (float)beta;
+    st->old = gamma;
+    set_alpha(st, gamma / den);
+}
 
 template <int TI, int AJ, int RY>
-__global__ void __launch_bounds__(AJ * RY, 2) k_pcf_up0(MgLvl L, const float* __restrict__ x0pre,
+__global__ void __launch_bounds__(AJ * RY, 2) k_pcc_up0(MgLvl L, const float* __restrict__ x0pre,
                                                         const float* __restrict__ final1, int NX1, int NY1, float alpha0,
                                                         PcVecs V, BicgPtrs P, PcfGeo g) {
-    constexpr int TJ = AJ - 4;
-    using D = MgStageDims<TI, AJ, RY>;
-    using T = MgTile<TI, AJ, RY>;
+    using T = MgTile3<TI, AJ, RY>;
+    constexpr int TJ = T::TJ, SA = 8 * T::A + T::XC;
     extern __shared__ __align__(16) float dsm[];
     pdl_wait();
     SolverState* st = P.st;
@@ -1605,30 +1677,28 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcf_up0(MgLvl L, const float* __
     const long long it = __ldcg(&st->iter);
     const float* r = (it & 1) ? V.r[1] : V.r[0];
     auto stage = [&](int sidx) {
-        float* b = dsm + sidx * D::kUp;
-        // x_pre is staged per tile: sx lives in the stage
-        return MgStage{b + T::A, nullptr, b + 2 * T::A, b + 3 * T::A, b, b + 8 * T::A};
+        float* b = dsm + sidx * SA;
+        return MgStage{b + T::A, nullptr, b + 2 * T::A, b + 3 * T::A, b, b + 8 * T::A, nullptr};
     };
-    Acc<float> acc[1];
+    Acc<float> acc[2];
     int t = blockIdx.x, sidx = 0;
-    if (t < g.ntiles) mg_up_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, x0pre, final1, NX1, NY1, r, stage(0));
+    if (t < g.ntiles) mg_up3_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, x0pre, final1, NX1, NY1, r, stage(0));
     cp_async_commit();
     for (; t < g.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
         if (tn < g.ntiles)
-            mg_up_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, x0pre, final1, NX1, NY1, r, stage(sidx ^ 1));
+            mg_up3_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, x0pre, final1, NX1, NY1, r, stage(sidx ^ 1));
         cp_async_commit();
         cp_async_wait_group<1>();
         __syncthreads();
-        mg_up_compute<TI, AJ, RY, PcUpOwn>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, alpha0, PcUpOwn{}, stage(sidx), V.z,
-                                           acc[0]);
+        mg_up3_compute<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, alpha0, stage(sidx), V.z, V.q, acc[0], acc[1]);
         __syncthreads();
         sidx ^= 1;
     }
     pdl_trigger();
-    double sres[1];
-    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], sres) && threadIdx.x == 0) {
-        pc_finish_rz(st, sres[0]);
+    double sres[2];
+    if (block_partials<2>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &st->ticket[0], sres) && threadIdx.x == 0) {
+        pcc_finish(st, sres[0], sres[1]);
         st->ticket[0] = 0;
     }
 }
@@ -1637,13 +1707,14 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcf_up0(MgLvl L, const float* __
 // resident (two per SM), at most one per tile; dynamic shared memory for two
 // stages (and DOWN's scratch x).
 struct PcfLaunch {
-    PcfGeo g;
+    PcfGeo gd, gu;
     int blocks;
     size_t smem_down, smem_up;
 };
 static int pcf_launch(const MgLvl& L0, PcfLaunch* out) {
-    using D = MgStageDims<kMgTI0, kMgAJ0, kMgRY0>;
-    constexpr size_t down = (2 * D::kDown + D::kX) * sizeof(float), up = 2 * D::kUp * sizeof(float);
+    using TD = MgTile<kMgTI0, kMgAJ0, kMgRY0>;
+    using TU = MgTile3<kMgTI0, kMgAJ0, kMgRY0>;
+    constexpr size_t down = (2 * 9 * TD::A + TD::A) * sizeof(float), up = 2 * (8 * TU::A + TU::XC) * sizeof(float);
     static std::mutex mu;
     static int sms[64] = {0}, per[64] = {0};
     int dev = 0;
@@ -1654,19 +1725,20 @@ static int pcf_launch(const MgLvl& L0, PcfLaunch* out) {
         if (!sms[dev]) {
             int n = 0, pd = 0, pu = 0;
             KC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-            KC_CUDA(cudaFuncSetAttribute(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            KC_CUDA(cudaFuncSetAttribute(k_pcc_down0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)down));
-            KC_CUDA(cudaFuncSetAttribute(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            KC_CUDA(cudaFuncSetAttribute(k_pcc_up0<kMgTI0, kMgAJ0, kMgRY0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)up));
-            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pd, k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, down));
-            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pu, k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, up));
+            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pd, k_pcc_down0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, down));
+            KC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pu, k_pcc_up0<kMgTI0, kMgAJ0, kMgRY0>, kMgNT0, up));
             per[dev] = std::max(1, std::min(pd, pu));
             sms[dev] = n;
         }
     }
-    const dim3 tg = mg_tile_grid(L0.NX, L0.NY, kMgTI0, kMgTJ0);
-    out->g = PcfGeo{(int)tg.x, (int)(tg.x * tg.y)};
-    out->blocks = std::max(1, std::min(out->g.ntiles, per[dev] * sms[dev]));
+    const dim3 td = mg_tile_grid(L0.NX, L0.NY, kMgTI0, TD::TJ), tu = mg_tile_grid(L0.NX, L0.NY, kMgTI0, TU::TJ);
+    out->gd = PcfGeo{(int)td.x, (int)(td.x * td.y)};
+    out->gu = PcfGeo{(int)tu.x, (int)(tu.x * tu.y)};
+    out->blocks = std::max(1, std::min(std::min(out->gd.ntiles, out->gu.ntiles), per[dev] * sms[dev]));
     out->smem_down = down;
     out->smem_up = up;
     return KC_OK;
@@ -2350,19 +2422,19 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
     int k1 = 0;
     for (int q = 0; q < m; ++q) {
         if (F.ok) {
-            // K2 and K3 ride in the V-cycle's level-0 launches; the chain is launched with
-            // programmatic dependencies (each kernel waits on its predecessor in-kernel)
+            // the single-reduction CG: its vector updates ride in the V-cycle's level-0
+            // launches; the chain is launched with programmatic dependencies (each kernel
+            // waits on its predecessor in-kernel)
             PcfLaunch pl;
             int rc = pcf_launch(F.L0, &pl);
             if (rc) return rc;
-            KC_CUDA(launch_chain(k_pc_1, sg, dim3(kThreads), 0, s, C, g, V, P));
-            KC_CUDA(launch_chain(k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_down, s,
-                                 F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1, pl.g));
+            KC_CUDA(launch_chain(k_pcc_down0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_down, s,
+                                 F.L0, F.x0pre, F.b1, F.NX1, F.NY1, V, P, 1, pl.gd));
             rc = mg_enqueue_coarse(A32, mg_ws, mo, done, s, &k1);
             if (rc) return rc;
-            KC_CUDA(launch_chain(k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_up, s, F.L0,
-                                 (const float*)F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P, pl.g));
-            k1 += 2;
+            KC_CUDA(launch_chain(k_pcc_up0<kMgTI0, kMgAJ0, kMgRY0>, dim3(pl.blocks), dim3(kMgNT0), pl.smem_up, s, F.L0,
+                                 (const float*)F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, V, P, pl.gu));
+            k1 += 2;   // level 0's DOWN and UP: with the coarse levels, the whole iteration
         } else {
             k_pc_1<<<sg, kThreads, 0, s>>>(C, g, V, P);
             k_pc_2<<<pb, kPwThreads, 0, s>>>(g.n, V, P);
@@ -2373,13 +2445,13 @@ static int launch_pc_iters(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
             k1 += 2;
         }
     }
-    if (kernels) *kernels = 1 + k1;
+    if (kernels) *kernels = (F.ok ? 0 : 1) + k1;
     return KC_OK;
 }
 
 // number of kernels one preconditioned CG iteration launches
 static int pc_iter_kernels(const kc_system* A32, void* mg_ws, const kc_mg_opts* mo) {
-    return 1 + mg_cycle_kernels(A32, mo) + (mg_fused(A32, mg_ws, mo).ok ? 0 : 2);
+    return mg_fused(A32, mg_ws, mo).ok ? mg_cycle_kernels(A32, mo) : 1 + mg_cycle_kernels(A32, mo) + 2;
 }
 // Multigrid-preconditioned FP32 Krylov solve (BiCGSTAB or CG) inside FP64
 // iterative refinement: r = b - A64 x in FP64, inner solve A32 d = r to
@@ -2411,7 +2483,7 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     for (int q = 0; q < 8; ++q) fv[q] = (float*)(base + L.off_vec[q]);
     double* d64 = (double*)(base + L.off_x);
     PbVecs V{fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], fv[6], fv[7], d64};
-    PcVecs W{{fv[0], fv[5]}, fv[1], {fv[2], fv[3]}, fv[4], d64};
+    PcVecs W{{fv[0], fv[5]}, fv[1], {fv[2], fv[3]}, fv[4], d64, {fv[6], fv[7]}};
     const long long n = A64->n;
     Geo g{(int)n, A64->stride};
     dim3 sg = stencil_grid(n, A64->stride);
@@ -2489,14 +2561,14 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
                 PcfLaunch pl;
                 rc = pcf_launch(F.L0, &pl);
                 if (rc) return rc;
-                k_pcf_down0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_down, s>>>(F.L0, F.x0pre, F.b1, F.NX1,
-                                                                                            F.NY1, W, P, 0, pl.g);
-                KC_LAUNCH_CHECK("k_pcf_down0");
+                k_pcc_down0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_down, s>>>(F.L0, F.x0pre, F.b1, F.NX1,
+                                                                                            F.NY1, W, P, 0, pl.gd);
+                KC_LAUNCH_CHECK("k_pcc_down0");
                 rc = mg_enqueue_coarse(A32, mg_ws, mg_opts, &P.st->done, s, &mk);
                 if (rc) return rc;
-                k_pcf_up0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_up, s>>>(F.L0, F.x0pre, F.final1, F.NX1,
-                                                                                        F.NY1, F.alpha0, W, P, pl.g);
-                KC_LAUNCH_CHECK("k_pcf_up0");
+                k_pcc_up0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_up, s>>>(F.L0, F.x0pre, F.final1, F.NX1,
+                                                                                        F.NY1, F.alpha0, W, P, pl.gu);
+                KC_LAUNCH_CHECK("k_pcc_up0");
             } else {
                 rc = mg_enqueue(A32, mg_ws, mg_opts, W.r[0], W.z, &P.st->done, s, &mk);
                 if (rc) return rc;
