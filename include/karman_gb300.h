@@ -176,6 +176,23 @@ int kc_jacobi(const kc_system* A, const double* b, const double* x, double* y, d
               int i0, int i1, int j0, int j1, double* max_diff_dev, void* ws, size_t ws_bytes,
               void* stream);
 
+/* Red-black Gauss-Seidel solve of an FP64 system (standard or Laplacian
+ * form): the Gauss-Seidel counterpart of the reference's Jacobi solves
+ * (pressure_valid.py:192-233; debug/20210828_karman_taihi.py:375-393), used
+ * for the channel's momentum systems, whose time term makes them strongly
+ * diagonally dominant.  One launch per sweep (the red cells, then the black
+ * ones, of a tile; colour = parity of i + j of the [n/stride][stride] view),
+ * which also sums the residual of the iterate it starts from: the stopping
+ * test ||b - A x|| < eps * (||b|| for rel_to = KC_REL_B, else ||b - A x0||)
+ * is checked one sweep late, after chunks of sweeps (check_every, or 4 up to
+ * 16) launched as CUDA graphs.  opts: eps, max_iter (sweeps), x0, rel_to,
+ * check_every, use_graph; precond must be KC_PRECOND_NONE.  Rows with a zero
+ * diagonal keep their x.  ws: kc_rbgs_ws_bytes(n, stride) bytes.
+ * info->iters: sweeps applied; info->rel_res: the last residual checked. */
+size_t kc_rbgs_ws_bytes(long long n, int stride);
+int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_bytes,
+            const kc_solve_opts* opts, kc_solve_info* info, void* stream);
+
 /* ---- multigrid preconditioner (FP32) --------------------------------------
  * The reference names multigrid as its missing next step (README.md:31;
  * debug/note.md:6); it has Jacobi only (karman_taichi.py:398-399).
@@ -389,17 +406,24 @@ int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, c
 /* ---- native SIMPLE step and the batched executor --------------------------- */
 /* One channel instance (caller-owned device buffers, shapes as kc_assemble_*).
  * precision KC_F64: the plain method (every solve FP64 BiCGSTAB, cold start,
- * rel. tol eps, cap n); KC_F32: the accelerated path (momentum: FP32 BiCGSTAB
- * in FP64 refinement, inner tol eps_inner; p': multigrid CG in FP64
- * refinement on coef_p32 in Laplacian form, inner tol eps_inner_p, with the
- * plain FP64 BiCGSTAB as fallback).  Workspaces: ws_u / ws_v of
- * kc_bicgstab_ws_bytes (F64) or kc_refined_ws_bytes (F32) bytes; ws_p of
- * kc_bicgstab_ws_bytes (F64) or the larger of that and kc_pbicgstab_ws_bytes
- * (F32); mg_ws of kc_mg_ws_bytes (F32 only); rws of kc_reduce_ws_bytes. */
+ * rel. tol eps, cap n); KC_F32: the accelerated path (momentum:
+ * KC_MOMENTUM_BICGSTAB, FP32 BiCGSTAB in FP64 refinement, inner tol
+ * eps_inner, or KC_MOMENTUM_RBGS, FP64 red-black Gauss-Seidel (kc_rbgs) with
+ * the refined BiCGSTAB as fallback, both from the previous outer iteration's
+ * u*, v* to ||b - A x|| / ||b|| < eps; p': multigrid CG in FP64 refinement
+ * on coef_p32 in Laplacian form, inner tol eps_inner_p, with the plain FP64
+ * BiCGSTAB as fallback).  Workspaces: ws_u / ws_v of kc_bicgstab_ws_bytes
+ * (F64) or the larger of kc_refined_ws_bytes and kc_rbgs_ws_bytes (F32)
+ * bytes; ws_p of kc_bicgstab_ws_bytes (F64) or the larger of that and
+ * kc_pbicgstab_ws_bytes (F32); mg_ws of kc_mg_ws_bytes (F32 only); rws of
+ * kc_reduce_ws_bytes. */
+#define KC_MOMENTUM_BICGSTAB 0
+#define KC_MOMENTUM_RBGS 1
 typedef struct {
     kc_phys phys;                       /* mode must be KC_MODE_CHANNEL */
     int precision, max_outer, use_graph;
     int persistent;                     /* 1: BiCGSTAB solves as one cooperative launch, 0: graph chunks */
+    int momentum, pad_m;                /* KC_F32 momentum solver: KC_MOMENTUM_BICGSTAB or KC_MOMENTUM_RBGS */
     double mass_tol, eps, eps_inner, eps_inner_p;
     double *u, *v, *p, *u0, *v0, *pcor, *u_mid, *v_mid;
     const unsigned char* solid;         /* [nx+2][ny+2], 1 = blocked cell */

@@ -64,6 +64,9 @@ class KcPhys(C.Structure):
                 ("alpha_m", C.c_double), ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
 
 
+MOMENTUM_BICGSTAB, MOMENTUM_RBGS = 0, 1
+
+
 class KcMgOpts(C.Structure):
     _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("coarsest_sweeps", C.c_int), ("max_levels", C.c_int),
                 ("tail", C.c_int), ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
@@ -72,6 +75,7 @@ class KcMgOpts(C.Structure):
 class KcChannel(C.Structure):
     _fields_ = [("phys", KcPhys),
                 ("precision", C.c_int), ("max_outer", C.c_int), ("use_graph", C.c_int), ("persistent", C.c_int),
+                ("momentum", C.c_int), ("pad_m", C.c_int),
                 ("mass_tol", C.c_double), ("eps", C.c_double), ("eps_inner", C.c_double), ("eps_inner_p", C.c_double)]
     _fields_ += [(k, C.c_void_p) for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid",
                                           "coef_u", "b_u", "coef_v", "b_v", "coef_p", "b_p",
@@ -121,6 +125,8 @@ SIGNATURES = {
     "kc_jacobi_ws_bytes": (S_, []),
     "kc_jacobi": (I_, [C.POINTER(KcSystem), P_, P_, P_, D_, I_, I_, I_, I_, P_, P_, S_, P_]),
     "kc_refined_ws_bytes": (S_, [L_, I_]),
+    "kc_rbgs_ws_bytes": (S_, [L_, I_]),
+    "kc_rbgs": (I_, [C.POINTER(KcSystem), P_, P_, P_, S_, C.POINTER(KcSolveOpts), C.POINTER(KcSolveInfo), P_]),
     "kc_bicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
                                  C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
     "kc_mg_default_opts": (None, [C.POINTER(KcMgOpts)]),

@@ -35,15 +35,30 @@ import torch
 from . import _lib as L
 from . import geometry
 from .config import ChannelConfig
-from .linalg import Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_refined, ptr, stream_handle
+from .linalg import (Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_refined, ptr, rbgs,
+                     stream_handle)
+
+
+# sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
+MOMENTUM_SWEEPS = 200
 
 
 class ChannelSolver:
     def __init__(self, cfg: ChannelConfig, device="cuda", precision="fp64", use_graph=True,
-                 eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4, native=True):
+                 eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4, native=True,
+                 momentum="bicgstab"):
+        """``momentum`` (mixed precision): "bicgstab", FP32 BiCGSTAB in FP64
+        refinement, or "rbgs", FP64 red-black Gauss-Seidel with the refined
+        BiCGSTAB as fallback (on GB300 an FP64 sweep is bound by the FP64
+        pipe, ~56 us at 2048 x 512, and 9-13 sweeps from the warm start cost
+        more than the refined BiCGSTAB); the FP64 path always uses the
+        reference's BiCGSTAB."""
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
+        if momentum not in ("rbgs", "bicgstab"):
+            raise ValueError("momentum must be 'rbgs' or 'bicgstab'")
         self.cfg, self.precision, self.use_graph = cfg, precision, use_graph
+        self.momentum = momentum if precision == "mixed" else "bicgstab"
         self.eps_inner, self.eps_inner_p = eps_inner, eps_inner_p
         self.learned = learned
         self.device = torch.device(device)
@@ -81,7 +96,7 @@ class ChannelSolver:
             if self.pcorr_precond == "mg":
                 self.mg = Multigrid(self.A_p32, **(mg_opts or {}))
         self.x0_p = None     # optional initial guess for p' (set by a learned predictor)
-        self.fallbacks = 0   # accelerated p' solves that fell back to plain BiCGSTAB
+        self.fallbacks = 0   # accelerated solves that fell back (p': plain BiCGSTAB; Gauss-Seidel momentum: refined BiCGSTAB)
         self.last_accel = None  # SolveInfo of the last accelerated p' solve
         ph = L.KcPhys()
         ph.nx, ph.ny, ph.mode = nx, ny, L.MODE_CHANNEL
@@ -132,8 +147,18 @@ class ChannelSolver:
                             persistent=self.persistent)
         # warm start from the previous outer iteration's u*, v* (karman_taichi.py:362-371 warm-starts too);
         # the stopping test is ||b - A x|| / ||b|| < eps, the reference's test for a cold start
-        return bicgstab_refined(A, A32, b, x, eps=cfg.eps, eps_inner=self.eps_inner, ws=ws,
+        before = 0
+        if self.momentum == "rbgs":
+            info = rbgs(A, b, x, eps=cfg.eps, max_iter=MOMENTUM_SWEEPS, warm=True, rel_to_b=True, ws=ws,
+                        use_graph=self.use_graph)
+            if info.ok:
+                return info
+            self.fallbacks += 1   # the refined BiCGSTAB takes over from where Gauss-Seidel stopped
+            before = info.iters
+        info = bicgstab_refined(A, A32, b, x, eps=cfg.eps, eps_inner=self.eps_inner, ws=ws,
                                 use_graph=self.use_graph, persistent=self.persistent, warm=True)
+        info.iters += before
+        return info
 
     def solve_momentum(self):
         iu = self._solve(self.A_u, getattr(self, "A_u32", None), self.b_u, self.u_mid, self.ws_u)
@@ -205,6 +230,7 @@ class ChannelSolver:
         c.phys = self.phys
         c.precision = L.F64 if self.precision == "fp64" else L.F32
         c.max_outer, c.use_graph, c.persistent = self.cfg.max_outer, int(self.use_graph), int(self.persistent)
+        c.momentum = L.MOMENTUM_RBGS if self.momentum == "rbgs" else L.MOMENTUM_BICGSTAB
         c.mass_tol, c.eps, c.eps_inner, c.eps_inner_p = self.cfg.mass_tol, self.cfg.eps, self.eps_inner, self.eps_inner_p
         for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid", "coef_u", "b_u", "coef_v", "b_v",
                   "coef_p", "b_p", "coef_u32", "b_u32", "coef_v32", "b_v32", "coef_p32", "b_p32", "mass", "pmax",
@@ -219,7 +245,7 @@ class ChannelSolver:
             elif k == "p":
                 sizes[k] = max(plain, lib.kc_pbicgstab_ws_bytes(A.n, A.stride))
             else:
-                sizes[k] = lib.kc_refined_ws_bytes(A.n, A.stride)
+                sizes[k] = max(lib.kc_refined_ws_bytes(A.n, A.stride), lib.kc_rbgs_ws_bytes(A.n, A.stride))
         for k, ws in (("u", self.ws_u), ("v", self.ws_v), ("p", self.ws_p)):
             buf = ws.get(sizes[k])
             setattr(c, "ws_" + k, buf.data_ptr())

@@ -36,6 +36,9 @@ kc_system sys_of(long long NX, long long NY, const void* coef, int dtype, int fo
     return A;
 }
 
+// sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
+constexpr long long kMomentumSweeps = 200;
+
 kc_solve_opts opts_of(double eps, long long max_iter, int rel_to, int check_every, int use_graph, int persistent) {
     kc_solve_opts o{};
     o.eps = eps;
@@ -52,16 +55,31 @@ kc_solve_opts opts_of(double eps, long long max_iter, int rel_to, int check_ever
     return o;
 }
 
-// One momentum / plain system solve as ChannelSolver._solve does it.
+// One momentum / plain system solve as ChannelSolver._solve does it; *fell_back
+// is set when the Gauss-Seidel solve missed eps and the refined BiCGSTAB took over.
 int solve_sys(const kc_channel* c, const kc_system& A64, const kc_system& A32, const double* b, double* x, void* ws,
-              size_t ws_bytes, kc_solve_info* info, cudaStream_t s) {
+              size_t ws_bytes, kc_solve_info* info, bool* fell_back, cudaStream_t s) {
+    *fell_back = false;
     if (c->precision == KC_F64) {
         const kc_solve_opts o = opts_of(c->eps, A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
         return kc_bicgstab(&A64, b, x, nullptr, ws, ws_bytes, &o, info, s);
     }
+    long long before = 0;
+    if (c->momentum == KC_MOMENTUM_RBGS) {
+        // red-black Gauss-Seidel from the previous outer iteration's u*, v*; the
+        // refined BiCGSTAB takes over, from where it stopped, if it misses eps
+        kc_solve_opts og = opts_of(c->eps, kMomentumSweeps, KC_REL_B, 0, c->use_graph, 0);
+        og.x0 = KC_X0_WARM;
+        const int rc = kc_rbgs(&A64, b, x, ws, ws_bytes, &og, info, s);
+        if (rc < 0 || info->status == KC_OK) return rc;
+        before = info->iters;
+        *fell_back = true;
+    }
     kc_solve_opts o = opts_of(c->eps, 50 * A64.n, KC_REL_R0, 0, c->use_graph, c->persistent);
     o.x0 = KC_X0_WARM;   // from the previous outer iteration's u*, v*
-    return kc_bicgstab_refined(&A64, &A32, b, x, ws, ws_bytes, &o, c->eps_inner, 30, info, s);
+    const int rc = kc_bicgstab_refined(&A64, &A32, b, x, ws, ws_bytes, &o, c->eps_inner, 30, info, s);
+    info->iters += before;
+    return rc;
 }
 
 }  // namespace
@@ -72,6 +90,8 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
     if (!c) return set_error("kc_channel_step: null channel"), KC_ERR_ARG;
     if (c->phys.mode != KC_MODE_CHANNEL) return set_error("kc_channel_step: phys.mode must be KC_MODE_CHANNEL"), KC_ERR_ARG;
     if (c->precision != KC_F64 && c->precision != KC_F32) return set_error("kc_channel_step: bad precision"), KC_ERR_ARG;
+    if (c->momentum != KC_MOMENTUM_BICGSTAB && c->momentum != KC_MOMENTUM_RBGS)
+        return set_error("kc_channel_step: bad momentum solver %d", c->momentum), KC_ERR_ARG;
     const bool mixed = c->precision == KC_F32;
     if (mixed && (!c->coef_u32 || !c->coef_v32 || !c->coef_p32 || !c->b_u32 || !c->b_v32 || !c->b_p32 || !c->mg_ws))
         return set_error("kc_channel_step: mixed precision needs the FP32 systems and a multigrid workspace"),
@@ -93,10 +113,12 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
                                   c->coef_u32, c->b_u32, c->coef_v32, c->b_v32, s);
         if (rc < 0) return rc;
         kc_solve_info iu{}, iv{}, ip{};
-        rc = solve_sys(c, Au, Au32, c->b_u, c->u_mid, c->ws_u, c->ws_u_bytes, &iu, s);
+        bool fu = false, fv = false;
+        rc = solve_sys(c, Au, Au32, c->b_u, c->u_mid, c->ws_u, c->ws_u_bytes, &iu, &fu, s);
         if (rc < 0) return rc;
-        rc = solve_sys(c, Av, Av32, c->b_v, c->v_mid, c->ws_v, c->ws_v_bytes, &iv, s);
+        rc = solve_sys(c, Av, Av32, c->b_v, c->v_mid, c->ws_v, c->ws_v_bytes, &iv, &fv, s);
         if (rc < 0) return rc;
+        S.fallbacks += (int)fu + (int)fv;
         rc = kc_relax_velocity(P, c->solid, c->u_mid, c->v_mid, c->u, c->v, nullptr, c->rws, s);
         if (rc < 0) return rc;
         rc = kc_outlet_conserve(P, c->u, s);

@@ -1832,10 +1832,11 @@ struct GraphKey {
     long long cs, es;
     int form = 0;
     unsigned long long ohash = 0;   // hash of the multigrid options (0: none)
+    const void* b = nullptr;        // a right-hand side the captured launches read (0: none)
     bool operator<(const GraphKey& o) const {
-        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es, form, ohash) <
+        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es, form, ohash, b) <
                std::tie(o.ws, o.coef, o.x, o.n, o.stride, o.dtype, o.pre, o.chunk, o.kind, o.cs, o.es, o.form,
-                        o.ohash);
+                        o.ohash, o.b);
     }
 };
 
@@ -2144,6 +2145,259 @@ int kc_bicgstab(const kc_system* A, const void* b, void* x, const void* M, void*
 int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
           kc_solve_info* info, void* stream) {
     return bicg_impl(A, b, x, nullptr, ws, ws_bytes, opts, info, stream, true);
+}
+
+}  // extern "C"
+
+// ---- red-black Gauss-Seidel (FP64) ------------------------------------------------------
+// A block owns a kGsTI x kGsTJ tile and stages x over the tile plus a 2-cell
+// halo (flat indices, as the stencil kernels: a link across the end of a row
+// reaches the next row's cell).  Phase 1 forms b - A x of the incoming x on
+// the owned cells (summed for the stopping test) and the new red values on
+// the owned cells and their 1-ring (from the staged black values); phase 2
+// updates the owned black cells from those red values.  Sweeps alternate
+// between the caller's x and a workspace copy (sweep k reads the copy of
+// parity k), so no block overwrites cells another block is still staging.
+// FP64 arithmetic runs at a small fraction of the FP32 rate on GB300: the
+// weights 1/d are formed once per solve, each update is one FMA.
+namespace kc {
+constexpr int kGsTI = 16, kGsAJ = 32, kGsRY = 8, kGsTJ = kGsAJ - 4, kGsNT = kGsAJ * kGsRY, kGsAI = kGsTI + 4;
+constexpr int kGsR1 = (kGsTI + 2 + kGsRY - 1) / kGsRY;   // rows of phase 1 per thread (owned + 1-ring)
+constexpr int kGsR2 = (kGsTI + kGsRY - 1) / kGsRY;       // rows of phase 2 per thread (owned)
+
+__device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0) : "memory");
+}
+
+__device__ __forceinline__ double gs_ax(const Coef<double>& A, int k, double xc, double xw, double xe, double xn,
+                                        double xs) {
+    double y = A.at(0, k) * xc;
+    if (A.lap) {
+        y = fma(A.at(1, k), xw - xc, y);
+        y = fma(A.at(2, k), xe - xc, y);
+        y = fma(A.at(3, k), xn - xc, y);
+        y = fma(A.at(4, k), xs - xc, y);
+    } else {
+        y = fma(A.at(1, k), xw, y);
+        y = fma(A.at(2, k), xe, y);
+        y = fma(A.at(3, k), xn, y);
+        y = fma(A.at(4, k), xs, y);
+    }
+    return y;
+}
+
+// weights 1/d (0 on rows with a zero diagonal) and (b, b)
+__global__ void __launch_bounds__(kPwThreads) k_rbgs_init(Coef<double> A, int n, const double* __restrict__ b,
+                                                          double* __restrict__ winv, BicgPtrs P, StartArgs sa) {
+    Acc<double> acc[1];
+    KC_PW_LOOP(n, {
+        double d = A.at(0, k);
+        if (A.lap) d = d - (((A.at(1, k) + A.at(2, k)) + A.at(3, k)) + A.at(4, k));
+        winv[k] = d != 0.0 ? 1.0 / d : 0.0;
+        const double bk = __ldg(b + k);
+        acc[0].add(bk, bk);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
+        SolverState* st = P.st;
+        st->hist = sa.hist;
+        st->hist_len = sa.hist_len;
+        st->iter = 0;
+        st->max_iter = sa.max_iter;
+        st->eps = sa.eps;
+        st->rel_to = sa.rel_to;
+        st->den = s[0];   // ||b||^2; replaced by ||b - A x0||^2 at the first sweep for KC_REL_R0
+        st->r0Tr = st->rTr = 0.0;
+        st->status = KC_MAXITER;
+        st->done = sa.max_iter <= 0 ? 1 : 0;
+        st->prev_rel = 1.0;
+        st->ticket[0] = 0;
+    }
+}
+
+__device__ __forceinline__ void gs_finish(SolverState* st, double rr) {
+    if (st->iter == 0) {
+        st->r0Tr = rr;
+        if (st->rel_to != KC_REL_B) st->den = rr;
+    }
+    record_history(st, st->iter, rr);
+    st->iter += 1;
+    st->rTr = rr;
+    const double rel = st->den > 0.0 ? sqrt(rr / st->den) : 0.0;
+    st->prev_rel = rel;
+    if (rel < st->eps) {
+        st->status = KC_OK;
+        st->done = 1;
+    } else if (!isfinite(rr)) {
+        st->status = KC_NONFINITE;
+        st->done = 1;
+    } else if (st->iter >= st->max_iter) {
+        st->status = KC_MAXITER;
+        st->done = 1;
+    }
+}
+
+__global__ void __launch_bounds__(kGsNT) k_rbgs_sweep(Coef<double> A, Geo g, const double* __restrict__ b,
+                                                      const double* __restrict__ winv, double* __restrict__ x0,
+                                                      double* __restrict__ x1, BicgPtrs P) {
+    SolverState* st = P.st;
+    if (solver_done(st)) return;
+    const bool odd = (__ldcg(&st->iter) & 1) != 0;   // set by the previous launch: the same in every block
+    const double* __restrict__ x = odd ? x1 : x0;
+    double* __restrict__ xo = odd ? x0 : x1;
+    __shared__ __align__(16) double sx[kGsAI][kGsAJ];
+    const int n = g.n, S = g.S;
+    const int i0 = blockIdx.y * kGsTI, j0 = blockIdx.x * kGsTJ;
+    const int tx = threadIdx.x & (kGsAJ - 1), ty = threadIdx.x / kGsAJ;
+    for (int a = ty; a < kGsAI; a += kGsRY) {
+        const long long kl = (long long)(i0 + a - 2) * S + (j0 + tx - 2);
+        const bool in = kl >= 0 && kl < n;
+        cp_async8(&sx[a][tx], x + (in ? kl : 0), in);
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    const int j = j0 + tx - 2;
+    const bool jown = tx >= 2 && tx < kGsTJ + 2 && j < S;
+    // phase 1: residual of the incoming x (owned cells), new red values (owned cells and 1-ring)
+    Acc<double> acc[1];
+    double xr[kGsR1];
+    bool wr[kGsR1];
+#pragma unroll
+    for (int m = 0; m < kGsR1; ++m) {
+        const int a = 1 + ty + kGsRY * m;
+        wr[m] = false;
+        xr[m] = 0.0;
+        if (a > kGsTI + 2 || tx < 1 || tx > kGsAJ - 2) continue;
+        const int i = i0 + a - 2;
+        const long long kl = (long long)i * S + j;
+        if (kl < 0 || kl >= n) continue;
+        // a staged position past the end of a row holds the flat cell kl of the next
+        // (previous) row; its neighbours are staged around it, so it is updated there
+        // too, with the colour of its own (row, column)
+        const int k = (int)kl;
+        const int colour = (j >= 0 && j < S) ? ((i + j) & 1) : (int)(((kl / S) + (kl % S)) & 1);
+        const double xc = sx[a][tx];
+        const double r = __ldg(b + k) - gs_ax(A, k, xc, sx[a - 1][tx], sx[a + 1][tx], sx[a][tx + 1], sx[a][tx - 1]);
+        if (jown && a >= 2 && a < kGsTI + 2) acc[0].add(r, r);
+        if (colour == 0) {
+            xr[m] = fma(__ldg(winv + k), r, xc);
+            wr[m] = true;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < kGsR1; ++m)
+        if (wr[m]) sx[1 + ty + kGsRY * m][tx] = xr[m];
+    __syncthreads();
+    // phase 2: black values of the owned cells from the new red ones; write the owned cells
+#pragma unroll
+    for (int m = 0; m < kGsR2; ++m) {
+        const int a = 2 + ty + kGsRY * m;
+        if (a >= kGsTI + 2 || !jown) continue;
+        const int i = i0 + a - 2;
+        const long long kl = (long long)i * S + j;
+        if (kl >= n) continue;
+        const int k = (int)kl;
+        double xc = sx[a][tx];
+        if (((i + j) & 1) != 0)
+            xc = fma(__ldg(winv + k), __ldg(b + k) - gs_ax(A, k, xc, sx[a - 1][tx], sx[a + 1][tx], sx[a][tx + 1],
+                                                          sx[a][tx - 1]),
+                     xc);
+        xo[k] = xc;
+    }
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) && threadIdx.x == 0) {
+        gs_finish(st, s[0]);
+        st->ticket[0] = 0;
+    }
+}
+
+static dim3 gs_grid(long long n, int S) {
+    const long long rows = (n + S - 1) / S;
+    return dim3((unsigned)((S + kGsTJ - 1) / kGsTJ), (unsigned)((rows + kGsTI - 1) / kGsTI));
+}
+
+struct GsLayout {
+    size_t off_state, off_partials, off_winv, off_x1, total;
+    int ld;
+};
+static GsLayout gs_layout(long long n, int S) {
+    GsLayout L{};
+    const dim3 g = gs_grid(n, std::max(S, 1));
+    const int nb = std::max<int>((int)(g.x * g.y), pw_blocks(n));
+    L.ld = (int)align256((size_t)nb * 8) / 8;
+    size_t off = 0;
+    L.off_state = off;
+    off = align256(off + sizeof(SolverState));
+    L.off_partials = off;
+    off = align256(off + (size_t)L.ld * sizeof(double));
+    L.off_winv = off;
+    off = align256(off + (size_t)n * sizeof(double));
+    L.off_x1 = off;
+    off = align256(off + (size_t)n * sizeof(double));
+    L.total = off;
+    return L;
+}
+}  // namespace kc
+
+extern "C" {
+
+size_t kc_rbgs_ws_bytes(long long n, int stride) {
+    if (n < 1 || stride < 1) return 0;
+    return gs_layout(n, stride).total;
+}
+
+int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_bytes, const kc_solve_opts* o,
+            kc_solve_info* info, void* stream) {
+    int rc = check_system(A);
+    if (rc) return rc;
+    if (A->dtype != KC_F64) return set_error("kc_rbgs: the system must be FP64"), KC_ERR_ARG;
+    if (!b || !x || !o) return set_error("kc_rbgs: null b, x or opts"), KC_ERR_ARG;
+    if (o->precond != KC_PRECOND_NONE) return set_error("kc_rbgs: no preconditioner applies"), KC_ERR_ARG;
+    const dim3 sg = gs_grid(A->n, A->stride);
+    if (sg.y > 65535u) return set_error("kc_rbgs: %lld rows of stride %d exceed the launch grid", A->n, A->stride),
+                              KC_ERR_ARG;
+    const GsLayout L = gs_layout(A->n, A->stride);
+    if (!ws || ws_bytes < L.total) return set_error("kc_rbgs: workspace %zu < %zu", ws_bytes, L.total), KC_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    char* base = (char*)ws;
+    BicgPtrs P{(SolverState*)(base + L.off_state), (double*)(base + L.off_partials), L.ld};
+    double* winv = (double*)(base + L.off_winv);
+    double* x1 = (double*)(base + L.off_x1);
+    const int pb = pw_blocks(A->n);
+    const Coef<double> C = coef_of<double>(A);
+    const Geo g{(int)A->n, A->stride};
+    KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
+    if (o->x0 != KC_X0_WARM) k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)A->n, x);
+    const StartArgs sa{o->eps, o->max_iter, 0, o->rel_to, o->history, o->history ? o->history_len : 0, 1e300};
+    k_rbgs_init<<<pb, kPwThreads, 0, s>>>(C, (int)A->n, b, winv, P, sa);
+    KC_LAUNCH_CHECK("k_rbgs_init");
+    count_launches(o->x0 != KC_X0_WARM ? 2 : 1);
+    GraphKey key{ws, A->coef, x, A->n, A->stride, KC_F64, 0, 16, 9, A->cs, A->es};
+    key.form = A->form;
+    key.b = b;
+    HostState h{};
+    rc = drive(o, key, P.st,
+               [&](int m, cudaStream_t ss) {
+                   for (int q = 0; q < m; ++q) k_rbgs_sweep<<<sg, kGsNT, 0, ss>>>(C, g, b, winv, x, x1, P);
+               },
+               &h, s, 1);
+    if (rc) return rc;
+    if (h.iter & 1) {   // an odd number of sweeps left the iterate in the copy
+        k_copy_f64<<<pb, kPwThreads, 0, s>>>((int)A->n, x1, x);
+        KC_LAUNCH_CHECK("kc_rbgs result");
+        count_launches(1);
+    }
+    if (info) {
+        info->status = h.status;
+        info->refinements = 0;
+        info->iters = h.iter;
+        info->rel_res = h.prev_rel;
+        info->r0 = sqrt(h.r0Tr);
+    }
+    return h.status;
 }
 
 }  // extern "C"

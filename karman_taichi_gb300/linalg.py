@@ -228,6 +228,29 @@ def cg(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=None,
     return SolveInfo(info.status, info.iters, info.rel_res, info.r0)
 
 
+def rbgs(A: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8, max_iter=200, warm=True, rel_to_b=True,
+         ws: Workspace | None = None, history: torch.Tensor | None = None, check_every=0,
+         use_graph=True) -> SolveInfo:
+    """Red-black Gauss-Seidel solve of an FP64 system until ||b - A x|| < eps
+    times ||b|| (``rel_to_b``) or ||b - A x0||; the Gauss-Seidel counterpart of
+    the reference's Jacobi solves (pressure_valid.py:192-233).  ``max_iter``
+    counts sweeps; ``warm`` starts from the given x."""
+    require_cuda(b, x)
+    if A.dtype != L.F64 or b.dtype != torch.float64 or x.dtype != torch.float64:
+        raise TypeError("rbgs solves FP64 systems")
+    if b.numel() != A.n or x.numel() != A.n:
+        raise ValueError(f"b/x have {b.numel()}/{x.numel()} elements, operator has {A.n}")
+    lib = L.load()
+    buf = (ws or Workspace(b.device)).get(lib.kc_rbgs_ws_bytes(A.n, A.stride))
+    o = _opts(eps, max_iter, L.X0_WARM if warm else L.X0_ZERO, L.PRECOND_NONE, 0,
+              L.REL_B if rel_to_b else L.REL_R0, check_every, use_graph, history, False)
+    info = L.KcSolveInfo()
+    rc = lib.kc_rbgs(C.byref(A.system), ptr(b), ptr(x), ptr(buf), buf.numel(), C.byref(o), C.byref(info),
+                     stream_handle(b.device))
+    L.check(rc, "kc_rbgs")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0)
+
+
 def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8,
                      eps_inner=1e-3, max_refine=30, max_iter=None, ws: Workspace | None = None,
                      use_graph=True, persistent=True, warm=False) -> SolveInfo:

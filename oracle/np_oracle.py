@@ -1204,3 +1204,36 @@ def jacobi_sweep(coef, b, x, S, omega=1.0, region=None):
     y = np.where(inside, (1.0 - omega) * x + omega * xm, x)
     d = np.abs(xm - x)[inside]
     return y, (float(d.max()) if d.size else 0.0)
+
+def rbgs_sweeps(coef, b, x, sweeps, S):
+    """Red-black Gauss-Seidel sweeps on the flat 5-point stencil (the
+    Gauss-Seidel counterpart of pressure_valid.py:192-233's Jacobi solves):
+    colour = parity of i + j of the [n/S][S] view; each sweep updates the red
+    cells from the previous black values, then the black cells from the new
+    red ones; rows with a zero diagonal keep their x.  coef: [5, n] standard
+    form, b, x: [n] (float64).  Returns x and the residual norms of the
+    iterate each sweep started from."""
+    coef = np.asarray(coef, dtype=np.float64).reshape(5, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    x = np.array(x, dtype=np.float64).reshape(-1)
+    n = b.size
+    k = np.arange(n)
+    red = ((k // S + k % S) % 2) == 0
+    d = coef[0]
+    winv = np.where(d != 0.0, 1.0 / np.where(d != 0.0, d, 1.0), 0.0)
+
+    def ax(x):   # links k -+ S (west, east) and k +- 1 (north, south); out of range: 0
+        xs = np.concatenate(([0.0] * S, x, [0.0] * S))
+        y = coef[0] * x + coef[1] * xs[0:n] + coef[2] * xs[2 * S:2 * S + n]
+        xf = np.concatenate(([0.0], x, [0.0]))
+        y = y + coef[3] * xf[2:n + 2] + coef[4] * xf[0:n]
+        return y
+
+    norms = []
+    for _ in range(sweeps):
+        r = b - ax(x)
+        norms.append(float(np.sqrt((r * r).sum())))
+        x = np.where(red, x + winv * r, x)
+        r = b - ax(x)
+        x = np.where(~red, x + winv * r, x)
+    return x, norms

@@ -37,18 +37,21 @@ def test_batched_instances_match_solo_runs(dev, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_native_step_matches_python_step(dev, precision):
-    """kc_channel_step makes the calls ChannelSolver's Python loop makes: same fields bit for bit."""
+@pytest.mark.parametrize("precision,momentum", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("mixed", "rbgs")])
+def test_native_step_matches_python_step(dev, precision, momentum):
+    """kc_channel_step makes the calls ChannelSolver's Python loop makes: same fields bit for bit
+    (momentum by the refined BiCGSTAB or by Gauss-Seidel)."""
     from karman_taichi_gb300.batch import batch_configs
     from karman_taichi_gb300.channel import ChannelSolver
     cfg = batch_configs(1, seed=5)[0].with_(max_outer=10)
-    a = ChannelSolver(cfg, device=dev, precision=precision, native=True)
-    b = ChannelSolver(cfg, device=dev, precision=precision, native=False)
+    a = ChannelSolver(cfg, device=dev, precision=precision, native=True, momentum=momentum)
+    b = ChannelSolver(cfg, device=dev, precision=precision, native=False, momentum=momentum)
     for _ in range(2):
         ra, rb = a.step(), b.step()
         assert ra[0]["outer"] == len(rb)
         assert ra[0]["it_p"] == sum(r["it_p"] for r in rb)
+        assert ra[0]["it_u"] == sum(r["it_u"] for r in rb)
+    assert a.fallbacks == b.fallbacks
     sa, sb = a.state_numpy(), b.state_numpy()
     for k in ("u", "v", "p", "u0", "v0"):
         assert np.array_equal(sa[k], sb[k]), k

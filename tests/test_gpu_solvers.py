@@ -264,3 +264,67 @@ def test_refined_mixed_precision(dev):
     r = b - O.to_csr(c, N) @ x.cpu().numpy()
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-9
     assert np.abs(x.cpu().numpy() - xs).max() <= 1e-6 * np.abs(xs).max()
+
+
+@pytest.mark.parametrize("sweeps", [1, 2, 3, 6])
+@pytest.mark.parametrize("n,S", [(7, 3), (1000, 33), (514 * 40 + 17, 514), (3000, 1)])
+def test_rbgs_sweeps_match_oracle(dev, n, S, sweeps):
+    """k red-black Gauss-Seidel sweeps equal the restatement's (FP64, to rounding):
+    odd and even sweep counts (the iterate alternates between x and a copy),
+    flat links across row ends, strips of one column."""
+    from karman_taichi_gb300 import linalg
+    c = _rand_system(n, S, 3, diag_shift=0.5)
+    b = np.random.default_rng(4).standard_normal(n)
+    x0 = np.random.default_rng(5).standard_normal(n)
+    x = _t(x0, dev)
+    info = linalg.rbgs(linalg.Stencil(_t(c, dev), stride=S), _t(b, dev), x, eps=1e-30, max_iter=sweeps, warm=True)
+    assert info.iters == sweeps and info.status == 1   # KC_MAXITER
+    ref, norms = O.rbgs_sweeps(c, b, x0, sweeps, S)
+    assert np.abs(x.cpu().numpy() - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    # the last residual checked is that of the iterate the last sweep started from
+    assert info.rel_res == pytest.approx(norms[-1] / np.linalg.norm(b), rel=1e-9)
+
+
+def test_rbgs_momentum_system_converges(dev):
+    """The channel's u-momentum system (diagonally dominant through the time
+    term): Gauss-Seidel reaches ||b - A x|| / ||b|| < 1e-10 from zero and agrees
+    with the FP64 BiCGSTAB solution; a warm start from that solution stops at
+    the first check."""
+    from karman_taichi_gb300 import linalg
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    s = ChannelSolver(get("channel_320x64"), device=dev, precision="mixed", native=False)
+    s.assemble_momentum()
+    x = _t(np.zeros(s.b_u.shape), dev)
+    info = linalg.rbgs(s.A_u, s.b_u, x, eps=1e-10, max_iter=500, warm=False)
+    assert info.ok and info.iters < 100, info
+    c = s.coef_u.cpu().numpy().reshape(5, -1)
+    S = s.coef_u.shape[2]
+    b = s.b_u.cpu().numpy().reshape(-1)
+    r = b - O.to_csr(c, S) @ x.cpu().numpy().reshape(-1)
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b)
+    xb = _t(np.zeros(s.b_u.shape), dev)
+    ib = linalg.bicgstab(s.A_u, s.b_u, xb, eps=1e-12)
+    assert ib.ok
+    xa, xr = x.cpu().numpy(), xb.cpu().numpy()
+    assert np.abs(xa - xr).max() <= 1e-8 * np.abs(xr).max()
+    warm = linalg.rbgs(s.A_u, s.b_u, xb, eps=1e-8, max_iter=500, warm=True)
+    assert warm.ok and warm.iters == 1
+
+
+def test_rbgs_rel_to_r0_and_bad_arguments(dev):
+    from karman_taichi_gb300 import linalg
+    c = _rand_system(400, 20, 6, diag_shift=0.5)
+    b = np.random.default_rng(7).standard_normal(400)
+    A = linalg.Stencil(_t(c, dev), stride=20)
+    x = _t(np.ones(400), dev)
+    info = linalg.rbgs(A, _t(b, dev), x, eps=1e-6, max_iter=500, warm=True, rel_to_b=False)
+    assert info.ok
+    r = b - O.to_csr(c, 20) @ x.cpu().numpy()
+    # stopped when the iterate the last sweep started from met the test; that sweep only lowered it
+    assert np.linalg.norm(r) < 1e-6 * info.r0
+    with pytest.raises(TypeError):
+        linalg.rbgs(linalg.Stencil(_t(c.astype(np.float32), dev), stride=20), _t(b.astype(np.float32), dev),
+                    _t(np.zeros(400, np.float32), dev))
+    with pytest.raises(ValueError):
+        linalg.rbgs(A, _t(b[:10], dev), _t(np.zeros(10), dev))
