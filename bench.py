@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes of the p' solve instead of tuning them before timing")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--spmv-sweep", action="store_true",
                     help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
@@ -161,7 +163,7 @@ def resolve_mode(mode, config="channel_2048x512"):
     """auto: the fastest accelerated configuration measured on GB300 -- mixed
     precision + multigrid CG (native step).  The learned initial guess is timed
     beside it (out["learned"]): with the exact-coarse multigrid the p' solve
-    needs ~36 CG iterations and the guess (~10% error) saves less than its
+    needs ~30 CG iterations and the guess (~10% error) saves less than its
     inference costs."""
     if mode != "auto":
         return mode
@@ -416,6 +418,12 @@ def run_gpu(args):
            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None}
 
     solver = make_solver(cfg, mode, dev)
+    tuned = None
+    if mode == "mixed" and not args.no_autotune:
+        # launch shapes of the p' solve (multigrid tail, tile sizes, CG chunk length), picked on
+        # this solver's state before anything is timed; the fields computed do not change
+        from karman_taichi_gb300.autotune import tune_pressure
+        tuned = tune_pressure(solver)
     ms, recs, launches, ck = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
     summ = summarize(recs)
     value = world * args.steps / (ms * 1e-3)
@@ -428,6 +436,8 @@ def run_gpu(args):
                        "parallelism": f"replicas x{world}",
                        "l2": "working set per step > 129 MB L2 (no flush needed)"},
                gpu_launches=launches, clocks=ck)
+    if tuned is not None:
+        out["config"]["autotune"] = {k: tuned[k] for k in ("tail", "big_cells", "check_every_p", "ms")}
     out["cell_updates_per_s"] = round(value * cfg.cells, 1)
     out["stats"] = summ
 
@@ -587,6 +597,10 @@ def run_batch(args):
            "steps": args.steps, "warmup": args.warmup}
     for key, workers, native in (("native_concurrent", args.batch_workers, True), ("sequential", 1, True)):
         b = BatchedChannels(cfgs, precision=mode, workers=workers)
+        if mode == "mixed" and not args.no_autotune:   # per grid size, before anything is timed
+            chosen = b.autotune()
+            out.setdefault("autotune", {k: {f: c[f] for f in ("tail", "big_cells", "check_every_p")}
+                                        for k, c in chosen.items()})
         run = b.step_native if native else b.step
         run(args.warmup)
         t = run(args.steps)

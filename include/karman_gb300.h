@@ -204,18 +204,22 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
  * coarsest_sweeps = 0: coarsening stops at <= 128 cells, whose dense
  * operator is inverted at setup (exact coarsest solve; a non-positive pivot
  * falls back to 64 Jacobi sweeps); > 0: coarsening stops at <= 1024 cells,
- * solved by that many Jacobi sweeps.  tail = 1 (with the fused cycle and the
- * exact coarsest solve) runs the levels of at most 1536 cells and the
- * coarsest solve in one single-block launch, their arithmetic unchanged;
- * 0 launches every level separately.  kc_mg_default_opts: nu 1/1, exact
- * coarsest solve, omega 1.1, alpha 1.8 (the tuned setting for the channel's
- * pressure correction), tail 1. */
+ * solved by that many Jacobi sweeps.  tail > 0 (with the fused cycle and the
+ * exact coarsest solve) runs the levels of at most `tail` cells and the
+ * coarsest solve in one single-block launch, their arithmetic unchanged,
+ * when their arrays fit the block's shared memory; 0 launches every level
+ * separately.  The fused cycle's levels below level 0 with at least
+ * big_cells cells use 16 x 60-cell tiles, smaller ones 8 x 28.  Neither
+ * changes the result.  kc_mg_default_opts: nu 1/1, exact coarsest solve,
+ * omega 1.1, alpha 1.8 (the tuned setting for the channel's pressure
+ * correction), tail 1536, big_cells 200000. */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */
     int coarsest_sweeps;          /* 0: exact coarsest solve; > 0: Jacobi sweeps            */
     int max_levels;
-    int tail;                     /* 1: the smallest levels in one single-block launch     */
+    int tail;                     /* levels of at most this many cells in one launch (0: off) */
+    int big_cells;                /* levels of at least this many cells use the large tiles */
     float omega[KC_MG_MAX_LEVELS];/* smoother weight per level                            */
     float alpha[KC_MG_MAX_LEVELS];/* coarse-correction scale per level                    */
 } kc_mg_opts;
@@ -423,7 +427,8 @@ typedef struct {
     kc_phys phys;                       /* mode must be KC_MODE_CHANNEL */
     int precision, max_outer, use_graph;
     int persistent;                     /* 1: BiCGSTAB solves as one cooperative launch, 0: graph chunks */
-    int momentum, pad_m;                /* KC_F32 momentum solver: KC_MOMENTUM_BICGSTAB or KC_MOMENTUM_RBGS */
+    int momentum;                       /* KC_F32 momentum solver: KC_MOMENTUM_BICGSTAB or KC_MOMENTUM_RBGS */
+    int check_every_p;                  /* KC_F32 p' solve: CG iterations per graph chunk between checks (0: 4) */
     double mass_tol, eps, eps_inner, eps_inner_p;
     double *u, *v, *p, *u0, *v0, *pcor, *u_mid, *v_mid;
     const unsigned char* solid;         /* [nx+2][ny+2], 1 = blocked cell */

@@ -69,13 +69,13 @@ MOMENTUM_BICGSTAB, MOMENTUM_RBGS = 0, 1
 
 class KcMgOpts(C.Structure):
     _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("coarsest_sweeps", C.c_int), ("max_levels", C.c_int),
-                ("tail", C.c_int), ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
+                ("tail", C.c_int), ("big_cells", C.c_int), ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
 
 
 class KcChannel(C.Structure):
     _fields_ = [("phys", KcPhys),
                 ("precision", C.c_int), ("max_outer", C.c_int), ("use_graph", C.c_int), ("persistent", C.c_int),
-                ("momentum", C.c_int), ("pad_m", C.c_int),
+                ("momentum", C.c_int), ("check_every_p", C.c_int),
                 ("mass_tol", C.c_double), ("eps", C.c_double), ("eps_inner", C.c_double), ("eps_inner_p", C.c_double)]
     _fields_ += [(k, C.c_void_p) for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid",
                                           "coef_u", "b_u", "coef_v", "b_v", "coef_p", "b_p",

@@ -1,0 +1,103 @@
+"""Launch-shape autotuner for the accelerated pressure-correction solve.
+
+The multigrid-preconditioned CG has three free choices that change its
+launches but not its arithmetic:
+
+* which coarse levels run in the one-block tail (``Multigrid.opts.tail``,
+  cells per level; 0 launches every level separately);
+* which levels below level 0 use the large 16 x 60-cell tiles instead of
+  8 x 28 (``Multigrid.opts.big_cells``);
+* how many CG iterations one captured graph chunk holds before the host reads
+  the solver state (``ChannelSolver.check_every_p``): fewer host round trips
+  against more launches of iterations that return at once once the solve has
+  converged.
+
+:func:`tune_pressure` times the solver's own p' solve under each candidate,
+one choice after the other (coordinate descent from the defaults), and keeps
+the fastest.  Every candidate computes the same fields bit for bit: the tail
+and the tile shapes do the same arithmetic per cell, and the convergence test
+runs on the device every iteration, whatever the chunk length.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from .linalg import TAIL_CELLS
+
+TAIL_CANDIDATES = (0, 384, TAIL_CELLS, 4352)
+BIG_CANDIDATES = (60000, 200000, 600000)
+CHUNK_CANDIDATES = (2, 4, 8)
+
+
+def _solve_ms(solver, reps: int) -> float:
+    """Best CUDA-event time of solver.solve_p() from p' = 0 (the first run of a
+    new launch shape also captures its graphs and is not timed)."""
+    dev = solver.device
+    best = math.inf
+    for k in range(reps + 1):
+        solver.pcor.zero_()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        solver.solve_p()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        if k > 0:
+            best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def _apply(solver, tail: int, big: int, chunk: int) -> None:
+    solver.mg.opts.tail = int(tail)
+    solver.mg.opts.big_cells = int(big)
+    solver.check_every_p = int(chunk)
+    solver._chan = None   # the native descriptor copies these: rebuild it
+
+
+def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDATES,
+                  chunks=CHUNK_CANDIDATES) -> dict:
+    """Pick the fastest launch shapes of ``solver``'s p' solve on its current
+    state and apply them.  Runs one outer iteration's stages up to the p'
+    assembly on the solver itself, then puts every field back, so the solver
+    continues exactly as if it had not been tuned.  Returns the choice and
+    the timings (ms per p' solve) behind it."""
+    if solver.mg is None:
+        raise ValueError("tuning needs the multigrid p' solve (precision='mixed', pcorr_precond='mg')")
+    names = ("u", "v", "p", "u0", "v0", "u_mid", "v_mid", "pcor")
+    saved = {k: getattr(solver, k).clone() for k in names}
+    fallbacks, history = solver.fallbacks, list(solver.history)
+    try:
+        solver.assemble_momentum()
+        solver.solve_momentum()
+        solver.relax()
+        solver.assemble_p()
+        choice = {"tail": int(solver.mg.opts.tail), "big_cells": int(solver.mg.opts.big_cells),
+                  "check_every_p": int(solver.check_every_p)}
+        timings = {}
+
+        def measure(c):
+            key = (c["tail"], c["big_cells"], c["check_every_p"])
+            if key not in timings:
+                _apply(solver, *key)
+                timings[key] = _solve_ms(solver, reps)
+            return timings[key]
+
+        for field, cands in (("tail", tails), ("big_cells", bigs), ("check_every_p", chunks)):
+            best_v, best_t = choice[field], measure(choice)
+            for v in cands:
+                t = measure(dict(choice, **{field: v}))
+                if t < best_t:
+                    best_v, best_t = v, t
+            choice[field] = best_v
+        _apply(solver, choice["tail"], choice["big_cells"], choice["check_every_p"])
+        result = dict(choice, ms=round(timings[(choice["tail"], choice["big_cells"], choice["check_every_p"])], 4),
+                      tried={f"tail={k[0]},big_cells={k[1]},check_every_p={k[2]}": round(t, 4)
+                             for k, t in timings.items()})
+    finally:
+        for k in names:
+            getattr(solver, k).copy_(saved[k])
+        solver.fallbacks, solver.history = fallbacks, history
+        torch.cuda.synchronize(solver.device)
+    return result

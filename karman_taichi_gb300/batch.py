@@ -79,6 +79,26 @@ class BatchedChannels:
                     self.records[k].append(self.solvers[k].step())
             self.streams[k].synchronize()
 
+    def autotune(self, reps=2):
+        """Pick the p' solve's launch shapes (multigrid tail, tile sizes, CG chunk
+        length; :mod:`karman_taichi_gb300.autotune`) once per grid size: tuned on
+        the first instance of each size, applied to every instance of that size.
+        The fields each instance computes do not change.  Returns
+        {"nx x ny": choice}."""
+        from .autotune import tune_pressure
+        chosen = {}
+        for k, s in enumerate(self.solvers):
+            key = f"{s.cfg.nx}x{s.cfg.ny}"
+            if key not in chosen:
+                with torch.cuda.stream(self.streams[k]):
+                    chosen[key] = tune_pressure(s, reps=reps)
+            c = chosen[key]
+            s.mg.opts.tail, s.mg.opts.big_cells = c["tail"], c["big_cells"]
+            s.check_every_p = c["check_every_p"]
+            s._chan = None
+        torch.cuda.synchronize(self.device)
+        return chosen
+
     def step_native(self, n_steps=1):
         """n_steps time steps of every instance by the library's native thread pool
         (kc_channel_batch_step); returns the wall time in seconds."""

@@ -108,6 +108,7 @@ class ChannelSolver:
         # Python loop below it is kept for the learned guess and for stage-by-stage use
         self.native = bool(native) and (precision == "fp64" or self.mg is not None)
         self.persistent = True   # BiCGSTAB solves as one cooperative launch (native step)
+        self.check_every_p = 4   # CG iterations per graph chunk between the host's convergence checks
         self._chan = None
         self.reset()
 
@@ -185,7 +186,8 @@ class ChannelSolver:
             self.mg.setup()
             # the pressure correction is symmetric: multigrid-preconditioned CG
             info = pcg_refined(self.A_p, self.A_p32, self.b_p, self.pcor, self.mg, eps=self.cfg.eps,
-                               eps_inner=self.eps_inner_p, x0=self.x0_p, ws=self.ws_p, use_graph=self.use_graph)
+                               eps_inner=self.eps_inner_p, x0=self.x0_p, ws=self.ws_p, use_graph=self.use_graph,
+                               check_every=self.check_every_p)
             self.last_accel = info
             if info.ok:
                 return info
@@ -231,6 +233,7 @@ class ChannelSolver:
         c.precision = L.F64 if self.precision == "fp64" else L.F32
         c.max_outer, c.use_graph, c.persistent = self.cfg.max_outer, int(self.use_graph), int(self.persistent)
         c.momentum = L.MOMENTUM_RBGS if self.momentum == "rbgs" else L.MOMENTUM_BICGSTAB
+        c.check_every_p = int(self.check_every_p)
         c.mass_tol, c.eps, c.eps_inner, c.eps_inner_p = self.cfg.mass_tol, self.cfg.eps, self.eps_inner, self.eps_inner_p
         for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid", "coef_u", "b_u", "coef_v", "b_v",
                   "coef_p", "b_p", "coef_u32", "b_u32", "coef_v32", "b_v32", "coef_p32", "b_p32", "mass", "pmax",

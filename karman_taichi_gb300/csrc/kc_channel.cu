@@ -129,7 +129,8 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
         if (mixed) {
             rc = kc_mg_setup(&Ap32, c->mg_ws, c->mg_ws_bytes, &c->mg_opts, s);
             if (rc < 0) return rc;
-            const kc_solve_opts o = opts_of(c->eps, 50 * Ap.n, KC_REL_B, 4, c->use_graph, 0);
+            const kc_solve_opts o =
+                opts_of(c->eps, 50 * Ap.n, KC_REL_B, c->check_every_p > 0 ? c->check_every_p : 4, c->use_graph, 0);
             rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, nullptr, c->mg_ws, &c->mg_opts, c->ws_p, c->ws_p_bytes,
                                 &o, c->eps_inner_p, 30, &ip, s);
             if (rc < 0) return rc;

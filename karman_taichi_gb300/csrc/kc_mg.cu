@@ -568,7 +568,9 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
 }
 
 // large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
-static inline bool mg_big(int NX, int NY) { return (long long)NX * NY >= 200000; }
+static inline bool mg_big(int NX, int NY, const kc_mg_opts* o) {
+    return (long long)NX * NY >= (o->big_cells > 0 ? o->big_cells : 200000);
+}
 
 // ---- host ----------------------------------------------------------------------------
 static int mg_levels(int NX, int NY, const kc_mg_opts* o, int* nx, int* ny) {
@@ -643,9 +645,9 @@ static bool mg_fusable(const MgLayout& M, const kc_mg_opts* o) {
 }
 
 static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, float* xout, float* bc, const int* done,
-                       cudaStream_t s) {
+                       const kc_mg_opts* o, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
-    if (l == 0 || mg_big(L.NX, L.NY))
+    if (l == 0 || mg_big(L.NX, L.NY, o))
         KC_CUDA(launch_chain(k_mg_down<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
                              dim3(kMgNT0), 0, s, G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done));
     else
@@ -656,9 +658,9 @@ static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, f
 }
 
 static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, const float* xc, float alpha,
-                     const float* b, float* xout, const int* done, cudaStream_t s) {
+                     const float* b, float* xout, const int* done, const kc_mg_opts* o, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
-    if (l == 0 || mg_big(L.NX, L.NY))
+    if (l == 0 || mg_big(L.NX, L.NY, o))
         KC_CUDA(launch_chain(k_mg_up<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
                              dim3(kMgNT0), 0, s, G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done));
     else
@@ -741,10 +743,10 @@ static unsigned tail_magic(int d) {
 // cycle, exact coarsest solve) and their arrays fit the block's shared memory.
 static TailPlan tail_plan(const MgLayout& M, const kc_mg_opts* o) {
     TailPlan P{};
-    if (!o->tail || o->coarsest_sweeps != 0 || !mg_fusable(M, o)) return P;
+    if (o->tail <= 0 || o->coarsest_sweeps != 0 || !mg_fusable(M, o)) return P;
     const int Lend = M.levels - 1;
     int Ls = 1;
-    while (Ls < Lend && (long long)M.nx[Ls] * M.ny[Ls] > kTailMax) ++Ls;
+    while (Ls < Lend && (long long)M.nx[Ls] * M.ny[Ls] > o->tail) ++Ls;
     if (Ls >= Lend) return P;
     size_t cells = 0;
     for (int l = Ls; l <= Lend; ++l) cells += (size_t)M.nx[l] * M.ny[l];
@@ -825,7 +827,7 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
         for (int l = 1; l < P.Ls; ++l) {
             const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
             rc = launch_down(M, L, l, (const float*)(base + M.off_b[l]), (float*)(base + M.off_x[l]),
-                             (float*)(base + M.off_b[l + 1]), done, s);
+                             (float*)(base + M.off_b[l + 1]), done, o, s);
             if (rc) return rc;
             ++nk;
         }
@@ -836,7 +838,7 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
             const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
             rc = launch_up(M, L, l, (const float*)(base + M.off_x[l]), mg_final(M, base, l + 1),
                            o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], (const float*)(base + M.off_b[l]),
-                           mg_final(M, base, l), done, s);
+                           mg_final(M, base, l), done, o, s);
             if (rc) return rc;
             ++nk;
         }
@@ -846,7 +848,7 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
     for (int l = 1; l + 1 < M.levels; ++l) {
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
         rc = launch_down(M, L, l, (const float*)(base + M.off_b[l]), (float*)(base + M.off_x[l]),
-                         (float*)(base + M.off_b[l + 1]), done, s);
+                         (float*)(base + M.off_b[l + 1]), done, o, s);
         if (rc) return rc;
         ++nk;
     }
@@ -863,7 +865,7 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
         rc = launch_up(M, L, l, (const float*)(base + M.off_x[l]), mg_final(M, base, l + 1),
                        o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], (const float*)(base + M.off_b[l]),
-                       mg_final(M, base, l), done, s);
+                       mg_final(M, base, l), done, o, s);
         if (rc) return rc;
         ++nk;
     }
@@ -881,12 +883,12 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
     char* base = (char*)ws;
     if (mg_fusable(M, o)) {
         const Lvl L0 = level_of(M, base, 0, (const float*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
-        int rc = launch_down(M, L0, 0, r, (float*)(base + M.off_x[0]), (float*)(base + M.off_b[1]), done, s);
+        int rc = launch_down(M, L0, 0, r, (float*)(base + M.off_x[0]), (float*)(base + M.off_b[1]), done, o, s);
         if (rc) return rc;
         int kc = 0;
         rc = mg_enqueue_coarse(A, ws, o, done, s, &kc);
         if (rc) return rc;
-        rc = launch_up(M, L0, 0, (const float*)(base + M.off_x[0]), mg_final(M, base, 1), o->alpha[0], r, z, done, s);
+        rc = launch_up(M, L0, 0, (const float*)(base + M.off_x[0]), mg_final(M, base, 1), o->alpha[0], r, z, done, o, s);
         if (rc) return rc;
         if (kernels) *kernels = kc + 2;
         return KC_OK;
@@ -958,7 +960,8 @@ void kc_mg_default_opts(kc_mg_opts* o) {
     o->nu_post = 1;
     o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
-    o->tail = 1;               // the levels of at most 1536 cells in one single-block launch
+    o->tail = kTailMax;        // the levels of at most 1536 cells in one single-block launch
+    o->big_cells = 200000;     // levels of 200k cells and more in 16 x 60 tiles
     for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
         o->omega[l] = 1.1f;
         o->alpha[l] = 1.8f;

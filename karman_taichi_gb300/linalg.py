@@ -273,22 +273,28 @@ def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tenso
     return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)
 
 
+TAIL_CELLS = 1536   # default: levels of at most this many cells run in the multigrid tail block
+
+
 class Multigrid:
     """Aggregation multigrid V-cycle (FP32) for a 2-D 5-point operator; the
     preconditioner of the mixed-precision pressure-correction solve.
     ``omega`` / ``alpha`` are per-level smoother weights and coarse-correction
     scales (scalars broadcast to all levels); ``coarsest_sweeps=0`` solves the
-    coarsest level (<= 128 cells) exactly.  ``tail=True`` runs the levels of at
-    most 1536 cells in one single-block launch (same arithmetic)."""
+    coarsest level (<= 128 cells) exactly.  ``tail`` runs the levels of at
+    most that many cells (True: 1536) in one single-block launch, ``big_cells``
+    picks the large tiles for the levels of at least that many cells; neither
+    changes the result (the launch shapes the autotuner chooses between)."""
 
     def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.1, alpha=1.8,
-                 max_levels=16, tail=True):
+                 max_levels=16, tail=True, big_cells=200000):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")
         self.A = A32
         o = L.KcMgOpts()
         o.nu_pre, o.nu_post, o.coarsest_sweeps, o.max_levels = nu_pre, nu_post, coarsest_sweeps, max_levels
-        o.tail = int(bool(tail))
+        o.tail = TAIL_CELLS if tail is True else int(tail)
+        o.big_cells = int(big_cells)
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
         al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
         for l in range(16):

@@ -276,3 +276,29 @@ def test_graph_cache_tells_forms_apart(dev):
     assert second.ok, second
     res = b.reshape(-1) - O.spmv(coef.reshape(5, -1), x.cpu().numpy().reshape(-1), NY)
     assert np.linalg.norm(res) / np.linalg.norm(b) < 1e-8
+
+
+def test_autotune_keeps_fields_and_state(dev):
+    """The autotuner picks launch shapes from its candidates, leaves the solver's
+    state as it found it, and the tuned solver steps to the same fields bit for bit."""
+    import numpy as np
+    from karman_taichi_gb300.autotune import BIG_CANDIDATES, CHUNK_CANDIDATES, TAIL_CANDIDATES, tune_pressure
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    cfg = get("channel_320x64")
+    a = ChannelSolver(cfg, device=dev, precision="mixed")
+    b = ChannelSolver(cfg, device=dev, precision="mixed")
+    a.step(); b.step()
+    before = a.state_numpy()
+    c = tune_pressure(a, reps=1)
+    assert c["tail"] in TAIL_CANDIDATES and c["big_cells"] in BIG_CANDIDATES
+    assert c["check_every_p"] in CHUNK_CANDIDATES and c["ms"] > 0 and len(c["tried"]) >= 3
+    after = a.state_numpy()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    for _ in range(2):
+        ra, rb = a.step(), b.step()
+        assert ra[0]["it_p"] == rb[0]["it_p"]
+    sa, sb = a.state_numpy(), b.state_numpy()
+    for k in ("u", "v", "p"):
+        assert np.array_equal(sa[k], sb[k]), k
