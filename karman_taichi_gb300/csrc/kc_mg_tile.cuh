@@ -47,6 +47,12 @@ __device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool v
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0)
                  : "memory");
 }
+// two consecutive floats at once (both addresses 8-byte aligned), zero-filled when !valid
+__device__ __forceinline__ void cp_async8f(float* smem, const float* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 // wait until at most N of this thread's most recent commit groups are pending
@@ -109,6 +115,23 @@ __device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, fl
         const int u = a * T::AJ + b;
 #pragma unroll
         for (int q = 0; q < 5; ++q) cp_async4(sc + q * T::A + u, g + q * L.cs, in);
+    }
+}
+
+// As mg_stage_coef with the halo H = 2, two columns per copy.  Needs an even
+// row length NY and an even tile origin j0: then a pair (j, j + 1) with j
+// even starts on an 8-byte boundary and lies wholly inside or outside the grid.
+template <int TI, class T>
+__device__ __forceinline__ void mg_stage_coef_pairs(const MgLvl& L, int i0, int j0, float* sc) {
+    constexpr int PJ = T::AJ / 2;
+    for (int e = threadIdx.x; e < T::AI * PJ; e += T::NT) {
+        const int a = e / PJ, b = 2 * (e - a * PJ);
+        const int i = i0 + a - 2, j = j0 + b - 2;
+        const bool in = i >= 0 && i < L.NX && j >= 0 && j < L.NY;
+        const float* g = in ? L.c + (long long)(i * L.NY + j) * L.es : L.c;
+        const int u = a * T::AJ + b;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) cp_async8f(sc + q * T::A + u, g + q * L.cs, in);
     }
 }
 

@@ -1558,11 +1558,28 @@ struct PcOwnR {
 };
 
 // DOWN_0 staging: r (sb), w (sq), s_old (ss), W, coefficients over the 2-cell-halo region
+// (pairs: the row length is even, so 8-byte copies move two cells; see mg_stage_coef_pairs)
 template <int TI, int AJ, int RY>
 __device__ __forceinline__ void pcc_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ r,
                                                const float* __restrict__ w, const float* __restrict__ s_old,
-                                               bool update, bool first, MgStage S) {
+                                               bool update, bool first, bool pairs, MgStage S) {
     using T = MgTile<TI, AJ, RY>;
+    if (pairs && L.es == 1) {
+        constexpr int PJ = AJ / 2;
+        for (int e = threadIdx.x; e < T::AI * PJ; e += T::NT) {
+            const int a = e / PJ, b = 2 * (e - a * PJ);
+            const int i = i0 + a - 2, j = j0 + b - 2;
+            const bool in = i >= 0 && i < L.NX && j >= 0 && j < L.NY;
+            const int k = in ? i * L.NY + j : 0;
+            const int u = a * T::AJ + b;
+            cp_async8f(S.sb + u, r + k, in);
+            if (update) cp_async8f(S.sq + u, w + k, in);
+            if (update && !first) cp_async8f(S.ss + u, s_old + k, in);
+            cp_async8f(S.sw + u, L.winv + k, in);
+        }
+        mg_stage_coef_pairs<TI, T>(L, i0, j0, S.sc);
+        return;
+    }
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
@@ -1607,18 +1624,25 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcc_down0(MgLvl L, float* __rest
     const float alpha = up ? __ldcg(&st->alpha_f) : 0.f, beta = up ? __ldcg(&st->beta_f) : 0.f;
     const PcMidCG<TI, TJ, NT> mid{V.x, V.p[0], V.z, __ldcg(&st->alpha), beta, L.NX, L.NY, up, first};
     const PcOwnR own{cur ? V.r[0] : V.r[1], up};
+    // 8-byte staging copies: even row length and tile width, 8-byte aligned planes
+    const bool pairs = (L.NY % 2 == 0) && (TJ % 2 == 0) && (L.cs % 2 == 0) &&
+                       ((reinterpret_cast<unsigned long long>(L.c) | reinterpret_cast<unsigned long long>(L.winv) |
+                         reinterpret_cast<unsigned long long>(r) | reinterpret_cast<unsigned long long>(V.q) |
+                         reinterpret_cast<unsigned long long>(s_old)) % 8 == 0);
     auto stage = [&](int sidx) {
         float* b = dsm + sidx * SA;
         return MgStage{b, b + T::A, b + 3 * T::A, b + 4 * T::A, dsm + 2 * SA, nullptr, b + 2 * T::A};
     };
     Acc<float> acc[1];
     int t = blockIdx.x, sidx = 0;
-    if (t < g.ntiles) pcc_down_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, V.q, s_old, up, first, stage(0));
+    if (t < g.ntiles)
+        pcc_down_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, V.q, s_old, up, first, pairs, stage(0));
     cp_async_commit();
     for (; t < g.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
         if (tn < g.ntiles)
-            pcc_down_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, V.q, s_old, up, first, stage(sidx ^ 1));
+            pcc_down_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, V.q, s_old, up, first, pairs,
+                                       stage(sidx ^ 1));
         cp_async_commit();
         const int i0 = pcf_i0(g, t, TI), j0 = pcf_j0(g, t, TJ);
         mid(i0, j0);
