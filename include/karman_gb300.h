@@ -211,8 +211,9 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
  * separately.  The fused cycle's levels below level 0 with at least
  * big_cells cells use 16 x 60-cell tiles, smaller ones 8 x 28.  Neither
  * changes the result.  kc_mg_default_opts: nu 1/1, exact coarsest solve,
- * omega 1.1, alpha 1.8 (the tuned setting for the channel's pressure
- * correction), tail 1536, big_cells 200000. */
+ * omega 1.0 on level 0 and 1.1 below, alpha 1.9 on level 0 and 2.0 below
+ * (the tuned setting for the channel's pressure correction), tail 1536,
+ * big_cells 200000. */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */

@@ -286,7 +286,7 @@ class Multigrid:
     picks the large tiles for the levels of at least that many cells; neither
     changes the result (the launch shapes the autotuner chooses between)."""
 
-    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.1, alpha=1.8,
+    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.1), alpha=(1.9, 2.0),
                  max_levels=16, tail=True, big_cells=200000):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")

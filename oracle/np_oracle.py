@@ -952,8 +952,8 @@ class MultigridOracle:
     COARSEST = 1024          # coarsest level of the Jacobi variant (cells)
     COARSEST_DIRECT = 128    # coarsest level of the direct variant (coarsest_sweeps = 0)
 
-    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=1.1, alpha=1.8, max_levels=16,
-                 lap=False):
+    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.1), alpha=(1.9, 2.0),
+                 max_levels=16, lap=False):
         f32 = np.float32
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
         al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
