@@ -481,6 +481,10 @@ int kc_post_process(int nx, int ny, double dx, double dy, const double* u, const
 /* ---- utilities ------------------------------------------------------------ */
 /* dst = src (device to device), e.g. time_forward (karman_taichi.py:617-622). */
 int kc_copy(void* dst, const void* src, size_t bytes, void* stream);
+/* dst[k] = (float)src[k], k < n (device FP64 -> device FP32), rounded to nearest, ties to even:
+ * the conversion every FP32 copy of an FP64 system in this library uses (the mixed-precision
+ * coefficient planes, right-hand sides and refinement residuals). */
+int kc_to_f32(const double* src, float* dst, long long n, void* stream);
 
 #ifdef __cplusplus
 }

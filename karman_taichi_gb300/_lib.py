@@ -153,6 +153,7 @@ SIGNATURES = {
     "kc_karman_puv_correction": (I_, [C.POINTER(KcKarman)] + [P_] * 10),
     "kc_karman_correct_conserv": (I_, [C.POINTER(KcKarman), P_, P_, P_, P_]),
     "kc_copy": (I_, [P_, P_, S_, P_]),
+    "kc_to_f32": (I_, [P_, P_, L_, P_]),
     "kc_unet_conv3x3": (I_, [P_, I_, I_, I_, P_, L_, P_, I_, I_, P_, P_, I_, P_]),
     "kc_unet_conv3x3_wgrad": (I_, [P_, P_, I_, I_, I_, I_, P_, P_, P_]),
     "kc_unet_flip_weights": (I_, [P_, I_, I_, I_, P_, P_]),

@@ -1,6 +1,7 @@
 // Library-level entry points of libkarman_gb300: version, status strings,
-// thread-local error text and device-to-device copies.
+// thread-local error text, device-to-device copies and FP64 -> FP32 copies.
 #include "kc_common.cuh"
+#include <algorithm>
 #include <string>
 #include <stdarg.h>
 #include <stdio.h>
@@ -101,6 +102,25 @@ int kc_copy(void* dst, const void* src, size_t bytes, void* stream) {
     return KC_OK;
 }
 
+}  // extern "C"
+
+namespace kc {
+__global__ void __launch_bounds__(256) k_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+    for (long long k = blockIdx.x * 256ll + threadIdx.x; k < n; k += (long long)gridDim.x * 256)
+        dst[k] = f64_to_f32(src[k]);
+}
+}  // namespace kc
+
+extern "C" {
+
+int kc_to_f32(const double* src, float* dst, long long n, void* stream) {
+    if (n < 0 || (n > 0 && (!src || !dst))) return kc::set_error("kc_to_f32: bad arguments"), KC_ERR_ARG;
+    if (n == 0) return KC_OK;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152ll * 8);
+    kc::k_to_f32<<<(unsigned)blocks, 256, 0, kc::as_stream(stream)>>>(src, dst, n);
+    KC_LAUNCH_CHECK("k_to_f32");
+    return KC_OK;
+}
 
 // sizeof of the ABI structs, for bindings that mirror them (ctypes, cgo, ...)
 size_t kc_struct_size(const char* name) {

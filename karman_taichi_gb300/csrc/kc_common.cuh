@@ -71,6 +71,27 @@ inline cudaError_t launch_chain(void (*kernel)(KArgs...), dim3 grid, dim3 block,
 const void* readback(const void* src, size_t bytes, cudaStream_t s);
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// binary64 -> binary32 with IEEE 754 round to nearest, ties to even, in
+// integer arithmetic: on GB300 the FP64 pipe issues a few operations per SM
+// per clock and the conversion instruction occupies it, while the integer
+// pipes are idle in the FP64 stage kernels.  Results in the normal binary32
+// range (biased binary64 exponent 897..1150) keep the top 23 fraction bits
+// and round on the 29 dropped ones; a carry out of the fraction steps the
+// exponent (up to infinity above the largest finite value, as RN does).
+// Zeros, subnormal results, overflow, infinities and NaN take the hardware
+// conversion.  Bit-identical to (float)x for every input.
+__device__ __forceinline__ float f64_to_f32(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32);
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    if (e - 897u > 1150u - 897u) return (float)x;
+    const unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+    unsigned r = ((e - 896u) << 23) | (unsigned)(m >> 29);
+    const unsigned rem = (unsigned)(m & 0x1FFFFFFFull), half = 0x10000000u;
+    r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;
+    return __uint_as_float(r | (hi & 0x80000000u));
+}
+
 // ---- warp / block reductions (fixed order => bitwise reproducible) --------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

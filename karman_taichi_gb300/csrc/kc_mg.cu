@@ -205,19 +205,21 @@ __global__ void k_mg_prolong(Lvl F, float* __restrict__ x, const float* __restri
 // A non-positive or non-finite pivot sets the flag and the cycle falls back
 // to kCoarseFallbackSweeps Jacobi sweeps.
 // The block is 32 x 32 threads; thread (ty, tx) keeps the entries of rows
-// ty + 32a and columns tx + 32c in registers (kGjR x kGjR of them), so a
+// ty + 32a and columns tx + 32c in registers (R x R of them, R = ceil(n / 32)
+// chosen at launch), so a
 // pivot step is one barrier and a few FMAs per entry: the pivot row and
 // column go through shared memory, double-buffered so that step p + 1 may
 // write while slow readers still read step p's copy.
 constexpr int kGjR = kCoarseDirectMax / 32;
 
+template <int R>
 __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __restrict__ inv, int* __restrict__ flag) {
     __shared__ float rowp[2][kCoarseDirectMax], colp[2][kCoarseDirectMax];
     const int n = L.NX * L.NY, NY = L.NY;
     const int tx = threadIdx.x, ty = threadIdx.y;
-    float a[kGjR][kGjR];
+    float a[R][R];
 #pragma unroll
-    for (int r = 0; r < kGjR; ++r) {
+    for (int r = 0; r < R; ++r) {
         const int i = ty + 32 * r;
         float d = 0.f, w = 0.f, ea = 0.f, no = 0.f, so = 0.f;
         if (i < n) {
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __rest
         }
         const int jr = i % NY;
 #pragma unroll
-        for (int c = 0; c < kGjR; ++c) {
+        for (int c = 0; c < R; ++c) {
             const int j = tx + 32 * c;
             float v = 0.f;
             if (i < n && j < n) {
@@ -251,18 +253,18 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __rest
         // the owners publish row p and column p as they stand before the step
         if (ty == pl) {
 #pragma unroll
-            for (int r = 0; r < kGjR; ++r)
+            for (int r = 0; r < R; ++r)
                 if (r == pr) {
 #pragma unroll
-                    for (int c = 0; c < kGjR; ++c) rowp[buf][tx + 32 * c] = a[r][c];
+                    for (int c = 0; c < R; ++c) rowp[buf][tx + 32 * c] = a[r][c];
                 }
         }
         if (tx == pl) {
 #pragma unroll
-            for (int c = 0; c < kGjR; ++c)
+            for (int c = 0; c < R; ++c)
                 if (c == pr) {
 #pragma unroll
-                    for (int r = 0; r < kGjR; ++r) colp[buf][ty + 32 * r] = a[r][c];
+                    for (int r = 0; r < R; ++r) colp[buf][ty + 32 * r] = a[r][c];
                 }
         }
         __syncthreads();
@@ -273,11 +275,11 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __rest
         }
         const float ip = 1.f / piv;
 #pragma unroll
-        for (int r = 0; r < kGjR; ++r) {
+        for (int r = 0; r < R; ++r) {
             const int i = ty + 32 * r;
             const float ci = colp[buf][i];
 #pragma unroll
-            for (int c = 0; c < kGjR; ++c) {
+            for (int c = 0; c < R; ++c) {
                 const int j = tx + 32 * c;
                 const float sp = j == p ? ip : rowp[buf][j] * ip;   // the scaled pivot row
                 a[r][c] = i == p ? sp : (j == p ? -ci * ip : fmaf(-ci, sp, a[r][c]));
@@ -285,9 +287,9 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_inverse(Lvl L, float* __rest
         }
     }
 #pragma unroll
-    for (int r = 0; r < kGjR; ++r)
+    for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int c = 0; c < kGjR; ++c) {
+        for (int c = 0; c < R; ++c) {
             const int i = ty + 32 * r, j = tx + 32 * c;
             if (i < n && j < n) inv[i * n + j] = a[r][c];
         }
@@ -701,7 +703,16 @@ int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o,
         const int nc = M.nx[l] * M.ny[l];
         const Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
         if (nc > kCoarseDirectMax) return set_error("kc_mg_setup: coarsest level of %d cells", nc), KC_ERR_ARG;
-        k_mg_coarse_inverse<<<1, dim3(32, 32), 0, s>>>(L, (float*)(base + M.off_inv), (int*)(base + M.off_flag));
+        float* inv = (float*)(base + M.off_inv);
+        int* flag = (int*)(base + M.off_flag);
+        static_assert(kGjR == 4, "register tiles of 1..4 rows per thread cover the coarsest level");
+        switch ((nc + 31) / 32) {   // the smallest tile that covers the level: a pivot step costs R x R per thread
+            case 0:
+            case 1: k_mg_coarse_inverse<1><<<1, dim3(32, 32), 0, s>>>(L, inv, flag); break;
+            case 2: k_mg_coarse_inverse<2><<<1, dim3(32, 32), 0, s>>>(L, inv, flag); break;
+            case 3: k_mg_coarse_inverse<3><<<1, dim3(32, 32), 0, s>>>(L, inv, flag); break;
+            default: k_mg_coarse_inverse<4><<<1, dim3(32, 32), 0, s>>>(L, inv, flag); break;
+        }
         KC_LAUNCH_CHECK("k_mg_coarse_inverse");
     }
     return KC_OK;

@@ -800,28 +800,31 @@ __global__ void __launch_bounds__(kPwThreads) k_cg_2(int n, T* __restrict__ x, B
 // =============================================================================
 // Mixed precision refinement helpers
 // =============================================================================
+// r = b - A x in FP64, its FP32 copy, ||r||^2 and (with_b) ||b||^2: b does not
+// change across the sweeps of one refinement, so only the first sums it.
 struct PolResid {
     static constexpr bool kAux = false;
     const double* __restrict__ x;
     const double* __restrict__ b;
     float* __restrict__ r32;
+    int with_b;
     __device__ __forceinline__ double pre(int k) const { return __ldg(x + k); }
     __device__ __forceinline__ double scale(int, double p) const { return p; }
     __device__ __forceinline__ void own(int, double) const {}
     __device__ __forceinline__ void sink(int k, double y, double, Acc<double> (&acc)[2]) const {
         const double bk = __ldg(b + k);
         const double rk = bk - y;
-        r32[k] = (float)rk;
+        r32[k] = f64_to_f32(rk);
         acc[0].add(rk, rk);
-        acc[1].add(bk, bk);
+        if (with_b) acc[1].add(bk, bk);
     }
 };
 
 __global__ void __launch_bounds__(kThreads)
     k_refine_resid(Coef<double> A, Geo g, const double* __restrict__ b, const double* __restrict__ x,
-                   float* __restrict__ r32, BicgPtrs P, double* out2) {
+                   float* __restrict__ r32, BicgPtrs P, double* out2, int with_b) {
     Acc<double> acc[2];
-    PolResid pol{x, b, r32};
+    PolResid pol{x, b, r32, with_b};
     stencil_tile<double, 2>(pol, A, g.n, g.S, acc);
     double s[2];
     if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &P.st->ticket[0], s) &&
@@ -2556,7 +2559,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
     double rel = 1.0, bb = 0.0, best = INFINITY;
     bool applied = false;
     for (int it = 0; it <= max_refine; ++it) {
-        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2);
+        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, it == 0);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[3];
         {
@@ -2564,7 +2567,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
             if (!hp) return KC_ERR_CUDA;
             memcpy(h2, hp, sizeof(h2));
         }
-        bb = h2[1];
+        if (it == 0) bb = h2[1];
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
         memcpy(&skipped, &h2[2], sizeof(int));
@@ -2780,7 +2783,7 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     key.form = A32->form;
     key.ohash = bytes_hash(mg_opts, sizeof(kc_mg_opts));
     for (int it = 0; it <= max_refine; ++it) {
-        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2);
+        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2, it == 0);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[3];
         {
@@ -2788,7 +2791,7 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
             if (!hp) return KC_ERR_CUDA;
             memcpy(h2, hp, sizeof(h2));
         }
-        bb = h2[1];
+        if (it == 0) bb = h2[1];
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
         memcpy(&skipped, &h2[2], sizeof(int));

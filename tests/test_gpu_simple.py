@@ -2,9 +2,10 @@
 CPU oracle (through the C ABI).
 
 Tolerances: assembly kernels are compiled without FMA contraction and follow
-the reference's operation order, so coefficients agree to <= 1e-14
-relative; fields after whole SIMPLE steps agree within 1e-6 relative (the
-FP64 tolerance), since only the solvers' summation order differs.
+the reference's operation order (the momentum rows' central part in an
+algebraically reduced form), so coefficients agree to <= 1e-14 relative;
+fields after whole SIMPLE steps agree within 1e-6 relative (the FP64
+tolerance), since only the solvers' summation order differs.
 """
 import numpy as np
 import pytest
@@ -62,6 +63,48 @@ def test_momentum_assembly_matches_oracle(dev):
     assert _rel(g.b_u.cpu().numpy(), orc.b_u) <= 1e-14
     assert _rel(g.coef_v.cpu().numpy(), orc.coef_v) <= 1e-14
     assert _rel(g.b_v.cpu().numpy(), orc.b_v) <= 1e-14
+
+
+def test_fp32_copies_round_to_nearest_even(dev):
+    """kc_to_f32 and the FP32 planes of the mixed-precision systems are the IEEE
+    round-to-nearest-even binary32 values of their FP64 sources, bit for bit:
+    random magnitudes over the whole binary32 range and beyond, exact ties,
+    the neighbours of ties, carries into the exponent, zeros, subnormal
+    results, overflow, infinities and NaN."""
+    import torch
+    from karman_taichi_gb300 import _lib as L
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.linalg import ptr, stream_handle
+    lib = L.load()
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal(4000).astype(np.float32)
+    lo, hi = f.astype(np.float64), np.nextafter(f, np.float32(np.inf)).astype(np.float64)
+    ties = (lo + hi) / 2   # exact in binary64: halfway between neighbouring binary32 values
+    top = np.float64(np.finfo(np.float32).max)
+    special = [0.0, -0.0, 1e-320, -1e-310, 2.0 ** -149, 2.0 ** -150, 3 * 2.0 ** -151, 1.1754943508222875e-38,
+               1.1754942e-38, 1 - 2.0 ** -30, 1 - 2.0 ** -25, 2 - 2.0 ** -24, top, top * (1 + 2.0 ** -25),
+               top * (1 + 2.0 ** -23), -top * (1 + 2.0 ** -24), 1e39, np.inf, -np.inf, np.nan]
+    vals = np.concatenate([rng.standard_normal(40000) * 10.0 ** rng.integers(-50, 50, 40000), lo, ties,
+                           np.nextafter(ties, 0), np.nextafter(ties, np.inf), special])
+    src = torch.from_numpy(vals).to(dev)
+    dst = torch.empty(len(vals), dtype=torch.float32, device=dev)
+    L.check(lib.kc_to_f32(ptr(src), ptr(dst), len(vals), stream_handle(dev)), "kc_to_f32")
+    got = dst.cpu().numpy().view(np.uint32)
+    want = vals.astype(np.float32).view(np.uint32)
+    nan = np.isnan(vals)
+    assert np.array_equal(got[~nan], want[~nan])
+    assert np.isnan(dst.cpu().numpy()[nan]).all()
+    assert lib.kc_to_f32(None, None, 0, stream_handle(dev)) == L.OK
+    assert lib.kc_to_f32(None, ptr(dst), 5, stream_handle(dev)) == L.ERR_ARG
+    # the mixed-precision momentum planes and right-hand sides are their FP64 systems rounded
+    cfg = _small_cfg()
+    g = ChannelSolver(cfg, device=dev, precision="mixed")
+    _perturbed(g)
+    g.assemble_momentum()
+    g.assemble_p()
+    for a64, a32 in ((g.coef_u, g.coef_u32), (g.b_u, g.b_u32), (g.coef_v, g.coef_v32), (g.b_v, g.b_v32),
+                     (g.coef_p[1:], g.coef_p32[1:]), (g.b_p, g.b_p32)):
+        assert torch.equal(a64.float().view(torch.int32), a32.contiguous().view(torch.int32))
 
 
 def test_pcorr_assembly_and_correction(dev):
