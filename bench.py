@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--batch-instances", type=int, default=0, metavar="N",
                     help="time the batched configuration (N independent channel instances, stream-parallel) and exit")
     ap.add_argument("--batch-workers", type=int, default=16)
+    ap.add_argument("--copies", type=int, default=0, metavar="N",
+                    help="step N seeded copies of --config concurrently (the batch executor) and one after another")
     ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
                     help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
                          "(the command the committed ncu summaries were captured on)")
@@ -582,19 +584,23 @@ def run_spmv_sweep(args):
     print(json.dumps({"spmv_sweep": rows}), flush=True)
 
 
-def run_batch(args):
+def run_batch(args, cfgs=None, workload=None):
     """Instance time steps/s of the batched configuration: N instances (sizes
     128x32 .. 640x128, D 4-16, Re 60-200) stepped concurrently, one CUDA stream
     per instance, against the same instances stepped one after another on one
-    stream.  W warm-up steps, then K timed steps of every instance."""
+    stream.  W warm-up steps, then K timed steps of every instance.  With
+    ``cfgs`` (``--copies``): those instances instead, e.g. seeded copies of one
+    preset."""
     import numpy as np
     import torch
     from karman_taichi_gb300.batch import BatchedChannels, batch_configs
     mode = "fp64" if args.mode == "fp64" else "mixed"
-    cfgs = batch_configs(args.batch_instances, seed=0)
+    if cfgs is None:
+        cfgs = batch_configs(args.batch_instances, seed=0)
+        workload = f"{len(cfgs)} channel instances, 128x32 .. 640x128"
     out = {"metric": "instance time steps/s, batched channel instances", "unit": "instance time steps/s",
-           "instances": len(cfgs), "cells": int(sum(c.cells for c in cfgs)), "mode": mode,
-           "steps": args.steps, "warmup": args.warmup}
+           "config": {"workload": workload}, "instances": len(cfgs), "cells": int(sum(c.cells for c in cfgs)),
+           "mode": mode, "steps": args.steps, "warmup": args.warmup}
     for key, workers, native in (("native_concurrent", args.batch_workers, True), ("sequential", 1, True)):
         b = BatchedChannels(cfgs, precision=mode, workers=workers)
         if mode == "mixed" and not args.no_autotune:   # per grid size, before anything is timed
@@ -604,7 +610,8 @@ def run_batch(args):
         run = b.step_native if native else b.step
         run(args.warmup)
         t = run(args.steps)
-        outer = np.mean([sum(s.get("outer", 1) for s in r) for rec in b.records for r in rec[args.warmup:]])
+        # the native driver records one entry per call (its last step's statistics): the timed call's
+        outer = np.mean([sum(s.get("outer", 1) for s in rec[-1]) for rec in b.records])
         out[key] = {"workers": workers, "driver": "native threads" if native else "python threads",
                     "seconds": round(t, 3),
                     "value": round(len(cfgs) * args.steps / t, 2),
@@ -637,6 +644,10 @@ if __name__ == "__main__":
         run_profile_outer(a)
     elif a.spmv_sweep:
         run_spmv_sweep(a)
+    elif a.copies > 0:
+        from karman_taichi_gb300.config import PRESETS
+        base = PRESETS[a.config]
+        run_batch(a, [base.with_(seed=k) for k in range(a.copies)], f"{base.name} x {a.copies} seeded copies")
     elif a.batch_instances > 0:
         run_batch(a)
     else:
