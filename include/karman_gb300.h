@@ -200,7 +200,9 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
  * coarsening, red-black Gauss-Seidel smoothing with per-level weights
  * omega[l], coarse corrections scaled by alpha[l].  Links across the end of a
  * row of [n/stride][stride] are treated as links to a zero cell.
- * nu_pre = nu_post = 1 selects the fused cycle (two launches per level).
+ * nu_pre / nu_post are the sweeps on level 0, nu_coarse (1..3 in the fused
+ * cycle; <= 0 reads as 1) those on every level below; nu_pre = nu_post = 1
+ * selects the fused cycle (two launches per level).
  * coarsest_sweeps = 0: coarsening stops at <= 128 cells, whose dense
  * operator is inverted at setup (exact coarsest solve; a non-positive pivot
  * falls back to 64 Jacobi sweeps); > 0: coarsening stops at <= 1024 cells,
@@ -210,10 +212,10 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
  * when their arrays fit the block's shared memory; 0 launches every level
  * separately.  The fused cycle's levels below level 0 with at least
  * big_cells cells use 16 x 60-cell tiles, smaller ones 8 x 28.  Neither
- * changes the result.  kc_mg_default_opts: nu 1/1, exact coarsest solve,
- * omega 1.0 on level 0 and 1.1 below, alpha 1.9 on level 0 and 2.0 below
- * (the tuned setting for the channel's pressure correction), tail 1536,
- * big_cells 200000. */
+ * changes the result.  kc_mg_default_opts: nu 1/1 on level 0 and 2 below,
+ * exact coarsest solve, omega 1.0 on level 0 and 1.5 below, alpha 1.9 on
+ * level 0 and 2.0 below (the tuned setting for the channel's pressure
+ * correction), tail 1536, big_cells 200000. */
 #define KC_MG_MAX_LEVELS 16
 typedef struct {
     int nu_pre, nu_post;          /* red-black sweeps before / after the coarse correction */
@@ -221,6 +223,7 @@ typedef struct {
     int max_levels;
     int tail;                     /* levels of at most this many cells in one launch (0: off) */
     int big_cells;                /* levels of at least this many cells use the large tiles */
+    int nu_coarse;                /* red-black sweeps before / after on the levels below 0  */
     float omega[KC_MG_MAX_LEVELS];/* smoother weight per level                            */
     float alpha[KC_MG_MAX_LEVELS];/* coarse-correction scale per level                    */
 } kc_mg_opts;

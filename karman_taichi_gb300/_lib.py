@@ -69,7 +69,8 @@ MOMENTUM_BICGSTAB, MOMENTUM_RBGS = 0, 1
 
 class KcMgOpts(C.Structure):
     _fields_ = [("nu_pre", C.c_int), ("nu_post", C.c_int), ("coarsest_sweeps", C.c_int), ("max_levels", C.c_int),
-                ("tail", C.c_int), ("big_cells", C.c_int), ("omega", C.c_float * 16), ("alpha", C.c_float * 16)]
+                ("tail", C.c_int), ("big_cells", C.c_int), ("nu_coarse", C.c_int), ("omega", C.c_float * 16),
+                ("alpha", C.c_float * 16)]
 
 
 class KcChannel(C.Structure):

@@ -349,28 +349,29 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
     if (k < n) x[k] = xs[cur][k];
 }
 
-// ---- fused cycle kernels (one pre- and one post-sweep per level) ---------------------
-template <int TI, int AJ, int RY, bool STAGED>
+// ---- fused cycle kernels (NU pre- and NU post-sweeps per level) ------------------------
+template <int TI, int AJ, int RY, bool STAGED, int NU>
 __global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
                                                      float* __restrict__ bc, int NXc, int NYc, const int* done) {
     pdl_wait();
-    if (TI < kMgTI0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
+    if (AJ < kMgAJ0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
     if (mg_done(done)) return;
-    mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, b, nullptr,
-                                                                0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc);
+    mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED, NU>(blockIdx.y * TI, blockIdx.x * mg_tj(AJ, NU), L, b,
+                                                                    nullptr, 0.f, MgNoMid{}, MgOwnNone{}, xout, bc,
+                                                                    NXc, NYc);
     pdl_trigger();
 }
 
-template <int TI, int AJ, int RY, bool STAGED>
+template <int TI, int AJ, int RY, bool STAGED, int NU>
 __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restrict__ xpre,
                                                    const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                    const float* __restrict__ b, float* __restrict__ xout,
                                                    const int* done) {
     pdl_wait();
-    if (TI < kMgTI0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
+    if (AJ < kMgAJ0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
     if (mg_done(done)) return;
-    mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED>(blockIdx.y * TI, blockIdx.x * (AJ - 4), L, xpre, xc, NXc, NYc, alpha, b,
-                                              MgOwnNone{}, xout);
+    mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED, NU>(blockIdx.y * TI, blockIdx.x * mg_tj(AJ, NU), L, xpre, xc, NXc, NYc,
+                                                  alpha, b, MgOwnNone{}, xout);
     pdl_trigger();
 }
 
@@ -397,6 +398,7 @@ struct TailLevel {
     const float* winv;   // smoother weights
     int NX, NY;
     float alpha;         // weight of the coarse correction prolonged into this level
+    int nu;              // red-black sweeps before and after the coarse correction
     int so;              // shared-memory offset (floats) of the level's arrays
     unsigned mNY, mHalf; // t / NY and t / ((NY + 1) / 2) by tdiv (exact for t, d < 2^16)
 };
@@ -477,7 +479,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
         for (int k = tid; k < A.n; k += kTailThreads) A.b[k] = __ldcg(T.b_in + k);
     }
     __syncthreads();
-    // downward: red start, black half-sweep, restriction
+    // downward: red start, 2 nu - 1 half-sweeps (black, red, ...), restriction
     for (int l = T.Ls; l < T.Lend; ++l) {
         const TailLevel& L = T.lv[l];
         const TailLevel& Q = T.lv[l + 1];
@@ -487,8 +489,10 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
             A.x[k] = ((i + j) & 1) == 0 ? A.w[k] * A.b[k] : 0.f;
         }
         __syncthreads();
-        tail_sweep(A, L, 1);
-        __syncthreads();
+        for (int h = 1; h < 2 * L.nu; ++h) {
+            tail_sweep(A, L, h & 1);
+            __syncthreads();
+        }
         const TailArr B = tail_arr(sm, Q);
         for (int t = tid; t < B.n; t += kTailThreads) {
             const int I = tdiv(t, Q.mNY), J = t - I * B.NY;
@@ -548,7 +552,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
         }
         __syncthreads();
     }
-    // upward: prolongation, black then red half-sweep
+    // upward: prolongation, nu sweeps (black then red half-sweep)
     for (int l = T.Lend - 1; l >= T.Ls; --l) {
         const TailLevel& L = T.lv[l];
         const TailLevel& Q = T.lv[l + 1];
@@ -560,10 +564,10 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
             A.x[k] = fmaf(L.alpha, xc[(i >> 1) * Q.NY + (j >> 1)], A.x[k]);
         }
         __syncthreads();
-        tail_sweep(A, L, 1);
-        __syncthreads();
-        tail_sweep(A, L, 0);
-        __syncthreads();
+        for (int h = 1; h <= 2 * L.nu; ++h) {
+            tail_sweep(A, L, h & 1);
+            __syncthreads();
+        }
     }
     const TailArr A = tail_arr(sm, T.lv[T.Ls]);
     for (int k = tid; k < A.n; k += kTailThreads) T.x_out[k] = A.x[k];
@@ -642,19 +646,52 @@ static Lvl level_of(const MgLayout& M, char* base, int l, const float* c0, long 
 
 static MgLvl mg_lvl(const Lvl& L) { return MgLvl{L.c, L.cs, L.es, L.NX, L.NY, L.lap, L.winv, L.iso}; }
 
+// red-black sweeps before and after the coarse correction on level l: nu_pre / nu_post on
+// level 0, nu_coarse (<= 0 read as 1) below
+static inline int mg_nu_coarse(const kc_mg_opts* o) { return std::max(1, o->nu_coarse); }
+static inline int mg_nu_pre(const kc_mg_opts* o, int l) { return l == 0 ? o->nu_pre : mg_nu_coarse(o); }
+static inline int mg_nu_post(const kc_mg_opts* o, int l) { return l == 0 ? o->nu_post : mg_nu_coarse(o); }
+
 static bool mg_fusable(const MgLayout& M, const kc_mg_opts* o) {
-    return o->nu_pre == 1 && o->nu_post == 1 && M.levels >= 2;
+    return o->nu_pre == 1 && o->nu_post == 1 && mg_nu_coarse(o) <= kMgMaxNu && M.levels >= 2;
+}
+
+template <int NU>
+static cudaError_t launch_down_nu(bool big, const MgLvl& G, const float* b, float* xout, float* bc, int NXc, int NYc,
+                                  const int* done, cudaStream_t s) {
+    if (big) {
+        constexpr int TI = mg_big_ti(NU);
+        return launch_chain(k_mg_down<TI, kMgAJ0, kMgRY0, (kMgStagedLarge || NU > 1), NU>,
+                            mg_tile_grid(G.NX, G.NY, TI, mg_tj(kMgAJ0, NU)), dim3(kMgNT0), 0, s, G, b, xout, bc, NXc,
+                            NYc, done);
+    }
+    return launch_chain(k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true, NU>, mg_tile_grid(G.NX, G.NY, kMgTI1, mg_tj(kMgAJ1, NU)),
+                        dim3(kMgNT1), 0, s, G, b, xout, bc, NXc, NYc, done);
+}
+
+template <int NU>
+static cudaError_t launch_up_nu(bool big, const MgLvl& G, const float* xpre, const float* xc, int NXc, int NYc,
+                                float alpha, const float* b, float* xout, const int* done, cudaStream_t s) {
+    if (big) {
+        constexpr int TI = mg_big_ti(NU);
+        return launch_chain(k_mg_up<TI, kMgAJ0, kMgRY0, (kMgStagedLarge || NU > 1), NU>,
+                            mg_tile_grid(G.NX, G.NY, TI, mg_tj(kMgAJ0, NU)), dim3(kMgNT0), 0, s, G, xpre, xc, NXc,
+                            NYc, alpha, b, xout, done);
+    }
+    return launch_chain(k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true, NU>, mg_tile_grid(G.NX, G.NY, kMgTI1, mg_tj(kMgAJ1, NU)),
+                        dim3(kMgNT1), 0, s, G, xpre, xc, NXc, NYc, alpha, b, xout, done);
 }
 
 static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, float* xout, float* bc, const int* done,
                        const kc_mg_opts* o, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
-    if (l == 0 || mg_big(L.NX, L.NY, o))
-        KC_CUDA(launch_chain(k_mg_down<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
-                             dim3(kMgNT0), 0, s, G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done));
-    else
-        KC_CUDA(launch_chain(k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true>, mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1),
-                             dim3(kMgNT1), 0, s, G, b, xout, bc, M.nx[l + 1], M.ny[l + 1], done));
+    const bool big = l == 0 || mg_big(L.NX, L.NY, o);
+    const int nu = l == 0 ? 1 : mg_nu_coarse(o);
+    const int NXc = M.nx[l + 1], NYc = M.ny[l + 1];
+    const cudaError_t e = nu == 1   ? launch_down_nu<1>(big, G, b, xout, bc, NXc, NYc, done, s)
+                          : nu == 2 ? launch_down_nu<2>(big, G, b, xout, bc, NXc, NYc, done, s)
+                                    : launch_down_nu<3>(big, G, b, xout, bc, NXc, NYc, done, s);
+    if (e != cudaSuccess) return cuda_status(e, "k_mg_down launch");
     KC_LAUNCH_CHECK_NC("k_mg_down");
     return KC_OK;
 }
@@ -662,12 +699,13 @@ static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, f
 static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, const float* xc, float alpha,
                      const float* b, float* xout, const int* done, const kc_mg_opts* o, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
-    if (l == 0 || mg_big(L.NX, L.NY, o))
-        KC_CUDA(launch_chain(k_mg_up<kMgTI0, kMgAJ0, kMgRY0, kMgStagedLarge>, mg_tile_grid(L.NX, L.NY, kMgTI0, kMgTJ0),
-                             dim3(kMgNT0), 0, s, G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done));
-    else
-        KC_CUDA(launch_chain(k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true>, mg_tile_grid(L.NX, L.NY, kMgTI1, kMgTJ1),
-                             dim3(kMgNT1), 0, s, G, xpre, xc, M.nx[l + 1], M.ny[l + 1], alpha, b, xout, done));
+    const bool big = l == 0 || mg_big(L.NX, L.NY, o);
+    const int nu = l == 0 ? 1 : mg_nu_coarse(o);
+    const int NXc = M.nx[l + 1], NYc = M.ny[l + 1];
+    const cudaError_t e = nu == 1   ? launch_up_nu<1>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s)
+                          : nu == 2 ? launch_up_nu<2>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s)
+                                    : launch_up_nu<3>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s);
+    if (e != cudaSuccess) return cuda_status(e, "k_mg_up launch");
     KC_LAUNCH_CHECK_NC("k_mg_up");
     return KC_OK;
 }
@@ -794,6 +832,7 @@ static int launch_tail(const TailPlan& P, const MgLayout& M, char* base, const k
         L.NX = M.nx[l];
         L.NY = M.ny[l];
         L.alpha = o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)];
+        L.nu = std::max(mg_nu_pre(o, l), mg_nu_post(o, l));   // 1 on level 0 (fused cycle), nu_coarse below
         L.so = off;
         L.mNY = tail_magic(L.NY);
         L.mHalf = tail_magic((L.NY + 1) / 2);
@@ -820,8 +859,10 @@ int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o) {
         const TailPlan P = tail_plan(M, o);
         return P.ok ? 2 * P.Ls + 1 : 2 * (M.levels - 1) + 1;
     }
-    const int down = 2 + 2 * std::max(0, o->nu_pre - 1) + 1, up = 1 + 2 * std::max(0, o->nu_post);
-    return (M.levels - 1) * (down + up) + 1;
+    int n = 1;
+    for (int l = 0; l + 1 < M.levels; ++l)
+        n += 2 + 2 * std::max(0, mg_nu_pre(o, l) - 1) + 1 + 1 + 2 * std::max(0, mg_nu_post(o, l));
+    return n;
 }
 
 // levels >= 1 of the fused cycle: b_1 in, final_1 out
@@ -911,7 +952,7 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
         bl[l] = l == 0 ? r : (const float*)(base + M.off_b[l]);
         xl[l] = l == 0 ? z : (float*)(base + M.off_x[l]);
     }
-    // downward leg: nu_pre red-black sweeps (the first from x = 0), restrict
+    // downward leg: nu_pre (level 0) / nu_coarse red-black sweeps (the first from x = 0), restrict
     for (int l = 0; l < M.levels; ++l) {
         Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
         const long long n = (long long)M.nx[l] * M.ny[l];
@@ -929,7 +970,7 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
         k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
         KC_LAUNCH_CHECK_NC("k_mg_rbgs");
         ++nk;
-        for (int q = 1; q < o->nu_pre; ++q) {
+        for (int q = 1; q < mg_nu_pre(o, l); ++q) {
             k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 0, done);
             k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
             KC_LAUNCH_CHECK_NC("k_mg_rbgs");
@@ -940,7 +981,7 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
         KC_LAUNCH_CHECK_NC("k_mg_restrict");
         ++nk;
     }
-    // upward leg: over-corrected prolongation, nu_post red-black sweeps
+    // upward leg: over-corrected prolongation, nu_post (level 0) / nu_coarse red-black sweeps
     for (int l = M.levels - 2; l >= 0; --l) {
         Lvl L = level_of(M, base, l, c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN);
         const long long n = (long long)M.nx[l] * M.ny[l];
@@ -948,7 +989,7 @@ int mg_enqueue(const kc_system* A, void* ws, const kc_mg_opts* o, const float* r
                                                 o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)], done);
         KC_LAUNCH_CHECK_NC("k_mg_prolong");
         ++nk;
-        for (int q = 0; q < o->nu_post; ++q) {
+        for (int q = 0; q < mg_nu_post(o, l); ++q) {
             k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 1, done);
             k_mg_rbgs<<<pw_grid(n), 256, 0, s>>>(L, bl[l], xl[l], 0, done);
             KC_LAUNCH_CHECK_NC("k_mg_rbgs");
@@ -969,15 +1010,19 @@ void kc_mg_default_opts(kc_mg_opts* o) {
     if (!o) return;
     o->nu_pre = 1;             // the fused two-launch-per-level cycle
     o->nu_post = 1;
+    o->nu_coarse = 2;          // two sweeps each way on the latency-bound levels below level 0
     o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
     o->tail = kTailMax;        // the levels of at most 1536 cells in one single-block launch
     o->big_cells = 200000;     // levels of 200k cells and more in 16 x 60 tiles
-    // measured on GB300 over five p' systems (three time points of the 2048 x 512 channel,
-    // the 320 x 64 channel, a random 1024^2 system): 2-4 CG iterations fewer per solve than
-    // the uniform omega 1.1 / alpha 1.8, no breakdown
+    // Level 0 (one sweep, the expensive level): omega 1.0, alpha 1.9 -- measured on GB300 over
+    // five p' systems (three time points of the 2048 x 512 channel, the 320 x 64 channel, a
+    // random 1024^2 system): 2-4 CG iterations fewer per solve than the uniform omega 1.1 /
+    // alpha 1.8.  Below (two sweeps, over-relaxed): omega 1.5, alpha 2.0 -- with the restated
+    // cycle on the 2050 x 514 p' system of the channel 17 CG iterations to 1e-8 against 26
+    // with one sweep of omega 1.1.
     for (int l = 0; l < KC_MG_MAX_LEVELS; ++l) {
-        o->omega[l] = l == 0 ? 1.0f : 1.1f;
+        o->omega[l] = l == 0 ? 1.0f : 1.5f;
         o->alpha[l] = l == 0 ? 1.9f : 2.0f;
     }
 }

@@ -17,6 +17,14 @@ constexpr int kMgTI0 = 16, kMgAJ0 = 64, kMgRY0 = 4, kMgTJ0 = kMgAJ0 - 4, kMgNT0 
 constexpr bool kMgStagedLarge = true;
 // tiles of the small levels: 8 x 28 owned cells, 32-wide staged rows
 constexpr int kMgTI1 = 8, kMgAJ1 = 32, kMgRY1 = 4, kMgTJ1 = kMgAJ1 - 4, kMgNT1 = kMgAJ1 * kMgRY1;
+// Levels >= 1 may take NU = 1..3 red-black sweeps before and after their
+// coarse correction (kc_mg_opts.nu_coarse): the staged halo is 2 NU cells, so
+// the large tiles keep 64-wide rows and lose rows as NU grows -- their nine
+// staged [TI + 4 NU][64] arrays stay within 48 KB of static shared memory --
+// and the small tiles keep 8 rows (24 x 32 at NU = 3: 24 KB).
+constexpr int kMgMaxNu = 3;
+__host__ __device__ constexpr int mg_big_ti(int nu) { return nu <= 1 ? kMgTI0 : (nu == 2 ? 12 : 8); }
+__host__ __device__ constexpr int mg_tj(int AJ, int nu) { return AJ - 4 * nu; }
 inline dim3 mg_tile_grid(int NX, int NY, int TI, int TJ) { return dim3((NY + TJ - 1) / TJ, (NX + TI - 1) / TI); }
 inline int mg_fused_blocks0(long long n, int S) {
     const dim3 g = mg_tile_grid((int)(n / S), S, kMgTI0, kMgTJ0);
@@ -36,8 +44,8 @@ MgLayout mg_layout(int NX, int NY, const kc_mg_opts* o);
 // number of kernels one mg_enqueue launches for A
 int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o);
 
-// The fused cycle (one pre- and one post-sweep per level, at least two
-// levels) split at level 0, for solvers that fuse their own pointwise work
+// The fused cycle (one pre- and one post-sweep on level 0, nu_coarse on the
+// levels below, at least two levels) split at level 0, for solvers that fuse their own pointwise work
 // into the level-0 launches: the caller's level-0 DOWN writes x0pre and b1,
 // mg_enqueue_coarse runs levels >= 1 and leaves their result in final1, the
 // caller's level-0 UP prolongs final1 with alpha0.

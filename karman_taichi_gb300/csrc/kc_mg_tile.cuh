@@ -1,21 +1,24 @@
-// Tile kernels of the fused multigrid V-cycle (one pre- and one post-smoothing
-// red-black sweep per level).  Per level l the cycle is two launches:
+// Tile kernels of the fused multigrid V-cycle (NU pre- and NU post-smoothing
+// red-black sweeps per level).  Per level l the cycle is two launches:
 //
 //   DOWN_l  x  = red half-sweep from 0     (x_red = W b, x_black = 0)
-//           x += W (b - A x) on black cells
+//           x += W (b - A x) on black cells, then red, black, ... (2 NU - 1 half-sweeps)
 //           b_{l+1}(I,J) = sum over the aggregate's coupled cells of b - A x
 //           writes x (the pre-smoothed iterate) and b_{l+1}
 //   UP_l    x  = x_pre + alpha P x_{l+1}   (coupled cells)
-//           x += W (b - A x) on black, then on red cells
+//           x += W (b - A x) on black, then on red cells (NU times)
 //           writes the level's output
 //
 // which is the same arithmetic as the unfused kernels (k_mg_first, k_mg_rbgs,
 // k_mg_restrict, k_mg_prolong).  A block owns a TI x TJ tile (TI, TJ even, so
-// every 2x2 aggregate lies in one tile) and stages a 2-cell halo in shared
-// memory: the black cells of the 1-cell ring need the red cells of the 2-cell
-// ring.  Halo values are recomputed by every block that needs them, never
-// exchanged, so a launch has no inter-block dependence.  The operator is the
-// 2-D 5-point stencil with zero values outside [0,NX) x [0,NY).
+// every 2x2 aggregate lies in one tile) and stages an H = 2 NU cell halo in
+// shared memory: half-sweep h runs over the staged region less h rings (its
+// cells need the previous half-sweep's values one ring further out), so after
+// the 2 NU - 1 pre-smoothing half-sweeps the tile and its 1-ring are exact --
+// what the residual needs -- and the 2 NU post-smoothing half-sweeps end
+// exactly on the tile.  Halo values are recomputed by every block that needs
+// them, never exchanged, so a launch has no inter-block dependence.  The
+// operator is the 2-D 5-point stencil with zero values outside [0,NX) x [0,NY).
 //
 // Staging is asynchronous (cp.async, zero-filled outside the grid): every
 // thread issues all of its copies before waiting, so a block has its whole
@@ -87,16 +90,18 @@ struct MgOwnNone {
     __device__ __forceinline__ void operator()(int, float, float, Sum&) const {}
 };
 
-// Tile geometry: rows of AJ = 32 or 64 staged cells (TJ = AJ - 4 owned
-// columns plus the 2-cell halo on each side), so a row is one or two warps
-// and every index is a shift; RY thread rows walk the AI = TI + 4 staged rows.
-// All staged arrays share the [AI][AJ] layout.  i0 and j0 are even (TI and TJ
-// are), so a cell's colour (i + j) & 1 is (a + b) & 1 in tile coordinates.
-template <int TI, int AJ_, int RY_>
+// Tile geometry: rows of AJ = 32 or 64 staged cells (TJ = AJ - 2H owned
+// columns plus the H-cell halo on each side), so a row is one or two warps
+// and every index is a shift; RY thread rows walk the AI = TI + 2H staged rows.
+// All staged arrays share the [AI][AJ] layout.  i0 - H and j0 - H are even
+// (TI, TJ and H are), so a cell's colour (i + j) & 1 is (a + b) & 1 in tile
+// coordinates and its aggregate's staged coarse index is (a >> 1, b >> 1).
+template <int TI, int AJ_, int RY_, int H_ = 2>
 struct MgTile {
-    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY;
-    static constexpr int TJ = AJ - 4, AI = TI + 4, A = AI * AJ;
-    static_assert(TI % 2 == 0 && TJ % 2 == 0, "aggregates must not straddle tiles");
+    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY, H = H_;
+    static constexpr int TJ = AJ - 2 * H, AI = TI + 2 * H, A = AI * AJ;
+    static_assert(H % 2 == 0 && H >= 2, "the halo is two cells per sweep");
+    static_assert(TI % 2 == 0 && TJ % 2 == 0 && TJ > 0, "aggregates must not straddle tiles");
     static_assert((AJ & (AJ - 1)) == 0, "row width must be a power of two");
     __device__ static __forceinline__ int tx() { return threadIdx.x & (AJ - 1); }
     __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
@@ -104,7 +109,7 @@ struct MgTile {
 
 // stage the 5 coefficient components over the whole staged region of the tile at (i0, j0)
 // (H: halo width, the region starts at (i0 - H, j0 - H))
-template <int TI, class T, int H = 2>
+template <int TI, class T, int H = T::H>
 __device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, float* sc) {
     const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
@@ -118,15 +123,15 @@ __device__ __forceinline__ void mg_stage_coef(const MgLvl& L, int i0, int j0, fl
     }
 }
 
-// As mg_stage_coef with the halo H = 2, two columns per copy.  Needs an even
-// row length NY and an even tile origin j0: then a pair (j, j + 1) with j
-// even starts on an 8-byte boundary and lies wholly inside or outside the grid.
+// As mg_stage_coef, two columns per copy.  Needs an even row length NY and
+// an even region origin j0 - H: then a pair (j, j + 1) with j even starts on
+// an 8-byte boundary and lies wholly inside or outside the grid.
 template <int TI, class T>
 __device__ __forceinline__ void mg_stage_coef_pairs(const MgLvl& L, int i0, int j0, float* sc) {
     constexpr int PJ = T::AJ / 2;
     for (int e = threadIdx.x; e < T::AI * PJ; e += T::NT) {
         const int a = e / PJ, b = 2 * (e - a * PJ);
-        const int i = i0 + a - 2, j = j0 + b - 2;
+        const int i = i0 + a - T::H, j = j0 + b - T::H;
         const bool in = i >= 0 && i < L.NX && j >= 0 && j < L.NY;
         const float* g = in ? L.c + (long long)(i * L.NY + j) * L.es : L.c;
         const int u = a * T::AJ + b;
@@ -146,7 +151,7 @@ struct MgCoef {
     __device__ __forceinline__ float get(int q, int u) const {
         if (STAGED) return sc[q * T::A + u];
         const int a = u / T::AJ, b = u - a * T::AJ;
-        const int i = i0 + a - 2, j = j0 + b - 2;
+        const int i = i0 + a - T::H, j = j0 + b - T::H;
         if (i < 0 || i >= L.NX || j < 0 || j >= L.NY) return 0.f;
         return __ldg(L.c + q * L.cs + (long long)(i * L.NY + j) * L.es);
     }
@@ -180,14 +185,15 @@ struct MgStageDims {
 };
 
 // DOWN, asynchronous part: stage b_in (and q) , W and the coefficients of the tile at (i0, j0)
-template <int TI, int AJ, int RY, bool HasQ>
+// (halo H cells)
+template <int TI, int AJ, int RY, bool HasQ, int H = 2>
 __device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
                                               const float* __restrict__ q, MgStage S) {
-    using T = MgTile<TI, AJ, RY>;
-    const int b = T::tx(), j = j0 + b - 2;
+    using T = MgTile<TI, AJ, RY, H>;
+    const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = i0 + a - 2;
+        const int i = i0 + a - H;
         const bool in = jin && i >= 0 && i < L.NX;
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
@@ -199,7 +205,8 @@ __device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, co
 }
 
 // DOWN, after the tile's copies have landed: b = b_in - alpha q, red start,
-// black half-sweep over the 1-cell ring, x and the restricted residual out
+// 2 NU - 1 half-sweeps (black, red, ...) over shrinking rings, x and the
+// restricted residual out
 // right-hand side of the DOWN pass at staged position u: b_in (MgPreB) or
 // b_in - alpha q (MgPreQ); k is the cell index of an owned cell, else -1
 struct MgPreB {
@@ -212,40 +219,44 @@ struct MgPreQ {
     }
 };
 
-template <int TI, int AJ, int RY, class Pre, class Own>
+template <int TI, int AJ, int RY, class Pre, class Own, int NU = 1>
 __device__ __forceinline__ void mg_down_compute_pre(int i0, int j0, const MgLvl& L, const Pre& pre, const Own& own,
                                                     MgStage S, float* __restrict__ xout, float* __restrict__ bc,
                                                     int NXc, int NYc, typename Own::Sum& sum) {
-    using T = MgTile<TI, AJ, RY>;
+    using T = MgTile<TI, AJ, RY, 2 * NU>;
+    constexpr int H = T::H;
     float* sb = S.sb;
     const float* sw = S.sw;
     float* sx = S.sx;
     const MgCoef<T, true> C{S.sc, L, i0, j0};
-    const int b = T::tx(), j = j0 + b - 2;
-    const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
+    const int b = T::tx(), j = j0 + b - H;
+    const bool jown = b >= H && b < T::TJ + H && j < L.NY;
     // b, owned cells, red start (x = W b on red, 0 on black)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
-        const int i = i0 + a - 2;
-        const int k = (jown && a >= 2 && a < TI + 2 && i < L.NX) ? i * L.NY + j : -1;
+        const int i = i0 + a - H;
+        const int k = (jown && a >= H && a < TI + H && i < L.NX) ? i * L.NY + j : -1;
         const float bv = pre(S, u, k);
         sb[u] = bv;
         if (k >= 0) own(k, bv, sum);
         sx[u] = ((a + b) & 1) == 0 ? sw[u] * bv : 0.f;
     }
     __syncthreads();
-    // black half-sweep over the 1-cell ring (reads red neighbours only)
-    if (b >= 1 && b < AJ - 1)
-        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
-            if (((a + b) & 1) == 0) continue;
-            const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-        }
-    __syncthreads();
+    // half-sweep h = 1 .. 2 NU - 1 (odd: black, even: red) over the region less h rings
+#pragma unroll
+    for (int h = 1; h < 2 * NU; ++h) {
+        if (b >= h && b < AJ - h)
+            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
+                if (((a + b) & 1) != (h & 1)) continue;
+                const int u = a * T::AJ + b;
+                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+            }
+        __syncthreads();
+    }
     // owned cells: write x
     if (jown)
-        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
-            const int i = i0 + a - 2;
+        for (int a = H + T::ty(); a < TI + H; a += T::RY) {
+            const int i = i0 + a - H;
             if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + b];
         }
     // aggregates: restricted residual over coupled cells
@@ -258,8 +269,8 @@ __device__ __forceinline__ void mg_down_compute_pre(int i0, int j0, const MgLvl&
         for (int di = 0; di < 2; ++di)
 #pragma unroll
             for (int dj = 0; dj < 2; ++dj) {
-                const int a = 2 * ag + di + 2, bb = 2 * bg + dj + 2;
-                if (i0 + a - 2 >= L.NX || j0 + bb - 2 >= L.NY) continue;
+                const int a = 2 * ag + di + H, bb = 2 * bg + dj + H;
+                if (i0 + a - H >= L.NX || j0 + bb - H >= L.NY) continue;
                 const int u = a * T::AJ + bb;
                 if (!C.linked(u)) continue;
                 s += sb[u] - C.ax(sx, u);
@@ -268,37 +279,40 @@ __device__ __forceinline__ void mg_down_compute_pre(int i0, int j0, const MgLvl&
     }
 }
 
-template <int TI, int AJ, int RY, bool HasQ, class Own>
+template <int TI, int AJ, int RY, bool HasQ, class Own, int NU = 1>
 __device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
                                                 MgStage S, float* __restrict__ xout, float* __restrict__ bc,
                                                 int NXc, int NYc, typename Own::Sum& sum) {
     if (HasQ)
-        mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, MgPreQ{alpha}, own, S, xout, bc, NXc, NYc, sum);
+        mg_down_compute_pre<TI, AJ, RY, MgPreQ, Own, NU>(i0, j0, L, MgPreQ{alpha}, own, S, xout, bc, NXc, NYc, sum);
     else
-        mg_down_compute_pre<TI, AJ, RY>(i0, j0, L, MgPreB{}, own, S, xout, bc, NXc, NYc, sum);
+        mg_down_compute_pre<TI, AJ, RY, MgPreB, Own, NU>(i0, j0, L, MgPreB{}, own, S, xout, bc, NXc, NYc, sum);
 }
 
 // DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
-template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true>
+// NU sweeps need the staged coefficients (STAGED); the unstaged variant is the one-sweep cycle.
+template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true, int NU = 1>
 __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
                                                           const float* __restrict__ q, float alpha, const Mid& mid,
                                                           const Own& own, float* __restrict__ xout,
                                                           float* __restrict__ bc, int NXc, int NYc) {
-    using T = MgTile<TI, AJ, RY>;
+    static_assert(STAGED || NU == 1, "several sweeps per level read the staged coefficients");
     if (STAGED) {
-        __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
-        __shared__ __align__(16) float sq[HasQ ? T::A : 1];
-        __shared__ __align__(16) float sc[5 * T::A];
+        using TS = MgTile<TI, AJ, RY, 2 * NU>;
+        __shared__ __align__(16) float sb[TS::A], sw[TS::A], sx[TS::A];
+        __shared__ __align__(16) float sq[HasQ ? TS::A : 1];
+        __shared__ __align__(16) float sc[5 * TS::A];
         const MgStage S{sb, sq, sw, sc, sx, nullptr, nullptr};
-        mg_down_issue<TI, AJ, RY, HasQ>(i0, j0, L, b_in, q, S);
+        mg_down_issue<TI, AJ, RY, HasQ, 2 * NU>(i0, j0, L, b_in, q, S);
         cp_async_commit();
         mid();
         cp_async_wait_all();
         __syncthreads();
         typename Own::Sum sum{};
-        mg_down_compute<TI, AJ, RY, HasQ, Own>(i0, j0, L, alpha, own, S, xout, bc, NXc, NYc, sum);
+        mg_down_compute<TI, AJ, RY, HasQ, Own, NU>(i0, j0, L, alpha, own, S, xout, bc, NXc, NYc, sum);
         return sum;
     }
+    using T = MgTile<TI, AJ, RY>;
     __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
     __shared__ __align__(16) float sq[HasQ ? T::A : 1];
     const MgCoef<T, false> C{nullptr, L, i0, j0};
@@ -364,16 +378,17 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
 }
 
 // UP, asynchronous part: stage x_pre, b_in, W, the coarse cells under the tile and the coefficients
-template <int TI, int AJ, int RY>
+// (halo H cells; the coarse cells under the staged region start at (i0 - H) / 2, (j0 - H) / 2)
+template <int TI, int AJ, int RY, int H = 2>
 __device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
                                             const float* __restrict__ xc, int NXc, int NYc,
                                             const float* __restrict__ b_in, MgStage S) {
-    using T = MgTile<TI, AJ, RY>;
-    constexpr int XI = TI / 2 + 2, XJ = AJ / 2;
-    const int b = T::tx(), j = j0 + b - 2;
+    using T = MgTile<TI, AJ, RY, H>;
+    constexpr int XI = TI / 2 + H, XJ = AJ / 2;
+    const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
-        const int i = i0 + a - 2;
+        const int i = i0 + a - H;
         const bool in = jin && i >= 0 && i < L.NX;
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
@@ -383,7 +398,7 @@ __device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, cons
     }
     for (int t = threadIdx.x; t < XI * XJ; t += T::NT) {
         const int ca = t / XJ, cb = t - ca * XJ;
-        const int I = (i0 >> 1) - 1 + ca, J = (j0 >> 1) - 1 + cb;
+        const int I = (i0 >> 1) - H / 2 + ca, J = (j0 >> 1) - H / 2 + cb;
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(S.sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
@@ -391,38 +406,41 @@ __device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, cons
 }
 
 // UP, after the copies have landed: prolong (coupled cells, told apart by
-// their links), black half-sweep over the 1-cell ring, red half-sweep on the
-// owned cells, write
-template <int TI, int AJ, int RY, class Own>
+// their links), half-sweeps black, red, ... over shrinking rings (2 NU in
+// all, the last -- red -- on the owned cells), write
+template <int TI, int AJ, int RY, class Own, int NU = 1>
 __device__ __forceinline__ void mg_up_compute(int i0, int j0, const MgLvl& L, float alpha, const Own& own,
                                               MgStage S, float* __restrict__ xout, typename Own::Sum& sum) {
-    using T = MgTile<TI, AJ, RY>;
-    constexpr int XJ = AJ / 2;
+    using T = MgTile<TI, AJ, RY, 2 * NU>;
+    constexpr int H = T::H, XJ = AJ / 2;
     float* sx = S.sx;
     const float* sb = S.sb;
     const float* sw = S.sw;
     const float* sxc = S.sxc;
     const MgCoef<T, true> C{S.sc, L, i0, j0};
-    const int b = T::tx(), j = j0 + b - 2;
-    // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-2, j0-2)
+    const int b = T::tx(), j = j0 + b - H;
+    // prolongation over the staged region (coupled cells only; a, b >= 0 <=> i, j >= i0-H, j0-H)
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int u = a * T::AJ + b;
         if (!C.linked(u)) continue;
         sx[u] = fmaf(alpha, sxc[(a >> 1) * XJ + (b >> 1)], sx[u]);
     }
     __syncthreads();
-    // black half-sweep over the 1-cell ring
-    if (b >= 1 && b < AJ - 1)
-        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
-            if (((a + b) & 1) == 0) continue;
-            const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-        }
-    __syncthreads();
-    // red half-sweep on the owned cells, then write
-    if (b >= 2 && b < T::TJ + 2 && j < L.NY)
-        for (int a = 2 + T::ty(); a < TI + 2; a += T::RY) {
-            const int i = i0 + a - 2;
+    // half-sweep h = 1 .. 2 NU - 1 (odd: black, even: red) over the region less h rings
+#pragma unroll
+    for (int h = 1; h < 2 * NU; ++h) {
+        if (b >= h && b < AJ - h)
+            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
+                if (((a + b) & 1) != (h & 1)) continue;
+                const int u = a * T::AJ + b;
+                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+            }
+        __syncthreads();
+    }
+    // the last (red) half-sweep on the owned cells, then write
+    if (b >= H && b < T::TJ + H && j < L.NY)
+        for (int a = H + T::ty(); a < TI + H; a += T::RY) {
+            const int i = i0 + a - H;
             if (i >= L.NX) continue;
             const int u = a * T::AJ + b;
             float xv = sx[u];
@@ -434,26 +452,29 @@ __device__ __forceinline__ void mg_up_compute(int i0, int j0, const MgLvl& L, fl
 }
 
 // UP tile at (i0, j0): prolong (coupled cells, told apart by their links),
-// black half-sweep over the 1-cell ring, red half-sweep on the owned cells.
-template <int TI, int AJ, int RY, class Own, bool STAGED = true>
+// then the NU post-smoothing sweeps (black, red), the last red half-sweep on the owned cells.
+template <int TI, int AJ, int RY, class Own, bool STAGED = true, int NU = 1>
 __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
                                                         const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                         const float* __restrict__ b_in, const Own& own,
                                                         float* __restrict__ xout) {
-    using T = MgTile<TI, AJ, RY>;
-    constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
+    static_assert(STAGED || NU == 1, "several sweeps per level read the staged coefficients");
     if (STAGED) {
-        __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
-        __shared__ __align__(16) float sc[5 * T::A];
+        using TS = MgTile<TI, AJ, RY, 2 * NU>;
+        constexpr int XIS = TI / 2 + TS::H, XJS = AJ / 2;   // coarse cells under the staged region
+        __shared__ __align__(16) float sx[TS::A], sb[TS::A], sw[TS::A], sxc[XIS * XJS];
+        __shared__ __align__(16) float sc[5 * TS::A];
         const MgStage S{sb, nullptr, sw, sc, sx, sxc, nullptr};
-        mg_up_issue<TI, AJ, RY>(i0, j0, L, xpre, xc, NXc, NYc, b_in, S);
+        mg_up_issue<TI, AJ, RY, 2 * NU>(i0, j0, L, xpre, xc, NXc, NYc, b_in, S);
         cp_async_commit();
         cp_async_wait_all();
         __syncthreads();
         typename Own::Sum sum{};
-        mg_up_compute<TI, AJ, RY, Own>(i0, j0, L, alpha, own, S, xout, sum);
+        mg_up_compute<TI, AJ, RY, Own, NU>(i0, j0, L, alpha, own, S, xout, sum);
         return sum;
     }
+    using T = MgTile<TI, AJ, RY>;
+    constexpr int XI = TI / 2 + 2, XJ = AJ / 2;   // coarse cells under the staged region
     __shared__ __align__(16) float sx[T::A], sb[T::A], sw[T::A], sxc[XI * XJ];
     const MgCoef<T, false> C{nullptr, L, i0, j0};
     const int b = T::tx(), j = j0 + b - 2;
@@ -512,7 +533,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
 // with the 2-cell halo.
 template <int TI, int AJ_, int RY_>
 struct MgTile3 {
-    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY;
+    static constexpr int AJ = AJ_, RY = RY_, NT = AJ * RY, H = 3;
     static constexpr int TJ = AJ - 6, AI = TI + 6, A = AI * AJ;
     static constexpr int XI = TI / 2 + 4, XJ = AJ / 2 + 1, XC = XI * XJ;   // coarse cells under the region
     static_assert(TI % 2 == 0 && TJ % 2 == 0, "aggregates must not straddle tiles");

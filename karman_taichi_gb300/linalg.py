@@ -279,20 +279,24 @@ TAIL_CELLS = 1536   # default: levels of at most this many cells run in the mult
 class Multigrid:
     """Aggregation multigrid V-cycle (FP32) for a 2-D 5-point operator; the
     preconditioner of the mixed-precision pressure-correction solve.
+    ``nu_pre`` / ``nu_post`` are the red-black sweeps on level 0, ``nu_coarse``
+    those on every level below (1..3 in the fused two-launch cycle);
     ``omega`` / ``alpha`` are per-level smoother weights and coarse-correction
-    scales (scalars broadcast to all levels); ``coarsest_sweeps=0`` solves the
-    coarsest level (<= 128 cells) exactly.  ``tail`` runs the levels of at
-    most that many cells (True: 1536) in one single-block launch, ``big_cells``
-    picks the large tiles for the levels of at least that many cells; neither
-    changes the result (the launch shapes the autotuner chooses between)."""
+    scales (scalars broadcast to all levels; the last entry repeats);
+    ``coarsest_sweeps=0`` solves the coarsest level (<= 128 cells) exactly.
+    ``tail`` runs the levels of at most that many cells (True: 1536) in one
+    single-block launch, ``big_cells`` picks the large tiles for the levels of
+    at least that many cells; neither changes the result (the launch shapes
+    the autotuner chooses between)."""
 
-    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.1), alpha=(1.9, 2.0),
-                 max_levels=16, tail=True, big_cells=200000):
+    def __init__(self, A32: Stencil, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.5), alpha=(1.9, 2.0),
+                 max_levels=16, tail=True, big_cells=200000, nu_coarse=2):
         if A32.dtype != L.F32:
             raise TypeError("multigrid runs on FP32 coefficients")
         self.A = A32
         o = L.KcMgOpts()
         o.nu_pre, o.nu_post, o.coarsest_sweeps, o.max_levels = nu_pre, nu_post, coarsest_sweeps, max_levels
+        o.nu_coarse = int(nu_coarse)
         o.tail = TAIL_CELLS if tail is True else int(tail)
         o.big_cells = int(big_cells)
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16

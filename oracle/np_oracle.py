@@ -945,21 +945,23 @@ class MultigridOracle:
     """2x2 Galerkin aggregation in Laplacian form (rows without off-diagonal
     links are isolated: solved pointwise, never aggregated, links into them
     folded into the row sum), red-black
-    Gauss-Seidel smoothing weighted by omega[l], coarse corrections scaled by
+    Gauss-Seidel smoothing weighted by omega[l] (nu_pre / nu_post sweeps on
+    level 0, nu_coarse on every level below), coarse corrections scaled by
     alpha[l]; on the coarsest level Jacobi sweeps (<= 1024 cells) or, with
     coarsest_sweeps = 0, the exact solve by a dense FP32 inverse (<= 128 cells)."""
 
     COARSEST = 1024          # coarsest level of the Jacobi variant (cells)
     COARSEST_DIRECT = 128    # coarsest level of the direct variant (coarsest_sweeps = 0)
 
-    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.1), alpha=(1.9, 2.0),
-                 max_levels=16, lap=False):
+    def __init__(self, coef, NX, NY, nu_pre=1, nu_post=1, coarsest_sweeps=0, omega=(1.0, 1.5), alpha=(1.9, 2.0),
+                 max_levels=16, lap=False, nu_coarse=2):
         f32 = np.float32
         om = list(omega) if hasattr(omega, "__len__") else [omega] * 16
         al = list(alpha) if hasattr(alpha, "__len__") else [alpha] * 16
         self.omega = [f32(om[min(l, len(om) - 1)]) for l in range(16)]
         self.alpha = [f32(al[min(l, len(al) - 1)]) for l in range(16)]
         self.nu_pre, self.nu_post, self.sweeps = nu_pre, nu_post, coarsest_sweeps
+        self.nu_coarse = max(1, nu_coarse)
         c = np.asarray(coef, dtype=f32).reshape(5, NX, NY)
         self.levels = [self._level(c, NX, NY, self.omega[0], lap)]
         target = self.COARSEST_DIRECT if coarsest_sweeps == 0 else self.COARSEST
@@ -1087,7 +1089,7 @@ class MultigridOracle:
             ii, jj = np.meshgrid(np.arange(L["NX"]), np.arange(L["NY"]), indexing="ij")
             x = np.where(((ii + jj) & 1) == 0, L["winv"] * b, np.float32(0)).astype(np.float32)
             self._rb(L, b, x, 1)
-            for _ in range(1, self.nu_pre):
+            for _ in range(1, self.nu_pre if l == 0 else self.nu_coarse):
                 self._rb(L, b, x, 0); self._rb(L, b, x, 1)
             xs.append(x)
             res = np.where(L["iso"], np.float32(0), b - self._Ax(L, x))
@@ -1100,7 +1102,7 @@ class MultigridOracle:
             xc = xs[l + 1]
             up = np.repeat(np.repeat(xc, 2, axis=0), 2, axis=1)[:L["NX"], :L["NY"]]
             xs[l] = np.where(L["iso"], xs[l], xs[l] + self.alpha[min(l, 15)] * up).astype(np.float32)
-            for _ in range(self.nu_post):
+            for _ in range(self.nu_post if l == 0 else self.nu_coarse):
                 self._rb(L, bs[l], xs[l], 1); self._rb(L, bs[l], xs[l], 0)
         return xs[0].reshape(-1)
 

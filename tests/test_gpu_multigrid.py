@@ -5,6 +5,8 @@ Tolerances: one V-cycle agrees with the FP32 NumPy restatement to 1e-4
 relative (both FP32; the GPU contracts to FMA); the refined solve meets the
 FP64 tolerance ||b - A x|| / ||b|| < 1e-8 and matches a direct solve to 1e-6.
 """
+import functools
+
 import numpy as np
 import pytest
 
@@ -83,6 +85,31 @@ def test_vcycle_matches_restatement(dev, alpha, lap, nu, coarsest):
     assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
+@functools.lru_cache(maxsize=None)
+def _pcorr_320x64():
+    return _channel_pcorr(320, 64, 8, 64, 32)
+
+
+@pytest.mark.parametrize("tail", [False, True])
+@pytest.mark.parametrize("big_cells", [1000, 200000])   # 1000: the large (64-wide) tiles on every level below 0
+@pytest.mark.parametrize("nu_coarse", [1, 2, 3])
+def test_vcycle_coarse_sweeps_match_restatement(dev, nu_coarse, big_cells, tail):
+    """nu_coarse red-black sweeps before and after the coarse correction on the
+    levels below level 0: the fused tile kernels (halo 2 nu_coarse) and the
+    one-block tail against the restatement."""
+    from karman_taichi_gb300 import linalg
+    coef, b = _pcorr_320x64()
+    NX, NY = coef.shape[1:]
+    c32, form = _fp32(coef, True)
+    A = linalg.Stencil(_t(c32, dev), form=form)
+    mg = linalg.Multigrid(A, nu_coarse=nu_coarse, big_cells=big_cells, tail=tail).setup()
+    r = np.random.default_rng(1).standard_normal(NX * NY).astype(np.float32)
+    r[coef[0].reshape(-1) == 0] = 0.0
+    z = mg.apply(_t(r.reshape(NX, NY), dev)).cpu().numpy().reshape(-1)
+    ref = O.MultigridOracle(c32.reshape(5, -1), NX, NY, lap=True, nu_coarse=nu_coarse).apply(r)
+    assert np.abs(z - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("tail", [False, True])
 def test_vcycle_launch_count(dev, tail):
     """The fused cycle launches two kernels per level above the coarsest; with
@@ -104,9 +131,10 @@ def test_vcycle_launch_count(dev, tail):
 
 # grids of the workloads (p' of the 320x64 and 2048x512 channels, the 1024^2 system,
 # a 4096x1024 channel, small batched instances, a strip): the tail starts at levels 1..6
+@pytest.mark.parametrize("nu_coarse", [2, 3])
 @pytest.mark.parametrize("shape", [(98, 42), (130, 34), (322, 66), (1026, 1026), (2050, 514), (4098, 1026),
                                    (3000, 7)])
-def test_tail_is_the_per_level_cycle(dev, shape):
+def test_tail_is_the_per_level_cycle(dev, shape, nu_coarse):
     """The smallest levels in one launch compute the V-cycle bit for bit as the
     one-launch-per-level cycle does."""
     import torch
@@ -121,7 +149,7 @@ def test_tail_is_the_per_level_cycle(dev, shape):
     lib = L.load()
     zs = []
     for tail in (False, True):
-        mg = linalg.Multigrid(A, tail=tail).setup()
+        mg = linalg.Multigrid(A, tail=tail, nu_coarse=nu_coarse).setup()
         n0 = lib.kc_launch_count()
         zs.append(mg.apply(rt))
         zs.append(mg.apply(rt))

@@ -106,11 +106,12 @@ def test_learned_initial_guess_saves_cg_iterations(dev):
     assert after < 0.5 * before, (before, after)
     # held-out systems: a run from another seeded initial state.  The network's
     # own gain is the initial error: ||x0 - p'|| / ||p'|| against 1 for x0 = 0.
-    # In CG iterations it pays against the uniformly weighted cycle (omega 1.1,
-    # alpha 1.8 on every level); the per-level weights of the default cycle
-    # remove the smooth error it predicts within a few iterations themselves.
+    # In CG iterations it pays against the uniform one-sweep cycle (omega 1.1,
+    # alpha 1.8, one sweep on every level); the default cycle's per-level
+    # weights and sweeps remove the smooth error it predicts within a few
+    # iterations themselves.
     solver2 = ChannelSolver(cfg.with_(seed=1), device=dev, precision="mixed")
-    weak = linalg.Multigrid(solver2.A_p32, omega=1.1, alpha=1.8)
+    weak = linalg.Multigrid(solver2.A_p32, omega=1.1, alpha=1.8, nu_coarse=1)
     guess = learned.LearnedGuess(net)
     it0 = it1 = 0
     errs = []
