@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
-                    help="keep the default launch shapes of the p' solve instead of tuning them before timing")
+                    help="keep the default cycle and launch shapes of the p' solve instead of tuning them "
+                         "before timing")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
     ap.add_argument("--spmv-sweep", action="store_true",
                     help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
@@ -422,10 +423,10 @@ def run_gpu(args):
     solver = make_solver(cfg, mode, dev)
     tuned = None
     if mode == "mixed" and not args.no_autotune:
-        # launch shapes of the p' solve (multigrid tail, tile sizes, CG chunk length), picked on
-        # this solver's state before anything is timed; the fields computed do not change
-        from karman_taichi_gb300.autotune import tune_pressure
-        tuned = tune_pressure(solver)
+        # the p' solve's cycle (sweeps below level 0) and launch shapes (multigrid tail, tile sizes,
+        # CG chunk length), picked on this solver's state before anything is timed
+        from karman_taichi_gb300.autotune import CYCLE_CANDIDATES, tune_pressure
+        tuned = tune_pressure(solver, cycles=CYCLE_CANDIDATES)
     ms, recs, launches, ck = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
     summ = summarize(recs)
     value = world * args.steps / (ms * 1e-3)
@@ -439,7 +440,8 @@ def run_gpu(args):
                        "l2": "working set per step > 129 MB L2 (no flush needed)"},
                gpu_launches=launches, clocks=ck)
     if tuned is not None:
-        out["config"]["autotune"] = {k: tuned[k] for k in ("tail", "big_cells", "check_every_p", "ms")}
+        out["config"]["autotune"] = {k: tuned[k] for k in ("nu_coarse", "omega_coarse", "tail", "big_cells",
+                                                           "check_every_p", "ms")}
     out["cell_updates_per_s"] = round(value * cfg.cells, 1)
     out["stats"] = summ
 
@@ -464,6 +466,9 @@ def run_gpu(args):
             have = False
         if have:
             lsol = make_solver(cfg, "learned", dev)
+            if tuned is not None:   # the same p' cycle and launch shapes as the timed run
+                from karman_taichi_gb300.autotune import apply_choice
+                apply_choice(lsol, tuned)
             lms, lrecs, _, _ = timed_steps(lsol, args.steps, args.warmup, 1, lib)
             lsum = summarize(lrecs)
             out["learned"] = {"value": round(args.steps / (lms * 1e-3), 5), "unit": "time steps/s",
@@ -604,8 +609,9 @@ def run_batch(args, cfgs=None, workload=None):
     for key, workers, native in (("native_concurrent", args.batch_workers, True), ("sequential", 1, True)):
         b = BatchedChannels(cfgs, precision=mode, workers=workers)
         if mode == "mixed" and not args.no_autotune:   # per grid size, before anything is timed
-            chosen = b.autotune()
-            out.setdefault("autotune", {k: {f: c[f] for f in ("tail", "big_cells", "check_every_p")}
+            from karman_taichi_gb300.autotune import CYCLE_CANDIDATES
+            chosen = b.autotune(cycles=CYCLE_CANDIDATES)
+            out.setdefault("autotune", {k: {f: c[f] for f in ("nu_coarse", "tail", "big_cells", "check_every_p")}
                                         for k, c in chosen.items()})
         run = b.step_native if native else b.step
         run(args.warmup)

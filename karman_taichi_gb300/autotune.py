@@ -17,6 +17,14 @@ one choice after the other (coordinate descent from the defaults), and keeps
 the fastest.  Every candidate computes the same fields bit for bit: the tail
 and the tile shapes do the same arithmetic per cell, and the convergence test
 runs on the device every iteration, whatever the chunk length.
+
+Optionally (``cycles``) it first picks the iteration schedule of the cycle
+itself: the red-black sweeps on the levels below level 0
+(``Multigrid.opts.nu_coarse``) with the smoother weight that goes with them.
+More sweeps cost more per V-cycle and save CG iterations; which wins depends
+on the grid (on GB300: three sweeps at 2048 x 512 and 4096 x 1024, two at
+320 x 64 and on the random 1024^2 system).  This choice changes the iterates
+-- every candidate still solves to the same tolerance -- so it is opt-in.
 """
 from __future__ import annotations
 
@@ -29,6 +37,9 @@ from .linalg import TAIL_CELLS
 TAIL_CANDIDATES = (0, 384, TAIL_CELLS, 4352)
 BIG_CANDIDATES = (60000, 200000, 600000)
 CHUNK_CANDIDATES = (2, 4, 8)
+# (sweeps on the levels below level 0, their smoother weight): the weight measured best for each
+# sweep count over the channel's p' systems
+CYCLE_CANDIDATES = ((2, 1.5), (3, 1.6))
 
 
 def _solve_ms(solver, reps: int) -> float:
@@ -56,13 +67,32 @@ def _apply(solver, tail: int, big: int, chunk: int) -> None:
     solver._chan = None   # the native descriptor copies these: rebuild it
 
 
+def _apply_cycle(solver, nu: int, omega: float) -> None:
+    """Sweeps and smoother weight of the levels below level 0 (the p' solve's
+    own kc_mg_setup recomputes the weights it derives from them)."""
+    o = solver.mg.opts
+    o.nu_coarse = int(nu)
+    for l in range(1, len(o.omega)):
+        o.omega[l] = float(omega)
+    solver._chan = None
+
+
+def apply_choice(solver, choice: dict) -> None:
+    """Apply a :func:`tune_pressure` result to another solver of the same grid."""
+    if "nu_coarse" in choice:
+        _apply_cycle(solver, choice["nu_coarse"], choice["omega_coarse"])
+    _apply(solver, choice["tail"], choice["big_cells"], choice["check_every_p"])
+
+
 def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDATES,
-                  chunks=CHUNK_CANDIDATES) -> dict:
+                  chunks=CHUNK_CANDIDATES, cycles=None) -> dict:
     """Pick the fastest launch shapes of ``solver``'s p' solve on its current
-    state and apply them.  Runs one outer iteration's stages up to the p'
-    assembly on the solver itself, then puts every field back, so the solver
-    continues exactly as if it had not been tuned.  Returns the choice and
-    the timings (ms per p' solve) behind it."""
+    state and apply them; with ``cycles`` (e.g. CYCLE_CANDIDATES: (nu_coarse,
+    omega below level 0) pairs) first the fastest cycle.  Runs one outer
+    iteration's stages up to the p' assembly on the solver itself, then puts
+    every field back, so the solver continues exactly as if it had not been
+    tuned (bit for bit without ``cycles``).  Returns the choice and the
+    timings (ms per p' solve) behind it."""
     if solver.mg is None:
         raise ValueError("tuning needs the multigrid p' solve (precision='mixed', pcorr_precond='mg')")
     names = ("u", "v", "p", "u0", "v0", "u_mid", "v_mid", "pcor")
@@ -73,6 +103,15 @@ def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDA
         solver.solve_momentum()
         solver.relax()
         solver.assemble_p()
+        o = solver.mg.opts
+        cycle = (int(o.nu_coarse), round(float(o.omega[1]), 6))
+        if cycles:
+            cyc_ms = {}
+            for nu, om in cycles:
+                _apply_cycle(solver, nu, om)
+                cyc_ms[(int(nu), round(float(om), 6))] = _solve_ms(solver, reps)
+            cycle = min(cyc_ms, key=cyc_ms.get)
+            _apply_cycle(solver, *cycle)
         choice = {"tail": int(solver.mg.opts.tail), "big_cells": int(solver.mg.opts.big_cells),
                   "check_every_p": int(solver.check_every_p)}
         timings = {}
@@ -92,9 +131,12 @@ def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDA
                     best_v, best_t = v, t
             choice[field] = best_v
         _apply(solver, choice["tail"], choice["big_cells"], choice["check_every_p"])
-        result = dict(choice, ms=round(timings[(choice["tail"], choice["big_cells"], choice["check_every_p"])], 4),
+        result = dict(choice, nu_coarse=cycle[0], omega_coarse=cycle[1],
+                      ms=round(timings[(choice["tail"], choice["big_cells"], choice["check_every_p"])], 4),
                       tried={f"tail={k[0]},big_cells={k[1]},check_every_p={k[2]}": round(t, 4)
                              for k, t in timings.items()})
+        if cycles:
+            result["tried"].update({f"nu_coarse={k[0]},omega_coarse={k[1]}": round(t, 4) for k, t in cyc_ms.items()})
     finally:
         for k in names:
             getattr(solver, k).copy_(saved[k])

@@ -79,23 +79,21 @@ class BatchedChannels:
                     self.records[k].append(self.solvers[k].step())
             self.streams[k].synchronize()
 
-    def autotune(self, reps=2):
+    def autotune(self, reps=2, cycles=None):
         """Pick the p' solve's launch shapes (multigrid tail, tile sizes, CG chunk
         length; :mod:`karman_taichi_gb300.autotune`) once per grid size: tuned on
         the first instance of each size, applied to every instance of that size.
-        The fields each instance computes do not change.  Returns
-        {"nx x ny": choice}."""
-        from .autotune import tune_pressure
+        The fields each instance computes do not change.  With ``cycles`` the
+        sweeps below level 0 are chosen too (the iterates then change within the
+        solve tolerance).  Returns {"nx x ny": choice}."""
+        from .autotune import apply_choice, tune_pressure
         chosen = {}
         for k, s in enumerate(self.solvers):
             key = f"{s.cfg.nx}x{s.cfg.ny}"
             if key not in chosen:
                 with torch.cuda.stream(self.streams[k]):
-                    chosen[key] = tune_pressure(s, reps=reps)
-            c = chosen[key]
-            s.mg.opts.tail, s.mg.opts.big_cells = c["tail"], c["big_cells"]
-            s.check_every_p = c["check_every_p"]
-            s._chan = None
+                    chosen[key] = tune_pressure(s, reps=reps, cycles=cycles)
+            apply_choice(s, chosen[key])
         torch.cuda.synchronize(self.device)
         return chosen
 

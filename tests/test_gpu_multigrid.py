@@ -330,3 +330,38 @@ def test_autotune_keeps_fields_and_state(dev):
     sa, sb = a.state_numpy(), b.state_numpy()
     for k in ("u", "v", "p"):
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_autotune_cycle_stage(dev):
+    """With cycles the tuner also picks the sweeps below level 0 (and their
+    weight) from its candidates, restores the solver's state, and the tuned
+    solver steps to the untuned solver's fields within the solve tolerance."""
+    import numpy as np
+    from karman_taichi_gb300.autotune import CYCLE_CANDIDATES, apply_choice, tune_pressure
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    cfg = get("channel_320x64")
+    a = ChannelSolver(cfg, device=dev, precision="mixed")
+    b = ChannelSolver(cfg, device=dev, precision="mixed")
+    a.step(); b.step()
+    before = a.state_numpy()
+    c = tune_pressure(a, reps=1, cycles=CYCLE_CANDIDATES)
+    assert (c["nu_coarse"], c["omega_coarse"]) in [(n, round(w, 6)) for n, w in CYCLE_CANDIDATES]
+    assert a.mg.opts.nu_coarse == c["nu_coarse"] and abs(a.mg.opts.omega[3] - c["omega_coarse"]) < 1e-6
+    assert sum(k.startswith("nu_coarse=") for k in c["tried"]) == len(CYCLE_CANDIDATES)
+    after = a.state_numpy()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
+    # every candidate cycle steps to the same fields within the solve tolerance
+    d = ChannelSolver(cfg, device=dev, precision="mixed")
+    d.step()
+    apply_choice(d, dict(c, nu_coarse=3, omega_coarse=1.6))
+    for _ in range(2):   # (this early transient of the 320 x 64 case runs the 50 outer iterations)
+        ra, rb, rd = a.step(), b.step(), d.step()
+        for r in (ra, rd):
+            assert abs(r[-1]["mass"] - rb[-1]["mass"]) <= 1e-4 * rb[-1]["mass"]
+    sb = b.state_numpy()
+    for s in (a, d):
+        st = s.state_numpy()
+        for k in ("u", "v", "p"):
+            assert np.abs(st[k] - sb[k]).max() <= 1e-5 * np.abs(sb[k]).max(), k
