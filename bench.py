@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="channel_2048x512")
     ap.add_argument("--mode", default="auto", choices=["auto", "fp64", "mixed", "learned"])
+    ap.add_argument("--momentum", default="bicgstab", choices=["bicgstab", "rbgs_refined", "rbgs"],
+                    help="momentum solver of the mixed path (ChannelSolver(momentum=...))")
     ap.add_argument("--compare-steps", type=int, default=2, help="timed steps of the FP64 plain comparison run")
     ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -154,12 +156,14 @@ def max_over_ranks(x, world):
 
 
 # ---------------------------------------------------------------------------------------------
-def make_solver(cfg, mode, dev):
+def make_solver(cfg, mode, dev, momentum="bicgstab"):
     from karman_taichi_gb300.channel import ChannelSolver
     if mode == "learned":
         from karman_taichi_gb300 import learned
         return learned.make_channel_solver(cfg, dev)
-    return ChannelSolver(cfg, device=dev, precision="fp64" if mode == "fp64" else "mixed")
+    if mode == "fp64":
+        return ChannelSolver(cfg, device=dev, precision="fp64")
+    return ChannelSolver(cfg, device=dev, precision="mixed", momentum=momentum)
 
 
 def resolve_mode(mode, config="channel_2048x512"):
@@ -420,7 +424,7 @@ def run_gpu(args):
     out = {"metric": METRIC, "unit": "time steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None}
 
-    solver = make_solver(cfg, mode, dev)
+    solver = make_solver(cfg, mode, dev, args.momentum)
     tuned = None
     if mode == "mixed" and not args.no_autotune:
         # the p' solve's cycle (sweeps below level 0) and launch shapes (multigrid tail, tile sizes,

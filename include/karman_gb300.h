@@ -160,6 +160,14 @@ size_t kc_refined_ws_bytes(long long n, int stride);
 int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b,
                         double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
                         double eps_inner, int max_refine, kc_solve_info* info, void* stream);
+/* The same refinement with FP32 red-black Gauss-Seidel sweeps as the inner
+ * solver (the Gauss-Seidel counterpart of the reference's Jacobi solves,
+ * pressure_valid.py:192-233): each sweep costs a fraction of a BiCGSTAB
+ * iteration, for diagonally dominant systems such as the momentum rows.
+ * info->iters counts sweeps.  Workspace: kc_refined_ws_bytes. */
+int kc_rbgs_refined(const kc_system* A64, const kc_system* A32, const double* b,
+                    double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
+                    double eps_inner, int max_refine, kc_solve_info* info, void* stream);
 
 /* One Jacobi sweep (FP64, standard form): x_mid = (b - sum_nb a_nb x_nb) / aP,
  * y = (1 - omega) x + omega x_mid on the cells (i, j) of the [n/stride][stride]
@@ -416,9 +424,12 @@ int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, c
  * precision KC_F64: the plain method (every solve FP64 BiCGSTAB, cold start,
  * rel. tol eps, cap n); KC_F32: the accelerated path (momentum:
  * KC_MOMENTUM_BICGSTAB, FP32 BiCGSTAB in FP64 refinement, inner tol
- * eps_inner, or KC_MOMENTUM_RBGS, FP64 red-black Gauss-Seidel (kc_rbgs) with
- * the refined BiCGSTAB as fallback, both from the previous outer iteration's
- * u*, v* to ||b - A x|| / ||b|| < eps; p': multigrid CG in FP64 refinement
+ * eps_inner; KC_MOMENTUM_RBGS_REFINED, FP32 red-black Gauss-Seidel in FP64
+ * refinement (kc_rbgs_refined, inner tol 1e-5, at most 200 sweeps); or
+ * KC_MOMENTUM_RBGS, FP64 red-black Gauss-Seidel (kc_rbgs, at most 200
+ * sweeps); the Gauss-Seidel variants hand over to the refined BiCGSTAB if
+ * they miss eps; all from the previous outer iteration's u*, v* to
+ * ||b - A x|| / ||b|| < eps; p': multigrid CG in FP64 refinement
  * on coef_p32 in Laplacian form, inner tol eps_inner_p, with the plain FP64
  * BiCGSTAB as fallback).  Workspaces: ws_u / ws_v of kc_bicgstab_ws_bytes
  * (F64) or the larger of kc_refined_ws_bytes and kc_rbgs_ws_bytes (F32)
@@ -427,11 +438,12 @@ int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, c
  * kc_reduce_ws_bytes. */
 #define KC_MOMENTUM_BICGSTAB 0
 #define KC_MOMENTUM_RBGS 1
+#define KC_MOMENTUM_RBGS_REFINED 2
 typedef struct {
     kc_phys phys;                       /* mode must be KC_MODE_CHANNEL */
     int precision, max_outer, use_graph;
     int persistent;                     /* 1: BiCGSTAB solves as one cooperative launch, 0: graph chunks */
-    int momentum;                       /* KC_F32 momentum solver: KC_MOMENTUM_BICGSTAB or KC_MOMENTUM_RBGS */
+    int momentum;                       /* KC_F32 momentum solver: KC_MOMENTUM_* */
     int check_every_p;                  /* KC_F32 p' solve: CG iterations per graph chunk between checks (0: 4) */
     double mass_tol, eps, eps_inner, eps_inner_p;
     double *u, *v, *p, *u0, *v0, *pcor, *u_mid, *v_mid;

@@ -64,7 +64,7 @@ class KcPhys(C.Structure):
                 ("alpha_m", C.c_double), ("alpha_u", C.c_double), ("alpha_p", C.c_double)]
 
 
-MOMENTUM_BICGSTAB, MOMENTUM_RBGS = 0, 1
+MOMENTUM_BICGSTAB, MOMENTUM_RBGS, MOMENTUM_RBGS_REFINED = 0, 1, 2
 
 
 class KcMgOpts(C.Structure):
@@ -130,6 +130,8 @@ SIGNATURES = {
     "kc_rbgs": (I_, [C.POINTER(KcSystem), P_, P_, P_, S_, C.POINTER(KcSolveOpts), C.POINTER(KcSolveInfo), P_]),
     "kc_bicgstab_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
                                  C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
+    "kc_rbgs_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, S_,
+                             C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
     "kc_mg_default_opts": (None, [C.POINTER(KcMgOpts)]),
     "kc_mg_ws_bytes": (S_, [L_, I_, C.POINTER(KcMgOpts)]),
     "kc_mg_setup": (I_, [C.POINTER(KcSystem), P_, S_, C.POINTER(KcMgOpts), P_]),

@@ -36,11 +36,14 @@ from . import _lib as L
 from . import geometry
 from .config import ChannelConfig
 from .linalg import (Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_refined, ptr, rbgs,
-                     stream_handle)
+                     rbgs_refined, stream_handle)
 
 
 # sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
 MOMENTUM_SWEEPS = 200
+# inner tolerance of the FP32 Gauss-Seidel sweeps of the momentum refinement: one pass from the
+# previous outer iteration's u*, v* usually meets the 1e-8 target
+EPS_INNER_GS = 1e-5
 
 
 class ChannelSolver:
@@ -48,15 +51,17 @@ class ChannelSolver:
                  eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4, native=True,
                  momentum="bicgstab"):
         """``momentum`` (mixed precision): "bicgstab", FP32 BiCGSTAB in FP64
-        refinement, or "rbgs", FP64 red-black Gauss-Seidel with the refined
-        BiCGSTAB as fallback (on GB300 an FP64 sweep is bound by the FP64
-        pipe, ~56 us at 2048 x 512, and 9-13 sweeps from the warm start cost
-        more than the refined BiCGSTAB); the FP64 path always uses the
-        reference's BiCGSTAB."""
+        refinement; "rbgs_refined", FP32 red-black Gauss-Seidel sweeps in FP64
+        refinement; or "rbgs", FP64 red-black Gauss-Seidel (on GB300 an FP64
+        sweep is bound by the FP64 pipe, ~56 us at 2048 x 512, and 9-13 sweeps
+        from the warm start cost more than the refined BiCGSTAB).  Both
+        Gauss-Seidel variants hand over to the refined BiCGSTAB, from where
+        they stopped, if they miss the tolerance.  The FP64 path always uses
+        the reference's BiCGSTAB."""
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
-        if momentum not in ("rbgs", "bicgstab"):
-            raise ValueError("momentum must be 'rbgs' or 'bicgstab'")
+        if momentum not in ("rbgs", "rbgs_refined", "bicgstab"):
+            raise ValueError("momentum must be 'rbgs', 'rbgs_refined' or 'bicgstab'")
         self.cfg, self.precision, self.use_graph = cfg, precision, use_graph
         self.momentum = momentum if precision == "mixed" else "bicgstab"
         self.eps_inner, self.eps_inner_p = eps_inner, eps_inner_p
@@ -149,7 +154,14 @@ class ChannelSolver:
         # warm start from the previous outer iteration's u*, v* (karman_taichi.py:362-371 warm-starts too);
         # the stopping test is ||b - A x|| / ||b|| < eps, the reference's test for a cold start
         before = 0
-        if self.momentum == "rbgs":
+        if self.momentum == "rbgs_refined":
+            info = rbgs_refined(A, A32, b, x, eps=cfg.eps, eps_inner=EPS_INNER_GS, max_iter=MOMENTUM_SWEEPS, ws=ws,
+                                use_graph=self.use_graph, warm=True)
+            if info.ok:
+                return info
+            self.fallbacks += 1   # the refined BiCGSTAB takes over from where Gauss-Seidel stopped
+            before = info.iters
+        elif self.momentum == "rbgs":
             info = rbgs(A, b, x, eps=cfg.eps, max_iter=MOMENTUM_SWEEPS, warm=True, rel_to_b=True, ws=ws,
                         use_graph=self.use_graph)
             if info.ok:
@@ -232,7 +244,8 @@ class ChannelSolver:
         c.phys = self.phys
         c.precision = L.F64 if self.precision == "fp64" else L.F32
         c.max_outer, c.use_graph, c.persistent = self.cfg.max_outer, int(self.use_graph), int(self.persistent)
-        c.momentum = L.MOMENTUM_RBGS if self.momentum == "rbgs" else L.MOMENTUM_BICGSTAB
+        c.momentum = {"rbgs": L.MOMENTUM_RBGS, "rbgs_refined": L.MOMENTUM_RBGS_REFINED}.get(self.momentum,
+                                                                                       L.MOMENTUM_BICGSTAB)
         c.check_every_p = int(self.check_every_p)
         c.mass_tol, c.eps, c.eps_inner, c.eps_inner_p = self.cfg.mass_tol, self.cfg.eps, self.eps_inner, self.eps_inner_p
         for k in ("u", "v", "p", "u0", "v0", "pcor", "u_mid", "v_mid", "solid", "coef_u", "b_u", "coef_v", "b_v",

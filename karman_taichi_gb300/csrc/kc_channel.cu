@@ -36,8 +36,10 @@ kc_system sys_of(long long NX, long long NY, const void* coef, int dtype, int fo
     return A;
 }
 
-// sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
+// sweeps the Gauss-Seidel momentum solves may take before the refined BiCGSTAB takes over
 constexpr long long kMomentumSweeps = 200;
+// inner tolerance of the FP32 Gauss-Seidel sweeps of the refined momentum solve
+constexpr double kEpsInnerGs = 1e-5;
 
 kc_solve_opts opts_of(double eps, long long max_iter, int rel_to, int check_every, int use_graph, int persistent) {
     kc_solve_opts o{};
@@ -65,7 +67,16 @@ int solve_sys(const kc_channel* c, const kc_system& A64, const kc_system& A32, c
         return kc_bicgstab(&A64, b, x, nullptr, ws, ws_bytes, &o, info, s);
     }
     long long before = 0;
-    if (c->momentum == KC_MOMENTUM_RBGS) {
+    if (c->momentum == KC_MOMENTUM_RBGS_REFINED) {
+        // FP32 red-black Gauss-Seidel sweeps in FP64 refinement from the previous outer
+        // iteration's u*, v*; the refined BiCGSTAB takes over, from where they stopped, if they miss eps
+        kc_solve_opts og = opts_of(c->eps, kMomentumSweeps, KC_REL_R0, 0, c->use_graph, 0);
+        og.x0 = KC_X0_WARM;
+        const int rc = kc_rbgs_refined(&A64, &A32, b, x, ws, ws_bytes, &og, kEpsInnerGs, 30, info, s);
+        if (rc < 0 || info->status == KC_OK) return rc;
+        before = info->iters;
+        *fell_back = true;
+    } else if (c->momentum == KC_MOMENTUM_RBGS) {
         // red-black Gauss-Seidel from the previous outer iteration's u*, v*; the
         // refined BiCGSTAB takes over, from where it stopped, if it misses eps
         kc_solve_opts og = opts_of(c->eps, kMomentumSweeps, KC_REL_B, 0, c->use_graph, 0);
@@ -90,7 +101,8 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
     if (!c) return set_error("kc_channel_step: null channel"), KC_ERR_ARG;
     if (c->phys.mode != KC_MODE_CHANNEL) return set_error("kc_channel_step: phys.mode must be KC_MODE_CHANNEL"), KC_ERR_ARG;
     if (c->precision != KC_F64 && c->precision != KC_F32) return set_error("kc_channel_step: bad precision"), KC_ERR_ARG;
-    if (c->momentum != KC_MOMENTUM_BICGSTAB && c->momentum != KC_MOMENTUM_RBGS)
+    if (c->momentum != KC_MOMENTUM_BICGSTAB && c->momentum != KC_MOMENTUM_RBGS &&
+        c->momentum != KC_MOMENTUM_RBGS_REFINED)
         return set_error("kc_channel_step: bad momentum solver %d", c->momentum), KC_ERR_ARG;
     const bool mixed = c->precision == KC_F32;
     if (mixed && (!c->coef_u32 || !c->coef_v32 || !c->coef_p32 || !c->b_u32 || !c->b_v32 || !c->b_p32 || !c->mg_ws))

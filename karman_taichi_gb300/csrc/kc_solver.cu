@@ -2189,6 +2189,8 @@ int kc_cg(const kc_system* A, const void* b, void* x, void* ws, size_t ws_bytes,
 // weights 1/d are formed once per solve, each update is one FMA.
 namespace kc {
 constexpr int kGsTI = 16, kGsAJ = 32, kGsRY = 8, kGsTJ = kGsAJ - 4, kGsNT = kGsAJ * kGsRY, kGsAI = kGsTI + 4;
+// sweeps per captured graph of the inner FP32 Gauss-Seidel solve (sweeps after convergence return at once)
+constexpr int kRbgsInnerChunk = 8;
 constexpr int kGsR1 = (kGsTI + 2 + kGsRY - 1) / kGsRY;   // rows of phase 1 per thread (owned + 1-ring)
 constexpr int kGsR2 = (kGsTI + kGsRY - 1) / kGsRY;       // rows of phase 2 per thread (owned)
 
@@ -2196,33 +2198,21 @@ __device__ __forceinline__ void cp_async8(double* smem, const double* gmem, bool
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 8 : 0) : "memory");
 }
-
-__device__ __forceinline__ double gs_ax(const Coef<double>& A, int k, double xc, double xw, double xe, double xn,
-                                        double xs) {
-    double y = A.at(0, k) * xc;
-    if (A.lap) {
-        y = fma(A.at(1, k), xw - xc, y);
-        y = fma(A.at(2, k), xe - xc, y);
-        y = fma(A.at(3, k), xn - xc, y);
-        y = fma(A.at(4, k), xs - xc, y);
-    } else {
-        y = fma(A.at(1, k), xw, y);
-        y = fma(A.at(2, k), xe, y);
-        y = fma(A.at(3, k), xn, y);
-        y = fma(A.at(4, k), xs, y);
-    }
-    return y;
-}
+__device__ __forceinline__ void cp_async_t(double* smem, const double* gmem, bool valid) { cp_async8(smem, gmem, valid); }
+__device__ __forceinline__ void cp_async_t(float* smem, const float* gmem, bool valid) { cp_async4(smem, gmem, valid); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
 // weights 1/d (0 on rows with a zero diagonal) and (b, b)
-__global__ void __launch_bounds__(kPwThreads) k_rbgs_init(Coef<double> A, int n, const double* __restrict__ b,
-                                                          double* __restrict__ winv, BicgPtrs P, StartArgs sa) {
-    Acc<double> acc[1];
+template <typename T>
+__global__ void __launch_bounds__(kPwThreads) k_rbgs_init(Coef<T> A, int n, const T* __restrict__ b,
+                                                          T* __restrict__ winv, BicgPtrs P, StartArgs sa) {
+    Acc<T> acc[1];
     KC_PW_LOOP(n, {
-        double d = A.at(0, k);
+        T d = A.at(0, k);
         if (A.lap) d = d - (((A.at(1, k) + A.at(2, k)) + A.at(3, k)) + A.at(4, k));
-        winv[k] = d != 0.0 ? 1.0 / d : 0.0;
-        const double bk = __ldg(b + k);
+        winv[k] = d != T(0) ? T(1) / d : T(0);
+        const T bk = __ldg(b + k);
         acc[0].add(bk, bk);
     })
     double s[1];
@@ -2265,51 +2255,86 @@ __device__ __forceinline__ void gs_finish(SolverState* st, double rr) {
     }
 }
 
-__global__ void __launch_bounds__(kGsNT) k_rbgs_sweep(Coef<double> A, Geo g, const double* __restrict__ b,
-                                                      const double* __restrict__ winv, double* __restrict__ x0,
-                                                      double* __restrict__ x1, BicgPtrs P) {
+// One sweep over a 16 x 28 tile: x, b, the weights and the five coefficients of
+// the tile and its 2-cell halo are staged together by cp.async (every load of
+// the sweep in flight at once; read from global memory phase by phase the
+// sweep waited on memory latency twice), then both half-sweeps run from
+// shared memory.
+template <typename T>
+__global__ void __launch_bounds__(kGsNT) k_rbgs_sweep(Coef<T> A, Geo g, const T* __restrict__ b,
+                                                      const T* __restrict__ winv, T* __restrict__ x0,
+                                                      T* __restrict__ x1, BicgPtrs P) {
     SolverState* st = P.st;
     if (solver_done(st)) return;
     const bool odd = (__ldcg(&st->iter) & 1) != 0;   // set by the previous launch: the same in every block
-    const double* __restrict__ x = odd ? x1 : x0;
-    double* __restrict__ xo = odd ? x0 : x1;
-    __shared__ __align__(16) double sx[kGsAI][kGsAJ];
+    const T* __restrict__ x = odd ? x1 : x0;
+    T* __restrict__ xo = odd ? x0 : x1;
+    __shared__ __align__(16) T sx[kGsAI][kGsAJ];
+    __shared__ __align__(16) T sb[kGsAI][kGsAJ];
+    __shared__ __align__(16) T sw[kGsAI][kGsAJ];
+    __shared__ __align__(16) T sc[5][kGsAI][kGsAJ];
     const int n = g.n, S = g.S;
     const int i0 = blockIdx.y * kGsTI, j0 = blockIdx.x * kGsTJ;
     const int tx = threadIdx.x & (kGsAJ - 1), ty = threadIdx.x / kGsAJ;
     for (int a = ty; a < kGsAI; a += kGsRY) {
         const long long kl = (long long)(i0 + a - 2) * S + (j0 + tx - 2);
         const bool in = kl >= 0 && kl < n;
-        cp_async8(&sx[a][tx], x + (in ? kl : 0), in);
+        const long long kk = in ? kl : 0;
+        cp_async_t(&sx[a][tx], x + kk, in);
+        cp_async_t(&sb[a][tx], b + kk, in);
+        cp_async_t(&sw[a][tx], winv + kk, in);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) cp_async_t(&sc[q][a][tx], A.c + q * A.cs + kk * A.es, in);
     }
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
+    // (A x) at staged position (a, t): diagonal first, then W, E, N, S by FMA
+    auto ax = [&](int a, int t) -> T {
+        const T xc = sx[a][t];
+        T y = sc[0][a][t] * xc;
+        if (A.lap) {
+            y = fma_t(sc[1][a][t], sx[a - 1][t] - xc, y);
+            y = fma_t(sc[2][a][t], sx[a + 1][t] - xc, y);
+            y = fma_t(sc[3][a][t], sx[a][t + 1] - xc, y);
+            y = fma_t(sc[4][a][t], sx[a][t - 1] - xc, y);
+        } else {
+            y = fma_t(sc[1][a][t], sx[a - 1][t], y);
+            y = fma_t(sc[2][a][t], sx[a + 1][t], y);
+            y = fma_t(sc[3][a][t], sx[a][t + 1], y);
+            y = fma_t(sc[4][a][t], sx[a][t - 1], y);
+        }
+        return y;
+    };
     const int j = j0 + tx - 2;
     const bool jown = tx >= 2 && tx < kGsTJ + 2 && j < S;
     // phase 1: residual of the incoming x (owned cells), new red values (owned cells and 1-ring)
-    Acc<double> acc[1];
-    double xr[kGsR1];
+    Acc<T> acc[1];
+    T xr[kGsR1];
     bool wr[kGsR1];
 #pragma unroll
     for (int m = 0; m < kGsR1; ++m) {
         const int a = 1 + ty + kGsRY * m;
         wr[m] = false;
-        xr[m] = 0.0;
+        xr[m] = T(0);
         if (a > kGsTI + 2 || tx < 1 || tx > kGsAJ - 2) continue;
         const int i = i0 + a - 2;
         const long long kl = (long long)i * S + j;
         if (kl < 0 || kl >= n) continue;
         // a staged position past the end of a row holds the flat cell kl of the next
         // (previous) row; its neighbours are staged around it, so it is updated there
-        // too, with the colour of its own (row, column)
-        const int k = (int)kl;
-        const int colour = (j >= 0 && j < S) ? ((i + j) & 1) : (int)(((kl / S) + (kl % S)) & 1);
-        const double xc = sx[a][tx];
-        const double r = __ldg(b + k) - gs_ax(A, k, xc, sx[a - 1][tx], sx[a + 1][tx], sx[a][tx + 1], sx[a][tx - 1]);
+        // too, with the colour of its own (row, column).  (kl < n < 2^31: 32-bit division,
+        // and only on those positions -- a 64-bit division per cell dominated the sweep.)
+        int colour = (i + j) & 1;
+        if (j < 0 || j >= S) {
+            const int kk = (int)kl, row = kk / S;
+            colour = (row + (kk - row * S)) & 1;
+        }
+        const T xc = sx[a][tx];
+        const T r = sb[a][tx] - ax(a, tx);
         if (jown && a >= 2 && a < kGsTI + 2) acc[0].add(r, r);
         if (colour == 0) {
-            xr[m] = fma(__ldg(winv + k), r, xc);
+            xr[m] = fma_t(sw[a][tx], r, xc);
             wr[m] = true;
         }
     }
@@ -2326,13 +2351,9 @@ __global__ void __launch_bounds__(kGsNT) k_rbgs_sweep(Coef<double> A, Geo g, con
         const int i = i0 + a - 2;
         const long long kl = (long long)i * S + j;
         if (kl >= n) continue;
-        const int k = (int)kl;
-        double xc = sx[a][tx];
-        if (((i + j) & 1) != 0)
-            xc = fma(__ldg(winv + k), __ldg(b + k) - gs_ax(A, k, xc, sx[a - 1][tx], sx[a + 1][tx], sx[a][tx + 1],
-                                                          sx[a][tx - 1]),
-                     xc);
-        xo[k] = xc;
+        T xc = sx[a][tx];
+        if (((i + j) & 1) != 0) xc = fma_t(sw[a][tx], sb[a][tx] - ax(a, tx), xc);
+        xo[kl] = xc;
     }
     double s[1];
     if (block_partials<1>(acc, P.partials, P.ld, block_id(), block_count(), &st->ticket[0], s) && threadIdx.x == 0) {
@@ -2350,7 +2371,8 @@ struct GsLayout {
     size_t off_state, off_partials, off_winv, off_x1, total;
     int ld;
 };
-static GsLayout gs_layout(long long n, int S) {
+// elem: bytes per vector element (8 for the FP64 solver, 4 for the FP32 inner solve of the refinement)
+static GsLayout gs_layout(long long n, int S, size_t elem = sizeof(double)) {
     GsLayout L{};
     const dim3 g = gs_grid(n, std::max(S, 1));
     const int nb = std::max<int>((int)(g.x * g.y), pw_blocks(n));
@@ -2361,11 +2383,57 @@ static GsLayout gs_layout(long long n, int S) {
     L.off_partials = off;
     off = align256(off + (size_t)L.ld * sizeof(double));
     L.off_winv = off;
-    off = align256(off + (size_t)n * sizeof(double));
+    off = align256(off + (size_t)n * elem);
     L.off_x1 = off;
-    off = align256(off + (size_t)n * sizeof(double));
+    off = align256(off + (size_t)n * elem);
     L.total = off;
     return L;
+}
+
+// Red-black Gauss-Seidel sweeps of A x = b (T = double: the FP64 solver; T = float: the
+// inner solve of kc_rbgs_refined) until the residual of the incoming iterate meets o->eps,
+// o->max_iter sweeps, or a non-finite residual.  Checked by the caller: A's dtype is T.
+template <typename T>
+static int rbgs_run(const kc_system* A, const T* b, T* x, void* ws, size_t ws_bytes, const kc_solve_opts* o,
+                    kc_solve_info* info, cudaStream_t s) {
+    const dim3 sg = gs_grid(A->n, A->stride);
+    if (sg.y > 65535u) return set_error("kc_rbgs: %lld rows of stride %d exceed the launch grid", A->n, A->stride),
+                              KC_ERR_ARG;
+    const GsLayout L = gs_layout(A->n, A->stride, sizeof(T));
+    if (!ws || ws_bytes < L.total) return set_error("kc_rbgs: workspace %zu < %zu", ws_bytes, L.total), KC_ERR_WORKSPACE;
+    char* base = (char*)ws;
+    BicgPtrs P{(SolverState*)(base + L.off_state), (double*)(base + L.off_partials), L.ld};
+    T* winv = (T*)(base + L.off_winv);
+    T* x1 = (T*)(base + L.off_x1);
+    const int pb = pw_blocks(A->n);
+    const Coef<T> C = coef_of<T>(A);
+    const Geo g{(int)A->n, A->stride};
+    KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
+    if (o->x0 != KC_X0_WARM) KC_CUDA(cudaMemsetAsync(x, 0, (size_t)A->n * sizeof(T), s));   // all-zero bits: +0
+    const StartArgs sa{o->eps, o->max_iter, 0, o->rel_to, o->history, o->history ? o->history_len : 0, 1e300};
+    k_rbgs_init<T><<<pb, kPwThreads, 0, s>>>(C, (int)A->n, b, winv, P, sa);
+    KC_LAUNCH_CHECK("k_rbgs_init");
+    GraphKey key{ws, A->coef, x, A->n, A->stride, sizeof(T) == 8 ? KC_F64 : KC_F32, 0, 16, 9, A->cs, A->es};
+    key.form = A->form;
+    key.b = b;
+    HostState h{};
+    int rc = drive(o, key, P.st,
+                   [&](int m, cudaStream_t ss) {
+                       for (int q = 0; q < m; ++q) k_rbgs_sweep<T><<<sg, kGsNT, 0, ss>>>(C, g, b, winv, x, x1, P);
+                   },
+                   &h, s, 1);
+    if (rc) return rc;
+    if (h.iter & 1) {   // an odd number of sweeps left the iterate in the copy
+        KC_CUDA(cudaMemcpyAsync(x, x1, (size_t)A->n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    }
+    if (info) {
+        info->status = h.status;
+        info->refinements = 0;
+        info->iters = h.iter;
+        info->rel_res = h.prev_rel;
+        info->r0 = sqrt(h.r0Tr);
+    }
+    return h.status;
 }
 }  // namespace kc
 
@@ -2383,48 +2451,7 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
     if (A->dtype != KC_F64) return set_error("kc_rbgs: the system must be FP64"), KC_ERR_ARG;
     if (!b || !x || !o) return set_error("kc_rbgs: null b, x or opts"), KC_ERR_ARG;
     if (o->precond != KC_PRECOND_NONE) return set_error("kc_rbgs: no preconditioner applies"), KC_ERR_ARG;
-    const dim3 sg = gs_grid(A->n, A->stride);
-    if (sg.y > 65535u) return set_error("kc_rbgs: %lld rows of stride %d exceed the launch grid", A->n, A->stride),
-                              KC_ERR_ARG;
-    const GsLayout L = gs_layout(A->n, A->stride);
-    if (!ws || ws_bytes < L.total) return set_error("kc_rbgs: workspace %zu < %zu", ws_bytes, L.total), KC_ERR_WORKSPACE;
-    cudaStream_t s = as_stream(stream);
-    char* base = (char*)ws;
-    BicgPtrs P{(SolverState*)(base + L.off_state), (double*)(base + L.off_partials), L.ld};
-    double* winv = (double*)(base + L.off_winv);
-    double* x1 = (double*)(base + L.off_x1);
-    const int pb = pw_blocks(A->n);
-    const Coef<double> C = coef_of<double>(A);
-    const Geo g{(int)A->n, A->stride};
-    KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
-    if (o->x0 != KC_X0_WARM) k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)A->n, x);
-    const StartArgs sa{o->eps, o->max_iter, 0, o->rel_to, o->history, o->history ? o->history_len : 0, 1e300};
-    k_rbgs_init<<<pb, kPwThreads, 0, s>>>(C, (int)A->n, b, winv, P, sa);
-    KC_LAUNCH_CHECK("k_rbgs_init");
-    count_launches(o->x0 != KC_X0_WARM ? 2 : 1);
-    GraphKey key{ws, A->coef, x, A->n, A->stride, KC_F64, 0, 16, 9, A->cs, A->es};
-    key.form = A->form;
-    key.b = b;
-    HostState h{};
-    rc = drive(o, key, P.st,
-               [&](int m, cudaStream_t ss) {
-                   for (int q = 0; q < m; ++q) k_rbgs_sweep<<<sg, kGsNT, 0, ss>>>(C, g, b, winv, x, x1, P);
-               },
-               &h, s, 1);
-    if (rc) return rc;
-    if (h.iter & 1) {   // an odd number of sweeps left the iterate in the copy
-        k_copy_f64<<<pb, kPwThreads, 0, s>>>((int)A->n, x1, x);
-        KC_LAUNCH_CHECK("kc_rbgs result");
-        count_launches(1);
-    }
-    if (info) {
-        info->status = h.status;
-        info->refinements = 0;
-        info->iters = h.iter;
-        info->rel_res = h.prev_rel;
-        info->r0 = sqrt(h.r0Tr);
-    }
-    return h.status;
+    return rbgs_run<double>(A, b, x, ws, ws_bytes, o, info, as_stream(stream));
 }
 
 }  // extern "C"
@@ -2508,8 +2535,8 @@ static RefineLayout refine_layout(long long n, int S) {
     off = align256(off + (size_t)n * 4);
     L.off_d32 = off;
     off = align256(off + (size_t)n * 4);
-    L.off_inner = off;
-    L.inner_bytes = bicg_layout(n, S, KC_F32).total;
+    L.off_inner = off;   // the inner FP32 solver's workspace: BiCGSTAB or red-black Gauss-Seidel
+    L.inner_bytes = std::max(bicg_layout(n, S, KC_F32).total, gs_layout(n, S, sizeof(float)).total);
     off = align256(off + L.inner_bytes);
     L.total = off;
     return L;
@@ -2520,19 +2547,26 @@ size_t kc_refined_ws_bytes(long long n, int stride) {
     return refine_layout(n, stride).total;
 }
 
-int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, void* ws,
-                        size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine,
-                        kc_solve_info* info, void* stream) {
+}  // extern "C"
+
+// FP64 iterative refinement around an FP32 inner solver: r = b - A64 x in FP64 (and its
+// FP32 copy), inner(io, info, r32, d32, inner workspace, bytes, stream) solves A32 d = r32
+// from d = 0 to io.eps relative to ||r32||, x += d; repeated until ||b - A64 x|| / ||b|| <
+// o->eps.  A sweep that raised the true residual is undone.
+template <class Inner>
+static int refined_core(const char* who, const kc_system* A64, const kc_system* A32, const double* b, double* x,
+                        void* ws, size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine,
+                        kc_solve_info* info, void* stream, Inner inner) {
     int rc = check_system(A64);
     if (rc) return rc;
     rc = check_system(A32);
     if (rc) return rc;
     if (A64->dtype != KC_F64 || A32->dtype != KC_F32 || A64->n != A32->n || A64->stride != A32->stride)
-        return set_error("kc_bicgstab_refined: need matching FP64 and FP32 systems"), KC_ERR_ARG;
-    if (!b || !x || !o) return set_error("kc_bicgstab_refined: null argument"), KC_ERR_ARG;
+        return set_error("%s: need matching FP64 and FP32 systems", who), KC_ERR_ARG;
+    if (!b || !x || !o) return set_error("%s: null argument", who), KC_ERR_ARG;
     RefineLayout L = refine_layout(A64->n, A64->stride);
     if (!ws || ws_bytes < L.total)
-        return set_error("kc_bicgstab_refined: workspace %zu < %zu", ws_bytes, L.total), KC_ERR_WORKSPACE;
+        return set_error("%s: workspace %zu < %zu", who, ws_bytes, L.total), KC_ERR_WORKSPACE;
     cudaStream_t s = as_stream(stream);
     char* base = (char*)ws;
     BicgPtrs P{(SolverState*)(base + L.off_state), (double*)(base + L.off_partials), L.ld};
@@ -2602,7 +2636,7 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         io.max_iter = o->max_iter - total;
         io.eps = std::max(eps_inner, 0.5 * o->eps / rel);   // no deeper than the target needs
         kc_solve_info ii{};
-        int r2 = kc_bicgstab(A32, r32, d32, nullptr, base + L.off_inner, L.inner_bytes, &io, &ii, stream);
+        int r2 = inner(io, &ii, r32, d32, base + L.off_inner, L.inner_bytes, stream);
         if (r2 < 0) return r2;
         total += ii.iters;
         ++sweeps;
@@ -2627,6 +2661,29 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
         info->r0 = sqrt(bb);
     }
     return status;
+}
+
+extern "C" {
+
+int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, void* ws,
+                        size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine,
+                        kc_solve_info* info, void* stream) {
+    return refined_core("kc_bicgstab_refined", A64, A32, b, x, ws, ws_bytes, o, eps_inner, max_refine, info, stream,
+                        [&](const kc_solve_opts& io, kc_solve_info* ii, const float* r, float* d, void* iw,
+                            size_t ib, void* st) { return kc_bicgstab(A32, r, d, nullptr, iw, ib, &io, ii, st); });
+}
+
+int kc_rbgs_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, void* ws,
+                    size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine, kc_solve_info* info,
+                    void* stream) {
+    return refined_core("kc_rbgs_refined", A64, A32, b, x, ws, ws_bytes, o, eps_inner, max_refine, info, stream,
+                        [&](const kc_solve_opts& io, kc_solve_info* ii, const float* r, float* d, void* iw,
+                            size_t ib, void* st) {
+                            kc_solve_opts g = io;
+                            g.persistent = 0;
+                            g.check_every = kRbgsInnerChunk;   // graph-captured chunks of sweeps
+                            return rbgs_run<float>(A32, r, d, iw, ib, &g, ii, as_stream(st));
+                        });
 }
 
 }  // extern "C"

@@ -273,6 +273,27 @@ def bicgstab_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tenso
     return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)
 
 
+def rbgs_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *, eps=1e-8,
+                 eps_inner=1e-5, max_refine=30, max_iter=None, ws: Workspace | None = None,
+                 use_graph=True, warm=False) -> SolveInfo:
+    """FP64-residual iterative refinement around FP32 red-black Gauss-Seidel
+    sweeps (``iters`` counts sweeps); stops when ||b - A64 x|| / ||b|| < eps.
+    For diagonally dominant systems (the momentum rows)."""
+    require_cuda(b, x)
+    if A64.dtype != L.F64 or A32.dtype != L.F32:
+        raise TypeError("rbgs_refined needs an FP64 and an FP32 operator")
+    lib = L.load()
+    nbytes = lib.kc_refined_ws_bytes(A64.n, A64.stride)
+    buf = (ws or Workspace(b.device)).get(nbytes)
+    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_WARM if warm else L.X0_ZERO,
+              L.PRECOND_NONE, 0, L.REL_R0, 0, use_graph, None, False)
+    info = L.KcSolveInfo()
+    rc = lib.kc_rbgs_refined(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x), ptr(buf), buf.numel(),
+                             C.byref(o), float(eps_inner), int(max_refine), C.byref(info), stream_handle(b.device))
+    L.check(rc, "kc_rbgs_refined")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements)
+
+
 TAIL_CELLS = 1536   # default: levels of at most this many cells run in the multigrid tail block
 
 

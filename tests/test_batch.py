@@ -37,7 +37,8 @@ def test_batched_instances_match_solo_runs(dev, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,momentum", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("mixed", "rbgs")])
+@pytest.mark.parametrize("precision,momentum", [("fp64", "bicgstab"), ("mixed", "bicgstab"), ("mixed", "rbgs"),
+                                                ("mixed", "rbgs_refined")])
 def test_native_step_matches_python_step(dev, precision, momentum):
     """kc_channel_step makes the calls ChannelSolver's Python loop makes: same fields bit for bit
     (momentum by the refined BiCGSTAB or by Gauss-Seidel)."""

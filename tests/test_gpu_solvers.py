@@ -312,6 +312,31 @@ def test_rbgs_momentum_system_converges(dev):
     assert warm.ok and warm.iters == 1
 
 
+def test_rbgs_refined_momentum_system(dev):
+    """FP32 red-black Gauss-Seidel inside FP64 refinement on the channel's
+    u-momentum system: meets ||b - A x|| / ||b|| < 1e-8 in FP64 from zero in a
+    few passes, agrees with the FP64 BiCGSTAB solution, and a warm start from
+    that solution needs no sweep."""
+    from karman_taichi_gb300 import linalg
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    s = ChannelSolver(get("channel_320x64"), device=dev, precision="mixed", native=False)
+    s.assemble_momentum()
+    x = _t(np.zeros(s.b_u.shape), dev)
+    info = linalg.rbgs_refined(s.A_u, s.A_u32, s.b_u, x, eps=1e-8, max_iter=500)
+    assert info.ok and 1 <= info.refinements <= 4 and info.iters < 200, info
+    c = s.coef_u.cpu().numpy().reshape(5, -1)
+    S = s.coef_u.shape[2]
+    b = s.b_u.cpu().numpy().reshape(-1)
+    r = b - O.to_csr(c, S) @ x.cpu().numpy().reshape(-1)
+    assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(b)
+    xb = _t(np.zeros(s.b_u.shape), dev)
+    assert linalg.bicgstab(s.A_u, s.b_u, xb, eps=1e-12).ok
+    assert np.abs(x.cpu().numpy() - xb.cpu().numpy()).max() <= 1e-6 * np.abs(xb.cpu().numpy()).max()
+    warm = linalg.rbgs_refined(s.A_u, s.A_u32, s.b_u, xb, eps=1e-8, warm=True)
+    assert warm.ok and warm.iters == 0 and warm.refinements == 0
+
+
 def test_rbgs_rel_to_r0_and_bad_arguments(dev):
     from karman_taichi_gb300 import linalg
     c = _rand_system(400, 20, 6, diag_shift=0.5)
