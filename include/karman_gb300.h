@@ -219,7 +219,9 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
  * coarsest solve in one single-block launch, their arithmetic unchanged,
  * when their arrays fit the block's shared memory; 0 launches every level
  * separately.  The fused cycle's levels below level 0 with at least
- * big_cells cells use 16 x 60-cell tiles, smaller ones 8 x 28.  Neither
+ * big_cells cells use 64-wide tiles (16 x 60 owned cells at one sweep,
+ * 12 x 56 at two, 8 x 52 at three), smaller ones 32-wide tiles (8 x 28,
+ * 8 x 24, 8 x 20).  Neither
  * changes the result.  kc_mg_default_opts: nu 1/1 on level 0 and 2 below,
  * exact coarsest solve, omega 1.0 on level 0 and 1.5 below, alpha 1.9 on
  * level 0 and 2.0 below (the tuned setting for the channel's pressure

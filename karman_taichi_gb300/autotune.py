@@ -5,8 +5,10 @@ launches but not its arithmetic:
 
 * which coarse levels run in the one-block tail (``Multigrid.opts.tail``,
   cells per level; 0 launches every level separately);
-* which levels below level 0 use the large 16 x 60-cell tiles instead of
-  8 x 28 (``Multigrid.opts.big_cells``);
+* which levels below level 0 use the large tiles (64-wide staged rows:
+  16 x 60, 12 x 56 or 8 x 52 owned cells for one, two or three sweeps)
+  instead of the small ones (32-wide rows: 8 x 28, 8 x 24, 8 x 20)
+  (``Multigrid.opts.big_cells``);
 * how many CG iterations one captured graph chunk holds before the host reads
   the solver state (``ChannelSolver.check_every_p``): fewer host round trips
   against more launches of iterations that return at once once the solve has

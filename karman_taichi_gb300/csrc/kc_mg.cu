@@ -573,7 +573,8 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int
     for (int k = tid; k < A.n; k += kTailThreads) T.x_out[k] = A.x[k];
 }
 
-// large levels use 16 x 60 tiles, small ones 8 x 28 (more blocks in flight)
+// large levels use the 64-wide tiles (16 x 60 owned cells at one sweep), small ones the 32-wide
+// tiles (8 x 28 at one sweep; more blocks in flight)
 static inline bool mg_big(int NX, int NY, const kc_mg_opts* o) {
     return (long long)NX * NY >= (o->big_cells > 0 ? o->big_cells : 200000);
 }
@@ -1014,7 +1015,7 @@ void kc_mg_default_opts(kc_mg_opts* o) {
     o->coarsest_sweeps = 0;    // exact coarsest solve
     o->max_levels = KC_MG_MAX_LEVELS;
     o->tail = kTailMax;        // the levels of at most 1536 cells in one single-block launch
-    o->big_cells = 200000;     // levels of 200k cells and more in 16 x 60 tiles
+    o->big_cells = 200000;     // levels of 200k cells and more in the 64-wide tiles
     // Level 0 (one sweep, the expensive level): omega 1.0, alpha 1.9 -- measured on GB300 over
     // five p' systems (three time points of the 2048 x 512 channel, the 320 x 64 channel, a
     // random 1024^2 system): 2-4 CG iterations fewer per solve than the uniform omega 1.1 /
