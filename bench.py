@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="channel_2048x512")
     ap.add_argument("--mode", default="auto", choices=["auto", "fp64", "mixed", "learned"])
-    ap.add_argument("--momentum", default="bicgstab", choices=["bicgstab", "rbgs_refined", "rbgs"],
+    ap.add_argument("--momentum", default="rbgs_refined", choices=["rbgs_refined", "bicgstab", "rbgs"],
                     help="momentum solver of the mixed path (ChannelSolver(momentum=...))")
     ap.add_argument("--compare-steps", type=int, default=2, help="timed steps of the FP64 plain comparison run")
     ap.add_argument("--no-compare", action="store_true")
@@ -156,7 +156,7 @@ def max_over_ranks(x, world):
 
 
 # ---------------------------------------------------------------------------------------------
-def make_solver(cfg, mode, dev, momentum="bicgstab"):
+def make_solver(cfg, mode, dev, momentum="rbgs_refined"):
     from karman_taichi_gb300.channel import ChannelSolver
     if mode == "learned":
         from karman_taichi_gb300 import learned

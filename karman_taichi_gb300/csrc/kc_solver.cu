@@ -2390,6 +2390,114 @@ static GsLayout gs_layout(long long n, int S, size_t elem = sizeof(double)) {
     return L;
 }
 
+// ---- several Gauss-Seidel sweeps per launch (the inner solve of kc_rbgs_refined) ----
+// A block stages its tile of b, the weights, the coefficients and the incoming
+// x with a 2 NU-cell halo (the multigrid tiles' layout) and runs NU sweeps (red,
+// black, ...) over shrinking rings in shared memory; half-sweep h covers the
+// region less h rings, so the last one ends exactly on the tile.  Staging,
+// launch and the absent per-sweep reduction are paid once per NU sweeps.  The
+// tile treats a link across the end of a row as a link to zero: valid for
+// systems whose rows never link across their ends (checked once per solve by
+// k_rows_wrap_links; the padded SIMPLE systems qualify), else the one-sweep
+// kernel above runs.  Ping-pong between two iterates: a block's halo reads
+// cells that other blocks update in the same launch.
+constexpr int kGsbNU = 2, kGsbTI = 12, kGsbAJ = 64, kGsbRY = 4;
+constexpr int kGsbSweeps = 12;   // sweeps per refinement pass unless opts->check_every says otherwise
+
+template <int TI, int AJ, int RY, int NU>
+__global__ void __launch_bounds__(AJ * RY) k_gs_block_sweeps(MgLvl L, const float* __restrict__ b,
+                                                             const float* __restrict__ xin, float* __restrict__ xout) {
+    using T = MgTile<TI, AJ, RY, 2 * NU>;
+    constexpr int H = T::H;
+    __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
+    __shared__ __align__(16) float sc[5 * T::A];
+    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * T::TJ;
+    const int bc = T::tx(), j = j0 + bc - H;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - H;
+        const bool in = jin && i >= 0 && i < L.NX;
+        const int k = in ? i * L.NY + j : 0;
+        const int u = a * T::AJ + bc;
+        cp_async4(sx + u, xin + k, in);
+        cp_async4(sb + u, b + k, in);
+        cp_async4(sw + u, L.winv + k, in);
+    }
+    mg_stage_coef<TI, T>(L, i0, j0, sc);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    const MgCoef<T, true> C{sc, L, i0, j0};
+#pragma unroll
+    for (int h = 1; h <= 2 * NU; ++h) {   // odd h: red ((i + j) even), even h: black
+        if (bc >= h && bc < AJ - h)
+            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
+                if (((a + bc) & 1) != ((h & 1) ? 0 : 1)) continue;
+                const int u = a * T::AJ + bc;
+                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+            }
+        __syncthreads();
+    }
+    if (bc >= H && bc < T::TJ + H && j < L.NY)
+        for (int a = H + T::ty(); a < TI + H; a += T::RY) {
+            const int i = i0 + a - H;
+            if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + bc];
+        }
+}
+
+// weights 1/d of the red-black sweeps (0 on rows with a zero diagonal)
+__global__ void __launch_bounds__(kPwThreads) k_gs_winv(Coef<float> A, int n, float* __restrict__ winv) {
+    KC_PW_LOOP(n, {
+        float d = A.at(0, k);
+        if (A.lap) d = d - (((A.at(1, k) + A.at(2, k)) + A.at(3, k)) + A.at(4, k));
+        winv[k] = d != 0.f ? 1.f / d : 0.f;
+    })
+}
+
+// *flag = 1 when some row links across its end (north link of its last cell or
+// south link of its first cell nonzero)
+__global__ void __launch_bounds__(kPwThreads) k_rows_wrap_links(Coef<float> A, int NX, int NY, int* __restrict__ flag) {
+    KC_PW_LOOP(NX, {
+        const int i = k;
+        if (A.at(3, i * NY + NY - 1) != 0.f || A.at(4, i * NY) != 0.f) *flag = 1;
+    })
+}
+
+// NU-sweep launches from d = 0 on A32 d = r (r32); sweeps rounded up to whole launches
+static int gs_blocked_run(const kc_system* A, const float* r, float* d, void* ws, size_t ws_bytes, int sweeps,
+                          kc_solve_info* info, cudaStream_t s) {
+    const GsLayout L = gs_layout(A->n, A->stride, sizeof(float));
+    if (!ws || ws_bytes < L.total) return set_error("kc_rbgs_refined: inner workspace %zu < %zu", ws_bytes, L.total),
+                                          KC_ERR_WORKSPACE;
+    char* base = (char*)ws;
+    float* winv = (float*)(base + L.off_winv);
+    float* d1 = (float*)(base + L.off_x1);
+    const int NY = A->stride, NX = (int)(A->n / A->stride);
+    const Coef<float> C = coef_of<float>(A);
+    k_gs_winv<<<pw_blocks(A->n), kPwThreads, 0, s>>>(C, (int)A->n, winv);
+    KC_LAUNCH_CHECK("k_gs_winv");
+    KC_CUDA(cudaMemsetAsync(d, 0, (size_t)A->n * sizeof(float), s));
+    const MgLvl G{(const float*)A->coef, A->cs, A->es, NX, NY, A->form == KC_FORM_LAPLACIAN, winv, nullptr};
+    const dim3 grid = mg_tile_grid(NX, NY, kGsbTI, kGsbAJ - 4 * kGsbNU);
+    const int launches = std::max(1, (sweeps + kGsbNU - 1) / kGsbNU);
+    float* cur = d;
+    float* nxt = d1;
+    for (int q = 0; q < launches; ++q) {
+        k_gs_block_sweeps<kGsbTI, kGsbAJ, kGsbRY, kGsbNU><<<grid, kGsbAJ * kGsbRY, 0, s>>>(G, r, cur, nxt);
+        KC_LAUNCH_CHECK("k_gs_block_sweeps");
+        std::swap(cur, nxt);
+    }
+    if (cur != d) KC_CUDA(cudaMemcpyAsync(d, cur, (size_t)A->n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (info) {
+        info->status = KC_OK;   // no inner residual test: the refinement checks the true residual
+        info->refinements = 0;
+        info->iters = (long long)launches * kGsbNU;
+        info->rel_res = 0.0;
+        info->r0 = 0.0;
+    }
+    return KC_OK;
+}
+
 // Red-black Gauss-Seidel sweeps of A x = b (T = double: the FP64 solver; T = float: the
 // inner solve of kc_rbgs_refined) until the residual of the incoming iterate meets o->eps,
 // o->max_iter sweeps, or a non-finite residual.  Checked by the caller: A's dtype is T.
@@ -2550,13 +2658,15 @@ size_t kc_refined_ws_bytes(long long n, int stride) {
 }  // extern "C"
 
 // FP64 iterative refinement around an FP32 inner solver: r = b - A64 x in FP64 (and its
-// FP32 copy), inner(io, info, r32, d32, inner workspace, bytes, stream) solves A32 d = r32
-// from d = 0 to io.eps relative to ||r32||, x += d; repeated until ||b - A64 x|| / ||b|| <
-// o->eps.  A sweep that raised the true residual is undone.
-template <class Inner>
+// FP32 copy), inner(io, info, r32, d32, inner workspace, bytes, stream, aux) solves A32 d =
+// r32 from d = 0 to io.eps relative to ||r32||, x += d; repeated until ||b - A64 x|| / ||b||
+// < o->eps.  A sweep that raised the true residual is undone.  prep(slot, stream) may
+// enqueue a device-side check that leaves an int in *slot; it comes back with the first
+// residual (no extra synchronisation) and reaches every inner call as aux.
+template <class Prep, class Inner>
 static int refined_core(const char* who, const kc_system* A64, const kc_system* A32, const double* b, double* x,
                         void* ws, size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine,
-                        kc_solve_info* info, void* stream, Inner inner) {
+                        kc_solve_info* info, void* stream, Prep prep, Inner inner) {
     int rc = check_system(A64);
     if (rc) return rc;
     rc = check_system(A32);
@@ -2580,6 +2690,11 @@ static int refined_core(const char* who, const kc_system* A64, const kc_system* 
     KC_CUDA(cudaMemsetAsync(P.st, 0, sizeof(SolverState), s));
     if (o->x0 != KC_X0_WARM) k_zero_f64<<<pb, kPwThreads, 0, s>>>((int)n, x);   // warm: x is the initial guess
     KC_CUDA(cudaMemsetAsync(out2, 0, 4 * sizeof(double), s));
+    {
+        const int prc = prep((int*)(out2 + 3), s);
+        if (prc < 0) return prc;
+    }
+    int aux = 0;
     kc_solve_opts io = *o;
     io.eps = eps_inner;
     io.x0 = KC_X0_ZERO;
@@ -2595,13 +2710,16 @@ static int refined_core(const char* who, const kc_system* A64, const kc_system* 
     for (int it = 0; it <= max_refine; ++it) {
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, it == 0);
         KC_LAUNCH_CHECK("k_refine_resid");
-        double h2[3];
+        double h2[4];
         {
             const void* hp = readback(out2, sizeof(h2), s);
             if (!hp) return KC_ERR_CUDA;
             memcpy(h2, hp, sizeof(h2));
         }
-        if (it == 0) bb = h2[1];
+        if (it == 0) {
+            bb = h2[1];
+            memcpy(&aux, &h2[3], sizeof(int));
+        }
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
         memcpy(&skipped, &h2[2], sizeof(int));
@@ -2636,7 +2754,7 @@ static int refined_core(const char* who, const kc_system* A64, const kc_system* 
         io.max_iter = o->max_iter - total;
         io.eps = std::max(eps_inner, 0.5 * o->eps / rel);   // no deeper than the target needs
         kc_solve_info ii{};
-        int r2 = inner(io, &ii, r32, d32, base + L.off_inner, L.inner_bytes, stream);
+        int r2 = inner(io, &ii, r32, d32, base + L.off_inner, L.inner_bytes, stream, aux);
         if (r2 < 0) return r2;
         total += ii.iters;
         ++sweeps;
@@ -2669,16 +2787,31 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
                         size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine,
                         kc_solve_info* info, void* stream) {
     return refined_core("kc_bicgstab_refined", A64, A32, b, x, ws, ws_bytes, o, eps_inner, max_refine, info, stream,
+                        [](int*, cudaStream_t) { return KC_OK; },
                         [&](const kc_solve_opts& io, kc_solve_info* ii, const float* r, float* d, void* iw,
-                            size_t ib, void* st) { return kc_bicgstab(A32, r, d, nullptr, iw, ib, &io, ii, st); });
+                            size_t ib, void* st, int) { return kc_bicgstab(A32, r, d, nullptr, iw, ib, &io, ii, st); });
 }
 
 int kc_rbgs_refined(const kc_system* A64, const kc_system* A32, const double* b, double* x, void* ws,
                     size_t ws_bytes, const kc_solve_opts* o, double eps_inner, int max_refine, kc_solve_info* info,
                     void* stream) {
+    // rows that never link across their ends (the padded SIMPLE systems): several sweeps per
+    // launch, o->check_every of them per refinement pass (0: kGsbSweeps); otherwise one sweep per
+    // launch with the residual tested every sweep
     return refined_core("kc_rbgs_refined", A64, A32, b, x, ws, ws_bytes, o, eps_inner, max_refine, info, stream,
+                        [&](int* flag, cudaStream_t st) {
+                            if (!A32 || A32->stride < 1 || A32->n % A32->stride) return KC_OK;   // checked later
+                            const int NX = (int)(A32->n / A32->stride);
+                            k_rows_wrap_links<<<pw_blocks(NX), kPwThreads, 0, st>>>(coef_of<float>(A32), NX,
+                                                                                     A32->stride, flag);
+                            KC_LAUNCH_CHECK("k_rows_wrap_links");
+                            return KC_OK;
+                        },
                         [&](const kc_solve_opts& io, kc_solve_info* ii, const float* r, float* d, void* iw,
-                            size_t ib, void* st) {
+                            size_t ib, void* st, int wraps) {
+                            if (!wraps)
+                                return gs_blocked_run(A32, r, d, iw, ib, o->check_every > 0 ? o->check_every : kGsbSweeps,
+                                                      ii, as_stream(st));
                             kc_solve_opts g = io;
                             g.persistent = 0;
                             g.check_every = kRbgsInnerChunk;   // graph-captured chunks of sweeps
