@@ -162,8 +162,11 @@ int kc_bicgstab_refined(const kc_system* A64, const kc_system* A32, const double
                         double eps_inner, int max_refine, kc_solve_info* info, void* stream);
 /* The same refinement with FP32 red-black Gauss-Seidel sweeps as the inner
  * solver (the Gauss-Seidel counterpart of the reference's Jacobi solves,
- * pressure_valid.py:192-233): each sweep costs a fraction of a BiCGSTAB
- * iteration, for diagonally dominant systems such as the momentum rows.
+ * pressure_valid.py:192-233), for diagonally dominant systems such as the
+ * momentum rows.  Systems whose rows never link across their ends (checked
+ * on the device): opts->check_every sweeps per refinement pass (0: 12), two
+ * per launch on staged tiles, no inner residual test; others: one sweep per
+ * launch, each pass to eps_inner.  opts->max_iter caps the sweeps in all.
  * info->iters counts sweeps.  Workspace: kc_refined_ws_bytes. */
 int kc_rbgs_refined(const kc_system* A64, const kc_system* A32, const double* b,
                     double* x, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
@@ -426,8 +429,9 @@ int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, c
  * precision KC_F64: the plain method (every solve FP64 BiCGSTAB, cold start,
  * rel. tol eps, cap n); KC_F32: the accelerated path (momentum:
  * KC_MOMENTUM_BICGSTAB, FP32 BiCGSTAB in FP64 refinement, inner tol
- * eps_inner; KC_MOMENTUM_RBGS_REFINED, FP32 red-black Gauss-Seidel in FP64
- * refinement (kc_rbgs_refined, inner tol 1e-5, at most 200 sweeps); or
+ * eps_inner; KC_MOMENTUM_RBGS_REFINED (the Python ChannelSolver's default),
+ * FP32 red-black Gauss-Seidel in FP64 refinement (kc_rbgs_refined, 12
+ * sweeps per refinement pass, at most 200 sweeps); or
  * KC_MOMENTUM_RBGS, FP64 red-black Gauss-Seidel (kc_rbgs, at most 200
  * sweeps); the Gauss-Seidel variants hand over to the refined BiCGSTAB if
  * they miss eps; all from the previous outer iteration's u*, v* to
