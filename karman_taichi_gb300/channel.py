@@ -41,8 +41,8 @@ from .linalg import (Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, 
 
 # sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
 MOMENTUM_SWEEPS = 200
-# inner tolerance of the FP32 Gauss-Seidel sweeps of the momentum refinement: one pass from the
-# previous outer iteration's u*, v* usually meets the 1e-8 target
+# inner tolerance of the one-sweep Gauss-Seidel path of the momentum refinement (systems whose rows
+# link across their ends; the channel's padded systems take 12 sweeps per pass without an inner test)
 EPS_INNER_GS = 1e-5
 
 

@@ -38,7 +38,8 @@ kc_system sys_of(long long NX, long long NY, const void* coef, int dtype, int fo
 
 // sweeps the Gauss-Seidel momentum solves may take before the refined BiCGSTAB takes over
 constexpr long long kMomentumSweeps = 200;
-// inner tolerance of the FP32 Gauss-Seidel sweeps of the refined momentum solve
+// inner tolerance of the one-sweep Gauss-Seidel path of the refined momentum solve (systems whose
+// rows link across their ends; the padded channel systems take 12 sweeps per pass, no inner test)
 constexpr double kEpsInnerGs = 1e-5;
 
 kc_solve_opts opts_of(double eps, long long max_iter, int rel_to, int check_every, int use_graph, int persistent) {

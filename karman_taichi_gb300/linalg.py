@@ -278,7 +278,9 @@ def rbgs_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, *
                  use_graph=True, warm=False) -> SolveInfo:
     """FP64-residual iterative refinement around FP32 red-black Gauss-Seidel
     sweeps (``iters`` counts sweeps); stops when ||b - A64 x|| / ||b|| < eps.
-    For diagonally dominant systems (the momentum rows)."""
+    For diagonally dominant systems (the momentum rows).  Systems whose rows
+    never link across their ends get 12 sweeps per refinement pass, two per
+    launch; others one sweep per launch to ``eps_inner``."""
     require_cuda(b, x)
     if A64.dtype != L.F64 or A32.dtype != L.F32:
         raise TypeError("rbgs_refined needs an FP64 and an FP32 operator")

@@ -337,6 +337,31 @@ def test_rbgs_refined_momentum_system(dev):
     assert warm.ok and warm.iters == 0 and warm.refinements == 0
 
 
+def test_rbgs_refined_rows_linked_across_ends(dev):
+    """A flat 5-point system whose rows link across their ends (every north and
+    south link set): kc_rbgs_refined takes the one-sweep kernel (flat wrap
+    handled) and meets the FP64 tolerance; the same system with those links
+    cut takes the several-sweeps-per-launch tiles and meets it too."""
+    from karman_taichi_gb300 import linalg
+    n, S = 40 * 37, 37
+    c = _rand_system(n, S, 11, diag_shift=1.0)
+    b = np.random.default_rng(12).standard_normal(n)
+    for cut in (False, True):
+        cc = c.copy()
+        if cut:
+            j = np.arange(n) % S
+            cc[3][j == S - 1] = 0.0
+            cc[4][j == 0] = 0.0
+            cc[0] = -(cc[1] + cc[2] + cc[3] + cc[4]) + 1.0
+        A64 = linalg.Stencil(_t(cc, dev), stride=S)
+        A32 = linalg.Stencil(_t(cc.astype(np.float32), dev), stride=S)
+        x = _t(np.zeros(n), dev)
+        info = linalg.rbgs_refined(A64, A32, _t(b, dev), x, eps=1e-8, max_iter=2000)
+        assert info.ok, (cut, info)
+        r = b - O.to_csr(cc, S) @ x.cpu().numpy()
+        assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(b), cut
+
+
 def test_rbgs_rel_to_r0_and_bad_arguments(dev):
     from karman_taichi_gb300 import linalg
     c = _rand_system(400, 20, 6, diag_shift=0.5)
