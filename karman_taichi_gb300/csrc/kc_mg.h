@@ -15,8 +15,8 @@ constexpr int kMgTI0 = 16, kMgAJ0 = 64, kMgRY0 = 4, kMgTJ0 = kMgAJ0 - 4, kMgNT0 
 // more resident blocks); staging measured faster on GB300 at 2050 x 514
 // (p' solve 5.30 vs 5.53 ms per outer iteration)
 constexpr bool kMgStagedLarge = true;
-// tiles of the small levels: 8 x 28 owned cells, 32-wide staged rows
-constexpr int kMgTI1 = 8, kMgAJ1 = 32, kMgRY1 = 4, kMgTJ1 = kMgAJ1 - 4, kMgNT1 = kMgAJ1 * kMgRY1;
+// tiles of the small levels: 8 rows, 32-wide staged rows (8 x 28 owned cells at one sweep)
+constexpr int kMgTI1 = 8, kMgAJ1 = 32, kMgRY1 = 4, kMgNT1 = kMgAJ1 * kMgRY1;
 // Levels >= 1 may take NU = 1..3 red-black sweeps before and after their
 // coarse correction (kc_mg_opts.nu_coarse): the staged halo is 2 NU cells, so
 // the large tiles keep 64-wide rows and lose rows as NU grows -- their nine

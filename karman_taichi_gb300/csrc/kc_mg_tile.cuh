@@ -176,13 +176,6 @@ struct MgStage {
     float* sxc;
     float* ss;    // a further staged array of the caller's (the single-reduction CG's previous s)
 };
-template <int TI, int AJ, int RY>
-struct MgStageDims {
-    using T = MgTile<TI, AJ, RY>;
-    static constexpr int XI = TI / 2 + 2, XJ = AJ / 2, XC = XI * XJ;
-    // floats of the staged (double-buffered) part and of the single scratch x
-    static constexpr int kDown = 8 * T::A, kUp = 8 * T::A + XC, kX = T::A;
-};
 
 // DOWN, asynchronous part: stage b_in (and q) , W and the coefficients of the tile at (i0, j0)
 // (halo H cells)
