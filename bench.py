@@ -146,13 +146,22 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The slowest rank's value (every rank gets it); on the process group's own
+    device (CUDA under NCCL, the host under gloo)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(world, steps, ms):
+    """Whole-job time steps/s of `world` replicas that each advanced `steps`
+    time steps, over the slowest rank's time `ms` (weak scaling)."""
+    return world * steps / (ms * 1e-3)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -433,7 +442,7 @@ def run_gpu(args):
         tuned = tune_pressure(solver, cycles=CYCLE_CANDIDATES)
     ms, recs, launches, ck = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
     summ = summarize(recs)
-    value = world * args.steps / (ms * 1e-3)
+    value = replica_value(world, args.steps, ms)
     out.update(value=round(value, 5), ms_per_step=round(ms / args.steps, 3),
                dtype="f64" if mode == "fp64" else ("f32+f64 (FP32 stencils/vectors, FP64 dots/residuals)"
                                                    + (" + bf16 U-Net initial guess" if mode == "learned" else "")),
