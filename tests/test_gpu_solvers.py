@@ -4,6 +4,7 @@ Tolerances: FP64 SpMV <= 1e-13 relative (only FMA contraction differs);
 FP64 solves agree with the oracle / direct solves to <= 1e-6 relative, the
 field tolerance of the FP64 path; FP32 SpMV <= 1e-5 relative.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -360,6 +361,32 @@ def test_rbgs_refined_rows_linked_across_ends(dev):
         assert info.ok, (cut, info)
         r = b - O.to_csr(cc, S) @ x.cpu().numpy()
         assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(b), cut
+
+
+def test_rbgs_refined_blocked_sweeps_match_global_sweeps(dev):
+    """The several-sweeps-per-launch tiles (shrinking halos, two sweeps per
+    launch) compute what global red-black sweeps compute: one refinement pass
+    of 4 sweeps from x = 0 on the channel's u-momentum system against the FP64
+    restatement's 4 sweeps (FP32 arithmetic: 1e-5)."""
+    from karman_taichi_gb300 import _lib as L, linalg
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    s = ChannelSolver(get("channel_320x64"), device=dev, precision="mixed", native=False)
+    s.assemble_momentum()
+    x = _t(np.zeros(s.b_u.shape), dev)
+    lib = L.load()
+    buf = linalg.Workspace(dev).get(lib.kc_refined_ws_bytes(s.A_u.n, s.A_u.stride))
+    o = linalg._opts(1e-12, 500, L.X0_ZERO, L.PRECOND_NONE, 0, L.REL_R0, 4, True, None, False)
+    info = L.KcSolveInfo()
+    rc = lib.kc_rbgs_refined(ctypes.byref(s.A_u.system), ctypes.byref(s.A_u32.system), linalg.ptr(s.b_u),
+                             linalg.ptr(x), linalg.ptr(buf), buf.numel(), ctypes.byref(o), 1e-5, 1,
+                             ctypes.byref(info), linalg.stream_handle(dev))
+    assert rc >= 0 and info.iters == 4 and info.refinements == 1, (rc, info.iters, info.refinements)
+    S = s.coef_u.shape[2]
+    ref, _ = O.rbgs_sweeps(s.coef_u.cpu().numpy().reshape(5, -1), s.b_u.cpu().numpy().reshape(-1),
+                           np.zeros(s.b_u.numel()), 4, S)
+    got = x.cpu().numpy().reshape(-1)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
 
 
 def test_rbgs_rel_to_r0_and_bad_arguments(dev):
