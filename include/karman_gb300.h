@@ -104,6 +104,15 @@ int         kc_device_count(void);
 long long   kc_launch_count(void);
 /* sizeof of an ABI struct by name ("kc_system", "kc_channel", ...; 0 if unknown). */
 size_t      kc_struct_size(const char* name);
+/* Solves that run in captured chunks of iterations (opts->use_graph) keep the
+ * instantiated graphs in a process-wide cache keyed by every pointer and
+ * parameter a graph bakes in.  No counterpart in the reference (it has no
+ * graphs).  kc_graph_cache_size: entries held.  kc_graph_cache_limit(cap):
+ * sets the most entries kept (least recently used evicted first; cap = 0
+ * only queries) and returns the previous limit (default 1024).  A graph
+ * evicted while another thread launches it is destroyed after that launch. */
+size_t      kc_graph_cache_size(void);
+size_t      kc_graph_cache_limit(size_t cap);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),
@@ -137,10 +146,13 @@ int kc_bicgstab(const kc_system* A, const void* b, void* x, const void* M,
  * rejected with KC_ERR_ARG and an explanation in kc_last_error().
  * The first call on a device looks up that array's device address (once per
  * device, with the device current); make that first call before any stream
- * capture.  Every call uses the same array and each call clears the state it
- * needs, but calls that overlap on the GPU (concurrent streams, threads or
- * processes sharing a context) race on it.  Iterations are launched directly
- * (opts->use_graph is ignored). */
+ * capture.  The address is kept for the life of the process and is not looked
+ * up again after cudaDeviceReset.  Every call uses the same array and each
+ * call clears the state it needs, but calls that overlap on the GPU
+ * (concurrent streams, threads or processes sharing a context) race on it.
+ * Iterations are launched directly (opts->use_graph is ignored).  Each call
+ * waits on the host for its solve: the solver state is copied back into a
+ * static pageable host buffer (no pinned host memory is allocated either). */
 #define KC_NOALLOC_MAX_N 65536
 int kc_bicgstab_noalloc(const kc_system* A, const void* b, void* x, const void* M,
                         const kc_solve_opts* opts, kc_solve_info* info, void* stream);

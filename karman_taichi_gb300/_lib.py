@@ -112,6 +112,8 @@ SIGNATURES = {
     "kc_device_count": (I_, []),
     "kc_launch_count": (L_, []),
     "kc_struct_size": (S_, [C.c_char_p]),
+    "kc_graph_cache_size": (S_, []),
+    "kc_graph_cache_limit": (S_, [S_]),
     "kc_spmv": (I_, [C.POINTER(KcSystem), P_, P_, P_]),
     "kc_dot_ws_bytes": (S_, [L_]),
     "kc_dot": (I_, [I_, L_, P_, P_, P_, P_, S_, P_]),

@@ -30,6 +30,10 @@ int cuda_status(cudaError_t e, const char* what) {
 
 namespace kc {
 
+static thread_local int g_pageable_depth = 0;
+PageableReadbacks::PageableReadbacks() { ++g_pageable_depth; }
+PageableReadbacks::~PageableReadbacks() { --g_pageable_depth; }
+
 const void* readback(const void* src, size_t bytes, cudaStream_t s) {
     struct Pinned {
         void* p = nullptr;
@@ -38,9 +42,19 @@ const void* readback(const void* src, size_t bytes, cudaStream_t s) {
         }
     };
     static thread_local Pinned buf;
+    alignas(64) static thread_local unsigned char pageable[4096];
     if (bytes > 4096) {
-        set_error("readback of %zu bytes exceeds the 4096-byte pinned buffer", bytes);
+        set_error("readback of %zu bytes exceeds the 4096-byte readback buffer", bytes);
         return nullptr;
+    }
+    if (g_pageable_depth > 0) {
+        cudaError_t e = cudaMemcpyAsync(pageable, src, bytes, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            cuda_status(e, "readback");
+            return nullptr;
+        }
+        return pageable;
     }
     if (!buf.p) {
         cudaError_t e = cudaMallocHost(&buf.p, 4096);

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cstring>
 #include <atomic>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -188,25 +189,31 @@ int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* stre
     int dev = 0;
     KC_CUDA(cudaGetDevice(&dev));
     workers = std::max(1, std::min(workers, n));
+    // the first failing instance's status and message are recorded together,
+    // under one lock, so the message always belongs to the returned status
     std::atomic<int> first_err{0};
-    std::vector<std::string> msgs(workers);
+    std::mutex err_mu;
+    std::string first_msg;
+    auto record = [&](int code, const std::string& msg) {
+        std::lock_guard<std::mutex> lk(err_mu);
+        if (first_err.load() == 0) {
+            first_msg = msg;
+            first_err.store(code);
+        }
+    };
     std::vector<std::thread> pool;
     pool.reserve(workers);
     for (int w = 0; w < workers; ++w) {
         pool.emplace_back([&, w] {
             if (cudaSetDevice(dev) != cudaSuccess) {
-                int z = 0;
-                first_err.compare_exchange_strong(z, KC_ERR_CUDA);
-                msgs[w] = "cudaSetDevice failed in a batch worker";
+                record(KC_ERR_CUDA, "cudaSetDevice failed in a batch worker");
                 return;
             }
             for (int k = w; k < n; k += workers) {
                 for (int t = 0; t < steps && first_err.load() == 0; ++t) {
                     const int rc = kc_channel_step(chs[k], stats ? &stats[k] : nullptr, streams[k]);
                     if (rc < 0) {
-                        int z = 0;
-                        first_err.compare_exchange_strong(z, rc);
-                        msgs[w] = "instance " + std::to_string(k) + ": " + kc_last_error();
+                        record(rc, "instance " + std::to_string(k) + ": " + kc_last_error());
                         return;
                     }
                 }
@@ -215,13 +222,7 @@ int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* stre
     }
     for (auto& t : pool) t.join();
     const int rc = first_err.load();
-    if (rc) {
-        for (const auto& m : msgs)
-            if (!m.empty()) {
-                set_error("kc_channel_batch_step: %s", m.c_str());
-                break;
-            }
-    }
+    if (rc) set_error("kc_channel_batch_step: %s", first_msg.c_str());
     return rc;
 }
 

@@ -69,6 +69,16 @@ inline cudaError_t launch_chain(void (*kernel)(KArgs...), dim3 grid, dim3 block,
 // pointer to the host copy (valid until this thread's next call), or null on
 // a CUDA error (reported through set_error).
 const void* readback(const void* src, size_t bytes, cudaStream_t s);
+// While an object of this type lives, readbacks of the constructing thread
+// copy into a static per-thread pageable buffer instead of the pinned one, so
+// that no host memory is allocated for them (the allocation-free entry points
+// use it; a pageable copy is slower but allocates nothing).
+struct PageableReadbacks {
+    PageableReadbacks();
+    ~PageableReadbacks();
+    PageableReadbacks(const PageableReadbacks&) = delete;
+    PageableReadbacks& operator=(const PageableReadbacks&) = delete;
+};
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // binary64 -> binary32 with IEEE 754 round to nearest, ties to even, in

@@ -41,6 +41,7 @@
 #include <algorithm>
 #include <mutex>
 #include <map>
+#include <memory>
 #include <tuple>
 #include <cstring>
 
@@ -1874,8 +1875,75 @@ static unsigned long long bytes_hash(const void* p, size_t n) {
     for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
     return h | 1ull;
 }
+// Cached executable graphs are reference counted: a caller takes a reference
+// under the lock and launches outside it, so an entry evicted by another
+// thread in between is destroyed only when the last holder drops it (and
+// cudaGraphExecDestroy of a graph still in flight frees it on completion).
+// When the cache is full the least recently used entry alone is evicted.
+struct GraphExec {
+    cudaGraphExec_t ex = nullptr;
+    explicit GraphExec(cudaGraphExec_t e) : ex(e) {}
+    ~GraphExec() {
+        if (ex) cudaGraphExecDestroy(ex);
+    }
+    GraphExec(const GraphExec&) = delete;
+    GraphExec& operator=(const GraphExec&) = delete;
+};
+struct GraphEntry {
+    std::shared_ptr<GraphExec> g;
+    unsigned long long last_use;
+};
+static size_t g_graph_cap = 1024;   // entries; set by kc_graph_cache_limit
 static std::mutex g_graph_mu;
-static std::map<std::pair<int, GraphKey>, cudaGraphExec_t> g_graphs;
+static std::map<std::pair<int, GraphKey>, GraphEntry> g_graphs;
+static unsigned long long g_graph_clock = 0;
+
+static std::shared_ptr<GraphExec> graph_lookup(int dev, const GraphKey& gk) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    auto it = g_graphs.find({dev, gk});
+    if (it == g_graphs.end()) return nullptr;
+    it->second.last_use = ++g_graph_clock;
+    return it->second.g;
+}
+
+static void graph_insert(int dev, const GraphKey& gk, std::shared_ptr<GraphExec> g) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    if (!g_graphs.count({dev, gk})) {
+        while (!g_graphs.empty() && g_graphs.size() >= g_graph_cap) {
+            auto lru = g_graphs.begin();
+            for (auto it = g_graphs.begin(); it != g_graphs.end(); ++it)
+                if (it->second.last_use < lru->second.last_use) lru = it;
+            g_graphs.erase(lru);
+        }
+    }
+    g_graphs[{dev, gk}] = GraphEntry{std::move(g), ++g_graph_clock};
+}
+
+}  // namespace kc
+
+extern "C" {
+size_t kc_graph_cache_size(void) {
+    std::lock_guard<std::mutex> lk(kc::g_graph_mu);
+    return kc::g_graphs.size();
+}
+
+size_t kc_graph_cache_limit(size_t cap) {
+    std::lock_guard<std::mutex> lk(kc::g_graph_mu);
+    const size_t old = kc::g_graph_cap;
+    if (cap > 0) {
+        kc::g_graph_cap = cap;
+        while (kc::g_graphs.size() > cap) {
+            auto lru = kc::g_graphs.begin();
+            for (auto it = kc::g_graphs.begin(); it != kc::g_graphs.end(); ++it)
+                if (it->second.last_use < lru->second.last_use) lru = it;
+            kc::g_graphs.erase(lru);
+        }
+    }
+    return old;
+}
+}  // extern "C"
+
+namespace kc {
 
 template <typename T, bool PRE>
 static void launch_bicg_iters(const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, int m,
@@ -1923,13 +1991,8 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
             KC_CUDA(cudaGetDevice(&dev));
             GraphKey gk = key;
             gk.chunk = m;
-            cudaGraphExec_t ex = nullptr;
-            {
-                std::lock_guard<std::mutex> lk(g_graph_mu);
-                auto it = g_graphs.find({dev, gk});
-                if (it != g_graphs.end()) ex = it->second;
-            }
-            if (!ex) {
+            std::shared_ptr<GraphExec> gx = graph_lookup(dev, gk);
+            if (!gx) {
                 cudaStream_t cap_s;
                 KC_CUDA(cudaStreamCreateWithFlags(&cap_s, cudaStreamNonBlocking));
                 cudaGraph_t graph;
@@ -1938,17 +2001,14 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
                 cudaError_t e = cudaStreamEndCapture(cap_s, &graph);
                 cudaStreamDestroy(cap_s);
                 if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+                cudaGraphExec_t ex = nullptr;
                 e = cudaGraphInstantiate(&ex, graph, 0);
                 cudaGraphDestroy(graph);
                 if (e != cudaSuccess) return cuda_status(e, "cudaGraphInstantiate");
-                std::lock_guard<std::mutex> lk(g_graph_mu);
-                if (g_graphs.size() >= 64) {  // bounded cache: drop everything when full
-                    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
-                    g_graphs.clear();
-                }
-                g_graphs[{dev, gk}] = ex;
+                gx = std::make_shared<GraphExec>(ex);
+                graph_insert(dev, gk, gx);
             }
-            KC_CUDA(cudaGraphLaunch(ex, s));
+            KC_CUDA(cudaGraphLaunch(gx->ex, s));
         } else {
             launch(m, s);
             KC_LAUNCH_CHECK_NC("solver iteration launch");
@@ -2574,6 +2634,8 @@ int kc_rbgs(const kc_system* A, const double* b, double* x, void* ws, size_t ws_
 // that loads the library until the process exits).  In host code the
 // array's name is only a host-side stand-in, so its device address is looked
 // up with cudaGetSymbolAddress, once per device, with that device current.
+// That address is kept for the life of the process: it is not looked up again
+// after a cudaDeviceReset or any other teardown of the device's context.
 namespace kc {
 constexpr size_t kNoallocBytes = 4718592;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
@@ -2619,6 +2681,9 @@ int kc_bicgstab_noalloc(const kc_system* A, const void* b, void* x, const void* 
     // the graph path would instantiate graphs (allocations); launch directly
     kc_solve_opts o = *opts;
     o.use_graph = 0;
+    // solver-state readbacks into a static pageable buffer: the pinned one is
+    // allocated (cudaMallocHost) on a thread's first readback
+    PageableReadbacks pageable;
     return bicg_impl(A, b, x, M, scratch, kNoallocBytes, &o, info, stream, false);
 }
 

@@ -73,3 +73,32 @@ def test_native_batch_matches_solo_runs(dev):
         for k in ("u", "v", "p"):
             assert np.array_equal(a[k], r[k]), (cfg.name, k)
     b.close()
+
+
+@pytest.mark.gpu
+def test_native_batch_with_graph_cache_eviction(dev):
+    """More captured-graph keys than the cache holds: 12 instances (at least three graph keys each:
+    workspaces, coefficients and iterates differ) stepped by 6 worker threads with the cache limited
+    to 8 entries, so graphs are evicted while other threads launch theirs.  Fields stay bitwise those
+    of solo runs, and the cache never holds more than its limit."""
+    from karman_taichi_gb300 import _lib as L
+    from karman_taichi_gb300.batch import BatchedChannels, batch_configs
+    from karman_taichi_gb300.channel import ChannelSolver
+    lib = L.load()
+    old = lib.kc_graph_cache_limit(8)
+    try:
+        cfgs = [c.with_(max_outer=6) for c in batch_configs(12, seed=9)]
+        b = BatchedChannels(cfgs, device=dev, precision="mixed", workers=6)
+        b.step_native(2)
+        assert lib.kc_graph_cache_size() <= 8
+        for cfg, s in zip(cfgs, b.solvers):
+            solo = ChannelSolver(cfg, device=dev, precision="mixed")
+            solo.persistent = False
+            solo.step(); solo.step()
+            a, r = s.state_numpy(), solo.state_numpy()
+            for k in ("u", "v", "p"):
+                assert np.array_equal(a[k], r[k]), (cfg.name, k)
+        b.close()
+    finally:
+        lib.kc_graph_cache_limit(old)
+    assert lib.kc_graph_cache_limit(0) == old
