@@ -19,12 +19,11 @@ has no exchange step) and `value` is all ranks' time steps / the slowest
 rank's time.
 
 `--impl reference` times the CPU restatement of the same plain method
-(oracle/kc_cpu.c, C + OpenMP, FP64) on all host cores.  A 2048 x 512 time
-step takes minutes of CPU work, so each reference "step" is a bounded sample
-(one SIMPLE outer iteration with every BiCGSTAB solve capped); the measured
-seconds per BiCGSTAB iteration are converted to time steps/s with the
-BiCGSTAB iterations per time step of the identical algorithm, recorded in
-profiles/iteration_counts.json by the GPU FP64 run.
+(oracle/kc_cpu.c, C + OpenMP, FP64) on all host cores: whole time steps of
+the seeded case from its initial state, every solve to convergence.  A
+2048 x 512 time step is about a minute of CPU work, so the arm times as many
+whole steps as fit its budget (at least one) and reports that count as
+"steps"; nothing is extrapolated.
 """
 from __future__ import annotations
 
@@ -42,7 +41,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Time steps/s at 2048x512: learned+mixed vs plain BiCGSTAB, same GB300, resid<=1e-6"
 # (the value line runs the fastest accelerated configuration; the learned variant is reported beside it)
-COUNTS = os.path.join(ROOT, "profiles", "iteration_counts.json")
 
 
 def parse():
@@ -62,7 +60,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default cycle and launch shapes of the p' solve instead of tuning them "
                          "before timing")
-    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="seconds of whole CPU time steps (at least one step is always timed)")
     ap.add_argument("--spmv-sweep", action="store_true",
                     help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
     ap.add_argument("--batch-instances", type=int, default=0, metavar="N",
@@ -205,15 +204,18 @@ def timed_steps(solver, K, W, world, lib, clocks=None):
     l0 = lib.kc_launch_count()
     if clocks:
         clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    recs = [solver.step() for _ in range(K)]
-    e1.record()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(K + 1)]
+    ev[0].record()
+    recs = []
+    for k in range(K):
+        recs.append(solver.step())
+        ev[k + 1].record()
     torch.cuda.synchronize()
     ck = clocks.stop() if clocks else None
     barrier(world)
-    ms = max_over_ranks(e0.elapsed_time(e1), world)
-    return ms, recs, lib.kc_launch_count() - l0, ck
+    ms = max_over_ranks(ev[0].elapsed_time(ev[K]), world)
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(K)]
+    return ms, recs, lib.kc_launch_count() - l0, ck, per_step
 
 
 def e2e_steps(solver, K, W, world):
@@ -365,49 +367,38 @@ def field_writer_roofline(solver, peak):
             "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
 
 
-def cpu_sample(cfg, budget_s, iters_per_step):
-    """C/OpenMP FP64 plain path on the host cores: one SIMPLE outer iteration
-    with each BiCGSTAB solve capped so the sample fits the budget."""
-    import numpy as np
+def cpu_whole_steps(cfg, budget_s, steps=None):
+    """C/OpenMP FP64 plain path on all host cores: whole time steps of the
+    seeded case from its initial state (every solve to its tolerance, outer
+    loop to its stop rule), as many as fit ``budget_s`` (at least one), or
+    exactly ``steps``.  Returns the time-steps/s figure and what was timed."""
     from karman_taichi_gb300 import geometry
     from oracle import cpu
     solid = geometry.solid_mask(cfg.nx, cfg.ny, cfg.obstacles)
     u, v, p = geometry.channel_initial_fields(cfg.nx, cfg.ny, solid, cfg.U, cfg.noise, cfg.seed)
-    # calibrate on a short capped sample, then size the real one
-    st = cpu.channel_run(cfg, solid, u.copy(), v.copy(), p.copy(), n_steps=1, max_total_outer=1, max_solver_iter=20)
-    per_iter = st["seconds"] / max(st["solver_iters"], 1)
-    cap = int(max(20, min(5000, budget_s / per_iter / 3)))
-    st = cpu.channel_run(cfg, solid, u, v, p, n_steps=1, max_total_outer=1, max_solver_iter=cap)
-    per_iter = st["seconds"] / max(st["solver_iters"], 1)
-    value = 1.0 / (per_iter * iters_per_step) if iters_per_step else None
-    return {"value": value, "unit": "time steps/s", "cores": cpu.threads(), "kind": "port",
-            "seconds_per_bicgstab_iter": per_iter,
-            "sample": f"1 SIMPLE outer iteration of {cfg.name} from the seeded initial state, each BiCGSTAB solve "
-                      f"capped at {cap} iterations ({st['solver_iters']} iterations in {st['seconds']:.1f} s); "
-                      f"converted with {iters_per_step:.0f} BiCGSTAB iterations per time step of the same "
-                      f"algorithm (GPU FP64 run)"}
-
-
-def load_counts(config):
-    try:
-        with open(COUNTS) as f:
-            return json.load(f).get(config)
-    except (OSError, ValueError):
-        return None
-
-
-def save_counts(config, d):
-    try:
-        data = {}
-        if os.path.exists(COUNTS):
-            with open(COUNTS) as f:
-                data = json.load(f)
-        data[config] = d
-        os.makedirs(os.path.dirname(COUNTS), exist_ok=True)
-        with open(COUNTS, "w") as f:
-            json.dump(data, f, indent=1, sort_keys=True)
-    except OSError:
-        pass
+    u0, v0 = u.copy(), v.copy()
+    # the library is loaded and its threads started before anything is timed
+    cpu.channel_run(cfg, solid, u.copy(), v.copy(), p.copy(), n_steps=1, max_total_outer=1, max_solver_iter=2)
+    done, secs, outer, its, first_ms, first_outer = 0, 0.0, 0, 0, None, None
+    while True:
+        st = cpu.channel_run(cfg, solid, u, v, p, u0, v0, n_steps=1)
+        done += 1
+        secs += st["seconds"]
+        outer += st["outer"]
+        its += st["solver_iters"]
+        if first_ms is None:
+            first_ms, first_outer = st["seconds"] * 1e3, st["outer"]
+        if steps is not None:
+            if done >= steps:
+                break
+        elif secs + st["seconds"] > budget_s:
+            break
+    return {"value": done / secs, "unit": "time steps/s", "cores": cpu.threads(), "kind": "port",
+            "steps_timed": done, "seconds": secs, "outer_iterations": outer,
+            "bicgstab_iterations": its, "first_step_ms": first_ms, "first_step_outer": first_outer,
+            "sample": f"time steps 1..{done} of {cfg.name} from the seeded initial state, whole steps "
+                      f"(BiCGSTAB solves to rel. tol {cfg.eps}, outer loop to max|mdiv| <= {cfg.mass_tol} "
+                      f"or {cfg.max_outer} iterations), {cpu.threads()} OpenMP threads"}
 
 
 def peaks():
@@ -440,7 +431,7 @@ def run_gpu(args):
         # CG chunk length), picked on this solver's state before anything is timed
         from karman_taichi_gb300.autotune import CYCLE_CANDIDATES, tune_pressure
         tuned = tune_pressure(solver, cycles=CYCLE_CANDIDATES)
-    ms, recs, launches, ck = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
+    ms, recs, launches, ck, per_step = timed_steps(solver, args.steps, args.warmup, world, lib, Clocks(local))
     summ = summarize(recs)
     value = replica_value(world, args.steps, ms)
     out.update(value=round(value, 5), ms_per_step=round(ms / args.steps, 3),
@@ -482,7 +473,7 @@ def run_gpu(args):
             if tuned is not None:   # the same p' cycle and launch shapes as the timed run
                 from karman_taichi_gb300.autotune import apply_choice
                 apply_choice(lsol, tuned)
-            lms, lrecs, _, _ = timed_steps(lsol, args.steps, args.warmup, 1, lib)
+            lms, lrecs, _, _, _ = timed_steps(lsol, args.steps, args.warmup, 1, lib)
             lsum = summarize(lrecs)
             out["learned"] = {"value": round(args.steps / (lms * 1e-3), 5), "unit": "time steps/s",
                               "ms_per_step": round(lms / args.steps, 3), "p_iters_per_step": lsum["p_iters_per_step"],
@@ -490,17 +481,22 @@ def run_gpu(args):
                               "note": "same steps with the U-Net initial guess of p' (Python-driven outer loop)"}
             del lsol
 
-    fp64_counts = summ if mode == "fp64" else None
     if rank == 0 and not args.no_compare and mode != "fp64":
-        # plain FP64 BiCGSTAB on the same GPU: the same first W + C time steps
-        C = args.compare_steps
+        # plain FP64 BiCGSTAB on the same GPU over time steps W+1 .. W+C of the same seeded case; the
+        # accelerated path's time for the same steps comes from the per-step events of the timed run
+        C = min(args.compare_steps, args.steps)
         ref = make_solver(cfg, "fp64", dev)
-        cms, crecs, _, _ = timed_steps(ref, C, args.warmup, 1, lib)
-        fp64_counts = summarize(crecs)
+        cms, crecs, _, _, _ = timed_steps(ref, C, args.warmup, 1, lib)
+        same = sum(per_step[:C])
         out["fp64_plain"] = {"value": round(C / (cms * 1e-3), 5), "unit": "time steps/s",
-                             "ms_per_step": round(cms / C, 3), "steps": C,
-                             "warmup": args.warmup, "stats": fp64_counts}
-        out["speedup_vs_fp64_plain"] = round(value / out["fp64_plain"]["value"], 3)
+                             "ms_per_step": round(cms / C, 3), "steps": C, "warmup": args.warmup,
+                             "window": f"time steps {args.warmup + 1}..{args.warmup + C}",
+                             "stats": summarize(crecs),
+                             "accelerated_same_steps": {"value": round(C / (same * 1e-3), 5),
+                                                        "ms_per_step": round(same / C, 3),
+                                                        "stats": summarize(recs[:C])}}
+        out["speedup_vs_fp64_plain"] = round(cms / same, 3)
+        out["speedup_vs_fp64_plain_window"] = f"time steps {args.warmup + 1}..{args.warmup + C}, both paths"
         # field error after the same W + C steps from the same initial state
         solver.reset()
         for _ in range(args.warmup + C):
@@ -509,14 +505,25 @@ def run_gpu(args):
         out["field_error_vs_fp64"] = {k: float(abs(a[k] - b[k]).max() / max(abs(b[k]).max(), 1e-300))
                                       for k in ("u", "v", "p")}
         out["field_error_vs_fp64"]["after_steps"] = args.warmup + C
-        out["field_error_vs_fp64"]["definition"] = "max |x - x_fp64| / max |x_fp64| over the padded field"
-    if rank == 0 and fp64_counts:
-        save_counts(cfg.name, {"solver_iters_per_step": fp64_counts["solver_iters_per_step"],
-                               "outer_per_step": fp64_counts["outer_per_step"],
-                               "source": "GPU FP64 plain run of bench.py (steps after warm-up)"})
+        out["field_error_vs_fp64"]["definition"] = ("max |x - x_fp64| / max |x_fp64| over the padded field; "
+                                                    "x_fp64: the GPU plain FP64 path (the oracle's algorithm)")
+        del ref
     if rank == 0 and world == 1 and not args.no_cpu:
-        cnt = fp64_counts or load_counts(cfg.name) or {}
-        out["cpu_baseline"] = cpu_sample(cfg, args.cpu_budget, cnt.get("solver_iters_per_step"))
+        out["cpu_baseline"] = cpu_whole_steps(cfg, args.cpu_budget)
+        # the GPU's time for the same time step (step 1 from the seeded state, kernels warm)
+        solver.reset()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        r1 = solver.step()
+        e1.record()
+        torch.cuda.synchronize()
+        g1 = e0.elapsed_time(e1)
+        cb = out["cpu_baseline"]
+        out["first_step"] = {"gpu_ms": round(g1, 3), "gpu_outer": sum(s.get("outer", 1) for s in r1),
+                             "cpu_ms": round(cb["first_step_ms"], 1), "cpu_outer": cb["first_step_outer"],
+                             "gpu_vs_cpu": round(cb["first_step_ms"] / g1, 1),
+                             "note": "time step 1 of the seeded case on both: the same work, timed on both sides"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -527,43 +534,27 @@ def run_gpu(args):
 def run_reference(args):
     """The reference arm: the plain method's CPU implementation (C + OpenMP
     restatement; the reference's Taichi CPU path needs taichi==0.9.0, which is
-    not installed), on all host cores, same config/metric/unit."""
+    not installed), on all host cores, same config/metric/unit.  Whole time
+    steps from the seeded initial state, as many as fit a budget of about two
+    minutes (at least one); "steps" is the number actually timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from karman_taichi_gb300 import geometry
     from karman_taichi_gb300.config import PRESETS
-    from oracle import cpu
     cfg = PRESETS[args.config]
-    cnt = load_counts(cfg.name)
-    if not cnt:
-        print(json.dumps({"impl": "reference", "unavailable": "no recorded BiCGSTAB iterations per time step "
-                          "(run the GPU arm once to record profiles/iteration_counts.json)"}))
-        return
-    its_per_step = cnt["solver_iters_per_step"]
-    solid = geometry.solid_mask(cfg.nx, cfg.ny, cfg.obstacles)
-    u, v, p = geometry.channel_initial_fields(cfg.nx, cfg.ny, solid, cfg.U, cfg.noise, cfg.seed)
-    st = cpu.channel_run(cfg, solid, u.copy(), v.copy(), p.copy(), n_steps=1, max_total_outer=1, max_solver_iter=10)
-    per = st["seconds"] / max(st["solver_iters"], 1)
-    budget = 60.0 / max(args.steps + args.warmup, 1)
-    cap = int(max(10, min(5000, budget / per / 3)))
-    samples = []
-    for k in range(args.warmup + args.steps):
-        uu, vv, pp = u.copy(), v.copy(), p.copy()
-        st = cpu.channel_run(cfg, solid, uu, vv, pp, n_steps=1, max_total_outer=1, max_solver_iter=cap)
-        if k >= args.warmup:
-            samples.append(st["seconds"] / max(st["solver_iters"], 1))
-    per = statistics.mean(samples)
-    value = 1.0 / (per * its_per_step)
+    cb = cpu_whole_steps(cfg, budget_s=120.0)
+    value = cb["value"]
     out = {"metric": METRIC, "value": value, "unit": "time steps/s", "impl": "reference", "n_gpus": 0,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic: seeded channel initial state",
-           "config": {"workload": cfg.name, "nx": cfg.nx, "ny": cfg.ny, "cells": cfg.cells, "mode": "fp64 plain"},
-           "cpu_baseline": {"value": value, "unit": "time steps/s", "cores": cpu.threads(), "kind": "port",
-                            "sample": f"each step: 1 SIMPLE outer iteration of {cfg.name}, BiCGSTAB solves capped "
-                                      f"at {cap} iterations; seconds per BiCGSTAB iteration x {its_per_step:.0f} "
-                                      f"iterations per time step ({cnt.get('source', '')})"},
+           "steps": cb["steps_timed"], "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+           "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic: seeded channel initial state",
+           "config": {"workload": cfg.name, "nx": cfg.nx, "ny": cfg.ny, "cells": cfg.cells, "mode": "fp64 plain",
+                      "timed": "whole time steps from the seeded initial state; a step is about a minute of CPU "
+                               "work, so fewer steps than requested are timed and no warm-up step is run"},
+           "cpu_baseline": {"value": value, "unit": "time steps/s", "cores": cb["cores"], "kind": "port",
+                            "sample": cb["sample"], "seconds": cb["seconds"],
+                            "outer_iterations": cb["outer_iterations"],
+                            "bicgstab_iterations": cb["bicgstab_iterations"]},
            "e2e": {"value": value, "unit": "time steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -113,6 +113,13 @@ size_t      kc_struct_size(const char* name);
  * evicted while another thread launches it is destroyed after that launch. */
 size_t      kc_graph_cache_size(void);
 size_t      kc_graph_cache_limit(size_t cap);
+/* Failure testing.  The persistent (cooperative) solvers meet at grid
+ * barriers whose waits give up after a bounded number of polls (about 0.5 s);
+ * the solve then ends with KC_ERR_CUDA ("grid barrier timed out") and the
+ * context stays usable.  This sets that bound for later launches (0: the
+ * default) and returns the previous setting, so a test can make a wait run
+ * out without any block hanging.  No counterpart in the reference. */
+unsigned    kc_debug_barrier_spin_limit(unsigned polls);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),
@@ -478,7 +485,9 @@ typedef struct {
 } kc_channel;
 
 typedef struct {
-    int outer, fallbacks, status, pad_;   /* status: KC_OK, or KC_MAXITER if a solve missed eps */
+    int outer, fallbacks, status, pad_;   /* status: KC_OK; KC_MAXITER if a solve missed eps;
+                                             KC_NONFINITE if a solve or the mass residual met a
+                                             NaN/Inf, which also ends the step's outer loop */
     long long it_u, it_v, it_p;
     double mass;                          /* max|mdiv| of the last outer iteration */
 } kc_channel_stats;

@@ -290,6 +290,10 @@ class ChannelSolver:
         for _ in range(self.cfg.max_outer):
             s = self.outer_iteration()
             rec.append(s)
+            # a NaN or Inf ends the step (as kc_channel_step does): the outer loop would only repeat it
+            if L.NONFINITE in s["st"] or not np.isfinite(s["mass"]):
+                s["status"] = L.NONFINITE
+                break
             if s["mass"] <= self.cfg.mass_tol:
                 break
         self.time_forward()

@@ -14,6 +14,7 @@
 // launches of small instances, and their kernels overlap on the GPU.
 #include "kc_common.cuh"
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <atomic>
 #include <mutex>
@@ -167,11 +168,21 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
         S.it_u += iu.iters;
         S.it_v += iv.iters;
         S.it_p += ip.iters;
-        if (iu.status != KC_OK || iv.status != KC_OK || ip.status != KC_OK) S.status = KC_MAXITER;
+        const bool nonfinite = iu.status == KC_NONFINITE || iv.status == KC_NONFINITE || ip.status == KC_NONFINITE;
+        if (nonfinite)
+            S.status = KC_NONFINITE;
+        else if ((iu.status != KC_OK || iv.status != KC_OK || ip.status != KC_OK) && S.status == KC_OK)
+            S.status = KC_MAXITER;
         const void* hp = readback(c->mass, sizeof(double), s);
         if (!hp) return KC_ERR_CUDA;
         memcpy(&mass, hp, sizeof(double));
         S.mass = mass;
+        // a NaN or Inf in the fields (the reference has no such check) ends the step: the outer
+        // loop would only repeat it; the status tells the caller
+        if (nonfinite || !std::isfinite(mass)) {
+            S.status = KC_NONFINITE;
+            break;
+        }
         if (mass <= c->mass_tol) break;
     }
     rc = kc_copy(c->u0, c->u, (size_t)((nx + 3) * (ny + 2)) * sizeof(double), s);

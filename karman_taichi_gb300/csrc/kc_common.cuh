@@ -220,7 +220,9 @@ struct GridBar {
 };
 constexpr unsigned kSpinLimit = 1u << 22;   // ~0.5 s at 40 ns per poll: far beyond any healthy wait
 
-__device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb) {
+// Every block of a cooperative launch calls this; returns false (and every
+// later call returns false at once) if any wait gave up after `limit` polls.
+__device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb, unsigned limit = kSpinLimit) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -236,7 +238,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, unsigned nb) {
             unsigned spins = 0;
             while (*gen == g) {
                 if (*err) break;
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(&bar->err, 1);
                     break;
                 }

@@ -39,10 +39,12 @@
 #include "kc_common.cuh"
 #include "kc_mg.h"
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <map>
 #include <memory>
 #include <tuple>
+#include <initializer_list>
 #include <cstring>
 
 namespace kc {
@@ -330,6 +332,125 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Coef<T> A, Geo g, const T* __
     Acc<T> acc[1];
     PolSpmv<T> pol{x, y};
     stencil_tile<T, 1>(pol, A, g.n, g.S, acc);
+}
+
+// ---- flat vectorised stencil passes ----------------------------------------------------
+// For SoA coefficient planes (es == 1) whose far stride S, plane stride cs and
+// size n are multiples of V, with V-aligned pointers: each thread owns chunks of
+// V consecutive cells and reads every coefficient, the operand and its +-S
+// neighbours with one V-wide (8- or 16-byte) load each; the +-1 neighbours of a
+// chunk are its own elements except one scalar load at each end.  No shared
+// memory and no barrier, so a block's loads are all in flight at once and the
+// launch runs at whatever occupancy the registers allow.  The arithmetic is
+// that of stencil_tile_at operation for operation (same products, same FMA
+// order), so the results are bitwise those of the tile kernels.
+template <typename T, int V>
+struct VecOf;
+template <>
+struct VecOf<double, 2> { using type = double2; };
+template <>
+struct VecOf<float, 4> { using type = float4; };
+template <>
+struct VecOf<float, 2> { using type = float2; };
+
+template <typename T, int V>
+__device__ __forceinline__ void ldg_vec(const T* __restrict__ p, T (&o)[V]) {
+    using VT = typename VecOf<T, V>::type;
+    const VT v = __ldg(reinterpret_cast<const VT*>(p));
+    const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+    for (int i = 0; i < V; ++i) o[i] = e[i];
+}
+template <typename T, int V>
+__device__ __forceinline__ void st_vec(T* __restrict__ p, const T (&o)[V]) {
+    using VT = typename VecOf<T, V>::type;
+    VT v;
+    T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+    for (int i = 0; i < V; ++i) e[i] = o[i];
+    *reinterpret_cast<VT*>(p) = v;
+}
+
+// y[k .. k+V) = (A x)[k .. k+V); reads outside [0, n) are 0
+template <typename T, int V>
+__device__ __forceinline__ void stencil_chunk(const Coef<T>& A, const T* __restrict__ x, int n, int S, int k,
+                                              T (&y)[V]) {
+    T c0[V], c1[V], c2[V], c3[V], c4[V], xc[V], xw[V], xe[V];
+    ldg_vec<T, V>(A.c + k, c0);
+    ldg_vec<T, V>(A.c + A.cs + k, c1);
+    ldg_vec<T, V>(A.c + 2 * A.cs + k, c2);
+    ldg_vec<T, V>(A.c + 3 * A.cs + k, c3);
+    ldg_vec<T, V>(A.c + 4 * A.cs + k, c4);
+    ldg_vec<T, V>(x + k, xc);
+    if (k >= S) {
+        ldg_vec<T, V>(x + k - S, xw);
+    } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) xw[i] = T(0);
+    }
+    if (k + S < n) {
+        ldg_vec<T, V>(x + k + S, xe);
+    } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) xe[i] = T(0);
+    }
+    const T xl = k > 0 ? __ldg(x + k - 1) : T(0);
+    const T xr = k + V < n ? __ldg(x + k + V) : T(0);
+#pragma unroll
+    for (int i = 0; i < V; ++i) {
+        const T o = xc[i];
+        const T xs = i > 0 ? xc[i - 1] : xl;
+        const T xn = i < V - 1 ? xc[i + 1] : xr;
+        T v = c0[i] * o;
+        if (A.lap) {
+            v = fmaT<T>(c1[i], xw[i] - o, v);
+            v = fmaT<T>(c2[i], xe[i] - o, v);
+            v = fmaT<T>(c3[i], xn - o, v);
+            v = fmaT<T>(c4[i], xs - o, v);
+        } else {
+            v = fmaT<T>(c1[i], xw[i], v);
+            v = fmaT<T>(c2[i], xe[i], v);
+            v = fmaT<T>(c3[i], xn, v);
+            v = fmaT<T>(c4[i], xs, v);
+        }
+        y[i] = v;
+    }
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(kThreads) k_spmv_vec(Coef<T> A, int n, int S, const T* __restrict__ x,
+                                                       T* __restrict__ y) {
+    const int nc = n / V;
+    for (int c = blockIdx.x * kThreads + threadIdx.x; c < nc; c += gridDim.x * kThreads) {
+        T out[V];
+        stencil_chunk<T, V>(A, x, n, S, c * V, out);
+        st_vec<T, V>(y + c * V, out);
+    }
+}
+
+// V for the flat vectorised passes on A with the given vector pointers (0: not applicable)
+template <typename T>
+static int vec_width(const kc_system* A, std::initializer_list<const void*> ptrs) {
+    if (A->es != 1) return 0;
+    for (int V : {int(16 / sizeof(T)), 2}) {
+        const size_t bytes = V * sizeof(T);
+        bool ok = A->stride % V == 0 && A->n % V == 0 && A->cs % V == 0 && ((uintptr_t)A->coef % bytes) == 0;
+        for (const void* q : ptrs) ok = ok && ((uintptr_t)q % bytes) == 0;
+        if (ok) return V;
+    }
+    return 0;
+}
+
+static int vec_blocks(long long chunks, int cap) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                       cudaSuccess)
+            sms = 152;
+    }
+    const long long want = (chunks + kThreads - 1) / kThreads;
+    return (int)std::max<long long>(1, std::min<long long>({want, (long long)sms * 8, (long long)cap}));
 }
 
 // ---- dot ----------------------------------------------------------------------
@@ -836,6 +957,43 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// The same pass in the flat vectorised form (SoA FP64 planes; see stencil_chunk):
+// per chunk of V cells r = b - A x, its FP32 copy, ||r||^2 and ||b||^2.  The grid
+// is capped at the partials the workspace holds (the tile grid's block count).
+template <int V>
+__global__ void __launch_bounds__(kThreads)
+    k_refine_resid_vec(Coef<double> A, int n, int S, const double* __restrict__ b, const double* __restrict__ x,
+                       float* __restrict__ r32, BicgPtrs P, double* out2, int with_b) {
+    Acc<double> acc[2];
+    const int nc = n / V;
+    for (int c = blockIdx.x * kThreads + threadIdx.x; c < nc; c += gridDim.x * kThreads) {
+        const int k = c * V;
+        double y[V], bb[V];
+        ldg_vec<double, V>(b + k, bb);
+        stencil_chunk<double, V>(A, x, n, S, k, y);
+        float rf[V];
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+            const double rk = bb[i] - y[i];
+            rf[i] = f64_to_f32(rk);
+            acc[0].add(rk, rk);
+            if (with_b) acc[1].add(bb[i], bb[i]);
+        }
+        if constexpr (V == 2) {
+            *reinterpret_cast<float2*>(r32 + k) = make_float2(rf[0], rf[1]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < V; ++i) r32[k + i] = rf[i];
+        }
+    }
+    double s[2];
+    if (block_partials<2>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
+        out2[0] = s[0];
+        out2[1] = s[1];
+        P.st->ticket[0] = 0;
+    }
+}
+
 // x += d, applied only when every entry of d is finite (flag[0] == 0; set by
 // k_flag_nonfinite), so a correction from a broken-down FP32 sweep is dropped.
 __global__ void __launch_bounds__(kPwThreads)
@@ -964,6 +1122,7 @@ __device__ __forceinline__ void for_tile_cells(int n, int S, int i0, int j0, F&&
 
 struct PersistGeo {
     int tiles_x, ntiles;
+    unsigned spin_limit;   // polls a grid-barrier wait may take before it gives up
 };
 
 template <typename T, bool PRE>
@@ -1012,7 +1171,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             store_block_partials<T, 1>(acc, P.partials, P.ld, 0, bid);
         }
-        if (!grid_sync(bar, G)) return;
+        if (!grid_sync(bar, G, pg.spin_limit)) return;
         {
             double s1[1];
             sum_partials<1>(P.partials, P.ld, 0, G, s1);
@@ -1042,7 +1201,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             store_block_partials<T, 2>(acc, P.partials, P.ld, 1, bid);
         }
-        if (!grid_sync(bar, G)) return;
+        if (!grid_sync(bar, G, pg.spin_limit)) return;
         {
             double s2[2];
             sum_partials<2>(P.partials, P.ld, 1, G, s2);
@@ -1080,7 +1239,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             store_block_partials<T, 2>(acc, P.partials, P.ld, 3, bid);
         }
-        if (!grid_sync(bar, G)) return;
+        if (!grid_sync(bar, G, pg.spin_limit)) return;
         {
             double s3[2];
             sum_partials<2>(P.partials, P.ld, 3, G, s3);
@@ -1179,7 +1338,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             store_block_partials<T, 1>(acc, P.partials, P.ld, 0, bid);
         }
-        if (!grid_sync(bar, G)) return;
+        if (!grid_sync(bar, G, pg.spin_limit)) return;
         {
             double s1[1];
             sum_partials<1>(P.partials, P.ld, 0, G, s1);
@@ -1206,7 +1365,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             store_block_partials<T, 1>(acc, P.partials, P.ld, 1, bid);
         }
-        if (!grid_sync(bar, G)) return;
+        if (!grid_sync(bar, G, pg.spin_limit)) return;
         {
             double s2[1];
             sum_partials<1>(P.partials, P.ld, 1, G, s2);
@@ -1826,6 +1985,17 @@ static Coef<T> coef_of(const kc_system* A) {
     return Coef<T>{(const T*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN ? 1 : 0};
 }
 
+// r = b - A x and its sums: the flat vectorised pass when A's layout allows it,
+// else the tile pass; both use at most the tile grid's block count of partials
+static void launch_refine_resid(const kc_system* A64, Geo g, dim3 sg, const double* b, const double* x, float* r32,
+                                BicgPtrs P, double* out2, bool with_b, cudaStream_t s) {
+    if (vec_width<double>(A64, {b, x}) == 2 && ((uintptr_t)r32 % 8) == 0)
+        k_refine_resid_vec<2><<<vec_blocks(A64->n / 2, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
+            coef_of<double>(A64), (int)A64->n, A64->stride, b, x, r32, P, out2, with_b ? 1 : 0);
+    else
+        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, with_b ? 1 : 0);
+}
+
 struct HostState {
     int status, done;
     long long iter;
@@ -2026,6 +2196,10 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
 
 using namespace kc;
 
+// polls before a grid-barrier wait of the persistent solvers gives up (0: kSpinLimit);
+// lowered only by tests, through kc_debug_barrier_spin_limit
+static std::atomic<unsigned> g_spin_limit{0};
+
 template <typename T, class K>
 static int launch_persistent(K kernel, const kc_system* A, T* x, const BicgVecs& V, const BicgPtrs& P, GridBar* bar,
                              cudaStream_t s) {
@@ -2052,7 +2226,8 @@ static int launch_persistent(K kernel, const kc_system* A, T* x, const BicgVecs&
     }
     if (per < 1) return set_error("persistent solver kernel cannot be resident"), KC_ERR_UNSUPPORTED;
     dim3 sg = stencil_grid(A->n, A->stride);
-    PersistGeo pg{(int)sg.x, (int)(sg.x * sg.y)};
+    const unsigned lim = g_spin_limit.load(std::memory_order_relaxed);
+    PersistGeo pg{(int)sg.x, (int)(sg.x * sg.y), lim ? lim : kSpinLimit};
     int G = std::max(1, std::min(pg.ntiles, sms * per));
     Coef<T> C = coef_of<T>(A);
     Geo g{(int)A->n, A->stride};
@@ -2135,6 +2310,10 @@ static int run_solver(const kc_system* A, const void* b, void* x, const void* M,
 
 extern "C" {
 
+unsigned kc_debug_barrier_spin_limit(unsigned polls) {
+    return g_spin_limit.exchange(polls, std::memory_order_relaxed);
+}
+
 int kc_spmv(const kc_system* A, const void* x, void* y, void* stream) {
     int rc = check_system(A);
     if (rc) return rc;
@@ -2142,10 +2321,25 @@ int kc_spmv(const kc_system* A, const void* x, void* y, void* stream) {
     cudaStream_t s = as_stream(stream);
     Geo g{(int)A->n, A->stride};
     dim3 sg = stencil_grid(A->n, A->stride);
-    if (A->dtype == KC_F64)
-        k_spmv<double><<<sg, kThreads, 0, s>>>(coef_of<double>(A), g, (const double*)x, (double*)y);
-    else
-        k_spmv<float><<<sg, kThreads, 0, s>>>(coef_of<float>(A), g, (const float*)x, (float*)y);
+    const int n = (int)A->n, S = A->stride;
+    if (A->dtype == KC_F64) {
+        const int V = vec_width<double>(A, {x, y});
+        if (V == 2)
+            k_spmv_vec<double, 2><<<vec_blocks(n / 2, 1 << 30), kThreads, 0, s>>>(coef_of<double>(A), n, S,
+                                                                                   (const double*)x, (double*)y);
+        else
+            k_spmv<double><<<sg, kThreads, 0, s>>>(coef_of<double>(A), g, (const double*)x, (double*)y);
+    } else {
+        const int V = vec_width<float>(A, {x, y});
+        if (V == 4)
+            k_spmv_vec<float, 4><<<vec_blocks(n / 4, 1 << 30), kThreads, 0, s>>>(coef_of<float>(A), n, S,
+                                                                                  (const float*)x, (float*)y);
+        else if (V == 2)
+            k_spmv_vec<float, 2><<<vec_blocks(n / 2, 1 << 30), kThreads, 0, s>>>(coef_of<float>(A), n, S,
+                                                                                  (const float*)x, (float*)y);
+        else
+            k_spmv<float><<<sg, kThreads, 0, s>>>(coef_of<float>(A), g, (const float*)x, (float*)y);
+    }
     KC_LAUNCH_CHECK("k_spmv");
     return KC_OK;
 }
@@ -2773,7 +2967,7 @@ static int refined_core(const char* who, const kc_system* A64, const kc_system* 
     double rel = 1.0, bb = 0.0, best = INFINITY;
     bool applied = false;
     for (int it = 0; it <= max_refine; ++it) {
-        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, it == 0);
+        launch_refine_resid(A64, g, sg, b, x, r32, P, out2, it == 0, s);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[4];
         {
@@ -3038,7 +3232,7 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     key.form = A32->form;
     key.ohash = bytes_hash(mg_opts, sizeof(kc_mg_opts));
     for (int it = 0; it <= max_refine; ++it) {
-        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, R, out2, it == 0);
+        launch_refine_resid(A64, g, sg, b, x, r32, R, out2, it == 0, s);
         KC_LAUNCH_CHECK("k_refine_resid");
         double h2[3];
         {

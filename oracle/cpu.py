@@ -26,12 +26,18 @@ def load():
         h.kc_cpu_channel_run.argtypes = [C.POINTER(CpuParams)] + [C.c_void_p] * 6 + [C.c_int, C.c_long, C.c_long,
                                                                                       C.c_void_p]
         h.kc_cpu_threads.restype = C.c_int
+        h.kc_cpu_set_threads.restype = None
+        h.kc_cpu_set_threads.argtypes = [C.c_int]
         _lib = h
     return _lib
 
 
 def threads() -> int:
     return load().kc_cpu_threads()
+
+
+def set_threads(n: int) -> None:
+    load().kc_cpu_set_threads(int(n))
 
 
 def params_of(cfg) -> CpuParams:

@@ -248,6 +248,11 @@ static void correct(const cpu_params* P, const unsigned char* sol, const double*
 
 int kc_cpu_threads(void) { return omp_get_max_threads(); }
 
+/* sets the OpenMP thread count of later calls (n < 1: leave it) */
+void kc_cpu_set_threads(int n) {
+    if (n >= 1) omp_set_num_threads(n);
+}
+
 /*
  * Runs SIMPLE outer iterations of the channel case (time steps of up to
  * max_outer iterations, stopping a step when the predicted field's max|mdiv|

@@ -1,0 +1,71 @@
+"""The 320 x 64 channel case as stated, all 20 time steps, on the GPU against
+the oracle.
+
+The case: 320 x 64 cells, dx = dy = 1/64, 8 x 8 blocked square at cells
+i in [60, 67], j in [28, 35], uniform inlet u = 1, zero-gradient outlet,
+no-slip walls, Re = 150, CFL 0.5, seeded noise on v; per time step SIMPLE
+outer iterations until max|mdiv| <= 1e-6 or 50; BiCGSTAB to rel. tol eps;
+relaxation 0.7 / 0.3 (the loop of karman_taichi.py:628-659 on the geometry
+of debug/karman_taichi.py:9-14's size).  The oracle run is the C/OpenMP
+restatement of the plain FP64 method (``oracle/kc_cpu.c``, pinned to the
+NumPy oracle by test_cpu_port.py), stored in ``tests/golden/`` by
+``make_oracle_runs.py``.
+
+Tolerances:
+* FP64, solves to 1e-12: the two runs differ by rounding only -- every step
+  takes the same number of outer iterations, fields agree to 1e-6 relative;
+* FP64 with the case's own eps = 1e-8: two solves that stop at a relative
+  residual of 1e-8 differ by up to cond(A) 1e-8, which the outer iterations
+  carry along; fields agree to 1e-4 and outer counts to +-1 per step;
+* mixed precision (FP32 stencils, FP64 refinement to the same 1e-8): fields
+  within 1e-4 of the FP64 oracle (the bound the accelerated path is held to),
+  outer counts +-1, every step reaching max|mdiv| <= 1e-6.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(tag):
+    path = os.path.join(GOLDEN, f"oracle_channel_320x64_eps{tag}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"{path} not generated")
+    d = np.load(path)
+    return d, json.loads(str(d["meta"]))
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("precision,tag,field_tol,outer_tol", [("fp64", "1e-12", 1e-6, 0),
+                                                               ("fp64", "1e-8", 1e-4, 1),
+                                                               ("mixed", "1e-8", 1e-4, 1)])
+def test_channel_320x64_twenty_steps_match_oracle(dev, precision, tag, field_tol, outer_tol):
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import PRESETS
+    d, m = _load(tag)
+    cfg = PRESETS["channel_320x64"].with_(eps=m["eps"])
+    assert m["n_steps"] == cfg.n_steps == 20
+    s = ChannelSolver(cfg, device=dev, precision=precision)
+    worst = {}
+    for k in range(cfg.n_steps):
+        rec = s.step()
+        outer = rec[0]["outer"] if "outer" in rec[0] else len(rec)
+        ref = m["steps"][k]
+        assert abs(outer - ref["outer"]) <= outer_tol, (k, outer, ref)
+        assert rec[-1]["mass"] <= cfg.mass_tol, (k, rec[-1]["mass"])
+        if f"step{k + 1}_u" in d:
+            st = s.state_numpy()
+            for name in ("u", "v", "p"):
+                e = _rel(st[name], d[f"step{k + 1}_{name}"])
+                worst[name] = max(worst.get(name, 0.0), e)
+                assert e <= field_tol, (k + 1, name, e)
+    assert s.fallbacks == 0
+    print(f"{precision} eps {tag}: worst field error vs oracle {worst}")

@@ -76,6 +76,35 @@ def test_spmv_aos_layout(dev):
     assert np.allclose(y.reshape(-1), O.spmv(c, x, NY), rtol=1e-13, atol=1e-13)
 
 
+@pytest.mark.parametrize("dtype,NX,NY,form", [("f64", 2050, 514, 0), ("f32", 2050, 514, 1), ("f32", 300, 64, 0),
+                                               ("f64", 41, 33, 1)])
+def test_spmv_flat_vector_pass_is_bitwise_the_tile_pass(dev, dtype, NX, NY, form):
+    """SoA planes with even (or multiple-of-4) strides take the flat vectorised pass (k_spmv_vec); the
+    same coefficients in the reference's [NX, NY, 5] layout take the tile pass (k_spmv).  Both evaluate
+    the stencil in the same operation order, so the results are bitwise equal (the odd 41 x 33 grid
+    takes the tile pass both ways)."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    c = _rand_system(NX * NY, NY, seed=NX).reshape(5, NX, NY)
+    soa = torch.from_numpy(c).to(dev, tdt).contiguous()
+    aos = soa.permute(1, 2, 0).contiguous()
+    x = torch.from_numpy(np.random.default_rng(6).standard_normal((NX, NY))).to(dev, tdt)
+    y1 = linalg.spmv(linalg.Stencil(soa, form=form), x)
+    y2 = linalg.spmv(linalg.Stencil(aos, form=form), x)
+    assert torch.equal(y1, y2)
+    ref = O.spmv(c if form == 0 else _lap_to_std(c), x.double().cpu().numpy(), NY)
+    tol = 1e-13 if dtype == "f64" else 1e-5
+    assert np.abs(y1.double().cpu().numpy().reshape(-1) - ref).max() <= tol * np.abs(ref).max()
+
+
+def _lap_to_std(c):
+    """Standard-form planes of a Laplacian-form system (component 0 holds the row sum)."""
+    s = c.copy()
+    s[0] = c[0] - c[1:].sum(axis=0)
+    return s
+
+
 def test_dot_deterministic(dev):
     from karman_taichi_gb300 import linalg
     rng = np.random.default_rng(2)
