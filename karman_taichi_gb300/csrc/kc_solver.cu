@@ -46,6 +46,7 @@
 #include <tuple>
 #include <initializer_list>
 #include <cstring>
+#include <cmath>
 
 namespace kc {
 
@@ -2979,6 +2980,12 @@ static int refined_core(const char* who, const kc_system* A64, const kc_system* 
             bb = h2[1];
             memcpy(&aux, &h2[3], sizeof(int));
         }
+        if (!std::isfinite(h2[0]) || !std::isfinite(bb)) {
+            // a NaN or Inf in b, x or the system: ||b|| or ||b - A x|| is not finite
+            rel = NAN;
+            status = KC_NONFINITE;
+            break;
+        }
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
         memcpy(&skipped, &h2[2], sizeof(int));
@@ -3241,6 +3248,12 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
             memcpy(h2, hp, sizeof(h2));
         }
         if (it == 0) bb = h2[1];
+        if (!std::isfinite(h2[0]) || !std::isfinite(bb)) {
+            // a NaN or Inf in b, x or the system: ||b|| or ||b - A x|| is not finite
+            rel = NAN;
+            status = KC_NONFINITE;
+            break;
+        }
         rel = bb > 0 ? sqrt(h2[0] / bb) : 0.0;
         int skipped = 0;
         memcpy(&skipped, &h2[2], sizeof(int));

@@ -19,7 +19,9 @@ Tolerances:
   carry along; fields agree to 1e-4 and outer counts to +-1 per step;
 * mixed precision (FP32 stencils, FP64 refinement to the same 1e-8): fields
   within 1e-4 of the FP64 oracle (the bound the accelerated path is held to),
-  outer counts +-1, every step reaching max|mdiv| <= 1e-6.
+  outer counts +-1.
+Every step ends by the stop rule: max|mdiv| <= 1e-6, or the 50-iteration cap
+(the first two steps, in the oracle's run as in these).
 """
 import json
 import os
@@ -60,7 +62,12 @@ def test_channel_320x64_twenty_steps_match_oracle(dev, precision, tag, field_tol
         outer = rec[0]["outer"] if "outer" in rec[0] else len(rec)
         ref = m["steps"][k]
         assert abs(outer - ref["outer"]) <= outer_tol, (k, outer, ref)
-        assert rec[-1]["mass"] <= cfg.mass_tol, (k, rec[-1]["mass"])
+        # the stop rule: max|mdiv| <= 1e-6 or 50 outer iterations (the first two steps of this
+        # case, in the oracle as here, end at the cap with max|mdiv| ~ 3e-6)
+        mass = rec[-1]["mass"]
+        assert mass <= cfg.mass_tol or outer == cfg.max_outer, (k, mass, outer)
+        if outer_tol == 0:
+            assert mass == pytest.approx(ref["mass"], rel=1e-3), (k, mass, ref)
         if f"step{k + 1}_u" in d:
             st = s.state_numpy()
             for name in ("u", "v", "p"):

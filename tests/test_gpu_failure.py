@@ -55,7 +55,7 @@ def test_grid_barrier_wait_runs_out_and_context_survives(dev):
     assert torch.equal(x, x_ref)
 
 
-@pytest.mark.parametrize("kind", ["bicgstab", "cg", "bicgstab_refined", "rbgs_refined"])
+@pytest.mark.parametrize("kind", ["bicgstab", "cg", "bicgstab_refined", "rbgs_refined", "pcg_refined"])
 def test_nan_in_rhs_is_reported(dev, kind):
     """A NaN in the right-hand side stops the solve with KC_NONFINITE (the reference iterates on)."""
     import torch
@@ -70,6 +70,13 @@ def test_nan_in_rhs_is_reported(dev, kind):
         info = linalg.bicgstab(A, b, x, eps=1e-8, max_iter=500)
     elif kind == "cg":
         info = linalg.cg(A, b, x, eps=1e-8, max_iter=500)
+    elif kind == "pcg_refined":
+        lap = c.clone()
+        lap[0] = c[0] + c[1:].sum(dim=0)        # Laplacian form: component 0 holds the row sum
+        A32 = linalg.Stencil(lap.float().contiguous(), form=L.FORM_LAPLACIAN)
+        mg = linalg.Multigrid(A32)
+        mg.setup()
+        info = linalg.pcg_refined(A, A32, b, x, mg, eps=1e-8)
     else:
         A32 = linalg.Stencil(c.float())
         if kind == "bicgstab_refined":
