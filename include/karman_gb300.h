@@ -293,6 +293,59 @@ int kc_pcg_refined(const kc_system* A64, const kc_system* A32, const double* b, 
                    size_t ws_bytes, const kc_solve_opts* opts, double eps_inner,
                    int max_refine, kc_solve_info* info, void* stream);
 
+/* The trained network applied from native code: features of A x = b (the p'
+ * system: b FP64 [NX][NY], coef32 its FP32 Laplacian-form SoA planes), the
+ * U-Net forward pass at half resolution, and x0 = the upsampled prediction
+ * (FP64 [NX][NY]) -- the same kernels, in the same order, as the Python
+ * trainer's forward pass.  params: the kc_unet_param_count() FP32
+ * parameters, layer by layer (w [9][cout][cin], b [cout]; head w [16], b [1]);
+ * params16: their BF16 copy.  ws: kc_unet_predict_ws_bytes(NX, NY), 256-byte
+ * aligned (features and activations).  No counterpart in the reference (it
+ * has no learned component). */
+typedef struct {
+    int NX, NY;
+    const void* params;
+    const void* params16;
+    void* ws;
+    size_t ws_bytes;
+} kc_unet_net;
+long long kc_unet_param_count(void);
+size_t kc_unet_predict_ws_bytes(int NX, int NY);
+int kc_unet_predict(const kc_unet_net* net, const double* b, const float* coef32, double* x0,
+                    void* stream);
+
+/* Flexible CG (FCG(1), FP64 outer vectors) for the symmetric pressure-correction
+ * system with a changing preconditioner: its first application is the trained
+ * network's prediction of A^-1 r (kc_unet_predict; net may be NULL), every
+ * later one a multigrid-preconditioned FP32 CG pass on A z = r (one sweep of
+ * kc_pcg_refined to eps_inner, inner_ws of kc_pbicgstab_ws_bytes).  This is the
+ * network in the role of the reference's right-preconditioner hooks
+ * p^ = M^-1 p, s^ = M^-1 s (bicgsolver.py:48-58; karman_taichi.py:398-399,
+ * 418-419), with M changing between iterations.  Each direction is
+ * A-orthogonalised against the previous one and its step length minimises
+ * the error's A-norm, so a poor prediction costs one short step.  A network
+ * direction that is not finite or not a descent direction is replaced by a
+ * multigrid pass (finfo->learned_rejected).  Two outer iterations in a row
+ * that cut ||b - A x|| by less than 10 % end the solve with KC_STALL (x the
+ * last iterate): the caller falls back to the plain BiCGSTAB.  KC_OK once
+ * ||b - A x|| / ||b|| < opts->eps on the true residual.  opts->x0:
+ * KC_X0_WARM starts from x; opts->max_iter caps the inner CG iterations;
+ * max_outer the outer ones.  info->iters: inner CG iterations;
+ * info->refinements: outer iterations.  ws: kc_pcg_flexible_ws_bytes(n)
+ * (5 FP64 vectors), 256-byte aligned; kc_mg_setup must have run on mg_ws. */
+typedef struct {
+    int learned_used;      /* the network's prediction was applied            */
+    int learned_rejected;  /* ... and replaced: not finite or not descending  */
+    int outer;             /* outer (flexible) iterations                     */
+    int pad_;
+} kc_flex_info;
+size_t kc_pcg_flexible_ws_bytes(long long n);
+int kc_pcg_flexible(const kc_system* A64, const kc_system* A32, const double* b, double* x,
+                    const kc_unet_net* net, void* mg_ws, const kc_mg_opts* mg_opts, void* inner_ws,
+                    size_t inner_ws_bytes, void* ws, size_t ws_bytes, const kc_solve_opts* opts,
+                    double eps_inner, int max_outer, kc_solve_info* info, kc_flex_info* finfo,
+                    void* stream);
+
 /* ---- SIMPLE assembly and correction (staggered padded fields) ----------- */
 #define KC_MODE_SIMPLE   0   /* simple.py set_bc incl. the east-wall aW term (simple.py:215) */
 #define KC_MODE_BICGSIMP 1   /* bicgsimp.py: east-wall fix (:196), p' pinned at (1,1) (:146-151) */
@@ -443,6 +496,7 @@ int kc_unet_guess_up2(const float* out, int Hh, int Wh, const float* coef32, int
 int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, const double* scales,
                          int Hh, int Wh, float* target, float* weight, void* stream);
 
+
 /* ---- native SIMPLE step and the batched executor --------------------------- */
 /* One channel instance (caller-owned device buffers, shapes as kc_assemble_*).
  * precision KC_F64: the plain method (every solve FP64 BiCGSTAB, cold start,
@@ -482,6 +536,12 @@ typedef struct {
     void* mg_ws;
     size_t mg_ws_bytes;
     kc_mg_opts mg_opts;
+    /* KC_F32 only, nullable: with a network, every p' solve is kc_pcg_flexible
+     * (the network's prediction as the first preconditioner application, then
+     * multigrid CG passes), in ws_flex of kc_pcg_flexible_ws_bytes(n_p) */
+    const kc_unet_net* learned;
+    void* ws_flex;
+    size_t ws_flex_bytes;
 } kc_channel;
 
 typedef struct {
@@ -490,6 +550,7 @@ typedef struct {
                                              NaN/Inf, which also ends the step's outer loop */
     long long it_u, it_v, it_p;
     double mass;                          /* max|mdiv| of the last outer iteration */
+    int learned, learned_rejected;        /* p' solves that applied / rejected the network */
 } kc_channel_stats;
 
 /* One time step: SIMPLE outer iterations (karman_taichi.py:633-659, simple.py:270-281)

@@ -83,12 +83,23 @@ class KcChannel(C.Structure):
                                           "coef_u32", "b_u32", "coef_v32", "b_v32", "coef_p32", "b_p32",
                                           "mass", "pmax", "rws", "ws_u", "ws_v", "ws_p")]
     _fields_ += [("ws_u_bytes", C.c_size_t), ("ws_v_bytes", C.c_size_t), ("ws_p_bytes", C.c_size_t),
-                 ("mg_ws", C.c_void_p), ("mg_ws_bytes", C.c_size_t), ("mg_opts", KcMgOpts)]
+                 ("mg_ws", C.c_void_p), ("mg_ws_bytes", C.c_size_t), ("mg_opts", KcMgOpts),
+                 ("learned", C.c_void_p), ("ws_flex", C.c_void_p), ("ws_flex_bytes", C.c_size_t)]
 
 
 class KcChannelStats(C.Structure):
     _fields_ = [("outer", C.c_int), ("fallbacks", C.c_int), ("status", C.c_int), ("pad_", C.c_int),
-                ("it_u", C.c_longlong), ("it_v", C.c_longlong), ("it_p", C.c_longlong), ("mass", C.c_double)]
+                ("it_u", C.c_longlong), ("it_v", C.c_longlong), ("it_p", C.c_longlong), ("mass", C.c_double),
+                ("learned", C.c_int), ("learned_rejected", C.c_int)]
+
+
+class KcUnetNet(C.Structure):
+    _fields_ = [("NX", C.c_int), ("NY", C.c_int), ("params", C.c_void_p), ("params16", C.c_void_p),
+                ("ws", C.c_void_p), ("ws_bytes", C.c_size_t)]
+
+
+class KcFlexInfo(C.Structure):
+    _fields_ = [("learned_used", C.c_int), ("learned_rejected", C.c_int), ("outer", C.c_int), ("pad_", C.c_int)]
 
 
 class KcKarman(C.Structure):
@@ -144,6 +155,13 @@ SIGNATURES = {
                                   P_, S_, C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
     "kc_pcg_refined": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, P_, P_, C.POINTER(KcMgOpts),
                             P_, S_, C.POINTER(KcSolveOpts), D_, I_, C.POINTER(KcSolveInfo), P_]),
+    "kc_pcg_flexible_ws_bytes": (S_, [L_]),
+    "kc_pcg_flexible": (I_, [C.POINTER(KcSystem), C.POINTER(KcSystem), P_, P_, C.POINTER(KcUnetNet), P_,
+                             C.POINTER(KcMgOpts), P_, S_, P_, S_, C.POINTER(KcSolveOpts), D_, I_,
+                             C.POINTER(KcSolveInfo), C.POINTER(KcFlexInfo), P_]),
+    "kc_unet_param_count": (L_, []),
+    "kc_unet_predict_ws_bytes": (S_, [I_, I_]),
+    "kc_unet_predict": (I_, [C.POINTER(KcUnetNet), P_, P_, P_, P_]),
     "kc_reduce_ws_bytes": (S_, []),
     "kc_assemble_momentum": (I_, [C.POINTER(KcPhys)] + [P_] * 14 + [P_]),
     "kc_apply_bc_values": (I_, [C.POINTER(KcPhys), P_, P_, P_]),

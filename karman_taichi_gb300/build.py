@@ -32,6 +32,7 @@ SOURCES = {
     "kc_fields.cu": [],
     "kc_channel.cu": [],
     "kc_smoothers.cu": [],
+    "kc_flex.cu": [],
 }
 
 

@@ -20,8 +20,9 @@ inside an FP64 iterative refinement; its pressure correction (symmetric) is
 solved by CG preconditioned with the aggregation multigrid V-cycle
 (``pcorr_precond='mg'``, the multigrid step the reference names as missing,
 README.md:31), and an
-optional ``learned`` object supplies the initial guess of p'
-(karman_taichi_gb300.learned).
+optional ``learned`` object supplies the trained network, applied as the
+first preconditioner application of a flexible CG for p'
+(karman_taichi_gb300.learned, kc_pcg_flexible).
 """
 from __future__ import annotations
 
@@ -35,8 +36,8 @@ import torch
 from . import _lib as L
 from . import geometry
 from .config import ChannelConfig
-from .linalg import (Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_refined, ptr, rbgs,
-                     rbgs_refined, stream_handle)
+from .linalg import (Multigrid, Stencil, Workspace, bicgstab, bicgstab_refined, pcg_flexible, pcg_refined, ptr,
+                     rbgs, rbgs_refined, stream_handle)
 
 
 # sweeps the Gauss-Seidel momentum solve may take before the refined BiCGSTAB takes over
@@ -102,7 +103,9 @@ class ChannelSolver:
             self.A_p32 = Stencil(self.coef_p32, form=L.FORM_LAPLACIAN)
             if self.pcorr_precond == "mg":
                 self.mg = Multigrid(self.A_p32, **(mg_opts or {}))
-        self.x0_p = None     # optional initial guess for p' (set by a learned predictor)
+        self.x0_p = None     # optional initial guess for p'
+        self.learned_stats = [0, 0]   # p' solves that applied / rejected the network's prediction
+        self._flex_ws = None
         self.fallbacks = 0   # accelerated solves that fell back (p': plain BiCGSTAB; Gauss-Seidel momentum: refined BiCGSTAB)
         self.last_accel = None  # SolveInfo of the last accelerated p' solve
         ph = L.KcPhys()
@@ -111,8 +114,8 @@ class ChannelSolver:
         ph.alpha_m, ph.alpha_u, ph.alpha_p = cfg.alpha_m, cfg.alpha_u, cfg.alpha_p
         self.phys = ph
         self.history = []        # per time step: list of per-outer-iteration records
-        # the native step (kc_channel_step) runs the whole outer loop in the library; the
-        # Python loop below it is kept for the learned guess and for stage-by-stage use
+        # the native step (kc_channel_step) runs the whole outer loop in the library (with the
+        # network, when one is attached); the Python loop below it is kept for stage-by-stage use
         self.native = bool(native) and (precision == "fp64" or self.mg is not None)
         self.persistent = True   # BiCGSTAB solves as one cooperative launch (native step)
         self.check_every_p = 4   # CG iterations per graph chunk between the host's convergence checks
@@ -194,8 +197,24 @@ class ChannelSolver:
                                       self._s()), "kc_assemble_pcorr")
 
     def solve_p(self):
-        if self.learned is not None:
-            self.x0_p = self.learned.predict(self)
+        if self.learned is not None and self.mg is not None:
+            # the network as the first preconditioner application of a flexible CG
+            self.mg.setup()
+            NX, NY = self.b_p.shape
+            info, fi = pcg_flexible(self.A_p, self.A_p32, self.b_p, self.pcor, self.mg,
+                                    net=self.learned.native(NX, NY), eps=self.cfg.eps, eps_inner=self.eps_inner_p,
+                                    ws=self._ws_flex(), inner_ws=self.ws_p, use_graph=self.use_graph,
+                                    check_every=self.check_every_p)
+            self.last_accel = info
+            self.learned_stats[0] += fi.learned_used
+            self.learned_stats[1] += fi.learned_rejected
+            if info.ok:
+                return info
+            self.fallbacks += 1
+            plain = bicgstab(self.A_p, self.b_p, self.pcor, eps=self.cfg.eps, max_iter=self.A_p.n, ws=self.ws_p,
+                             use_graph=self.use_graph, persistent=self.persistent)
+            plain.iters += info.iters
+            return plain
         if self.mg is not None:
             self.mg.setup()
             # the pressure correction is symmetric: multigrid-preconditioned CG
@@ -212,6 +231,11 @@ class ChannelSolver:
             plain.iters += info.iters
             return plain
         return self._solve(self.A_p, getattr(self, "A_p32", None), self.b_p, self.pcor, self.ws_p)
+
+    def _ws_flex(self):
+        if self._flex_ws is None:
+            self._flex_ws = Workspace(self.device)
+        return self._flex_ws
 
     def correct(self):
         lib = L.load()
@@ -270,6 +294,12 @@ class ChannelSolver:
             setattr(c, "ws_" + k + "_bytes", buf.numel())
         if self.mg is not None:
             c.mg_ws, c.mg_ws_bytes, c.mg_opts = self.mg.ws.data_ptr(), self.mg.ws.numel(), self.mg.opts
+        if self.learned is not None and self.mg is not None:
+            NX, NY = self.b_p.shape
+            self._net = self.learned.native(NX, NY)          # kept alive with the descriptor
+            buf = self._ws_flex().get(lib.kc_pcg_flexible_ws_bytes(self.A_p.n))
+            c.learned = C.addressof(self._net)
+            c.ws_flex, c.ws_flex_bytes = buf.data_ptr(), buf.numel()
         self._chan = c
         return c
 
@@ -277,6 +307,8 @@ class ChannelSolver:
         st = L.KcChannelStats()
         L.check(L.load().kc_channel_step(C.byref(self.native_struct()), C.byref(st), self._s()), "kc_channel_step")
         self.fallbacks += st.fallbacks
+        self.learned_stats[0] += st.learned
+        self.learned_stats[1] += st.learned_rejected
         rec = [dict(mass=st.mass, it_u=st.it_u, it_v=st.it_v, it_p=st.it_p, outer=st.outer, status=st.status)]
         self.history.append(rec)
         return rec
@@ -284,7 +316,7 @@ class ChannelSolver:
     def step(self):
         """One time step; returns the per-outer-iteration records (native: one record
         with the step's totals and its outer-iteration count)."""
-        if self.native and self.learned is None:
+        if self.native:
             return self._step_native()
         rec = []
         for _ in range(self.cfg.max_outer):

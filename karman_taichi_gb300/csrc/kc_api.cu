@@ -148,6 +148,8 @@ size_t kc_struct_size(const char* name) {
     if (n == "kc_karman") return sizeof(kc_karman);
     if (n == "kc_channel") return sizeof(kc_channel);
     if (n == "kc_channel_stats") return sizeof(kc_channel_stats);
+    if (n == "kc_unet_net") return sizeof(kc_unet_net);
+    if (n == "kc_flex_info") return sizeof(kc_flex_info);
     return 0;
 }
 }  // extern "C"

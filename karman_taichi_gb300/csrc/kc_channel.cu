@@ -146,9 +146,19 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
             if (rc < 0) return rc;
             const kc_solve_opts o =
                 opts_of(c->eps, 50 * Ap.n, KC_REL_B, c->check_every_p > 0 ? c->check_every_p : 4, c->use_graph, 0);
-            rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, nullptr, c->mg_ws, &c->mg_opts, c->ws_p, c->ws_p_bytes,
-                                &o, c->eps_inner_p, 30, &ip, s);
-            if (rc < 0) return rc;
+            if (c->learned) {
+                // the network as the first preconditioner application of a flexible CG
+                kc_flex_info fi{};
+                rc = kc_pcg_flexible(&Ap, &Ap32, c->b_p, c->pcor, c->learned, c->mg_ws, &c->mg_opts, c->ws_p,
+                                     c->ws_p_bytes, c->ws_flex, c->ws_flex_bytes, &o, c->eps_inner_p, 30, &ip, &fi, s);
+                if (rc < 0) return rc;
+                S.learned += fi.learned_used;
+                S.learned_rejected += fi.learned_rejected;
+            } else {
+                rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, nullptr, c->mg_ws, &c->mg_opts, c->ws_p,
+                                    c->ws_p_bytes, &o, c->eps_inner_p, 30, &ip, s);
+                if (rc < 0) return rc;
+            }
             if (ip.status != KC_OK) {   // accelerated solve stalled: plain BiCGSTAB is the fallback
                 ++S.fallbacks;
                 const long long before = ip.iters;

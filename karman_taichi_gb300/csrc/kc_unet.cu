@@ -702,3 +702,120 @@ int kc_unet_target_down2(const double* p, const float* coef32, int NX, int NY, c
 }
 
 }  // extern "C"
+
+// ---- native prediction: features -> U-Net forward -> upsampled guess ------------------------
+// The fixed architecture (4 levels, 16/32/48/64 channels, two 3x3 convolutions
+// with ReLU per level, 2x2 average pooling, nearest upsampling with skip
+// concatenation, 1x1 head) run from C++, so that a caller without Python (the
+// native SIMPLE step) can apply the network.  Parameters are one flat buffer,
+// layer by layer: w [9][cout][cin] then b [cout], then the head's w [16] and
+// b [1]; `params` is the FP32 copy (biases, head), `params16` the BF16 copy
+// (convolution weights) at the same element offsets.
+namespace {
+struct UnetLayer {
+    int cin, cout;
+};
+constexpr int kUnetLayers = 14;
+constexpr UnetLayer kUnet[kUnetLayers] = {{16, 16}, {16, 16}, {16, 32}, {32, 32}, {32, 48}, {48, 48}, {48, 64},
+                                          {64, 64}, {112, 48}, {48, 48}, {80, 32}, {32, 32}, {48, 16}, {16, 16}};
+
+struct UnetPlan {
+    int Hf, Wf, Hh, Wh;          // full-resolution feature grid, network grid
+    size_t off[32];              // byte offsets in the workspace
+    size_t total;
+};
+// workspace slots
+enum { kSlotFull, kFluid, kScales, kFeatWs, kIn, kE0a, kS0, kX1, kE1a, kS1, kX2, kE2a, kS2, kX3, kB3a, kY3, kC2, kD2a,
+       kY2, kC1, kD1a, kY1, kC0, kD0a, kY0, kOut, kSlots };
+
+UnetPlan unet_plan(int NX, int NY) {
+    UnetPlan P{};
+    P.Hf = (NX + 15) / 16 * 16;
+    P.Wf = (NY + 15) / 16 * 16;
+    P.Hh = P.Hf / 2;
+    P.Wh = P.Wf / 2;
+    const size_t h0 = (size_t)P.Hh * P.Wh, h1 = h0 / 4, h2 = h0 / 16, h3 = h0 / 64, b2 = 2;
+    const size_t bytes[kSlots] = {(size_t)P.Hf * P.Wf * 16 * b2, (size_t)NX * NY * 4, 4 * 8,
+                                  kc_unet_features_ws_bytes(NX), h0 * 16 * b2, h0 * 16 * b2, h0 * 16 * b2,
+                                  h1 * 16 * b2, h1 * 32 * b2, h1 * 32 * b2, h2 * 32 * b2, h2 * 48 * b2,
+                                  h2 * 48 * b2, h3 * 48 * b2, h3 * 64 * b2, h3 * 64 * b2, h2 * 112 * b2,
+                                  h2 * 48 * b2, h2 * 48 * b2, h1 * 80 * b2, h1 * 32 * b2, h1 * 32 * b2,
+                                  h0 * 48 * b2, h0 * 16 * b2, h0 * 16 * b2, h0 * 4};
+    size_t o = 0;
+    for (int q = 0; q < kSlots; ++q) {
+        P.off[q] = o;
+        o = align256(o + bytes[q]);
+    }
+    P.total = o;
+    return P;
+}
+}  // namespace
+
+extern "C" {
+
+long long kc_unet_param_count(void) {
+    long long n = 0;
+    for (const auto& l : kUnet) n += 9ll * l.cout * l.cin + l.cout;
+    return n + 16 + 1;
+}
+
+size_t kc_unet_predict_ws_bytes(int NX, int NY) {
+    if (NX < 1 || NY < 1) return 0;
+    return unet_plan(NX, NY).total;
+}
+
+int kc_unet_predict(const kc_unet_net* net, const double* b, const float* coef32, double* x0, void* stream) {
+    if (!net || !net->params || !net->params16 || !b || !coef32 || !x0)
+        return set_error("kc_unet_predict: null argument"), KC_ERR_ARG;
+    const int NX = net->NX, NY = net->NY;
+    if (NX < 2 || NY < 2) return set_error("kc_unet_predict: grid %d x %d too small", NX, NY), KC_ERR_ARG;
+    const UnetPlan P = unet_plan(NX, NY);
+    if (!net->ws || net->ws_bytes < P.total || ((uintptr_t)net->ws & 255))
+        return set_error("kc_unet_predict: workspace %zu bytes (256-aligned) < required %zu", net->ws_bytes, P.total),
+               KC_ERR_WORKSPACE;
+    char* w = (char*)net->ws;
+    auto at = [&](int slot) { return (void*)(w + P.off[slot]); };
+    int rc = kc_unet_features(b, coef32, NX, NY, P.Hf, P.Wf, at(kSlotFull), (float*)at(kFluid), (double*)at(kScales),
+                              at(kFeatWs), kc_unet_features_ws_bytes(NX), stream);
+    if (rc) return rc;
+    rc = kc_unet_pool2(at(kSlotFull), P.Hf, P.Wf, 16, at(kIn), stream);
+    if (rc) return rc;
+    // parameter offsets, in elements, layer by layer
+    long long wo[kUnetLayers], bo[kUnetLayers], o = 0;
+    for (int l = 0; l < kUnetLayers; ++l) {
+        wo[l] = o;
+        o += 9ll * kUnet[l].cout * kUnet[l].cin;
+        bo[l] = o;
+        o += kUnet[l].cout;
+    }
+    const long long head_w = o, head_b = o + 16;
+    const float* pf = (const float*)net->params;
+    const unsigned short* p16 = (const unsigned short*)net->params16;
+    int dims[4][2] = {{P.Hh, P.Wh}, {P.Hh / 2, P.Wh / 2}, {P.Hh / 4, P.Wh / 4}, {P.Hh / 8, P.Wh / 8}};
+    auto conv = [&](int l, int lvl, int sx, int sy) {
+        return kc_unet_conv3x3(at(sx), dims[lvl][0], dims[lvl][1], kUnet[l].cin, p16 + wo[l], 0, pf + bo[l],
+                               kUnet[l].cout, 1, nullptr, at(sy), 0, stream);
+    };
+    // encoder
+    if ((rc = conv(0, 0, kIn, kE0a)) || (rc = conv(1, 0, kE0a, kS0))) return rc;
+    if ((rc = kc_unet_pool2(at(kS0), dims[0][0], dims[0][1], 16, at(kX1), stream))) return rc;
+    if ((rc = conv(2, 1, kX1, kE1a)) || (rc = conv(3, 1, kE1a, kS1))) return rc;
+    if ((rc = kc_unet_pool2(at(kS1), dims[1][0], dims[1][1], 32, at(kX2), stream))) return rc;
+    if ((rc = conv(4, 2, kX2, kE2a)) || (rc = conv(5, 2, kE2a, kS2))) return rc;
+    if ((rc = kc_unet_pool2(at(kS2), dims[2][0], dims[2][1], 48, at(kX3), stream))) return rc;
+    // bottleneck
+    if ((rc = conv(6, 3, kX3, kB3a)) || (rc = conv(7, 3, kB3a, kY3))) return rc;
+    // decoder
+    if ((rc = kc_unet_up2_concat(at(kY3), 64, at(kS2), 48, dims[2][0], dims[2][1], at(kC2), stream))) return rc;
+    if ((rc = conv(8, 2, kC2, kD2a)) || (rc = conv(9, 2, kD2a, kY2))) return rc;
+    if ((rc = kc_unet_up2_concat(at(kY2), 48, at(kS1), 32, dims[1][0], dims[1][1], at(kC1), stream))) return rc;
+    if ((rc = conv(10, 1, kC1, kD1a)) || (rc = conv(11, 1, kD1a, kY1))) return rc;
+    if ((rc = kc_unet_up2_concat(at(kY1), 32, at(kS0), 16, dims[0][0], dims[0][1], at(kC0), stream))) return rc;
+    if ((rc = conv(12, 0, kC0, kD0a)) || (rc = conv(13, 0, kD0a, kY0))) return rc;
+    if ((rc = kc_unet_head(at(kY0), 16, (long long)P.Hh * P.Wh, pf + head_w, pf + head_b, (float*)at(kOut), stream)))
+        return rc;
+    return kc_unet_guess_up2((const float*)at(kOut), P.Hh, P.Wh, coef32, NX, NY, (const double*)at(kScales), x0,
+                             stream);
+}
+
+}  // extern "C"

@@ -300,6 +300,26 @@ class UNet:
                                     ptr(loss), stream_handle(self.device)), "kc_unet_mse")
         return loss, dout
 
+    # ---- native use ---------------------------------------------------------------------
+    def native_net(self, NX, NY):
+        """A ``kc_unet_net`` for the p' grid [NX][NY]: this network's FP32 and
+        BF16 parameters and a device workspace, for kc_unet_predict and the
+        flexible solve of the native SIMPLE step (no Python in the loop)."""
+        lib = L.load()
+        if lib.kc_unet_param_count() != self.n_params:
+            raise ValueError("parameter layout differs from the library's U-Net")
+        key = (NX, NY)
+        if getattr(self, "_native", None) is None or self._native[0] != key:
+            nbytes = lib.kc_unet_predict_ws_bytes(NX, NY)
+            ws = torch.zeros(nbytes + 256, dtype=torch.uint8, device=self.device)
+            off = (-ws.data_ptr()) % 256
+            n = L.KcUnetNet()
+            n.NX, n.NY = NX, NY
+            n.params, n.params16 = self.p.data_ptr(), self.p16.data_ptr()
+            n.ws, n.ws_bytes = ws.data_ptr() + off, nbytes
+            self._native = (key, n, ws)
+        return self._native[1]
+
     # ---- persistence --------------------------------------------------------------------
     def save(self, path):
         os.makedirs(os.path.dirname(path), exist_ok=True)
@@ -366,13 +386,20 @@ class Featurizer:
 
 
 class LearnedGuess:
-    """ChannelSolver hook: predict(solver) -> FP64 initial guess of p'."""
+    """ChannelSolver hook.  The accelerated solver applies the network through
+    ``native(NX, NY)`` as the first preconditioner application of a flexible
+    CG (kc_pcg_flexible, inside the native step); ``predict(solver)`` is the
+    same prediction driven from Python (training, tests, the initial-guess
+    use)."""
 
     def __init__(self, net: UNet):
         self.net = net
         self.fz = None
         self.x0 = None
         self.calls = 0
+
+    def native(self, NX, NY):
+        return self.net.native_net(NX, NY)
 
     def predict(self, solver):
         NX, NY = solver.b_p.shape

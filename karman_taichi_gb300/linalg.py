@@ -378,3 +378,27 @@ def pcg_refined(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, mg
     iterative refinement; same contract as :func:`pbicgstab_refined`."""
     return _mg_refined("kc_pcg_refined", A64, A32, b, x, mg, eps, eps_inner, max_refine, max_iter, x0, ws,
                        use_graph, check_every)
+
+
+def pcg_flexible(A64: Stencil, A32: Stencil, b: torch.Tensor, x: torch.Tensor, mg: Multigrid, *, net=None,
+                 eps=1e-8, eps_inner=1e-4, max_outer=30, max_iter=None, warm=False, ws: Workspace | None = None,
+                 inner_ws: Workspace | None = None, use_graph=True, check_every=4):
+    """Flexible CG (FP64 outer vectors) whose first preconditioner application
+    is the trained network's prediction (``net``: a ``kc_unet_net`` structure,
+    see ``learned.UNet.native_net``; None for none) and every later one a
+    multigrid-preconditioned FP32 CG pass (kc_pcg_flexible).  Returns
+    (SolveInfo, KcFlexInfo); KC_STALL when two outer iterations in a row cut
+    the residual by less than 10 %."""
+    require_cuda(b, x)
+    lib = L.load()
+    buf = (ws or Workspace(b.device)).get(lib.kc_pcg_flexible_ws_bytes(A64.n))
+    ibuf = (inner_ws or Workspace(b.device)).get(lib.kc_pbicgstab_ws_bytes(A64.n, A64.stride))
+    o = _opts(eps, 50 * A64.n if max_iter is None else max_iter, L.X0_WARM if warm else L.X0_ZERO, L.PRECOND_NONE, 0,
+              L.REL_B, check_every, use_graph, None, False)
+    info, fi = L.KcSolveInfo(), L.KcFlexInfo()
+    rc = lib.kc_pcg_flexible(C.byref(A64.system), C.byref(A32.system), ptr(b), ptr(x),
+                             C.byref(net) if net is not None else None, ptr(mg.ws), C.byref(mg.opts), ptr(ibuf),
+                             ibuf.numel(), ptr(buf), buf.numel(), C.byref(o), float(eps_inner), int(max_outer),
+                             C.byref(info), C.byref(fi), stream_handle(b.device))
+    L.check(rc, "kc_pcg_flexible")
+    return SolveInfo(info.status, info.iters, info.rel_res, info.r0, info.refinements), fi

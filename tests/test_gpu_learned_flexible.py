@@ -1,0 +1,141 @@
+"""The trained network as a flexible preconditioner of the p' solve.
+
+kc_unet_predict runs the U-Net from native code; kc_pcg_flexible is a
+flexible CG (FP64 outer vectors) whose first preconditioner application is
+the network's prediction and every later one a multigrid CG pass; the native
+SIMPLE step uses it when a network is attached.  These tests check the native
+prediction against the Python-driven forward pass (the same kernels in the
+same order: bitwise), the flexible solve against the multigrid CG solve (both
+to ||b - A x|| / ||b|| < 1e-8: solutions agree to 1e-6 relative), the
+rejection of a poisoned network (NaN parameters: its direction is replaced by
+a multigrid pass, the solve still converges), the fallback to the plain
+BiCGSTAB when the flexible solve stalls, and that the native step with a
+network computes what the Python step computes (bitwise).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(nx=128, ny=32, max_outer=4):
+    from karman_taichi_gb300.config import ChannelConfig
+    return ChannelConfig("flex", nx, ny, 1.0 / ny, 6, (("circle", nx // 4, ny // 2, 6),), max_outer=max_outer)
+
+
+def _assembled(dev, cfg=None):
+    """A mixed-precision channel solver with its first p' system assembled."""
+    from karman_taichi_gb300.channel import ChannelSolver
+    s = ChannelSolver(cfg or _cfg(), device=dev, precision="mixed", native=False)
+    s.assemble_momentum(); s.solve_momentum(); s.relax(); s.assemble_p()
+    s.mg.setup()
+    return s
+
+
+def _net(dev, seed=0):
+    from karman_taichi_gb300 import learned
+    return learned.UNet(dev, seed=seed)
+
+
+def test_native_prediction_is_the_python_forward_pass(dev):
+    import ctypes as C
+    import torch
+    from karman_taichi_gb300 import _lib as L, learned
+    from karman_taichi_gb300.linalg import stream_handle
+    s = _assembled(dev)
+    g = learned.LearnedGuess(_net(dev))
+    x_py = g.predict(s).clone()
+    NX, NY = s.b_p.shape
+    x_nat = torch.zeros_like(x_py)
+    rc = L.load().kc_unet_predict(C.byref(g.native(NX, NY)), s.b_p.data_ptr(), s.coef_p32.data_ptr(),
+                                  x_nat.data_ptr(), stream_handle(s.device))
+    L.check(rc, "kc_unet_predict")
+    torch.cuda.synchronize()
+    assert torch.isfinite(x_nat).all()
+    assert torch.equal(x_nat, x_py)
+
+
+@pytest.mark.parametrize("with_net", [True, False])
+def test_flexible_solve_matches_multigrid_cg(dev, with_net):
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    s = _assembled(dev)
+    NX, NY = s.b_p.shape
+    net = _net(dev).native_net(NX, NY) if with_net else None
+    x = torch.zeros_like(s.b_p)
+    info, fi = linalg.pcg_flexible(s.A_p, s.A_p32, s.b_p, x, s.mg, net=net, eps=1e-8)
+    assert info.status == L.OK, info
+    assert fi.learned_used == (1 if with_net else 0) and fi.learned_rejected == 0 and fi.outer >= 1
+    ref = torch.zeros_like(s.b_p)
+    r = linalg.pcg_refined(s.A_p, s.A_p32, s.b_p, ref, s.mg, eps=1e-8)
+    assert r.ok
+    err = (x - ref).abs().max() / ref.abs().max()
+    assert err < 1e-6, float(err)
+    # the true residual meets the tolerance
+    res = s.b_p - linalg.spmv(s.A_p, x)
+    assert float(res.norm() / s.b_p.norm()) < 1e-8
+
+
+def test_poisoned_network_is_rejected(dev):
+    """NaN parameters: the network's direction is not finite, a multigrid pass replaces it, the solve
+    converges to the same solution."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    s = _assembled(dev)
+    NX, NY = s.b_p.shape
+    u = _net(dev)
+    u.p.fill_(float("nan"))
+    u._sync_bf16()
+    x = torch.zeros_like(s.b_p)
+    info, fi = linalg.pcg_flexible(s.A_p, s.A_p32, s.b_p, x, s.mg, net=u.native_net(NX, NY), eps=1e-8)
+    assert info.status == L.OK, info
+    assert fi.learned_used == 1 and fi.learned_rejected == 1
+    ref = torch.zeros_like(s.b_p)
+    assert linalg.pcg_refined(s.A_p, s.A_p32, s.b_p, ref, s.mg, eps=1e-8).ok
+    assert float((x - ref).abs().max() / ref.abs().max()) < 1e-6
+
+
+def test_stalled_flexible_solve_falls_back_to_plain_bicgstab(dev):
+    """With the FP32 copy of the p' system poisoned (links scaled by seeded random factors) the
+    multigrid passes aim at another operator: the flexible solve stalls (or breaks down), the solver
+    counts a fallback and the plain FP64 BiCGSTAB solves p' to the same fields as a clean run."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, learned
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfg = _cfg(max_outer=3).with_(eps=1e-10)
+    net = _net(dev)
+    poisoned = ChannelSolver(cfg, device=dev, precision="mixed", native=False, learned=learned.LearnedGuess(net))
+    clean = ChannelSolver(cfg, device=dev, precision="mixed", native=False, learned=learned.LearnedGuess(net))
+    g = torch.Generator(device=dev).manual_seed(5)
+    orig = poisoned.assemble_p
+
+    def assemble_then_poison():
+        orig()
+        noise = 0.5 + torch.rand(poisoned.coef_p32[1:].shape, generator=g, device=dev, dtype=torch.float32)
+        poisoned.coef_p32[1:].mul_(noise)
+
+    poisoned.assemble_p = assemble_then_poison
+    rp, rc = poisoned.step(), clean.step()
+    assert poisoned.fallbacks >= len(rp) and clean.fallbacks == 0
+    assert poisoned.last_accel.status != L.OK
+    assert all(r["st"][2] == L.OK for r in rp)
+    a, b = poisoned.state_numpy(), clean.state_numpy()
+    for k in ("u", "v", "p"):
+        assert np.abs(a[k] - b[k]).max() <= 1e-6 * np.abs(b[k]).max(), k
+
+
+def test_native_step_with_network_matches_python_step(dev):
+    from karman_taichi_gb300 import learned
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfg = _cfg(max_outer=5)
+    net = _net(dev, seed=3)
+    a = ChannelSolver(cfg, device=dev, precision="mixed", native=True, learned=learned.LearnedGuess(net))
+    b = ChannelSolver(cfg, device=dev, precision="mixed", native=False, learned=learned.LearnedGuess(net))
+    for _ in range(2):
+        ra, rb = a.step(), b.step()
+        assert ra[0]["outer"] == len(rb)
+        assert ra[0]["it_p"] == sum(r["it_p"] for r in rb)
+    assert a.learned_stats == b.learned_stats and a.learned_stats[0] == 2 * cfg.max_outer
+    sa, sb = a.state_numpy(), b.state_numpy()
+    for k in ("u", "v", "p", "u0", "v0"):
+        assert np.array_equal(sa[k], sb[k]), k
