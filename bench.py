@@ -478,7 +478,12 @@ def run_gpu(args):
             out["learned"] = {"value": round(args.steps / (lms * 1e-3), 5), "unit": "time steps/s",
                               "ms_per_step": round(lms / args.steps, 3), "p_iters_per_step": lsum["p_iters_per_step"],
                               "outer_per_step": lsum["outer_per_step"], "mass_residual_max": lsum["mass_residual_max"],
-                              "note": "same steps with the U-Net initial guess of p' (Python-driven outer loop)"}
+                              "network_applied": lsol.learned_stats[0], "network_rejected": lsol.learned_stats[1],
+                              "fallbacks": lsol.fallbacks,
+                              "window": f"time steps {args.warmup + 1}..{args.warmup + args.steps}, as value",
+                              "note": "same steps, native step; every p' solve a flexible CG whose first "
+                                      "preconditioner application is the U-Net's prediction, then multigrid CG "
+                                      "passes (kc_pcg_flexible); p_iters_per_step counts the inner CG iterations"}
             del lsol
 
     if rank == 0 and not args.no_compare and mode != "fp64":
