@@ -64,6 +64,9 @@ def parse():
                     help="seconds of whole CPU time steps (at least one step is always timed)")
     ap.add_argument("--spmv-sweep", action="store_true",
                     help="time k_spmv (FP64, FP32) on random 5-point systems of 1M, 4M and 17M cells and exit")
+    ap.add_argument("--pcorr1024", action="store_true",
+                    help="the isolated 1024 x 1024 pressure-correction solve (random aP, 5%% blocked blobs), plain "
+                         "FP64 BiCGSTAB and FP32 multigrid CG in FP64 refinement, to rel. tol 1e-8, and exit")
     ap.add_argument("--batch-instances", type=int, default=0, metavar="N",
                     help="time the batched configuration (N independent channel instances, stream-parallel) and exit")
     ap.add_argument("--batch-workers", type=int, default=16)
@@ -598,6 +601,80 @@ def run_spmv_sweep(args):
     print(json.dumps({"spmv_sweep": rows}), flush=True)
 
 
+def run_pcorr1024(args):
+    """The isolated 1024 x 1024 p' solve: plain FP64 BiCGSTAB (the reference
+    method, persistent launch) and the FP32 multigrid-preconditioned CG in FP64
+    refinement (kc_pcg_refined), both to ||r||/||b|| < 1e-8 from x = 0.  Each
+    solve is timed with CUDA events after one untimed solve of the same
+    system (graphs instantiated, multigrid set up); the multigrid setup is
+    timed separately.  Error: max |x - x_fp64| / max |x_fp64|."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, linalg
+    from karman_taichi_gb300.workloads import pcorr_random_system
+    peak, kind = peaks()
+    dev = torch.device("cuda", 0)
+    c, b = pcorr_random_system(1024, seed=0)
+    n = c[0].size
+    c64 = torch.from_numpy(c).to(dev)
+    lap = c64.clone()
+    lap[0] = c64[0] + (((c64[1] + c64[2]) + c64[3]) + c64[4])
+    A64 = linalg.Stencil(c64)
+    A32 = linalg.Stencil(lap.float().contiguous(), form=L.FORM_LAPLACIAN)
+    bt = torch.from_numpy(b).to(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    out = {"metric": "isolated p' solve, 1024 x 1024, rel. tol 1e-8", "config": {"workload": "pcorr_random_1024",
+           "cells": int(n), "blocked": 0.05, "aP_face": "log-uniform [1, 10]"}, "peak_gbs": peak, "peak_kind": kind}
+    # plain FP64 BiCGSTAB
+    ws = linalg.Workspace(dev)
+    x64 = torch.zeros_like(bt)
+    linalg.bicgstab(A64, bt, x64, eps=1e-8, max_iter=n, ws=ws)
+    x64.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record()
+    i64 = linalg.bicgstab(A64, bt, x64, eps=1e-8, max_iter=n, ws=ws)
+    e1.record()
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1)
+    alg64 = 27 * 8 * n * i64.iters
+    out["fp64_bicgstab"] = {"status": i64.status_name, "iters": i64.iters, "ms": round(t64, 3),
+                            "ms_per_iter": round(t64 / max(i64.iters, 1), 4),
+                            "achieved_gbs": round(alg64 / (t64 * 1e-3) / 1e9, 1),
+                            "frac": round(alg64 / (t64 * 1e-3) / 1e9 / peak, 4),
+                            "bytes_note": "27 words (8 B) per cell per iteration"}
+    # FP32 multigrid CG in FP64 refinement
+    mg = linalg.Multigrid(A32)
+    torch.cuda.synchronize()
+    e0.record()
+    mg.setup()
+    e1.record()
+    torch.cuda.synchronize()
+    tsetup = e0.elapsed_time(e1)
+    wsp = linalg.Workspace(dev)
+    x32 = torch.zeros_like(bt)
+    linalg.pcg_refined(A64, A32, bt, x32, mg, eps=1e-8, ws=wsp)
+    x32.zero_()
+    torch.cuda.synchronize()
+    e0.record()
+    im = linalg.pcg_refined(A64, A32, bt, x32, mg, eps=1e-8, ws=wsp)
+    e1.record()
+    torch.cuda.synchronize()
+    tm = e0.elapsed_time(e1)
+    algm = PCG_MG_BYTES_PER_CELL * n * im.iters + (im.refinements + 1) * 7 * 8 * n
+    out["mixed_mg_cg"] = {"status": im.status_name, "iters": im.iters, "refinements": im.refinements,
+                          "ms": round(tm, 3), "ms_per_iter": round(tm / max(im.iters, 1), 4),
+                          "setup_ms": round(tsetup, 3),
+                          "achieved_gbs": round(algm / (tm * 1e-3) / 1e9, 1),
+                          "frac": round(algm / (tm * 1e-3) / 1e9 / peak, 4),
+                          "bytes_note": f"{PCG_MG_BYTES_PER_CELL} B per cell per CG iteration + 56 B per cell per "
+                                        "FP64 refinement residual"}
+    res = lambda x: float((bt - linalg.spmv(A64, x)).norm() / bt.norm())
+    out["rel_residual"] = {"fp64_bicgstab": res(x64), "mixed_mg_cg": res(x32)}
+    out["error_vs_fp64"] = float((x32 - x64).abs().max() / x64.abs().max())
+    out["speedup_mixed_vs_fp64"] = round(t64 / tm, 2)
+    print(json.dumps(out), flush=True)
+
+
 def run_batch(args, cfgs=None, workload=None):
     """Instance time steps/s of the batched configuration: N instances (sizes
     128x32 .. 640x128, D 4-16, Re 60-200) stepped concurrently, one CUDA stream
@@ -659,6 +736,8 @@ if __name__ == "__main__":
         run_profile_outer(a)
     elif a.spmv_sweep:
         run_spmv_sweep(a)
+    elif a.pcorr1024:
+        run_pcorr1024(a)
     elif a.copies > 0:
         from karman_taichi_gb300.config import PRESETS
         base = PRESETS[a.config]

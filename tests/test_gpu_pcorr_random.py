@@ -43,3 +43,13 @@ def test_pcorr_random_1024_fp64_and_mixed_agree(dev):
         assert np.linalg.norm(res) / np.linalg.norm(b) < 1e-11
     a1, a2 = x1.cpu().numpy(), x2.cpu().numpy()
     assert np.abs(a1 - a2).max() <= 1e-6 * np.abs(a1).max()
+
+
+def test_workload_generator_is_the_oracle_system():
+    """bench.py builds the 1024 x 1024 system with the package's generator; it is the oracle's, array
+    for array."""
+    from karman_taichi_gb300.workloads import pcorr_random_system
+    for N, seed in ((64, 1), (130, 4)):
+        c1, b1 = pcorr_random_system(N, seed=seed)
+        c2, b2 = O.pcorr_random_system(N, seed=seed)
+        assert np.array_equal(c1, c2) and np.array_equal(b1, b2)
