@@ -404,6 +404,18 @@ int kc_correct(const kc_phys* P, const double* pcor, const double* coef_u,
                double* p, double* pcor_max_dev, void* ws, void* stream);
 
 /* mdiv and max|mdiv| of the current field (simple.py:137-141; bicgsimp.py:114-122). */
+/* One in-place lexicographic relaxation sweep of A x = b over the box
+ * i in [i0, i1), j in [j0, j1) of a [NX][NY] field, i outer and j inner, as
+ * jacosimp.py:226-247 runs it in Python scope:
+ *   x_mid = (-aW x[i-1,j] - aE x[i+1,j] - aN x[i,j+1] - aS x[i,j-1] + b) / aP
+ *   relax: x_mid[i,j] = x_mid, x = (1 - omega) x + omega x_mid;  else x = x_mid
+ * where the west and south neighbours already hold this sweep's values.  One
+ * block sweeps the anti-diagonals in order: the serial sweep's values exactly
+ * (FP64, the reference's operation order).  Coefficient c of (i, j) at
+ * coef[c*cs + (i*NY + j)*es]; the box must leave a 1-cell ring. */
+int kc_lex_sweep(const double* coef, long long cs, long long es, int NX, int NY, int i0, int i1,
+                 int j0, int j1, const double* b, double* x, double* x_mid, double omega, int relax,
+                 void* stream);
 int kc_mass_residual(const kc_phys* P, const double* u, const double* v,
                      const unsigned char* solid, double* mdiv, double* mass_dev,
                      void* ws, void* stream);

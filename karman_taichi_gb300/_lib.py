@@ -162,6 +162,7 @@ SIGNATURES = {
     "kc_unet_param_count": (L_, []),
     "kc_unet_predict_ws_bytes": (S_, [I_, I_]),
     "kc_unet_predict": (I_, [C.POINTER(KcUnetNet), P_, P_, P_, P_]),
+    "kc_lex_sweep": (I_, [P_, L_, L_, I_, I_, I_, I_, I_, I_, P_, P_, P_, D_, I_, P_]),
     "kc_reduce_ws_bytes": (S_, []),
     "kc_assemble_momentum": (I_, [C.POINTER(KcPhys)] + [P_] * 14 + [P_]),
     "kc_apply_bc_values": (I_, [C.POINTER(KcPhys), P_, P_, P_]),

@@ -676,3 +676,56 @@ int kc_mass_residual(const kc_phys* P, const double* u, const double* v, const u
 }
 
 }  // extern "C"
+
+// ---- lexicographic relaxation sweep (jacosimp.py) -------------------------------------------
+// jacosimp.py:226-247 relaxes u, v and p' in Python scope, in place, i outer
+// and j inner: cell (i, j) reads its west (i-1, j) and south (i, j-1)
+// neighbours already updated in this sweep and its east and north neighbours
+// not yet updated.  Cells on one anti-diagonal i + j = d depend only on
+// diagonal d - 1, so one block sweeping the diagonals in order, with a barrier
+// between them, produces the serial sweep's values exactly; every cell's
+// arithmetic is the reference's expression in its order (this unit is
+// compiled without FMA contraction).
+namespace kc {
+__global__ void __launch_bounds__(1024)
+    k_lex_sweep(const double* __restrict__ c, long long cs, long long es, int NY, int i0, int i1, int j0, int j1,
+                const double* __restrict__ b, double* x, double* x_mid, double omega, int relax) {
+    const int ni = i1 - i0, nj = j1 - j0;
+    for (int d = 0; d < ni + nj - 1; ++d) {
+        const int a_lo = d - nj + 1 > 0 ? d - nj + 1 : 0, a_hi = d < ni - 1 ? d : ni - 1;
+        for (int a = a_lo + (int)threadIdx.x; a <= a_hi; a += (int)blockDim.x) {
+            const long long i = i0 + a, j = j0 + (d - a);
+            const long long k = i * NY + j;
+            const double* ck = c + k * es;
+            const double xm =
+                ((((-ck[cs] * x[k - NY]) - ck[2 * cs] * x[k + NY]) - ck[3 * cs] * x[k + 1]) - ck[4 * cs] * x[k - 1] +
+                 b[k]) / ck[0];
+            if (relax) {
+                x_mid[k] = xm;
+                x[k] = (1.0 - omega) * x[k] + omega * xm;
+            } else {
+                x[k] = xm;
+            }
+        }
+        __syncthreads();
+    }
+}
+}  // namespace kc
+
+extern "C" {
+
+int kc_lex_sweep(const double* coef, long long cs, long long es, int NX, int NY, int i0, int i1, int j0, int j1,
+                 const double* b, double* x, double* x_mid, double omega, int relax, void* stream) {
+    if (!coef || !b || !x || (relax && !x_mid)) return set_error("kc_lex_sweep: null argument"), KC_ERR_ARG;
+    if (NX < 3 || NY < 3 || cs < 1 || es < 1)
+        return set_error("kc_lex_sweep: bad grid %d x %d or strides", NX, NY), KC_ERR_ARG;
+    if (i0 < 1 || i1 > NX - 1 || j0 < 1 || j1 > NY - 1 || i0 >= i1 || j0 >= j1)
+        return set_error("kc_lex_sweep: box [%d, %d) x [%d, %d) must lie inside the 1-cell ring of %d x %d", i0, i1,
+                         j0, j1, NX, NY),
+               KC_ERR_ARG;
+    k_lex_sweep<<<1, 1024, 0, as_stream(stream)>>>(coef, cs, es, NY, i0, i1, j0, j1, b, x, x_mid, omega, relax);
+    KC_LAUNCH_CHECK("k_lex_sweep");
+    return KC_OK;
+}
+
+}  // extern "C"

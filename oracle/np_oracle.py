@@ -287,6 +287,8 @@ class SimpleOracle:
         self.rho, self.mu, self.dt = 1.0, 0.01, 10000.0
         self.alpha_p = self.alpha_u = self.alpha_m = 0.001
         self.bicgsimp = bicgsimp
+        if bicgsimp:   # bicgsimp.py:18-25
+            self.dt, self.alpha_p, self.alpha_u, self.alpha_m = 1e12, 0.1, 0.8, 0.05
         z = np.zeros
         self.u = z((nx + 3, ny + 2)); self.v = z((nx + 2, ny + 3))
         self.u_mid = z((nx + 3, ny + 2)); self.v_mid = z((nx + 2, ny + 3))
@@ -403,7 +405,8 @@ class SimpleOracle:
             rv = bicgstab(self.coef_v, self.b_v, self.b_v.shape[1], eps=eps)
             self.u_mid[...] = ru.x.reshape(self.u_mid.shape)
             self.v_mid[...] = rv.x.reshape(self.v_mid.shape)
-            self.update_velocity()
+            # bicgsimp.py:209-210 returns update_velocity's max-change residual
+            self.last_momentum_residual = self.update_velocity()
         return ru, rv
 
     def solve_pcorrection_eqn(self, eps=1e-2):  # simple.py:252-255
@@ -1182,6 +1185,71 @@ def pcorr_random_system(N=1024, seed=0, blocked=0.05):
     m[pin] = False
     b[m] -= b[m].mean()
     return c, b
+
+
+def lex_sweep(coef, b, x, box, omega=1.0, relax=True, x_mid=None):
+    """One in-place lexicographic relaxation sweep over the box (i0, i1, j0, j1),
+    i outer and j inner, as jacosimp.py:226-247 runs it in Python scope: each
+    cell reads its west and south neighbours already updated.  The cells of an
+    anti-diagonal i + j = d depend only on diagonal d - 1, so the sweep is
+    evaluated diagonal by diagonal with NumPy, each cell in the reference's
+    operation order.  coef: [5][NX][NY]."""
+    i0, i1, j0, j1 = box
+    ni, nj = i1 - i0, j1 - j0
+    for d in range(ni + nj - 1):
+        a = np.arange(max(0, d - nj + 1), min(ni - 1, d) + 1)
+        i, j = i0 + a, j0 + (d - a)
+        xm = ((((-coef[1, i, j] * x[i - 1, j]) - coef[2, i, j] * x[i + 1, j]) - coef[3, i, j] * x[i, j + 1])
+              - coef[4, i, j] * x[i, j - 1] + b[i, j]) / coef[0, i, j]
+        if relax:
+            if x_mid is not None:
+                x_mid[i, j] = xm
+            x[i, j] = (1.0 - omega) * x[i, j] + omega * xm
+        else:
+            x[i, j] = xm
+    return x
+
+
+class JacoSimpleOracle(SimpleOracle):
+    """Restatement of jacosimp.py:9-272: simple.py's assembly (jacosimp.py's
+    compute_coef_u/v/p and set_bc are simple.py's), lexicographic relaxation
+    sweeps instead of solves, constants of jacosimp.py:18-25."""
+
+    def __init__(self, lx, ly, nx, ny):
+        super().__init__(lx, ly, nx, ny)
+        self.dt = 100000.0
+        self.alpha_p = 0.01
+        self.alpha_u = 0.01
+        self.alpha = 0.1
+
+    def jaco_momentum(self):  # jacosimp.py:226-240
+        nx, ny = self.nx, self.ny
+        self.compute_coef_u(); self.compute_coef_v(); self.set_bc()
+        lex_sweep(self.coef_u, self.b_u, self.u, (2, nx + 1, 1, ny + 1), self.alpha_u, True, self.u_mid)
+        lex_sweep(self.coef_v, self.b_v, self.v, (1, nx + 1, 2, ny + 1), self.alpha_u, True, self.v_mid)
+
+    def jaco_pcorrection(self):  # jacosimp.py:242-247
+        self.compute_coef_p()
+        lex_sweep(self.coef_p, self.mdiv, self.pcor, (1, self.nx + 1, 1, self.ny + 1), 1.0, False)
+
+    def update_pressure(self):  # jacosimp.py:212-216
+        nx, ny = self.nx, self.ny
+        self.p[1:nx + 1, 1:ny + 1] += self.alpha_p * self.pcor[1:nx + 1, 1:ny + 1]
+
+    def jaco_update_velocity(self):  # jacosimp.py:218-224
+        nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
+        pc = self.pcor
+        I, J = slice(2, nx + 1), slice(1, ny + 1)
+        self.u[I, J] += self.alpha * (pc[1:nx, J] - pc[I, J]) * dy / self.coef_u[0, I, J]
+        I, J = slice(1, nx + 1), slice(2, ny + 1)
+        self.v[I, J] += self.alpha * (pc[I, 1:ny] - pc[I, J]) * dx / self.coef_v[0, I, J]
+
+    def jaco_step(self):  # one step of jacosimp.py:253-268
+        self.jaco_momentum()
+        self.jaco_pcorrection()
+        self.update_pressure()
+        self.jaco_update_velocity()
+        self.compute_mdiv()
 
 
 def jacobi_sweep(coef, b, x, S, omega=1.0, region=None):

@@ -11,7 +11,8 @@ mount this repository was built beside) and runs only where that tree is;
 the tests read the committed ``.npz`` files and never import the reference.
 
 Usage:  python tests/golden/make_golden.py [case ...]
-Cases:  solvers  simple_cavity  karman_320x64  karman_640x128_fills
+Cases:  solvers  simple_cavity  bicgsimp_cavity  jacosimp_cavity  karman_320x64
+        karman_640x128_fills
         (default: all; each writes golden_<case>.npz)
 
 What is run, and what is skipped, per case:
@@ -377,7 +378,71 @@ def case_karman_640x128_fills(seed=11):
     save("karman_640x128_fills", {"ct": ct.astype(np.int8)}, meta)
 
 
-CASES = {"solvers": case_solvers, "simple_cavity": case_simple_cavity, "karman_320x64": case_karman_320x64,
+def case_bicgsimp_cavity(n_sub=8):
+    """bicgsimp.py's cavity (SIMPLESolver(1.0, 1.0, 50, 50), lid tangential velocity 1.0,
+    bicgsimp.py:333-371) stepped through the body of its SIMPLE loop (bicgsimp.py:302-326) with the
+    persistent solvers of bicgsimp.py:260-262; the matplotlib and GUI lines of solve() and the
+    module-level demo are not executed."""
+    install_standin()
+    sys.path.insert(0, REF)
+    mod, skipped = load_module("bicgsimp", os.path.join(REF, "bicgsimp.py"), keep_demo=False)
+    from bicgsolver import BICGSolver
+    from cgsolver import CGSolver
+    s = mod.SIMPLESolver(1.0, 1.0, 50, 50)
+    s.bc["n"][1] = 1.0
+    s.init()
+    s.u_momentum_solver = BICGSolver(s.coef_u, s.b_u, s.u_mid)
+    s.v_momentum_solver = BICGSolver(s.coef_v, s.b_v, s.v_mid)
+    s.p_correction_solver = CGSolver(s.coef_p, s.b_p, s.pcor)
+    arrays, subs = {}, []
+    for sub in range(n_sub):
+        mres = s.bicg_solve_momentum_eqn(1)
+        s.bicg_solve_pcorrection_eqn(1e-8)
+        s.correct_pressure()
+        s.correct_velocity()
+        cres = s.compute_mdiv()
+        subs.append(dict(momentum_residual=float(mres), continuity_residual=float(cres),
+                         cg_iters=len(s.p_correction_solver.history) - 1))
+        print(sub, subs[-1], flush=True)
+        if sub in (0, n_sub - 1):
+            for name in ("u", "v", "p", "pcor"):
+                arrays[f"sub{sub}_{name}"] = getattr(s, name).to_numpy()
+    meta = dict(lx=1.0, ly=1.0, nx=50, ny=50, bc_n_tangential=1.0, n_sub=n_sub, subs=subs, skipped_lines=skipped,
+                source="bicgsimp.py:258-330 (loop body :302-326), persistent solvers :260-262")
+    save("bicgsimp_cavity", arrays, meta)
+
+
+def case_jacosimp_cavity(n_steps=20):
+    """jacosimp.py's cavity (SIMPLESolver(1.0, 1.0, 51, 51), lid tangential velocity 1.0,
+    jacosimp.py:274-290): n_steps steps of its solve() loop (jacosimp.py:249-272) without the
+    every-100-steps dumps and its prints; the module-level demo is not executed."""
+    install_standin()
+    sys.path.insert(0, REF)
+    mod, skipped = load_module("jacosimp", os.path.join(REF, "jacosimp.py"), keep_demo=False)
+    s = mod.SIMPLESolver(1.0, 1.0, 51, 51)
+    s.bc["n"][1] = 1.0
+    s.init()
+    arrays = {}
+    for step in range(n_steps):
+        s.solve_momentum_eqn()
+        if step == 0:
+            arrays["step0_u_mid"] = s.u_mid.to_numpy()
+            arrays["step0_v_mid"] = s.v_mid.to_numpy()
+            arrays["step0_u_sweep"] = s.u.to_numpy()
+            arrays["step0_v_sweep"] = s.v.to_numpy()
+        s.solve_pcorrection_eqn()
+        s.update_pressure()
+        s.update_velocity()
+        s.compute_mdiv()
+        if step in (0, 4, n_steps - 1):
+            for name in ("u", "v", "p", "pcor", "mdiv"):
+                arrays[f"step{step}_{name}"] = getattr(s, name).to_numpy()
+    meta = dict(lx=1.0, ly=1.0, nx=51, ny=51, bc_n_tangential=1.0, n_steps=n_steps, saved_steps=[0, 4, n_steps - 1],
+                skipped_lines=skipped, source="jacosimp.py:11-272 (solve loop :249-272)")
+    save("jacosimp_cavity", arrays, meta)
+
+
+CASES = {"solvers": case_solvers, "bicgsimp_cavity": case_bicgsimp_cavity, "jacosimp_cavity": case_jacosimp_cavity, "simple_cavity": case_simple_cavity, "karman_320x64": case_karman_320x64,
          "karman_640x128_fills": case_karman_640x128_fills}
 
 if __name__ == "__main__":
