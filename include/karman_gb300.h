@@ -293,6 +293,27 @@ int kc_pcg_refined(const kc_system* A64, const kc_system* A32, const double* b, 
                    size_t ws_bytes, const kc_solve_opts* opts, double eps_inner,
                    int max_refine, kc_solve_info* info, void* stream);
 
+/* Initial guess for the next system of a sequence by Galerkin projection onto
+ * earlier solutions: x0 = Z y with (Z^T A Z) y = Z^T b, Z = [Z[0] .. Z[m-1]]
+ * (FP64 n-vectors, newest first).  x0 minimises the error's A-norm over
+ * span(Z), so for a symmetric positive definite A it starts no further from
+ * the solution than x0 = 0.  The SIMPLE loop solves one p' system per outer
+ * iteration (karman_taichi.py:633-659; simple.py:270-281) and successive
+ * corrections keep their shape: with the last four solutions the guess's
+ * relative residual is ~1e-4.  A vector whose Cholesky pivot falls below
+ * 1e-12 of its diagonal is dropped with the older ones; *used (nullable)
+ * gets the count kept.  m = 0 gives x0 = 0.  ws: kc_recycle_ws_bytes(n, m),
+ * 256-byte aligned.  No counterpart in the reference. */
+#define KC_RECYCLE_MAX 4
+size_t kc_recycle_ws_bytes(long long n, int m);
+int kc_recycle_guess(const kc_system* A64, const double* b, const double* const* Z, int m,
+                     double* x0, void* ws, size_t ws_bytes, int* used, void* stream);
+/* Ring of earlier solutions kept by a driver: count stored (<= capacity), head
+ * the slot the next solution goes to. */
+typedef struct {
+    int count, head;
+} kc_recycle_state;
+
 /* The trained network applied from native code: features of A x = b (the p'
  * system: b FP64 [NX][NY], coef32 its FP32 Laplacian-form SoA planes), the
  * U-Net forward pass at half resolution, and x0 = the upsampled prediction
@@ -554,7 +575,19 @@ typedef struct {
     const kc_unet_net* learned;
     void* ws_flex;
     size_t ws_flex_bytes;
+    /* KC_F32 without a network: recycle > 0 starts every p' solve from the
+     * Galerkin projection onto the last `recycle` (<= KC_RECYCLE_MAX) p'
+     * solutions (kc_recycle_guess).  ws_recycle: kc_channel_recycle_ws_bytes
+     * (the ring of solutions, the guess, the projection's scratch); rstate:
+     * the caller's ring bookkeeping, {0, 0} for an empty ring (reset it when
+     * the fields are reset). */
+    int recycle;
+    int pad2_;
+    void* ws_recycle;
+    size_t ws_recycle_bytes;
+    kc_recycle_state* rstate;
 } kc_channel;
+size_t kc_channel_recycle_ws_bytes(long long n_p, int recycle);
 
 typedef struct {
     int outer, fallbacks, status, pad_;   /* status: KC_OK; KC_MAXITER if a solve missed eps;

@@ -84,7 +84,13 @@ class KcChannel(C.Structure):
                                           "mass", "pmax", "rws", "ws_u", "ws_v", "ws_p")]
     _fields_ += [("ws_u_bytes", C.c_size_t), ("ws_v_bytes", C.c_size_t), ("ws_p_bytes", C.c_size_t),
                  ("mg_ws", C.c_void_p), ("mg_ws_bytes", C.c_size_t), ("mg_opts", KcMgOpts),
-                 ("learned", C.c_void_p), ("ws_flex", C.c_void_p), ("ws_flex_bytes", C.c_size_t)]
+                 ("learned", C.c_void_p), ("ws_flex", C.c_void_p), ("ws_flex_bytes", C.c_size_t),
+                 ("recycle", C.c_int), ("pad2_", C.c_int), ("ws_recycle", C.c_void_p),
+                 ("ws_recycle_bytes", C.c_size_t), ("rstate", C.c_void_p)]
+
+
+class KcRecycleState(C.Structure):
+    _fields_ = [("count", C.c_int), ("head", C.c_int)]
 
 
 class KcChannelStats(C.Structure):
@@ -163,6 +169,9 @@ SIGNATURES = {
     "kc_unet_predict_ws_bytes": (S_, [I_, I_]),
     "kc_unet_predict": (I_, [C.POINTER(KcUnetNet), P_, P_, P_, P_]),
     "kc_lex_sweep": (I_, [P_, L_, L_, I_, I_, I_, I_, I_, I_, P_, P_, P_, D_, I_, P_]),
+    "kc_recycle_ws_bytes": (S_, [L_, I_]),
+    "kc_recycle_guess": (I_, [C.POINTER(KcSystem), P_, P_, I_, P_, P_, S_, C.POINTER(C.c_int), P_]),
+    "kc_channel_recycle_ws_bytes": (S_, [L_, I_]),
     "kc_reduce_ws_bytes": (S_, []),
     "kc_assemble_momentum": (I_, [C.POINTER(KcPhys)] + [P_] * 14 + [P_]),
     "kc_apply_bc_values": (I_, [C.POINTER(KcPhys), P_, P_, P_]),

@@ -33,6 +33,7 @@ SOURCES = {
     "kc_channel.cu": [],
     "kc_smoothers.cu": [],
     "kc_flex.cu": [],
+    "kc_recycle.cu": [],
 }
 
 

@@ -50,7 +50,7 @@ EPS_INNER_GS = 1e-5
 class ChannelSolver:
     def __init__(self, cfg: ChannelConfig, device="cuda", precision="fp64", use_graph=True,
                  eps_inner=1e-3, learned=None, pcorr_precond="mg", mg_opts=None, eps_inner_p=1e-4, native=True,
-                 momentum="rbgs_refined"):
+                 momentum="rbgs_refined", recycle=4):
         """``momentum`` (mixed precision): "rbgs_refined" (default), FP32
         red-black Gauss-Seidel sweeps in FP64 refinement (several sweeps per
         launch; 12.95 against 11.53 time steps/s at 2048 x 512 on GB300);
@@ -60,7 +60,9 @@ class ChannelSolver:
         from the warm start cost more than the refined BiCGSTAB).  Both
         Gauss-Seidel variants hand over to the refined BiCGSTAB, from where
         they stopped, if they miss the tolerance.  The FP64 path always uses
-        the reference's BiCGSTAB."""
+        the reference's BiCGSTAB.  ``recycle`` (mixed precision without a
+        network): every p' solve starts from the Galerkin projection onto the
+        last ``recycle`` p' solutions (kc_recycle_guess; 0: from zero)."""
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         if momentum not in ("rbgs", "rbgs_refined", "bicgstab"):
@@ -106,6 +108,21 @@ class ChannelSolver:
         self.x0_p = None     # optional initial guess for p'
         self.learned_stats = [0, 0]   # p' solves that applied / rejected the network's prediction
         self._flex_ws = None
+        self.recycle = int(recycle) if (precision == "mixed" and learned is None and self.mg is not None) else 0
+        self._rstate = L.KcRecycleState()
+        self._rc_buf = None
+        if self.recycle:
+            n = (nx + 2) * (ny + 2)
+            nbytes = L.load().kc_channel_recycle_ws_bytes(n, self.recycle)
+            self._rc_raw = torch.zeros(nbytes + 256, dtype=torch.uint8, device=self.device)
+            off = (-self._rc_raw.data_ptr()) % 256
+            a256 = lambda b: (b + 255) // 256 * 256
+            R = self.recycle
+            # the native step's layout: R ring slots, the guess, the projection's scratch
+            self._rc_buf = self._rc_raw[off:off + nbytes]
+            self._rc_ring = self._rc_buf[:R * n * 8].view(torch.float64).view(R, n)
+            self._rc_x0 = self._rc_buf[a256(R * n * 8):a256(R * n * 8) + n * 8].view(torch.float64)
+            self._rc_ws = self._rc_buf[a256(R * n * 8) + a256(n * 8):]
         self.fallbacks = 0   # accelerated solves that fell back (p': plain BiCGSTAB; Gauss-Seidel momentum: refined BiCGSTAB)
         self.last_accel = None  # SolveInfo of the last accelerated p' solve
         ph = L.KcPhys()
@@ -130,6 +147,7 @@ class ChannelSolver:
         self.set_state(u, v, p)
 
     def set_state(self, u, v, p, u0=None, v0=None):
+        self._rstate.count = self._rstate.head = 0   # new fields: the ring of p' solutions starts empty
         def put(dst, src):
             src = torch.as_tensor(src, dtype=torch.float64)
             dst.copy_(src.to(self.device, non_blocking=True))
@@ -217,10 +235,15 @@ class ChannelSolver:
             return plain
         if self.mg is not None:
             self.mg.setup()
+            x0 = self.x0_p
+            if self.recycle and x0 is None:
+                x0 = self._recycle_guess()
             # the pressure correction is symmetric: multigrid-preconditioned CG
             info = pcg_refined(self.A_p, self.A_p32, self.b_p, self.pcor, self.mg, eps=self.cfg.eps,
-                               eps_inner=self.eps_inner_p, x0=self.x0_p, ws=self.ws_p, use_graph=self.use_graph,
+                               eps_inner=self.eps_inner_p, x0=x0, ws=self.ws_p, use_graph=self.use_graph,
                                check_every=self.check_every_p)
+            if self.recycle:
+                self._recycle_push()
             self.last_accel = info
             if info.ok:
                 return info
@@ -229,8 +252,29 @@ class ChannelSolver:
             plain = bicgstab(self.A_p, self.b_p, self.pcor, eps=self.cfg.eps, max_iter=self.A_p.n, ws=self.ws_p,
                              use_graph=self.use_graph, persistent=self.persistent)
             plain.iters += info.iters
+            if self.recycle:   # the ring keeps the solution the step goes on with
+                self._rstate.head = (self._rstate.head - 1) % self.recycle
+                self._rstate.count -= 1
+                self._recycle_push()
             return plain
         return self._solve(self.A_p, getattr(self, "A_p32", None), self.b_p, self.pcor, self.ws_p)
+
+    # ---- recycling: the ring of p' solutions in one buffer laid out as the native step's ------------
+    def _recycle_guess(self):
+        """x0 from the projection onto the stored solutions, newest first (None when the ring is empty)."""
+        m, R = self._rstate.count, self.recycle
+        if m == 0:
+            return None
+        Z = (C.c_void_p * m)(*[self._rc_ring[(self._rstate.head - 1 - i) % R].data_ptr() for i in range(m)])
+        L.check(L.load().kc_recycle_guess(C.byref(self.A_p.system), ptr(self.b_p), Z, m, ptr(self._rc_x0),
+                                          ptr(self._rc_ws), self._rc_ws.numel(), None, self._s()),
+                "kc_recycle_guess")
+        return self._rc_x0
+
+    def _recycle_push(self):
+        self._rc_ring[self._rstate.head].copy_(self.pcor.view(-1))
+        self._rstate.head = (self._rstate.head + 1) % self.recycle
+        self._rstate.count = min(self._rstate.count + 1, self.recycle)
 
     def _ws_flex(self):
         if self._flex_ws is None:
@@ -294,6 +338,10 @@ class ChannelSolver:
             setattr(c, "ws_" + k + "_bytes", buf.numel())
         if self.mg is not None:
             c.mg_ws, c.mg_ws_bytes, c.mg_opts = self.mg.ws.data_ptr(), self.mg.ws.numel(), self.mg.opts
+        if self.recycle:
+            c.recycle = self.recycle
+            c.ws_recycle, c.ws_recycle_bytes = self._rc_buf.data_ptr(), self._rc_buf.numel()
+            c.rstate = C.addressof(self._rstate)
         if self.learned is not None and self.mg is not None:
             NX, NY = self.b_p.shape
             self._net = self.learned.native(NX, NY)          # kept alive with the descriptor

@@ -150,6 +150,7 @@ size_t kc_struct_size(const char* name) {
     if (n == "kc_channel_stats") return sizeof(kc_channel_stats);
     if (n == "kc_unet_net") return sizeof(kc_unet_net);
     if (n == "kc_flex_info") return sizeof(kc_flex_info);
+    if (n == "kc_recycle_state") return sizeof(kc_recycle_state);
     return 0;
 }
 }  // extern "C"

@@ -96,9 +96,27 @@ int solve_sys(const kc_channel* c, const kc_system& A64, const kc_system& A32, c
     return rc;
 }
 
+// ring of the last p' solutions in ws_recycle: slot q at q * n doubles
+double* ring_slot(const kc_channel* c, int q) {
+    const long long n = (long long)(c->phys.nx + 2) * (c->phys.ny + 2);
+    return (double*)c->ws_recycle + (size_t)q * n;
+}
+// the stored solutions, newest first
+int ring_vectors(const kc_channel* c, const double** Z) {
+    const int m = c->rstate->count;
+    for (int i = 0; i < m; ++i) Z[i] = ring_slot(c, ((c->rstate->head - 1 - i) % c->recycle + c->recycle) % c->recycle);
+    return m;
+}
+
 }  // namespace
 
 extern "C" {
+
+size_t kc_channel_recycle_ws_bytes(long long n_p, int recycle) {
+    if (n_p < 1 || recycle < 1 || recycle > KC_RECYCLE_MAX) return 0;
+    return align256((size_t)recycle * n_p * sizeof(double)) + align256((size_t)n_p * sizeof(double)) +
+           kc_recycle_ws_bytes(n_p, recycle);
+}
 
 int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
     if (!c) return set_error("kc_channel_step: null channel"), KC_ERR_ARG;
@@ -123,6 +141,20 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
     kc_channel_stats S{};
     int rc = KC_OK;
     double mass = 0.0;
+    const bool recycling = mixed && !c->learned && c->recycle > 0;
+    double* rc_x0 = nullptr;
+    void* rc_ws = nullptr;
+    size_t rc_ws_bytes = 0;
+    if (recycling) {
+        if (c->recycle > KC_RECYCLE_MAX || !c->rstate || !c->ws_recycle ||
+            c->ws_recycle_bytes < kc_channel_recycle_ws_bytes(Ap.n, c->recycle) || ((uintptr_t)c->ws_recycle & 255))
+            return set_error("kc_channel_step: recycle = %d needs rstate and a 256-aligned ws_recycle of %zu bytes",
+                             c->recycle, kc_channel_recycle_ws_bytes(Ap.n, c->recycle)),
+                   KC_ERR_WORKSPACE;
+        rc_x0 = (double*)((char*)c->ws_recycle + align256((size_t)c->recycle * Ap.n * sizeof(double)));
+        rc_ws = (char*)rc_x0 + align256((size_t)Ap.n * sizeof(double));
+        rc_ws_bytes = kc_recycle_ws_bytes(Ap.n, c->recycle);
+    }
     for (int outer = 0; outer < c->max_outer; ++outer) {
         rc = kc_assemble_momentum(P, c->u, c->v, c->p, c->u0, c->v0, c->solid, c->coef_u, c->b_u, c->coef_v, c->b_v,
                                   c->coef_u32, c->b_u32, c->coef_v32, c->b_v32, s);
@@ -155,7 +187,18 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
                 S.learned += fi.learned_used;
                 S.learned_rejected += fi.learned_rejected;
             } else {
-                rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, nullptr, c->mg_ws, &c->mg_opts, c->ws_p,
+                const double* x0 = nullptr;
+                if (recycling) {
+                    // start from the projection onto the last solutions (kc_recycle_guess)
+                    const double* Z[KC_RECYCLE_MAX];
+                    const int m = ring_vectors(c, Z);
+                    if (m > 0) {
+                        rc = kc_recycle_guess(&Ap, c->b_p, Z, m, rc_x0, rc_ws, rc_ws_bytes, nullptr, s);
+                        if (rc < 0) return rc;
+                        x0 = rc_x0;
+                    }
+                }
+                rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, x0, c->mg_ws, &c->mg_opts, c->ws_p,
                                     c->ws_p_bytes, &o, c->eps_inner_p, 30, &ip, s);
                 if (rc < 0) return rc;
             }
@@ -171,6 +214,12 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
             const kc_solve_opts o = opts_of(c->eps, Ap.n, KC_REL_R0, 0, c->use_graph, c->persistent);
             rc = kc_bicgstab(&Ap, c->b_p, c->pcor, nullptr, c->ws_p, c->ws_p_bytes, &o, &ip, s);
             if (rc < 0) return rc;
+        }
+        if (recycling) {   // the solution joins the ring (the oldest leaves)
+            rc = kc_copy(ring_slot(c, c->rstate->head), c->pcor, (size_t)Ap.n * sizeof(double), s);
+            if (rc < 0) return rc;
+            c->rstate->head = (c->rstate->head + 1) % c->recycle;
+            c->rstate->count = std::min(c->rstate->count + 1, c->recycle);
         }
         rc = kc_correct(P, c->pcor, c->coef_u, c->coef_v, c->solid, c->u, c->v, c->p, c->pmax, c->rws, s);
         if (rc < 0) return rc;

@@ -78,6 +78,7 @@ def test_struct_layouts_match_the_header():
     for name, cls in (("kc_system", L.KcSystem), ("kc_solve_opts", L.KcSolveOpts), ("kc_solve_info", L.KcSolveInfo),
                       ("kc_mg_opts", L.KcMgOpts), ("kc_phys", L.KcPhys), ("kc_karman", L.KcKarman),
                       ("kc_channel", L.KcChannel), ("kc_channel_stats", L.KcChannelStats),
-                      ("kc_unet_net", L.KcUnetNet), ("kc_flex_info", L.KcFlexInfo)):
+                      ("kc_unet_net", L.KcUnetNet), ("kc_flex_info", L.KcFlexInfo),
+                      ("kc_recycle_state", L.KcRecycleState)):
         assert lib.kc_struct_size(name.encode()) == C.sizeof(cls), name
     assert lib.kc_struct_size(b"nope") == 0
