@@ -2193,6 +2193,83 @@ static int drive(const kc_solve_opts* o, const GraphKey& key, const SolverState*
     return KC_OK;
 }
 
+// ---- device-side loop over whole iterations (conditional WHILE graph node) --------------------
+// One captured iteration runs inside a WHILE node whose condition the last
+// kernel of the body sets from the solver state: the loop ends when the solve
+// is done (converged, capped, broken down) or after `cap` iterations, without
+// a host round trip or a launch past convergence.  The body-execution count
+// lives in st->ticket[3] (zero at the start of every solve), so the loop is
+// bounded by construction.
+__global__ void k_while_cond(SolverState* st, unsigned cap, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const unsigned c = ++st->ticket[3];
+    cudaGraphSetConditional(h, (__ldcg(&st->done) == 0 && c < cap) ? 1u : 0u);
+}
+
+constexpr unsigned kWhileCap = 1024;    // iterations one launch of the loop may run
+static std::atomic<int> g_while_ok{1};  // cleared when the driver refuses conditional nodes
+
+// Runs the solve's iterations as one graph launch; returns 1 when it ran (state in h), 0 when the
+// caller should use the chunked loop instead, < 0 on a CUDA error.
+template <class Launcher>
+static int drive_while(const GraphKey& key, SolverState* st, Launcher&& launch1, HostState* h, cudaStream_t s,
+                       int kernels_per_iter) {
+    if (!g_while_ok.load(std::memory_order_relaxed)) return 0;
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    GraphKey gk = key;
+    gk.chunk = -1;
+    gk.kind += 100;
+    std::shared_ptr<GraphExec> gx = graph_lookup(dev, gk);
+    if (!gx) {
+        cudaGraph_t g = nullptr;
+        KC_CUDA(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle hnd;
+        cudaGraphNodeParams cp{};
+        cudaGraphNode_t node;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&hnd, g, 1, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = hnd;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+        }
+        if (e != cudaSuccess) {   // no conditional nodes here: the chunked loop
+            cudaGetLastError();
+            cudaGraphDestroy(g);
+            g_while_ok.store(0);
+            return 0;
+        }
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        cudaStream_t cap_s;
+        KC_CUDA(cudaStreamCreateWithFlags(&cap_s, cudaStreamNonBlocking));
+        e = cudaStreamBeginCaptureToGraph(cap_s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            launch1(cap_s);
+            k_while_cond<<<1, 32, 0, cap_s>>>(st, kWhileCap, hnd);
+            cudaGraph_t out = nullptr;
+            e = cudaStreamEndCapture(cap_s, &out);
+        }
+        cudaStreamDestroy(cap_s);
+        cudaGraphExec_t ex = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            g_while_ok.store(0);
+            return 0;
+        }
+        gx = std::make_shared<GraphExec>(ex);
+        graph_insert(dev, gk, gx);
+    }
+    KC_CUDA(cudaGraphLaunch(gx->ex, s));
+    int rc = read_state(st, h, s);
+    if (rc) return rc;
+    count_launches(h->iter * (long long)(kernels_per_iter + 1));
+    return 1;
+}
+
 }  // namespace kc
 
 using namespace kc;
@@ -3325,11 +3402,20 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
         io.check_every = o->check_every > 0 ? o->check_every : 4;
         const int per_iter = cg ? pc_iter_kernels(A32, mg_ws, mg_opts) : 5 + 2 * mg_cycle_kernels(A32, mg_opts);
         HostState h{};
-        if (cg)
+        int ran = 0;
+        if (cg && io.use_graph) {
+            // the iterations loop on the device; the chunked loop below finishes a solve the
+            // device loop left unfinished (its iteration cap) or runs where it is unavailable
+            ran = drive_while(key, P.st,
+                              [&](cudaStream_t ss) { (void)launch_pc_iters(A32, mg_ws, mg_opts, W, P, 1, ss, nullptr); },
+                              &h, s, per_iter);
+            if (ran < 0) return ran;
+        }
+        if (cg && (!ran || !h.done))
             rc = drive(&io, key, P.st,
                        [&](int m, cudaStream_t ss) { (void)launch_pc_iters(A32, mg_ws, mg_opts, W, P, m, ss, nullptr); },
                        &h, s, per_iter);
-        else
+        else if (!cg)
             rc = drive(&io, key, P.st,
                        [&](int m, cudaStream_t ss) { (void)launch_pb_iters(A32, mg_ws, mg_opts, V, P, m, ss, nullptr); },
                        &h, s, per_iter);
