@@ -100,6 +100,9 @@ def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDA
     names = ("u", "v", "p", "u0", "v0", "u_mid", "v_mid", "pcor")
     saved = {k: getattr(solver, k).clone() for k in names}
     fallbacks, history = solver.fallbacks, list(solver.history)
+    # the trial solves start from zero and leave the ring of earlier p' solutions untouched
+    recycle = getattr(solver, "recycle", 0)
+    solver.recycle = 0
     try:
         solver.assemble_momentum()
         solver.solve_momentum()
@@ -143,5 +146,6 @@ def tune_pressure(solver, reps: int = 3, tails=TAIL_CANDIDATES, bigs=BIG_CANDIDA
         for k in names:
             getattr(solver, k).copy_(saved[k])
         solver.fallbacks, solver.history = fallbacks, history
+        solver.recycle = recycle
         torch.cuda.synchronize(solver.device)
     return result
