@@ -678,7 +678,7 @@ int kc_mass_residual(const kc_phys* P, const double* u, const double* v, const u
 }  // extern "C"
 
 // ---- lexicographic relaxation sweep (jacosimp.py) -------------------------------------------
-// jacosimp.py:226-247 relaxes u, v and p' in Python scope, in place, i outer
+// jacosimp.py:210-238 relaxes u, v and p' in Python scope, in place, i outer
 // and j inner: cell (i, j) reads its west (i-1, j) and south (i, j-1)
 // neighbours already updated in this sweep and its east and north neighbours
 // not yet updated.  Cells on one anti-diagonal i + j = d depend only on

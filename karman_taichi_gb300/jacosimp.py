@@ -2,9 +2,9 @@
 
 The lid-driven cavity SIMPLE variant that relaxes the equations instead of
 solving them: each step makes one in-place lexicographic sweep of the u and
-v momentum equations (under-relaxed by alpha_u, jacosimp.py:226-240) and one
-of the pressure correction (right-hand side mdiv, jacosimp.py:242-247), then
-corrects p (alpha_p) and u, v (alpha), jacosimp.py:212-224.  The sweeps run
+v momentum equations (under-relaxed by alpha_u, jacosimp.py:210-228) and one
+of the pressure correction (right-hand side mdiv, jacosimp.py:230-238), then
+corrects p (alpha_p) and u, v (alpha), jacosimp.py:194-208.  The sweeps run
 on the GPU as anti-diagonal wavefronts (``kc_lex_sweep``), which give the
 serial sweep's values exactly; assembly, boundary folding, the mass source
 and the corrections are the kernels of ``simple.SIMPLESolver`` (jacosimp.py's
@@ -33,7 +33,7 @@ class SIMPLESolver(simple.SIMPLESolver):
                                       float(omega), int(relax), self._s()), "kc_lex_sweep")
 
     def solve_momentum_eqn(self):
-        """jacosimp.py:226-240: coefficients, boundary folding, then one under-relaxed
+        """jacosimp.py:210-228: coefficients, boundary folding, then one under-relaxed
         lexicographic sweep of u over i in [2, nx], j in [1, ny] and of v over i in [1, nx],
         j in [2, ny]."""
         nx, ny = self.nx, self.ny
@@ -44,17 +44,17 @@ class SIMPLESolver(simple.SIMPLESolver):
         self._sweep(self.coef_v, self.b_v, self.v, self.v_mid, (1, nx + 1, 2, ny + 1), self.alpha_u, True)
 
     def solve_pcorrection_eqn(self):
-        """jacosimp.py:242-247: p' coefficients and mdiv, then one lexicographic sweep of
+        """jacosimp.py:230-238: p' coefficients and mdiv, then one lexicographic sweep of
         p' (right-hand side mdiv) over i in [1, nx], j in [1, ny]."""
         self.compute_coef_p()
         self._sweep(self.coef_p, self.mdiv, self.pcor, None, (1, self.nx + 1, 1, self.ny + 1), 1.0, False)
 
     def update_pressure(self):
-        """jacosimp.py:212-216: p += alpha_p p'."""
+        """jacosimp.py:194-198: p += alpha_p p'."""
         self._correct(0.0, self.alpha_p)
 
     def update_velocity(self):
-        """jacosimp.py:218-224: u += alpha (p'_W - p') dy / aP, v likewise."""
+        """jacosimp.py:200-208: u += alpha (p'_W - p') dy / aP, v likewise."""
         self._correct(self.alpha, 0.0)
 
     def solve(self, n_steps=60000, callback=None):

@@ -1189,7 +1189,7 @@ def pcorr_random_system(N=1024, seed=0, blocked=0.05):
 
 def lex_sweep(coef, b, x, box, omega=1.0, relax=True, x_mid=None):
     """One in-place lexicographic relaxation sweep over the box (i0, i1, j0, j1),
-    i outer and j inner, as jacosimp.py:226-247 runs it in Python scope: each
+    i outer and j inner, as jacosimp.py:210-238 runs it in Python scope: each
     cell reads its west and south neighbours already updated.  The cells of an
     anti-diagonal i + j = d depend only on diagonal d - 1, so the sweep is
     evaluated diagonal by diagonal with NumPy, each cell in the reference's
@@ -1222,21 +1222,21 @@ class JacoSimpleOracle(SimpleOracle):
         self.alpha_u = 0.01
         self.alpha = 0.1
 
-    def jaco_momentum(self):  # jacosimp.py:226-240
+    def jaco_momentum(self):  # jacosimp.py:210-228
         nx, ny = self.nx, self.ny
         self.compute_coef_u(); self.compute_coef_v(); self.set_bc()
         lex_sweep(self.coef_u, self.b_u, self.u, (2, nx + 1, 1, ny + 1), self.alpha_u, True, self.u_mid)
         lex_sweep(self.coef_v, self.b_v, self.v, (1, nx + 1, 2, ny + 1), self.alpha_u, True, self.v_mid)
 
-    def jaco_pcorrection(self):  # jacosimp.py:242-247
+    def jaco_pcorrection(self):  # jacosimp.py:230-238
         self.compute_coef_p()
         lex_sweep(self.coef_p, self.mdiv, self.pcor, (1, self.nx + 1, 1, self.ny + 1), 1.0, False)
 
-    def update_pressure(self):  # jacosimp.py:212-216
+    def update_pressure(self):  # jacosimp.py:194-198
         nx, ny = self.nx, self.ny
         self.p[1:nx + 1, 1:ny + 1] += self.alpha_p * self.pcor[1:nx + 1, 1:ny + 1]
 
-    def jaco_update_velocity(self):  # jacosimp.py:218-224
+    def jaco_update_velocity(self):  # jacosimp.py:200-208
         nx, ny, dx, dy = self.nx, self.ny, self.dx, self.dy
         pc = self.pcor
         I, J = slice(2, nx + 1), slice(1, ny + 1)
