@@ -276,6 +276,7 @@ def roofline_p_solve(solver, mode, peak):
     bytes/cell/iteration over its 2L launches per iteration (L multigrid
     levels); each FP64 refinement residual adds (5 coef + x + b) x 8 B/cell."""
     import torch
+    solver.outer_iteration()   # one untimed outer iteration through the same Python-driven stages first
     solver.assemble_momentum()
     solver.solve_momentum()
     solver.relax()

@@ -108,10 +108,12 @@ class ChannelSolver:
         self.x0_p = None     # optional initial guess for p'
         self.learned_stats = [0, 0]   # p' solves that applied / rejected the network's prediction
         self._flex_ws = None
+        self._side = None   # the stream the p' hierarchy is built on while the recycled guess forms
         self.recycle = int(recycle) if (precision == "mixed" and learned is None and self.mg is not None) else 0
         self._rstate = L.KcRecycleState()
         self._rc_buf = None
         if self.recycle:
+            self._side = torch.cuda.Stream(device=self.device)
             n = (nx + 2) * (ny + 2)
             nbytes = L.load().kc_channel_recycle_ws_bytes(n, self.recycle)
             self._rc_raw = torch.zeros(nbytes + 256, dtype=torch.uint8, device=self.device)
@@ -234,10 +236,18 @@ class ChannelSolver:
             plain.iters += info.iters
             return plain
         if self.mg is not None:
-            self.mg.setup()
             x0 = self.x0_p
-            if self.recycle and x0 is None:
+            if self.recycle and x0 is None and self._rstate.count > 0:
+                # the hierarchy on a side stream while the guess forms on this one (as the native step)
+                main = torch.cuda.current_stream(self.device)
+                side = self._side
+                side.wait_stream(main)
+                with torch.cuda.stream(side):
+                    self.mg.setup()
                 x0 = self._recycle_guess()
+                main.wait_stream(side)
+            else:
+                self.mg.setup()
             # the pressure correction is symmetric: multigrid-preconditioned CG
             info = pcg_refined(self.A_p, self.A_p32, self.b_p, self.pcor, self.mg, eps=self.cfg.eps,
                                eps_inner=self.eps_inner_p, x0=x0, ws=self.ws_p, use_graph=self.use_graph,

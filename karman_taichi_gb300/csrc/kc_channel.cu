@@ -108,6 +108,40 @@ int ring_vectors(const kc_channel* c, const double** Z) {
     return m;
 }
 
+// A second stream per host thread and device: the multigrid setup of a p'
+// solve (launch-latency-bound: one small launch per level and a one-block
+// coarsest inverse) runs on it while the recycled guess (FP64-pipe-bound)
+// runs on the caller's stream; the caller's stream then waits for it.
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~SideStream() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (s) cudaStreamDestroy(s);
+    }
+};
+SideStream* side_stream() {
+    static thread_local SideStream side[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        set_error("side stream: no current device below 64");
+        return nullptr;
+    }
+    SideStream& d = side[dev];
+    if (!d.s) {
+        cudaError_t e = cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&d.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cuda_status(e, "side stream");
+            return nullptr;
+        }
+    }
+    return &d;
+}
+
 }  // namespace
 
 extern "C" {
@@ -174,8 +208,25 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
                                c->b_p32, nullptr, c->mass, c->rws, s);
         if (rc < 0) return rc;
         if (mixed) {
-            rc = kc_mg_setup(&Ap32, c->mg_ws, c->mg_ws_bytes, &c->mg_opts, s);
-            if (rc < 0) return rc;
+            const double* Z[KC_RECYCLE_MAX];
+            const int m = recycling ? ring_vectors(c, Z) : 0;
+            if (m > 0) {
+                // the hierarchy on the side stream while the guess forms on this one: the
+                // projection onto the last solutions (kc_recycle_guess)
+                SideStream* sd = side_stream();
+                if (!sd) return KC_ERR_CUDA;
+                KC_CUDA(cudaEventRecord(sd->fork, s));
+                KC_CUDA(cudaStreamWaitEvent(sd->s, sd->fork, 0));
+                rc = kc_mg_setup(&Ap32, c->mg_ws, c->mg_ws_bytes, &c->mg_opts, sd->s);
+                if (rc < 0) return rc;
+                KC_CUDA(cudaEventRecord(sd->join, sd->s));
+                rc = kc_recycle_guess(&Ap, c->b_p, Z, m, rc_x0, rc_ws, rc_ws_bytes, nullptr, s);
+                if (rc < 0) return rc;
+                KC_CUDA(cudaStreamWaitEvent(s, sd->join, 0));
+            } else {
+                rc = kc_mg_setup(&Ap32, c->mg_ws, c->mg_ws_bytes, &c->mg_opts, s);
+                if (rc < 0) return rc;
+            }
             const kc_solve_opts o =
                 opts_of(c->eps, 50 * Ap.n, KC_REL_B, c->check_every_p > 0 ? c->check_every_p : 4, c->use_graph, 0);
             if (c->learned) {
@@ -187,17 +238,7 @@ int kc_channel_step(const kc_channel* c, kc_channel_stats* st, void* stream) {
                 S.learned += fi.learned_used;
                 S.learned_rejected += fi.learned_rejected;
             } else {
-                const double* x0 = nullptr;
-                if (recycling) {
-                    // start from the projection onto the last solutions (kc_recycle_guess)
-                    const double* Z[KC_RECYCLE_MAX];
-                    const int m = ring_vectors(c, Z);
-                    if (m > 0) {
-                        rc = kc_recycle_guess(&Ap, c->b_p, Z, m, rc_x0, rc_ws, rc_ws_bytes, nullptr, s);
-                        if (rc < 0) return rc;
-                        x0 = rc_x0;
-                    }
-                }
+                const double* x0 = m > 0 ? rc_x0 : nullptr;
                 rc = kc_pcg_refined(&Ap, &Ap32, c->b_p, c->pcor, x0, c->mg_ws, &c->mg_opts, c->ws_p,
                                     c->ws_p_bytes, &o, c->eps_inner_p, 30, &ip, s);
                 if (rc < 0) return rc;
