@@ -72,6 +72,11 @@ def parse():
     ap.add_argument("--batch-workers", type=int, default=16)
     ap.add_argument("--copies", type=int, default=0, metavar="N",
                     help="step N seeded copies of --config concurrently (the batch executor) and one after another")
+    ap.add_argument("--long-run", type=int, default=0, metavar="N",
+                    help="the long run of --config (default channel_4096x1024): its seeded copies advanced "
+                         "together for N time steps with wake probes (shedding period and its drift), then the "
+                         "plain FP64 method's first --fp64-steps steps against copy 0, and exit")
+    ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
                     help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
                          "(the command the committed ncu summaries were captured on)")
@@ -718,6 +723,123 @@ def run_batch(args, cfgs=None, workload=None):
     print(json.dumps(out), flush=True)
 
 
+def shedding(sig, dt, min_amp=1e-3, frac=0.6):
+    """Shedding period of one wake probe (v behind a cylinder, one sample per
+    time step).  Over the last ``frac`` of the run the signal less a quadratic
+    fit is taken; where its half peak-to-peak amplitude exceeds ``min_amp`` (in
+    units of the inlet velocity) the period is twice the mean spacing of its
+    zero crossings (interpolated), and with five crossings or more the drift is
+    the relative change of that period between the first and the second half
+    of the crossings."""
+    import numpy as np
+    x = np.asarray(sig, dtype=np.float64)
+    n = len(x)
+    lo = int(n * (1 - frac))
+    t = np.arange(lo, n, dtype=np.float64)
+    d = x[lo:] - np.polyval(np.polyfit(t, x[lo:], 2), t)
+    amp = float(np.ptp(d) / 2)
+    out = {"window": [lo, n], "amplitude": round(amp, 6)}
+    if amp < min_amp:
+        out.update(period_steps=None, note="no oscillation above the threshold")
+        return out
+    k = np.nonzero(np.signbit(d[1:]) != np.signbit(d[:-1]))[0]
+    tz = lo + k + d[k] / (d[k] - d[k + 1])
+    out["crossings"] = int(len(tz))
+    if len(tz) < 2:
+        out.update(period_steps=None, note="fewer than two crossings: the period is longer than the window")
+        return out
+    half = np.diff(tz)
+    per = 2.0 * float(np.mean(half))
+    out.update(period_steps=round(per, 2), period_time=per * dt)
+    if len(tz) >= 5:
+        m = len(half) // 2
+        p_a, p_b = 2.0 * float(np.mean(half[:m])), 2.0 * float(np.mean(half[m:]))
+        out.update(period_first_half=round(p_a, 2), period_second_half=round(p_b, 2), drift=round((p_b - p_a) / p_a, 4))
+    else:
+        out.update(drift=None, note="fewer than five crossings: drift not measurable")
+    return out
+
+
+def run_long(args):
+    """The long run: the preset's seeded copies (inlet noise seed k for copy k)
+    advanced together by the batch executor, mixed path, autotuned, for N time
+    steps; after every step v is sampled four diameters behind each cylinder on
+    its axis (device-side gather, read once at the end).  Reports instance time
+    steps/s, the mass residual reached, the shedding period per copy and probe
+    and its drift, the spread of the period over the copies, and the field error
+    of copy 0 against the plain FP64 method after its first --fp64-steps steps."""
+    import numpy as np
+    import torch
+    from karman_taichi_gb300.batch import BatchedChannels
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import PRESETS
+    from karman_taichi_gb300.autotune import CYCLE_CANDIDATES
+    name = args.config if args.config != "channel_2048x512" else "channel_4096x1024"
+    base = PRESETS[name]
+    copies = max(1, base.copies)
+    cfgs = [base.with_(seed=k) for k in range(copies)]
+    N = args.long_run
+    dev = torch.device("cuda", 0)
+    b = BatchedChannels(cfgs, precision="mixed", workers=copies)
+    chosen = b.autotune(cycles=CYCLE_CANDIDATES)
+    for s in b.solvers:
+        s.reset()
+    probes = [(ci + 4 * D, cj) for (_, ci, cj, D) in base.obstacles]
+    idx = torch.tensor([i * (base.ny + 3) + j for (i, j) in probes], dtype=torch.long, device=dev)
+    samples = torch.zeros(N, copies, len(probes), dtype=torch.float64, device=dev)
+    snap = None
+    mass_max, outer, status_bad = 0.0, [], 0
+    t_total = 0.0
+    clocks = Clocks(0)
+    clocks.start()
+    for t in range(N):
+        t_total += b.step_native(1)
+        for k, s in enumerate(b.solvers):
+            samples[t, k] = s.v.reshape(-1).index_select(0, idx)
+            rec = b.records[k][-1][0]
+            mass_max = max(mass_max, rec["mass"])
+            outer.append(rec["outer"])
+            status_bad += rec["status"] != 0
+        if t + 1 == args.fp64_steps:
+            snap = {f: getattr(b.solvers[0], f).clone() for f in ("u", "v", "p")}
+        for rec in b.records:   # keep only the last record per instance
+            del rec[:-1]
+    ck = clocks.stop()
+    sig = samples.cpu().numpy()
+    dt = base.dt
+    shed = [[shedding(sig[:, k, q], dt) for q in range(len(probes))] for k in range(copies)]
+    pers = [x["period_steps"] for row in shed for x in row if x.get("period_steps")]
+    out = {"metric": "instance time steps/s, long run", "unit": "instance time steps/s",
+           "config": {"workload": f"{name} x {copies} seeded copies", "nx": base.nx, "ny": base.ny,
+                      "Re": base.Re, "obstacles": [list(o) for o in base.obstacles], "dt": dt, "steps": N,
+                      "mode": "mixed", "autotune": {k: {f: c[f] for f in ("nu_coarse", "tail", "big_cells",
+                                                                           "check_every_p")}
+                                                    for k, c in chosen.items()}},
+           "value": round(copies * N / t_total, 3), "seconds": round(t_total, 1),
+           "cell_updates_per_s": round(copies * base.cells * N / t_total, 1),
+           "outer_per_step": round(float(np.mean(outer)), 2), "mass_residual_max": mass_max,
+           "steps_not_converged": int(status_bad), "clocks": ck,
+           "probes": {"points": [list(p) for p in probes], "field": "v", "per_copy": shed},
+           "period_spread_over_copies": (round((max(pers) - min(pers)) / float(np.mean(pers)), 4)
+                                         if len(pers) >= 2 else None),
+           "probe_history_copy0_every_10_steps": np.round(sig[::10, 0, :], 7).tolist()}
+    b.close()
+    del b
+    torch.cuda.empty_cache()
+    if args.fp64_steps > 0 and snap is not None:
+        ref = ChannelSolver(cfgs[0], device=dev, precision="fp64")
+        ref.reset()
+        t0 = time.perf_counter()
+        for _ in range(args.fp64_steps):
+            ref.step()
+        torch.cuda.synchronize()
+        err = {f: float((snap[f] - getattr(ref, f)).abs().max() / getattr(ref, f).abs().max())
+               for f in ("u", "v", "p")}
+        out["field_error_vs_fp64"] = dict(err, after_steps=args.fp64_steps, fp64_seconds=round(time.perf_counter() - t0, 1),
+                                          definition="max |x - x_fp64| / max |x_fp64| over the padded field, copy 0")
+    print(json.dumps(out), flush=True)
+
+
 def run_profile_outer(args):
     import torch
     from karman_taichi_gb300.config import PRESETS
@@ -735,6 +857,8 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.profile_outer > 0:
         run_profile_outer(a)
+    elif a.long_run > 0:
+        run_long(a)
     elif a.spmv_sweep:
         run_spmv_sweep(a)
     elif a.pcorr1024:
