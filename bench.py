@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--batch-instances", type=int, default=0, metavar="N",
                     help="time the batched configuration (N independent channel instances, stream-parallel) and exit")
     ap.add_argument("--batch-workers", type=int, default=16)
+    ap.add_argument("--batch-executors", default="fused,native",
+                    help="comma-separated executors of the batched configuration, timed in turn: fused (one "
+                         "persistent launch for all instances and steps), native (one stream per instance, native "
+                         "threads), sequential (one stream); the first gives the line's value")
     ap.add_argument("--copies", type=int, default=0, metavar="N",
                     help="step N seeded copies of --config concurrently (the batch executor) and one after another")
     ap.add_argument("--long-run", type=int, default=0, metavar="N",
@@ -683,11 +687,15 @@ def run_pcorr1024(args):
 
 def run_batch(args, cfgs=None, workload=None):
     """Instance time steps/s of the batched configuration: N instances (sizes
-    128x32 .. 640x128, D 4-16, Re 60-200) stepped concurrently, one CUDA stream
-    per instance, against the same instances stepped one after another on one
-    stream.  W warm-up steps, then K timed steps of every instance.  With
-    ``cfgs`` (``--copies``): those instances instead, e.g. seeded copies of one
-    preset."""
+    128x32 .. 640x128, D 4-16, Re 60-200).  Executors (--batch-executors):
+    ``fused``, every instance and every timed step in ONE persistent launch
+    (kc_channel_batch_fused, block k = instance k); ``native``, one CUDA stream
+    per instance driven by native threads (kc_channel_batch_step);
+    ``sequential``, the instances one after another on one stream.  Each
+    executor starts from the seeded initial state: W warm-up steps, then K
+    timed steps of every instance.  With ``cfgs`` (``--copies``): those
+    instances instead, e.g. seeded copies of one preset (native and
+    sequential only)."""
     import numpy as np
     import torch
     from karman_taichi_gb300.batch import BatchedChannels, batch_configs
@@ -698,28 +706,56 @@ def run_batch(args, cfgs=None, workload=None):
     out = {"metric": "instance time steps/s, batched channel instances", "unit": "instance time steps/s",
            "config": {"workload": workload}, "instances": len(cfgs), "cells": int(sum(c.cells for c in cfgs)),
            "mode": mode, "steps": args.steps, "warmup": args.warmup}
-    for key, workers, native in (("native_concurrent", args.batch_workers, True), ("sequential", 1, True)):
+    execs = [e.strip() for e in args.batch_executors.split(",") if e.strip()]
+    if args.copies:
+        execs = [e for e in execs if e != "fused"] or ["native"]
+    plan = {"fused": ("fused", 1), "native": ("native_concurrent", args.batch_workers),
+            "sequential": ("sequential", 1)}
+    first = None
+    for e in execs:
+        key, workers = plan[e]
         b = BatchedChannels(cfgs, precision=mode, workers=workers)
         if mode == "mixed" and not args.no_autotune:   # per grid size, before anything is timed
             from karman_taichi_gb300.autotune import CYCLE_CANDIDATES
             chosen = b.autotune(cycles=CYCLE_CANDIDATES)
             out.setdefault("autotune", {k: {f: c[f] for f in ("nu_coarse", "tail", "big_cells", "check_every_p")}
                                         for k, c in chosen.items()})
-        run = b.step_native if native else b.step
-        run(args.warmup)
-        t = run(args.steps)
-        # the native driver records one entry per call (its last step's statistics): the timed call's
-        outer = np.mean([sum(s.get("outer", 1) for s in rec[-1]) for rec in b.records])
-        out[key] = {"workers": workers, "driver": "native threads" if native else "python threads",
-                    "seconds": round(t, 3),
-                    "value": round(len(cfgs) * args.steps / t, 2),
-                    "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
-                    "outer_per_step": round(float(outer), 2)}
+        if e == "fused":
+            from karman_taichi_gb300 import _lib as L
+            lib = L.load()
+            run = b.step_fused
+            run(args.warmup)
+            l0 = lib.kc_launch_count()
+            t = run(args.steps)
+            launches = lib.kc_launch_count() - l0
+            tot = b.fused_totals
+            outer = float(np.mean([x["outer"] for x in tot])) / max(1, args.steps)
+            out[key] = {"driver": "one persistent launch (kc_channel_batch_fused), block k = instance k",
+                        "seconds": round(t, 3), "value": round(len(cfgs) * args.steps / t, 2),
+                        "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
+                        "outer_per_step": round(outer, 2), "gpu_launches": int(launches),
+                        "it_p_per_step": round(float(np.mean([x["it_p"] for x in tot])) / max(1, args.steps), 1),
+                        "mass_residual_max": max(x["mass_max"] for x in tot),
+                        "instances_with_unconverged_solves": int(sum(x["unconverged_solves"] > 0 for x in tot)),
+                        "instances_not_finite": int(sum(x["status"] == 4 for x in tot))}
+        else:
+            run = b.step_native
+            run(args.warmup)
+            t = run(args.steps)
+            # the native driver records one entry per call (its last step's statistics): the timed call's
+            outer = np.mean([sum(s.get("outer", 1) for s in rec[-1]) for rec in b.records])
+            out[key] = {"workers": workers, "driver": "native threads", "seconds": round(t, 3),
+                        "value": round(len(cfgs) * args.steps / t, 2),
+                        "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
+                        "outer_per_step_last": round(float(outer), 2)}
+        first = first or key
         b.close()
         del b
         torch.cuda.empty_cache()
-    out["value"] = out["native_concurrent"]["value"]
-    out["speedup_concurrent_vs_sequential"] = round(out["native_concurrent"]["value"] / out["sequential"]["value"], 2)
+    out["value"] = out[first]["value"]
+    keys = [plan[e][0] for e in execs]
+    for a in keys[1:]:
+        out[f"speedup_{first}_vs_{a}"] = round(out[first]["value"] / out[a]["value"], 2)
     print(json.dumps(out), flush=True)
 
 

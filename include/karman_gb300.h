@@ -608,6 +608,24 @@ int kc_channel_step(const kc_channel* ch, kc_channel_stats* stats, void* stream)
 int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* streams, int workers,
                           int steps, kc_channel_stats* stats);
 
+/* n instances advanced by `steps` time steps in ONE kernel launch, block k
+ * running instance k's whole time steps (the mixed path: momentum by FP32
+ * red-black Gauss-Seidel in FP64 refinement, p' by multigrid CG in FP64
+ * refinement from p' = 0, the instance's mg_opts omega / alpha / nu_coarse;
+ * outer loop to mass_tol or max_outer, then u0 = u, v0 = v).  Every instance
+ * must be KC_F32 in KC_MODE_CHANNEL; of its buffers only the fields, the
+ * FP64 systems and their FP32 copies are used (ws_* and mg_ws are not).  An
+ * instance computes bit for bit what it computes in a batch of one.  ws:
+ * kc_channel_batch_fused_ws_bytes(chs, n), 256-byte aligned.  last / total
+ * (host arrays of n, nullable): each instance's last step, and the sums over
+ * the steps (mass: the largest last-outer mass residual).  In the statistics
+ * `fallbacks` counts solves that ended without reaching eps (the launch has
+ * no fallback solver).  Blocks until the launch has finished.  The
+ * reference's drivers have no batched counterpart. */
+size_t kc_channel_batch_fused_ws_bytes(const kc_channel* const* chs, int n);
+int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void* ws, size_t ws_bytes,
+                           kc_channel_stats* last, kc_channel_stats* total, void* stream);
+
 /* ---- output post-processing ----------------------------------------------- */
 /* post_process_field (karman_taichi.py:545-583) on the padded staggered fields
  * (u [nx+3][ny+2], v [nx+2][ny+3], p and pcor [nx+2][ny+2]):

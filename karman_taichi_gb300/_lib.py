@@ -204,6 +204,9 @@ SIGNATURES = {
     "kc_channel_step": (I_, [C.POINTER(KcChannel), C.POINTER(KcChannelStats), P_]),
     "kc_channel_batch_step": (I_, [C.POINTER(C.POINTER(KcChannel)), I_, C.POINTER(P_), I_, I_,
                                    C.POINTER(KcChannelStats)]),
+    "kc_channel_batch_fused_ws_bytes": (S_, [C.POINTER(C.POINTER(KcChannel)), I_]),
+    "kc_channel_batch_fused": (I_, [C.POINTER(C.POINTER(KcChannel)), I_, I_, P_, S_, C.POINTER(KcChannelStats),
+                                    C.POINTER(KcChannelStats), P_]),
     "kc_post_process_ws_bytes": (S_, []),
     "kc_post_process": (I_, [I_, I_, D_, D_, P_, P_, P_, P_, P_, P_, P_, P_, P_, P_, S_, P_]),
     "kc_unet_features_ws_bytes": (S_, [I_]),

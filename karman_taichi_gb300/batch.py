@@ -70,6 +70,8 @@ class BatchedChannels:
         self.pool = ThreadPoolExecutor(max_workers=self.workers)
         self.records = [[] for _ in self.configs]
         self._err = None
+        self._fused_ws = None
+        self.fused_totals = None
 
     def _run_group(self, w, n_steps):
         torch.cuda.set_device(self.device)
@@ -116,6 +118,42 @@ class BatchedChannels:
             st = stats[k]
             self.records[k].append([dict(mass=st.mass, it_u=st.it_u, it_v=st.it_v, it_p=st.it_p, outer=st.outer,
                                          status=st.status)])
+        return t
+
+    def step_fused(self, n_steps=1):
+        """n_steps time steps of every instance in ONE kernel launch
+        (kc_channel_batch_fused: block k runs instance k's time steps, every
+        stage of the mixed path inside the kernel).  Statistics go to
+        ``records`` as for step_native (the last step) and ``fused_totals``
+        (sums over the call's steps); returns the wall time in seconds."""
+        import ctypes as C
+        from . import _lib as L
+        n = len(self.solvers)
+        lib = L.load()
+        chans = [s.native_struct() for s in self.solvers]
+        arr = (C.POINTER(L.KcChannel) * n)(*[C.pointer(c) for c in chans])
+        need = lib.kc_channel_batch_fused_ws_bytes(arr, n)
+        if need == 0:
+            raise RuntimeError("kc_channel_batch_fused_ws_bytes: " + lib.kc_last_error().decode())
+        if self._fused_ws is None or self._fused_ws.numel() < need + 256:
+            self._fused_ws = torch.empty(need + 256, dtype=torch.uint8, device=self.device)
+        off = (-self._fused_ws.data_ptr()) % 256
+        last = (L.KcChannelStats * n)()
+        total = (L.KcChannelStats * n)()
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        L.check(lib.kc_channel_batch_fused(arr, n, n_steps, self._fused_ws.data_ptr() + off, need, last, total,
+                                           stream), "kc_channel_batch_fused")
+        torch.cuda.synchronize(self.device)
+        t = time.perf_counter() - t0
+        self.fused_totals = []
+        for k in range(n):
+            st, tt = last[k], total[k]
+            self.records[k].append([dict(mass=st.mass, it_u=st.it_u, it_v=st.it_v, it_p=st.it_p, outer=st.outer,
+                                         status=st.status)])
+            self.fused_totals.append(dict(outer=tt.outer, it_u=tt.it_u, it_v=tt.it_v, it_p=tt.it_p,
+                                          mass_max=tt.mass, status=tt.status, unconverged_solves=tt.fallbacks))
         return t
 
     def step(self, n_steps=1):

@@ -34,6 +34,7 @@ SOURCES = {
     "kc_smoothers.cu": [],
     "kc_flex.cu": [],
     "kc_recycle.cu": [],
+    "kc_batch.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

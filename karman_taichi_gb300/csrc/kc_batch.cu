@@ -1,0 +1,1036 @@
+// The batched channel executor as one persistent launch.
+//
+// kc_channel_batch_fused advances n independent channel instances (uneven
+// grid sizes) by `steps` time steps in ONE kernel launch: block b owns
+// instance b and runs its whole SIMPLE time steps -- the outer loop of
+// karman_taichi.py:633-659 / simple.py:270-281 with the stages of the mixed
+// path -- with block barriers between the phases and nothing on the host
+// between them.  Instances never wait on each other, so the launch needs no
+// grid-wide synchronisation and no instance can hold another up.  Per outer
+// iteration, per instance:
+//
+//   assemble_momentum   u_row / v_row (kc_simple.cuh) on every face: the
+//                       FP64 systems and their FP32 copies, bit for bit the
+//                       rows kc_assemble_momentum writes
+//   u*, v*              FP32 red-black Gauss-Seidel (12 sweeps per pass) in
+//                       FP64 refinement from the previous outer iteration's
+//                       u*, v*, to ||b - A x|| / ||b|| < eps, at most 200
+//                       sweeps (kc_rbgs_refined's method)
+//   relax, outlet       u = a u* + (1 - a) u, v alike; the outlet column's
+//                       zero gradient and mass-flow rescale
+//   assemble_pcorr      the p' rows (FP64, the FP32 Laplacian-form copy) and
+//                       the mass residual max |mdiv| over fluid cells
+//   p'                  multigrid-preconditioned FP32 CG in FP64 refinement
+//                       from p' = 0 to rel. tol eps (inner tol eps_inner_p);
+//                       aggregation multigrid as kc_mg.cu (2x2 aggregates,
+//                       Galerkin coarse rows in Laplacian form, isolated
+//                       rows, red-black smoothing with the instance's
+//                       mg_opts omega / alpha / nu_coarse), the coarsest
+//                       level (<= 64 cells) solved by its dense inverse
+//   correct             u, v, p corrections (kc_correct's arithmetic)
+//
+// and the outer loop stops when the mass residual is <= mass_tol or after
+// max_outer iterations; then u0 = u, v0 = v.  FP64 inner products and
+// residual norms are block reductions in a fixed order, so every instance
+// computes bit for bit what it computes alone in a batch of one, whatever
+// else shares the launch.  The block reductions differ in order from the
+// per-instance multi-block kernels of kc_channel_step, so the two agree to
+// rounding, not bitwise.
+//
+// Why one block per instance: an instance of the batched configuration has
+// 4k-83k cells; as separate launches every stage is a few microseconds of
+// launch latency for a fraction of a microsecond of work, and the GPU idles
+// between them.  Here the phases of one instance are separated by a block
+// barrier (~0.1 us) and the 256 instances of the batch stream through HBM
+// together, one block per SM slot.
+//
+// Loads use the coherent path throughout (no __ldg): every array is written
+// by an earlier phase of the same launch.
+#include "kc_simple.cuh"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace kc {
+namespace {
+
+constexpr int kBT = 512;                 // threads per instance block
+constexpr int kBWarps = kBT / 32;
+constexpr int kBLevels = 12;             // multigrid levels at most
+constexpr int kBCoarse = 64;             // cells of the coarsest level at most (dense inverse in shared memory)
+constexpr int kBGsSweeps = 12;           // Gauss-Seidel sweeps per momentum refinement pass
+constexpr long long kBMomentumSweeps = 200;
+constexpr int kBMaxRefine = 30;
+constexpr int kBMaxCg = 1000;            // CG iterations per refinement pass at most
+constexpr int kBCoarseFallbackSweeps = 64;
+
+// exact e / d for 0 <= e < 2^32 / d by a multiply-high (m = 0 stands for d = 1)
+struct Div {
+    unsigned m;
+    __device__ __forceinline__ int q(int e) const { return m ? (int)__umulhi((unsigned)e, m) : e; }
+};
+inline Div div_of(int d) { return Div{d == 1 ? 0u : (unsigned)((1ull << 32) / (unsigned)d + 1)}; }
+
+struct BLvl {
+    float* c;             // 5 planes [NX][NY], Laplacian form (level 0: the FP32 p' copy)
+    float* b;             // right-hand side (level 0: CG's residual)
+    float* x;             // iterate (level 0: CG's z)
+    float* w;             // smoother weights
+    unsigned char* iso;   // rows without links
+    int NX, NY;
+    Div dy;
+    float omega, alpha;   // smoother weight, weight of the coarse correction prolonged into this level
+    int nu;               // red-black sweeps before and after the coarse correction
+};
+
+struct BInst {
+    kc_phys P;
+    SimpleK K;
+    int max_outer;
+    double mass_tol, eps, eps_inner_p;
+    double *u, *v, *p, *u0, *v0, *pc, *um, *vm;
+    const unsigned char* solid;
+    double *cu, *bu, *cv, *bv, *cp, *bp;
+    float *cu32, *bu32, *cv32, *bv32, *cp32, *bp32;
+    float *gw, *r32, *d32;                 // momentum: Gauss-Seidel weights, FP32 residual, correction
+    float *cr, *cz, *cpv, *cq, *cd;        // p' CG: r, z, p, q and the correction
+    BLvl lv[kBLevels];
+    int levels;
+    Div du, dv, dp;                        // row lengths of the u, v and p grids
+    kc_channel_stats* last;                // per instance: the last step's statistics
+    kc_channel_stats* total;               // ... and the sums over the launch's steps
+};
+
+// ---- block reductions with the result in every thread -------------------------
+template <int NV>
+__device__ __forceinline__ void bsum(double (&v)[NV]) {
+    __shared__ double sh[NV][kBWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        const double s = warp_sum(v[q]);
+        if (lane == 0) sh[q][w] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < kBWarps; ++i) s += sh[q][i];
+        v[q] = s;
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ double bmax(double v) {
+    __shared__ double sh[kBWarps];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    v = warp_max(v);
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double m = 0.0;
+#pragma unroll
+    for (int i = 0; i < kBWarps; ++i) m = fmax(m, sh[i]);
+    __syncthreads();
+    return m;
+}
+
+// ---- 5-point stencils over [NX][NY] with zero values outside -------------------
+// standard form (momentum rows): y = c0 x + c1 xW + c2 xE + c3 xN + c4 xS
+template <typename T, typename X>
+__device__ __forceinline__ X row_std(const T* c, long long n, const X* x, int NX, int NY, int k, int i, int j) {
+    const X xk = x[k];
+    const X xw = i > 0 ? x[k - NY] : X(0), xe = i + 1 < NX ? x[k + NY] : X(0);
+    const X xn = j + 1 < NY ? x[k + 1] : X(0), xs = j > 0 ? x[k - 1] : X(0);
+    X y = X(c[k]) * xk;
+    y = fma(X(c[n + k]), xw, y);
+    y = fma(X(c[2 * n + k]), xe, y);
+    y = fma(X(c[3 * n + k]), xn, y);
+    y = fma(X(c[4 * n + k]), xs, y);
+    return y;
+}
+// Laplacian form (p' and coarse rows): y = c0 x + sum c_nb (x_nb - x)
+__device__ __forceinline__ float row_lap(const float* c, int n, const float* x, int NX, int NY, int k, int i, int j) {
+    const float xk = x[k];
+    const float xw = i > 0 ? x[k - NY] : 0.f, xe = i + 1 < NX ? x[k + NY] : 0.f;
+    const float xn = j + 1 < NY ? x[k + 1] : 0.f, xs = j > 0 ? x[k - 1] : 0.f;
+    float y = c[k] * xk;
+    y = fmaf(c[n + k], xw - xk, y);
+    y = fmaf(c[2 * n + k], xe - xk, y);
+    y = fmaf(c[3 * n + k], xn - xk, y);
+    y = fmaf(c[4 * n + k], xs - xk, y);
+    return y;
+}
+
+// ---- stage 1: momentum assembly ------------------------------------------------
+__device__ void b_assemble_momentum(const BInst& I) {
+    const kc_phys& P = I.P;
+    const Dims D = dims_of(P);
+    const Solid S{I.solid, D.NYp};
+    {
+        const int NX = D.nx + 3, NY = D.NYu, n = NX * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.du.q(k), j = k - i * NY;
+            double c[5], b;
+            u_row(P, I.K, D, S, I.u, I.v, I.p, I.u0, i, j, c, b);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                I.cu[(long long)q * n + k] = c[q];
+                I.cu32[(long long)q * n + k] = f64_to_f32(c[q]);
+            }
+            I.bu[k] = b;
+            I.bu32[k] = f64_to_f32(b);
+        }
+    }
+    {
+        const int NX = D.nx + 2, NY = D.NYv, n = NX * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.dv.q(k), j = k - i * NY;
+            double c[5], b;
+            v_row(P, I.K, D, S, I.u, I.v, I.p, I.v0, i, j, c, b);
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                I.cv[(long long)q * n + k] = c[q];
+                I.cv32[(long long)q * n + k] = f64_to_f32(c[q]);
+            }
+            I.bv[k] = b;
+            I.bv32[k] = f64_to_f32(b);
+        }
+    }
+    __syncthreads();
+}
+
+// ---- stage 2: a momentum system by FP32 red-black Gauss-Seidel in FP64 refinement ----
+// r32 = b - A x in FP64, returns {||r||^2, ||b||^2}
+__device__ __forceinline__ void b_resid64(const double* c, const double* bvec, const double* x, float* r32, int NX,
+                                          int NY, Div dy, double (&s)[2]) {
+    const int n = NX * NY;
+    double rr = 0.0, bb = 0.0;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        const int i = dy.q(k), j = k - i * NY;
+        const double bk = bvec[k];
+        const double r = bk - row_std<double, double>(c, n, x, NX, NY, k, i, j);
+        r32[k] = f64_to_f32(r);
+        rr = fma(r, r, rr);
+        bb = fma(bk, bk, bb);
+    }
+    s[0] = rr;
+    s[1] = bb;
+    bsum<2>(s);
+}
+
+// status of a refinement pass over {||r||^2, ||b||^2}, as refined_core in kc_solver.cu:
+// 0 go on, 1 stop with *status set
+struct Refine {
+    double best = INFINITY, bb = 0.0, rel = 1.0;
+    int stalls = 0;
+    bool applied = false;
+    __device__ int check(int it, const double (&s)[2], int* status, bool* undo) {
+        *undo = false;
+        if (it == 0) bb = s[1];
+        if (!isfinite(s[0]) || !isfinite(bb)) {
+            rel = NAN;
+            *status = KC_NONFINITE;
+            return 1;
+        }
+        rel = bb > 0 ? sqrt(s[0] / bb) : 0.0;
+        if (applied && !(rel < best)) {   // the last correction raised the true residual: undo it
+            *undo = true;
+            rel = best;
+            *status = KC_STALL;
+            return 1;
+        }
+        applied = false;
+        return 0;
+    }
+};
+
+__device__ void b_gs_refined(const double* c, const double* bvec, const float* c32, double* x, int NX, int NY, Div dy,
+                             const BInst& I, long long* iters, int* status_out) {
+    const int n = NX * NY;
+    float* gw = I.gw;
+    float* r = I.r32;
+    float* d = I.d32;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        const float a = c32[k];
+        gw[k] = a != 0.f ? 1.f / a : 0.f;
+    }
+    Refine R;
+    int status = KC_MAXITER;
+    long long total = 0;
+    for (int it = 0; it <= kBMaxRefine; ++it) {
+        double s[2];
+        b_resid64(c, bvec, x, r, NX, NY, dy, s);   // (its barrier also publishes gw and the last x)
+        bool undo = false;
+        if (R.check(it, s, &status, &undo)) {
+            if (undo) {
+                for (int k = threadIdx.x; k < n; k += kBT) x[k] -= (double)d[k];
+                __syncthreads();
+            }
+            break;
+        }
+        if (R.bb == 0.0 || R.rel < I.eps) {
+            status = KC_OK;
+            break;
+        }
+        if (R.rel >= 0.9 * R.best) {
+            if (++R.stalls >= 2) {
+                status = KC_STALL;
+                break;
+            }
+        } else {
+            R.stalls = 0;
+        }
+        R.best = fmin(R.best, R.rel);
+        if (it == kBMaxRefine || total >= kBMomentumSweeps) break;
+        // kBGsSweeps red-black sweeps of A32 d = r from d = 0 (red first)
+        for (int k = threadIdx.x; k < n; k += kBT) {   // the first (red) half-sweep from d = 0
+            const int i = dy.q(k), j = k - i * NY;
+            d[k] = ((i + j) & 1) == 0 ? gw[k] * r[k] : 0.f;
+        }
+        __syncthreads();
+        for (int h = 1; h < 2 * kBGsSweeps; ++h) {
+            const int col = h & 1;
+            for (int k = threadIdx.x; k < n; k += kBT) {
+                const int i = dy.q(k), j = k - i * NY;
+                if (((i + j) & 1) != col) continue;
+                const float y = row_std<float, float>(c32, n, d, NX, NY, k, i, j);
+                d[k] = fmaf(gw[k], r[k] - y, d[k]);
+            }
+            __syncthreads();
+        }
+        total += kBGsSweeps;
+        int bad = 0;
+        for (int k = threadIdx.x; k < n; k += kBT) bad |= !isfinite(d[k]);
+        bad = __syncthreads_or(bad);
+        if (bad) {
+            status = KC_NONFINITE;
+            break;
+        }
+        for (int k = threadIdx.x; k < n; k += kBT) x[k] += (double)d[k];
+        __syncthreads();   // the next residual reads x's neighbours
+        R.applied = true;
+    }
+    __syncthreads();
+    *iters += total;
+    *status_out = status;
+}
+
+// ---- stage 3: under-relaxation and the outlet column (k_relax, k_outlet_conserve) ----
+__device__ void b_relax_outlet(const BInst& I) {
+    const kc_phys& P = I.P;
+    const Dims D = dims_of(P);
+    const Solid S{I.solid, D.NYp};
+    const double a = P.alpha_m;
+    {
+        const int NY = D.NYu, n = (D.nx + 3) * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.du.q(k), j = k - i * NY;
+            if (unk_u(P, S, i, j)) I.u[k] = a * I.um[k] + I.K.one_m_am * I.u[k];
+        }
+    }
+    {
+        const int NY = D.NYv, n = (D.nx + 2) * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.dv.q(k), j = k - i * NY;
+            if (unk_v(P, S, i, j)) I.v[k] = a * I.vm[k] + I.K.one_m_am * I.v[k];
+        }
+    }
+    __syncthreads();
+    // outlet: zero gradient, then the outflow rescaled to the inflow
+    double acc[2] = {0.0, 0.0};
+    for (int j = 1 + threadIdx.x; j <= D.ny; j += kBT) {
+        const double w = I.u[(long long)D.nx * D.NYu + j];
+        I.u[(long long)(D.nx + 1) * D.NYu + j] = w;
+        acc[0] += I.u[(long long)1 * D.NYu + j];
+        acc[1] += w;
+    }
+    bsum<2>(acc);
+    const double coef = acc[0] / acc[1];
+    for (int j = 1 + threadIdx.x; j <= D.ny; j += kBT) {
+        double* o = I.u + (long long)(D.nx + 1) * D.NYu + j;
+        *o = coef * *o;
+    }
+    __syncthreads();
+}
+
+// ---- stage 4: p' rows and the mass residual (the channel branch of k_assemble_pcorr) ----
+__device__ double b_assemble_pcorr(const BInst& I) {
+    const kc_phys& P = I.P;
+    const Dims D = dims_of(P);
+    const Solid S{I.solid, D.NYp};
+    const int NX = D.nx + 2, NY = D.NYp, n = NX * NY;
+    const int nx = D.nx, ny = D.ny;
+    const double rho = P.rho, dx = P.dx, dy = P.dy;
+    const double* u = I.u;
+    const double* v = I.v;
+    double mx = 0.0;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        const int i = I.dp.q(k), j = k - i * NY;
+        double c[5] = {0, 0, 0, 0, 0}, b = 0.0, xs = 0.0;
+        if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
+            const double md = rho * (u[(long long)i * D.NYu + j] - u[(long long)(i + 1) * D.NYu + j]) * dy +
+                              rho * (v[(long long)i * D.NYv + j] - v[(long long)i * D.NYv + j + 1]) * dx;
+            if (S.cell(i, j)) {
+                c[0] = 1.0;
+            } else {
+                const double tw = I.K.nrdy2 / I.cu[(long long)i * D.NYu + j];
+                const double te = I.K.nrdy2 / I.cu[(long long)(i + 1) * D.NYu + j];
+                const double tv = I.K.nrdx2 / I.cv[(long long)i * D.NYv + j];
+                const double tn = I.K.nrdx2 / I.cv[(long long)i * D.NYv + j + 1];
+                double aW = 0.0, aE = 0.0, aN = 0.0, aS = 0.0;
+                if (unk_u(P, S, i, j)) aW = tw;
+                if (unk_u(P, S, i + 1, j)) aE = te;
+                if (i == nx && unk_u(P, S, nx, j)) aE = tw;   // the outlet row links to face nx again
+                if (unk_v(P, S, i, j + 1)) aN = tn;
+                if (unk_v(P, S, i, j)) aS = tv;
+                xs = aW + aE + aN + aS;
+                c[0] = -xs;
+                c[1] = aW;
+                c[2] = aE;
+                c[3] = aN;
+                c[4] = aS;
+                b = md;
+                mx = fmax(mx, fabs(md));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 5; ++q) I.cp[(long long)q * n + k] = c[q];
+        I.bp[k] = b;
+        I.cp32[k] = f64_to_f32(c[0] + xs);   // Laplacian form: component 0 is the row sum
+#pragma unroll
+        for (int q = 1; q < 5; ++q) I.cp32[(long long)q * n + k] = f64_to_f32(c[q]);
+        I.bp32[k] = f64_to_f32(b);
+    }
+    return bmax(mx);   // (its barriers publish the rows)
+}
+
+// ---- stage 5: the p' solve --------------------------------------------------------
+// hierarchy: smoother weights and isolation flags of level 0, then the Galerkin
+// coarse rows level by level (k_mg_diag0, k_mg_coarsen), then the coarsest inverse
+__device__ void b_mg_setup(const BInst& I, float* inv, int* inv_bad) {
+    {
+        const BLvl& L = I.lv[0];
+        const int n = L.NX * L.NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const float w = L.c[n + k], ea = L.c[2 * n + k], no = L.c[3 * n + k], so = L.c[4 * n + k];
+            const float d = L.c[k] - (w + ea + no + so);
+            const bool linked = w != 0.f || ea != 0.f || no != 0.f || so != 0.f;
+            L.iso[k] = linked ? 0 : 1;
+            L.w[k] = d == 0.f ? 0.f : (linked ? L.omega / d : 1.f / d);
+        }
+        __syncthreads();
+    }
+    for (int l = 0; l + 1 < I.levels; ++l) {
+        const BLvl& F = I.lv[l];
+        const BLvl& Q = I.lv[l + 1];
+        const int nf = F.NX * F.NY, nc = Q.NX * Q.NY;
+        for (int kc = threadIdx.x; kc < nc; kc += kBT) {
+            const int Ic = Q.dy.q(kc), Jc = kc - Ic * Q.NY;
+            float rs = 0.f, aW = 0.f, aE = 0.f, aN = 0.f, aS = 0.f;
+            for (int di = 0; di < 2; ++di) {
+                const int i = 2 * Ic + di;
+                if (i >= F.NX) continue;
+                for (int dj = 0; dj < 2; ++dj) {
+                    const int j = 2 * Jc + dj;
+                    if (j >= F.NY) continue;
+                    const int k = i * F.NY + j;
+                    if (F.iso[k]) continue;
+                    const float w = F.c[nf + k], ea = F.c[2 * nf + k], no = F.c[3 * nf + k], so = F.c[4 * nf + k];
+                    float r = F.c[k];
+                    if (i - 1 < 0 || F.iso[k - F.NY]) r -= w;
+                    else if (di == 0) aW += w;
+                    if (i + 1 >= F.NX || F.iso[k + F.NY]) r -= ea;
+                    else if (di == 1) aE += ea;
+                    if (j + 1 >= F.NY || F.iso[k + 1]) r -= no;
+                    else if (dj == 1) aN += no;
+                    if (j - 1 < 0 || F.iso[k - 1]) r -= so;
+                    else if (dj == 0) aS += so;
+                    rs += r;
+                }
+            }
+            Q.c[kc] = rs;
+            Q.c[nc + kc] = aW;
+            Q.c[2 * nc + kc] = aE;
+            Q.c[3 * nc + kc] = aN;
+            Q.c[4 * nc + kc] = aS;
+            const bool linked = aW != 0.f || aE != 0.f || aN != 0.f || aS != 0.f;
+            const float d = rs - (aW + aE + aN + aS);
+            Q.iso[kc] = linked ? 0 : 1;
+            Q.w[kc] = d == 0.f ? 0.f : (linked ? Q.omega / d : 1.f / d);
+        }
+        __syncthreads();
+    }
+    // coarsest: Gauss-Jordan inversion in shared memory, no pivoting (the Galerkin operator of
+    // the symmetric p' rows with the outlet folded into the row sums is positive definite; a row
+    // without coupled children gets a unit diagonal and a zero right-hand side)
+    const BLvl& C = I.lv[I.levels - 1];
+    const int nc = C.NX * C.NY;
+    for (int e = threadIdx.x; e < nc * nc; e += kBT) {
+        const int i = e / nc, j = e - i * nc;
+        const float w = C.c[nc + i], ea = C.c[2 * nc + i], no = C.c[3 * nc + i], so = C.c[4 * nc + i];
+        float d = C.c[i] - (((w + ea) + no) + so);
+        if (w == 0.f && ea == 0.f && no == 0.f && so == 0.f && d == 0.f) d = 1.f;
+        const int jr = i % C.NY;
+        float val = 0.f;
+        if (j == i) val = d;
+        else if (j == i - C.NY) val = w;
+        else if (j == i + C.NY) val = ea;
+        else if (j == i + 1 && jr + 1 < C.NY) val = no;
+        else if (j == i - 1 && jr >= 1) val = so;
+        inv[e] = val;
+    }
+    __shared__ float rowp[kBCoarse], colp[kBCoarse];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int p = 0; p < nc; ++p) {
+        if (threadIdx.x < nc) {
+            rowp[threadIdx.x] = inv[p * nc + threadIdx.x];
+            colp[threadIdx.x] = inv[threadIdx.x * nc + p];
+        }
+        __syncthreads();
+        const float piv = rowp[p];
+        if (!(piv > 0.f) || !isfinite(piv)) {   // uniform: every thread reads the same pivot
+            if (threadIdx.x == 0) bad = 1;
+            break;
+        }
+        const float ip = 1.f / piv;
+        for (int e = threadIdx.x; e < nc * nc; e += kBT) {
+            const int i = e / nc, j = e - i * nc;
+            const float sp = j == p ? ip : rowp[j] * ip;
+            inv[e] = i == p ? sp : (j == p ? -colp[i] * ip : fmaf(-colp[i], sp, inv[e]));
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    *inv_bad = bad;
+    __syncthreads();
+}
+
+// one V-cycle z = M r on the hierarchy (level 0: b = r, x = z), kc_mg.cu's cycle:
+// down: red start x = W b, 2 nu - 1 half-sweeps (black, red, ...), restriction of the
+// residual over coupled cells; coarsest: x = A^-1 b; up: prolongation onto coupled cells
+// scaled by alpha, 2 nu half-sweeps (black, red, ...)
+__device__ __forceinline__ void b_half_sweep(const BLvl& L, int col) {
+    const int n = L.NX * L.NY;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        const int i = L.dy.q(k), j = k - i * L.NY;
+        if (((i + j) & 1) != col) continue;
+        const float r = L.b[k] - row_lap(L.c, n, L.x, L.NX, L.NY, k, i, j);
+        L.x[k] = fmaf(L.w[k], r, L.x[k]);
+    }
+    __syncthreads();
+}
+
+__device__ void b_vcycle(const BInst& I, const float* inv, int inv_bad) {
+    const int Lc = I.levels - 1;
+    for (int l = 0; l < Lc; ++l) {
+        const BLvl& L = I.lv[l];
+        const BLvl& Q = I.lv[l + 1];
+        const int n = L.NX * L.NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = L.dy.q(k), j = k - i * L.NY;
+            L.x[k] = ((i + j) & 1) == 0 ? L.w[k] * L.b[k] : 0.f;
+        }
+        __syncthreads();
+        for (int h = 1; h < 2 * L.nu; ++h) b_half_sweep(L, h & 1);
+        const int nc = Q.NX * Q.NY;
+        for (int kc = threadIdx.x; kc < nc; kc += kBT) {
+            const int Ic = Q.dy.q(kc), Jc = kc - Ic * Q.NY;
+            float s = 0.f;
+            for (int di = 0; di < 2; ++di) {
+                const int i = 2 * Ic + di;
+                if (i >= L.NX) continue;
+                for (int dj = 0; dj < 2; ++dj) {
+                    const int j = 2 * Jc + dj;
+                    if (j >= L.NY) continue;
+                    const int k = i * L.NY + j;
+                    if (L.iso[k]) continue;
+                    s += L.b[k] - row_lap(L.c, n, L.x, L.NX, L.NY, k, i, j);
+                }
+            }
+            Q.b[kc] = s;
+        }
+        __syncthreads();
+    }
+    {
+        const BLvl& C = I.lv[Lc];
+        const int n = C.NX * C.NY;
+        if (!inv_bad) {
+            const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+            for (int i = wp; i < n; i += kBWarps) {
+                float s = 0.f;
+                for (int j = lane; j < n; j += 32) s = fmaf(inv[i * n + j], C.b[j], s);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFull, s, o);
+                if (lane == 0) C.x[i] = s;
+            }
+            __syncthreads();
+        } else {   // Jacobi sweeps (the inverse failed)
+            for (int k = threadIdx.x; k < n; k += kBT) C.x[k] = C.w[k] * C.b[k];
+            __syncthreads();
+            for (int sw = 1; sw < kBCoarseFallbackSweeps; ++sw) {
+                float xn[2] = {0.f, 0.f};
+                int q = 0;
+                for (int k = threadIdx.x; k < n; k += kBT, ++q) {
+                    const int i = C.dy.q(k), j = k - i * C.NY;
+                    xn[q & 1] = C.x[k] + C.w[k] * (C.b[k] - row_lap(C.c, n, C.x, C.NX, C.NY, k, i, j));
+                }
+                __syncthreads();
+                q = 0;
+                for (int k = threadIdx.x; k < n; k += kBT, ++q) C.x[k] = xn[q & 1];
+                __syncthreads();
+            }
+        }
+    }
+    for (int l = Lc - 1; l >= 0; --l) {
+        const BLvl& L = I.lv[l];
+        const BLvl& Q = I.lv[l + 1];
+        const int n = L.NX * L.NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            if (L.iso[k]) continue;
+            const int i = L.dy.q(k), j = k - i * L.NY;
+            L.x[k] = fmaf(L.alpha, Q.x[(i >> 1) * Q.NY + (j >> 1)], L.x[k]);
+        }
+        __syncthreads();
+        for (int h = 1; h <= 2 * L.nu; ++h) b_half_sweep(L, h & 1);
+    }
+}
+
+// multigrid-preconditioned CG on the FP32 p' rows: A d = r from d = 0 to ||r_k|| <= eps_in ||r_0||
+// (r is overwritten); FP64 inner products.  Returns the iterations, *status.
+__device__ int b_pcg(const BInst& I, double eps_in, const float* inv, int inv_bad, int* status) {
+    const BLvl& L0 = I.lv[0];
+    const int NX = L0.NX, NY = L0.NY, n = NX * NY;
+    const float* c = L0.c;
+    float* r = I.cr;
+    float* z = I.cz;
+    float* p = I.cpv;
+    float* q = I.cq;
+    float* d = I.cd;
+    double s1[1];
+    double rr0 = 0.0;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        d[k] = 0.f;
+        rr0 = fma((double)r[k], (double)r[k], rr0);
+    }
+    s1[0] = rr0;
+    bsum<1>(s1);
+    rr0 = s1[0];
+    *status = KC_OK;
+    if (rr0 == 0.0) return 0;
+    const double stop2 = eps_in * eps_in * rr0;
+    b_vcycle(I, inv, inv_bad);
+    double rho = 0.0;
+    for (int k = threadIdx.x; k < n; k += kBT) {
+        p[k] = z[k];
+        rho = fma((double)r[k], (double)z[k], rho);
+    }
+    s1[0] = rho;
+    bsum<1>(s1);
+    rho = s1[0];
+    int it = 0;
+    *status = KC_MAXITER;
+    while (it < kBMaxCg) {
+        if (!(rho > 0.0)) {   // (r, M r) <= 0: M is not positive definite
+            *status = isfinite(rho) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            break;
+        }
+        double pq = 0.0;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = L0.dy.q(k), j = k - i * NY;
+            const float y = row_lap(c, n, p, NX, NY, k, i, j);
+            q[k] = y;
+            pq = fma((double)p[k], (double)y, pq);
+        }
+        s1[0] = pq;
+        bsum<1>(s1);
+        pq = s1[0];
+        if (!(pq > 0.0)) {
+            *status = isfinite(pq) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            break;
+        }
+        const double alpha = rho / pq;
+        const float af = (float)alpha;
+        double rr = 0.0;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            d[k] = fmaf(af, p[k], d[k]);
+            const float rn = fmaf(-af, q[k], r[k]);
+            r[k] = rn;
+            rr = fma((double)rn, (double)rn, rr);
+        }
+        s1[0] = rr;
+        bsum<1>(s1);
+        rr = s1[0];
+        ++it;
+        if (!isfinite(rr)) {
+            *status = KC_NONFINITE;
+            break;
+        }
+        if (rr <= stop2) {
+            *status = KC_OK;
+            break;
+        }
+        b_vcycle(I, inv, inv_bad);
+        double rz = 0.0;
+        for (int k = threadIdx.x; k < n; k += kBT) rz = fma((double)r[k], (double)z[k], rz);
+        s1[0] = rz;
+        bsum<1>(s1);
+        const float beta = (float)(s1[0] / rho);
+        rho = s1[0];
+        for (int k = threadIdx.x; k < n; k += kBT) p[k] = fmaf(beta, p[k], z[k]);
+        __syncthreads();
+    }
+    return it;
+}
+
+// p' = 0, then FP32 CG passes on the FP64 residual until ||b - A p'|| / ||b|| < eps
+__device__ void b_pcorr_solve(const BInst& I, float* inv, int* inv_bad_s, long long* iters, int* status_out) {
+    const Dims D = dims_of(I.P);
+    const int NX = D.nx + 2, NY = D.NYp, n = NX * NY;
+    double* x = I.pc;
+    for (int k = threadIdx.x; k < n; k += kBT) x[k] = 0.0;
+    b_mg_setup(I, inv, inv_bad_s);
+    const int inv_bad = *inv_bad_s;
+    Refine R;
+    int status = KC_MAXITER;
+    long long total = 0;
+    for (int it = 0; it <= kBMaxRefine; ++it) {
+        double s[2];
+        b_resid64(I.cp, I.bp, x, I.cr, NX, NY, I.dp, s);
+        bool undo = false;
+        if (R.check(it, s, &status, &undo)) {
+            if (undo) {
+                for (int k = threadIdx.x; k < n; k += kBT) x[k] -= (double)I.cd[k];
+                __syncthreads();
+            }
+            break;
+        }
+        if (R.bb == 0.0 || R.rel < I.eps) {
+            status = KC_OK;
+            break;
+        }
+        if (R.rel >= 0.9 * R.best) {
+            if (++R.stalls >= 2) {
+                status = KC_STALL;
+                break;
+            }
+        } else {
+            R.stalls = 0;
+        }
+        R.best = fmin(R.best, R.rel);
+        if (it == kBMaxRefine) break;
+        int st = KC_OK;
+        const int k_it = b_pcg(I, fmax(I.eps_inner_p, 0.5 * I.eps / R.rel), inv, inv_bad, &st);
+        total += k_it;
+        int bad = 0;
+        for (int k = threadIdx.x; k < n; k += kBT) bad |= !isfinite(I.cd[k]);
+        bad = __syncthreads_or(bad);
+        if (!bad)
+            for (int k = threadIdx.x; k < n; k += kBT) x[k] += (double)I.cd[k];
+        __syncthreads();   // the next residual reads x's neighbours
+        R.applied = !bad;
+        if ((st != KC_OK && k_it == 0) || bad) {
+            status = bad ? KC_NONFINITE : st;
+            break;
+        }
+    }
+    __syncthreads();
+    *iters += total;
+    *status_out = status;
+}
+
+// ---- stage 6: corrections (the channel branch of k_correct) ----------------------
+__device__ void b_correct(const BInst& I) {
+    const kc_phys& P = I.P;
+    const Dims D = dims_of(P);
+    const Solid S{I.solid, D.NYp};
+    const int nx = D.nx, ny = D.ny;
+    const double au = P.alpha_u, ap = P.alpha_p, dx = P.dx, dy = P.dy;
+    const double* pc = I.pc;
+#define BPC_(a, bb) pc[(long long)(a) * D.NYp + (bb)]
+    {
+        const int NY = D.NYu, n = (nx + 3) * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.du.q(k), j = k - i * NY;
+            if (unk_u(P, S, i, j)) {
+                I.u[k] = I.u[k] + au * (BPC_(i - 1, j) - BPC_(i, j)) * dy / I.cu[k];
+            } else if (i == nx + 1 && j >= 1 && j <= ny && unk_u(P, S, nx, j)) {
+                I.u[k] = I.u[k] + au * (BPC_(nx, j) - BPC_(nx + 1, j)) * dy / I.cu[(long long)nx * D.NYu + j];
+            }
+        }
+    }
+    {
+        const int NY = D.NYv, n = (nx + 2) * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.dv.q(k), j = k - i * NY;
+            if (unk_v(P, S, i, j)) I.v[k] = I.v[k] + au * (BPC_(i, j - 1) - BPC_(i, j)) * dx / I.cv[k];
+        }
+    }
+    {
+        const int NY = D.NYp, n = (nx + 2) * NY;
+        for (int k = threadIdx.x; k < n; k += kBT) {
+            const int i = I.dp.q(k), j = k - i * NY;
+            if (i >= 1 && i <= nx && j >= 1 && j <= ny && !S.cell(i, j)) I.p[k] = I.p[k] + ap * pc[k];
+        }
+    }
+#undef BPC_
+    __syncthreads();
+}
+
+// ---- the kernel: block b advances instance b by `steps` time steps ------------------
+__global__ void __launch_bounds__(kBT, 2) k_batch_steps(const BInst* __restrict__ insts, int steps) {
+    const BInst& I = insts[blockIdx.x];
+    __shared__ float inv[kBCoarse * kBCoarse];
+    __shared__ int inv_bad;
+    const Dims D = dims_of(I.P);
+    kc_channel_stats tot{};
+    kc_channel_stats S{};
+    for (int step = 0; step < steps; ++step) {
+        S = kc_channel_stats{};
+        double mass = 0.0;
+        for (int outer = 0; outer < I.max_outer; ++outer) {
+            b_assemble_momentum(I);
+            int su = KC_OK, sv = KC_OK, sp = KC_OK;
+            b_gs_refined(I.cu, I.bu, I.cu32, I.um, D.nx + 3, D.NYu, I.du, I, &S.it_u, &su);
+            b_gs_refined(I.cv, I.bv, I.cv32, I.vm, D.nx + 2, D.NYv, I.dv, I, &S.it_v, &sv);
+            b_relax_outlet(I);
+            mass = b_assemble_pcorr(I);
+            b_pcorr_solve(I, inv, &inv_bad, &S.it_p, &sp);
+            b_correct(I);
+            S.outer += 1;
+            const bool nonfinite = su == KC_NONFINITE || sv == KC_NONFINITE || sp == KC_NONFINITE;
+            if (nonfinite) S.status = KC_NONFINITE;
+            else if ((su != KC_OK || sv != KC_OK || sp != KC_OK) && S.status == KC_OK) S.status = KC_MAXITER;
+            S.fallbacks += (su != KC_OK) + (sv != KC_OK) + (sp != KC_OK);
+            S.mass = mass;
+            if (nonfinite || !isfinite(mass)) {
+                S.status = KC_NONFINITE;
+                break;
+            }
+            if (mass <= I.mass_tol) break;
+        }
+        // time_forward
+        {
+            const int nu = (D.nx + 3) * D.NYu, nv = (D.nx + 2) * D.NYv;
+            for (int k = threadIdx.x; k < nu; k += kBT) I.u0[k] = I.u[k];
+            for (int k = threadIdx.x; k < nv; k += kBT) I.v0[k] = I.v[k];
+            __syncthreads();
+        }
+        tot.outer += S.outer;
+        tot.fallbacks += S.fallbacks;
+        tot.it_u += S.it_u;
+        tot.it_v += S.it_v;
+        tot.it_p += S.it_p;
+        tot.mass = fmax(tot.mass, S.mass);
+        if (S.status != KC_OK && tot.status == KC_OK) tot.status = S.status;
+        if (S.status == KC_NONFINITE) break;
+    }
+    if (threadIdx.x == 0) {
+        *I.last = S;
+        *I.total = tot;
+    }
+}
+
+}  // namespace
+}  // namespace kc
+
+using namespace kc;
+
+namespace {
+
+struct BSizes {
+    long long nu, nv, np;
+    int levels;
+    int NX[kBLevels], NY[kBLevels];
+};
+BSizes sizes_of(const kc_channel* c) {
+    BSizes z{};
+    const int nx = c->phys.nx, ny = c->phys.ny;
+    z.nu = (long long)(nx + 3) * (ny + 2);
+    z.nv = (long long)(nx + 2) * (ny + 3);
+    z.np = (long long)(nx + 2) * (ny + 2);
+    z.NX[0] = nx + 2;
+    z.NY[0] = ny + 2;
+    int L = 0;
+    while (L + 1 < kBLevels && (long long)z.NX[L] * z.NY[L] > kBCoarse) {
+        z.NX[L + 1] = (z.NX[L] + 1) / 2;
+        z.NY[L + 1] = (z.NY[L] + 1) / 2;
+        ++L;
+    }
+    z.levels = L + 1;
+    return z;
+}
+// bytes of one instance's scratch: Gauss-Seidel weights, FP32 residual and correction over the
+// larger momentum grid; CG r, z, p, q, d; per level >= 1 five coefficient planes, b, x, w and the
+// flags; level 0's w and flags
+size_t inst_bytes(const BSizes& z) {
+    const long long nm = std::max(z.nu, z.nv);
+    size_t o = 3 * align256((size_t)nm * 4) + 5 * align256((size_t)z.np * 4);
+    o += align256((size_t)z.np * 4) + align256((size_t)z.np);
+    for (int l = 1; l < z.levels; ++l) {
+        const size_t n = (size_t)z.NX[l] * z.NY[l];
+        o += align256(5 * n * 4) + 3 * align256(n * 4) + align256(n);
+    }
+    return o;
+}
+size_t head_bytes(int n) {
+    return align256((size_t)n * sizeof(BInst)) + 2 * align256((size_t)n * sizeof(kc_channel_stats));
+}
+
+int check_channel(const kc_channel* c, int k) {
+    if (!c) return set_error("kc_channel_batch_fused: instance %d is null", k), KC_ERR_ARG;
+    if (c->phys.mode != KC_MODE_CHANNEL)
+        return set_error("kc_channel_batch_fused: instance %d: phys.mode must be KC_MODE_CHANNEL", k), KC_ERR_ARG;
+    if (c->precision != KC_F32)
+        return set_error("kc_channel_batch_fused: instance %d: the batched launch runs the mixed path (KC_F32)", k),
+               KC_ERR_ARG;
+    if (c->phys.nx < 2 || c->phys.ny < 2 || (long long)(c->phys.nx + 3) * (c->phys.ny + 3) >= (1ll << 22))
+        return set_error("kc_channel_batch_fused: instance %d: grid %d x %d outside [2, ...] and 4M cells", k,
+                         c->phys.nx, c->phys.ny),
+               KC_ERR_ARG;
+    // exact row indices by multiply-high need cells x row length < 2^32 on every grid
+    if ((long long)(c->phys.nx + 3) * (c->phys.ny + 3) * (c->phys.ny + 3) >= (1ll << 32))
+        return set_error("kc_channel_batch_fused: instance %d: grid %d x %d too large", k, c->phys.nx, c->phys.ny),
+               KC_ERR_UNSUPPORTED;
+    const BSizes z = sizes_of(c);
+    if ((long long)z.NX[z.levels - 1] * z.NY[z.levels - 1] > kBCoarse)
+        return set_error("kc_channel_batch_fused: instance %d: grid %d x %d does not coarsen to %d cells in %d levels",
+                         k, c->phys.nx, c->phys.ny, kBCoarse, kBLevels),
+               KC_ERR_UNSUPPORTED;
+    const void* need[] = {c->u, c->v, c->p, c->u0, c->v0, c->pcor, c->u_mid, c->v_mid, c->solid, c->coef_u,
+                          c->b_u, c->coef_v, c->b_v, c->coef_p, c->b_p, c->coef_u32, c->b_u32, c->coef_v32,
+                          c->b_v32, c->coef_p32, c->b_p32};
+    for (const void* q : need)
+        if (!q) return set_error("kc_channel_batch_fused: instance %d: a field or system buffer is null", k), KC_ERR_ARG;
+    return KC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t kc_channel_batch_fused_ws_bytes(const kc_channel* const* chs, int n) {
+    if (!chs || n < 1) return 0;
+    size_t total = head_bytes(n);
+    for (int k = 0; k < n; ++k) {
+        if (!chs[k]) return 0;
+        total += inst_bytes(sizes_of(chs[k]));
+    }
+    return total;
+}
+
+int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void* ws, size_t ws_bytes,
+                           kc_channel_stats* last, kc_channel_stats* total, void* stream) {
+    if (!chs || n < 0 || steps < 0) return set_error("kc_channel_batch_fused: bad arguments"), KC_ERR_ARG;
+    if (n == 0 || steps == 0) return KC_OK;
+    for (int k = 0; k < n; ++k) {
+        const int rc = check_channel(chs[k], k);
+        if (rc) return rc;
+    }
+    const size_t need = kc_channel_batch_fused_ws_bytes(chs, n);
+    if (!ws || ws_bytes < need || ((uintptr_t)ws & 255))
+        return set_error("kc_channel_batch_fused: workspace %zu bytes (256-aligned) < required %zu", ws_bytes, need),
+               KC_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    char* base = (char*)ws;
+    BInst* d_inst = (BInst*)base;
+    kc_channel_stats* d_last = (kc_channel_stats*)(base + align256((size_t)n * sizeof(BInst)));
+    kc_channel_stats* d_total =
+        (kc_channel_stats*)((char*)d_last + align256((size_t)n * sizeof(kc_channel_stats)));
+    char* o = base + head_bytes(n);
+    std::vector<BInst> h(n);
+    for (int k = 0; k < n; ++k) {
+        const kc_channel* c = chs[k];
+        const BSizes z = sizes_of(c);
+        BInst& I = h[k];
+        memset(&I, 0, sizeof(BInst));
+        I.P = c->phys;
+        I.K = consts_of(c->phys);
+        I.max_outer = c->max_outer;
+        I.mass_tol = c->mass_tol;
+        I.eps = c->eps;
+        I.eps_inner_p = c->eps_inner_p > 0 ? c->eps_inner_p : 1e-4;
+        I.u = c->u;
+        I.v = c->v;
+        I.p = c->p;
+        I.u0 = c->u0;
+        I.v0 = c->v0;
+        I.pc = c->pcor;
+        I.um = c->u_mid;
+        I.vm = c->v_mid;
+        I.solid = c->solid;
+        I.cu = c->coef_u;
+        I.bu = c->b_u;
+        I.cv = c->coef_v;
+        I.bv = c->b_v;
+        I.cp = c->coef_p;
+        I.bp = c->b_p;
+        I.cu32 = c->coef_u32;
+        I.bu32 = c->b_u32;
+        I.cv32 = c->coef_v32;
+        I.bv32 = c->b_v32;
+        I.cp32 = c->coef_p32;
+        I.bp32 = c->b_p32;
+        const long long nm = std::max(z.nu, z.nv);
+        auto take = [&](size_t bytes) {
+            char* q = o;
+            o += align256(bytes);
+            return q;
+        };
+        I.gw = (float*)take((size_t)nm * 4);
+        I.r32 = (float*)take((size_t)nm * 4);
+        I.d32 = (float*)take((size_t)nm * 4);
+        I.cr = (float*)take((size_t)z.np * 4);
+        I.cz = (float*)take((size_t)z.np * 4);
+        I.cpv = (float*)take((size_t)z.np * 4);
+        I.cq = (float*)take((size_t)z.np * 4);
+        I.cd = (float*)take((size_t)z.np * 4);
+        I.levels = z.levels;
+        const kc_mg_opts& mo = c->mg_opts;
+        for (int l = 0; l < z.levels; ++l) {
+            BLvl& L = I.lv[l];
+            L.NX = z.NX[l];
+            L.NY = z.NY[l];
+            L.dy = div_of(L.NY);
+            const size_t nl = (size_t)L.NX * L.NY;
+            if (l == 0) {
+                L.c = c->coef_p32;
+                L.b = I.cr;
+                L.x = I.cz;
+                L.w = (float*)take(nl * 4);
+                L.iso = (unsigned char*)take(nl);
+            } else {
+                L.c = (float*)take(5 * nl * 4);
+                L.b = (float*)take(nl * 4);
+                L.x = (float*)take(nl * 4);
+                L.w = (float*)take(nl * 4);
+                L.iso = (unsigned char*)take(nl);
+            }
+            const int li = std::min(l, KC_MG_MAX_LEVELS - 1);
+            L.omega = mo.omega[li] != 0.f ? mo.omega[li] : (l == 0 ? 1.0f : 1.5f);
+            L.alpha = mo.alpha[li] != 0.f ? mo.alpha[li] : (l == 0 ? 1.9f : 2.0f);
+            L.nu = l == 0 ? std::max(1, mo.nu_pre) : std::max(1, mo.nu_coarse);
+        }
+        I.du = div_of(c->phys.ny + 2);
+        I.dv = div_of(c->phys.ny + 3);
+        I.dp = div_of(c->phys.ny + 2);
+        I.last = d_last + k;
+        I.total = d_total + k;
+    }
+    if ((size_t)(o - base) > ws_bytes) return set_error("kc_channel_batch_fused: workspace layout overflow"), KC_ERR_WORKSPACE;
+    KC_CUDA(cudaMemcpyAsync(d_inst, h.data(), (size_t)n * sizeof(BInst), cudaMemcpyHostToDevice, s));
+    k_batch_steps<<<n, kBT, 0, s>>>(d_inst, steps);
+    KC_LAUNCH_CHECK("k_batch_steps");
+    count_launches(1);
+    std::vector<kc_channel_stats> hs(2 * (size_t)n);
+    KC_CUDA(cudaMemcpyAsync(hs.data(), d_last, (size_t)n * sizeof(kc_channel_stats), cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaMemcpyAsync(hs.data() + n, d_total, (size_t)n * sizeof(kc_channel_stats), cudaMemcpyDeviceToHost, s));
+    KC_CUDA(cudaStreamSynchronize(s));
+    if (last) memcpy(last, hs.data(), (size_t)n * sizeof(kc_channel_stats));
+    if (total) memcpy(total, hs.data() + n, (size_t)n * sizeof(kc_channel_stats));
+    return KC_OK;
+}
+
+}  // extern "C"
