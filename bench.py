@@ -689,7 +689,7 @@ def run_batch(args, cfgs=None, workload=None):
     """Instance time steps/s of the batched configuration: N instances (sizes
     128x32 .. 640x128, D 4-16, Re 60-200).  Executors (--batch-executors):
     ``fused``, every instance and every timed step in ONE persistent launch
-    (kc_channel_batch_fused, block k = instance k); ``native``, one CUDA stream
+    (kc_channel_batch_fused: each large instance on a block of its own, the others four to a block); ``native``, one CUDA stream
     per instance driven by native threads (kc_channel_batch_step);
     ``sequential``, the instances one after another on one stream.  Each
     executor starts from the seeded initial state: W warm-up steps, then K
@@ -730,7 +730,7 @@ def run_batch(args, cfgs=None, workload=None):
             launches = lib.kc_launch_count() - l0
             tot = b.fused_totals
             outer = float(np.mean([x["outer"] for x in tot])) / max(1, args.steps)
-            out[key] = {"driver": "one persistent launch (kc_channel_batch_fused), block k = instance k",
+            out[key] = {"driver": "one persistent launch (kc_channel_batch_fused): instances of >= 40k p cells on a 1024-thread block each, the others on 256 threads four to a block",
                         "seconds": round(t, 3), "value": round(len(cfgs) * args.steps / t, 2),
                         "cell_updates_per_s": round(out["cells"] * args.steps / t, 1),
                         "outer_per_step": round(outer, 2), "gpu_launches": int(launches),

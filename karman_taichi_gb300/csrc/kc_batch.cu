@@ -1,13 +1,15 @@
 // The batched channel executor as one persistent launch.
 //
 // kc_channel_batch_fused advances n independent channel instances (uneven
-// grid sizes) by `steps` time steps in ONE kernel launch: block b owns
-// instance b and runs its whole SIMPLE time steps -- the outer loop of
+// grid sizes) by `steps` time steps in ONE kernel launch: a group of threads
+// owns an instance -- a whole 1024-thread block for an instance of at least
+// 40k p cells, a quarter block (256 threads, four instances to a block)
+// otherwise -- and runs its whole SIMPLE time steps (the outer loop of
 // karman_taichi.py:633-659 / simple.py:270-281 with the stages of the mixed
-// path -- with block barriers between the phases and nothing on the host
-// between them.  Instances never wait on each other, so the launch needs no
-// grid-wide synchronisation and no instance can hold another up.  Per outer
-// iteration, per instance:
+// path), with a named barrier of its own between the phases and nothing on
+// the host between them.  Instances never wait on each other, so the launch
+// needs no grid-wide synchronisation and no instance can hold another up.
+// Per outer iteration, per instance:
 //
 //   assemble_momentum   u_row / v_row (kc_simple.cuh) on every face: the
 //                       FP64 systems and their FP32 copies, bit for bit the
@@ -30,19 +32,22 @@
 //   correct             u, v, p corrections (kc_correct's arithmetic)
 //
 // and the outer loop stops when the mass residual is <= mass_tol or after
-// max_outer iterations; then u0 = u, v0 = v.  FP64 inner products and
-// residual norms are block reductions in a fixed order, so every instance
+// max_outer iterations; then u0 = u, v0 = v.  Residual norms (FP64) and the
+// CG inner products (double-float) are group reductions in a fixed order, and
+// an instance's thread count depends on its size alone, so every instance
 // computes bit for bit what it computes alone in a batch of one, whatever
-// else shares the launch.  The block reductions differ in order from the
+// else shares the launch.  The reductions differ in order from the
 // per-instance multi-block kernels of kc_channel_step, so the two agree to
 // rounding, not bitwise.
 //
-// Why one block per instance: an instance of the batched configuration has
-// 4k-83k cells; as separate launches every stage is a few microseconds of
-// launch latency for a fraction of a microsecond of work, and the GPU idles
-// between them.  Here the phases of one instance are separated by a block
-// barrier (~0.1 us) and the 256 instances of the batch stream through HBM
-// together, one block per SM slot.
+// Why a block (or a quarter) per instance: an instance of the batched
+// configuration has 4k-83k cells; as separate launches every stage is a few
+// microseconds of launch latency for a fraction of a microsecond of work.
+// Here the phases of one instance are separated by a barrier (~0.1 us), the
+// large instances each get an SM of their own, and four small ones share
+// one: the 256 instances of the batch fit in one wave of 141 blocks.  The
+// launch ends with its slowest instance, so the sizes are balanced per
+// thread: 83k cells on 1024 threads, at most 22k on 256.
 //
 // Loads use the coherent path throughout (no __ldg): every array is written
 // by an earlier phase of the same launch.
@@ -55,8 +60,10 @@
 namespace kc {
 namespace {
 
-constexpr int kBT = 512;                 // threads per instance block
-constexpr int kBWarps = kBT / 32;
+constexpr int kBBlock = 1024;            // threads per block
+constexpr int kBGroups = 4;              // instances per block at most
+constexpr int kBBigCells = 40000;        // instances of at least this many p cells get a whole block, the
+                                         // others 256 threads (four to a block)
 constexpr int kBLevels = 12;             // multigrid levels at most
 constexpr int kBCoarse = 64;             // cells of the coarsest level at most (dense inverse in shared memory)
 constexpr int kBGsSweeps = 12;           // Gauss-Seidel sweeps per momentum refinement pass
@@ -72,6 +79,30 @@ struct Div {
 };
 inline Div div_of(int d) { return Div{d == 1 ? 0u : (unsigned)((1ull << 32) / (unsigned)d + 1)}; }
 
+// The threads of one instance: a whole block (1024) or a quarter of one (256).  Its phases are
+// separated by a named barrier of its own (id gi + 1, nt threads), so the instances sharing a
+// block never wait on each other.
+struct Grp {
+    int tid, nt, gi;
+    __device__ __forceinline__ void sync() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(gi + 1), "r"(nt) : "memory");
+    }
+    // barrier that also returns whether p was nonzero in any thread of the group
+    __device__ __forceinline__ int any(int p) const {
+        int r;
+        asm volatile(
+            "{\n\t.reg .pred q, o;\n\t"
+            "setp.ne.s32 q, %1, 0;\n\t"
+            "bar.red.or.pred o, %2, %3, q;\n\t"
+            "selp.s32 %0, 1, 0, o;\n\t}"
+            : "=r"(r)
+            : "r"(p), "r"(gi + 1), "r"(nt)
+            : "memory");
+        return r;
+    }
+    __device__ __forceinline__ int warps() const { return nt >> 5; }
+};
+
 struct BLvl {
     float* c;             // 5 planes [NX][NY], Laplacian form (level 0: the FP32 p' copy)
     float* b;             // right-hand side (level 0: CG's residual)
@@ -79,7 +110,7 @@ struct BLvl {
     float* w;             // smoother weights
     unsigned char* iso;   // rows without links
     int NX, NY;
-    Div dy;
+    Div dy, dh;           // division by NY and by (NY + 1) / 2 (the cells of one colour in a row)
     float omega, alpha;   // smoother weight, weight of the coarse correction prolonged into this level
     int nu;               // red-black sweeps before and after the coarse correction
 };
@@ -98,40 +129,62 @@ struct BInst {
     BLvl lv[kBLevels];
     int levels;
     Div du, dv, dp;                        // row lengths of the u, v and p grids
+    Div dhu, dhv;                          // ... and their halves rounded up (the u and v grids)
+    int nt;                                // threads of the instance (1024 or 256)
     kc_channel_stats* last;                // per instance: the last step's statistics
     kc_channel_stats* total;               // ... and the sums over the launch's steps
 };
 
-// ---- block reductions with the result in every thread -------------------------
+// ---- group reductions with the result in every thread (fixed order) ---------------
 template <int NV>
-__device__ __forceinline__ void bsum(double (&v)[NV]) {
-    __shared__ double sh[NV][kBWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+__device__ __forceinline__ void bsum(const Grp& g, double (&v)[NV]) {
+    __shared__ double sh[kBGroups][NV][32];
+    const int lane = g.tid & 31, w = g.tid >> 5, nw = g.warps();
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         const double s = warp_sum(v[q]);
-        if (lane == 0) sh[q][w] = s;
+        if (lane == 0) sh[g.gi][q][w] = s;
     }
-    __syncthreads();
+    g.sync();
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
         double s = 0.0;
-#pragma unroll
-        for (int i = 0; i < kBWarps; ++i) s += sh[q][i];
+        for (int i = 0; i < nw; ++i) s += sh[g.gi][q][i];
         v[q] = s;
     }
-    __syncthreads();
+    g.sync();
 }
-__device__ __forceinline__ double bmax(double v) {
-    __shared__ double sh[kBWarps];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    v = warp_max(v);
-    if (lane == 0) sh[w] = v;
-    __syncthreads();
-    double m = 0.0;
+// double-float sums of FP32 products (Acc<float>), as doubles in every thread
+template <int NV>
+__device__ __forceinline__ void bsum_df(const Grp& g, const Acc<float> (&a)[NV], double (&out)[NV]) {
+    __shared__ DF sh[kBGroups][NV][32];
+    const int lane = g.tid & 31, w = g.tid >> 5, nw = g.warps();
 #pragma unroll
-    for (int i = 0; i < kBWarps; ++i) m = fmax(m, sh[i]);
-    __syncthreads();
+    for (int q = 0; q < NV; ++q) {
+        DF v = a[q].s;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = df_add(v, DF{__shfl_down_sync(kFull, v.hi, o), __shfl_down_sync(kFull, v.lo, o)});
+        if (lane == 0) sh[g.gi][q][w] = v;
+    }
+    g.sync();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        DF v = sh[g.gi][q][0];
+        for (int i = 1; i < nw; ++i) v = df_add(v, sh[g.gi][q][i]);
+        out[q] = (double)v.hi + (double)v.lo;
+    }
+    g.sync();
+}
+__device__ __forceinline__ double bmax(const Grp& g, double v) {
+    __shared__ double sh[kBGroups][32];
+    const int lane = g.tid & 31, w = g.tid >> 5, nw = g.warps();
+    v = warp_max(v);
+    if (lane == 0) sh[g.gi][w] = v;
+    g.sync();
+    double m = 0.0;
+    for (int i = 0; i < nw; ++i) m = fmax(m, sh[g.gi][i]);
+    g.sync();
     return m;
 }
 
@@ -162,14 +215,73 @@ __device__ __forceinline__ float row_lap(const float* c, int n, const float* x, 
     return y;
 }
 
+// One red-black half-sweep x += W (b - A x) over the cells (i, j) with (i + j) & 1 == col, in
+// standard (LAP false) or Laplacian form.  A thread walks the cells of its colour only and keeps
+// U of them in flight: every load of a group is issued before any of its stores, so the group's
+// memory latencies overlap (the stores could alias the next cell's loads for all the compiler
+// knows; they do not: a cell reads only cells of the other colour).
+template <bool LAP, int U>
+__device__ __forceinline__ void hs_sweep(const Grp& g, const float* c, const float* b, const float* w, float* x, int NX, int NY,
+                                         Div dh, int col) {
+    const int half = (NY + 1) >> 1, cnt = NX * half, n = NX * NY;
+    for (int e0 = g.tid; e0 < cnt; e0 += g.nt * U) {
+        int kk[U];
+        float a0[U], a1[U], a2[U], a3[U], a4[U], xc[U], xw[U], xe[U], xn[U], xs[U], bk[U], wk[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * g.nt;
+            int k = -1, i = 0, j = 0;
+            if (e < cnt) {
+                i = dh.q(e);
+                j = 2 * (e - i * half) + ((i + col) & 1);
+                if (j < NY) k = i * NY + j;
+            }
+            kk[u] = k;
+            if (k >= 0) {
+                xc[u] = x[k];
+                xw[u] = i > 0 ? x[k - NY] : 0.f;
+                xe[u] = i + 1 < NX ? x[k + NY] : 0.f;
+                xn[u] = j + 1 < NY ? x[k + 1] : 0.f;
+                xs[u] = j > 0 ? x[k - 1] : 0.f;
+                a0[u] = c[k];
+                a1[u] = c[n + k];
+                a2[u] = c[2 * n + k];
+                a3[u] = c[3 * n + k];
+                a4[u] = c[4 * n + k];
+                bk[u] = b[k];
+                wk[u] = w[k];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (kk[u] < 0) continue;
+            const float o = xc[u];
+            float y = a0[u] * o;
+            if (LAP) {
+                y = fmaf(a1[u], xw[u] - o, y);
+                y = fmaf(a2[u], xe[u] - o, y);
+                y = fmaf(a3[u], xn[u] - o, y);
+                y = fmaf(a4[u], xs[u] - o, y);
+            } else {
+                y = fmaf(a1[u], xw[u], y);
+                y = fmaf(a2[u], xe[u], y);
+                y = fmaf(a3[u], xn[u], y);
+                y = fmaf(a4[u], xs[u], y);
+            }
+            x[kk[u]] = fmaf(wk[u], bk[u] - y, o);
+        }
+    }
+    g.sync();
+}
+
 // ---- stage 1: momentum assembly ------------------------------------------------
-__device__ void b_assemble_momentum(const BInst& I) {
+__device__ __noinline__ void b_assemble_momentum(const Grp& g, const BInst& I) {
     const kc_phys& P = I.P;
     const Dims D = dims_of(P);
     const Solid S{I.solid, D.NYp};
     {
         const int NX = D.nx + 3, NY = D.NYu, n = NX * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.du.q(k), j = k - i * NY;
             double c[5], b;
             u_row(P, I.K, D, S, I.u, I.v, I.p, I.u0, i, j, c, b);
@@ -184,7 +296,7 @@ __device__ void b_assemble_momentum(const BInst& I) {
     }
     {
         const int NX = D.nx + 2, NY = D.NYv, n = NX * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.dv.q(k), j = k - i * NY;
             double c[5], b;
             v_row(P, I.K, D, S, I.u, I.v, I.p, I.v0, i, j, c, b);
@@ -197,26 +309,41 @@ __device__ void b_assemble_momentum(const BInst& I) {
             I.bv32[k] = f64_to_f32(b);
         }
     }
-    __syncthreads();
+    g.sync();
 }
 
 // ---- stage 2: a momentum system by FP32 red-black Gauss-Seidel in FP64 refinement ----
 // r32 = b - A x in FP64, returns {||r||^2, ||b||^2}
-__device__ __forceinline__ void b_resid64(const double* c, const double* bvec, const double* x, float* r32, int NX,
+__device__ __forceinline__ void b_resid64(const Grp& g, const double* c, const double* bvec, const double* x, float* r32, int NX,
                                           int NY, Div dy, double (&s)[2]) {
     const int n = NX * NY;
     double rr = 0.0, bb = 0.0;
-    for (int k = threadIdx.x; k < n; k += kBT) {
-        const int i = dy.q(k), j = k - i * NY;
-        const double bk = bvec[k];
-        const double r = bk - row_std<double, double>(c, n, x, NX, NY, k, i, j);
-        r32[k] = f64_to_f32(r);
-        rr = fma(r, r, rr);
-        bb = fma(bk, bk, bb);
+    constexpr int U = 2;   // cells in flight per thread: loads before stores
+    for (int k0 = g.tid; k0 < n; k0 += g.nt * U) {
+        double bk[U], y[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * g.nt;
+            if (k < n) {
+                const int i = dy.q(k), j = k - i * NY;
+                bk[u] = bvec[k];
+                y[u] = row_std<double, double>(c, n, x, NX, NY, k, i, j);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + u * g.nt;
+            if (k < n) {
+                const double r = bk[u] - y[u];
+                r32[k] = f64_to_f32(r);
+                rr = fma(r, r, rr);
+                bb = fma(bk[u], bk[u], bb);
+            }
+        }
     }
     s[0] = rr;
     s[1] = bb;
-    bsum<2>(s);
+    bsum<2>(g, s);
 }
 
 // status of a refinement pass over {||r||^2, ||b||^2}, as refined_core in kc_solver.cu:
@@ -245,13 +372,13 @@ struct Refine {
     }
 };
 
-__device__ void b_gs_refined(const double* c, const double* bvec, const float* c32, double* x, int NX, int NY, Div dy,
-                             const BInst& I, long long* iters, int* status_out) {
+__device__ __noinline__ void b_gs_refined(const Grp& g, const double* c, const double* bvec, const float* c32, double* x, int NX, int NY, Div dy,
+                             Div dh, const BInst& I, long long* iters, int* status_out) {
     const int n = NX * NY;
     float* gw = I.gw;
     float* r = I.r32;
     float* d = I.d32;
-    for (int k = threadIdx.x; k < n; k += kBT) {
+    for (int k = g.tid; k < n; k += g.nt) {
         const float a = c32[k];
         gw[k] = a != 0.f ? 1.f / a : 0.f;
     }
@@ -260,12 +387,12 @@ __device__ void b_gs_refined(const double* c, const double* bvec, const float* c
     long long total = 0;
     for (int it = 0; it <= kBMaxRefine; ++it) {
         double s[2];
-        b_resid64(c, bvec, x, r, NX, NY, dy, s);   // (its barrier also publishes gw and the last x)
+        b_resid64(g, c, bvec, x, r, NX, NY, dy, s);   // (its barrier also publishes gw and the last x)
         bool undo = false;
         if (R.check(it, s, &status, &undo)) {
             if (undo) {
-                for (int k = threadIdx.x; k < n; k += kBT) x[k] -= (double)d[k];
-                __syncthreads();
+                for (int k = g.tid; k < n; k += g.nt) x[k] -= (double)d[k];
+                g.sync();
             }
             break;
         }
@@ -284,78 +411,69 @@ __device__ void b_gs_refined(const double* c, const double* bvec, const float* c
         R.best = fmin(R.best, R.rel);
         if (it == kBMaxRefine || total >= kBMomentumSweeps) break;
         // kBGsSweeps red-black sweeps of A32 d = r from d = 0 (red first)
-        for (int k = threadIdx.x; k < n; k += kBT) {   // the first (red) half-sweep from d = 0
+        for (int k = g.tid; k < n; k += g.nt) {   // the first (red) half-sweep from d = 0
             const int i = dy.q(k), j = k - i * NY;
             d[k] = ((i + j) & 1) == 0 ? gw[k] * r[k] : 0.f;
         }
-        __syncthreads();
-        for (int h = 1; h < 2 * kBGsSweeps; ++h) {
-            const int col = h & 1;
-            for (int k = threadIdx.x; k < n; k += kBT) {
-                const int i = dy.q(k), j = k - i * NY;
-                if (((i + j) & 1) != col) continue;
-                const float y = row_std<float, float>(c32, n, d, NX, NY, k, i, j);
-                d[k] = fmaf(gw[k], r[k] - y, d[k]);
-            }
-            __syncthreads();
-        }
+        g.sync();
+        for (int h = 1; h < 2 * kBGsSweeps; ++h) hs_sweep<false, 2>(g, c32, r, gw, d, NX, NY, dh, h & 1);
         total += kBGsSweeps;
         int bad = 0;
-        for (int k = threadIdx.x; k < n; k += kBT) bad |= !isfinite(d[k]);
-        bad = __syncthreads_or(bad);
+        for (int k = g.tid; k < n; k += g.nt) bad |= !isfinite(d[k]);
+        bad = g.any(bad);
         if (bad) {
             status = KC_NONFINITE;
             break;
         }
-        for (int k = threadIdx.x; k < n; k += kBT) x[k] += (double)d[k];
-        __syncthreads();   // the next residual reads x's neighbours
+        for (int k = g.tid; k < n; k += g.nt) x[k] += (double)d[k];
+        g.sync();   // the next residual reads x's neighbours
         R.applied = true;
     }
-    __syncthreads();
+    g.sync();
     *iters += total;
     *status_out = status;
 }
 
 // ---- stage 3: under-relaxation and the outlet column (k_relax, k_outlet_conserve) ----
-__device__ void b_relax_outlet(const BInst& I) {
+__device__ __noinline__ void b_relax_outlet(const Grp& g, const BInst& I) {
     const kc_phys& P = I.P;
     const Dims D = dims_of(P);
     const Solid S{I.solid, D.NYp};
     const double a = P.alpha_m;
     {
         const int NY = D.NYu, n = (D.nx + 3) * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.du.q(k), j = k - i * NY;
             if (unk_u(P, S, i, j)) I.u[k] = a * I.um[k] + I.K.one_m_am * I.u[k];
         }
     }
     {
         const int NY = D.NYv, n = (D.nx + 2) * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.dv.q(k), j = k - i * NY;
             if (unk_v(P, S, i, j)) I.v[k] = a * I.vm[k] + I.K.one_m_am * I.v[k];
         }
     }
-    __syncthreads();
+    g.sync();
     // outlet: zero gradient, then the outflow rescaled to the inflow
     double acc[2] = {0.0, 0.0};
-    for (int j = 1 + threadIdx.x; j <= D.ny; j += kBT) {
+    for (int j = 1 + g.tid; j <= D.ny; j += g.nt) {
         const double w = I.u[(long long)D.nx * D.NYu + j];
         I.u[(long long)(D.nx + 1) * D.NYu + j] = w;
         acc[0] += I.u[(long long)1 * D.NYu + j];
         acc[1] += w;
     }
-    bsum<2>(acc);
+    bsum<2>(g, acc);
     const double coef = acc[0] / acc[1];
-    for (int j = 1 + threadIdx.x; j <= D.ny; j += kBT) {
+    for (int j = 1 + g.tid; j <= D.ny; j += g.nt) {
         double* o = I.u + (long long)(D.nx + 1) * D.NYu + j;
         *o = coef * *o;
     }
-    __syncthreads();
+    g.sync();
 }
 
 // ---- stage 4: p' rows and the mass residual (the channel branch of k_assemble_pcorr) ----
-__device__ double b_assemble_pcorr(const BInst& I) {
+__device__ __noinline__ double b_assemble_pcorr(const Grp& g, const BInst& I) {
     const kc_phys& P = I.P;
     const Dims D = dims_of(P);
     const Solid S{I.solid, D.NYp};
@@ -365,7 +483,7 @@ __device__ double b_assemble_pcorr(const BInst& I) {
     const double* u = I.u;
     const double* v = I.v;
     double mx = 0.0;
-    for (int k = threadIdx.x; k < n; k += kBT) {
+    for (int k = g.tid; k < n; k += g.nt) {
         const int i = I.dp.q(k), j = k - i * NY;
         double c[5] = {0, 0, 0, 0, 0}, b = 0.0, xs = 0.0;
         if (i >= 1 && i <= nx && j >= 1 && j <= ny) {
@@ -402,30 +520,30 @@ __device__ double b_assemble_pcorr(const BInst& I) {
         for (int q = 1; q < 5; ++q) I.cp32[(long long)q * n + k] = f64_to_f32(c[q]);
         I.bp32[k] = f64_to_f32(b);
     }
-    return bmax(mx);   // (its barriers publish the rows)
+    return bmax(g, mx);   // (its barriers publish the rows)
 }
 
 // ---- stage 5: the p' solve --------------------------------------------------------
 // hierarchy: smoother weights and isolation flags of level 0, then the Galerkin
 // coarse rows level by level (k_mg_diag0, k_mg_coarsen), then the coarsest inverse
-__device__ void b_mg_setup(const BInst& I, float* inv, int* inv_bad) {
+__device__ __noinline__ void b_mg_setup(const Grp& g, const BInst& I, float* inv, int* inv_bad) {
     {
         const BLvl& L = I.lv[0];
         const int n = L.NX * L.NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const float w = L.c[n + k], ea = L.c[2 * n + k], no = L.c[3 * n + k], so = L.c[4 * n + k];
             const float d = L.c[k] - (w + ea + no + so);
             const bool linked = w != 0.f || ea != 0.f || no != 0.f || so != 0.f;
             L.iso[k] = linked ? 0 : 1;
             L.w[k] = d == 0.f ? 0.f : (linked ? L.omega / d : 1.f / d);
         }
-        __syncthreads();
+        g.sync();
     }
     for (int l = 0; l + 1 < I.levels; ++l) {
         const BLvl& F = I.lv[l];
         const BLvl& Q = I.lv[l + 1];
         const int nf = F.NX * F.NY, nc = Q.NX * Q.NY;
-        for (int kc = threadIdx.x; kc < nc; kc += kBT) {
+        for (int kc = g.tid; kc < nc; kc += g.nt) {
             const int Ic = Q.dy.q(kc), Jc = kc - Ic * Q.NY;
             float rs = 0.f, aW = 0.f, aE = 0.f, aN = 0.f, aS = 0.f;
             for (int di = 0; di < 2; ++di) {
@@ -459,14 +577,14 @@ __device__ void b_mg_setup(const BInst& I, float* inv, int* inv_bad) {
             Q.iso[kc] = linked ? 0 : 1;
             Q.w[kc] = d == 0.f ? 0.f : (linked ? Q.omega / d : 1.f / d);
         }
-        __syncthreads();
+        g.sync();
     }
     // coarsest: Gauss-Jordan inversion in shared memory, no pivoting (the Galerkin operator of
     // the symmetric p' rows with the outlet folded into the row sums is positive definite; a row
     // without coupled children gets a unit diagonal and a zero right-hand side)
     const BLvl& C = I.lv[I.levels - 1];
     const int nc = C.NX * C.NY;
-    for (int e = threadIdx.x; e < nc * nc; e += kBT) {
+    for (int e = g.tid; e < nc * nc; e += g.nt) {
         const int i = e / nc, j = e - i * nc;
         const float w = C.c[nc + i], ea = C.c[2 * nc + i], no = C.c[3 * nc + i], so = C.c[4 * nc + i];
         float d = C.c[i] - (((w + ea) + no) + so);
@@ -480,63 +598,59 @@ __device__ void b_mg_setup(const BInst& I, float* inv, int* inv_bad) {
         else if (j == i - 1 && jr >= 1) val = so;
         inv[e] = val;
     }
-    __shared__ float rowp[kBCoarse], colp[kBCoarse];
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
+    __shared__ float rowp_s[kBGroups][kBCoarse], colp_s[kBGroups][kBCoarse];
+    __shared__ int bad_s[kBGroups];
+    float* rowp = rowp_s[g.gi];
+    float* colp = colp_s[g.gi];
+    int& bad = bad_s[g.gi];
+    if (g.tid == 0) bad = 0;
+    g.sync();
     for (int p = 0; p < nc; ++p) {
-        if (threadIdx.x < nc) {
-            rowp[threadIdx.x] = inv[p * nc + threadIdx.x];
-            colp[threadIdx.x] = inv[threadIdx.x * nc + p];
+        if (g.tid < nc) {
+            rowp[g.tid] = inv[p * nc + g.tid];
+            colp[g.tid] = inv[g.tid * nc + p];
         }
-        __syncthreads();
+        g.sync();
         const float piv = rowp[p];
         if (!(piv > 0.f) || !isfinite(piv)) {   // uniform: every thread reads the same pivot
-            if (threadIdx.x == 0) bad = 1;
+            if (g.tid == 0) bad = 1;
             break;
         }
         const float ip = 1.f / piv;
-        for (int e = threadIdx.x; e < nc * nc; e += kBT) {
+        for (int e = g.tid; e < nc * nc; e += g.nt) {
             const int i = e / nc, j = e - i * nc;
             const float sp = j == p ? ip : rowp[j] * ip;
             inv[e] = i == p ? sp : (j == p ? -colp[i] * ip : fmaf(-colp[i], sp, inv[e]));
         }
-        __syncthreads();
+        g.sync();
     }
-    __syncthreads();
+    g.sync();
     *inv_bad = bad;
-    __syncthreads();
+    g.sync();
 }
 
 // one V-cycle z = M r on the hierarchy (level 0: b = r, x = z), kc_mg.cu's cycle:
 // down: red start x = W b, 2 nu - 1 half-sweeps (black, red, ...), restriction of the
 // residual over coupled cells; coarsest: x = A^-1 b; up: prolongation onto coupled cells
 // scaled by alpha, 2 nu half-sweeps (black, red, ...)
-__device__ __forceinline__ void b_half_sweep(const BLvl& L, int col) {
-    const int n = L.NX * L.NY;
-    for (int k = threadIdx.x; k < n; k += kBT) {
-        const int i = L.dy.q(k), j = k - i * L.NY;
-        if (((i + j) & 1) != col) continue;
-        const float r = L.b[k] - row_lap(L.c, n, L.x, L.NX, L.NY, k, i, j);
-        L.x[k] = fmaf(L.w[k], r, L.x[k]);
-    }
-    __syncthreads();
+__device__ __forceinline__ void b_half_sweep(const Grp& g, const BLvl& L, int col) {
+    hs_sweep<true, 2>(g, L.c, L.b, L.w, L.x, L.NX, L.NY, L.dh, col);
 }
 
-__device__ void b_vcycle(const BInst& I, const float* inv, int inv_bad) {
+__device__ __noinline__ void b_vcycle(const Grp& g, const BInst& I, const float* inv, int inv_bad) {
     const int Lc = I.levels - 1;
     for (int l = 0; l < Lc; ++l) {
         const BLvl& L = I.lv[l];
         const BLvl& Q = I.lv[l + 1];
         const int n = L.NX * L.NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = L.dy.q(k), j = k - i * L.NY;
             L.x[k] = ((i + j) & 1) == 0 ? L.w[k] * L.b[k] : 0.f;
         }
-        __syncthreads();
-        for (int h = 1; h < 2 * L.nu; ++h) b_half_sweep(L, h & 1);
+        g.sync();
+        for (int h = 1; h < 2 * L.nu; ++h) b_half_sweep(g, L, h & 1);
         const int nc = Q.NX * Q.NY;
-        for (int kc = threadIdx.x; kc < nc; kc += kBT) {
+        for (int kc = g.tid; kc < nc; kc += g.nt) {
             const int Ic = Q.dy.q(kc), Jc = kc - Ic * Q.NY;
             float s = 0.f;
             for (int di = 0; di < 2; ++di) {
@@ -552,35 +666,35 @@ __device__ void b_vcycle(const BInst& I, const float* inv, int inv_bad) {
             }
             Q.b[kc] = s;
         }
-        __syncthreads();
+        g.sync();
     }
     {
         const BLvl& C = I.lv[Lc];
         const int n = C.NX * C.NY;
         if (!inv_bad) {
-            const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-            for (int i = wp; i < n; i += kBWarps) {
+            const int lane = g.tid & 31, wp = g.tid >> 5;
+            for (int i = wp; i < n; i += g.warps()) {
                 float s = 0.f;
                 for (int j = lane; j < n; j += 32) s = fmaf(inv[i * n + j], C.b[j], s);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFull, s, o);
                 if (lane == 0) C.x[i] = s;
             }
-            __syncthreads();
+            g.sync();
         } else {   // Jacobi sweeps (the inverse failed)
-            for (int k = threadIdx.x; k < n; k += kBT) C.x[k] = C.w[k] * C.b[k];
-            __syncthreads();
+            for (int k = g.tid; k < n; k += g.nt) C.x[k] = C.w[k] * C.b[k];
+            g.sync();
             for (int sw = 1; sw < kBCoarseFallbackSweeps; ++sw) {
                 float xn[2] = {0.f, 0.f};
                 int q = 0;
-                for (int k = threadIdx.x; k < n; k += kBT, ++q) {
+                for (int k = g.tid; k < n; k += g.nt, ++q) {
                     const int i = C.dy.q(k), j = k - i * C.NY;
                     xn[q & 1] = C.x[k] + C.w[k] * (C.b[k] - row_lap(C.c, n, C.x, C.NX, C.NY, k, i, j));
                 }
-                __syncthreads();
+                g.sync();
                 q = 0;
-                for (int k = threadIdx.x; k < n; k += kBT, ++q) C.x[k] = xn[q & 1];
-                __syncthreads();
+                for (int k = g.tid; k < n; k += g.nt, ++q) C.x[k] = xn[q & 1];
+                g.sync();
             }
         }
     }
@@ -588,19 +702,20 @@ __device__ void b_vcycle(const BInst& I, const float* inv, int inv_bad) {
         const BLvl& L = I.lv[l];
         const BLvl& Q = I.lv[l + 1];
         const int n = L.NX * L.NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             if (L.iso[k]) continue;
             const int i = L.dy.q(k), j = k - i * L.NY;
             L.x[k] = fmaf(L.alpha, Q.x[(i >> 1) * Q.NY + (j >> 1)], L.x[k]);
         }
-        __syncthreads();
-        for (int h = 1; h <= 2 * L.nu; ++h) b_half_sweep(L, h & 1);
+        g.sync();
+        for (int h = 1; h <= 2 * L.nu; ++h) b_half_sweep(g, L, h & 1);
     }
 }
 
 // multigrid-preconditioned CG on the FP32 p' rows: A d = r from d = 0 to ||r_k|| <= eps_in ||r_0||
-// (r is overwritten); FP64 inner products.  Returns the iterations, *status.
-__device__ int b_pcg(const BInst& I, double eps_in, const float* inv, int inv_bad, int* status) {
+// (r is overwritten); inner products of the FP32 vectors in double-float accumulation (exact
+// products, about 48-bit sums), the scalars in FP64.  Returns the iterations, *status.
+__device__ __noinline__ int b_pcg(const Grp& g, const BInst& I, double eps_in, const float* inv, int inv_bad, int* status) {
     const BLvl& L0 = I.lv[0];
     const int NX = L0.NX, NY = L0.NY, n = NX * NY;
     const float* c = L0.c;
@@ -610,26 +725,25 @@ __device__ int b_pcg(const BInst& I, double eps_in, const float* inv, int inv_ba
     float* q = I.cq;
     float* d = I.cd;
     double s1[1];
-    double rr0 = 0.0;
-    for (int k = threadIdx.x; k < n; k += kBT) {
+    Acc<float> a1[1];
+    for (int k = g.tid; k < n; k += g.nt) {
         d[k] = 0.f;
-        rr0 = fma((double)r[k], (double)r[k], rr0);
+        a1[0].add(r[k], r[k]);
     }
-    s1[0] = rr0;
-    bsum<1>(s1);
-    rr0 = s1[0];
+    bsum_df<1>(g, a1, s1);
+    const double rr0 = s1[0];
     *status = KC_OK;
     if (rr0 == 0.0) return 0;
     const double stop2 = eps_in * eps_in * rr0;
-    b_vcycle(I, inv, inv_bad);
-    double rho = 0.0;
-    for (int k = threadIdx.x; k < n; k += kBT) {
-        p[k] = z[k];
-        rho = fma((double)r[k], (double)z[k], rho);
+    b_vcycle(g, I, inv, inv_bad);
+    a1[0] = Acc<float>{};
+    for (int k = g.tid; k < n; k += g.nt) {
+        const float zk = z[k];
+        p[k] = zk;
+        a1[0].add(r[k], zk);
     }
-    s1[0] = rho;
-    bsum<1>(s1);
-    rho = s1[0];
+    bsum_df<1>(g, a1, s1);
+    double rho = s1[0];
     int it = 0;
     *status = KC_MAXITER;
     while (it < kBMaxCg) {
@@ -637,32 +751,61 @@ __device__ int b_pcg(const BInst& I, double eps_in, const float* inv, int inv_ba
             *status = isfinite(rho) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
             break;
         }
-        double pq = 0.0;
-        for (int k = threadIdx.x; k < n; k += kBT) {
-            const int i = L0.dy.q(k), j = k - i * NY;
-            const float y = row_lap(c, n, p, NX, NY, k, i, j);
-            q[k] = y;
-            pq = fma((double)p[k], (double)y, pq);
+        a1[0] = Acc<float>{};
+        for (int k0 = g.tid; k0 < n; k0 += g.nt * 2) {
+            float y[2], pk[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) {
+                    const int i = L0.dy.q(k), j = k - i * NY;
+                    y[u] = row_lap(c, n, p, NX, NY, k, i, j);
+                    pk[u] = p[k];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) {
+                    q[k] = y[u];
+                    a1[0].add(pk[u], y[u]);
+                }
+            }
         }
-        s1[0] = pq;
-        bsum<1>(s1);
-        pq = s1[0];
+        bsum_df<1>(g, a1, s1);
+        const double pq = s1[0];
         if (!(pq > 0.0)) {
             *status = isfinite(pq) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
             break;
         }
         const double alpha = rho / pq;
         const float af = (float)alpha;
-        double rr = 0.0;
-        for (int k = threadIdx.x; k < n; k += kBT) {
-            d[k] = fmaf(af, p[k], d[k]);
-            const float rn = fmaf(-af, q[k], r[k]);
-            r[k] = rn;
-            rr = fma((double)rn, (double)rn, rr);
+        a1[0] = Acc<float>{};
+        for (int k0 = g.tid; k0 < n; k0 += g.nt * 4) {
+            float pk[4], qk[4], rk[4], dk[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) {
+                    pk[u] = p[k];
+                    qk[u] = q[k];
+                    rk[u] = r[k];
+                    dk[u] = d[k];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) {
+                    d[k] = fmaf(af, pk[u], dk[u]);
+                    const float rn = fmaf(-af, qk[u], rk[u]);
+                    r[k] = rn;
+                    a1[0].add(rn, rn);
+                }
+            }
         }
-        s1[0] = rr;
-        bsum<1>(s1);
-        rr = s1[0];
+        bsum_df<1>(g, a1, s1);
+        const double rr = s1[0];
         ++it;
         if (!isfinite(rr)) {
             *status = KC_NONFINITE;
@@ -672,38 +815,52 @@ __device__ int b_pcg(const BInst& I, double eps_in, const float* inv, int inv_ba
             *status = KC_OK;
             break;
         }
-        b_vcycle(I, inv, inv_bad);
-        double rz = 0.0;
-        for (int k = threadIdx.x; k < n; k += kBT) rz = fma((double)r[k], (double)z[k], rz);
-        s1[0] = rz;
-        bsum<1>(s1);
+        b_vcycle(g, I, inv, inv_bad);
+        a1[0] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) a1[0].add(r[k], z[k]);
+        bsum_df<1>(g, a1, s1);
         const float beta = (float)(s1[0] / rho);
         rho = s1[0];
-        for (int k = threadIdx.x; k < n; k += kBT) p[k] = fmaf(beta, p[k], z[k]);
-        __syncthreads();
+        for (int k0 = g.tid; k0 < n; k0 += g.nt * 4) {
+            float pk[4], zk[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) {
+                    pk[u] = p[k];
+                    zk[u] = z[k];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = k0 + u * g.nt;
+                if (k < n) p[k] = fmaf(beta, pk[u], zk[u]);
+            }
+        }
+        g.sync();
     }
     return it;
 }
 
 // p' = 0, then FP32 CG passes on the FP64 residual until ||b - A p'|| / ||b|| < eps
-__device__ void b_pcorr_solve(const BInst& I, float* inv, int* inv_bad_s, long long* iters, int* status_out) {
+__device__ __noinline__ void b_pcorr_solve(const Grp& g, const BInst& I, float* inv, int* inv_bad_s, long long* iters, int* status_out) {
     const Dims D = dims_of(I.P);
     const int NX = D.nx + 2, NY = D.NYp, n = NX * NY;
     double* x = I.pc;
-    for (int k = threadIdx.x; k < n; k += kBT) x[k] = 0.0;
-    b_mg_setup(I, inv, inv_bad_s);
+    for (int k = g.tid; k < n; k += g.nt) x[k] = 0.0;
+    b_mg_setup(g, I, inv, inv_bad_s);
     const int inv_bad = *inv_bad_s;
     Refine R;
     int status = KC_MAXITER;
     long long total = 0;
     for (int it = 0; it <= kBMaxRefine; ++it) {
         double s[2];
-        b_resid64(I.cp, I.bp, x, I.cr, NX, NY, I.dp, s);
+        b_resid64(g, I.cp, I.bp, x, I.cr, NX, NY, I.dp, s);
         bool undo = false;
         if (R.check(it, s, &status, &undo)) {
             if (undo) {
-                for (int k = threadIdx.x; k < n; k += kBT) x[k] -= (double)I.cd[k];
-                __syncthreads();
+                for (int k = g.tid; k < n; k += g.nt) x[k] -= (double)I.cd[k];
+                g.sync();
             }
             break;
         }
@@ -722,27 +879,27 @@ __device__ void b_pcorr_solve(const BInst& I, float* inv, int* inv_bad_s, long l
         R.best = fmin(R.best, R.rel);
         if (it == kBMaxRefine) break;
         int st = KC_OK;
-        const int k_it = b_pcg(I, fmax(I.eps_inner_p, 0.5 * I.eps / R.rel), inv, inv_bad, &st);
+        const int k_it = b_pcg(g, I, fmax(I.eps_inner_p, 0.5 * I.eps / R.rel), inv, inv_bad, &st);
         total += k_it;
         int bad = 0;
-        for (int k = threadIdx.x; k < n; k += kBT) bad |= !isfinite(I.cd[k]);
-        bad = __syncthreads_or(bad);
+        for (int k = g.tid; k < n; k += g.nt) bad |= !isfinite(I.cd[k]);
+        bad = g.any(bad);
         if (!bad)
-            for (int k = threadIdx.x; k < n; k += kBT) x[k] += (double)I.cd[k];
-        __syncthreads();   // the next residual reads x's neighbours
+            for (int k = g.tid; k < n; k += g.nt) x[k] += (double)I.cd[k];
+        g.sync();   // the next residual reads x's neighbours
         R.applied = !bad;
         if ((st != KC_OK && k_it == 0) || bad) {
             status = bad ? KC_NONFINITE : st;
             break;
         }
     }
-    __syncthreads();
+    g.sync();
     *iters += total;
     *status_out = status;
 }
 
 // ---- stage 6: corrections (the channel branch of k_correct) ----------------------
-__device__ void b_correct(const BInst& I) {
+__device__ __noinline__ void b_correct(const Grp& g, const BInst& I) {
     const kc_phys& P = I.P;
     const Dims D = dims_of(P);
     const Solid S{I.solid, D.NYp};
@@ -752,7 +909,7 @@ __device__ void b_correct(const BInst& I) {
 #define BPC_(a, bb) pc[(long long)(a) * D.NYp + (bb)]
     {
         const int NY = D.NYu, n = (nx + 3) * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.du.q(k), j = k - i * NY;
             if (unk_u(P, S, i, j)) {
                 I.u[k] = I.u[k] + au * (BPC_(i - 1, j) - BPC_(i, j)) * dy / I.cu[k];
@@ -763,27 +920,24 @@ __device__ void b_correct(const BInst& I) {
     }
     {
         const int NY = D.NYv, n = (nx + 2) * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.dv.q(k), j = k - i * NY;
             if (unk_v(P, S, i, j)) I.v[k] = I.v[k] + au * (BPC_(i, j - 1) - BPC_(i, j)) * dx / I.cv[k];
         }
     }
     {
         const int NY = D.NYp, n = (nx + 2) * NY;
-        for (int k = threadIdx.x; k < n; k += kBT) {
+        for (int k = g.tid; k < n; k += g.nt) {
             const int i = I.dp.q(k), j = k - i * NY;
             if (i >= 1 && i <= nx && j >= 1 && j <= ny && !S.cell(i, j)) I.p[k] = I.p[k] + ap * pc[k];
         }
     }
 #undef BPC_
-    __syncthreads();
+    g.sync();
 }
 
-// ---- the kernel: block b advances instance b by `steps` time steps ------------------
-__global__ void __launch_bounds__(kBT, 2) k_batch_steps(const BInst* __restrict__ insts, int steps) {
-    const BInst& I = insts[blockIdx.x];
-    __shared__ float inv[kBCoarse * kBCoarse];
-    __shared__ int inv_bad;
+// ---- one instance's time steps --------------------------------------------------
+__device__ __noinline__ void b_run(const Grp& g, const BInst& I, int steps, float* inv, int* inv_bad) {
     const Dims D = dims_of(I.P);
     kc_channel_stats tot{};
     kc_channel_stats S{};
@@ -791,14 +945,14 @@ __global__ void __launch_bounds__(kBT, 2) k_batch_steps(const BInst* __restrict_
         S = kc_channel_stats{};
         double mass = 0.0;
         for (int outer = 0; outer < I.max_outer; ++outer) {
-            b_assemble_momentum(I);
+            b_assemble_momentum(g, I);
             int su = KC_OK, sv = KC_OK, sp = KC_OK;
-            b_gs_refined(I.cu, I.bu, I.cu32, I.um, D.nx + 3, D.NYu, I.du, I, &S.it_u, &su);
-            b_gs_refined(I.cv, I.bv, I.cv32, I.vm, D.nx + 2, D.NYv, I.dv, I, &S.it_v, &sv);
-            b_relax_outlet(I);
-            mass = b_assemble_pcorr(I);
-            b_pcorr_solve(I, inv, &inv_bad, &S.it_p, &sp);
-            b_correct(I);
+            b_gs_refined(g, I.cu, I.bu, I.cu32, I.um, D.nx + 3, D.NYu, I.du, I.dhu, I, &S.it_u, &su);
+            b_gs_refined(g, I.cv, I.bv, I.cv32, I.vm, D.nx + 2, D.NYv, I.dv, I.dhv, I, &S.it_v, &sv);
+            b_relax_outlet(g, I);
+            mass = b_assemble_pcorr(g, I);
+            b_pcorr_solve(g, I, inv, inv_bad, &S.it_p, &sp);
+            b_correct(g, I);
             S.outer += 1;
             const bool nonfinite = su == KC_NONFINITE || sv == KC_NONFINITE || sp == KC_NONFINITE;
             if (nonfinite) S.status = KC_NONFINITE;
@@ -811,12 +965,11 @@ __global__ void __launch_bounds__(kBT, 2) k_batch_steps(const BInst* __restrict_
             }
             if (mass <= I.mass_tol) break;
         }
-        // time_forward
-        {
+        {   // time_forward
             const int nu = (D.nx + 3) * D.NYu, nv = (D.nx + 2) * D.NYv;
-            for (int k = threadIdx.x; k < nu; k += kBT) I.u0[k] = I.u[k];
-            for (int k = threadIdx.x; k < nv; k += kBT) I.v0[k] = I.v[k];
-            __syncthreads();
+            for (int k = g.tid; k < nu; k += g.nt) I.u0[k] = I.u[k];
+            for (int k = g.tid; k < nv; k += g.nt) I.v0[k] = I.v[k];
+            g.sync();
         }
         tot.outer += S.outer;
         tot.fallbacks += S.fallbacks;
@@ -827,9 +980,30 @@ __global__ void __launch_bounds__(kBT, 2) k_batch_steps(const BInst* __restrict_
         if (S.status != KC_OK && tot.status == KC_OK) tot.status = S.status;
         if (S.status == KC_NONFINITE) break;
     }
-    if (threadIdx.x == 0) {
+    if (g.tid == 0) {
         *I.last = S;
         *I.total = tot;
+    }
+}
+
+// ---- the kernel: block b runs the instances slots[first_b .. first_b + count_b) ------
+// (one of 1024 threads, or up to four of 256), each on its own threads and barrier
+__global__ void __launch_bounds__(kBBlock, 1)
+    k_batch_steps(const BInst* __restrict__ insts, const int* __restrict__ slots, const int2* __restrict__ blocks,
+                  int steps) {
+    extern __shared__ __align__(16) float b_dyn[];   // the coarsest inverse of each instance of the block
+    __shared__ int inv_bad[kBGroups];
+    const int2 bl = blocks[blockIdx.x];
+    int base = 0;
+    for (int q = 0; q < bl.y; ++q) {
+        const int id = slots[bl.x + q];
+        const int nt = insts[id].nt;
+        if ((int)threadIdx.x < base + nt) {
+            const Grp g{(int)threadIdx.x - base, nt, q};
+            b_run(g, insts[id], steps, b_dyn + q * kBCoarse * kBCoarse, &inv_bad[q]);
+            return;
+        }
+        base += nt;
     }
 }
 
@@ -875,8 +1049,15 @@ size_t inst_bytes(const BSizes& z) {
     }
     return o;
 }
+// descriptors, the two statistics arrays, the instance order and the block table
 size_t head_bytes(int n) {
-    return align256((size_t)n * sizeof(BInst)) + 2 * align256((size_t)n * sizeof(kc_channel_stats));
+    return align256((size_t)n * sizeof(BInst)) + 2 * align256((size_t)n * sizeof(kc_channel_stats)) +
+           align256((size_t)n * sizeof(int)) + align256((size_t)n * sizeof(int2));
+}
+// threads of an instance: a whole block for the large ones, a quarter block for the rest -- a
+// function of the instance alone, so an instance computes the same in any batch
+int inst_threads(const kc_channel* c) {
+    return (long long)(c->phys.nx + 2) * (c->phys.ny + 2) >= kBBigCells ? kBBlock : kBBlock / kBGroups;
 }
 
 int check_channel(const kc_channel* c, int k) {
@@ -939,6 +1120,8 @@ int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void*
     kc_channel_stats* d_last = (kc_channel_stats*)(base + align256((size_t)n * sizeof(BInst)));
     kc_channel_stats* d_total =
         (kc_channel_stats*)((char*)d_last + align256((size_t)n * sizeof(kc_channel_stats)));
+    int* d_slots = (int*)((char*)d_total + align256((size_t)n * sizeof(kc_channel_stats)));
+    int2* d_blocks = (int2*)((char*)d_slots + align256((size_t)n * sizeof(int)));
     char* o = base + head_bytes(n);
     std::vector<BInst> h(n);
     for (int k = 0; k < n; ++k) {
@@ -994,6 +1177,7 @@ int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void*
             L.NX = z.NX[l];
             L.NY = z.NY[l];
             L.dy = div_of(L.NY);
+            L.dh = div_of((L.NY + 1) / 2);
             const size_t nl = (size_t)L.NX * L.NY;
             if (l == 0) {
                 L.c = c->coef_p32;
@@ -1016,14 +1200,38 @@ int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void*
         I.du = div_of(c->phys.ny + 2);
         I.dv = div_of(c->phys.ny + 3);
         I.dp = div_of(c->phys.ny + 2);
+        I.dhu = div_of((c->phys.ny + 3) / 2);
+        I.dhv = div_of((c->phys.ny + 4) / 2);
+        I.nt = inst_threads(c);
         I.last = d_last + k;
         I.total = d_total + k;
     }
+    // blocks: each large instance alone, then the others four to a block, largest first
+    std::vector<int> order(n);
+    for (int k = 0; k < n; ++k) order[k] = k;
+    auto cells = [&](int k) { return (long long)(chs[k]->phys.nx + 2) * (chs[k]->phys.ny + 2); };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (h[a].nt != h[b].nt) return h[a].nt > h[b].nt;
+        return cells(a) > cells(b);
+    });
+    std::vector<int2> blocks;
+    for (int q = 0; q < n;) {
+        int used = 0, first = q;
+        while (q < n && used + h[order[q]].nt <= kBBlock && q - first < kBGroups) used += h[order[q++]].nt;
+        blocks.push_back(make_int2(first, q - first));
+    }
     if ((size_t)(o - base) > ws_bytes) return set_error("kc_channel_batch_fused: workspace layout overflow"), KC_ERR_WORKSPACE;
     KC_CUDA(cudaMemcpyAsync(d_inst, h.data(), (size_t)n * sizeof(BInst), cudaMemcpyHostToDevice, s));
-    k_batch_steps<<<n, kBT, 0, s>>>(d_inst, steps);
+    KC_CUDA(cudaMemcpyAsync(d_slots, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s));
+    KC_CUDA(cudaMemcpyAsync(d_blocks, blocks.data(), blocks.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    constexpr size_t dyn = (size_t)kBGroups * kBCoarse * kBCoarse * sizeof(float);
+    static bool attr_set = false;   // (set once per process; idempotent)
+    if (!attr_set) {
+        KC_CUDA(cudaFuncSetAttribute(k_batch_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        attr_set = true;
+    }
+    k_batch_steps<<<(unsigned)blocks.size(), kBBlock, dyn, s>>>(d_inst, d_slots, d_blocks, steps);
     KC_LAUNCH_CHECK("k_batch_steps");
-    count_launches(1);
     std::vector<kc_channel_stats> hs(2 * (size_t)n);
     KC_CUDA(cudaMemcpyAsync(hs.data(), d_last, (size_t)n * sizeof(kc_channel_stats), cudaMemcpyDeviceToHost, s));
     KC_CUDA(cudaMemcpyAsync(hs.data() + n, d_total, (size_t)n * sizeof(kc_channel_stats), cudaMemcpyDeviceToHost, s));

@@ -209,6 +209,39 @@ struct ReduceWs {
 };
 constexpr int kReduceMaxBlocks = 4096;
 
+// ---- inner-product accumulators -------------------------------------------------
+// FP64 accumulation, and for FP32 vectors a double-float one: every product
+// split exactly into a float pair (fmaf) and summed in float-pair arithmetic
+// (about 48 bits), all on the FP32 pipe -- GB300 issues FP64 at a small
+// fraction of the FP32 rate.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+};
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+template <>
+struct Acc<float> {
+    DF s{0.f, 0.f};
+    __device__ __forceinline__ void add(float a, float b) {
+        const float p = a * b;
+        const float e = fmaf(a, b, -p);   // a*b == p + e exactly
+        s = df_add(s, DF{p, e});
+    }
+};
+
 // ---- bounded grid barrier for cooperative (persistent) kernels ---------------
 // Blocks meet here between phases.  A wait gives up after kSpinLimit polls,
 // raises err and every block leaves: no wait can run forever.

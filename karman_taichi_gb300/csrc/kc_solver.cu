@@ -134,35 +134,6 @@ struct Scal<float> {
     __device__ static float beta(const SolverState* s) { return __ldcg(&s->beta_f); }
 };
 
-// ---- inner-product accumulators -------------------------------------------------
-template <typename T>
-struct Acc;
-template <>
-struct Acc<double> {
-    double s = 0.0;
-    __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
-};
-struct DF {
-    float hi, lo;
-};
-__device__ __forceinline__ DF df_add(DF a, DF b) {
-    const float s = a.hi + b.hi;
-    const float bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    const float h = s + e;
-    return {h, e - (h - s)};
-}
-template <>
-struct Acc<float> {
-    DF s{0.f, 0.f};
-    __device__ __forceinline__ void add(float a, float b) {
-        const float p = a * b;
-        const float e = fmaf(a, b, -p);   // a*b == p + e exactly
-        s = df_add(s, DF{p, e});
-    }
-};
-
 // Thread 0 publishes the block's partials, fences, and takes a ticket; the
 // last block to arrive gets true (no block ever waits on another).
 __device__ __forceinline__ bool publish_and_arrive(unsigned* ticket, unsigned nb) {
