@@ -736,7 +736,8 @@ def run_batch(args, cfgs=None, workload=None):
                         "outer_per_step": round(outer, 2), "gpu_launches": int(launches),
                         "it_p_per_step": round(float(np.mean([x["it_p"] for x in tot])) / max(1, args.steps), 1),
                         "mass_residual_max": max(x["mass_max"] for x in tot),
-                        "instances_with_unconverged_solves": int(sum(x["unconverged_solves"] > 0 for x in tot)),
+                        "fallbacks": int(sum(x["fallbacks"] for x in tot)),
+                        "instances_with_an_unconverged_solve": int(sum(x["status"] not in (0, 4) for x in tot)),
                         "instances_not_finite": int(sum(x["status"] == 4 for x in tot))}
         else:
             run = b.step_native

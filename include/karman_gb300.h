@@ -618,10 +618,11 @@ int kc_channel_batch_step(const kc_channel* const* chs, int n, void* const* stre
  * instance computes bit for bit what it computes in a batch of one.  ws:
  * kc_channel_batch_fused_ws_bytes(chs, n), 256-byte aligned.  last / total
  * (host arrays of n, nullable): each instance's last step, and the sums over
- * the steps (mass: the largest last-outer mass residual).  In the statistics
- * `fallbacks` counts solves that ended without reaching eps (the launch has
- * no fallback solver).  Blocks until the launch has finished.  The
- * reference's drivers have no batched counterpart. */
+ * the steps (mass: the largest last-outer mass residual).  A momentum solve
+ * whose Gauss-Seidel sweeps miss eps, and a p' solve whose multigrid CG
+ * stalls, continue with FP32 BiCGSTAB in FP64 refinement (counted in
+ * `fallbacks`).  Blocks until the launch has finished.  The reference's
+ * drivers have no batched counterpart. */
 size_t kc_channel_batch_fused_ws_bytes(const kc_channel* const* chs, int n);
 int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void* ws, size_t ws_bytes,
                            kc_channel_stats* last, kc_channel_stats* total, void* stream);

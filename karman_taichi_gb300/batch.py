@@ -153,7 +153,7 @@ class BatchedChannels:
             self.records[k].append([dict(mass=st.mass, it_u=st.it_u, it_v=st.it_v, it_p=st.it_p, outer=st.outer,
                                          status=st.status)])
             self.fused_totals.append(dict(outer=tt.outer, it_u=tt.it_u, it_v=tt.it_v, it_p=tt.it_p,
-                                          mass_max=tt.mass, status=tt.status, unconverged_solves=tt.fallbacks))
+                                          mass_max=tt.mass, status=tt.status, fallbacks=tt.fallbacks))
         return t
 
     def step(self, n_steps=1):

@@ -71,6 +71,7 @@ constexpr long long kBMomentumSweeps = 200;
 constexpr int kBMaxRefine = 30;
 constexpr int kBMaxCg = 1000;            // CG iterations per refinement pass at most
 constexpr int kBCoarseFallbackSweeps = 64;
+constexpr int kBMaxBicg = 4000;          // fallback BiCGSTAB iterations per refinement pass at most
 
 // exact e / d for 0 <= e < 2^32 / d by a multiply-high (m = 0 stands for d = 1)
 struct Div {
@@ -125,6 +126,8 @@ struct BInst {
     double *cu, *bu, *cv, *bv, *cp, *bp;
     float *cu32, *bu32, *cv32, *bv32, *cp32, *bp32;
     float *gw, *r32, *d32;                 // momentum: Gauss-Seidel weights, FP32 residual, correction
+    float *bt[5];                          // fallback BiCGSTAB: r~, p, v, s, t (the larger grid's size)
+    double eps_inner;                      // inner tolerance of the fallback BiCGSTAB passes
     float *cr, *cz, *cpv, *cq, *cd;        // p' CG: r, z, p, q and the correction
     BLvl lv[kBLevels];
     int levels;
@@ -372,8 +375,182 @@ struct Refine {
     }
 };
 
+// ---- the fallback: FP32 BiCGSTAB in FP64 refinement (kc_bicgstab_refined's method) ----
+// y = A32 x on cell k (standard or Laplacian form)
+__device__ __forceinline__ float row32(bool lap, const float* c, int n, const float* x, int NX, int NY, int k, int i,
+                                       int j) {
+    return lap ? row_lap(c, n, x, NX, NY, k, i, j) : row_std<float, float>(c, n, x, NX, NY, k, i, j);
+}
+// A32 d = r from d = 0 to ||r_k|| <= eps_in ||r_0|| (r is overwritten); returns the iterations, *status
+__device__ int b_bicg_inner(const Grp& g, const BInst& I, bool lap, const float* c, int NX, int NY, Div dy, float* r,
+                            float* d, double eps_in, int max_it, int* status) {
+    const int n = NX * NY;
+    float* rt = I.bt[0];
+    float* p = I.bt[1];
+    float* v = I.bt[2];
+    float* sv = I.bt[3];
+    float* t = I.bt[4];
+    double s1[1], s2[2];
+    Acc<float> a1[1], a2[2];
+    for (int k = g.tid; k < n; k += g.nt) {
+        const float rk = r[k];
+        rt[k] = rk;
+        p[k] = 0.f;
+        v[k] = 0.f;
+        d[k] = 0.f;
+        a1[0].add(rk, rk);
+    }
+    bsum_df<1>(g, a1, s1);
+    const double rr0 = s1[0];
+    *status = KC_OK;
+    if (rr0 == 0.0) return 0;
+    const double stop2 = eps_in * eps_in * rr0;
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    int it = 0;
+    *status = KC_MAXITER;
+    while (it < max_it) {
+        a1[0] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) a1[0].add(rt[k], r[k]);
+        bsum_df<1>(g, a1, s1);
+        const double rho_n = s1[0];
+        if (rho_n == 0.0 || !isfinite(rho_n)) {
+            *status = isfinite(rho_n) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            break;
+        }
+        const float beta = (float)((rho_n / rho) * (alpha / omega));
+        const float om = (float)omega;
+        for (int k = g.tid; k < n; k += g.nt) p[k] = fmaf(beta, fmaf(-om, v[k], p[k]), r[k]);
+        g.sync();
+        a1[0] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) {
+            const int i = dy.q(k), j = k - i * NY;
+            const float y = row32(lap, c, n, p, NX, NY, k, i, j);
+            v[k] = y;
+            a1[0].add(rt[k], y);
+        }
+        bsum_df<1>(g, a1, s1);
+        if (s1[0] == 0.0 || !isfinite(s1[0])) {
+            *status = isfinite(s1[0]) ? KC_BREAKDOWN_RHO : KC_NONFINITE;
+            break;
+        }
+        alpha = rho_n / s1[0];
+        const float af = (float)alpha;
+        a1[0] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) {
+            const float sk = fmaf(-af, v[k], r[k]);
+            sv[k] = sk;
+            a1[0].add(sk, sk);
+        }
+        bsum_df<1>(g, a1, s1);
+        ++it;
+        if (s1[0] <= stop2) {   // s is small enough: x += alpha p
+            for (int k = g.tid; k < n; k += g.nt) d[k] = fmaf(af, p[k], d[k]);
+            g.sync();
+            *status = KC_OK;
+            break;
+        }
+        a2[0] = Acc<float>{};
+        a2[1] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) {
+            const int i = dy.q(k), j = k - i * NY;
+            const float y = row32(lap, c, n, sv, NX, NY, k, i, j);
+            t[k] = y;
+            a2[0].add(y, sv[k]);
+            a2[1].add(y, y);
+        }
+        bsum_df<2>(g, a2, s2);
+        if (!(s2[1] > 0.0) || !isfinite(s2[0])) {
+            *status = isfinite(s2[1]) ? KC_BREAKDOWN_OMEGA : KC_NONFINITE;
+            for (int k = g.tid; k < n; k += g.nt) d[k] = fmaf(af, p[k], d[k]);
+            g.sync();
+            break;
+        }
+        omega = s2[0] / s2[1];
+        const float wf = (float)omega;
+        a1[0] = Acc<float>{};
+        for (int k = g.tid; k < n; k += g.nt) {
+            d[k] = fmaf(wf, sv[k], fmaf(af, p[k], d[k]));
+            const float rn = fmaf(-wf, t[k], sv[k]);
+            r[k] = rn;
+            a1[0].add(rn, rn);
+        }
+        bsum_df<1>(g, a1, s1);
+        rho = rho_n;
+        if (!isfinite(s1[0])) {
+            *status = KC_NONFINITE;
+            break;
+        }
+        if (s1[0] <= stop2) {
+            *status = KC_OK;
+            break;
+        }
+        if (omega == 0.0) {
+            *status = KC_BREAKDOWN_OMEGA;
+            break;
+        }
+    }
+    return it;
+}
+
+// FP64 refinement with the FP32 BiCGSTAB inner passes, from the x given; the refinement
+// rules of b_gs_refined
+__device__ __noinline__ void b_bicg_refined(const Grp& g, const BInst& I, bool lap, const double* c,
+                                            const double* bvec, const float* c32, double* x, int NX, int NY, Div dy,
+                                            long long max_iter, long long* iters, int* status_out) {
+    const int n = NX * NY;
+    float* r = I.r32;
+    float* d = I.d32;
+    Refine R;
+    int status = KC_MAXITER;
+    long long total = 0;
+    for (int it = 0; it <= kBMaxRefine; ++it) {
+        double s[2];
+        b_resid64(g, c, bvec, x, r, NX, NY, dy, s);
+        bool undo = false;
+        if (R.check(it, s, &status, &undo)) {
+            if (undo) {
+                for (int k = g.tid; k < n; k += g.nt) x[k] -= (double)d[k];
+                g.sync();
+            }
+            break;
+        }
+        if (R.bb == 0.0 || R.rel < I.eps) {
+            status = KC_OK;
+            break;
+        }
+        if (R.rel >= 0.9 * R.best) {
+            if (++R.stalls >= 2) {
+                status = KC_STALL;
+                break;
+            }
+        } else {
+            R.stalls = 0;
+        }
+        R.best = fmin(R.best, R.rel);
+        if (it == kBMaxRefine || total >= max_iter) break;
+        int st = KC_OK;
+        const int k_it = b_bicg_inner(g, I, lap, c32, NX, NY, dy, r, d, fmax(I.eps_inner, 0.5 * I.eps / R.rel),
+                                      (int)(max_iter - total < kBMaxBicg ? max_iter - total : kBMaxBicg), &st);
+        total += k_it;
+        int bad = 0;
+        for (int k = g.tid; k < n; k += g.nt) bad |= !isfinite(d[k]);
+        bad = g.any(bad);
+        if (!bad)
+            for (int k = g.tid; k < n; k += g.nt) x[k] += (double)d[k];
+        g.sync();
+        R.applied = !bad;
+        if ((st != KC_OK && k_it == 0) || bad) {
+            status = bad ? KC_NONFINITE : st;
+            break;
+        }
+    }
+    g.sync();
+    *iters += total;
+    *status_out = status;
+}
+
 __device__ __noinline__ void b_gs_refined(const Grp& g, const double* c, const double* bvec, const float* c32, double* x, int NX, int NY, Div dy,
-                             Div dh, const BInst& I, long long* iters, int* status_out) {
+                             Div dh, const BInst& I, long long* iters, int* fallbacks, int* status_out) {
     const int n = NX * NY;
     float* gw = I.gw;
     float* r = I.r32;
@@ -431,6 +608,12 @@ __device__ __noinline__ void b_gs_refined(const Grp& g, const double* c, const d
     }
     g.sync();
     *iters += total;
+    if (status != KC_OK && status != KC_NONFINITE) {
+        // the sweeps missed eps: the refined BiCGSTAB takes over from the best iterate, as the
+        // native step does (kc_channel_step's solve_sys)
+        ++*fallbacks;
+        b_bicg_refined(g, I, false, c, bvec, c32, x, NX, NY, dy, 50ll * n, iters, &status);
+    }
     *status_out = status;
 }
 
@@ -947,17 +1130,25 @@ __device__ __noinline__ void b_run(const Grp& g, const BInst& I, int steps, floa
         for (int outer = 0; outer < I.max_outer; ++outer) {
             b_assemble_momentum(g, I);
             int su = KC_OK, sv = KC_OK, sp = KC_OK;
-            b_gs_refined(g, I.cu, I.bu, I.cu32, I.um, D.nx + 3, D.NYu, I.du, I.dhu, I, &S.it_u, &su);
-            b_gs_refined(g, I.cv, I.bv, I.cv32, I.vm, D.nx + 2, D.NYv, I.dv, I.dhv, I, &S.it_v, &sv);
+            b_gs_refined(g, I.cu, I.bu, I.cu32, I.um, D.nx + 3, D.NYu, I.du, I.dhu, I, &S.it_u, &S.fallbacks, &su);
+            b_gs_refined(g, I.cv, I.bv, I.cv32, I.vm, D.nx + 2, D.NYv, I.dv, I.dhv, I, &S.it_v, &S.fallbacks, &sv);
             b_relax_outlet(g, I);
             mass = b_assemble_pcorr(g, I);
             b_pcorr_solve(g, I, inv, inv_bad, &S.it_p, &sp);
+            if (sp != KC_OK && sp != KC_NONFINITE) {
+                // the multigrid CG stalled: the refined BiCGSTAB from p' = 0 takes over (the native step
+                // falls back to the plain FP64 BiCGSTAB here; on one SM that is too slow to use)
+                ++S.fallbacks;
+                const int NXp = D.nx + 2, np = NXp * D.NYp;
+                for (int k = g.tid; k < np; k += g.nt) I.pc[k] = 0.0;
+                g.sync();
+                b_bicg_refined(g, I, true, I.cp, I.bp, I.cp32, I.pc, NXp, D.NYp, I.dp, 50ll * np, &S.it_p, &sp);
+            }
             b_correct(g, I);
             S.outer += 1;
             const bool nonfinite = su == KC_NONFINITE || sv == KC_NONFINITE || sp == KC_NONFINITE;
             if (nonfinite) S.status = KC_NONFINITE;
             else if ((su != KC_OK || sv != KC_OK || sp != KC_OK) && S.status == KC_OK) S.status = KC_MAXITER;
-            S.fallbacks += (su != KC_OK) + (sv != KC_OK) + (sp != KC_OK);
             S.mass = mass;
             if (nonfinite || !isfinite(mass)) {
                 S.status = KC_NONFINITE;
@@ -1041,7 +1232,7 @@ BSizes sizes_of(const kc_channel* c) {
 // flags; level 0's w and flags
 size_t inst_bytes(const BSizes& z) {
     const long long nm = std::max(z.nu, z.nv);
-    size_t o = 3 * align256((size_t)nm * 4) + 5 * align256((size_t)z.np * 4);
+    size_t o = 8 * align256((size_t)nm * 4) + 5 * align256((size_t)z.np * 4);
     o += align256((size_t)z.np * 4) + align256((size_t)z.np);
     for (int l = 1; l < z.levels; ++l) {
         const size_t n = (size_t)z.NX[l] * z.NY[l];
@@ -1165,6 +1356,8 @@ int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void*
         I.gw = (float*)take((size_t)nm * 4);
         I.r32 = (float*)take((size_t)nm * 4);
         I.d32 = (float*)take((size_t)nm * 4);
+        for (int q = 0; q < 5; ++q) I.bt[q] = (float*)take((size_t)nm * 4);
+        I.eps_inner = c->eps_inner > 0 ? c->eps_inner : 1e-3;
         I.cr = (float*)take((size_t)z.np * 4);
         I.cz = (float*)take((size_t)z.np * 4);
         I.cpv = (float*)take((size_t)z.np * 4);

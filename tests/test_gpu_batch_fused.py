@@ -105,3 +105,25 @@ def test_fused_poisoned_instance_stops_alone(dev):
             assert np.array_equal(b.solvers[k].state_numpy()[f], one.solvers[0].state_numpy()[f])
         one.close()
     b.close()
+
+
+def test_fused_momentum_fallback_tracks_native_step(dev):
+    """A 128 x 32 channel with a 15-cell cylinder at Re 181 (instance 238 of the seeded 256-instance
+    batch): a few steps in, the Gauss-Seidel momentum solves miss eps and the refined BiCGSTAB takes
+    over, in the fused launch as in the native step; the per-step mass residuals stay those of the
+    native step (to the solves' tolerance) instead of drifting away."""
+    from karman_taichi_gb300.batch import BatchedChannels, batch_configs
+    from karman_taichi_gb300.channel import ChannelSolver
+    cfg = batch_configs(256, seed=0)[238]
+    assert (cfg.nx, cfg.ny, cfg.D) == (128, 32, 15)
+    b = BatchedChannels([cfg], device=dev, precision="mixed", workers=1)
+    solo = ChannelSolver(cfg, device=dev, precision="mixed", recycle=0)
+    fallbacks = 0
+    for t in range(12):
+        b.step_fused(1)
+        fallbacks += b.fused_totals[0]["fallbacks"]
+        mf = b.records[0][-1][0]["mass"]
+        ms = solo.step()[0]["mass"]
+        assert abs(mf - ms) <= 1e-3 * ms + 1e-12, (t, mf, ms)
+    assert solo.fallbacks > 0 and fallbacks > 0
+    b.close()
