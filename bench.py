@@ -80,7 +80,9 @@ def parse():
                     help="the long run of --config (default channel_4096x1024): its seeded copies advanced "
                          "together for N time steps with wake probes (shedding period and its drift), then the "
                          "plain FP64 method's first --fp64-steps steps against copy 0, and exit")
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=0,
+                    help="the long run's FP64 comparison: steps of the plain method against copy 0 (at 4096x1024 "
+                         "its p' BiCGSTAB stagnates within the first step)")
     ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
                     help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
                          "(the command the committed ncu summaries were captured on)")
