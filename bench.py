@@ -83,6 +83,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=0,
                     help="the long run's FP64 comparison: steps of the plain method against copy 0 (at 4096x1024 "
                          "its p' BiCGSTAB stagnates within the first step)")
+    ap.add_argument("--no-device-loop", action="store_true",
+                    help="run the multigrid CG's iterations as graph-captured chunks instead of a conditional "
+                         "WHILE graph node (kc_device_loop(0)): the same kernels, listed by ncu")
     ap.add_argument("--profile-outer", type=int, default=0, metavar="N",
                     help="run N SIMPLE outer iterations of --mode from the seeded state, untimed, and exit "
                          "(the command the committed ncu summaries were captured on)")
@@ -892,6 +895,9 @@ def run_profile_outer(args):
 
 if __name__ == "__main__":
     a = parse()
+    if a.no_device_loop:
+        from karman_taichi_gb300 import _lib as _L
+        _L.load().kc_device_loop(0)
     if a.impl == "reference":
         run_reference(a)
     elif a.profile_outer > 0:

@@ -120,6 +120,14 @@ size_t      kc_graph_cache_limit(size_t cap);
  * default) and returns the previous setting, so a test can make a wait run
  * out without any block hanging.  No counterpart in the reference. */
 unsigned    kc_debug_barrier_spin_limit(unsigned polls);
+/* The multigrid CG's iterations run in a CUDA graph whose conditional WHILE
+ * node repeats one iteration until the solver is done (one launch per
+ * refinement pass).  enable = 0 uses graph-captured chunks of iterations
+ * with a host check between chunks instead (the same kernels and results;
+ * profilers list kernels of such graphs, not those under a conditional
+ * node), 1 the device loop; returns the previous setting (< 0: only
+ * queries).  No counterpart in the reference. */
+int         kc_device_loop(int enable);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),

@@ -2363,6 +2363,11 @@ unsigned kc_debug_barrier_spin_limit(unsigned polls) {
     return g_spin_limit.exchange(polls, std::memory_order_relaxed);
 }
 
+int kc_device_loop(int enable) {
+    if (enable < 0) return g_while_ok.load(std::memory_order_relaxed);
+    return g_while_ok.exchange(enable ? 1 : 0, std::memory_order_relaxed);
+}
+
 int kc_spmv(const kc_system* A, const void* x, void* y, void* stream) {
     int rc = check_system(A);
     if (rc) return rc;
