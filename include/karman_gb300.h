@@ -128,13 +128,6 @@ unsigned    kc_debug_barrier_spin_limit(unsigned polls);
  * node), 1 the device loop; returns the previous setting (< 0: only
  * queries).  No counterpart in the reference. */
 int         kc_device_loop(int enable);
-/* The fused multigrid cycle's levels below level 0 (down legs, the one-block
- * tail, up legs) run as one cooperative launch with grid barriers between
- * the phases, where the driver supports a cooperative launch in a graph
- * (probed once); enable = 0 launches them one by one (the same kernels'
- * arithmetic, bitwise the same cycle).  Returns whether the one-launch chain
- * was in use (enable < 0: only queries).  No counterpart in the reference. */
-int         kc_mg_chain(int enable);
 
 /* ---- stencil linear algebra --------------------------------------------- */
 /* y = A x.  Replaces BICGSolver.compute_Ap/compute_As (bicgsolver.py:65-76),

@@ -133,7 +133,6 @@ SIGNATURES = {
     "kc_graph_cache_limit": (S_, [S_]),
     "kc_debug_barrier_spin_limit": (C.c_uint, [C.c_uint]),
     "kc_device_loop": (I_, [I_]),
-    "kc_mg_chain": (I_, [I_]),
     "kc_spmv": (I_, [C.POINTER(KcSystem), P_, P_, P_]),
     "kc_dot_ws_bytes": (S_, [L_]),
     "kc_dot": (I_, [I_, L_, P_, P_, P_, P_, S_, P_]),

@@ -31,7 +31,6 @@
 #include "kc_common.cuh"
 #include "kc_mg.h"
 #include <algorithm>
-#include <atomic>
 #include <mutex>
 
 namespace kc {
@@ -441,11 +440,10 @@ __device__ __forceinline__ TailArr tail_arr(float* sm, const TailLevel& L) {
 }
 
 // half-sweep x += W (b - A x) over the cells of colour col ((i + j) & 1)
-template <int NTH>
 __device__ __forceinline__ void tail_sweep(const TailArr& A, const TailLevel& L, int col) {
     const int half = (A.NY + 1) >> 1;
     const int cnt = A.NX * half;
-    for (int e = threadIdx.x; e < cnt; e += NTH) {
+    for (int e = threadIdx.x; e < cnt; e += kTailThreads) {
         const int i = tdiv(e, L.mHalf), m = e - i * half;
         const int j = 2 * m + ((i + col) & 1);
         if (j >= A.NY) continue;
@@ -455,13 +453,8 @@ __device__ __forceinline__ void tail_sweep(const TailArr& A, const TailLevel& L,
     }
 }
 
-// The tail's two parts: staging of what does not depend on the previous
-// launch (weights, coefficients, the coarsest inverse), then the cycle from
-// b_in to x_out.  NTH threads; the result does not depend on NTH (every cell
-// of a half-sweep, every restricted and prolonged cell and every row of the
-// coarsest product is computed by one thread or warp in a fixed order).
-template <int NTH>
-__device__ __forceinline__ void tail_stage(const MgTail& T, float* sm) {
+__global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int* done) {
+    extern __shared__ __align__(16) float sm[];
     const int tid = threadIdx.x;
     // weights, coefficients and the inverse first: they do not depend on the previous launch
     for (int l = T.Ls; l <= T.Lend; ++l) {
@@ -469,7 +462,7 @@ __device__ __forceinline__ void tail_stage(const MgTail& T, float* sm) {
         const TailArr A = tail_arr(sm, L);
         float* w = const_cast<float*>(A.w);
         float* c = const_cast<float*>(A.c);
-        for (int k = tid; k < A.n; k += NTH) {
+        for (int k = tid; k < A.n; k += kTailThreads) {
             w[k] = __ldg(L.winv + k);
 #pragma unroll
             for (int q = 0; q < 5; ++q) c[q * A.n + k] = __ldg(L.c + q * A.n + k);
@@ -477,16 +470,13 @@ __device__ __forceinline__ void tail_stage(const MgTail& T, float* sm) {
     }
     const int nc = T.lv[T.Lend].NX * T.lv[T.Lend].NY;
     float* inv = sm + T.inv_so;
-    for (int e = tid; e < nc * nc; e += NTH) inv[e] = __ldg(T.inv + e);
-}
-
-template <int NTH>
-__device__ __forceinline__ void tail_solve(const MgTail& T, float* sm) {
-    const int tid = threadIdx.x;
-    const float* inv = sm + T.inv_so;
+    for (int e = tid; e < nc * nc; e += kTailThreads) inv[e] = __ldg(T.inv + e);
+    pdl_wait();
+    pdl_trigger();
+    if (mg_done(done)) return;
     {
         const TailArr A = tail_arr(sm, T.lv[T.Ls]);
-        for (int k = tid; k < A.n; k += NTH) A.b[k] = __ldcg(T.b_in + k);
+        for (int k = tid; k < A.n; k += kTailThreads) A.b[k] = __ldcg(T.b_in + k);
     }
     __syncthreads();
     // downward: red start, 2 nu - 1 half-sweeps (black, red, ...), restriction
@@ -494,17 +484,17 @@ __device__ __forceinline__ void tail_solve(const MgTail& T, float* sm) {
         const TailLevel& L = T.lv[l];
         const TailLevel& Q = T.lv[l + 1];
         const TailArr A = tail_arr(sm, L);
-        for (int k = tid; k < A.n; k += NTH) {
+        for (int k = tid; k < A.n; k += kTailThreads) {
             const int i = tdiv(k, L.mNY), j = k - i * A.NY;
             A.x[k] = ((i + j) & 1) == 0 ? A.w[k] * A.b[k] : 0.f;
         }
         __syncthreads();
         for (int h = 1; h < 2 * L.nu; ++h) {
-            tail_sweep<NTH>(A, L, h & 1);
+            tail_sweep(A, L, h & 1);
             __syncthreads();
         }
         const TailArr B = tail_arr(sm, Q);
-        for (int t = tid; t < B.n; t += NTH) {
+        for (int t = tid; t < B.n; t += kTailThreads) {
             const int I = tdiv(t, Q.mNY), J = t - I * B.NY;
             float s = 0.f;
 #pragma unroll
@@ -525,7 +515,7 @@ __device__ __forceinline__ void tail_solve(const MgTail& T, float* sm) {
         const TailArr A = tail_arr(sm, T.lv[T.Lend]);
         const int n = A.n;
         if (!__ldcg(T.inv_bad)) {
-            const int lane = tid & 31, wp = tid >> 5, nw = NTH >> 5;
+            const int lane = tid & 31, wp = tid >> 5, nw = kTailThreads >> 5;
             for (int i = wp; i < n; i += nw) {
                 float sacc = 0.f;
                 for (int j = lane; j < n; j += 32) sacc = fmaf(inv[i * n + j], A.b[j], sacc);
@@ -568,28 +558,19 @@ __device__ __forceinline__ void tail_solve(const MgTail& T, float* sm) {
         const TailLevel& Q = T.lv[l + 1];
         const TailArr A = tail_arr(sm, L);
         const float* xc = sm + Q.so;
-        for (int k = tid; k < A.n; k += NTH) {
+        for (int k = tid; k < A.n; k += kTailThreads) {
             if (!A.linked(k)) continue;
             const int i = tdiv(k, L.mNY), j = k - i * A.NY;
             A.x[k] = fmaf(L.alpha, xc[(i >> 1) * Q.NY + (j >> 1)], A.x[k]);
         }
         __syncthreads();
         for (int h = 1; h <= 2 * L.nu; ++h) {
-            tail_sweep<NTH>(A, L, h & 1);
+            tail_sweep(A, L, h & 1);
             __syncthreads();
         }
     }
     const TailArr A = tail_arr(sm, T.lv[T.Ls]);
-    for (int k = tid; k < A.n; k += NTH) T.x_out[k] = A.x[k];
-}
-
-__global__ void __launch_bounds__(kTailThreads, 1) k_mg_tail(MgTail T, const int* done) {
-    extern __shared__ __align__(16) float sm[];
-    tail_stage<kTailThreads>(T, sm);
-    pdl_wait();
-    pdl_trigger();
-    if (mg_done(done)) return;
-    tail_solve<kTailThreads>(T, sm);
+    for (int k = tid; k < A.n; k += kTailThreads) T.x_out[k] = A.x[k];
 }
 
 // large levels use the 64-wide tiles (16 x 60 owned cells at one sweep), small ones the 32-wide
@@ -638,8 +619,6 @@ MgLayout mg_layout(int NX, int NY, const kc_mg_opts* o) {
     off = align256(off + (size_t)kCoarseDirectMax * kCoarseDirectMax * 4);
     M.off_flag = off;
     off = align256(off + 16);
-    M.off_bar = off;
-    off = align256(off + sizeof(GridBar));
     M.total = off;
     return M;
 }
@@ -734,8 +713,6 @@ static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, 
 
 static inline unsigned pw_grid(long long n) { return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096)); }
 
-static void chain_probe(cudaStream_t s);
-
 int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o, cudaStream_t s) {
     if (!A || !A->coef || A->dtype != KC_F32) return set_error("multigrid needs FP32 coefficients"), KC_ERR_ARG;
     const int NY = A->stride;
@@ -745,8 +722,6 @@ int mg_setup(const kc_system* A, void* ws, size_t ws_bytes, const kc_mg_opts* o,
     if (!ws || ws_bytes < M.total) return set_error("multigrid workspace %zu < %zu", ws_bytes, M.total), KC_ERR_WORKSPACE;
     char* base = (char*)ws;
     const float* c0 = (const float*)A->coef;
-    KC_CUDA(cudaMemsetAsync(base + M.off_bar, 0, sizeof(GridBar), s));
-    chain_probe(s);
     k_mg_diag0<<<pw_grid(A->n), 256, 0, s>>>(c0, A->cs, A->es, A->form == KC_FORM_LAPLACIAN, (int)A->n, o->omega[0],
                                               (float*)(base + M.off_winv[0]), (unsigned char*)(base + M.off_iso[0]));
     KC_LAUNCH_CHECK("k_mg_diag0");
@@ -878,310 +853,11 @@ static int launch_tail(const TailPlan& P, const MgLayout& M, char* base, const k
     return KC_OK;
 }
 
-// ---- the coarse chain in one cooperative launch ----------------------------------------
-// Levels 1 .. Ls-1 down, the tail, levels Ls-1 .. 1 up: 2 (Ls - 1) + 1 launches of a few
-// microseconds each, every one waiting for its predecessor to drain.  Here one
-// cooperative launch runs them all with a grid barrier between the phases: blocks
-// 1 .. G-1 take the tiles of each level in turn (the tile functions of k_mg_down / k_mg_up,
-// the small levels' 8 x 24 tiles on 256 threads), block 0 stages the tail's constant
-// arrays while the others run the down legs and then runs the tail (tail_stage /
-// tail_solve on 256 threads).  Every cell is computed by the same operations as in the
-// separate launches, so the cycle's result is bitwise the same.  A barrier that times out
-// (co-residency is guaranteed by the cooperative launch; the bound is a guard) ends the
-// launch with a NaN in the level-1 output, which the calling solve reports as non-finite.
-constexpr int kChainThreads = 256;
-constexpr int kChainRY1 = kChainThreads / kMgAJ1;   // small tiles: 8 x 24 owned cells, 8 thread rows
-
-struct ChainLevel {
-    MgLvl L;
-    const float* b;    // the level's right-hand side
-    float* xpre;       // its pre-smoothed iterate
-    float* bc;         // the next level's right-hand side
-    float* xfin;       // its output
-    const float* xc;   // the next level's output
-    int NXc, NYc;
-    float alpha;
-    int big;           // 64-wide tiles
-    int tiles_x, ntiles;
-};
-struct MgChain {
-    ChainLevel lv[KC_MG_MAX_LEVELS];
-    int Ls;
-    MgTail T;
-    GridBar* bar;
-};
-
-template <int TI, int AJ, int RY, int NU>
-__device__ __forceinline__ void chain_down_tiles(const ChainLevel& C, float* dyn) {
-    using TS = MgTile<TI, AJ, RY, 2 * NU>;
-    const MgStage S{dyn, nullptr, dyn + TS::A, dyn + 3 * TS::A, dyn + 2 * TS::A, nullptr, nullptr};
-    for (int t = blockIdx.x - 1; t < C.ntiles; t += gridDim.x - 1) {
-        const int ty = t / C.tiles_x, tx = t - ty * C.tiles_x;
-        const int i0 = ty * TI, j0 = tx * mg_tj(AJ, NU);
-        mg_down_issue<TI, AJ, RY, false, 2 * NU>(i0, j0, C.L, C.b, nullptr, S);
-        cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
-        MgOwnNone::Sum sum{};
-        mg_down_compute<TI, AJ, RY, false, MgOwnNone, NU>(i0, j0, C.L, 0.f, MgOwnNone{}, S, C.xpre, C.bc, C.NXc,
-                                                           C.NYc, sum);
-        __syncthreads();   // the stage is refilled by the next tile
-    }
-}
-template <int TI, int AJ, int RY, int NU>
-__device__ __forceinline__ void chain_up_tiles(const ChainLevel& C, float* dyn) {
-    using TS = MgTile<TI, AJ, RY, 2 * NU>;
-    const MgStage S{dyn, nullptr, dyn + TS::A, dyn + 3 * TS::A, dyn + 2 * TS::A, dyn + 8 * TS::A, nullptr};
-    for (int t = blockIdx.x - 1; t < C.ntiles; t += gridDim.x - 1) {
-        const int ty = t / C.tiles_x, tx = t - ty * C.tiles_x;
-        const int i0 = ty * TI, j0 = tx * mg_tj(AJ, NU);
-        mg_up_issue<TI, AJ, RY, 2 * NU>(i0, j0, C.L, C.xpre, C.xc, C.NXc, C.NYc, C.b, S);
-        cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
-        MgOwnNone::Sum sum{};
-        mg_up_compute<TI, AJ, RY, MgOwnNone, NU>(i0, j0, C.L, C.alpha, MgOwnNone{}, S, C.xfin, sum);
-        __syncthreads();
-    }
-}
-
-template <int NU>
-__global__ void __launch_bounds__(kChainThreads) k_mg_chain(MgChain C, const int* done) {
-    extern __shared__ __align__(16) float dyn[];
-    constexpr int TIB = mg_big_ti(NU);
-    pdl_wait();
-    if (mg_done(done)) return;
-    const unsigned nb = gridDim.x;
-    bool ok = true;
-    if (blockIdx.x == 0) tail_stage<kChainThreads>(C.T, dyn);   // meanwhile, the others run the down legs
-    for (int l = 1; l < C.Ls && ok; ++l) {
-        if (blockIdx.x > 0) {
-            if (C.lv[l].big) chain_down_tiles<TIB, kMgAJ0, kMgRY0, NU>(C.lv[l], dyn);
-            else chain_down_tiles<kMgTI1, kMgAJ1, kChainRY1, NU>(C.lv[l], dyn);
-        }
-        ok = grid_sync(C.bar, nb);
-    }
-    if (ok) {
-        if (blockIdx.x == 0) {
-            __syncthreads();
-            tail_solve<kChainThreads>(C.T, dyn);
-        }
-        ok = grid_sync(C.bar, nb);
-    }
-    for (int l = C.Ls - 1; l >= 1 && ok; --l) {
-        if (blockIdx.x > 0) {
-            if (C.lv[l].big) chain_up_tiles<TIB, kMgAJ0, kMgRY0, NU>(C.lv[l], dyn);
-            else chain_up_tiles<kMgTI1, kMgAJ1, kChainRY1, NU>(C.lv[l], dyn);
-        }
-        if (l > 1) ok = grid_sync(C.bar, nb);
-    }
-    if (!ok && threadIdx.x == 0) C.lv[1].xfin[0] = __int_as_float(0x7fc00000);
-    pdl_trigger();
-}
-
-template <int NU>
-static size_t chain_tile_smem() {
-    using TB = MgTile<mg_big_ti(NU), kMgAJ0, kMgRY0, 2 * NU>;
-    using TL = MgTile<kMgTI1, kMgAJ1, kChainRY1, 2 * NU>;
-    const size_t big = 8 * TB::A + (size_t)(mg_big_ti(NU) / 2 + TB::H) * (kMgAJ0 / 2);
-    const size_t small = 8 * TL::A + (size_t)(kMgTI1 / 2 + TL::H) * (kMgAJ1 / 2);
-    return std::max(big, small) * sizeof(float);
-}
-
-static std::atomic<int> g_chain_supported{1};   // cleared when the driver refuses the cooperative launch in a graph
-static std::atomic<int> g_chain_on{1};          // kc_mg_chain
-static bool chain_enabled() {
-    return g_chain_supported.load(std::memory_order_relaxed) && g_chain_on.load(std::memory_order_relaxed);
-}
-
-template <int NU>
-static cudaError_t chain_attrs(size_t smem, int* blocks) {
-    // the per-device occupancy for this shared-memory size, cached
-    static std::mutex mu;
-    static int sms[64] = {0};
-    static size_t set_smem[64] = {0};
-    static int per_sm[64] = {0};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(mu);
-    if (!sms[dev]) {
-        int coop = 0;
-        e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-        if (e != cudaSuccess) return e;
-        if (!coop) return cudaErrorNotSupported;
-        e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-    }
-    if (set_smem[dev] != smem) {
-        e = cudaFuncSetAttribute(k_mg_chain<NU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[dev], k_mg_chain<NU>, kChainThreads, smem);
-        if (e != cudaSuccess) return e;
-        set_smem[dev] = smem;
-    }
-    *blocks = per_sm[dev] * sms[dev];
-    return cudaSuccess;
-}
-
-template <int NU>
-static int launch_chain_nu(const MgChain& C, size_t smem, int max_tiles, const int* done, cudaStream_t s) {
-    int blocks = 0;
-    cudaError_t e = chain_attrs<NU>(smem, &blocks);
-    if (e != cudaSuccess) return cuda_status(e, "k_mg_chain attributes");
-    blocks = std::min(blocks, max_tiles + 1);
-    if (blocks < 2) return set_error("k_mg_chain: fewer than two resident blocks"), KC_ERR_UNSUPPORTED;
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(blocks);
-    cfg.blockDim = dim3(kChainThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, k_mg_chain<NU>, C, done);
-    if (e != cudaSuccess) return cuda_status(e, "k_mg_chain launch");
-    return KC_OK;
-}
-
-// the chain for levels 1 .. P.Ls - 1 and the tail; KC_ERR_UNSUPPORTED when it does not apply
-static int launch_mg_chain(const TailPlan& P, const MgLayout& M, char* base, const kc_system* A, const kc_mg_opts* o,
-                           const int* done, cudaStream_t s) {
-    const int nu = mg_nu_coarse(o);
-    if (!chain_enabled() || P.Ls < 2 || nu > 3) return KC_ERR_UNSUPPORTED;
-    MgChain C{};
-    C.Ls = P.Ls;
-    C.bar = (GridBar*)(base + M.off_bar);
-    const float* c0 = (const float*)A->coef;
-    const int lap0 = A->form == KC_FORM_LAPLACIAN;
-    int max_tiles = 0;
-    for (int l = 1; l < P.Ls; ++l) {
-        ChainLevel& L = C.lv[l];
-        const Lvl lv = level_of(M, base, l, c0, A->cs, A->es, lap0);
-        L.L = mg_lvl(lv);
-        L.b = (const float*)(base + M.off_b[l]);
-        L.xpre = (float*)(base + M.off_x[l]);
-        L.bc = (float*)(base + M.off_b[l + 1]);
-        L.xfin = mg_final(M, base, l);
-        L.xc = mg_final(M, base, l + 1);
-        L.NXc = M.nx[l + 1];
-        L.NYc = M.ny[l + 1];
-        L.alpha = o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)];
-        L.big = mg_big(lv.NX, lv.NY, o) ? 1 : 0;
-        const int TI = L.big ? mg_big_ti(nu) : kMgTI1, TJ = mg_tj(L.big ? kMgAJ0 : kMgAJ1, nu);
-        L.tiles_x = (lv.NY + TJ - 1) / TJ;
-        L.ntiles = L.tiles_x * ((lv.NX + TI - 1) / TI);
-        max_tiles = std::max(max_tiles, L.ntiles);
-    }
-    // the tail's description, as launch_tail builds it
-    {
-        MgTail& T = C.T;
-        int off = 0;
-        for (int l = P.Ls; l <= P.Lend; ++l) {
-            TailLevel& L = T.lv[l];
-            L.c = (const float*)(base + M.off_coef[l]);
-            L.winv = (const float*)(base + M.off_winv[l]);
-            L.NX = M.nx[l];
-            L.NY = M.ny[l];
-            L.alpha = o->alpha[std::min(l, KC_MG_MAX_LEVELS - 1)];
-            L.nu = std::max(mg_nu_pre(o, l), mg_nu_post(o, l));
-            L.so = off;
-            L.mNY = tail_magic(L.NY);
-            L.mHalf = tail_magic((L.NY + 1) / 2);
-            off += kTailArrays * L.NX * L.NY;
-        }
-        T.inv_so = off;
-        T.Ls = P.Ls;
-        T.Lend = P.Lend;
-        T.b_in = (const float*)(base + M.off_b[P.Ls]);
-        T.x_out = mg_final(M, base, P.Ls);
-        T.inv = (const float*)(base + M.off_inv);
-        T.inv_bad = (const int*)(base + M.off_flag);
-    }
-    size_t smem = 0;
-    switch (nu) {
-        case 1: smem = chain_tile_smem<1>(); break;
-        case 2: smem = chain_tile_smem<2>(); break;
-        default: smem = chain_tile_smem<3>(); break;
-    }
-    smem = std::max(smem, P.smem);
-    switch (nu) {
-        case 1: return launch_chain_nu<1>(C, smem, max_tiles, done, s);
-        case 2: return launch_chain_nu<2>(C, smem, max_tiles, done, s);
-        default: return launch_chain_nu<3>(C, smem, max_tiles, done, s);
-    }
-}
-
-// Once per process (outside any capture): can a cooperative launch of the chain, followed by a
-// programmatic-dependent launch, be captured into a graph, instantiated and replayed?  The
-// replay's kernels return at once (their "done" word is set).  Anything refused marks the chain
-// unsupported, and the cycle keeps its separate launches.
-static void chain_probe(cudaStream_t s) {
-    static std::mutex mu;
-    static bool done = false;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
-        cudaGetLastError();
-        return;   // not inside a capture: allocation and a capture of its own would break the caller's
-    }
-    std::lock_guard<std::mutex> lk(mu);
-    if (done) return;
-    done = true;
-    {
-        int* flag = nullptr;
-        cudaStream_t ps = nullptr;
-        cudaGraph_t g = nullptr;
-        cudaGraphExec_t ge = nullptr;
-        bool ok = cudaMalloc(&flag, sizeof(int)) == cudaSuccess &&
-                  cudaMemset(flag, 0xff, sizeof(int)) == cudaSuccess &&
-                  cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking) == cudaSuccess;
-        if (ok) ok = cudaStreamBeginCapture(ps, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-        if (ok) {
-            MgChain C{};
-            int blocks = 0;
-            const size_t smem = chain_tile_smem<1>();
-            bool launched = chain_attrs<1>(smem, &blocks) == cudaSuccess && blocks >= 2;
-            if (launched) {
-                cudaLaunchConfig_t cfg{};
-                cfg.gridDim = dim3(2);
-                cfg.blockDim = dim3(kChainThreads);
-                cfg.dynamicSmemBytes = smem;
-                cfg.stream = ps;
-                cudaLaunchAttribute at[1];
-                at[0].id = cudaLaunchAttributeCooperative;
-                at[0].val.cooperative = 1;
-                cfg.attrs = at;
-                cfg.numAttrs = 1;
-                launched = cudaLaunchKernelEx(&cfg, k_mg_chain<1>, C, (const int*)flag) == cudaSuccess;
-                // and a dependent launch after it, as the level-0 kernel that follows the chain
-                launched = launched && launch_chain(k_mg_coarsest, dim3(1), dim3(32), 0, ps, Lvl{},
-                                                    (const float*)nullptr, (float*)nullptr, 0,
-                                                    (const float*)nullptr, (const int*)nullptr,
-                                                    (const int*)flag) == cudaSuccess;
-            }
-            const bool ended = cudaStreamEndCapture(ps, &g) == cudaSuccess;
-            ok = launched && ended && g && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
-            // one replay: every kernel of it returns at once (the flag is set)
-            ok = ok && cudaGraphLaunch(ge, ps) == cudaSuccess && cudaStreamSynchronize(ps) == cudaSuccess;
-        }
-        if (ge) cudaGraphExecDestroy(ge);
-        if (g) cudaGraphDestroy(g);
-        if (ps) cudaStreamDestroy(ps);
-        if (flag) cudaFree(flag);
-        cudaGetLastError();
-        if (!ok) g_chain_supported.store(0);
-    }
-}
-
 int mg_cycle_kernels(const kc_system* A, const kc_mg_opts* o) {
     const int NY = A->stride;
     const MgLayout M = mg_layout((int)(A->n / NY), NY, o);
     if (mg_fusable(M, o)) {
         const TailPlan P = tail_plan(M, o);
-        if (P.ok && P.Ls >= 2 && chain_enabled() && mg_nu_coarse(o) <= 3) return 3;
         return P.ok ? 2 * P.Ls + 1 : 2 * (M.levels - 1) + 1;
     }
     int n = 1;
@@ -1200,16 +876,6 @@ int mg_enqueue_coarse(const kc_system* A, void* ws, const kc_mg_opts* o, const i
     const int lap0 = A->form == KC_FORM_LAPLACIAN;
     int nk = 0, rc;
     const TailPlan P = tail_plan(M, o);
-    if (P.ok && P.Ls >= 2 && chain_enabled()) {
-        // levels 1 .. Ls-1 and the tail in one cooperative launch
-        rc = launch_mg_chain(P, M, base, A, o, done, s);
-        if (rc == KC_OK) {
-            KC_LAUNCH_CHECK_NC("k_mg_chain");
-            if (kernels) *kernels = 1;
-            return KC_OK;
-        }
-        if (rc != KC_ERR_UNSUPPORTED) return rc;
-    }
     if (P.ok) {   // levels 1..Ls-1 one launch each, Ls..coarsest in the tail block
         for (int l = 1; l < P.Ls; ++l) {
             const Lvl L = level_of(M, base, l, c0, A->cs, A->es, lap0);
@@ -1379,12 +1045,6 @@ int kc_mg_setup(const kc_system* A32, void* mg_ws, size_t mg_ws_bytes, const kc_
         opts = &d;
     }
     return mg_setup(A32, mg_ws, mg_ws_bytes, opts, as_stream(stream));
-}
-
-int kc_mg_chain(int enable) {
-    const int prev = chain_enabled() ? 1 : 0;
-    if (enable >= 0) g_chain_on.store(enable ? 1 : 0, std::memory_order_relaxed);
-    return prev;
 }
 
 int kc_mg_apply(const kc_system* A32, void* mg_ws, const kc_mg_opts* opts, const float* r, float* z, void* stream) {

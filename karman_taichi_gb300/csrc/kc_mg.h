@@ -37,7 +37,6 @@ struct MgLayout {
     size_t off_winv[KC_MG_MAX_LEVELS], off_iso[KC_MG_MAX_LEVELS], off_coef[KC_MG_MAX_LEVELS];
     size_t off_b[KC_MG_MAX_LEVELS], off_x[KC_MG_MAX_LEVELS], off_t[KC_MG_MAX_LEVELS];
     size_t off_inv, off_flag;   // direct coarsest solve: dense inverse, failure flag
-    size_t off_bar;             // grid barrier of the one-launch coarse chain
     size_t total;
 };
 

@@ -29,35 +29,3 @@ def test_device_loop_and_chunked_graphs_agree_bitwise(dev):
         assert torch.equal(out[1][0], out[0][0])
     finally:
         lib.kc_device_loop(prev)
-
-
-def test_one_launch_coarse_chain_is_the_separate_launches(dev):
-    """The levels below level 0 as one cooperative launch (kc_mg_chain) against one launch per
-    level: the V-cycle bit for bit, and the refined multigrid CG with the same iterations and
-    solution (levels 1-3 by tiles, the tail below)."""
-    import torch
-    from karman_taichi_gb300 import _lib as L, linalg
-    from karman_taichi_gb300.channel import ChannelSolver
-    from karman_taichi_gb300.config import ChannelConfig
-    cfg = ChannelConfig("chain", 1024, 256, 1.0 / 256, 16, (("circle", 200, 128, 16),), max_outer=4)
-    s = ChannelSolver(cfg, device=dev, precision="mixed", recycle=0)
-    s.assemble_momentum(); s.solve_momentum(); s.relax(); s.assemble_p()
-    s.mg.setup()
-    lib = L.load()
-    prev = lib.kc_mg_chain(-1)
-    try:
-        r = torch.randn(s.b_p.numel(), generator=torch.Generator().manual_seed(3), dtype=torch.float32).to(dev)
-        out = {}
-        for chain in (1, 0):
-            lib.kc_mg_chain(chain)
-            z = s.mg.apply(r)
-            x = torch.zeros_like(s.b_p)
-            info = linalg.pcg_refined(s.A_p, s.A_p32, s.b_p, x, s.mg, eps=1e-8)
-            assert info.ok, info
-            out[chain] = (z, x, info.iters)
-        assert torch.equal(out[1][0], out[0][0])
-        assert out[1][2] == out[0][2]
-        assert torch.equal(out[1][1], out[0][1])
-        assert bool(torch.isfinite(out[1][0]).all())
-    finally:
-        lib.kc_mg_chain(prev)
