@@ -160,9 +160,10 @@ int kc_bicgstab(const kc_system* A, const void* b, void* x, const void* M,
  * limits the system to KC_NOALLOC_MAX_N unknowns; larger systems are
  * rejected with KC_ERR_ARG and an explanation in kc_last_error().
  * The first call on a device looks up that array's device address (once per
- * device, with the device current); make that first call before any stream
- * capture.  The address is kept for the life of the process and is not looked
- * up again after cudaDeviceReset.  Every call uses the same array and each
+ * device, with the device current); the address is kept for the life of the
+ * process and is not looked up again after cudaDeviceReset.  Every call
+ * synchronises with the host (it reads the solver state back), so no call can
+ * be captured into a CUDA graph.  Every call uses the same array and each
  * call clears the state it needs, but calls that overlap on the GPU
  * (concurrent streams, threads or processes sharing a context) race on it.
  * Iterations are launched directly (opts->use_graph is ignored).  Each call
