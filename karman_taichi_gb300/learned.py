@@ -447,6 +447,105 @@ def collect_pairs(solver, n_steps, every=1, max_pairs=None):
     return pairs
 
 
+class PairStore:
+    """Training pairs kept on the device in compact form, for the large training
+    sets (about 3 MB a pair at the 2048 x 512 channel's half resolution, against
+    11 MB for the network's 16-channel bf16 input): the NFEAT real feature
+    channels (bf16), the target (bf16; it is normalised to unit RMS, and
+    8 mantissa bits are far below the prediction's error) and the fluid weight
+    (uint8 quarters: a 2 x 2 average of a 0/1 mask).  Indexing gives the
+    (features, target, weight, count) tuples `train` and `mean_loss` take,
+    through one reusable set of full-size buffers."""
+
+    def __init__(self, capacity, Hh, Wh, device):
+        dev = torch.device(device)
+        self.capacity, self.Hh, self.Wh = int(capacity), Hh, Wh
+        self.feat = torch.empty((self.capacity, Hh, Wh, NFEAT), dtype=torch.bfloat16, device=dev)
+        self.tgt = torch.empty((self.capacity, Hh, Wh), dtype=torch.bfloat16, device=dev)
+        self.wq = torch.empty((self.capacity, Hh, Wh), dtype=torch.uint8, device=dev)
+        self.count = []
+        self._feat = torch.zeros((Hh, Wh, CIN), dtype=torch.bfloat16, device=dev)
+        self._tgt = torch.empty((Hh, Wh), dtype=torch.float32, device=dev)
+        self._wgt = torch.empty((Hh, Wh), dtype=torch.float32, device=dev)
+
+    def __len__(self):
+        return len(self.count)
+
+    def full(self):
+        return len(self.count) >= self.capacity
+
+    def add(self, feat, tgt, wgt):
+        k = len(self.count)
+        self.feat[k].copy_(feat[..., :NFEAT])
+        self.tgt[k].copy_(tgt)
+        self.wq[k].copy_(torch.round(wgt * 4).to(torch.uint8))
+        self.count.append(float(wgt.sum().item()))
+
+    def __getitem__(self, k):
+        self._feat[..., :NFEAT].copy_(self.feat[k])
+        self._tgt.copy_(self.tgt[k])
+        self._wgt.copy_(self.wq[k].to(torch.float32) * 0.25)
+        return self._feat, self._tgt, self._wgt, self.count[k]
+
+
+def collect_runs(cfgs, n_steps, store, every=1, device="cuda"):
+    """Fills `store` with pairs from the SIMPLE runs of `cfgs` (one after the
+    other, `n_steps` time steps each, every `every`-th outer iteration),
+    stopping when it is full; returns the pairs taken per run."""
+    from .channel import ChannelSolver
+    taken = []
+    for cfg in cfgs:
+        if store.full():
+            break
+        solver = ChannelSolver(cfg, device=device, precision="mixed")
+        NX, NY = solver.b_p.shape
+        fz = Featurizer(NX, NY, solver.device)
+        assert (fz.Hh, fz.Wh) == (store.Hh, store.Wh), "every run must have the store's grid"
+        k = before = len(store)
+        for _ in range(n_steps):
+            for _ in range(solver.cfg.max_outer):
+                solver.assemble_momentum()
+                solver.solve_momentum()
+                solver.relax()
+                solver.assemble_p()
+                take = k % every == 0 and not store.full()
+                if take:
+                    feat = fz(solver.b_p, solver.coef_p32)
+                    scales = fz.scales.clone()
+                solver.solve_p()
+                if take:
+                    fz.scales.copy_(scales)
+                    tgt, wgt = fz.target(solver.pcor, solver.coef_p32)
+                    store.add(feat, tgt, wgt)
+                k += 1
+                solver.correct()
+                if float(solver.mass[0].item()) <= solver.cfg.mass_tol:
+                    break
+            solver.time_forward()
+            if store.full():
+                break
+        taken.append(len(store) - before)
+        del solver, fz
+        torch.cuda.empty_cache()
+    return taken
+
+
+def training_configs(base, n, seed=0):
+    """Channels of the 2048 x 512 kind for the training set: the base grid and
+    inlet, the cylinder's diameter (24-40 cells), centre (x 300-500, y 256 +- 26)
+    and Re (100-200) drawn per run, per-run initial noise (seeds from 100:
+    the benchmark's seed 0 and the default training seed 7 are not among them)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n):
+        D = int(rng.integers(24, 41))
+        ci = int(rng.integers(300, 501))
+        cj = int(256 + rng.integers(-26, 27))
+        Re = float(rng.uniform(100.0, 200.0))
+        out.append(base.with_(name=base.name, D=D, obstacles=(("circle", ci, cj, D),), Re=Re, seed=100 + r))
+    return out
+
+
 def train(net, pairs, steps, lr=1e-3, batch=4, seed=0, log_every=0):
     """Adam on the mean squared error over fluid cells: `batch` pairs per step
     (gradients accumulated), learning rate on a cosine schedule."""
@@ -493,7 +592,8 @@ def make_channel_solver(cfg, device):
 
 
 def main(argv=None):
-    """python -m karman_taichi_gb300.learned --config channel_2048x512 --steps-sim 20 --train-steps 1500"""
+    """python -m karman_taichi_gb300.learned --config channel_2048x512 --steps-sim 20 --train-steps 1500
+    python -m karman_taichi_gb300.learned --pairs 20000 --runs 24 --steps-sim 150 --train-steps 5000"""
     import argparse
     from .channel import ChannelSolver
     from .config import get
@@ -505,21 +605,38 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=7,
                     help="seed of the initial-state noise of the training run (the benchmark runs seed 0)")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--pairs", type=int, default=0,
+                    help="collect this many pairs from --runs varied channels of the config's grid into an "
+                         "on-device store (0: the pairs of one run of --steps-sim steps)")
+    ap.add_argument("--runs", type=int, default=24)
     a = ap.parse_args(argv)
     cfg = get(a.config).with_(seed=a.seed)
     dev = torch.device("cuda", 0)
     t0 = time.time()
-    solver = ChannelSolver(cfg, device=dev, precision="mixed")
-    pairs = collect_pairs(solver, a.steps_sim)
-    torch.cuda.synchronize()
-    print(f"{len(pairs)} pairs from {a.steps_sim} time steps (seed {a.seed}) in {time.time() - t0:.1f} s", flush=True)
+    if a.pairs > 0:
+        probe = Featurizer(cfg.nx + 2, cfg.ny + 2, dev)
+        pairs = PairStore(a.pairs, probe.Hh, probe.Wh, dev)
+        del probe
+        taken = collect_runs(training_configs(get(a.config), a.runs), a.steps_sim, pairs, device=dev)
+        torch.cuda.synchronize()
+        print(f"{len(pairs)} pairs from {len(taken)} runs of up to {a.steps_sim} time steps {taken} in "
+              f"{time.time() - t0:.1f} s", flush=True)
+        held = [pairs[int(k)] for k in np.linspace(0, len(pairs) - 1, 8).astype(int)]
+        sample = lambda: [(f.clone(), t.clone(), w.clone(), c) for f, t, w, c in held]
+    else:
+        solver = ChannelSolver(cfg, device=dev, precision="mixed")
+        pairs = collect_pairs(solver, a.steps_sim)
+        torch.cuda.synchronize()
+        print(f"{len(pairs)} pairs from {a.steps_sim} time steps (seed {a.seed}) in {time.time() - t0:.1f} s",
+              flush=True)
+        sample = lambda: pairs
     net = UNet(dev, seed=0)
-    before = mean_loss(net, pairs)
+    before = mean_loss(net, sample())
     t0 = time.time()
     hist = train(net, pairs, a.train_steps, lr=a.lr, log_every=max(1, a.train_steps // 10))
     torch.cuda.synchronize()
     print(f"trained {a.train_steps} steps in {time.time() - t0:.1f} s: mean loss {before:.4g} -> "
-          f"{mean_loss(net, pairs):.4g}; {hist}", flush=True)
+          f"{mean_loss(net, sample()):.4g} (on {len(sample())} pairs); {hist}", flush=True)
     path = a.out or weights_path(cfg.name)
     net.save(path)
     print("saved", path, flush=True)
