@@ -139,3 +139,42 @@ def test_native_step_with_network_matches_python_step(dev):
     sa, sb = a.state_numpy(), b.state_numpy()
     for k in ("u", "v", "p", "u0", "v0"):
         assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_committed_weights_on_held_out_systems(dev):
+    """The committed weights (trained on 20,000 pairs of other 2048 x 512 runs) on the benchmark's
+    own channel (seed 0, never in the training set), against the default cycle: the prediction
+    is far closer to p' than the zero start (what the network gains), and the flexible solve it
+    seeds converges to the multigrid CG's solution -- in about as many CG iterations, which is
+    why it does not pay (the inference is added to every solve)."""
+    import torch
+    from karman_taichi_gb300 import _lib as L, learned, linalg
+    from karman_taichi_gb300.channel import ChannelSolver
+    from karman_taichi_gb300.config import get
+    if not learned.available("channel_2048x512"):
+        pytest.skip("no committed weights")
+    cfg = get("channel_2048x512")
+    s = ChannelSolver(cfg, device=dev, precision="mixed", native=False, recycle=0)
+    s.step()
+    net = learned.UNet.load(learned.weights_path(cfg.name), device=dev)
+    guess = learned.LearnedGuess(net)
+    errs, it_mg, it_fx = [], 0, 0
+    for _ in range(3):
+        s.assemble_momentum(); s.solve_momentum(); s.relax(); s.assemble_p()
+        s.mg.setup()
+        ref = torch.zeros_like(s.b_p)
+        info = linalg.pcg_refined(s.A_p, s.A_p32, s.b_p, ref, s.mg, eps=1e-8)
+        assert info.ok
+        it_mg += info.iters
+        x0 = guess.predict(s).clone()
+        errs.append(float(torch.linalg.norm(x0 - ref) / torch.linalg.norm(ref)))
+        NX, NY = s.b_p.shape
+        x = torch.zeros_like(s.b_p)
+        fi_info, fi = linalg.pcg_flexible(s.A_p, s.A_p32, s.b_p, x, s.mg, net=net.native_net(NX, NY), eps=1e-8)
+        assert fi_info.status == L.OK and fi.learned_used == 1
+        it_fx += fi_info.iters
+        assert float((x - ref).abs().max() / ref.abs().max()) < 1e-6
+        s.pcor.copy_(ref)
+        s.correct()
+    assert max(errs) < 0.5, errs
+    assert it_fx <= 2 * it_mg, (it_fx, it_mg)
