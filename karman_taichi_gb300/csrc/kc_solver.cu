@@ -2717,37 +2717,52 @@ __global__ void __launch_bounds__(AJ * RY) k_gs_block_sweeps(MgLvl L, const floa
                                                              const float* __restrict__ xin, float* __restrict__ xout) {
     using T = MgTile<TI, AJ, RY, 2 * NU>;
     constexpr int H = T::H;
-    __shared__ __align__(16) float sb[T::A], sw[T::A], sx[T::A];
-    __shared__ __align__(16) float sc[5 * T::A];
+    constexpr int R = (T::AI + RY - 1) / RY;   // staged rows per thread
+    __shared__ __align__(16) float sx[T::A];
     const int i0 = blockIdx.y * TI, j0 = blockIdx.x * T::TJ;
-    const int bc = T::tx(), j = j0 + bc - H;
+    const int bc = T::tx(), ty = T::ty(), j = j0 + bc - H;
     const bool jin = j >= 0 && j < L.NY;
-    for (int a = T::ty(); a < T::AI; a += T::RY) {
+    // A thread updates the same column cells in every half-sweep: their coefficients, weights and
+    // right-hand sides stay in registers (zero outside the grid), only x goes through shared
+    // memory -- 5 shared-memory reads per cell update instead of 12.
+    float c0[R], c1[R], c2[R], c3[R], c4[R], wv[R], bv[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int a = ty + r * RY;
         const int i = i0 + a - H;
-        const bool in = jin && i >= 0 && i < L.NX;
-        const int k = in ? i * L.NY + j : 0;
-        const int u = a * T::AJ + bc;
-        cp_async4(sx + u, xin + k, in);
-        cp_async4(sb + u, b + k, in);
-        cp_async4(sw + u, L.winv + k, in);
+        const bool in = a < T::AI && jin && i >= 0 && i < L.NX;
+        const long long k = in ? (long long)i * L.NY + j : 0;
+        if (a < T::AI) cp_async4(sx + a * T::AJ + bc, xin + k, in);
+        const float* g = L.c + k * L.es;
+        c0[r] = in ? __ldg(g) : 0.f;
+        c1[r] = in ? __ldg(g + L.cs) : 0.f;
+        c2[r] = in ? __ldg(g + 2 * L.cs) : 0.f;
+        c3[r] = in ? __ldg(g + 3 * L.cs) : 0.f;
+        c4[r] = in ? __ldg(g + 4 * L.cs) : 0.f;
+        wv[r] = in ? __ldg(L.winv + k) : 0.f;
+        bv[r] = in ? __ldg(b + k) : 0.f;
     }
-    mg_stage_coef<TI, T>(L, i0, j0, sc);
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
-    const MgCoef<T, true> C{sc, L, i0, j0};
 #pragma unroll
     for (int h = 1; h <= 2 * NU; ++h) {   // odd h: red ((i + j) even), even h: black
-        if (bc >= h && bc < AJ - h)
-            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
-                if (((a + bc) & 1) != ((h & 1) ? 0 : 1)) continue;
+        if (bc >= h && bc < AJ - h) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int a = ty + r * RY;
+                if (a < h || a >= T::AI - h || ((a + bc) & 1) != ((h & 1) ? 0 : 1)) continue;
                 const int u = a * T::AJ + bc;
-                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
+                const float xv = sx[u];
+                const float y = mg_row(c0[r], c1[r], c2[r], c3[r], c4[r], L.lap, xv, sx[u - T::AJ], sx[u + T::AJ],
+                                       sx[u + 1], sx[u - 1]);
+                sx[u] = fmaf(wv[r], bv[r] - y, xv);
             }
+        }
         __syncthreads();
     }
     if (bc >= H && bc < T::TJ + H && j < L.NY)
-        for (int a = H + T::ty(); a < TI + H; a += T::RY) {
+        for (int a = H + ty; a < TI + H; a += T::RY) {
             const int i = i0 + a - H;
             if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + bc];
         }
