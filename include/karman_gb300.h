@@ -120,13 +120,16 @@ size_t      kc_graph_cache_limit(size_t cap);
  * default) and returns the previous setting, so a test can make a wait run
  * out without any block hanging.  No counterpart in the reference. */
 unsigned    kc_debug_barrier_spin_limit(unsigned polls);
-/* The multigrid CG's iterations run in a CUDA graph whose conditional WHILE
- * node repeats one iteration until the solver is done (one launch per
- * refinement pass).  enable = 0 uses graph-captured chunks of iterations
- * with a host check between chunks instead (the same kernels and results;
- * profilers list kernels of such graphs, not those under a conditional
- * node), 1 the device loop; returns the previous setting (< 0: only
- * queries).  No counterpart in the reference. */
+/* The multigrid-CG refinement (kc_pcg_refined with opts->use_graph) runs as
+ * one CUDA graph launch: a conditional WHILE node over the refinement passes
+ * (FP64 residual, the pass's decisions in a one-thread kernel, the inner
+ * solve) whose body holds a nested WHILE node over the CG iterations; one
+ * readback at the end.  enable = 0 runs the refinement passes from the host
+ * and the CG iterations in graph-captured chunks with a host check between
+ * chunks (the same kernels, decisions and results; profilers list kernels of
+ * such graphs, not those under a conditional node), 1 the device loops;
+ * returns the previous setting (< 0: only queries).  No counterpart in the
+ * reference. */
 int         kc_device_loop(int enable);
 
 /* ---- stencil linear algebra --------------------------------------------- */

@@ -2003,10 +2003,12 @@ struct GraphKey {
     int form = 0;
     unsigned long long ohash = 0;   // hash of the multigrid options (0: none)
     const void* b = nullptr;        // a right-hand side the captured launches read (0: none)
+    const void* c64 = nullptr;      // the FP64 system and iterate of a captured refinement (0: none)
+    const void* x64 = nullptr;
     bool operator<(const GraphKey& o) const {
-        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es, form, ohash, b) <
+        return std::tie(ws, coef, x, n, stride, dtype, pre, chunk, kind, cs, es, form, ohash, b, c64, x64) <
                std::tie(o.ws, o.coef, o.x, o.n, o.stride, o.dtype, o.pre, o.chunk, o.kind, o.cs, o.es, o.form,
-                        o.ohash, o.b);
+                        o.ohash, o.b, o.c64, o.x64);
     }
 };
 
@@ -3264,6 +3266,259 @@ static int pc_iter_kernels(const kc_system* A32, void* mg_ws, const kc_mg_opts* 
 // ||b - A64 x|| / ||b|| < eps.  A correction that raises the true residual is
 // undone and ends the solve with KC_STALL, as do two sweeps in a row that
 // gain less than 10 %.
+// ---- the whole refinement on the device (the multigrid CG path) --------------------------
+// The host loop of mg_refined reads the FP64 residual norms back after every
+// refinement pass and decides there (converged, stalled, undo, next inner
+// tolerance), and launches the next pass: a host round trip with the GPU idle
+// per pass.  Here the same decisions run in a one-thread kernel, and the whole
+// refinement is one graph launch: an outer WHILE node whose body is [FP64
+// residual, decision, undo, inner start, first V-cycle, the inner CG loop (a
+// nested WHILE node), correction], then one readback of the final state.  The
+// decision kernel sets both loops' conditions and, when the refinement ends,
+// marks the inner solver done, so the rest of that body pass does nothing.
+// The arithmetic of every decision is the host loop's (IEEE sqrt and
+// division), so the iterates, the iteration counts and the result are the
+// same bit for bit.  (The host loop finishes an inner solve that reached the
+// device loop's 1024-iteration cap with chunked graphs; here the refinement
+// goes on from the true residual.)
+struct RefState {
+    double bb, best, rel, eps, eps_inner, eps_in;
+    long long total, max_iter;
+    int it, max_refine, stalls, applied, status, done, undo, sweeps;
+};
+static_assert(sizeof(RefState) <= 192, "the refinement state lives in the 256-byte output slot");
+
+__global__ void k_ref_init(RefState* R, double eps, double eps_inner, long long max_iter, int max_refine) {
+    if (threadIdx.x || blockIdx.x) return;
+    R->bb = 0.0;
+    R->best = INFINITY;
+    R->rel = 1.0;
+    R->eps = eps;
+    R->eps_inner = eps_inner;
+    R->eps_in = eps_inner;
+    R->total = 0;
+    R->max_iter = max_iter;
+    R->it = 0;
+    R->max_refine = max_refine;
+    R->stalls = R->applied = R->done = R->undo = R->sweeps = 0;
+    R->status = KC_MAXITER;
+}
+
+__global__ void k_ref_decide(RefState* R, const double* __restrict__ out2, int* flag, SolverState* st,
+                             cudaGraphConditionalHandle ho, cudaGraphConditionalHandle hi) {
+    if (threadIdx.x || blockIdx.x) return;
+    bool stop = false;
+    int status = KC_MAXITER;
+    const double h0 = __ldcg(out2);
+    const int skipped = __ldcg(flag);
+    if (R->it == 0) R->bb = __ldcg(out2 + 1);
+    const double bb = R->bb;
+    double rel;
+    if (!isfinite(h0) || !isfinite(bb)) {   // a NaN or Inf in b, x or the system
+        rel = NAN;
+        status = KC_NONFINITE;
+        stop = true;
+    } else {
+        rel = bb > 0 ? sqrt(h0 / bb) : 0.0;
+        if (R->applied && skipped == 0 && !(rel < R->best)) {   // the last correction raised the residual
+            R->undo = 1;
+            rel = R->best;
+            status = KC_STALL;
+            stop = true;
+        } else {
+            R->applied = 0;
+            if (bb == 0.0 || rel < R->eps) {
+                status = KC_OK;
+                stop = true;
+            } else if (!isfinite(rel)) {
+                status = KC_NONFINITE;
+                stop = true;
+            } else {
+                if (rel >= 0.9 * R->best) {
+                    if (++R->stalls >= 2) {
+                        status = KC_STALL;
+                        stop = true;
+                    }
+                } else {
+                    R->stalls = 0;
+                }
+                if (!stop) {
+                    R->best = fmin(R->best, rel);
+                    if (R->it == R->max_refine || R->total >= R->max_iter) stop = true;   // KC_MAXITER
+                }
+            }
+        }
+    }
+    R->rel = rel;
+    R->it += 1;
+    if (stop) {
+        R->status = status;
+        R->done = 1;
+        st->done = 1;   // the rest of this pass: every inner kernel returns at once
+        cudaGraphSetConditional(hi, 0u);
+        cudaGraphSetConditional(ho, 0u);
+        return;
+    }
+    R->eps_in = fmax(R->eps_inner, 0.5 * R->eps / rel);
+    *flag = 0;
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(st);   // the inner state from zero
+    for (unsigned q = 0; q < sizeof(SolverState) / sizeof(unsigned long long); ++q) w[q] = 0ull;
+    cudaGraphSetConditional(hi, 1u);
+    cudaGraphSetConditional(ho, 1u);
+}
+
+__global__ void __launch_bounds__(kPwThreads) k_ref_undo(int n, const double* __restrict__ d, double* __restrict__ x,
+                                                         const RefState* R) {
+    if (!__ldcg(&R->undo)) return;
+    KC_PW_LOOP(n, { x[k] -= __ldg(d + k); })
+}
+
+// k_bicg_init_cold for the inner pass, its tolerance and cap from the refinement state
+__global__ void __launch_bounds__(kPwThreads)
+    k_bicg_init_cold_ref(int n, const float* __restrict__ b, float* __restrict__ x, float* __restrict__ r,
+                         float* __restrict__ rt, BicgPtrs P, const RefState* R) {
+    if (__ldcg(&R->done)) return;
+    Acc<float> acc[1];
+    KC_PW_LOOP(n, {
+        const float bk = __ldg(b + k);
+        r[k] = bk;
+        rt[k] = bk;
+        x[k] = 0.f;
+        acc[0].add(bk, bk);
+    })
+    double s[1];
+    if (block_partials<1>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
+        const StartArgs sa{__ldcg(&R->eps_in), __ldcg(&R->max_iter) - __ldcg(&R->total), 0, KC_REL_R0, nullptr, 0,
+                           1e30};
+        bicg_start(P.st, s[0], s[0], sa);
+        P.st->ticket[0] = 0;
+    }
+}
+
+__global__ void k_ref_after(RefState* R, const SolverState* st, cudaGraphConditionalHandle ho) {
+    if (threadIdx.x || blockIdx.x || R->done) return;
+    R->total += st->iter;
+    R->sweeps += 1;
+    R->applied = 1;
+    if (st->status != KC_OK && st->iter == 0) {
+        R->status = st->status;
+        R->done = 1;
+        cudaGraphSetConditional(ho, 0u);
+    }
+}
+
+static std::atomic<int> g_refloop_ok{1};   // cleared when the nested conditional graph is refused
+
+// The refinement of the multigrid CG as one graph launch; returns 1 when it ran (info filled),
+// 0 when the caller should run the host loop, < 0 on a CUDA error.
+template <class First, class Iter1>
+static int refine_on_device(const GraphKey& key, const kc_system* A64, Geo g, dim3 sg, const double* b, double* x,
+                            float* r32, BicgPtrs P, BicgPtrs Rr, double* out2, int* flag, PbVecs V, double* d64,
+                            const kc_solve_opts* o, double eps_inner, int max_refine, First&& first, Iter1&& iter1,
+                            int kernels_per_iter, kc_solve_info* info, int* status_out, cudaStream_t s) {
+    if (!g_refloop_ok.load(std::memory_order_relaxed) || !g_while_ok.load(std::memory_order_relaxed)) return 0;
+    const long long n = A64->n;
+    const int pb = pw_blocks(n);
+    RefState* R = reinterpret_cast<RefState*>(out2 + 8);
+    int dev = 0;
+    KC_CUDA(cudaGetDevice(&dev));
+    GraphKey gk = key;
+    gk.chunk = -2;
+    gk.kind += 200;
+    std::shared_ptr<GraphExec> gx = graph_lookup(dev, gk);
+    if (!gx) {
+        bool ok = true;
+        cudaGraph_t gr = nullptr;
+        cudaStream_t cs = nullptr, cs2 = nullptr;
+        cudaGraphConditionalHandle ho{}, hi{};
+        cudaGraphNodeParams cpo{}, cpi{};
+        cudaGraphNode_t onode, inode;
+        ok = cudaGraphCreate(&gr, 0) == cudaSuccess &&
+             cudaGraphConditionalHandleCreate(&ho, gr, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        if (ok) {
+            cpo.type = cudaGraphNodeTypeConditional;
+            cpo.conditional.handle = ho;
+            cpo.conditional.type = cudaGraphCondTypeWhile;
+            cpo.conditional.size = 1;
+            ok = cudaGraphAddNode(&onode, gr, nullptr, nullptr, 0, &cpo) == cudaSuccess;
+        }
+        cudaGraph_t body = ok ? cpo.conditional.phGraph_out[0] : nullptr;
+        ok = ok && cudaGraphConditionalHandleCreate(&hi, body, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+        ok = ok && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) == cudaSuccess;
+        if (ok && cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                      cudaSuccess) {
+            launch_refine_resid(A64, g, sg, b, x, r32, Rr, out2, true, cs);   // ||b||^2 too: the first pass keeps it
+            k_ref_decide<<<1, 32, 0, cs>>>(R, out2, flag, P.st, ho, hi);
+            k_ref_undo<<<pb, kPwThreads, 0, cs>>>((int)n, d64, x, R);
+            k_bicg_init_cold_ref<<<pb, kPwThreads, 0, cs>>>((int)n, r32, V.sh, V.r, V.rt, P, R);
+            k_zero_f64<<<pb, kPwThreads, 0, cs>>>((int)n, d64);
+            first(cs);   // the first V-cycle (returns at once when the refinement is done)
+            // the inner CG loop: a WHILE node added to the capture by hand, its body captured on cs2
+            cudaStreamCaptureStatus cst;
+            cudaGraph_t cg = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            ok = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd) == cudaSuccess &&
+                 cst == cudaStreamCaptureStatusActive;
+            if (ok) {
+                cpi.type = cudaGraphNodeTypeConditional;
+                cpi.conditional.handle = hi;
+                cpi.conditional.type = cudaGraphCondTypeWhile;
+                cpi.conditional.size = 1;
+                ok = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &cpi) == cudaSuccess &&
+                     cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                         cudaSuccess;
+            }
+            if (ok && cudaStreamBeginCaptureToGraph(cs2, cpi.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                    cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                iter1(cs2);
+                k_while_cond<<<1, 32, 0, cs2>>>(P.st, kWhileCap, hi);
+                cudaGraph_t o2 = nullptr;
+                ok = cudaStreamEndCapture(cs2, &o2) == cudaSuccess;
+            } else {
+                ok = false;
+            }
+            k_flag_nonfinite_f64<<<pb, kPwThreads, 0, cs>>>((int)n, d64, flag);
+            k_add_f64<<<pb, kPwThreads, 0, cs>>>((int)n, d64, x, flag);
+            k_ref_after<<<1, 32, 0, cs>>>(R, P.st, ho);
+            cudaGraph_t o1 = nullptr;
+            ok = (cudaStreamEndCapture(cs, &o1) == cudaSuccess) && ok;
+        } else {
+            ok = false;
+        }
+        if (cs2) cudaStreamDestroy(cs2);
+        if (cs) cudaStreamDestroy(cs);
+        cudaGraphExec_t ex = nullptr;
+        if (ok) ok = cudaGraphInstantiate(&ex, gr, 0) == cudaSuccess;
+        if (gr) cudaGraphDestroy(gr);
+        if (!ok) {
+            cudaGetLastError();
+            g_refloop_ok.store(0);
+            return 0;
+        }
+        gx = std::make_shared<GraphExec>(ex);
+        graph_insert(dev, gk, gx);
+    }
+    k_ref_init<<<1, 32, 0, s>>>(R, o->eps, eps_inner, o->max_iter, max_refine);
+    KC_LAUNCH_CHECK("k_ref_init");
+    KC_CUDA(cudaGraphLaunch(gx->ex, s));
+    const void* hp = readback(R, sizeof(RefState), s);
+    if (!hp) return KC_ERR_CUDA;
+    RefState h;
+    memcpy(&h, hp, sizeof(RefState));
+    count_launches(h.total * (long long)(kernels_per_iter + 1) + 12ll * h.it);
+    if (info) {
+        info->status = h.status;
+        info->refinements = h.sweeps;
+        info->iters = h.total;
+        info->rel_res = h.rel;
+        info->r0 = sqrt(h.bb);
+    }
+    *status_out = h.status;
+    return 1;
+}
+
 static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const double* b, double* x, const double* x0,
                       void* mg_ws, const kc_mg_opts* mg_opts, void* ws, size_t ws_bytes, const kc_solve_opts* o,
                       double eps_inner, int max_refine, kc_solve_info* info, void* stream) {
@@ -3306,6 +3561,38 @@ static int mg_refined(bool cg, const kc_system* A64, const kc_system* A32, const
     GraphKey key{ws, A32->coef, mg_ws, n, A32->stride, KC_F32, cg ? 8 : 7, 4, 2, A32->cs, A32->es};
     key.form = A32->form;
     key.ohash = bytes_hash(mg_opts, sizeof(kc_mg_opts));
+    if (cg && o->use_graph) {
+        // the whole refinement as one graph launch (falls back to the host loop below where the
+        // driver refuses nested conditional nodes)
+        GraphKey rk = key;
+        rk.x64 = x;
+        rk.b = b;
+        rk.c64 = A64->coef;
+        const int per_iter = pc_iter_kernels(A32, mg_ws, mg_opts);
+        int dst = KC_MAXITER;
+        const int ran = refine_on_device(
+            rk, A64, g, sg, b, x, r32, P, R, out2, flag, V, d64, o, eps_inner, max_refine,
+            [&](cudaStream_t cs) {
+                const MgFused F = mg_fused(A32, mg_ws, mg_opts);
+                int mk = 0;
+                if (F.ok) {
+                    PcfLaunch pl;
+                    if (pcf_launch(F.L0, &pl)) return;
+                    k_pcc_down0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_down, cs>>>(
+                        F.L0, F.x0pre, F.b1, F.NX1, F.NY1, W, P, 0, pl.gd);
+                    (void)mg_enqueue_coarse(A32, mg_ws, mg_opts, &P.st->done, cs, &mk);
+                    k_pcc_up0<kMgTI0, kMgAJ0, kMgRY0><<<pl.blocks, kMgNT0, pl.smem_up, cs>>>(
+                        F.L0, F.x0pre, F.final1, F.NX1, F.NY1, F.alpha0, W, P, pl.gu);
+                } else {
+                    (void)mg_enqueue(A32, mg_ws, mg_opts, W.r[0], W.z, &P.st->done, cs, &mk);
+                    k_pc_3<<<pb, kPwThreads, 0, cs>>>((int)n, W, P);
+                }
+            },
+            [&](cudaStream_t cs) { (void)launch_pc_iters(A32, mg_ws, mg_opts, W, P, 1, cs, nullptr); }, per_iter,
+            info, &dst, s);
+        if (ran < 0) return ran;
+        if (ran) return dst;
+    }
     for (int it = 0; it <= max_refine; ++it) {
         launch_refine_resid(A64, g, sg, b, x, r32, R, out2, it == 0, s);
         KC_LAUNCH_CHECK("k_refine_resid");
