@@ -128,8 +128,9 @@ unsigned    kc_debug_barrier_spin_limit(unsigned polls);
  * and the CG iterations in graph-captured chunks with a host check between
  * chunks (the same kernels, decisions and results; profilers list kernels of
  * such graphs, not those under a conditional node), 1 the device loops;
- * returns the previous setting (< 0: only queries).  No counterpart in the
- * reference. */
+ * returns the previous setting; enable < 0 only queries: bit 0 the CG loop,
+ * bit 1 the refinement loop (each cleared once the driver refuses it).  No
+ * counterpart in the reference. */
 int         kc_device_loop(int enable);
 
 /* ---- stencil linear algebra --------------------------------------------- */

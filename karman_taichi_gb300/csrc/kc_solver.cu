@@ -2181,6 +2181,7 @@ __global__ void k_while_cond(SolverState* st, unsigned cap, cudaGraphConditional
 
 constexpr unsigned kWhileCap = 1024;    // iterations one launch of the loop may run
 static std::atomic<int> g_while_ok{1};  // cleared when the driver refuses conditional nodes
+static std::atomic<int> g_refloop_ok{1};   // cleared when the nested conditional graph is refused
 
 // Runs the solve's iterations as one graph launch; returns 1 when it ran (state in h), 0 when the
 // caller should use the chunked loop instead, < 0 on a CUDA error.
@@ -2366,7 +2367,9 @@ unsigned kc_debug_barrier_spin_limit(unsigned polls) {
 }
 
 int kc_device_loop(int enable) {
-    if (enable < 0) return g_while_ok.load(std::memory_order_relaxed);
+    if (enable < 0)   // bit 0: the CG iteration loop, bit 1: the refinement loop (not refused by the driver)
+        return g_while_ok.load(std::memory_order_relaxed) |
+               (g_while_ok.load(std::memory_order_relaxed) && g_refloop_ok.load(std::memory_order_relaxed) ? 2 : 0);
     return g_while_ok.exchange(enable ? 1 : 0, std::memory_order_relaxed);
 }
 
@@ -3407,7 +3410,6 @@ __global__ void k_ref_after(RefState* R, const SolverState* st, cudaGraphConditi
     }
 }
 
-static std::atomic<int> g_refloop_ok{1};   // cleared when the nested conditional graph is refused
 
 // The refinement of the multigrid CG as one graph launch; returns 1 when it ran (info filled),
 // 0 when the caller should run the host loop, < 0 on a CUDA error.
