@@ -55,6 +55,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 namespace kc {
@@ -1418,10 +1419,17 @@ int kc_channel_batch_fused(const kc_channel* const* chs, int n, int steps, void*
     KC_CUDA(cudaMemcpyAsync(d_slots, order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, s));
     KC_CUDA(cudaMemcpyAsync(d_blocks, blocks.data(), blocks.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
     constexpr size_t dyn = (size_t)kBGroups * kBCoarse * kBCoarse * sizeof(float);
-    static bool attr_set = false;   // (set once per process; idempotent)
-    if (!attr_set) {
-        KC_CUDA(cudaFuncSetAttribute(k_batch_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        attr_set = true;
+    {   // the dynamic shared memory limit, once per device
+        static std::mutex mu;
+        static bool set[64] = {false};
+        int dev = 0;
+        KC_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64) return set_error("kc_channel_batch_fused: device index %d", dev), KC_ERR_ARG;
+        std::lock_guard<std::mutex> lk(mu);
+        if (!set[dev]) {
+            KC_CUDA(cudaFuncSetAttribute(k_batch_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+            set[dev] = true;
+        }
     }
     k_batch_steps<<<(unsigned)blocks.size(), kBBlock, dyn, s>>>(d_inst, d_slots, d_blocks, steps);
     KC_LAUNCH_CHECK("k_batch_steps");
