@@ -319,8 +319,6 @@ __global__ void __launch_bounds__(kThreads) k_spmv(Coef<T> A, Geo g, const T* __
 template <typename T, int V>
 struct VecOf;
 template <>
-struct VecOf<double, 1> { using type = double; };
-template <>
 struct VecOf<double, 2> { using type = double2; };
 template <>
 struct VecOf<float, 4> { using type = float4; };
@@ -1959,16 +1957,12 @@ static Coef<T> coef_of(const kc_system* A) {
     return Coef<T>{(const T*)A->coef, A->cs, A->es, A->form == KC_FORM_LAPLACIAN ? 1 : 0};
 }
 
-// r = b - A x and its sums: the flat pass (two cells per thread when A's layout allows
-// 16-byte loads, else one -- an odd row length such as the v system's) for SoA planes, else
-// the tile pass; all use at most the tile grid's block count of partials
+// r = b - A x and its sums: the flat vectorised pass when A's layout allows it,
+// else the tile pass; both use at most the tile grid's block count of partials
 static void launch_refine_resid(const kc_system* A64, Geo g, dim3 sg, const double* b, const double* x, float* r32,
                                 BicgPtrs P, double* out2, bool with_b, cudaStream_t s) {
     if (vec_width<double>(A64, {b, x}) == 2 && ((uintptr_t)r32 % 8) == 0)
         k_refine_resid_vec<2><<<vec_blocks(A64->n / 2, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
-            coef_of<double>(A64), (int)A64->n, A64->stride, b, x, r32, P, out2, with_b ? 1 : 0);
-    else if (A64->es == 1)
-        k_refine_resid_vec<1><<<vec_blocks(A64->n, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
             coef_of<double>(A64), (int)A64->n, A64->stride, b, x, r32, P, out2, with_b ? 1 : 0);
     else
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, with_b ? 1 : 0);
