@@ -108,3 +108,26 @@ def test_bicgsimp_cavity_matches_reference(dev):
             for name in ("u", "v", "p", "pcor"):
                 assert rel(getattr(g, name).cpu().numpy(), d[f"sub{sub}_{name}"]) <= (1e-2 if name == "pcor" else 1e-3), \
                     (sub, name)
+
+
+def test_bicgsimp_cavity_runs_to_its_stop_rule(dev):
+    """bicgsimp.py's own case (50 x 50, lid u = 1, Re 100) to its stop rule: the substeps, the
+    final residuals and the centreline profiles its plot compares with Ghia et al. (1982) are those
+    committed by tests/golden/make_cavity_profiles.py (which compare_ghia.py sets against the
+    reference's data file: within 0.004 in u and 0.009 in v of the lid velocity)."""
+    import os
+    import numpy as np
+    import torch
+    from karman_taichi_gb300.simple import SIMPLESolver
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "cavity_bicgsimp_50x50_profiles.npz"))
+    s = SIMPLESolver(1.0, 1.0, 50, 50, device=dev, bicgsimp=True)
+    s.bc["n"][1] = 1.0
+    last = {}
+    s.solve(n_steps=10000, callback=lambda step, m, c: last.update(step=step, m=m, c=c))
+    torch.cuda.synchronize()
+    assert last["step"] + 1 == int(ref["substeps"])
+    assert last["m"] < 1e-2 and last["c"] < 1e-6
+    u = s.u.cpu().numpy()[26, 1:51]
+    v = s.v.cpu().numpy()[1:51, 26]
+    assert np.abs(u - ref["u_at_x05"]).max() <= 1e-9
+    assert np.abs(v - ref["v_at_y05"]).max() <= 1e-9
