@@ -350,15 +350,30 @@ __global__ void __launch_bounds__(kCoarsestMax) k_mg_coarsest(Lvl L, const float
 }
 
 // ---- fused cycle kernels (NU pre- and NU post-sweeps per level) ------------------------
+// The grid dependency wait, then (small levels: one wave) the early trigger
+// that lets the next grid queue up, then the solver's done flag.
+template <bool SMALL>
+struct MgGate {
+    const int* done;
+    __device__ __forceinline__ bool operator()() const {
+        pdl_wait();
+        if (SMALL) pdl_trigger();
+        return !mg_done(done);
+    }
+};
+
+// early != 0 (levels below 0): the launch before this one is a kernel of the
+// cycle, which waits for its own predecessor before it lets this grid start,
+// so what launches further back wrote (the setup's weights and coefficients,
+// the level's pre-smoothed iterate and right-hand side) is final: the tile
+// stages it before the wait, behind the previous grid.
 template <int TI, int AJ, int RY, bool STAGED, int NU>
 __global__ void __launch_bounds__(AJ * RY) k_mg_down(MgLvl L, const float* __restrict__ b, float* __restrict__ xout,
-                                                     float* __restrict__ bc, int NXc, int NYc, const int* done) {
-    pdl_wait();
-    if (AJ < kMgAJ0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
-    if (mg_done(done)) return;
-    mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED, NU>(blockIdx.y * TI, blockIdx.x * mg_tj(AJ, NU), L, b,
-                                                                    nullptr, 0.f, MgNoMid{}, MgOwnNone{}, xout, bc,
-                                                                    NXc, NYc);
+                                                     float* __restrict__ bc, int NXc, int NYc, const int* done,
+                                                     int early) {
+    mg_down_tile<TI, AJ, RY, false, MgNoMid, MgOwnNone, STAGED, NU>(
+        blockIdx.y * TI, blockIdx.x * mg_tj(AJ, NU), L, b, nullptr, 0.f, MgNoMid{}, MgOwnNone{}, xout, bc, NXc, NYc,
+        MgGate<(AJ < kMgAJ0)>{done}, early != 0);
     pdl_trigger();
 }
 
@@ -366,12 +381,10 @@ template <int TI, int AJ, int RY, bool STAGED, int NU>
 __global__ void __launch_bounds__(AJ * RY) k_mg_up(MgLvl L, const float* __restrict__ xpre,
                                                    const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                    const float* __restrict__ b, float* __restrict__ xout,
-                                                   const int* done) {
-    pdl_wait();
-    if (AJ < kMgAJ0) pdl_trigger();   // small levels: one wave, let the next grid queue up at once
-    if (mg_done(done)) return;
+                                                   const int* done, int early) {
     mg_up_tile<TI, AJ, RY, MgOwnNone, STAGED, NU>(blockIdx.y * TI, blockIdx.x * mg_tj(AJ, NU), L, xpre, xc, NXc, NYc,
-                                                  alpha, b, MgOwnNone{}, xout);
+                                                  alpha, b, MgOwnNone{}, xout, MgGate<(AJ < kMgAJ0)>{done},
+                                                  early != 0);
     pdl_trigger();
 }
 
@@ -659,39 +672,41 @@ static bool mg_fusable(const MgLayout& M, const kc_mg_opts* o) {
 
 template <int NU>
 static cudaError_t launch_down_nu(bool big, const MgLvl& G, const float* b, float* xout, float* bc, int NXc, int NYc,
-                                  const int* done, cudaStream_t s) {
+                                  const int* done, int early, cudaStream_t s) {
     if (big) {
         constexpr int TI = mg_big_ti(NU);
         return launch_chain(k_mg_down<TI, kMgAJ0, kMgRY0, (kMgStagedLarge || NU > 1), NU>,
                             mg_tile_grid(G.NX, G.NY, TI, mg_tj(kMgAJ0, NU)), dim3(kMgNT0), 0, s, G, b, xout, bc, NXc,
-                            NYc, done);
+                            NYc, done, early);
     }
     return launch_chain(k_mg_down<kMgTI1, kMgAJ1, kMgRY1, true, NU>, mg_tile_grid(G.NX, G.NY, kMgTI1, mg_tj(kMgAJ1, NU)),
-                        dim3(kMgNT1), 0, s, G, b, xout, bc, NXc, NYc, done);
+                        dim3(kMgNT1), 0, s, G, b, xout, bc, NXc, NYc, done, early);
 }
 
 template <int NU>
 static cudaError_t launch_up_nu(bool big, const MgLvl& G, const float* xpre, const float* xc, int NXc, int NYc,
-                                float alpha, const float* b, float* xout, const int* done, cudaStream_t s) {
+                                float alpha, const float* b, float* xout, const int* done, int early, cudaStream_t s) {
     if (big) {
         constexpr int TI = mg_big_ti(NU);
         return launch_chain(k_mg_up<TI, kMgAJ0, kMgRY0, (kMgStagedLarge || NU > 1), NU>,
                             mg_tile_grid(G.NX, G.NY, TI, mg_tj(kMgAJ0, NU)), dim3(kMgNT0), 0, s, G, xpre, xc, NXc,
-                            NYc, alpha, b, xout, done);
+                            NYc, alpha, b, xout, done, early);
     }
     return launch_chain(k_mg_up<kMgTI1, kMgAJ1, kMgRY1, true, NU>, mg_tile_grid(G.NX, G.NY, kMgTI1, mg_tj(kMgAJ1, NU)),
-                        dim3(kMgNT1), 0, s, G, xpre, xc, NXc, NYc, alpha, b, xout, done);
+                        dim3(kMgNT1), 0, s, G, xpre, xc, NXc, NYc, alpha, b, xout, done, early);
 }
 
+// level 0 follows launches outside the cycle: its staging waits for the previous grid
 static int launch_down(const MgLayout& M, const Lvl& L, int l, const float* b, float* xout, float* bc, const int* done,
                        const kc_mg_opts* o, cudaStream_t s) {
     const MgLvl G = mg_lvl(L);
     const bool big = l == 0 || mg_big(L.NX, L.NY, o);
     const int nu = l == 0 ? 1 : mg_nu_coarse(o);
     const int NXc = M.nx[l + 1], NYc = M.ny[l + 1];
-    const cudaError_t e = nu == 1   ? launch_down_nu<1>(big, G, b, xout, bc, NXc, NYc, done, s)
-                          : nu == 2 ? launch_down_nu<2>(big, G, b, xout, bc, NXc, NYc, done, s)
-                                    : launch_down_nu<3>(big, G, b, xout, bc, NXc, NYc, done, s);
+    const int early = l > 0;
+    const cudaError_t e = nu == 1   ? launch_down_nu<1>(big, G, b, xout, bc, NXc, NYc, done, early, s)
+                          : nu == 2 ? launch_down_nu<2>(big, G, b, xout, bc, NXc, NYc, done, early, s)
+                                    : launch_down_nu<3>(big, G, b, xout, bc, NXc, NYc, done, early, s);
     if (e != cudaSuccess) return cuda_status(e, "k_mg_down launch");
     KC_LAUNCH_CHECK_NC("k_mg_down");
     return KC_OK;
@@ -703,9 +718,10 @@ static int launch_up(const MgLayout& M, const Lvl& L, int l, const float* xpre, 
     const bool big = l == 0 || mg_big(L.NX, L.NY, o);
     const int nu = l == 0 ? 1 : mg_nu_coarse(o);
     const int NXc = M.nx[l + 1], NYc = M.ny[l + 1];
-    const cudaError_t e = nu == 1   ? launch_up_nu<1>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s)
-                          : nu == 2 ? launch_up_nu<2>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s)
-                                    : launch_up_nu<3>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, s);
+    const int early = l > 0;
+    const cudaError_t e = nu == 1   ? launch_up_nu<1>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, early, s)
+                          : nu == 2 ? launch_up_nu<2>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, early, s)
+                                    : launch_up_nu<3>(big, G, xpre, xc, NXc, NYc, alpha, b, xout, done, early, s);
     if (e != cudaSuccess) return cuda_status(e, "k_mg_up launch");
     KC_LAUNCH_CHECK_NC("k_mg_up");
     return KC_OK;

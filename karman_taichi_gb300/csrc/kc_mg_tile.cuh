@@ -177,11 +177,25 @@ struct MgStage {
     float* ss;    // a further staged array of the caller's (the single-reduction CG's previous s)
 };
 
-// DOWN, asynchronous part: stage b_in (and q) , W and the coefficients of the tile at (i0, j0)
-// (halo H cells)
+// DOWN, asynchronous part, in two halves by what they depend on: the smoother
+// weights and coefficients (written by the hierarchy's setup, several launches
+// back) and the right-hand side b_in (and q), which the previous launch of the
+// cycle writes.  Halo H cells.
+template <int TI, int AJ, int RY, int H = 2>
+__device__ __forceinline__ void mg_down_issue_fixed(int i0, int j0, const MgLvl& L, MgStage S) {
+    using T = MgTile<TI, AJ, RY, H>;
+    const int b = T::tx(), j = j0 + b - H;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - H;
+        const bool in = jin && i >= 0 && i < L.NX;
+        cp_async4(S.sw + a * T::AJ + b, L.winv + (in ? i * L.NY + j : 0), in);
+    }
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
 template <int TI, int AJ, int RY, bool HasQ, int H = 2>
-__device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
-                                              const float* __restrict__ q, MgStage S) {
+__device__ __forceinline__ void mg_down_issue_rhs(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
+                                                  const float* __restrict__ q, MgStage S) {
     using T = MgTile<TI, AJ, RY, H>;
     const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
@@ -192,9 +206,7 @@ __device__ __forceinline__ void mg_down_issue(int i0, int j0, const MgLvl& L, co
         const int u = a * T::AJ + b;
         cp_async4(S.sb + u, b_in + k, in);
         if (HasQ) cp_async4(S.sq + u, q + k, in);
-        cp_async4(S.sw + u, L.winv + k, in);
     }
-    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
 }
 
 // DOWN, after the tile's copies have landed: b = b_in - alpha q, red start,
@@ -284,11 +296,16 @@ __device__ __forceinline__ void mg_down_compute(int i0, int j0, const MgLvl& L, 
 
 // DOWN tile at (i0, j0) (multiples of TI, TJ).  b = HasQ ? b_in - alpha q : b_in over the staged region.
 // NU sweeps need the staged coefficients (STAGED); the unstaged variant is the one-sweep cycle.
-template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true, int NU = 1>
+// gate() runs the grid dependency wait and returns false when the solve is
+// over; with early, the weights and coefficients are staged before it (the
+// caller guarantees that the launch before this one waited for its own
+// predecessor first, so the setup that wrote them has finished).
+template <int TI, int AJ, int RY, bool HasQ, class Mid, class Own, bool STAGED = true, int NU = 1, class Gate>
 __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ b_in,
                                                           const float* __restrict__ q, float alpha, const Mid& mid,
                                                           const Own& own, float* __restrict__ xout,
-                                                          float* __restrict__ bc, int NXc, int NYc) {
+                                                          float* __restrict__ bc, int NXc, int NYc, const Gate& gate,
+                                                          bool early) {
     static_assert(STAGED || NU == 1, "several sweeps per level read the staged coefficients");
     if (STAGED) {
         using TS = MgTile<TI, AJ, RY, 2 * NU>;
@@ -296,7 +313,13 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
         __shared__ __align__(16) float sq[HasQ ? TS::A : 1];
         __shared__ __align__(16) float sc[5 * TS::A];
         const MgStage S{sb, sq, sw, sc, sx, nullptr, nullptr};
-        mg_down_issue<TI, AJ, RY, HasQ, 2 * NU>(i0, j0, L, b_in, q, S);
+        if (early) mg_down_issue_fixed<TI, AJ, RY, 2 * NU>(i0, j0, L, S);
+        if (!gate()) {
+            cp_async_wait_all();
+            return typename Own::Sum{};
+        }
+        if (!early) mg_down_issue_fixed<TI, AJ, RY, 2 * NU>(i0, j0, L, S);
+        mg_down_issue_rhs<TI, AJ, RY, HasQ, 2 * NU>(i0, j0, L, b_in, q, S);
         cp_async_commit();
         mid();
         cp_async_wait_all();
@@ -313,6 +336,7 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
     const bool jin = j >= 0 && j < L.NY;
     const bool jown = b >= 2 && b < T::TJ + 2 && j < L.NY;
     typename Own::Sum sum{};
+    if (!gate()) return sum;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
@@ -370,14 +394,13 @@ __device__ __forceinline__ typename Own::Sum mg_down_tile(int i0, int j0, const 
     return sum;
 }
 
-// UP, asynchronous part: stage x_pre, b_in, W, the coarse cells under the tile and the coefficients
-// (halo H cells; the coarse cells under the staged region start at (i0 - H) / 2, (j0 - H) / 2)
+// UP, asynchronous part, in two halves by what they depend on: x_pre, b_in, W
+// and the coefficients (written launches back), and the coarse cells under
+// the tile (the previous launch's result; they start at (i0 - H) / 2, (j0 - H) / 2).
 template <int TI, int AJ, int RY, int H = 2>
-__device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
-                                            const float* __restrict__ xc, int NXc, int NYc,
-                                            const float* __restrict__ b_in, MgStage S) {
+__device__ __forceinline__ void mg_up_issue_fixed(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
+                                                  const float* __restrict__ b_in, MgStage S) {
     using T = MgTile<TI, AJ, RY, H>;
-    constexpr int XI = TI / 2 + H, XJ = AJ / 2;
     const int b = T::tx(), j = j0 + b - H;
     const bool jin = j >= 0 && j < L.NY;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
@@ -389,13 +412,19 @@ __device__ __forceinline__ void mg_up_issue(int i0, int j0, const MgLvl& L, cons
         cp_async4(S.sb + u, b_in + k, in);
         cp_async4(S.sw + u, L.winv + k, in);
     }
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
+template <int TI, int AJ, int RY, int H = 2>
+__device__ __forceinline__ void mg_up_issue_coarse(int i0, int j0, const float* __restrict__ xc, int NXc, int NYc,
+                                                   MgStage S) {
+    using T = MgTile<TI, AJ, RY, H>;
+    constexpr int XI = TI / 2 + H, XJ = AJ / 2;
     for (int t = threadIdx.x; t < XI * XJ; t += T::NT) {
         const int ca = t / XJ, cb = t - ca * XJ;
         const int I = (i0 >> 1) - H / 2 + ca, J = (j0 >> 1) - H / 2 + cb;
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(S.sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
 }
 
 // UP, after the copies have landed: prolong (coupled cells, told apart by
@@ -446,11 +475,12 @@ __device__ __forceinline__ void mg_up_compute(int i0, int j0, const MgLvl& L, fl
 
 // UP tile at (i0, j0): prolong (coupled cells, told apart by their links),
 // then the NU post-smoothing sweeps (black, red), the last red half-sweep on the owned cells.
-template <int TI, int AJ, int RY, class Own, bool STAGED = true, int NU = 1>
+// gate and early as for mg_down_tile (early: x_pre, b_in, W and the coefficients before the wait)
+template <int TI, int AJ, int RY, class Own, bool STAGED = true, int NU = 1, class Gate>
 __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
                                                         const float* __restrict__ xc, int NXc, int NYc, float alpha,
                                                         const float* __restrict__ b_in, const Own& own,
-                                                        float* __restrict__ xout) {
+                                                        float* __restrict__ xout, const Gate& gate, bool early) {
     static_assert(STAGED || NU == 1, "several sweeps per level read the staged coefficients");
     if (STAGED) {
         using TS = MgTile<TI, AJ, RY, 2 * NU>;
@@ -458,7 +488,13 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
         __shared__ __align__(16) float sx[TS::A], sb[TS::A], sw[TS::A], sxc[XIS * XJS];
         __shared__ __align__(16) float sc[5 * TS::A];
         const MgStage S{sb, nullptr, sw, sc, sx, sxc, nullptr};
-        mg_up_issue<TI, AJ, RY, 2 * NU>(i0, j0, L, xpre, xc, NXc, NYc, b_in, S);
+        if (early) mg_up_issue_fixed<TI, AJ, RY, 2 * NU>(i0, j0, L, xpre, b_in, S);
+        if (!gate()) {
+            cp_async_wait_all();
+            return typename Own::Sum{};
+        }
+        if (!early) mg_up_issue_fixed<TI, AJ, RY, 2 * NU>(i0, j0, L, xpre, b_in, S);
+        mg_up_issue_coarse<TI, AJ, RY, 2 * NU>(i0, j0, xc, NXc, NYc, S);
         cp_async_commit();
         cp_async_wait_all();
         __syncthreads();
@@ -473,6 +509,7 @@ __device__ __forceinline__ typename Own::Sum mg_up_tile(int i0, int j0, const Mg
     const int b = T::tx(), j = j0 + b - 2;
     const bool jin = j >= 0 && j < L.NY;
     typename Own::Sum sum{};
+    if (!gate()) return sum;
     for (int a = T::ty(); a < T::AI; a += T::RY) {
         const int i = i0 + a - 2;
         const bool in = jin && i >= 0 && i < L.NX;
@@ -535,11 +572,11 @@ struct MgTile3 {
     __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
 };
 
-// stage x_pre, b, W, the coefficients and the coarse cells for the tile at (i0, j0) (region from i0 - 3, j0 - 3)
+// stage x_pre, W and the coefficients of the tile at (i0, j0) (region from i0 - 3, j0 - 3): data
+// written launches back
 template <int TI, int AJ, int RY>
-__device__ __forceinline__ void mg_up3_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
-                                             const float* __restrict__ xc, int NXc, int NYc,
-                                             const float* __restrict__ b_in, MgStage S) {
+__device__ __forceinline__ void mg_up3_issue_fixed(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
+                                                   MgStage S) {
     using T = MgTile3<TI, AJ, RY>;
     const int b = T::tx(), j = j0 + b - 3;
     const bool jin = j >= 0 && j < L.NY;
@@ -549,8 +586,21 @@ __device__ __forceinline__ void mg_up3_issue(int i0, int j0, const MgLvl& L, con
         const int k = in ? i * L.NY + j : 0;
         const int u = a * T::AJ + b;
         cp_async4(S.sx + u, xpre + k, in);
-        cp_async4(S.sb + u, b_in + k, in);
         cp_async4(S.sw + u, L.winv + k, in);
+    }
+    mg_stage_coef<TI, T, 3>(L, i0, j0, S.sc);
+}
+// stage b and the coarse cells under the tile (the coarse result: the previous launch's)
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void mg_up3_issue_rest(int i0, int j0, const MgLvl& L, const float* __restrict__ xc,
+                                                  int NXc, int NYc, const float* __restrict__ b_in, MgStage S) {
+    using T = MgTile3<TI, AJ, RY>;
+    const int b = T::tx(), j = j0 + b - 3;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 3;
+        const bool in = jin && i >= 0 && i < L.NX;
+        cp_async4(S.sb + a * T::AJ + b, b_in + (in ? i * L.NY + j : 0), in);
     }
     for (int t = threadIdx.x; t < T::XC; t += T::NT) {
         const int ca = t / T::XJ, cb = t - ca * T::XJ;
@@ -558,7 +608,13 @@ __device__ __forceinline__ void mg_up3_issue(int i0, int j0, const MgLvl& L, con
         const bool in = I >= 0 && I < NXc && J >= 0 && J < NYc;
         cp_async4(S.sxc + t, xc + (in ? I * NYc + J : 0), in);
     }
-    mg_stage_coef<TI, T, 3>(L, i0, j0, S.sc);
+}
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void mg_up3_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ xpre,
+                                             const float* __restrict__ xc, int NXc, int NYc,
+                                             const float* __restrict__ b_in, MgStage S) {
+    mg_up3_issue_fixed<TI, AJ, RY>(i0, j0, L, xpre, S);
+    mg_up3_issue_rest<TI, AJ, RY>(i0, j0, L, xc, NXc, NYc, b_in, S);
 }
 
 // prolong, black half-sweep over the 2-ring, red half-sweep over the 1-ring;

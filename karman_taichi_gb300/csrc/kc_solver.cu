@@ -1692,14 +1692,39 @@ struct PcOwnR {
     }
 };
 
-// DOWN_0 staging: r (sb), w (sq), s_old (ss), W, coefficients over the 2-cell-halo region
-// (pairs: the row length is even, so 8-byte copies move two cells; see mg_stage_coef_pairs)
+// DOWN_0 staging over the 2-cell-halo region, in two halves: W and the
+// coefficients (the setup's), and r (sb), w (sq), s_old (ss) (the iteration's).
+// Pairs: the row length is even, so 8-byte copies move two cells (see
+// mg_stage_coef_pairs).
 template <int TI, int AJ, int RY>
-__device__ __forceinline__ void pcc_down_issue(int i0, int j0, const MgLvl& L, const float* __restrict__ r,
-                                               const float* __restrict__ w, const float* __restrict__ s_old,
-                                               bool update, bool first, bool pairs, MgStage S) {
+__device__ __forceinline__ void pcc_down_issue_fixed(int i0, int j0, const MgLvl& L, bool pairs, MgStage S) {
     using T = MgTile<TI, AJ, RY>;
     if (pairs && L.es == 1) {
+        constexpr int PJ = AJ / 2;
+        for (int e = threadIdx.x; e < T::AI * PJ; e += T::NT) {
+            const int a = e / PJ, b = 2 * (e - a * PJ);
+            const int i = i0 + a - 2, j = j0 + b - 2;
+            const bool in = i >= 0 && i < L.NX && j >= 0 && j < L.NY;
+            cp_async8f(S.sw + a * T::AJ + b, L.winv + (in ? i * L.NY + j : 0), in);
+        }
+        mg_stage_coef_pairs<TI, T>(L, i0, j0, S.sc);
+        return;
+    }
+    const int b = T::tx(), j = j0 + b - 2;
+    const bool jin = j >= 0 && j < L.NY;
+    for (int a = T::ty(); a < T::AI; a += T::RY) {
+        const int i = i0 + a - 2;
+        const bool in = jin && i >= 0 && i < L.NX;
+        cp_async4(S.sw + a * T::AJ + b, L.winv + (in ? i * L.NY + j : 0), in);
+    }
+    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
+}
+template <int TI, int AJ, int RY>
+__device__ __forceinline__ void pcc_down_issue_vec(int i0, int j0, const MgLvl& L, const float* __restrict__ r,
+                                                   const float* __restrict__ w, const float* __restrict__ s_old,
+                                                   bool update, bool first, bool pairs, MgStage S) {
+    using T = MgTile<TI, AJ, RY>;
+    if (pairs) {
         constexpr int PJ = AJ / 2;
         for (int e = threadIdx.x; e < T::AI * PJ; e += T::NT) {
             const int a = e / PJ, b = 2 * (e - a * PJ);
@@ -1710,9 +1735,7 @@ __device__ __forceinline__ void pcc_down_issue(int i0, int j0, const MgLvl& L, c
             cp_async8f(S.sb + u, r + k, in);
             if (update) cp_async8f(S.sq + u, w + k, in);
             if (update && !first) cp_async8f(S.ss + u, s_old + k, in);
-            cp_async8f(S.sw + u, L.winv + k, in);
         }
-        mg_stage_coef_pairs<TI, T>(L, i0, j0, S.sc);
         return;
     }
     const int b = T::tx(), j = j0 + b - 2;
@@ -1725,9 +1748,7 @@ __device__ __forceinline__ void pcc_down_issue(int i0, int j0, const MgLvl& L, c
         cp_async4(S.sb + u, r + k, in);
         if (update) cp_async4(S.sq + u, w + k, in);
         if (update && !first) cp_async4(S.ss + u, s_old + k, in);
-        cp_async4(S.sw + u, L.winv + k, in);
     }
-    mg_stage_coef<TI, T>(L, i0, j0, S.sc);
 }
 
 // The level-0 kernels walk the tiles of the grid with a two-stage pipeline:
@@ -1747,37 +1768,52 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcc_down0(MgLvl L, float* __rest
     using T = MgTile<TI, AJ, RY>;
     constexpr int SA = 9 * T::A;   // staged floats per stage: sb, sq, ss, sw, sc[5]
     extern __shared__ __align__(16) float dsm[];
+    const bool up = update != 0;
+    auto stage = [&](int sidx) {
+        float* b = dsm + sidx * SA;
+        return MgStage{b, b + T::A, b + 3 * T::A, b + 4 * T::A, dsm + 2 * SA, nullptr, b + 2 * T::A};
+    };
+    // 8-byte staging copies: even row length and tile width, 8-byte aligned planes
+    const bool even = (L.NY % 2 == 0) && (TJ % 2 == 0);
+    const bool pairs_c = even && (L.cs % 2 == 0) &&
+                         ((reinterpret_cast<unsigned long long>(L.c) | reinterpret_cast<unsigned long long>(L.winv)) %
+                          8 == 0);
+    int t = blockIdx.x, sidx = 0;
+    // inside the iterations (update) the launch before this one is the previous iteration's
+    // UP_0 or none, and the setup that wrote W and the coefficients ran launches earlier: the
+    // first tile stages them before the grid dependency wait
+    if (up && t < g.ntiles) pcc_down_issue_fixed<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, pairs_c, stage(0));
     pdl_wait();
     SolverState* st = P.st;
-    if (solver_done(st)) return;
+    if (solver_done(st)) {
+        cp_async_wait_all();
+        return;
+    }
     const long long it = __ldcg(&st->iter);
     const int cur = (int)(it & 1);
-    const bool up = update != 0, first = it == 0;
+    const bool first = it == 0;
     const float* r = cur ? V.r[1] : V.r[0];   // (selected, not indexed: no local copy of V)
     const float* s_old = cur ? V.s[1] : V.s[0];
     float* s_new = cur ? V.s[0] : V.s[1];
     const float alpha = up ? __ldcg(&st->alpha_f) : 0.f, beta = up ? __ldcg(&st->beta_f) : 0.f;
     const PcMidCG<TI, TJ, NT> mid{V.x, V.p[0], V.z, __ldcg(&st->alpha), beta, L.NX, L.NY, up, first};
     const PcOwnR own{cur ? V.r[0] : V.r[1], up};
-    // 8-byte staging copies: even row length and tile width, 8-byte aligned planes
-    const bool pairs = (L.NY % 2 == 0) && (TJ % 2 == 0) && (L.cs % 2 == 0) &&
-                       ((reinterpret_cast<unsigned long long>(L.c) | reinterpret_cast<unsigned long long>(L.winv) |
-                         reinterpret_cast<unsigned long long>(r) | reinterpret_cast<unsigned long long>(V.q) |
-                         reinterpret_cast<unsigned long long>(s_old)) % 8 == 0);
-    auto stage = [&](int sidx) {
-        float* b = dsm + sidx * SA;
-        return MgStage{b, b + T::A, b + 3 * T::A, b + 4 * T::A, dsm + 2 * SA, nullptr, b + 2 * T::A};
-    };
+    const bool pairs_v = even && ((reinterpret_cast<unsigned long long>(r) | reinterpret_cast<unsigned long long>(V.q) |
+                                   reinterpret_cast<unsigned long long>(s_old)) % 8 == 0);
     Acc<float> acc[1];
-    int t = blockIdx.x, sidx = 0;
-    if (t < g.ntiles)
-        pcc_down_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, V.q, s_old, up, first, pairs, stage(0));
+    if (t < g.ntiles) {
+        if (!up) pcc_down_issue_fixed<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, pairs_c, stage(0));
+        pcc_down_issue_vec<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, r, V.q, s_old, up, first, pairs_v,
+                                       stage(0));
+    }
     cp_async_commit();
     for (; t < g.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
-        if (tn < g.ntiles)
-            pcc_down_issue<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, V.q, s_old, up, first, pairs,
-                                       stage(sidx ^ 1));
+        if (tn < g.ntiles) {
+            pcc_down_issue_fixed<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, pairs_c, stage(sidx ^ 1));
+            pcc_down_issue_vec<TI, AJ, RY>(pcf_i0(g, tn, TI), pcf_j0(g, tn, TJ), L, r, V.q, s_old, up, first, pairs_v,
+                                           stage(sidx ^ 1));
+        }
         cp_async_commit();
         const int i0 = pcf_i0(g, t, TI), j0 = pcf_j0(g, t, TJ);
         mid(i0, j0);
@@ -1830,18 +1866,26 @@ __global__ void __launch_bounds__(AJ * RY, 2) k_pcc_up0(MgLvl L, const float* __
     using T = MgTile3<TI, AJ, RY>;
     constexpr int TJ = T::TJ, SA = 8 * T::A + T::XC;
     extern __shared__ __align__(16) float dsm[];
-    pdl_wait();
-    SolverState* st = P.st;
-    if (solver_done(st)) return;
-    const long long it = __ldcg(&st->iter);
-    const float* r = (it & 1) ? V.r[1] : V.r[0];
     auto stage = [&](int sidx) {
         float* b = dsm + sidx * SA;
         return MgStage{b + T::A, nullptr, b + 2 * T::A, b + 3 * T::A, b, b + 8 * T::A, nullptr};
     };
-    Acc<float> acc[2];
     int t = blockIdx.x, sidx = 0;
-    if (t < g.ntiles) mg_up3_issue<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, x0pre, final1, NX1, NY1, r, stage(0));
+    // the launch before this one is the cycle's level-1 UP (or its tail), which waits for its
+    // own predecessor before it lets this grid start: the pre-smoothed x0pre (DOWN_0's), W and
+    // the coefficients are final, and the first tile stages them before the wait
+    if (t < g.ntiles) mg_up3_issue_fixed<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, x0pre, stage(0));
+    pdl_wait();
+    SolverState* st = P.st;
+    if (solver_done(st)) {
+        cp_async_wait_all();
+        return;
+    }
+    const long long it = __ldcg(&st->iter);
+    const float* r = (it & 1) ? V.r[1] : V.r[0];
+    Acc<float> acc[2];
+    if (t < g.ntiles)
+        mg_up3_issue_rest<TI, AJ, RY>(pcf_i0(g, t, TI), pcf_j0(g, t, TJ), L, final1, NX1, NY1, r, stage(0));
     cp_async_commit();
     for (; t < g.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
