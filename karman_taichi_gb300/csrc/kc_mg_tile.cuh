@@ -107,6 +107,23 @@ struct MgTile {
     __device__ static __forceinline__ int ty() { return threadIdx.x / AJ; }
 };
 
+// Visits the cells of colour col ((a + b) & 1) in rows [a0, a1) and columns
+// [b0, b1) of a tile staged as [AI][AJ], handing f their staged index.  AJ / 2
+// threads share a row, thread m taking column 2 m or 2 m + 1 (whichever has the
+// colour), so every lane of a warp has a cell: with one thread per column,
+// every other lane would sit out each half-sweep.  Which thread updates a cell
+// does not change what it computes.
+template <class T, class F>
+__device__ __forceinline__ void mg_colour_cells(int col, int a0, int a1, int b0, int b1, const F& f) {
+    constexpr int HJ = T::AJ / 2, RP = T::NT / HJ;   // threads per row, rows per pass
+    static_assert(T::NT % HJ == 0, "whole rows per pass");
+    const int m = threadIdx.x & (HJ - 1);
+    for (int a = a0 + (int)threadIdx.x / HJ; a < a1; a += RP) {
+        const int b = 2 * m + ((a + col) & 1);
+        if (b >= b0 && b < b1) f(a * T::AJ + b);
+    }
+}
+
 // stage the 5 coefficient components over the whole staged region of the tile at (i0, j0)
 // (H: halo width, the region starts at (i0 - H, j0 - H))
 template <int TI, class T, int H = T::H>
@@ -250,12 +267,8 @@ __device__ __forceinline__ void mg_down_compute_pre(int i0, int j0, const MgLvl&
     // half-sweep h = 1 .. 2 NU - 1 (odd: black, even: red) over the region less h rings
 #pragma unroll
     for (int h = 1; h < 2 * NU; ++h) {
-        if (b >= h && b < AJ - h)
-            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
-                if (((a + b) & 1) != (h & 1)) continue;
-                const int u = a * T::AJ + b;
-                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-            }
+        mg_colour_cells<T>(h & 1, h, T::AI - h, h, AJ - h,
+                           [&](int u) { sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]); });
         __syncthreads();
     }
     // owned cells: write x
@@ -451,12 +464,8 @@ __device__ __forceinline__ void mg_up_compute(int i0, int j0, const MgLvl& L, fl
     // half-sweep h = 1 .. 2 NU - 1 (odd: black, even: red) over the region less h rings
 #pragma unroll
     for (int h = 1; h < 2 * NU; ++h) {
-        if (b >= h && b < AJ - h)
-            for (int a = h + T::ty(); a < T::AI - h; a += T::RY) {
-                if (((a + b) & 1) != (h & 1)) continue;
-                const int u = a * T::AJ + b;
-                sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-            }
+        mg_colour_cells<T>(h & 1, h, T::AI - h, h, AJ - h,
+                           [&](int u) { sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]); });
         __syncthreads();
     }
     // the last (red) half-sweep on the owned cells, then write
@@ -638,20 +647,11 @@ __device__ __forceinline__ void mg_up3_compute(int i0, int j0, const MgLvl& L, f
     }
     __syncthreads();
     // black half-sweep over the 2-ring and inside ((a + b) odd <=> (i + j) odd: the offset 3 + 3 is even)
-    if (b >= 1 && b < AJ - 1)
-        for (int a = 1 + T::ty(); a < T::AI - 1; a += T::RY) {
-            if (((a + b) & 1) == 0) continue;
-            const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-        }
+    const auto relax = [&](int u) { sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]); };
+    mg_colour_cells<T>(1, 1, T::AI - 1, 1, AJ - 1, relax);
     __syncthreads();
     // red half-sweep over the 1-ring and inside
-    if (b >= 2 && b < AJ - 2)
-        for (int a = 2 + T::ty(); a < T::AI - 2; a += T::RY) {
-            if (((a + b) & 1) != 0) continue;
-            const int u = a * T::AJ + b;
-            sx[u] = fmaf(sw[u], sb[u] - C.ax(sx, u), sx[u]);
-        }
+    mg_colour_cells<T>(0, 2, T::AI - 2, 2, AJ - 2, relax);
     __syncthreads();
     // owned cells: z, w = A z, (r, z), (w, z)
     if (b >= 3 && b < T::TJ + 3 && j < L.NY)

@@ -2766,55 +2766,75 @@ __global__ void __launch_bounds__(AJ * RY) k_gs_block_sweeps(MgLvl L, const floa
                                                              const float* __restrict__ xin, float* __restrict__ xout) {
     using T = MgTile<TI, AJ, RY, 2 * NU>;
     constexpr int H = T::H;
-    constexpr int R = (T::AI + RY - 1) / RY;   // staged rows per thread
+    // AJ / 2 threads to a staged row, thread m holding its columns 2m and 2m + 1 -- one cell of
+    // each colour -- in RP rows a = a0, a0 + RP, ...; RP is even, so every row of a thread has
+    // the same parity and its red cell is the same column in all of them.  Each half-sweep
+    // then gives every thread one cell per row: no lane of a warp sits out.
+    constexpr int HJ = AJ / 2, RP = T::NT / HJ;
+    constexpr int R = (T::AI + RP - 1) / RP;   // staged rows per thread
+    static_assert(T::NT % HJ == 0 && RP % 2 == 0, "whole rows per pass, an even row step");
     __shared__ __align__(16) float sx[T::A];
     const int i0 = blockIdx.y * TI, j0 = blockIdx.x * T::TJ;
-    const int bc = T::tx(), ty = T::ty(), j = j0 + bc - H;
-    const bool jin = j >= 0 && j < L.NY;
-    // A thread updates the same column cells in every half-sweep: their coefficients, weights and
+    const int m = threadIdx.x & (HJ - 1), a0 = threadIdx.x / HJ;
+    // the thread's red column ((a + b) even; i0 - H and j0 - H are even) and black column
+    const int bcol[2] = {2 * m + (a0 & 1), 2 * m + 1 - (a0 & 1)};
+    // A thread updates the same cells in every half-sweep: their coefficients, weights and
     // right-hand sides stay in registers (zero outside the grid), only x goes through shared
-    // memory -- 5 shared-memory reads per cell update instead of 12.
-    float c0[R], c1[R], c2[R], c3[R], c4[R], wv[R], bv[R];
+    // memory -- 5 shared-memory reads per cell update instead of 12.  [colour][row]
+    float c0[2][R], c1[2][R], c2[2][R], c3[2][R], c4[2][R], wv[2][R], bv[2][R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const int a = ty + r * RY;
-        const int i = i0 + a - H;
-        const bool in = a < T::AI && jin && i >= 0 && i < L.NX;
-        const long long k = in ? (long long)i * L.NY + j : 0;
-        if (a < T::AI) cp_async4(sx + a * T::AJ + bc, xin + k, in);
-        const float* g = L.c + k * L.es;
-        c0[r] = in ? __ldg(g) : 0.f;
-        c1[r] = in ? __ldg(g + L.cs) : 0.f;
-        c2[r] = in ? __ldg(g + 2 * L.cs) : 0.f;
-        c3[r] = in ? __ldg(g + 3 * L.cs) : 0.f;
-        c4[r] = in ? __ldg(g + 4 * L.cs) : 0.f;
-        wv[r] = in ? __ldg(L.winv + k) : 0.f;
-        bv[r] = in ? __ldg(b + k) : 0.f;
+    for (int q = 0; q < 2; ++q) {
+        const int j = j0 + bcol[q] - H;
+        const bool jin = j >= 0 && j < L.NY;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int a = a0 + r * RP;
+            const int i = i0 + a - H;
+            const bool in = a < T::AI && jin && i >= 0 && i < L.NX;
+            const long long k = in ? (long long)i * L.NY + j : 0;
+            if (a < T::AI) cp_async4(sx + a * T::AJ + bcol[q], xin + k, in);
+            const float* g = L.c + k * L.es;
+            c0[q][r] = in ? __ldg(g) : 0.f;
+            c1[q][r] = in ? __ldg(g + L.cs) : 0.f;
+            c2[q][r] = in ? __ldg(g + 2 * L.cs) : 0.f;
+            c3[q][r] = in ? __ldg(g + 3 * L.cs) : 0.f;
+            c4[q][r] = in ? __ldg(g + 4 * L.cs) : 0.f;
+            wv[q][r] = in ? __ldg(L.winv + k) : 0.f;
+            bv[q][r] = in ? __ldg(b + k) : 0.f;
+        }
     }
     cp_async_commit();
     cp_async_wait_all();
     __syncthreads();
 #pragma unroll
     for (int h = 1; h <= 2 * NU; ++h) {   // odd h: red ((i + j) even), even h: black
+        const int q = (h & 1) ? 0 : 1;
+        const int bc = bcol[q];
         if (bc >= h && bc < AJ - h) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                const int a = ty + r * RY;
-                if (a < h || a >= T::AI - h || ((a + bc) & 1) != ((h & 1) ? 0 : 1)) continue;
+                const int a = a0 + r * RP;
+                if (a < h || a >= T::AI - h) continue;
                 const int u = a * T::AJ + bc;
                 const float xv = sx[u];
-                const float y = mg_row(c0[r], c1[r], c2[r], c3[r], c4[r], L.lap, xv, sx[u - T::AJ], sx[u + T::AJ],
-                                       sx[u + 1], sx[u - 1]);
-                sx[u] = fmaf(wv[r], bv[r] - y, xv);
+                const float y = mg_row(c0[q][r], c1[q][r], c2[q][r], c3[q][r], c4[q][r], L.lap, xv, sx[u - T::AJ],
+                                       sx[u + T::AJ], sx[u + 1], sx[u - 1]);
+                sx[u] = fmaf(wv[q][r], bv[q][r] - y, xv);
             }
         }
         __syncthreads();
     }
-    if (bc >= H && bc < T::TJ + H && j < L.NY)
-        for (int a = H + ty; a < TI + H; a += T::RY) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int bc = bcol[q], j = j0 + bc - H;
+        if (bc < H || bc >= T::TJ + H || j >= L.NY) continue;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int a = a0 + r * RP;
             const int i = i0 + a - H;
-            if (i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + bc];
+            if (a >= H && a < TI + H && i < L.NX) xout[i * L.NY + j] = sx[a * T::AJ + bc];
         }
+    }
 }
 
 // weights 1/d of the red-black sweeps (0 on rows with a zero diagonal)
