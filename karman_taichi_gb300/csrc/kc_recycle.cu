@@ -197,8 +197,12 @@ __global__ void __launch_bounds__(kRcThreads) k_rc_combine(long long n, RcVecs V
     }
 }
 
-int rc_blocks(long long n) {
-    return (int)std::max<long long>(1, std::min<long long>((n + kRcThreads * 4 - 1) / (kRcThreads * 4), kRcMaxBlocks));
+// cells per thread: 4 for the combine pass (memory-bound: many loads in flight), 16 for the
+// Gram pass, which is bound by the FP64 pipe -- its per-thread block reduction of the
+// m (m + 3) / 2 sums (70 FP64 adds at m = 4) then costs an eighth of the pass instead of half
+int rc_blocks(long long n, int per_thread = 4) {
+    const long long c = (long long)kRcThreads * per_thread;
+    return (int)std::max<long long>(1, std::min<long long>((n + c - 1) / c, kRcMaxBlocks));
 }
 
 template <int M>
@@ -207,12 +211,12 @@ int rc_run(long long n, const RcSys& A, const RcVecs& V, const double* b, const 
     double* partials = (double*)(base + L.partials);
     double* out = (double*)(base + L.out);
     double* coef = (double*)(base + L.coef);
-    const int nb = rc_blocks(n);
+    const int nb = rc_blocks(n, 16);
     k_rc_gram<M><<<nb, kRcThreads, 0, s>>>(n, A, V, b, partials);
     KC_LAUNCH_CHECK("k_rc_gram");
     k_rc_fold_solve<M><<<1, kRcThreads, 0, s>>>(partials, nb, out, coef);
     KC_LAUNCH_CHECK("k_rc_fold_solve");
-    k_rc_combine<M><<<nb, kRcThreads, 0, s>>>(n, V, coef, x0);
+    k_rc_combine<M><<<rc_blocks(n), kRcThreads, 0, s>>>(n, V, coef, x0);
     KC_LAUNCH_CHECK("k_rc_combine");
     return KC_OK;
 }

@@ -425,6 +425,15 @@ static int vec_blocks(long long chunks, int cap) {
     return (int)std::max<long long>(1, std::min<long long>({want, (long long)sms * 8, (long long)cap}));
 }
 
+// Grid of a flat FP64 pass that also sums per thread and block (the refinement
+// residual): about cpt chunks a thread.  Its block reduction costs each thread
+// ten FP64 adds per summed value, a fixed price against the FP64 pipe that a
+// thread handling only a few cells pays several times over.
+static int red_blocks(long long chunks, int cpt, int cap) {
+    const long long want = (chunks + (long long)kThreads * cpt - 1) / ((long long)kThreads * cpt);
+    return (int)std::max<long long>(1, std::min<long long>({want, (long long)vec_blocks(chunks, cap)}));
+}
+
 // ---- dot ----------------------------------------------------------------------
 struct DotWs {
     unsigned ticket[4];
@@ -2006,7 +2015,7 @@ static Coef<T> coef_of(const kc_system* A) {
 static void launch_refine_resid(const kc_system* A64, Geo g, dim3 sg, const double* b, const double* x, float* r32,
                                 BicgPtrs P, double* out2, bool with_b, cudaStream_t s) {
     if (vec_width<double>(A64, {b, x}) == 2 && ((uintptr_t)r32 % 8) == 0)
-        k_refine_resid_vec<2><<<vec_blocks(A64->n / 2, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
+        k_refine_resid_vec<2><<<red_blocks(A64->n / 2, 8, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
             coef_of<double>(A64), (int)A64->n, A64->stride, b, x, r32, P, out2, with_b ? 1 : 0);
     else
         k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, with_b ? 1 : 0);
