@@ -923,15 +923,20 @@ struct PolResid {
     }
 };
 
+// A block walks the tiles t = blockIdx.x, + gridDim.x, ... (tiles_x per tile
+// row): several tiles a block, so that the block reduction's FP64 adds are
+// paid once per several tiles' cells.
 __global__ void __launch_bounds__(kThreads)
-    k_refine_resid(Coef<double> A, Geo g, const double* __restrict__ b, const double* __restrict__ x,
-                   float* __restrict__ r32, BicgPtrs P, double* out2, int with_b) {
+    k_refine_resid(Coef<double> A, Geo g, int tiles_x, int ntiles, const double* __restrict__ b,
+                   const double* __restrict__ x, float* __restrict__ r32, BicgPtrs P, double* out2, int with_b) {
     Acc<double> acc[2];
     PolResid pol{x, b, r32, with_b};
-    stencil_tile<double, 2>(pol, A, g.n, g.S, acc);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        stencil_tile_at<double, 2>(pol, A, g.n, g.S, (t / tiles_x) * kTI, (t % tiles_x) * kTJ, acc);
+        __syncthreads();   // the next tile restages the shared operand
+    }
     double s[2];
-    if (block_partials<2>(acc, P.partials, P.ld, block_id(), block_count(), &P.st->ticket[0], s) &&
-        threadIdx.x == 0) {
+    if (block_partials<2>(acc, P.partials, P.ld, blockIdx.x, gridDim.x, &P.st->ticket[0], s) && threadIdx.x == 0) {
         out2[0] = s[0];
         out2[1] = s[1];
         P.st->ticket[0] = 0;
@@ -2017,8 +2022,11 @@ static void launch_refine_resid(const kc_system* A64, Geo g, dim3 sg, const doub
     if (vec_width<double>(A64, {b, x}) == 2 && ((uintptr_t)r32 % 8) == 0)
         k_refine_resid_vec<2><<<red_blocks(A64->n / 2, 8, (int)(sg.x * sg.y)), kThreads, 0, s>>>(
             coef_of<double>(A64), (int)A64->n, A64->stride, b, x, r32, P, out2, with_b ? 1 : 0);
-    else
-        k_refine_resid<<<sg, kThreads, 0, s>>>(coef_of<double>(A64), g, b, x, r32, P, out2, with_b ? 1 : 0);
+    else {
+        const int ntiles = (int)(sg.x * sg.y), nb = std::max(1, (ntiles + 3) / 4);   // four tiles a block
+        k_refine_resid<<<nb, kThreads, 0, s>>>(coef_of<double>(A64), g, (int)sg.x, ntiles, b, x, r32, P, out2,
+                                               with_b ? 1 : 0);
+    }
 }
 
 struct HostState {
