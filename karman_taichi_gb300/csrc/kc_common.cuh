@@ -41,6 +41,13 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // are visible (at once when the kernel was launched without the attribute),
 // so it must come before any read of a predecessor's output.  pdl_trigger()
 // lets the next grid's blocks be scheduled while this grid finishes.
+// Invariant of the chain: every kernel in it calls pdl_wait() before
+// pdl_trigger().  A grid therefore starts only once the grid two launches
+// back has completed, and the multigrid tiles (k_mg_down / k_mg_up below
+// level 0, k_pcc_down0 inside the iterations, k_pcc_up0) stage what launches
+// further back wrote -- the hierarchy's weights and coefficients, a level's
+// pre-smoothed iterate -- before their own wait.  A kernel added to the
+// chain must keep that order.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
